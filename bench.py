@@ -1,0 +1,531 @@
+#!/usr/bin/env python3
+"""Benchmark: FP32 Black-Scholes call+put over 2^24 options on one GB300 per rank.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--suite]
+
+One step is one evaluation of the Black-Scholes statement over the whole
+2^24-option batch (S, K, T resident in HBM; 335 MB of compulsory traffic,
+larger than the 129 MB L2, so no flush is needed between steps).  Prints one
+JSON line.  --suite also prints one line per other configuration (saxpy,
+sdot, inner/outer folds, FP64 Black-Scholes, batched sigma-delta).
+--impl reference times the CPU restatement of NT2's SIMD+OpenMP path on the
+host cores instead (rank 0 only).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Black-Scholes options/s & % HBM peak; serving p99 latency vs launch-per-call"
+N_OPTIONS = 1 << 24
+R, SIGMA = 0.02, 0.30
+BYTES_PER_OPTION = 20            # S, K, T read; call, put written (float32)
+NOMINAL_HBM_GBS = 8000.0
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(name: str):
+    """dram bytes per launch recorded from an ncu capture in profiles/<name>.md ("traffic_bytes_per_launch: X")."""
+    p = os.path.join(ROOT, "profiles", name + ".md")
+    try:
+        for line in open(p):
+            if line.strip().startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].strip().split()[0])
+    except Exception:
+        pass
+    return None
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the bench runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return self
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                self.samples.append((time.time(), float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                pass
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self, t0: float, t1: float):
+        win = [s for s in self.samples if t0 - 0.15 <= s[0] <= t1 + 0.15]
+        src = "timed_region"
+        if not win:
+            win = self.samples
+            src = "whole_run"
+        if not win:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in win for i, v in enumerate(s[3]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(s[1] for s in win), "sm_max_mhz": max(s[2] for s in win),
+                "reasons": reasons, "samples": len(win), "window": src}
+
+
+# --------------------------------------------------------------- helpers
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def max_over_ranks(x: float, ws: int):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws: int):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def bs_tables(n: int, seed: int):
+    import torch
+    import nt2_gb300.api as api
+    S = torch.empty(n, dtype=torch.float32, device="cuda")
+    K = torch.empty(n, dtype=torch.float32, device="cuda")
+    T = torch.empty(n, dtype=torch.float32, device="cuda")
+    api.fill_uniform(S, 5.0, 30.0, seed * 3 + 1)
+    api.fill_uniform(K, 1.0, 100.0, seed * 3 + 2)
+    api.fill_uniform(T, 0.25, 10.0, seed * 3 + 3)
+    return S, K, T
+
+
+def time_device(fn, steps: int, warmup: int, ws: int):
+    """CUDA-event time of `steps` calls on torch's current stream, max over ranks (ms per step)."""
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    barrier(ws)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    t0 = time.time()
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t1 = time.time()
+    barrier(ws)
+    ms = e0.elapsed_time(e1) / steps
+    return max_over_ranks(ms, ws), t0, t1
+
+
+# ---------------------------------------------------------- CPU baseline
+def cpu_baseline(sample: int = 1 << 22, seconds: float = 4.0):
+    """The oracle's NT2-restated SIMD+OpenMP Black-Scholes on the host cores (options/s, median of reps)."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    L = oracle_lib.load()
+    rng = np.random.default_rng(1)
+    S = rng.uniform(5, 30, sample).astype(np.float32)
+    K = rng.uniform(1, 100, sample).astype(np.float32)
+    T = rng.uniform(0.25, 10, sample).astype(np.float32)
+    call = np.empty_like(S)
+    put = np.empty_like(S)
+    threads = L.nt2o_max_threads()
+    L.nt2o_bs_f(S, K, T, R, SIGMA, call, put, sample, 0, threads)
+    rates = []
+    t_end = time.perf_counter() + seconds
+    while time.perf_counter() < t_end or len(rates) < 3:
+        t = time.perf_counter()
+        L.nt2o_bs_f(S, K, T, R, SIGMA, call, put, sample, 0, threads)
+        rates.append(sample / (time.perf_counter() - t))
+    return {"value": statistics.median(rates), "unit": "options/s", "cores": threads, "kind": "port",
+            "sample": f"{sample} options per rep (1/{N_OPTIONS // sample} of the 2^24-option batch), "
+                      f"{len(rates)} reps, median; NT2 scalar+OpenMP restatement (oracle/nt2_oracle.c, -O2)"}
+
+
+# -------------------------------------------------------------- serving
+def serving_bench(seconds: float = 1.0, rates=(1000, 10000, 50000), seed: int = 7):
+    """Poisson arrivals of Black-Scholes requests (sizes log-uniform 256..2^22 options) into the
+    continuous-batching server and into a one-launch-per-request server on the same GPU."""
+    import numpy as np
+    import torch
+    from nt2_gb300.server import Server
+    pool_n = 1 << 24
+    S, K, T = bs_tables(pool_n, seed=99)
+    torch.cuda.synchronize()
+    rng = np.random.default_rng(seed)
+    out = {}
+
+    def run(mode, rate, dur):
+        coalesce = mode == "batched"
+        srv = Server(budget_bytes=40 << 30, max_batch_requests=4096, max_inflight_batches=3 if coalesce else 1,
+                     coalesce=coalesce)
+        nreq = max(8, int(rate * dur))
+        sizes = np.exp(rng.uniform(math.log(256), math.log(1 << 22), nreq)).astype(np.int64)
+        offs = (rng.integers(0, pool_n - (1 << 22), nreq) // 4) * 4
+        gaps = rng.exponential(1.0 / rate, nreq) if rate else np.zeros(nreq)
+        tickets = []
+        lat = []
+        done = threading.Event()
+        sp, kp, tp = S.data_ptr(), K.data_ptr(), T.data_ptr()
+
+        def reaper():
+            i = 0
+            while i < nreq:
+                while i >= len(tickets):
+                    time.sleep(0)
+                t = tickets[i]
+                srv.wait(t, 120000)
+                lat.append(srv.latency_ns(t))
+                srv.release(t)
+                i += 1
+            done.set()
+
+        th = threading.Thread(target=reaper, daemon=True)
+        th.start()
+        t0 = time.perf_counter()
+        next_t = t0
+        for i in range(nreq):
+            next_t += gaps[i]
+            while time.perf_counter() < next_t:
+                pass
+            o = int(offs[i]) * 4
+            tickets.append(srv.submit_ptr(sp + o, kp + o, tp + o, R, SIGMA, int(sizes[i])))
+        done.wait(300)
+        t1 = time.perf_counter()
+        st = srv.stats()
+        srv.close()
+        lat_us = np.array(lat) / 1e3
+        return {"requests": nreq, "options_per_s": float(sizes.sum() / (t1 - t0)),
+                "p50_us": float(np.percentile(lat_us, 50)), "p99_us": float(np.percentile(lat_us, 99)),
+                "launches": int(st["launches"]), "batches": int(st["batches"])}
+
+    for rate in rates:
+        out[f"{rate}_req_s"] = {m: run(m, rate, seconds) for m in ("batched", "launch_per_request")}
+    # saturation: all requests offered at once (small requests, where launch cost dominates)
+    sat_rng = np.random.default_rng(seed + 1)
+
+    def saturate(mode, nreq=20000, lo=256, hi=1 << 14):
+        coalesce = mode == "batched"
+        srv = Server(budget_bytes=40 << 30, max_batch_requests=4096, max_inflight_batches=3 if coalesce else 1,
+                     coalesce=coalesce)
+        sizes = np.exp(sat_rng.uniform(math.log(lo), math.log(hi), nreq)).astype(np.int64)
+        offs = (sat_rng.integers(0, pool_n - hi, nreq) // 4) * 4
+        sp, kp, tp = S.data_ptr(), K.data_ptr(), T.data_ptr()
+        t0 = time.perf_counter()
+        ts = [srv.submit_ptr(sp + int(o) * 4, kp + int(o) * 4, tp + int(o) * 4, R, SIGMA, int(n))
+              for o, n in zip(offs, sizes)]
+        srv.drain(300000)
+        t1 = time.perf_counter()
+        lat = np.array([srv.latency_ns(t) for t in ts]) / 1e3
+        for t in ts:
+            srv.release(t)
+        st = srv.stats()
+        srv.close()
+        return {"requests": nreq, "options_per_s": float(sizes.sum() / (t1 - t0)),
+                "p50_us": float(np.percentile(lat, 50)), "p99_us": float(np.percentile(lat, 99)),
+                "launches": int(st["launches"])}
+
+    sat = {m: saturate(m) for m in ("batched", "launch_per_request")}
+    sat["throughput_ratio"] = sat["batched"]["options_per_s"] / sat["launch_per_request"]["options_per_s"]
+    out["saturation_small_requests"] = sat
+    return out
+
+
+# ------------------------------------------------------------- our arm
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    import nt2_gb300.api as api
+    from nt2_gb300._lib import lib
+    api.init(torch.cuda.current_device())
+    L = lib()
+    n = N_OPTIONS
+    S, K, T = bs_tables(n, seed=rank)
+    call = torch.empty_like(S)
+    put = torch.empty_like(S)
+    stream = torch.cuda.current_stream().cuda_stream
+    sp, kp, tp, cp, pp = S.data_ptr(), K.data_ptr(), T.data_ptr(), call.data_ptr(), put.data_ptr()
+
+    def step():
+        st = L.nt2cuda_blackscholes_f32(sp, kp, tp, R, SIGMA, cp, pp, n, 0, 0, stream)
+        if st:
+            raise RuntimeError(f"blackscholes status {st}")
+
+    sampler = ClockSampler(torch.cuda.current_device()).start()
+    time.sleep(0.3)
+    ms, t0, t1 = time_device(step, args.steps, max(args.warmup, 3), ws)
+    value = ws * n / (ms * 1e-3)
+    peak, peak_kind = peaks()
+    achieved = BYTES_PER_OPTION * n / (ms * 1e-3) / 1e9
+    traffic = profiled_traffic("k_blackscholes_f32_n16777216")
+
+    # e2e: host (pinned) buffers through the C ABI, copies inside the timed region
+    Sh, Kh, Th = (a.cpu().pin_memory() for a in (S, K, T))
+    ch = torch.empty(n, dtype=torch.float32).pin_memory()
+    ph = torch.empty(n, dtype=torch.float32).pin_memory()
+    hs = [a.data_ptr() for a in (Sh, Kh, Th, ch, ph)]
+
+    def e2e_step():
+        st = L.nt2cuda_blackscholes_f32_host(hs[0], hs[1], hs[2], R, SIGMA, hs[3], hs[4], n, 0, 0)
+        if st:
+            raise RuntimeError(f"blackscholes_host status {st}")
+
+    for _ in range(3):
+        e2e_step()
+    e2e_steps = max(3, min(args.steps, 200))
+    barrier(ws)
+    te0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    te1 = time.perf_counter()
+    e2e_ms = max_over_ranks((te1 - te0) * 1e3 / e2e_steps, ws)
+    # results of the e2e path equal the device path's
+    torch.cuda.synchronize()
+    same = bool(torch.equal(ch, call.cpu()) and torch.equal(ph, put.cpu()))
+    sampler.stop()
+    clocks = sampler.summary(t0, t1)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "options/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded counter-based uniforms: S~U[5,30], "
+        "K~U[1,100], T~U[0.25,10]; r=0.02, sigma=0.30)",
+        "config": {"workload": "Black-Scholes call+put, FP32, 2^24 options per GPU, normcdf via erfc, "
+                   "NT2 unfused arithmetic (bit-exact with the oracle)",
+                   "options_per_gpu": n, "parallelism": f"replicas x{ws}",
+                   "l2": "inputs+outputs 335 MB > 129 MB L2, no flush needed"},
+        "hbm_frac_measured": achieved / peak, "hbm_frac_nominal": achieved / NOMINAL_HBM_GBS,
+        "gb_per_s": achieved,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_launch": BYTES_PER_OPTION * n},
+        "e2e": {"value": ws * n / (e2e_ms * 1e-3), "unit": "options/s", "h2d_bytes_per_step": 12 * n,
+                "d2h_bytes_per_step": 8 * n, "ms_per_step": e2e_ms, "steps": e2e_steps,
+                "results_equal_device_path": same},
+        "gpu_launches": args.steps,
+        "clocks": clocks,
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline()
+    if rank == 0 and ws == 1 and not args.no_serving:
+        try:
+            line["serving"] = serving_bench()
+        except Exception as e:          # the headline number stands without it
+            line["serving"] = {"error": repr(e)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if args.suite and rank == 0:
+        for extra in suite(ws):
+            print(json.dumps(extra), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def suite(ws: int):
+    """One line per other configuration (device time, inputs resident, > L2 or flushed)."""
+    import torch
+    import nt2_gb300.api as api
+    from nt2_gb300 import video
+    peak, _ = peaks()
+    out = []
+
+    def line(name, ms, bytes_, units, unit):
+        gbs = bytes_ / (ms * 1e-3) / 1e9
+        return {"config": name, "ms": ms, "gb_per_s": gbs, "hbm_frac_measured": gbs / peak,
+                "hbm_frac_nominal": gbs / NOMINAL_HBM_GBS, "value": units / (ms * 1e-3), "unit": unit}
+
+    n = 1 << 24
+    x = torch.empty(n, device="cuda")
+    y = torch.empty(n, device="cuda")
+    api.fill_uniform(x, -1, 1, 1)
+    api.fill_uniform(y, -1, 1, 2)
+    ms, _, _ = time_device(lambda: api.saxpy(2.5, x, y), 200, 5, ws)
+    out.append(line("saxpy f32 2^24", ms, 12 * n, n, "elements/s"))
+    n = 1 << 26
+    x = torch.empty(n, device="cuda")
+    y = torch.empty(n, device="cuda")
+    api.fill_normal(x, 1)
+    api.fill_normal(y, 2)
+    o = torch.empty(1, device="cuda")
+    ms, _, _ = time_device(lambda: api.dot(x, y, out=o), 100, 5, ws)
+    out.append(line("sdot f32 2^26 compensated", ms, 8 * n, n, "elements/s"))
+    ms, _, _ = time_device(lambda: api.dot(x, y, compensated=False, out=o), 100, 5, ws)
+    out.append(line("sdot f32 2^26 plain", ms, 8 * n, n, "elements/s"))
+    rows, cols = 8192, 4096
+    A = torch.empty(rows * cols, device="cuda")
+    api.fill_normal(A, 3)
+    oc = torch.empty(cols, device="cuda")
+    orow = torch.empty(rows, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def with_flush(fn):
+        def f():
+            flush.zero_()
+            fn()
+        return f
+
+    def flush_ms():
+        m, _, _ = time_device(lambda: flush.zero_(), 50, 3, ws)
+        return m
+
+    fm = flush_ms()
+    ms, _, _ = time_device(with_flush(lambda: api.sum_colmajor(A, rows, cols, 1, out=oc)), 50, 3, ws)
+    out.append(line("inner_fold column sums 8192x4096 f32 compensated (L2 flushed)", ms - fm,
+                    4 * rows * cols + 4 * cols, rows * cols, "elements/s"))
+    ms, _, _ = time_device(with_flush(lambda: api.sum_colmajor(A, rows, cols, 2, out=orow)), 50, 3, ws)
+    out.append(line("outer_fold row sums 8192x4096 f32 compensated (L2 flushed)", ms - fm,
+                    4 * rows * cols + 4 * rows, rows * cols, "elements/s"))
+    n = 1 << 24
+    S = torch.empty(n, dtype=torch.float64, device="cuda")
+    K = torch.empty(n, dtype=torch.float64, device="cuda")
+    T = torch.empty(n, dtype=torch.float64, device="cuda")
+    api.fill_uniform(S, 5, 30, 1)
+    api.fill_uniform(K, 1, 100, 2)
+    api.fill_uniform(T, 0.25, 10, 3)
+    c = torch.empty_like(S)
+    p = torch.empty_like(S)
+    ms, _, _ = time_device(lambda: api.blackscholes(S, K, T, R, SIGMA, call=c, put=p), 20, 3, ws)
+    out.append(line("Black-Scholes f64 2^24 (FP64-issue bound)", ms, 40 * n, n, "options/s"))
+    del S, K, T, c, p
+    S, K, T = bs_tables(1 << 24, 5)
+    c = torch.empty_like(S)
+    p = torch.empty_like(S)
+    ms, _, _ = time_device(lambda: api.blackscholes(S, K, T, R, SIGMA, call=c, put=p, fused=True), 200, 5, ws)
+    out.append(line("Black-Scholes f32 2^24 fused FMA", ms, 20 * (1 << 24), 1 << 24, "options/s"))
+    ms, _, _ = time_device(lambda: api.blackscholes(S, K, T, R, SIGMA, call=c, put=p, cdf="fastnormcdf"), 200, 5,
+                           ws)
+    out.append(line("Black-Scholes f32 2^24 fastnormcdf", ms, 20 * (1 << 24), 1 << 24, "options/s"))
+    del S, K, T, c, p
+    batch = video.make_batch(256, 8, seed=11)
+    torch.cuda.synchronize()
+    plan = api.SigmaDeltaPlan(batch, 8, init=True)
+    ms, _, _ = time_device(plan.launch, 20, 3, ws)
+    pf = video.pixel_frames(batch, 8, True)
+    out.append(line("sigmadelta 256 streams x 8 frames uint8 (graph)", ms, video.bytes_moved(batch, 8, True), pf,
+                    "pixel-frames/s"))
+    plan.close()
+    return out
+
+
+# ---------------------------------------------------------- reference arm
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    L = oracle_lib.load()
+    sample = 1 << 20
+    rng = np.random.default_rng(1)
+    S = rng.uniform(5, 30, sample).astype(np.float32)
+    K = rng.uniform(1, 100, sample).astype(np.float32)
+    T = rng.uniform(0.25, 10, sample).astype(np.float32)
+    call = np.empty_like(S)
+    put = np.empty_like(S)
+    threads = L.nt2o_max_threads()
+    steps = args.steps
+    for _ in range(max(args.warmup, 3)):
+        L.nt2o_bs_f(S, K, T, R, SIGMA, call, put, sample, 0, threads)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        L.nt2o_bs_f(S, K, T, R, SIGMA, call, put, sample, 0, threads)
+    t1 = time.perf_counter()
+    ms = (t1 - t0) * 1e3 / steps
+    value = sample / (ms * 1e-3)
+    desc = (f"{sample} options per step (1/{N_OPTIONS // sample} of the 2^24-option batch); NT2's SIMD+OpenMP "
+            "Black-Scholes path restated in C (oracle/nt2_oracle.c) because NT2 itself needs Boost, which is "
+            "absent; scalar+OpenMP, as NT2 runs on aarch64 (no Boost.SIMD NEON backend)")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "options/s", "n_gpus": ws, "steps": steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "Black-Scholes call+put, FP32, normcdf via erfc (bounded CPU sample)",
+                   "options_per_step": sample},
+        "cpu_baseline": {"value": value, "unit": "options/s", "cores": threads, "kind": "port", "sample": desc},
+        "e2e": {"value": value, "unit": "options/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--suite", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,259 @@
+/*
+ * nt2cuda.h -- C ABI of the GB300 (sm_103a) evaluator for NT2 table
+ * expressions.
+ *
+ * NT2 evaluates `table = expression` through compile-time dispatch on a
+ * "site" (cpu_ < simd_ < openmp_/tbb_/hpx_ < shared_memory_) and never leaves
+ * the CPU.  This library is the device side of a new site: each entry point
+ * below is what that site's overloads of transform_, inner_fold_ and
+ * outer_fold_ call (or what any other language binds), with plain pointers
+ * and sizes only.  Paths in the citations are relative to the NT2 source tree.
+ *
+ * Conventions
+ *   - Table pointers are DEVICE pointers (HBM) unless the name ends in _host.
+ *     Tables are dense and column-major, as nt2::table is.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *     Calls are stream-ordered and return once the work is enqueued, except
+ *     the _host entry points, which return with the results in host memory.
+ *   - Every entry point returns an nt2cuda_status; none calls exit() or traps.
+ *   - `fused` = 0 evaluates NT2's fma/fnms/Horner steps unfused (bit-exact
+ *     with NT2 built without FMA contraction); 1 uses hardware FMA.
+ */
+#ifndef NT2CUDA_H_INCLUDED
+#define NT2CUDA_H_INCLUDED
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef void* nt2cuda_stream;
+
+/* Status codes.  NT2's OpenMP spawners capture worker exceptions and drop
+ * them (modules/arch/openmp/include/nt2/sdk/openmp/spawner/transform.hpp:40-69);
+ * here every failure is returned to the caller. */
+typedef enum {
+  NT2CUDA_OK = 0,
+  NT2CUDA_ERR_ARG = 1,        /* bad pointer, size, shape or option       */
+  NT2CUDA_ERR_OOM = 2,        /* device or pinned allocation failed       */
+  NT2CUDA_ERR_BUDGET = 3,     /* request exceeds the server memory budget */
+  NT2CUDA_ERR_LAUNCH = 4,     /* kernel launch failed                     */
+  NT2CUDA_ERR_TIMEOUT = 5,    /* a bounded wait ran out                   */
+  NT2CUDA_ERR_CUDA = 6,       /* other CUDA runtime error                 */
+  NT2CUDA_ERR_NOT_READY = 7,  /* asynchronous result not ready yet        */
+  NT2CUDA_ERR_ALIAS = 8,      /* tables of one statement partially overlap */
+  NT2CUDA_ERR_STATE = 9       /* object used in the wrong state           */
+} nt2cuda_status;
+
+const char* nt2cuda_status_string(int status);
+int nt2cuda_version(void);
+
+/* ------------------------------------------------------------ device ---- */
+/* Selects the device and creates its context.  Replaces the cuda_ site's
+ * implicit setup (modules/arch/cuda/include/nt2/sdk/cuda/cuda.hpp:16-24). */
+nt2cuda_status nt2cuda_init(int device);
+nt2cuda_status nt2cuda_device_info(int* sm_count, size_t* free_bytes, size_t* total_bytes);
+nt2cuda_status nt2cuda_last_cuda_error(int* code);
+
+/* Device-resident table storage.  Replaces cuda_buffer's cudaMalloc /
+ * cudaMemcpyAsync members (modules/arch/cuda/include/nt2/sdk/cuda/memory/buffer.hpp:36-242),
+ * whose host-to-device constructor copies a fixed 10 elements (:107-112);
+ * these copy exactly `bytes`. */
+nt2cuda_status nt2cuda_alloc(size_t bytes, void** ptr);
+nt2cuda_status nt2cuda_free(void* ptr);
+nt2cuda_status nt2cuda_alloc_host(size_t bytes, void** ptr);   /* pinned */
+nt2cuda_status nt2cuda_free_host(void* ptr);
+nt2cuda_status nt2cuda_memcpy_h2d(void* dst, const void* src, size_t bytes, nt2cuda_stream stream);
+nt2cuda_status nt2cuda_memcpy_d2h(void* dst, const void* src, size_t bytes, nt2cuda_stream stream);
+nt2cuda_status nt2cuda_memcpy_d2d(void* dst, const void* src, size_t bytes, nt2cuda_stream stream);
+nt2cuda_status nt2cuda_stream_create(nt2cuda_stream* stream);
+nt2cuda_status nt2cuda_stream_destroy(nt2cuda_stream stream);
+nt2cuda_status nt2cuda_stream_sync(nt2cuda_stream stream);
+
+/* ------------------------------------------------- elementwise transform -- */
+/* Elementwise functors for nt2cuda_map_*: NT2's exp/log/erfc/normcdf/
+ * fastnormcdf/sqrt (modules/core/exponential/include/nt2/exponential/functions/generic/exp.hpp:19-32,
+ * generic/log.hpp:20-31, modules/core/euler/include/nt2/euler/functions/simd/common/erfc.hpp:46-123,
+ * modules/core/statistics/include/nt2/statistics/functions/generic/normcdf.hpp:28-34,
+ * generic/fastnormcdf.hpp:33-55, boost/simd/arithmetic/functions/scalar/sqrt.hpp:21-62). */
+enum {
+  NT2CUDA_OP_EXP = 0,
+  NT2CUDA_OP_LOG = 1,
+  NT2CUDA_OP_ERFC = 2,
+  NT2CUDA_OP_NORMCDF = 3,
+  NT2CUDA_OP_FASTNORMCDF = 4, /* float only, as in NT2 */
+  NT2CUDA_OP_SQRT = 5
+};
+
+/* y = op(x).  Replaces `y = nt2::op(x)` evaluated by transform_
+ * (modules/core/base/include/nt2/core/functions/transform.hpp:23-69). */
+nt2cuda_status nt2cuda_map_f32(int op, const float* x, float* y, size_t n, int fused, nt2cuda_stream stream);
+nt2cuda_status nt2cuda_map_f64(int op, const double* x, double* y, size_t n, int fused, nt2cuda_stream stream);
+
+/* Y = alpha*X + Y (demo/saxpy/nt2/saxpy_nt2.cpp:39-42). */
+nt2cuda_status nt2cuda_saxpy_f32(float alpha, const float* x, float* y, size_t n, int fused, nt2cuda_stream stream);
+nt2cuda_status nt2cuda_saxpy_f64(double alpha, const double* x, double* y, size_t n, int fused, nt2cuda_stream stream);
+
+/* gr = 0.3*r + 0.59*g + 0.11*b (demo/rgb2grey/nt2/rgb2grey_nt2.cpp:42-45). */
+nt2cuda_status nt2cuda_rgb2grey_f32(const float* r, const float* g, const float* b, float* gr, size_t n,
+                                    int fused, nt2cuda_stream stream);
+
+/* Black-Scholes call and put over n options with scalar rate r and
+ * volatility sigma, as the NT2 statement
+ *   tie(call,put) = tie(fnms(e,cdf(d2),S*cdf(d1)), fnms(S,cdf(-d1),e*cdf(-d2)))
+ *   with d1 = (log(S/K) + fma(sqr(sigma),0.5,r)*T)/(sigma*sqrt(T)),
+ *        d2 = d1 - sigma*sqrt(T), e = K*exp(-r*T)
+ * in one pass (a tie() assignment, modules/core/container/table/include/nt2/core/functions/expr/tie.hpp:40-74).
+ * cdf_kind 0 = normcdf via erfc, 1 = fastnormcdf (float only). */
+nt2cuda_status nt2cuda_blackscholes_f32(const float* S, const float* K, const float* T, float r, float sigma,
+                                        float* call, float* put, size_t n, int cdf_kind, int fused,
+                                        nt2cuda_stream stream);
+nt2cuda_status nt2cuda_blackscholes_f64(const double* S, const double* K, const double* T, double r,
+                                        double sigma, double* call, double* put, size_t n, int fused,
+                                        nt2cuda_stream stream);
+
+/* The Black-Scholes demo statement, verbatim
+ * (demo/blackscholes/nt2/blackandscholes_nt2.cpp:55-59): five input tables,
+ * one output R = fnms(X*exp(-r*T), fastnormcdf(d2), S*fastnormcdf(d1)),
+ * d1 = log(S/X) + (fma(sqr(v),0.5,r)*T)/(v*sqrt(T)), d2 = fnms(v, sqrt(T), d1). */
+nt2cuda_status nt2cuda_blackscholes_demo_f32(const float* S, const float* X, const float* T, const float* r,
+                                             const float* v, float* R, size_t n, int fused,
+                                             nt2cuda_stream stream);
+
+/* Host-buffer form of nt2cuda_blackscholes_f32 for NT2 tables that live in
+ * host memory: copies in, evaluates and copies out in pipelined chunks on
+ * library-owned streams and device staging, and returns when call/put hold
+ * the results.  Host buffers should be pinned for full copy bandwidth. */
+nt2cuda_status nt2cuda_blackscholes_f32_host(const float* S, const float* K, const float* T, float r,
+                                             float sigma, float* call, float* put, size_t n, int cdf_kind,
+                                             int fused);
+
+/* ------------------------------------------------------------- folds ---- */
+/* globalsum(X) and globalsum(X*Y) (modules/core/reduction/include/nt2/core/functions/globalsum.hpp:75-88,
+ * demo/sdot/nt2/sdot_nt2.cpp:35-38): the inner_fold over one column of n
+ * elements.  *out is a DEVICE scalar.  compensated = 1 accumulates FP32 with
+ * TwoSum-compensated partials; 0 is the plain tree sum.  The block
+ * decomposition depends only on n, so results are bitwise reproducible.
+ * The first call on a stream allocates that stream's scratch. */
+nt2cuda_status nt2cuda_globalsum_f32(const float* x, size_t n, float* out, int compensated, nt2cuda_stream stream);
+nt2cuda_status nt2cuda_dot_f32(const float* x, const float* y, size_t n, float* out, int compensated,
+                               nt2cuda_stream stream);
+nt2cuda_status nt2cuda_globalsum_f64(const double* x, size_t n, double* out, nt2cuda_stream stream);
+nt2cuda_status nt2cuda_dot_f64(const double* x, const double* y, size_t n, double* out, nt2cuda_stream stream);
+
+/* sum(A,1): column sums of a rows x cols column-major table -> out[cols]
+ * (inner_fold, modules/core/reduction/include/nt2/core/functions/inner_fold.hpp:21-58,
+ *  modules/arch/shared_memory/include/nt2/core/functions/shared_memory/inner_fold.hpp:24-63). */
+nt2cuda_status nt2cuda_sum_inner_f32(const float* A, size_t rows, size_t cols, float* out, int compensated,
+                                     nt2cuda_stream stream);
+nt2cuda_status nt2cuda_sum_inner_f64(const double* A, size_t rows, size_t cols, double* out,
+                                     nt2cuda_stream stream);
+/* sum(A,2): row sums -> out[rows] (outer_fold,
+ * modules/core/reduction/include/nt2/core/functions/outer_fold.hpp:17-55,
+ * modules/arch/shared_memory/include/nt2/core/functions/shared_memory/outer_fold.hpp:22-51). */
+nt2cuda_status nt2cuda_sum_outer_f32(const float* A, size_t rows, size_t cols, float* out, int compensated,
+                                     nt2cuda_stream stream);
+nt2cuda_status nt2cuda_sum_outer_f64(const double* A, size_t rows, size_t cols, double* out,
+                                     nt2cuda_stream stream);
+
+/* --------------------------------------------------------- sigmadelta ---- */
+/* One grey video stream for the batched sigma-delta background subtraction
+ * (demo/sigmadelta/nt2/sigmadelta_nt2.cpp:37-58, 85-106).  frames holds
+ * nframes planes of width*height uint8 pixels, frame_stride bytes apart;
+ * labels receives one plane per processed frame, label_stride bytes apart;
+ * bkg and var (width*height each) are the background and variance state. */
+typedef struct {
+  const uint8_t* frames;
+  size_t frame_stride;
+  uint8_t* bkg;
+  uint8_t* var;
+  uint8_t* labels;
+  size_t label_stride;
+  uint32_t width;
+  uint32_t height;
+} nt2cuda_sd_stream;
+
+/* Process nframes frames of every stream in one persistent launch over a
+ * (stream, tile) work-list.  init = 1: bkg = frame 0, var = 1, then frames
+ * 1..nframes-1 are processed (nframes-1 label planes); init = 0: all nframes
+ * frames are processed from the given bkg/var.  `streams` is a HOST array. */
+nt2cuda_status nt2cuda_sigmadelta_batch_u8(const nt2cuda_sd_stream* streams, int nstreams, int nframes, int init,
+                                           nt2cuda_stream stream);
+
+/* The same work captured once in a CUDA graph and replayed. */
+typedef struct nt2cuda_sd_plan nt2cuda_sd_plan;
+nt2cuda_status nt2cuda_sigmadelta_plan_create(const nt2cuda_sd_stream* streams, int nstreams, int nframes, int init,
+                                              nt2cuda_stream stream, nt2cuda_sd_plan** plan);
+nt2cuda_status nt2cuda_sigmadelta_plan_launch(nt2cuda_sd_plan* plan, nt2cuda_stream stream);
+nt2cuda_status nt2cuda_sigmadelta_plan_destroy(nt2cuda_sd_plan* plan);
+
+/* ----------------------------------------------------------- serving ---- */
+/* Continuous-batching request server for Black-Scholes pricing requests.
+ * NT2 has no counterpart: it evaluates one synchronous statement at a time
+ * on the calling thread (modules/core/sdk/include/nt2/core/container/dsl/expression.hpp:161-191).
+ * Requests carry DEVICE input tables (which must stay valid until the request
+ * completes); outputs are written to server-owned device slots admitted
+ * against budget_bytes and stay resident until nt2cuda_server_release.
+ * coalesce = 1 launches every admitted request of a step in one kernel over a
+ * (request, tile) work-list; 0 launches one kernel per request.  At most
+ * max_inflight_batches launches are on the device at once. */
+typedef struct {
+  size_t budget_bytes;        /* device memory for request outputs          */
+  int max_batch_requests;     /* requests coalesced into one launch         */
+  int max_inflight_batches;   /* launches on the device at once (streams)   */
+  int coalesce;               /* 1 = batched work-list, 0 = launch per request */
+  int fused;
+  int cdf_kind;               /* 0 = normcdf, 1 = fastnormcdf               */
+  int wait_timeout_ms;        /* default bound of waits (<= 0: 60000)       */
+} nt2cuda_server_config;
+
+typedef struct {
+  uint64_t submitted, completed, batches, launches, options;
+  size_t reserved_bytes, peak_reserved_bytes;
+  uint64_t admission_waits;   /* submissions that could not be admitted at once */
+} nt2cuda_server_stats;
+
+typedef struct nt2cuda_server nt2cuda_server;
+
+nt2cuda_status nt2cuda_server_create(const nt2cuda_server_config* cfg, nt2cuda_server** server);
+nt2cuda_status nt2cuda_server_destroy(nt2cuda_server* server);
+/* Enqueue one request; never blocks.  Returns NT2CUDA_ERR_BUDGET if the
+ * request alone exceeds the budget.  The ticket identifies the request. */
+nt2cuda_status nt2cuda_server_submit(nt2cuda_server* server, const float* S, const float* K, const float* T, float r,
+                                     float sigma, size_t n, uint64_t* ticket);
+/* NT2CUDA_OK with the device output pointers once done, else NT2CUDA_ERR_NOT_READY. */
+nt2cuda_status nt2cuda_server_poll(nt2cuda_server* server, uint64_t ticket, float** call, float** put);
+/* Bounded wait (timeout_ms < 0: the configured default); NT2CUDA_ERR_TIMEOUT when it runs out. */
+nt2cuda_status nt2cuda_server_wait(nt2cuda_server* server, uint64_t ticket, int timeout_ms, float** call,
+                                   float** put);
+/* Return a finished request's output slots to the budget. */
+nt2cuda_status nt2cuda_server_release(nt2cuda_server* server, uint64_t ticket);
+/* Submit-to-completion latency of a finished request. */
+nt2cuda_status nt2cuda_server_latency_ns(nt2cuda_server* server, uint64_t ticket, uint64_t* ns);
+nt2cuda_status nt2cuda_server_drain(nt2cuda_server* server, int timeout_ms);
+nt2cuda_status nt2cuda_server_get_stats(nt2cuda_server* server, nt2cuda_server_stats* stats);
+
+/* ------------------------------------------------------------ tuning ---- */
+/* Times the transform variants of one entry point at size n on scratch
+ * tables and records the fastest for n's size bucket.  kernel: "saxpy_f32",
+ * "bs_f32", "bs_f64", "map_f32". */
+nt2cuda_status nt2cuda_autotune(const char* kernel, size_t n, int* best_unroll, int* best_waves, float* best_ms);
+/* Tuning table as text ("key@bucket unroll waves" lines). */
+nt2cuda_status nt2cuda_tuning_export(char* buf, size_t cap, size_t* needed);
+nt2cuda_status nt2cuda_tuning_import(const char* text, int* entries);
+
+/* ---------------------------------------------------- synthetic inputs ---- */
+/* Seeded counter-based generators (SplitMix64 of seed and element index),
+ * so a table's contents depend only on (seed, index). */
+nt2cuda_status nt2cuda_fill_uniform_f32(float* x, size_t n, float lo, float hi, uint64_t seed, nt2cuda_stream stream);
+nt2cuda_status nt2cuda_fill_uniform_f64(double* x, size_t n, double lo, double hi, uint64_t seed,
+                                        nt2cuda_stream stream);
+nt2cuda_status nt2cuda_fill_normal_f32(float* x, size_t n, uint64_t seed, nt2cuda_stream stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NT2CUDA_H_INCLUDED */

@@ -1,0 +1,253 @@
+"""Table-expression evaluation on the GPU through the nt2cuda C ABI.
+
+Functions take torch tensors as tables (device memory owned by torch) and
+call the C entry points on torch's current CUDA stream, so they compose
+with torch work.  Names and argument meanings follow NT2's
+(saxpy, blackscholes, globalsum, sum(A, dim), sigmadelta).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Sequence
+
+import torch
+
+from ._lib import SdStream, check, lib
+
+OPS = {"exp": 0, "log": 1, "erfc": 2, "normcdf": 3, "fastnormcdf": 4, "sqrt": 5}
+CDF = {"normcdf": 0, "fastnormcdf": 1}
+
+
+def _stream() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+def _dev(t: torch.Tensor, dtype=None, name: str = "table") -> int:
+    if not t.is_cuda:
+        raise ValueError(f"{name} must be a CUDA tensor")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+    if dtype is not None and t.dtype != dtype:
+        raise TypeError(f"{name} must be {dtype}, got {t.dtype}")
+    return t.data_ptr()
+
+
+def init(device: int = 0) -> None:
+    check(lib().nt2cuda_init(device), "init")
+
+
+def map_(op: str, x: torch.Tensor, out: torch.Tensor | None = None, fused: bool = False) -> torch.Tensor:
+    """out = nt2::op(x) for op in exp, log, erfc, normcdf, fastnormcdf, sqrt."""
+    out = torch.empty_like(x) if out is None else out
+    L = lib()
+    if x.dtype == torch.float32:
+        st = L.nt2cuda_map_f32(OPS[op], _dev(x), _dev(out, torch.float32), x.numel(), int(fused), _stream())
+    elif x.dtype == torch.float64:
+        st = L.nt2cuda_map_f64(OPS[op], _dev(x), _dev(out, torch.float64), x.numel(), int(fused), _stream())
+    else:
+        raise TypeError("map_ takes float32 or float64 tables")
+    check(st, f"map_({op})")
+    return out
+
+
+def saxpy(alpha: float, x: torch.Tensor, y: torch.Tensor, fused: bool = False) -> torch.Tensor:
+    """Y = alpha*X + Y, in place."""
+    if x.numel() != y.numel():
+        raise ValueError("x and y must have the same size")
+    L = lib()
+    if y.dtype == torch.float32:
+        st = L.nt2cuda_saxpy_f32(alpha, _dev(x, torch.float32), _dev(y), y.numel(), int(fused), _stream())
+    elif y.dtype == torch.float64:
+        st = L.nt2cuda_saxpy_f64(alpha, _dev(x, torch.float64), _dev(y), y.numel(), int(fused), _stream())
+    else:
+        raise TypeError("saxpy takes float32 or float64 tables")
+    check(st, "saxpy")
+    return y
+
+
+def rgb2grey(r: torch.Tensor, g: torch.Tensor, b: torch.Tensor, out: torch.Tensor | None = None,
+             fused: bool = False) -> torch.Tensor:
+    out = torch.empty_like(r) if out is None else out
+    check(lib().nt2cuda_rgb2grey_f32(_dev(r, torch.float32), _dev(g, torch.float32), _dev(b, torch.float32),
+                                     _dev(out, torch.float32), r.numel(), int(fused), _stream()), "rgb2grey")
+    return out
+
+
+def blackscholes(S: torch.Tensor, K: torch.Tensor, T: torch.Tensor, r: float, sigma: float,
+                 call: torch.Tensor | None = None, put: torch.Tensor | None = None,
+                 cdf: str = "normcdf", fused: bool = False):
+    """(call, put) prices for n options; float32 or float64 tables."""
+    n = S.numel()
+    if K.numel() != n or T.numel() != n:
+        raise ValueError("S, K, T must have the same size")
+    call = torch.empty_like(S) if call is None else call
+    put = torch.empty_like(S) if put is None else put
+    L = lib()
+    if S.dtype == torch.float32:
+        st = L.nt2cuda_blackscholes_f32(_dev(S), _dev(K, torch.float32), _dev(T, torch.float32), r, sigma,
+                                        _dev(call, torch.float32), _dev(put, torch.float32), n, CDF[cdf],
+                                        int(fused), _stream())
+    elif S.dtype == torch.float64:
+        if cdf != "normcdf":
+            raise ValueError("fastnormcdf is float32 only")
+        st = L.nt2cuda_blackscholes_f64(_dev(S), _dev(K, torch.float64), _dev(T, torch.float64), r, sigma,
+                                        _dev(call, torch.float64), _dev(put, torch.float64), n, int(fused),
+                                        _stream())
+    else:
+        raise TypeError("blackscholes takes float32 or float64 tables")
+    check(st, "blackscholes")
+    return call, put
+
+
+def blackscholes_demo(S, X, T, r, v, out=None, fused: bool = False) -> torch.Tensor:
+    """The demo statement with five float32 tables (r and v are tables)."""
+    out = torch.empty_like(S) if out is None else out
+    check(lib().nt2cuda_blackscholes_demo_f32(_dev(S, torch.float32), _dev(X, torch.float32),
+                                              _dev(T, torch.float32), _dev(r, torch.float32),
+                                              _dev(v, torch.float32), _dev(out, torch.float32), S.numel(),
+                                              int(fused), _stream()), "blackscholes_demo")
+    return out
+
+
+def blackscholes_host(S, K, T, r: float, sigma: float, call, put, cdf: str = "normcdf", fused: bool = False):
+    """Host-buffer form: S, K, T, call, put are CPU float32 tensors (pinned for best speed)."""
+    for t in (S, K, T, call, put):
+        if t.is_cuda or not t.is_contiguous() or t.dtype != torch.float32:
+            raise ValueError("host tables must be contiguous CPU float32 tensors")
+    check(lib().nt2cuda_blackscholes_f32_host(S.data_ptr(), K.data_ptr(), T.data_ptr(), r, sigma, call.data_ptr(),
+                                              put.data_ptr(), S.numel(), CDF[cdf], int(fused)),
+          "blackscholes_host")
+    return call, put
+
+
+def globalsum(x: torch.Tensor, compensated: bool = True, out: torch.Tensor | None = None) -> torch.Tensor:
+    """globalsum(X) as a 1-element device table."""
+    out = torch.empty(1, dtype=x.dtype, device=x.device) if out is None else out
+    L = lib()
+    if x.dtype == torch.float32:
+        st = L.nt2cuda_globalsum_f32(_dev(x), x.numel(), _dev(out, torch.float32), int(compensated), _stream())
+    elif x.dtype == torch.float64:
+        st = L.nt2cuda_globalsum_f64(_dev(x), x.numel(), _dev(out, torch.float64), _stream())
+    else:
+        raise TypeError("globalsum takes float32 or float64 tables")
+    check(st, "globalsum")
+    return out
+
+
+def dot(x: torch.Tensor, y: torch.Tensor, compensated: bool = True, out: torch.Tensor | None = None):
+    """globalsum(X*Y) (the sdot demo) as a 1-element device table."""
+    if x.numel() != y.numel():
+        raise ValueError("x and y must have the same size")
+    out = torch.empty(1, dtype=x.dtype, device=x.device) if out is None else out
+    L = lib()
+    if x.dtype == torch.float32:
+        st = L.nt2cuda_dot_f32(_dev(x), _dev(y, torch.float32), x.numel(), _dev(out, torch.float32),
+                               int(compensated), _stream())
+    elif x.dtype == torch.float64:
+        st = L.nt2cuda_dot_f64(_dev(x), _dev(y, torch.float64), x.numel(), _dev(out, torch.float64), _stream())
+    else:
+        raise TypeError("dot takes float32 or float64 tables")
+    check(st, "dot")
+    return out
+
+
+def sum_colmajor(A: torch.Tensor, rows: int, cols: int, dim: int, compensated: bool = True,
+                 out: torch.Tensor | None = None) -> torch.Tensor:
+    """sum(A, dim) of a rows x cols column-major table stored flat in A (NT2 layout).
+
+    dim = 1: column sums (inner_fold) -> cols values; dim = 2: row sums (outer_fold) -> rows values.
+    """
+    if A.numel() != rows * cols:
+        raise ValueError("A must hold rows*cols elements")
+    if dim not in (1, 2):
+        raise ValueError("dim must be 1 or 2")
+    m = cols if dim == 1 else rows
+    out = torch.empty(m, dtype=A.dtype, device=A.device) if out is None else out
+    L = lib()
+    if A.dtype == torch.float32:
+        fn = L.nt2cuda_sum_inner_f32 if dim == 1 else L.nt2cuda_sum_outer_f32
+        st = fn(_dev(A), rows, cols, _dev(out, torch.float32), int(compensated), _stream())
+    elif A.dtype == torch.float64:
+        fn = L.nt2cuda_sum_inner_f64 if dim == 1 else L.nt2cuda_sum_outer_f64
+        st = fn(_dev(A), rows, cols, _dev(out, torch.float64), _stream())
+    else:
+        raise TypeError("sum takes float32 or float64 tables")
+    check(st, f"sum(A,{dim})")
+    return out
+
+
+def sd_streams(entries: Sequence[dict]) -> C.Array:
+    """Build an nt2cuda_sd_stream array from dicts of tensors and sizes."""
+    arr = (SdStream * len(entries))()
+    for i, e in enumerate(entries):
+        arr[i] = SdStream(_dev(e["frames"], torch.uint8), e["frame_stride"], _dev(e["bkg"], torch.uint8),
+                          _dev(e["var"], torch.uint8), _dev(e["labels"], torch.uint8), e["label_stride"],
+                          e["width"], e["height"])
+    return arr
+
+
+def sigmadelta_batch(entries: Sequence[dict], nframes: int, init: bool = True) -> None:
+    arr = sd_streams(entries)
+    check(lib().nt2cuda_sigmadelta_batch_u8(arr, len(entries), nframes, int(init), _stream()), "sigmadelta_batch")
+
+
+class SigmaDeltaPlan:
+    """The batched sigma-delta launch captured once in a CUDA graph."""
+
+    def __init__(self, entries: Sequence[dict], nframes: int, init: bool = True):
+        self._arr = sd_streams(entries)
+        self._p = C.c_void_p()
+        check(lib().nt2cuda_sigmadelta_plan_create(self._arr, len(entries), nframes, int(init), _stream(),
+                                                   C.byref(self._p)), "sigmadelta_plan_create")
+
+    def launch(self) -> None:
+        check(lib().nt2cuda_sigmadelta_plan_launch(self._p, _stream()), "sigmadelta_plan_launch")
+
+    def close(self) -> None:
+        if self._p:
+            lib().nt2cuda_sigmadelta_plan_destroy(self._p)
+            self._p = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def fill_uniform(x: torch.Tensor, lo: float, hi: float, seed: int) -> torch.Tensor:
+    L = lib()
+    if x.dtype == torch.float32:
+        st = L.nt2cuda_fill_uniform_f32(_dev(x), x.numel(), lo, hi, seed, _stream())
+    elif x.dtype == torch.float64:
+        st = L.nt2cuda_fill_uniform_f64(_dev(x), x.numel(), lo, hi, seed, _stream())
+    else:
+        raise TypeError("fill_uniform takes float32 or float64 tables")
+    check(st, "fill_uniform")
+    return x
+
+
+def fill_normal(x: torch.Tensor, seed: int) -> torch.Tensor:
+    check(lib().nt2cuda_fill_normal_f32(_dev(x, torch.float32), x.numel(), seed, _stream()), "fill_normal")
+    return x
+
+
+def autotune(kernel: str, n: int):
+    u, w, ms = C.c_int(), C.c_int(), C.c_float()
+    check(lib().nt2cuda_autotune(kernel.encode(), n, C.byref(u), C.byref(w), C.byref(ms)), "autotune")
+    return u.value, w.value, ms.value
+
+
+def tuning_export() -> str:
+    L = lib()
+    need = C.c_size_t()
+    check(L.nt2cuda_tuning_export(None, 0, C.byref(need)), "tuning_export")
+    buf = C.create_string_buffer(need.value)
+    check(L.nt2cuda_tuning_export(buf, need.value, C.byref(need)), "tuning_export")
+    return buf.value.decode()
+
+
+def tuning_import(text: str) -> int:
+    n = C.c_int()
+    check(lib().nt2cuda_tuning_import(text.encode(), C.byref(n)), "tuning_import")
+    return n.value

@@ -1,0 +1,313 @@
+// capi_transform.cu -- C-ABI entry points for elementwise statements: the
+// NT2 transform_ site overload lowered for the demo and benchmark statements.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <mutex>
+#include <vector>
+#include "internal.cuh"
+#include "nt2cuda/blackscholes.cuh"
+#include "nt2cuda/expr.cuh"
+#include "nt2cuda/launch.cuh"
+
+using namespace nt2cuda;
+using namespace nt2cuda::detail_capi;
+
+namespace {
+
+template <class T, class E> inline assign<T, E> asg(T* out, E e) { return assign<T, E>{out, e}; }
+template <class T> inline term<T> tm(const T* p) { return term<T>{p}; }
+template <class T> inline scal<T> sc(T v) { return scal<T>{v}; }
+template <class Tag, class... C> inline node<Tag, C...> nd(C... c) { return node<Tag, C...>{c...}; }
+
+template <bool F, class P> nt2cuda_status run(const P& p, size_t n, nt2cuda_stream s, const char* key)
+{
+  return launch_status(transform<F>(p, n, as_stream(s), key));
+}
+
+template <bool F, class T> nt2cuda_status map_impl(int op, const T* x, T* y, size_t n, nt2cuda_stream s)
+{
+  auto X = tm(x);
+  switch (op) {
+    case NT2CUDA_OP_EXP: return run<F>(make_prog(asg(y, nd<tag::exp_>(X))), n, s, "map");
+    case NT2CUDA_OP_LOG: return run<F>(make_prog(asg(y, nd<tag::log_>(X))), n, s, "map");
+    case NT2CUDA_OP_ERFC: return run<F>(make_prog(asg(y, nd<tag::erfc_>(X))), n, s, "map");
+    case NT2CUDA_OP_NORMCDF: return run<F>(make_prog(asg(y, nd<tag::normcdf_>(X))), n, s, "map");
+    case NT2CUDA_OP_SQRT: return run<F>(make_prog(asg(y, nd<tag::sqrt_>(X))), n, s, "map");
+    case NT2CUDA_OP_FASTNORMCDF:
+      if constexpr (sizeof(T) == 4) return run<F>(make_prog(asg(y, nd<tag::fastnormcdf_>(X))), n, s, "map");
+      else return NT2CUDA_ERR_ARG;
+    default: return NT2CUDA_ERR_ARG;
+  }
+}
+
+// Y = alpha*X + Y; the proto optimizer turns a*b+c into fma(a,b,c)
+// (boost/simd/operator/functions/optimize/plus.hpp:20-45).
+template <bool F, class T> nt2cuda_status saxpy_impl(T a, const T* x, T* y, size_t n, nt2cuda_stream s)
+{
+  return run<F>(make_prog(asg(y, nd<tag::fma_>(sc(a), tm(x), tm((const T*)y)))), n, s,
+                sizeof(T) == 4 ? "saxpy_f32" : "saxpy_f64");
+}
+
+// gr = T(0.3)*r + T(0.59)*g + T(0.11)*b  ->  fma(0.11, b, fma(0.3, r, 0.59*g))
+template <bool F> nt2cuda_status rgb2grey_impl(const float* r, const float* g, const float* b, float* gr,
+                                               size_t n, nt2cuda_stream s)
+{
+  auto e = nd<tag::fma_>(sc(0.11f), tm(b),
+                         nd<tag::fma_>(sc(0.3f), tm(r), nd<tag::multiplies_>(sc(0.59f), tm(g))));
+  return run<F>(make_prog(asg(gr, e)), n, s, "rgb2grey");
+}
+
+// The demo statement, lowered through the generic expression engine.
+template <bool F> nt2cuda_status bs_demo_impl(const float* S, const float* X, const float* T, const float* r,
+                                              const float* v, float* R, size_t n, nt2cuda_stream s)
+{
+  auto Sa = tm(S); auto Xa = tm(X); auto Ta = tm(T); auto ra = tm(r); auto va = tm(v);
+  auto da = nd<tag::sqrt_>(Ta);
+  // log(Sa/Xa) + (fma(sqr(va),0.5,ra)*Ta)/(va*da)
+  auto d1 = nd<tag::plus_>(nd<tag::log_>(nd<tag::divides_>(Sa, Xa)),
+                           nd<tag::divides_>(nd<tag::multiplies_>(nd<tag::fma_>(nd<tag::sqr_>(va), sc(0.5f), ra), Ta),
+                                             nd<tag::multiplies_>(va, da)));
+  auto d2 = nd<tag::fnms_>(va, da, d1);
+  auto R0 = nd<tag::fnms_>(nd<tag::multiplies_>(Xa, nd<tag::exp_>(nd<tag::multiplies_>(nd<tag::unary_minus_>(ra), Ta))),
+                           nd<tag::fastnormcdf_>(d2),
+                           nd<tag::multiplies_>(Sa, nd<tag::fastnormcdf_>(d1)));
+  return run<F>(make_prog(asg(R, R0)), n, s, "bs_demo_f32");
+}
+
+template <class T> bool aligned16(const T* p) { return ((uintptr_t)p & 15u) == 0; }
+
+template <class T, int CDF, bool F>
+nt2cuda_status bs_launch(const T* S, const T* K, const T* Tm, T r, T v, T* call, T* put, size_t n,
+                         cudaStream_t s, int unroll, int waves)
+{
+  if (n == 0) return NT2CUDA_OK;
+  size_t nn = n;
+  void* args[] = {(void*)&S, (void*)&K, (void*)&Tm, (void*)&r, (void*)&v, (void*)&call, (void*)&put, (void*)&nn};
+  if (!(aligned16(S) && aligned16(K) && aligned16(Tm) && aligned16(call) && aligned16(put)))
+    return launch_status(launch_persistent(k_blackscholes_scalar<T, CDF, F>, n, 256, waves, s, args));
+  constexpr int V = 16 / (int)sizeof(T);
+  size_t groups = n / V;
+  switch (unroll) {
+    case 1: return launch_status(launch_persistent(k_blackscholes<T, CDF, F, 1>, groups, 256, waves, s, args));
+    case 4: return launch_status(launch_persistent(k_blackscholes<T, CDF, F, 4>, groups, 256, waves, s, args));
+    default: return launch_status(launch_persistent(k_blackscholes<T, CDF, F, 2>, groups, 256, waves, s, args));
+  }
+}
+
+template <class T>
+nt2cuda_status bs_dispatch(const T* S, const T* K, const T* Tm, T r, T v, T* call, T* put, size_t n,
+                           int cdf, int fused, cudaStream_t s, int unroll, int waves)
+{
+  if (n && (!S || !K || !Tm || !call || !put)) return NT2CUDA_ERR_ARG;
+  if (cdf != CDF_NORMCDF && cdf != CDF_FASTNORMCDF) return NT2CUDA_ERR_ARG;
+  if constexpr (sizeof(T) == 8) {
+    if (cdf != CDF_NORMCDF) return NT2CUDA_ERR_ARG;
+    return fused ? bs_launch<T, CDF_NORMCDF, true>(S, K, Tm, r, v, call, put, n, s, unroll, waves)
+                 : bs_launch<T, CDF_NORMCDF, false>(S, K, Tm, r, v, call, put, n, s, unroll, waves);
+  } else {
+    if (cdf == CDF_FASTNORMCDF)
+      return fused ? bs_launch<T, CDF_FASTNORMCDF, true>(S, K, Tm, r, v, call, put, n, s, unroll, waves)
+                   : bs_launch<T, CDF_FASTNORMCDF, false>(S, K, Tm, r, v, call, put, n, s, unroll, waves);
+    return fused ? bs_launch<T, CDF_NORMCDF, true>(S, K, Tm, r, v, call, put, n, s, unroll, waves)
+                 : bs_launch<T, CDF_NORMCDF, false>(S, K, Tm, r, v, call, put, n, s, unroll, waves);
+  }
+}
+
+const char* bs_key(size_t bytes) { return bytes == 4 ? "bs_f32" : "bs_f64"; }
+
+// ---------------------------------------------- host-buffer pipeline state
+struct host_pipeline {
+  std::mutex m;
+  static constexpr int NS = 3;
+  cudaStream_t st[NS] = {nullptr, nullptr, nullptr};
+  float* buf[NS][5] = {};
+  size_t chunk = 0;
+  int dev = -1;
+};
+host_pipeline& hp() { static host_pipeline p; return p; }
+
+}  // namespace
+
+extern "C" {
+
+nt2cuda_status nt2cuda_map_f32(int op, const float* x, float* y, size_t n, int fused, nt2cuda_stream s)
+{
+  if (n && (!x || !y)) return NT2CUDA_ERR_ARG;
+  return fused ? map_impl<true>(op, x, y, n, s) : map_impl<false>(op, x, y, n, s);
+}
+
+nt2cuda_status nt2cuda_map_f64(int op, const double* x, double* y, size_t n, int fused, nt2cuda_stream s)
+{
+  if (n && (!x || !y)) return NT2CUDA_ERR_ARG;
+  return fused ? map_impl<true>(op, x, y, n, s) : map_impl<false>(op, x, y, n, s);
+}
+
+nt2cuda_status nt2cuda_saxpy_f32(float a, const float* x, float* y, size_t n, int fused, nt2cuda_stream s)
+{
+  if (n && (!x || !y)) return NT2CUDA_ERR_ARG;
+  return fused ? saxpy_impl<true>(a, x, y, n, s) : saxpy_impl<false>(a, x, y, n, s);
+}
+
+nt2cuda_status nt2cuda_saxpy_f64(double a, const double* x, double* y, size_t n, int fused, nt2cuda_stream s)
+{
+  if (n && (!x || !y)) return NT2CUDA_ERR_ARG;
+  return fused ? saxpy_impl<true>(a, x, y, n, s) : saxpy_impl<false>(a, x, y, n, s);
+}
+
+nt2cuda_status nt2cuda_rgb2grey_f32(const float* r, const float* g, const float* b, float* gr, size_t n,
+                                    int fused, nt2cuda_stream s)
+{
+  if (n && (!r || !g || !b || !gr)) return NT2CUDA_ERR_ARG;
+  return fused ? rgb2grey_impl<true>(r, g, b, gr, n, s) : rgb2grey_impl<false>(r, g, b, gr, n, s);
+}
+
+nt2cuda_status nt2cuda_blackscholes_demo_f32(const float* S, const float* X, const float* T, const float* r,
+                                             const float* v, float* R, size_t n, int fused, nt2cuda_stream s)
+{
+  if (n && (!S || !X || !T || !r || !v || !R)) return NT2CUDA_ERR_ARG;
+  return fused ? bs_demo_impl<true>(S, X, T, r, v, R, n, s) : bs_demo_impl<false>(S, X, T, r, v, R, n, s);
+}
+
+nt2cuda_status nt2cuda_blackscholes_f32(const float* S, const float* K, const float* T, float r, float sigma,
+                                        float* call, float* put, size_t n, int cdf_kind, int fused,
+                                        nt2cuda_stream s)
+{
+  tuning::params p = tuning::lookup(bs_key(4), n);
+  return bs_dispatch<float>(S, K, T, r, sigma, call, put, n, cdf_kind, fused, as_stream(s), p.unroll, p.waves);
+}
+
+nt2cuda_status nt2cuda_blackscholes_f64(const double* S, const double* K, const double* T, double r,
+                                        double sigma, double* call, double* put, size_t n, int fused,
+                                        nt2cuda_stream s)
+{
+  tuning::params p = tuning::lookup(bs_key(8), n);
+  return bs_dispatch<double>(S, K, T, r, sigma, call, put, n, CDF_NORMCDF, fused, as_stream(s), p.unroll,
+                             p.waves);
+}
+
+nt2cuda_status nt2cuda_blackscholes_f32_host(const float* S, const float* K, const float* T, float r,
+                                             float sigma, float* call, float* put, size_t n, int cdf_kind,
+                                             int fused)
+{
+  if (n == 0) return NT2CUDA_OK;
+  if (!S || !K || !T || !call || !put) return NT2CUDA_ERR_ARG;
+  host_pipeline& P = hp();
+  std::lock_guard<std::mutex> g(P.m);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const size_t chunk = (size_t)1 << 21;   // options per pipeline stage (8 MiB per table)
+  if (P.dev != dev || P.chunk < chunk) {
+    for (int i = 0; i < host_pipeline::NS; ++i) {
+      for (int j = 0; j < 5; ++j) { if (P.buf[i][j]) cudaFree(P.buf[i][j]); P.buf[i][j] = nullptr; }
+      if (P.st[i]) cudaStreamDestroy(P.st[i]);
+      P.st[i] = nullptr;
+    }
+    P.chunk = 0;
+    P.dev = -1;
+    for (int i = 0; i < host_pipeline::NS; ++i) {
+      cudaError_t e = cudaStreamCreateWithFlags(&P.st[i], cudaStreamNonBlocking);
+      if (e != cudaSuccess) return from_cuda(e);
+      for (int j = 0; j < 5; ++j) {
+        e = cudaMalloc(&P.buf[i][j], chunk * sizeof(float));
+        if (e != cudaSuccess) return from_cuda(e);
+      }
+    }
+    P.chunk = chunk;
+    P.dev = dev;
+  }
+  tuning::params tp = tuning::lookup(bs_key(4), chunk);
+  size_t nchunks = (n + chunk - 1) / chunk;
+  for (size_t c = 0; c < nchunks; ++c) {
+    int i = (int)(c % host_pipeline::NS);
+    cudaStream_t st = P.st[i];
+    size_t off = c * chunk, cnt = (n - off) < chunk ? (n - off) : chunk;
+    size_t b = cnt * sizeof(float);
+    float** d = P.buf[i];
+    cudaMemcpyAsync(d[0], S + off, b, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(d[1], K + off, b, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(d[2], T + off, b, cudaMemcpyHostToDevice, st);
+    nt2cuda_status rs = bs_dispatch<float>(d[0], d[1], d[2], r, sigma, d[3], d[4], cnt, cdf_kind, fused, st,
+                                           tp.unroll, tp.waves);
+    if (rs != NT2CUDA_OK) { for (int k = 0; k < host_pipeline::NS; ++k) cudaStreamSynchronize(P.st[k]); return rs; }
+    cudaMemcpyAsync(call + off, d[3], b, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(put + off, d[4], b, cudaMemcpyDeviceToHost, st);
+  }
+  cudaError_t err = cudaSuccess;
+  for (int i = 0; i < host_pipeline::NS; ++i) {
+    cudaError_t e = cudaStreamSynchronize(P.st[i]);
+    if (e != cudaSuccess) err = e;
+  }
+  return from_cuda(err);
+}
+
+// ------------------------------------------------------------ autotuner
+nt2cuda_status nt2cuda_autotune(const char* kernel, size_t n, int* best_unroll, int* best_waves, float* best_ms)
+{
+  if (!kernel || n == 0) return NT2CUDA_ERR_ARG;
+  std::string k(kernel);
+  const bool f64 = (k == "bs_f64" || k == "saxpy_f64");
+  const size_t es = f64 ? 8 : 4;
+  if (!(k == "bs_f32" || k == "bs_f64" || k == "saxpy_f32" || k == "saxpy_f64")) return NT2CUDA_ERR_ARG;
+  void* buf[5] = {};
+  for (int j = 0; j < 5; ++j) {
+    cudaError_t e = cudaMalloc(&buf[j], n * es);
+    if (e != cudaSuccess) { for (int q = 0; q < j; ++q) cudaFree(buf[q]); return from_cuda(e); }
+  }
+  cudaStream_t s;
+  cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  if (f64) {
+    nt2cuda_fill_uniform_f64((double*)buf[0], n, 5.0, 30.0, 1, s);
+    nt2cuda_fill_uniform_f64((double*)buf[1], n, 1.0, 100.0, 2, s);
+    nt2cuda_fill_uniform_f64((double*)buf[2], n, 0.25, 10.0, 3, s);
+  } else {
+    nt2cuda_fill_uniform_f32((float*)buf[0], n, 5.0f, 30.0f, 1, s);
+    nt2cuda_fill_uniform_f32((float*)buf[1], n, 1.0f, 100.0f, 2, s);
+    nt2cuda_fill_uniform_f32((float*)buf[2], n, 0.25f, 10.0f, 3, s);
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int unrolls[3] = {1, 2, 4};
+  const int wavesv[3] = {1, 2, 4};
+  float best = 1e30f;
+  tuning::params bp;
+  nt2cuda_status st = NT2CUDA_OK;
+  for (int ui = 0; ui < 3 && st == NT2CUDA_OK; ++ui)
+    for (int wi = 0; wi < 3 && st == NT2CUDA_OK; ++wi) {
+      auto once = [&]() -> nt2cuda_status {
+        if (k == "bs_f32")
+          return bs_dispatch<float>((float*)buf[0], (float*)buf[1], (float*)buf[2], 0.02f, 0.30f, (float*)buf[3],
+                                    (float*)buf[4], n, CDF_NORMCDF, 0, s, unrolls[ui], wavesv[wi]);
+        if (k == "bs_f64")
+          return bs_dispatch<double>((double*)buf[0], (double*)buf[1], (double*)buf[2], 0.02, 0.30,
+                                     (double*)buf[3], (double*)buf[4], n, CDF_NORMCDF, 0, s, unrolls[ui],
+                                     wavesv[wi]);
+        tuning::set(k.c_str(), n, tuning::params{unrolls[ui], wavesv[wi]});
+        if (k == "saxpy_f32") return nt2cuda_saxpy_f32(2.5f, (float*)buf[0], (float*)buf[1], n, 0, s);
+        return nt2cuda_saxpy_f64(2.5, (double*)buf[0], (double*)buf[1], n, 0, s);
+      };
+      for (int w = 0; w < 2 && st == NT2CUDA_OK; ++w) st = once();
+      cudaEventRecord(e0, s);
+      const int reps = 5;
+      for (int rr = 0; rr < reps && st == NT2CUDA_OK; ++rr) st = once();
+      cudaEventRecord(e1, s);
+      cudaEventSynchronize(e1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      ms /= reps;
+      if (ms < best) { best = ms; bp = tuning::params{unrolls[ui], wavesv[wi]}; }
+    }
+  if (st == NT2CUDA_OK) tuning::set(k.c_str(), n, bp);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamSynchronize(s);
+  cudaStreamDestroy(s);
+  for (int j = 0; j < 5; ++j) cudaFree(buf[j]);
+  if (st != NT2CUDA_OK) return st;
+  if (best_unroll) *best_unroll = bp.unroll;
+  if (best_waves) *best_waves = bp.waves;
+  if (best_ms) *best_ms = best;
+  return NT2CUDA_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,110 @@
+// nt2cuda/blackscholes.cuh -- the Black-Scholes call/put statement lowered
+// by hand into one kernel.
+//
+// NT2 user code:
+//   da  = sqrt(T);  vda = v*da;
+//   d1  = (log(S/K) + fma(sqr(v),0.5,r)*T) / vda;   d2 = d1 - vda;
+//   e   = K*exp(-r*T);
+//   tie(call, put) = tie(fnms(e, normcdf(d2), S*normcdf(d1)),
+//                        fnms(S, normcdf(-d1), e*normcdf(-d2)));
+// (modules/core/container/table/include/nt2/core/functions/expr/tie.hpp:40-74 for tie,
+//  demo/blackscholes/nt2_merged/blackandscholes_nt2_merged.cpp:57-64 for the merged form).
+// The generic lowering in expr.cuh would evaluate four erfc; here normcdf(x)
+// and normcdf(-x) share one erfc core (math::normcdf_pair), which is
+// bit-identical because NT2's erfc only uses the sign and |argument|.  The
+// scalar subexpression fma(sqr(v),0.5,r) is formed once per thread; NT2
+// forms it per element from the same splatted scalars, with the same result.
+// The proto optimizer's a + b*c -> fma(b,c,a) rewrite
+// (modules/boost/simd/base/include/boost/simd/operator/functions/optimize/plus.hpp:20-45)
+// applies to log(S/K) + c*T, which is why that sum is a madd.
+#pragma once
+#include <cuda_runtime.h>
+#include "math.cuh"
+#include "memory.cuh"
+
+namespace nt2cuda {
+
+enum { CDF_NORMCDF = 0, CDF_FASTNORMCDF = 1 };
+
+template <class T, int CDF, bool F>
+__device__ __forceinline__ void bs_lane(T S, T K, T Tm, T r, T v, T c, T& call, T& put)
+{
+  using namespace math;
+  T da = sqrt_(Tm);
+  T vda = mul(v, da);
+  T d1 = div(madd<F>(c, Tm, log<F>(div(S, K))), vda);
+  T d2 = sub(d1, vda);
+  T e = mul(K, exp<F>(mul(-r, Tm)));
+  T n1, m1, n2, m2;
+  if constexpr (CDF == CDF_FASTNORMCDF) {
+    fastnormcdf_pair<F>(d1, n1, m1);
+    fastnormcdf_pair<F>(d2, n2, m2);
+  } else {
+    normcdf_pair<F>(d1, n1, m1);
+    normcdf_pair<F>(d2, n2, m2);
+  }
+  call = nmsub<F>(e, n2, mul(S, n1));
+  put = nmsub<F>(S, m1, mul(e, m2));
+}
+
+// V options per thread per group (16 bytes of each input), U groups in
+// flight per grid-stride trip.
+template <class T, int CDF, bool F, int U>
+__global__ void __launch_bounds__(256) k_blackscholes(const T* __restrict__ S, const T* __restrict__ K,
+                                                      const T* __restrict__ Tm, T r, T v,
+                                                      T* __restrict__ call, T* __restrict__ put, size_t n)
+{
+  constexpr int V = 16 / (int)sizeof(T);
+  const T c = math::madd<F>(math::mul(v, v), T(0.5), r);
+  const size_t ngroups = n / V;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t g = tid;
+  for (; g + (size_t)(U - 1) * stride < ngroups; g += (size_t)U * stride) {
+    T s[U][V], k[U][V], t[U][V];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      size_t i = (g + (size_t)u * stride) * V;
+      mem::load_vec<T, V, true>(S, i, s[u]);
+      mem::load_vec<T, V, true>(K, i, k[u]);
+      mem::load_vec<T, V, true>(Tm, i, t[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      T oc[V], op[V];
+#pragma unroll
+      for (int l = 0; l < V; ++l) bs_lane<T, CDF, F>(s[u][l], k[u][l], t[u][l], r, v, c, oc[l], op[l]);
+      size_t i = (g + (size_t)u * stride) * V;
+      mem::store_vec<T, V>(call, i, oc);
+      mem::store_vec<T, V>(put, i, op);
+    }
+  }
+  for (; g < ngroups; g += stride) {
+    T s[V], k[V], t[V], oc[V], op[V];
+    size_t i = g * V;
+    mem::load_vec<T, V, true>(S, i, s);
+    mem::load_vec<T, V, true>(K, i, k);
+    mem::load_vec<T, V, true>(Tm, i, t);
+#pragma unroll
+    for (int l = 0; l < V; ++l) bs_lane<T, CDF, F>(s[l], k[l], t[l], r, v, c, oc[l], op[l]);
+    mem::store_vec<T, V>(call, i, oc);
+    mem::store_vec<T, V>(put, i, op);
+  }
+  const size_t tail0 = ngroups * V;
+  if (tid < n - tail0) {
+    size_t i = tail0 + tid;
+    bs_lane<T, CDF, F>(S[i], K[i], Tm[i], r, v, c, call[i], put[i]);
+  }
+}
+
+// Misaligned tables: one option per thread per trip.
+template <class T, int CDF, bool F>
+__global__ void __launch_bounds__(256) k_blackscholes_scalar(const T* S, const T* K, const T* Tm, T r, T v,
+                                                             T* call, T* put, size_t n)
+{
+  const T c = math::madd<F>(math::mul(v, v), T(0.5), r);
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    bs_lane<T, CDF, F>(S[i], K[i], Tm[i], r, v, c, call[i], put[i]);
+}
+
+}  // namespace nt2cuda

@@ -1,0 +1,325 @@
+// nt2cuda/expr.cuh -- device mirror of an NT2 table expression and its
+// compile-time lowering into one fused elementwise kernel.
+//
+// An NT2 assignment `out = f(g(X), Y, s)` is a Boost.Proto tree whose leaves
+// are table terminals and splatted scalars
+// (modules/core/sdk/include/nt2/core/container/dsl/expression.hpp:161-191);
+// NT2 evaluates it per index in the SIMD transform loop
+// (modules/core/base/include/nt2/core/functions/simd/transform.hpp:40-57),
+// recursing through the tree (modules/core/sdk/include/nt2/dsl/functions/generic/run.hpp:180-222)
+// down to terminal loads and scalar splats
+// (modules/core/sdk/include/nt2/dsl/functions/container/terminal.hpp:77-129,180-198).
+//
+// Here the same tree is a plain C++ type: term<T> (a table in HBM),
+// scal<T> (a scalar), node<Tag, Children...>.  `regs<E,V>` mirrors the tree
+// with V register lanes per terminal; `load` fills them with 16-byte loads,
+// `get(l)` evaluates the tree on lane l.  `assign<T,E>` pairs an output table
+// with an expression, and a program is a list of assigns (several for NT2's
+// tie(), modules/core/container/table/include/nt2/core/functions/expr/tie.hpp:40-74).
+// k_transform<Prog> is the single fused kernel for the whole statement.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+#include <limits>
+#include <type_traits>
+#include "math.cuh"
+#include "memory.cuh"
+
+namespace nt2cuda {
+
+// ------------------------------------------------------------------- tags
+// Functor tags, named after NT2's (boost::simd::tag::plus_, nt2::tag::exp_, ...).
+namespace tag {
+struct plus_ {}; struct minus_ {}; struct multiplies_ {}; struct divides_ {};
+struct unary_minus_ {}; struct fma_ {}; struct fnms_ {}; struct sqr_ {}; struct sqrt_ {};
+struct rec_ {}; struct abs_ {}; struct exp_ {}; struct log_ {}; struct erfc_ {};
+struct normcdf_ {}; struct fastnormcdf_ {}; struct max_ {}; struct min_ {};
+struct adds_ {}; struct subs_ {}; struct selinc_ {}; struct seldec_ {}; struct if_else_ {};
+struct if_zero_else_one_ {}; struct is_less_ {}; struct is_greater_ {};
+struct is_less_equal_ {}; struct is_greater_equal_ {}; struct is_equal_ {};
+struct is_not_equal_ {}; struct oneminus_ {}; struct minusone_ {};
+}  // namespace tag
+
+// ------------------------------------------------------------ tree nodes
+template <class T> struct term { const T* p; };
+template <class T> struct scal { T v; };
+template <class Tag, class... C> struct node;
+template <class Tag, class A> struct node<Tag, A> { A a; };
+template <class Tag, class A, class B> struct node<Tag, A, B> { A a; B b; };
+template <class Tag, class A, class B, class C> struct node<Tag, A, B, C> { A a; B b; C c; };
+
+template <class T, class E> struct assign { T* out; E e; };
+
+// ---------------------------------------------------------------- functors
+// One lane of each functor.  F selects fused multiply-adds (see math.cuh).
+template <class Tag, bool F> struct fn;
+
+#define NT2CUDA_BIN(TAG, EXPR)                                                   \
+  template <bool F> struct fn<tag::TAG, F> {                                     \
+    template <class A, class B>                                                  \
+    __device__ __forceinline__ static auto apply(A a, B b) { return EXPR; }      \
+  };
+#define NT2CUDA_UN(TAG, EXPR)                                                    \
+  template <bool F> struct fn<tag::TAG, F> {                                     \
+    template <class A>                                                           \
+    __device__ __forceinline__ static auto apply(A a) { return EXPR; }           \
+  };
+
+namespace detail {
+template <class T> __device__ __forceinline__ T add(T a, T b) {
+  if constexpr (std::is_floating_point<T>::value) return math::add(a, b); else return (T)(a + b); }
+template <class T> __device__ __forceinline__ T sub(T a, T b) {
+  if constexpr (std::is_floating_point<T>::value) return math::sub(a, b); else return (T)(a - b); }
+template <class T> __device__ __forceinline__ T mul(T a, T b) {
+  if constexpr (std::is_floating_point<T>::value) return math::mul(a, b); else return (T)(a * b); }
+template <class T> __device__ __forceinline__ T dv(T a, T b) {
+  if constexpr (std::is_floating_point<T>::value) return math::div(a, b); else return (T)(a / b); }
+template <bool F, class T> __device__ __forceinline__ T madd(T a, T b, T c) {
+  if constexpr (std::is_floating_point<T>::value) return math::madd<F>(a, b, c); else return (T)(a * b + c); }
+template <bool F, class T> __device__ __forceinline__ T nmsub(T a, T b, T c) {
+  if constexpr (std::is_floating_point<T>::value) return math::nmsub<F>(a, b, c); else return (T)(c - a * b); }
+// saturated add/sub of unsigned integers (boost/simd/arithmetic/functions/scalar/adds.hpp:65)
+template <class T> __device__ __forceinline__ T adds(T a, T b) {
+  if constexpr (std::is_floating_point<T>::value) return math::add(a, b);
+  else if constexpr (std::is_unsigned<T>::value) { T s = (T)(a + b); return s < a ? (T)~T(0) : s; }
+  else {
+    using W = long long; W s = (W)a + (W)b;
+    W lo = (W)std::numeric_limits<T>::min(), hi = (W)std::numeric_limits<T>::max();
+    return (T)(s < lo ? lo : (s > hi ? hi : s));
+  }
+}
+template <class T> __device__ __forceinline__ T subs(T a, T b) {
+  if constexpr (std::is_floating_point<T>::value) return math::sub(a, b);
+  else if constexpr (std::is_unsigned<T>::value) { return a > b ? (T)(a - b) : (T)0; }
+  else {
+    using W = long long; W s = (W)a - (W)b;
+    W lo = (W)std::numeric_limits<T>::min(), hi = (W)std::numeric_limits<T>::max();
+    return (T)(s < lo ? lo : (s > hi ? hi : s));
+  }
+}
+}  // namespace detail
+
+NT2CUDA_BIN(plus_, detail::add(a, (A)b))
+NT2CUDA_BIN(minus_, detail::sub(a, (A)b))
+NT2CUDA_BIN(multiplies_, detail::mul(a, (A)b))
+NT2CUDA_BIN(divides_, detail::dv(a, (A)b))
+NT2CUDA_BIN(max_, (a > (A)b ? a : (A)b))
+NT2CUDA_BIN(min_, (a < (A)b ? a : (A)b))
+NT2CUDA_BIN(adds_, detail::adds(a, (A)b))
+NT2CUDA_BIN(subs_, detail::subs(a, (A)b))
+NT2CUDA_BIN(is_less_, (bool)(a < b))
+NT2CUDA_BIN(is_greater_, (bool)(a > b))
+NT2CUDA_BIN(is_less_equal_, (bool)(a <= b))
+NT2CUDA_BIN(is_greater_equal_, (bool)(a >= b))
+NT2CUDA_BIN(is_equal_, (bool)(a == b))
+NT2CUDA_BIN(is_not_equal_, (bool)(a != b))
+// selinc(c,x) = c ? x+1 : x ; seldec(c,x) = c ? x-1 : x
+// (boost/simd/boolean/functions/scalar/selinc.hpp:27, seldec.hpp:27)
+NT2CUDA_BIN(selinc_, (a ? (B)(b + 1) : b))
+NT2CUDA_BIN(seldec_, (a ? (B)(b - 1) : b))
+NT2CUDA_UN(unary_minus_, (A)(-a))
+NT2CUDA_UN(sqr_, detail::mul(a, a))
+NT2CUDA_UN(sqrt_, math::sqrt_(a))
+NT2CUDA_UN(rec_, detail::dv((A)1, a))
+NT2CUDA_UN(abs_, (a < (A)0 ? (A)(-a) : a))
+NT2CUDA_UN(oneminus_, detail::sub((A)1, a))
+NT2CUDA_UN(minusone_, detail::sub(a, (A)1))
+NT2CUDA_UN(exp_, math::exp<F>(a))
+NT2CUDA_UN(log_, math::log<F>(a))
+NT2CUDA_UN(erfc_, math::erfc<F>(a))
+NT2CUDA_UN(normcdf_, math::normcdf<F>(a))
+NT2CUDA_UN(fastnormcdf_, math::fastnormcdf<F>(a))
+// if_zero_else_one(c) = c ? 0 : 1 (boost/simd/boolean/functions/scalar/if_zero_else_one.hpp:28-50);
+// the result type is the caller's element type, carried by the node.
+#undef NT2CUDA_BIN
+#undef NT2CUDA_UN
+
+template <bool F> struct fn<tag::fma_, F> {
+  template <class A, class B, class C>
+  __device__ __forceinline__ static A apply(A a, B b, C c) { return detail::madd<F>(a, (A)b, (A)c); }
+};
+template <bool F> struct fn<tag::fnms_, F> {
+  template <class A, class B, class C>
+  __device__ __forceinline__ static A apply(A a, B b, C c) { return detail::nmsub<F>(a, (A)b, (A)c); }
+};
+template <bool F> struct fn<tag::if_else_, F> {
+  template <class A, class B, class C>
+  __device__ __forceinline__ static B apply(A a, B b, C c) { return a ? b : (B)c; }
+};
+
+// ------------------------------------------------------------ value types
+template <class E> struct value_of;
+template <class T> struct value_of<term<T>> { using type = T; };
+template <class T> struct value_of<scal<T>> { using type = T; };
+template <class Tag, class... C> struct value_of<node<Tag, C...>> {
+  using type = decltype(fn<Tag, false>::apply(std::declval<typename value_of<C>::type>()...));
+};
+// if_zero_else_one carries its result type in a scal<R> second child that is never read.
+template <class A, class R> struct value_of<node<tag::if_zero_else_one_, A, scal<R>>> { using type = R; };
+
+// Smallest element size among the terminals (drives the lane count).
+template <class E> struct min_elem;
+template <class T> struct min_elem<term<T>> { static constexpr int value = (int)sizeof(T); };
+template <class T> struct min_elem<scal<T>> { static constexpr int value = 1 << 20; };
+constexpr int min_of() { return 1 << 20; }
+template <class... R> constexpr int min_of(int a, R... r) { return a < min_of(r...) ? a : min_of(r...); }
+template <class Tag, class... C> struct min_elem<node<Tag, C...>> {
+  static constexpr int value = min_of(min_elem<C>::value...);
+};
+
+// ---------------------------------------------------------- register lanes
+template <class E, int V> struct regs;
+
+template <class T, int V> struct regs<term<T>, V> {
+  T v[V];
+  template <bool Stream> __device__ __forceinline__ void load(const term<T>& t, size_t i) {
+    mem::load_vec<T, V, Stream>(t.p, i, v);
+  }
+  template <bool Stream> __device__ __forceinline__ void load_one(const term<T>& t, size_t i, int l) {
+    v[l] = t.p[i];
+  }
+  template <bool F> __device__ __forceinline__ T get(const term<T>&, int l) const { return v[l]; }
+};
+
+template <class T, int V> struct regs<scal<T>, V> {
+  template <bool Stream> __device__ __forceinline__ void load(const scal<T>&, size_t) {}
+  template <bool Stream> __device__ __forceinline__ void load_one(const scal<T>&, size_t, int) {}
+  template <bool F> __device__ __forceinline__ T get(const scal<T>& s, int) const { return s.v; }
+};
+
+template <class Tag, class A, int V> struct regs<node<Tag, A>, V> {
+  regs<A, V> ra;
+  template <bool S> __device__ __forceinline__ void load(const node<Tag, A>& n, size_t i) { ra.template load<S>(n.a, i); }
+  template <bool S> __device__ __forceinline__ void load_one(const node<Tag, A>& n, size_t i, int l) { ra.template load_one<S>(n.a, i, l); }
+  template <bool F> __device__ __forceinline__ auto get(const node<Tag, A>& n, int l) const {
+    return fn<Tag, F>::apply(ra.template get<F>(n.a, l));
+  }
+};
+
+template <class Tag, class A, class B, int V> struct regs<node<Tag, A, B>, V> {
+  regs<A, V> ra; regs<B, V> rb;
+  template <bool S> __device__ __forceinline__ void load(const node<Tag, A, B>& n, size_t i) {
+    ra.template load<S>(n.a, i); rb.template load<S>(n.b, i);
+  }
+  template <bool S> __device__ __forceinline__ void load_one(const node<Tag, A, B>& n, size_t i, int l) {
+    ra.template load_one<S>(n.a, i, l); rb.template load_one<S>(n.b, i, l);
+  }
+  template <bool F> __device__ __forceinline__ auto get(const node<Tag, A, B>& n, int l) const {
+    if constexpr (std::is_same<Tag, tag::if_zero_else_one_>::value) {
+      using R = typename value_of<node<Tag, A, B>>::type;
+      return ra.template get<F>(n.a, l) ? R(0) : R(1);
+    } else {
+      return fn<Tag, F>::apply(ra.template get<F>(n.a, l), rb.template get<F>(n.b, l));
+    }
+  }
+};
+
+template <class Tag, class A, class B, class C, int V> struct regs<node<Tag, A, B, C>, V> {
+  regs<A, V> ra; regs<B, V> rb; regs<C, V> rc;
+  template <bool S> __device__ __forceinline__ void load(const node<Tag, A, B, C>& n, size_t i) {
+    ra.template load<S>(n.a, i); rb.template load<S>(n.b, i); rc.template load<S>(n.c, i);
+  }
+  template <bool S> __device__ __forceinline__ void load_one(const node<Tag, A, B, C>& n, size_t i, int l) {
+    ra.template load_one<S>(n.a, i, l); rb.template load_one<S>(n.b, i, l); rc.template load_one<S>(n.c, i, l);
+  }
+  template <bool F> __device__ __forceinline__ auto get(const node<Tag, A, B, C>& n, int l) const {
+    return fn<Tag, F>::apply(ra.template get<F>(n.a, l), rb.template get<F>(n.b, l), rc.template get<F>(n.c, l));
+  }
+};
+
+// ------------------------------------------------------------- programs
+// prog<A0, A...>: the assigns of one statement, evaluated per index in order.
+template <class... As> struct prog;
+template <> struct prog<> {};
+template <class A0, class... As> struct prog<A0, As...> { A0 head; prog<As...> tail; };
+
+template <class... As> __host__ __device__ inline prog<As...> make_prog(As... as);
+template <> __host__ __device__ inline prog<> make_prog() { return prog<>{}; }
+template <class A0, class... As> __host__ __device__ inline prog<A0, As...> make_prog(A0 a0, As... as)
+{
+  return prog<A0, As...>{a0, make_prog(as...)};
+}
+
+// Lane count: enough lanes that the smallest element type moves 16 bytes.
+template <class P> struct prog_min_elem;
+template <> struct prog_min_elem<prog<>> { static constexpr int value = 1 << 20; };
+template <class T, class E, class... As> struct prog_min_elem<prog<assign<T, E>, As...>> {
+  static constexpr int a = min_elem<E>::value < (int)sizeof(T) ? min_elem<E>::value : (int)sizeof(T);
+  static constexpr int b = prog_min_elem<prog<As...>>::value;
+  static constexpr int value = a < b ? a : b;
+};
+template <class P> struct base_lanes {
+  static constexpr int m = prog_min_elem<P>::value;
+  static constexpr int value = m >= 16 ? 1 : 16 / m;
+};
+
+template <class P, int V> struct pregs;
+template <int V> struct pregs<prog<>, V> {
+  template <bool S> __device__ __forceinline__ void load(const prog<>&, size_t) {}
+  template <bool F> __device__ __forceinline__ void compute_store(const prog<>&, size_t) {}
+  template <bool F> __device__ __forceinline__ void ordered(const prog<>&, size_t) {}
+};
+template <class T, class E, class... As, int V> struct pregs<prog<assign<T, E>, As...>, V> {
+  using P = prog<assign<T, E>, As...>;
+  regs<E, V> r;
+  pregs<prog<As...>, V> rest;
+  template <bool S> __device__ __forceinline__ void load(const P& p, size_t i) {
+    r.template load<S>(p.head.e, i);
+    rest.template load<S>(p.tail, i);
+  }
+  template <bool F> __device__ __forceinline__ void store_head(const P& p, size_t i) {
+    T out[V];
+#pragma unroll
+    for (int l = 0; l < V; ++l) out[l] = (T)r.template get<F>(p.head.e, l);
+    mem::store_vec<T, V>(p.head.out, i, out);
+  }
+  template <bool F> __device__ __forceinline__ void compute_store(const P& p, size_t i) {
+    store_head<F>(p, i);
+    rest.template compute_store<F>(p.tail, i);
+  }
+  // Load, compute and store each assign in turn with coherent loads, so an
+  // assign reads the outputs that earlier assigns of the statement wrote.
+  template <bool F> __device__ __forceinline__ void ordered(const P& p, size_t i) {
+    r.template load<false>(p.head.e, i);
+    store_head<F>(p, i);
+    rest.template ordered<F>(p.tail, i);
+  }
+};
+
+// ---------------------------------------------------------- the kernel
+// Persistent grid-stride transform.  Each thread owns groups of V contiguous
+// elements and keeps U groups in flight per trip; the n % V tail is done one
+// element per thread by the first threads of the grid.
+template <bool F, bool Ordered, int V, int U, class P>
+__global__ void __launch_bounds__(256) k_transform(P p, size_t n)
+{
+  const size_t ngroups = n / V;
+  const size_t T = (size_t)gridDim.x * blockDim.x;
+  const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t g = tid;
+  for (; g + (size_t)(U - 1) * T < ngroups; g += (size_t)U * T) {
+    pregs<P, V> r[U];
+    if constexpr (!Ordered) {
+#pragma unroll
+      for (int u = 0; u < U; ++u) r[u].template load<true>(p, (g + (size_t)u * T) * V);
+#pragma unroll
+      for (int u = 0; u < U; ++u) r[u].template compute_store<F>(p, (g + (size_t)u * T) * V);
+    } else {
+#pragma unroll
+      for (int u = 0; u < U; ++u) r[u].template ordered<F>(p, (g + (size_t)u * T) * V);
+    }
+  }
+  for (; g < ngroups; g += T) {
+    pregs<P, V> r;
+    if constexpr (!Ordered) { r.template load<true>(p, g * V); r.template compute_store<F>(p, g * V); }
+    else r.template ordered<F>(p, g * V);
+  }
+  const size_t tail0 = ngroups * V;
+  if (tid < n - tail0) {
+    pregs<P, 1> r;
+    r.template ordered<F>(p, tail0 + tid);
+  }
+}
+
+}  // namespace nt2cuda

@@ -1,0 +1,312 @@
+// nt2cuda/math.cuh -- NT2's elementwise math functors on sm_103a.
+//
+// Each functor follows the NT2 algorithm that the SIMD transform body runs
+// (file:line cited per function, paths relative to the NT2 source tree).
+// NT2's generic fma/fnms are `a*b+c` rounded twice
+// (modules/boost/simd/base/include/boost/simd/arithmetic/functions/generic/fma.hpp:32),
+// so the default here (Fused = false) spells every multiply and add with the
+// _rn intrinsics: nvcc never contracts them, whatever flags the including
+// translation unit uses, and the results are bit-identical to NT2 evaluated
+// without contraction.  Fused = true turns each NT2 fma/fnms/horner step into
+// one hardware FMA, which is what NT2 compiled with FMA contraction computes;
+// its ULP distance to the unfused form is measured by the parity tests.
+// Division and square root are always the IEEE-rounded forms, as in NT2.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace nt2cuda {
+namespace math {
+
+// ------------------------------------------------------------ primitives
+__device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float sqrt_(float a) { return __fsqrt_rn(a); }
+__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double sqrt_(double a) { return __dsqrt_rn(a); }
+
+// NT2 fma(a,b,c) = a*b+c ; fnms(a,b,c) = c-a*b
+template <bool F> __device__ __forceinline__ float madd(float a, float b, float c)
+{ return F ? __fmaf_rn(a, b, c) : __fadd_rn(__fmul_rn(a, b), c); }
+template <bool F> __device__ __forceinline__ float nmsub(float a, float b, float c)
+{ return F ? __fmaf_rn(-a, b, c) : __fsub_rn(c, __fmul_rn(a, b)); }
+template <bool F> __device__ __forceinline__ double madd(double a, double b, double c)
+{ return F ? __fma_rn(a, b, c) : __dadd_rn(__dmul_rn(a, b), c); }
+template <bool F> __device__ __forceinline__ double nmsub(double a, double b, double c)
+{ return F ? __fma_rn(-a, b, c) : __dsub_rn(c, __dmul_rn(a, b)); }
+
+__device__ __forceinline__ float fbits(uint32_t u) { return __uint_as_float(u); }
+__device__ __forceinline__ double dbits(uint64_t u) { return __longlong_as_double((long long)u); }
+
+// Static Horner, coefficients (bit patterns) in decreasing powers:
+// modules/core/polynomials/include/nt2/polynomials/functions/scalar/impl/horner.hpp:26-45
+template <bool F, int N>
+__device__ __forceinline__ float horner(float x, const uint32_t (&c)[N])
+{
+  float acc = fbits(c[0]);
+#pragma unroll
+  for (int i = 1; i < N; ++i) acc = madd<F>(x, acc, fbits(c[i]));
+  return acc;
+}
+template <bool F, int N>
+__device__ __forceinline__ double horner(double x, const uint64_t (&c)[N])
+{
+  double acc = dbits(c[0]);
+#pragma unroll
+  for (int i = 1; i < N; ++i) acc = madd<F>(x, acc, dbits(c[i]));
+  return acc;
+}
+
+// --------------------------------------------------------------- constants
+// Bit patterns from each constant's BOOST_SIMD_CONSTANT_REGISTER line.
+struct cf {
+  static constexpr uint32_t maxlog = 0x42b0c0a5u, minlog = 0xc2b0c0a5u, invlog_2 = 0x3fb8aa3bu,
+                            log_2hi = 0x3f318000u, log_2lo = 0xb95e8083u, sqrt_2o_2 = 0x3f3504f3u,
+                            twothird = 0x3f2aaaabu, invsqrt_2pi = 0x3ecc422au,
+                            smallestposval = 0x00800000u, twotonmb = 0x4b000000u,
+                            mlogtwo2nmb = 0xc17f1402u;
+};
+struct cd {
+  static constexpr uint64_t maxlog = 0x40862e42fefa39efull, minlog = 0xc086232bdd7abcd2ull,
+                            invlog_2 = 0x3ff71547652b82feull, log_2hi = 0x3fe62e42fee00000ull,
+                            log_2lo = 0x3dea39ef35793c76ull, sqrt_2o_2 = 0x3fe6a09e667f3bcdull;
+};
+
+// ---------------------------------------------------------------- float exp
+// reduce/approx: modules/core/exponential/include/nt2/exponential/functions/scalar/impl/expo/f_expo_reduction.hpp:62-85
+// selections:    .../exponential/functions/simd/common/impl/expo/expo_base.hpp:48-62
+// scale by 2^k:  .../exponential/functions/scalar/impl/expo/expo_scale.hpp:26-35
+template <bool F = false>
+__device__ __forceinline__ float exp(float a0)
+{
+  constexpr uint32_t P[5] = {0x3ab778cfu, 0x3c098d8bu, 0x3d2aa957u, 0x3e2aa9a5u, 0x3f000000u};
+  float k = rintf(mul(fbits(cf::invlog_2), a0));
+  float x = nmsub<F>(k, fbits(cf::log_2hi), a0);
+  x = nmsub<F>(k, fbits(cf::log_2lo), x);
+  float y = horner<F>(x, P);
+  float c = add(madd<F>(y, mul(x, x), x), 1.0f);
+  unsigned ik = (unsigned)((int)k + 127);              // k in [-127,127] on the kept lanes
+  float r = mul(c, __uint_as_float(ik << 23));
+  r = (a0 <= fbits(cf::minlog)) ? 0.0f : r;
+  r = (a0 >= fbits(cf::maxlog)) ? __int_as_float(0x7f800000) : r;
+  return (a0 != a0) ? a0 : r;
+}
+
+// ---------------------------------------------------------------- float log
+// modules/core/exponential/include/nt2/exponential/functions/simd/common/impl/logs/f_log.hpp:101-124, finalize :173-186
+// kernel: .../exponential/functions/scalar/impl/logs/f_kernel.hpp:43-73
+template <bool F = false>
+__device__ __forceinline__ float log(float a0)
+{
+  constexpr uint32_t P[8] = {0xbda5dff0u, 0x3e0229f9u, 0xbe04d6b7u, 0x3e116e80u,
+                             0xbe2a6aa0u, 0x3e4cd0a3u, 0xbe800064u, 0x3eaaaaa9u};
+  float z = a0, t = 0.0f;
+  if (fabsf(z) < fbits(cf::smallestposval)) { z = mul(z, fbits(cf::twotonmb)); t = fbits(cf::mlogtwo2nmb); }
+  uint32_t u = __float_as_uint(z);
+  int e = (int)((u & 0x7f800000u) >> 23) - 126;
+  float x = __uint_as_float((u & ~0x7f800000u) | 0x3f000000u);   // fast_frexp
+  bool lt = x < fbits(cf::sqrt_2o_2);
+  float fe = lt ? add((float)e, -1.0f) : (float)e;
+  x = sub(lt ? add(x, x) : x, 1.0f);
+  float x2 = mul(x, x);
+  float y = mul(mul(horner<F>(x, P), x), x2);
+  y = madd<F>(fe, fbits(cf::log_2lo), y);
+  y = madd<F>(-0.5f, x2, y);
+  float r = madd<F>(fbits(cf::log_2hi), fe, add(add(x, y), t));
+  r = (a0 < 0.0f || a0 != a0) ? __int_as_float(0x7fffffff) : r;
+  r = (a0 == __int_as_float(0x7f800000)) ? a0 : r;
+  return (a0 == 0.0f) ? __int_as_float(0xff800000) : r;
+}
+
+// --------------------------------------------------------------- float erfc
+// modules/core/euler/include/nt2/euler/functions/simd/common/erfc.hpp:92-121
+// kernels: modules/core/euler/include/nt2/euler/functions/details/erf_kernel.hpp:48-85
+// erfc_abs(x) is the |a0| part, shared by erfc(a) and erfc(-a):
+// erfc(a) = a < 0 ? 2 - erfc_abs(|a|) : erfc_abs(|a|).
+template <bool F = false>
+__device__ __forceinline__ float erfc_abs(float x)
+{
+  constexpr uint32_t P2[11] = {0xc0283611u, 0x40d67e3bu, 0xc0cd1a85u, 0x4050b063u,
+                               0xbfaea865u, 0x3e2006f0u, 0x3e1175c7u, 0x3ec4ca6eu,
+                               0x3e243828u, 0xbf918a62u, 0x3f0a0e8bu};
+  constexpr uint32_t P3[9] = {0x41aa8e55u, 0x401b5680u, 0xc010d956u, 0x3f2cff3bu,
+                              0xc016c985u, 0xbffc9284u, 0xbfa11698u, 0xbe036d7eu, 0x3f7ffffeu};
+  float z = div(x, add(1.0f, x));
+  float r1;
+  if (x < fbits(cf::twothird)) {
+    r1 = mul(sub(1.0f, z), horner<F>(z, P3));
+  } else {
+    float zz = sub(z, 0.4f);
+    r1 = mul(exp<F>(-mul(x, x)), horner<F>(zz, P2));
+  }
+  return (x == __int_as_float(0x7f800000)) ? 0.0f : r1;
+}
+
+template <bool F = false>
+__device__ __forceinline__ float erfc(float a0)
+{
+  float r1 = erfc_abs<F>(fabsf(a0));
+  return (a0 < 0.0f) ? sub(2.0f, r1) : r1;
+}
+
+// normcdf(x) = 0.5*erfc(-sqrt(2)/2 * x):
+// modules/core/statistics/include/nt2/statistics/functions/generic/normcdf.hpp:28-34
+template <bool F = false>
+__device__ __forceinline__ float normcdf(float a0)
+{
+  return mul(0.5f, erfc<F>(mul(-fbits(cf::sqrt_2o_2), a0)));
+}
+
+// normcdf(x) and normcdf(-x) from one erfc core.  normcdf(-x) evaluates
+// erfc(+c*x) = erfc(-(-c*x)), and erfc only looks at the sign and |arg|,
+// so both results are bit-identical to two separate normcdf calls.
+template <bool F = false>
+__device__ __forceinline__ void normcdf_pair(float a0, float& pos, float& neg)
+{
+  float y = mul(-fbits(cf::sqrt_2o_2), a0);
+  float r1 = erfc_abs<F>(fabsf(y));
+  float two_m = sub(2.0f, r1);
+  pos = mul(0.5f, (y < 0.0f) ? two_m : r1);
+  neg = mul(0.5f, (-y < 0.0f) ? two_m : r1);
+}
+
+// fastnormcdf (Abramowitz-Stegun 26.2.17):
+// modules/core/statistics/include/nt2/statistics/functions/generic/fastnormcdf.hpp:33-53
+template <bool F = false>
+__device__ __forceinline__ float fastnormcdf(float a0)
+{
+  constexpr uint32_t P[5] = {0x3faa466fu, 0xbfe91eeau, 0x3fe40778u, 0xbeb68f87u, 0x3ea385fau};
+  float l = fabsf(a0);
+  float k = div(1.0f, madd<F>(0.2316419f, l, 1.0f));
+  float w = horner<F>(k, P);
+  w = mul(w, mul(mul(k, fbits(cf::invsqrt_2pi)), exp<F>(mul(-mul(l, l), 0.5f))));
+  return (a0 > 0.0f) ? sub(1.0f, w) : w;
+}
+
+// fastnormcdf(x) and fastnormcdf(-x): w depends on |x| only.
+template <bool F = false>
+__device__ __forceinline__ void fastnormcdf_pair(float a0, float& pos, float& neg)
+{
+  constexpr uint32_t P[5] = {0x3faa466fu, 0xbfe91eeau, 0x3fe40778u, 0xbeb68f87u, 0x3ea385fau};
+  float l = fabsf(a0);
+  float k = div(1.0f, madd<F>(0.2316419f, l, 1.0f));
+  float w = horner<F>(k, P);
+  w = mul(w, mul(mul(k, fbits(cf::invsqrt_2pi)), exp<F>(mul(-mul(l, l), 0.5f))));
+  float om = sub(1.0f, w);
+  pos = (a0 > 0.0f) ? om : w;
+  neg = (-a0 > 0.0f) ? om : w;
+}
+
+// --------------------------------------------------------------- double exp
+// modules/core/exponential/include/nt2/exponential/functions/scalar/impl/expo/d_expo_reduction.hpp:57-82
+// selections: .../exponential/functions/simd/common/impl/expo/expo_base.hpp:31-45
+template <bool F = false>
+__device__ __forceinline__ double exp(double a0)
+{
+  constexpr uint64_t P[5] = {0x3e66376972bea4d0ull, 0xbebbbd41c5d26bf1ull, 0x3f11566aaf25de2cull,
+                             0xbf66c16c16bebd93ull, 0x3fc555555555553eull};
+  double k = rint(mul(dbits(cd::invlog_2), a0));
+  double hi = nmsub<F>(k, dbits(cd::log_2hi), a0);
+  double lo = mul(k, dbits(cd::log_2lo));
+  double x = sub(hi, lo);
+  double t = mul(x, x);
+  double c = nmsub<F>(t, horner<F>(t, P), x);
+  c = sub(1.0, sub(sub(lo, div(mul(x, c), sub(2.0, c))), hi));
+  unsigned long long ik = (unsigned long long)((long long)k + 1023);
+  double r = mul(c, __longlong_as_double((long long)(ik << 52)));
+  r = (a0 <= dbits(cd::minlog)) ? 0.0 : r;
+  r = (a0 >= dbits(cd::maxlog)) ? __longlong_as_double(0x7ff0000000000000ll) : r;
+  return (a0 != a0) ? a0 : r;
+}
+
+// --------------------------------------------------------------- double log
+// modules/core/exponential/include/nt2/exponential/functions/simd/common/impl/logs/d_log.hpp:57-98, finalize :124-137
+template <bool F = false>
+__device__ __forceinline__ double log(double a0)
+{
+  constexpr uint64_t T1[3] = {0x3fc39a09d078c69full, 0x3fcc71c51d8e78afull, 0x3fd999999997fa04ull};
+  constexpr uint64_t T2[4] = {0x3fc2f112df3e5244ull, 0x3fc7466496cb03deull, 0x3fd2492494229359ull,
+                              0x3fe5555555555593ull};
+  unsigned long long u = (unsigned long long)__double_as_longlong(a0);
+  long long k = (long long)((u & 0x7ff0000000000000ull) >> 52) - 1022;
+  double x = __longlong_as_double((long long)((u & ~0x7ff0000000000000ull) | 0x3fe0000000000000ull));
+  bool lt = dbits(cd::sqrt_2o_2) > x;
+  k = k + (lt ? -1 : 0);
+  double f = sub(add(x, lt ? x : 0.0), 1.0);
+  double dk = (double)k;
+  double s = div(f, add(2.0, f));
+  double z = mul(s, s);
+  double w = mul(z, z);
+  double t1 = mul(w, horner<F>(w, T1));
+  double t2 = mul(z, horner<F>(w, T2));
+  double R = add(t2, t1);
+  double hfsq = mul(0.5, mul(f, f));
+  double y = sub(mul(dk, dbits(cd::log_2hi)),
+                 sub(sub(hfsq, madd<F>(s, add(hfsq, R), mul(dk, dbits(cd::log_2lo)))), f));
+  y = (a0 < 0.0 || a0 != a0) ? __longlong_as_double(0x7fffffffffffffffll) : y;
+  y = (a0 == __longlong_as_double(0x7ff0000000000000ll)) ? a0 : y;
+  return (a0 == 0.0) ? __longlong_as_double((long long)0xfff0000000000000ull) : y;
+}
+
+// -------------------------------------------------------------- double erfc
+// modules/core/euler/include/nt2/euler/functions/simd/common/erfc.hpp:46-89
+// kernels: modules/core/euler/include/nt2/euler/functions/details/erf_kernel.hpp:101-163
+template <bool F = false>
+__device__ __forceinline__ double erfc_abs(double x)
+{
+  constexpr uint64_t E1P[5] = {0x3f110512d5b20332ull, 0x3f53b7664358865aull, 0x3fa4a59a4f02579cull,
+                               0x3fc16500f106c0a5ull, 0x3ff20dd750429b61ull};
+  constexpr uint64_t E1Q[5] = {0x3f37ea4332348252ull, 0x3f8166f75999dbd1ull, 0x3fb64536ca92ea2full,
+                               0x3fdd0a84eb1ca867ull, 0x3ff0000000000000ull};
+  constexpr uint64_t E2P[7] = {0x0ull, 0x3f7cf4cfe0aacbb4ull, 0x3fb2488a6b5cb5e5ull, 0x3fd53dd7a67c7e9full,
+                               0x3fec1986509e687bull, 0x3ff54dfe9b258a60ull, 0x3feffffffbbb552bull};
+  constexpr uint64_t E2Q[7] = {0x3f89a996639b0d00ull, 0x3fc033c113a7deeeull, 0x3fe307622fcff772ull,
+                               0x3ff9e677c2777c3cull, 0x40053b1052dca8bdull, 0x4003adeae79b9708ull,
+                               0x3ff0000000000000ull};
+  constexpr uint64_t E3P[7] = {0x0ull, 0x3f971d0907ea7a92ull, 0x3fc42210f88b9d43ull, 0x3fe29be1cff90d94ull,
+                               0x3ff44744306832aeull, 0x3ff9fa202deb88e5ull, 0x3fefff5a9e697ae2ull};
+  constexpr uint64_t E3Q[7] = {0x3fa47bd61bbb3843ull, 0x3fd1d7ab774bb837ull, 0x3ff0cfd4cb6cde9full,
+                               0x400315ffdfd5ce91ull, 0x400afd487397568full, 0x400602f24bf3fdb6ull,
+                               0x3ff0000000000000ull};
+  double xx = mul(x, x);
+  double r1;
+  if (x < 0.65) {
+    r1 = sub(1.0, mul(x, div(horner<F>(xx, E1P), horner<F>(xx, E1Q))));
+  } else {
+    double ex = exp<F>(-xx);
+    if (x < 2.2) r1 = mul(ex, div(horner<F>(x, E2P), horner<F>(x, E2Q)));
+    else         r1 = mul(ex, div(horner<F>(x, E3P), horner<F>(x, E3Q)));
+  }
+  return (x == __longlong_as_double(0x7ff0000000000000ll)) ? 0.0 : r1;
+}
+
+template <bool F = false>
+__device__ __forceinline__ double erfc(double a0)
+{
+  double r1 = erfc_abs<F>(fabs(a0));
+  return (a0 < 0.0) ? sub(2.0, r1) : r1;
+}
+
+template <bool F = false>
+__device__ __forceinline__ double normcdf(double a0)
+{
+  return mul(0.5, erfc<F>(mul(-dbits(cd::sqrt_2o_2), a0)));
+}
+
+template <bool F = false>
+__device__ __forceinline__ void normcdf_pair(double a0, double& pos, double& neg)
+{
+  double y = mul(-dbits(cd::sqrt_2o_2), a0);
+  double r1 = erfc_abs<F>(fabs(y));
+  double two_m = sub(2.0, r1);
+  pos = mul(0.5, (y < 0.0) ? two_m : r1);
+  neg = mul(0.5, (-y < 0.0) ? two_m : r1);
+}
+
+}  // namespace math
+}  // namespace nt2cuda

@@ -1,0 +1,502 @@
+// server.cu -- continuous-batching request loop for Black-Scholes pricing
+// requests of mixed sizes.
+//
+// NT2 has no serving layer; every evaluation is one synchronous statement on
+// the calling thread.  This server accepts requests whose inputs are already
+// resident in HBM, keeps their outputs resident in a device arena admitted
+// against a memory budget, and coalesces whatever requests are admitted at
+// each step into one launch over a (request, tile) work-list.  Up to
+// max_inflight_batches launches are on the device at once (one stream each),
+// so requests that arrive while a batch runs are admitted and launched
+// without waiting for it.  All waiting happens on the host with bounded
+// waits; no kernel spins.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+#include "internal.cuh"
+#include "nt2cuda/blackscholes.cuh"
+#include "nt2cuda/launch.cuh"
+
+using namespace nt2cuda;
+using namespace nt2cuda::detail_capi;
+
+namespace {
+
+using clk = std::chrono::steady_clock;
+inline uint64_t now_ns()
+{
+  return (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(clk::now().time_since_epoch()).count();
+}
+
+constexpr size_t BS_TILE = 256 * 4 * 2;   // options per work-list tile (2 groups of 4 per thread)
+
+struct req_desc {
+  const float* S;
+  const float* K;
+  const float* T;
+  float* call;
+  float* put;
+  uint64_t n;
+  float r, sigma;
+  uint32_t vec_ok;
+  uint32_t pad;
+};
+
+// One launch over all requests of a batch.  Each block takes tiles from the
+// work-list; tile_start[i] is the first tile of request i.  The per-option
+// arithmetic is bs_lane, the same function the single-request kernel uses,
+// so a request's results do not depend on what it was batched with.
+template <int CDF, bool F>
+__global__ void __launch_bounds__(256) k_bs_batch(const req_desc* __restrict__ desc,
+                                                  const uint64_t* __restrict__ tile_start, int nreq)
+{
+  __shared__ int s_req;
+  const uint64_t total = tile_start[nreq];
+  for (uint64_t t = blockIdx.x; t < total; t += gridDim.x) {
+    if (threadIdx.x == 0) {
+      int lo = 0, hi = nreq - 1;
+      while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (tile_start[mid] <= t) lo = mid; else hi = mid - 1;
+      }
+      s_req = lo;
+    }
+    __syncthreads();
+    const int ri = s_req;
+    const req_desc d = desc[ri];
+    const uint64_t t0 = tile_start[ri];
+    __syncthreads();
+    const float c = math::madd<F>(math::mul(d.sigma, d.sigma), 0.5f, d.r);
+    const uint64_t base = (t - t0) * BS_TILE;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const uint64_t i = base + (uint64_t)h * 1024 + (uint64_t)threadIdx.x * 4;
+      if (i >= d.n) continue;
+      if (d.vec_ok && i + 4 <= d.n) {
+        float s[4], k[4], tt[4], oc[4], op[4];
+        mem::load_vec<float, 4, true>(d.S, i, s);
+        mem::load_vec<float, 4, true>(d.K, i, k);
+        mem::load_vec<float, 4, true>(d.T, i, tt);
+#pragma unroll
+        for (int l = 0; l < 4; ++l) bs_lane<float, CDF, F>(s[l], k[l], tt[l], d.r, d.sigma, c, oc[l], op[l]);
+        mem::store_vec<float, 4>(d.call, i, oc);
+        mem::store_vec<float, 4>(d.put, i, op);
+      } else {
+        const uint64_t e = (i + 4 < d.n) ? i + 4 : d.n;
+        for (uint64_t q = i; q < e; ++q)
+          bs_lane<float, CDF, F>(d.S[q], d.K[q], d.T[q], d.r, d.sigma, c, d.call[q], d.put[q]);
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------- device arena
+// First-fit allocator over one cudaMalloc'd region; offsets are 256-aligned.
+class arena {
+ public:
+  bool init(size_t bytes)
+  {
+    cap_ = bytes;
+    if (cudaMalloc(&base_, bytes) != cudaSuccess) { base_ = nullptr; return false; }
+    free_[0] = bytes;
+    return true;
+  }
+  ~arena() { if (base_) cudaFree(base_); }
+  bool alloc(size_t bytes, size_t* off)
+  {
+    bytes = (bytes + 255) / 256 * 256;
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second >= bytes) {
+        *off = it->first;
+        size_t rest = it->second - bytes, o = it->first + bytes;
+        free_.erase(it);
+        if (rest) free_[o] = rest;
+        return true;
+      }
+    }
+    return false;
+  }
+  void release(size_t off, size_t bytes)
+  {
+    bytes = (bytes + 255) / 256 * 256;
+    auto it = free_.emplace(off, bytes).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) { it->second += nx->second; free_.erase(nx); }
+    if (it != free_.begin()) {
+      auto pv = std::prev(it);
+      if (pv->first + pv->second == it->first) { pv->second += it->second; free_.erase(it); }
+    }
+  }
+  char* ptr(size_t off) const { return (char*)base_ + off; }
+  size_t capacity() const { return cap_; }
+
+ private:
+  void* base_ = nullptr;
+  size_t cap_ = 0;
+  std::map<size_t, size_t> free_;
+};
+
+enum req_state { WAITING = 0, ADMITTED = 1, LAUNCHED = 2, DONE = 3 };
+
+struct request {
+  uint64_t id;
+  req_desc d;
+  size_t off = 0, bytes = 0;
+  int state = WAITING;
+  uint64_t t_submit = 0, t_done = 0;
+};
+
+struct batch;
+
+struct slot {
+  cudaStream_t stream = nullptr;
+  req_desc* h_desc = nullptr;     // pinned
+  uint64_t* h_tiles = nullptr;    // pinned
+  req_desc* d_desc = nullptr;
+  uint64_t* d_tiles = nullptr;
+  bool busy = false;
+};
+
+}  // namespace
+
+struct nt2cuda_server {
+  nt2cuda_server_config cfg;
+  int device = 0;
+  arena mem;
+  std::mutex m;
+  std::condition_variable cv_work;   // worker: new admitted requests or stop
+  std::condition_variable cv_done;   // clients: completions, freed slots, freed memory
+  std::unordered_map<uint64_t, request> reqs;
+  std::deque<uint64_t> waiting;      // submitted, not yet admitted (budget)
+  std::deque<uint64_t> admitted;     // admitted, not yet launched
+  std::vector<slot> slots;
+  uint64_t next_id = 1;
+  size_t reserved = 0;
+  bool stop = false;
+  std::thread worker;
+  nt2cuda_server_stats st{};
+  nt2cuda_status worker_error = NT2CUDA_OK;
+};
+
+namespace {
+
+struct batch {
+  nt2cuda_server* srv;
+  int slot;
+  std::vector<uint64_t> ids;
+};
+
+void admit_locked(nt2cuda_server* s)
+{
+  while (!s->waiting.empty()) {
+    request& r = s->reqs[s->waiting.front()];
+    size_t off;
+    if (s->reserved + r.bytes > s->cfg.budget_bytes || !s->mem.alloc(r.bytes, &off)) break;
+    r.off = off;
+    r.d.call = (float*)s->mem.ptr(off);
+    r.d.put = (float*)s->mem.ptr(off + (r.bytes / 2));
+    r.state = ADMITTED;
+    s->reserved += r.bytes;
+    s->st.reserved_bytes = s->reserved;
+    if (s->reserved > s->st.peak_reserved_bytes) s->st.peak_reserved_bytes = s->reserved;
+    s->admitted.push_back(r.id);
+    s->waiting.pop_front();
+  }
+}
+
+void CUDART_CB on_batch_done(void* p)
+{
+  batch* b = (batch*)p;
+  nt2cuda_server* s = b->srv;
+  uint64_t t = now_ns();
+  {
+    std::lock_guard<std::mutex> g(s->m);
+    for (uint64_t id : b->ids) {
+      auto it = s->reqs.find(id);
+      if (it == s->reqs.end()) continue;
+      it->second.state = DONE;
+      it->second.t_done = t;
+      s->st.completed++;
+    }
+    s->slots[(size_t)b->slot].busy = false;
+  }
+  s->cv_done.notify_all();
+  s->cv_work.notify_all();
+  delete b;
+}
+
+template <int CDF, bool F>
+nt2cuda_status launch_batch(nt2cuda_server* s, slot& sl, int nreq)
+{
+  cudaError_t e = cudaMemcpyAsync(sl.d_desc, sl.h_desc, (size_t)nreq * sizeof(req_desc), cudaMemcpyHostToDevice,
+                                  sl.stream);
+  if (e != cudaSuccess) return from_cuda(e);
+  e = cudaMemcpyAsync(sl.d_tiles, sl.h_tiles, ((size_t)nreq + 1) * 8, cudaMemcpyHostToDevice, sl.stream);
+  if (e != cudaSuccess) return from_cuda(e);
+  uint64_t tiles = sl.h_tiles[nreq];
+  int per_sm = resident_blocks(k_bs_batch<CDF, F>, 256);
+  uint64_t grid = (uint64_t)sm_count() * (uint64_t)per_sm;
+  if (grid > tiles) grid = tiles;
+  if (grid < 1) grid = 1;
+  k_bs_batch<CDF, F><<<(unsigned)grid, 256, 0, sl.stream>>>(sl.d_desc, sl.d_tiles, nreq);
+  (void)s;
+  return launch_status(cudaSuccess);
+}
+
+nt2cuda_status launch_single(nt2cuda_server* s, slot& sl, const req_desc& d)
+{
+  int cdf = s->cfg.cdf_kind, fused = s->cfg.fused;
+  // one launch per request: the plain single-statement entry point
+  return nt2cuda_blackscholes_f32(d.S, d.K, d.T, d.r, d.sigma, d.call, d.put, (size_t)d.n, cdf, fused,
+                                  reinterpret_cast<nt2cuda_stream>(sl.stream));
+}
+
+void worker_loop(nt2cuda_server* s)
+{
+  cudaSetDevice(s->device);
+  const int maxb = s->cfg.coalesce ? std::max(1, s->cfg.max_batch_requests) : 1;
+  for (;;) {
+    std::unique_lock<std::mutex> lk(s->m);
+    int si = -1;
+    s->cv_work.wait(lk, [&] {
+      if (s->stop) return true;
+      if (s->admitted.empty()) return false;
+      for (size_t i = 0; i < s->slots.size(); ++i)
+        if (!s->slots[i].busy) { si = (int)i; return true; }
+      return false;
+    });
+    if (s->stop) return;
+    slot& sl = s->slots[(size_t)si];
+    batch* b = new batch{s, si, {}};
+    int nreq = 0;
+    uint64_t tiles = 0;
+    while (!s->admitted.empty() && nreq < maxb) {
+      request& r = s->reqs[s->admitted.front()];
+      s->admitted.pop_front();
+      r.state = LAUNCHED;
+      sl.h_desc[nreq] = r.d;
+      sl.h_tiles[nreq] = tiles;
+      tiles += (r.d.n + BS_TILE - 1) / BS_TILE;
+      b->ids.push_back(r.id);
+      ++nreq;
+    }
+    sl.h_tiles[nreq] = tiles;
+    sl.busy = true;
+    s->st.batches++;
+    lk.unlock();
+
+    nt2cuda_status rs = NT2CUDA_OK;
+    if (s->cfg.coalesce) {
+      const bool F = s->cfg.fused != 0;
+      if (s->cfg.cdf_kind == CDF_FASTNORMCDF)
+        rs = F ? launch_batch<CDF_FASTNORMCDF, true>(s, sl, nreq) : launch_batch<CDF_FASTNORMCDF, false>(s, sl, nreq);
+      else
+        rs = F ? launch_batch<CDF_NORMCDF, true>(s, sl, nreq) : launch_batch<CDF_NORMCDF, false>(s, sl, nreq);
+      lk.lock();
+      s->st.launches++;
+      lk.unlock();
+    } else {
+      for (int i = 0; i < nreq && rs == NT2CUDA_OK; ++i) rs = launch_single(s, sl, sl.h_desc[i]);
+      lk.lock();
+      s->st.launches += (uint64_t)nreq;
+      lk.unlock();
+    }
+    if (rs == NT2CUDA_OK) rs = from_cuda(cudaLaunchHostFunc(sl.stream, on_batch_done, b));
+    if (rs != NT2CUDA_OK) {
+      lk.lock();
+      s->worker_error = rs;
+      for (uint64_t id : b->ids) { request& r = s->reqs[id]; r.state = DONE; r.t_done = now_ns(); }
+      sl.busy = false;
+      lk.unlock();
+      s->cv_done.notify_all();
+      delete b;
+    }
+  }
+}
+
+nt2cuda_status wait_done_locked(nt2cuda_server* s, std::unique_lock<std::mutex>& lk, uint64_t id, int timeout_ms)
+{
+  auto it = s->reqs.find(id);
+  if (it == s->reqs.end()) return NT2CUDA_ERR_ARG;
+  if (it->second.state == DONE) return NT2CUDA_OK;
+  if (timeout_ms == 0) return NT2CUDA_ERR_NOT_READY;
+  auto pred = [&] {
+    auto j = s->reqs.find(id);
+    return j == s->reqs.end() || j->second.state == DONE;
+  };
+  if (timeout_ms < 0) timeout_ms = s->cfg.wait_timeout_ms;
+  if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred)) return NT2CUDA_ERR_TIMEOUT;
+  return s->reqs.count(id) ? NT2CUDA_OK : NT2CUDA_ERR_ARG;
+}
+
+}  // namespace
+
+extern "C" {
+
+nt2cuda_status nt2cuda_server_create(const nt2cuda_server_config* cfg, nt2cuda_server** out)
+{
+  if (!cfg || !out) return NT2CUDA_ERR_ARG;
+  *out = nullptr;
+  if (cfg->budget_bytes < 4096 || cfg->max_inflight_batches < 1 || cfg->max_inflight_batches > 16 ||
+      cfg->max_batch_requests < 1 || cfg->max_batch_requests > (1 << 20) ||
+      (cfg->cdf_kind != CDF_NORMCDF && cfg->cdf_kind != CDF_FASTNORMCDF))
+    return NT2CUDA_ERR_ARG;
+  nt2cuda_server* s = new nt2cuda_server();
+  s->cfg = *cfg;
+  if (s->cfg.wait_timeout_ms <= 0) s->cfg.wait_timeout_ms = 60000;
+  cudaGetDevice(&s->device);
+  if (!s->mem.init(cfg->budget_bytes)) { delete s; return NT2CUDA_ERR_OOM; }
+  s->slots.resize((size_t)cfg->max_inflight_batches);
+  const int maxb = cfg->coalesce ? cfg->max_batch_requests : 1;
+  for (slot& sl : s->slots) {
+    bool ok = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaMallocHost(&sl.h_desc, (size_t)maxb * sizeof(req_desc)) == cudaSuccess &&
+              cudaMallocHost(&sl.h_tiles, ((size_t)maxb + 1) * 8) == cudaSuccess &&
+              cudaMalloc(&sl.d_desc, (size_t)maxb * sizeof(req_desc)) == cudaSuccess &&
+              cudaMalloc(&sl.d_tiles, ((size_t)maxb + 1) * 8) == cudaSuccess;
+    if (!ok) { nt2cuda_server_destroy(s); return NT2CUDA_ERR_OOM; }
+  }
+  s->worker = std::thread(worker_loop, s);
+  *out = s;
+  return NT2CUDA_OK;
+}
+
+nt2cuda_status nt2cuda_server_destroy(nt2cuda_server* s)
+{
+  if (!s) return NT2CUDA_OK;
+  {
+    std::lock_guard<std::mutex> g(s->m);
+    s->stop = true;
+  }
+  s->cv_work.notify_all();
+  if (s->worker.joinable()) s->worker.join();
+  for (slot& sl : s->slots) if (sl.stream) cudaStreamSynchronize(sl.stream);
+  for (slot& sl : s->slots) {
+    if (sl.stream) cudaStreamDestroy(sl.stream);
+    if (sl.h_desc) cudaFreeHost(sl.h_desc);
+    if (sl.h_tiles) cudaFreeHost(sl.h_tiles);
+    if (sl.d_desc) cudaFree(sl.d_desc);
+    if (sl.d_tiles) cudaFree(sl.d_tiles);
+  }
+  delete s;
+  return NT2CUDA_OK;
+}
+
+nt2cuda_status nt2cuda_server_submit(nt2cuda_server* s, const float* S, const float* K, const float* T, float r,
+                                     float sigma, size_t n, uint64_t* ticket)
+{
+  if (!s || !ticket || n == 0 || !S || !K || !T) return NT2CUDA_ERR_ARG;
+  const size_t half = (n * sizeof(float) + 255) / 256 * 256;
+  const size_t bytes = 2 * half;
+  if (bytes > s->cfg.budget_bytes) return NT2CUDA_ERR_BUDGET;
+  {
+    std::lock_guard<std::mutex> g(s->m);
+    if (s->worker_error != NT2CUDA_OK) return s->worker_error;
+    request q;
+    q.id = s->next_id++;
+    q.d.S = S;
+    q.d.K = K;
+    q.d.T = T;
+    q.d.call = nullptr;
+    q.d.put = nullptr;
+    q.d.n = (uint64_t)n;
+    q.d.r = r;
+    q.d.sigma = sigma;
+    // outputs are 256-aligned arena slots; inputs decide the vector path
+    q.d.vec_ok = ((((uintptr_t)S | (uintptr_t)K | (uintptr_t)T) & 15u) == 0) ? 1u : 0u;
+    q.d.pad = 0;
+    q.bytes = bytes;
+    q.t_submit = now_ns();
+    s->reqs.emplace(q.id, q);
+    s->waiting.push_back(q.id);
+    s->st.submitted++;
+    s->st.options += (uint64_t)n;
+    size_t before = s->admitted.size();
+    admit_locked(s);
+    if (s->admitted.size() == before) s->st.admission_waits++;
+    *ticket = q.id;
+  }
+  s->cv_work.notify_one();
+  return NT2CUDA_OK;
+}
+
+nt2cuda_status nt2cuda_server_poll(nt2cuda_server* s, uint64_t ticket, float** call, float** put)
+{
+  return nt2cuda_server_wait(s, ticket, 0, call, put);
+}
+
+nt2cuda_status nt2cuda_server_wait(nt2cuda_server* s, uint64_t ticket, int timeout_ms, float** call, float** put)
+{
+  if (!s) return NT2CUDA_ERR_ARG;
+  std::unique_lock<std::mutex> lk(s->m);
+  nt2cuda_status st = wait_done_locked(s, lk, ticket, timeout_ms);
+  if (st != NT2CUDA_OK) return st;
+  const request& r = s->reqs[ticket];
+  if (call) *call = r.d.call;
+  if (put) *put = r.d.put;
+  return s->worker_error;
+}
+
+nt2cuda_status nt2cuda_server_release(nt2cuda_server* s, uint64_t ticket)
+{
+  if (!s) return NT2CUDA_ERR_ARG;
+  {
+    std::lock_guard<std::mutex> g(s->m);
+    auto it = s->reqs.find(ticket);
+    if (it == s->reqs.end()) return NT2CUDA_ERR_ARG;
+    if (it->second.state != DONE) return NT2CUDA_ERR_STATE;
+    if (it->second.d.call) {
+      s->mem.release(it->second.off, it->second.bytes);
+      s->reserved -= it->second.bytes;
+      s->st.reserved_bytes = s->reserved;
+    }
+    s->reqs.erase(it);
+    admit_locked(s);
+  }
+  s->cv_work.notify_one();
+  return NT2CUDA_OK;
+}
+
+nt2cuda_status nt2cuda_server_latency_ns(nt2cuda_server* s, uint64_t ticket, uint64_t* ns)
+{
+  if (!s || !ns) return NT2CUDA_ERR_ARG;
+  std::lock_guard<std::mutex> g(s->m);
+  auto it = s->reqs.find(ticket);
+  if (it == s->reqs.end()) return NT2CUDA_ERR_ARG;
+  if (it->second.state != DONE) return NT2CUDA_ERR_NOT_READY;
+  *ns = it->second.t_done - it->second.t_submit;
+  return NT2CUDA_OK;
+}
+
+nt2cuda_status nt2cuda_server_drain(nt2cuda_server* s, int timeout_ms)
+{
+  if (!s) return NT2CUDA_ERR_ARG;
+  std::unique_lock<std::mutex> lk(s->m);
+  if (timeout_ms < 0) timeout_ms = s->cfg.wait_timeout_ms;
+  auto pred = [&] {
+    if (!s->waiting.empty() || !s->admitted.empty()) return false;
+    for (auto& kv : s->reqs) if (kv.second.state != DONE) return false;
+    return true;
+  };
+  if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred)) return NT2CUDA_ERR_TIMEOUT;
+  return s->worker_error;
+}
+
+nt2cuda_status nt2cuda_server_get_stats(nt2cuda_server* s, nt2cuda_server_stats* out)
+{
+  if (!s || !out) return NT2CUDA_ERR_ARG;
+  std::lock_guard<std::mutex> g(s->m);
+  *out = s->st;
+  return NT2CUDA_OK;
+}
+
+}  // extern "C"

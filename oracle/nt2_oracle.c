@@ -1,0 +1,720 @@
+/*
+ * nt2_oracle.c -- CPU restatement of NT2's table-expression hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the parity checker for the CUDA
+ * evaluator in nt2_gb300/ and the timed CPU baseline of bench.py.  Only
+ * tests/, __graft_entry__.smoke() and bench.py's CPU legs load it; the
+ * product path never calls it and has no CPU fallback.
+ *
+ * What it restates (paths relative to the NT2 source tree):
+ *   - the Boost.SIMD / NT2 math functors used by the saxpy, sdot,
+ *     Black-Scholes, rgb2grey and sigmadelta expressions, in the form that
+ *     NT2's SIMD transform body evaluates (the simd/common/... files), with
+ *     the generic unfused fma/fnms (a*b+c rounded twice,
+ *     modules/boost/simd/base/include/boost/simd/arithmetic/functions/generic/fma.hpp:32,
+ *     generic/fnms.hpp:32);
+ *   - the elementwise transform loop with NT2's OpenMP chunking
+ *     (modules/arch/shared_memory/include/nt2/core/functions/shared_memory/transform.hpp:36-48,
+ *      modules/arch/openmp/include/nt2/sdk/openmp/spawner/transform.hpp:47-72);
+ *   - the inner_fold / outer_fold accumulation orders
+ *     (modules/core/reduction/include/nt2/core/functions/simd/inner_fold.hpp:49-66,
+ *      modules/core/reduction/include/nt2/core/functions/details/outer_fold_step.hpp:33-67);
+ *   - NT2's ulpdist
+ *     (modules/boost/simd/base/include/boost/simd/ieee/functions/scalar/ulpdist.hpp:64-83).
+ *
+ * Parity is pinned against NT2's own unit-test values (tests/test_oracle_golden.py).
+ * Build: cc -O2 -ffp-contract=off -fopenmp -fPIC -shared (oracle/build_oracle.py).
+ * -ffp-contract=off is required: NT2's fma/fnms/horner round twice.
+ */
+#include <float.h>
+#include <stddef.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <unistd.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define EXPORT __attribute__((visibility("default")))
+
+static inline float fb(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
+static inline uint32_t bf(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
+static inline double db(uint64_t u) { double d; memcpy(&d, &u, 8); return d; }
+static inline uint64_t bd(double d) { uint64_t u; memcpy(&u, &d, 8); return u; }
+
+/* ------------------------------------------------------------- ulpdist -- */
+/* boost/simd/ieee/functions/scalar/ulpdist.hpp:64-83: |a-b| rescaled by the
+ * larger frexp exponent, divided by Eps.  Adjacent floats are 0.5 apart.
+ * Infinities: equal infinities are 0, anything else against one is +inf. */
+EXPORT double nt2o_ulpdist_f(float a0, float a1)
+{
+  if (a0 == a1) return 0.0;
+  if (isnan(a0) && isnan(a1)) return 0.0;
+  if (isnan(a0) || isnan(a1) || isinf(a0) || isinf(a1)) return INFINITY;
+  int e1, e2;
+  float m1 = frexpf(a0, &e1), m2 = frexpf(a1, &e2);
+  int expo = -(e1 > e2 ? e1 : e2);
+  float e = (e1 == e2) ? fabsf(m1 - m2) : fabsf(ldexpf(a0, expo) - ldexpf(a1, expo));
+  return (double)(e / FLT_EPSILON);
+}
+
+EXPORT double nt2o_ulpdist_d(double a0, double a1)
+{
+  if (a0 == a1) return 0.0;
+  if (isnan(a0) && isnan(a1)) return 0.0;
+  if (isnan(a0) || isnan(a1) || isinf(a0) || isinf(a1)) return INFINITY;
+  int e1, e2;
+  double m1 = frexp(a0, &e1), m2 = frexp(a1, &e2);
+  int expo = -(e1 > e2 ? e1 : e2);
+  double e = (e1 == e2) ? fabs(m1 - m2) : fabs(ldexp(a0, expo) - ldexp(a1, expo));
+  return e / DBL_EPSILON;
+}
+
+/* Max ulpdist over two arrays, and index of the worst element. */
+EXPORT double nt2o_max_ulp_f(const float* a, const float* b, size_t n, size_t* where)
+{
+  double m = 0.0; size_t w = 0;
+  for (size_t i = 0; i < n; ++i) {
+    double d = nt2o_ulpdist_f(a[i], b[i]);
+    if (d > m) { m = d; w = i; }
+  }
+  if (where) *where = w;
+  return m;
+}
+
+EXPORT double nt2o_max_ulp_d(const double* a, const double* b, size_t n, size_t* where)
+{
+  double m = 0.0; size_t w = 0;
+  for (size_t i = 0; i < n; ++i) {
+    double d = nt2o_ulpdist_d(a[i], b[i]);
+    if (d > m) { m = d; w = i; }
+  }
+  if (where) *where = w;
+  return m;
+}
+
+/* ------------------------------------------------------------ constants -- */
+/* Float / double bit patterns of the Boost.SIMD / NT2 constants
+ * (BOOST_SIMD_CONSTANT_REGISTER lines of each constant's header). */
+#define MAXLOG_F      fb(0x42b0c0a5u)   /* exponential/constants/maxlog.hpp:29 */
+#define MINLOG_F      fb(0xc2b0c0a5u)   /* exponential/constants/minlog.hpp:29 */
+#define INVLOG_2_F    fb(0x3fb8aa3bu)   /* exponential/constants/invlog_2.hpp:29 */
+#define LOG_2HI_F     fb(0x3f318000u)   /* exponential/constants/log_2hi.hpp:29 */
+#define LOG_2LO_F     fb(0xb95e8083u)   /* exponential/constants/log_2lo.hpp:29 */
+#define SQRT_2O_2_F   fb(0x3f3504f3u)   /* boost/simd/constant/constants/sqrt_2o_2.hpp:30 */
+#define TWOTHIRD_F    fb(0x3f2aaaabu)   /* boost/simd/constant/constants/twothird.hpp:30 */
+#define INVSQRT_2PI_F fb(0x3ecc422au)   /* trigonometric/constants/invsqrt_2pi.hpp:28 */
+#define SMALLESTPOSVAL_F fb(0x00800000u)
+#define TWOTONMB_F    fb(0x4b000000u)
+#define MLOGTWO2NMB_F fb(0xc17f1402u)   /* exponential/constants/mlogtwo2nmb.hpp:29 */
+
+#define MAXLOG_D      db(0x40862e42fefa39efull)
+#define MINLOG_D      db(0xc086232bdd7abcd2ull)
+#define INVLOG_2_D    db(0x3ff71547652b82feull)
+#define LOG_2HI_D     db(0x3fe62e42fee00000ull)
+#define LOG_2LO_D     db(0x3dea39ef35793c76ull)
+#define SQRT_2O_2_D   db(0x3fe6a09e667f3bcdull)
+
+/* ------------------------------------------------------------- helpers -- */
+/* round2even: boost/simd/arithmetic/functions/scalar/round2even.hpp:29-36
+ * (the 2^nmb add/subtract trick == round-half-even in the default mode). */
+static inline float  r2e_f(float a)  { return rintf(a); }
+static inline double r2e_d(double a) { return rint(a); }
+
+/* scale(y,k) = y * 2^k through the exponent bits:
+ * exponential/functions/scalar/impl/expo/expo_scale.hpp:26-35 */
+static inline float scale_f(float y, float k)
+{
+  uint32_t ik = (uint32_t)((int32_t)k + 127);
+  return y * fb(ik << 23);
+}
+static inline double scale_d(double y, double k)
+{
+  uint64_t ik = (uint64_t)((int64_t)k + 1023);
+  return y * db(ik << 52);
+}
+
+/* fast_frexp: boost/simd/ieee/functions/scalar/fast_frexp.hpp:48-56 */
+static inline float frexp_f(float a0, int32_t* e)
+{
+  uint32_t u = bf(a0);
+  *e = (int32_t)((u & 0x7f800000u) >> 23) - 126;
+  return fb((u & ~0x7f800000u) | 0x3f000000u);
+}
+static inline double frexp_d(double a0, int64_t* e)
+{
+  uint64_t u = bd(a0);
+  *e = (int64_t)((u & 0x7ff0000000000000ull) >> 52) - 1022;
+  return db((u & ~0x7ff0000000000000ull) | 0x3fe0000000000000ull);
+}
+
+/* Static Horner, coefficients in decreasing powers, unfused fma(x,acc,c):
+ * polynomials/functions/scalar/impl/horner.hpp:26-45 */
+static inline float horner_f(float x, const uint32_t* c, int n)
+{
+  float acc = fb(c[0]);
+  for (int i = 1; i < n; ++i) acc = x * acc + fb(c[i]);
+  return acc;
+}
+static inline double horner_d(double x, const uint64_t* c, int n)
+{
+  double acc = db(c[0]);
+  for (int i = 1; i < n; ++i) acc = x * acc + db(c[i]);
+  return acc;
+}
+
+/* ------------------------------------------------------------ float exp -- */
+/* exponential/functions/scalar/impl/expo/f_expo_reduction.hpp:62-85 (approx,
+ * reduce) with the selection order of
+ * exponential/functions/simd/common/impl/expo/expo_base.hpp:48-62. */
+static const uint32_t EXP_F_P[5] = {0x3ab778cfu, 0x3c098d8bu, 0x3d2aa957u, 0x3e2aa9a5u, 0x3f000000u};
+
+EXPORT float nt2o_exp_f(float a0)
+{
+  if (isnan(a0)) return a0;
+  if (a0 >= MAXLOG_F) return INFINITY;
+  if (a0 <= MINLOG_F) return 0.0f;
+  float k = r2e_f(INVLOG_2_F * a0);
+  float x = a0 - k * LOG_2HI_F;
+  x = x - k * LOG_2LO_F;
+  float y = horner_f(x, EXP_F_P, 5);
+  float c = (y * (x * x) + x) + 1.0f;
+  return scale_f(c, k);
+}
+
+/* ------------------------------------------------------------ float log -- */
+/* exponential/functions/simd/common/impl/logs/f_log.hpp:101-124 + finalize
+ * :173-186, kernel exponential/functions/scalar/impl/logs/f_kernel.hpp:43-73 */
+static const uint32_t LOG_F_P[8] = {0xbda5dff0u, 0x3e0229f9u, 0xbe04d6b7u, 0x3e116e80u,
+                                    0xbe2a6aa0u, 0x3e4cd0a3u, 0xbe800064u, 0x3eaaaaa9u};
+
+EXPORT float nt2o_log_f(float a0)
+{
+  float z = a0, t = 0.0f;
+  if (fabsf(z) < SMALLESTPOSVAL_F) { z = z * TWOTONMB_F; t = MLOGTWO2NMB_F; }
+  int32_t e;
+  float x = frexp_f(z, &e);
+  int lt = x < SQRT_2O_2_F;
+  float fe = lt ? ((float)e + -1.0f) : (float)e;
+  x = (lt ? x + x : x) - 1.0f;
+  float x2 = x * x;
+  float y = (horner_f(x, LOG_F_P, 8) * x) * x2;
+  y = fe * LOG_2LO_F + y;
+  y = -0.5f * x2 + y;
+  float r = LOG_2HI_F * fe + ((x + y) + t);
+  if (a0 < 0.0f || isnan(a0)) r = NAN;
+  if (a0 == INFINITY) r = a0;
+  if (a0 == 0.0f) r = -INFINITY;
+  return r;
+}
+
+/* ----------------------------------------------------------- float erfc -- */
+/* euler/functions/simd/common/erfc.hpp:92-121, kernels
+ * euler/functions/details/erf_kernel.hpp:48-85 (erfc2 degree 10, erfc3 degree 8) */
+static const uint32_t ERFC2_F_P[11] = {0xc0283611u, 0x40d67e3bu, 0xc0cd1a85u, 0x4050b063u,
+                                       0xbfaea865u, 0x3e2006f0u, 0x3e1175c7u, 0x3ec4ca6eu,
+                                       0x3e243828u, 0xbf918a62u, 0x3f0a0e8bu};
+static const uint32_t ERFC3_F_P[9] = {0x41aa8e55u, 0x401b5680u, 0xc010d956u, 0x3f2cff3bu,
+                                      0xc016c985u, 0xbffc9284u, 0xbfa11698u, 0xbe036d7eu,
+                                      0x3f7ffffeu};
+
+/* erfc of |a0| only (the part shared by erfc(a) and erfc(-a)) */
+static inline float erfc_abs_f(float x)
+{
+  float z = x / (1.0f + x);
+  float r1;
+  if (x < TWOTHIRD_F) {
+    r1 = (1.0f - z) * horner_f(z, ERFC3_F_P, 9);
+  } else {
+    z = z - 0.4f;
+    r1 = nt2o_exp_f(-(x * x)) * horner_f(z, ERFC2_F_P, 11);
+  }
+  if (x == INFINITY) r1 = 0.0f;
+  return r1;
+}
+
+EXPORT float nt2o_erfc_f(float a0)
+{
+  float r1 = erfc_abs_f(fabsf(a0));
+  return (a0 < 0.0f) ? 2.0f - r1 : r1;
+}
+
+/* normcdf(x) = 0.5*erfc(-sqrt(2)/2*x): statistics/functions/generic/normcdf.hpp:28-34 */
+EXPORT float nt2o_normcdf_f(float a0)
+{
+  return 0.5f * nt2o_erfc_f((-SQRT_2O_2_F) * a0);
+}
+
+/* fastnormcdf (Abramowitz-Stegun 26.2.17): statistics/functions/generic/fastnormcdf.hpp:33-53 */
+static const uint32_t FNCDF_P[5] = {0x3faa466fu, 0xbfe91eeau, 0x3fe40778u, 0xbeb68f87u, 0x3ea385fau};
+
+EXPORT float nt2o_fastnormcdf_f(float a0)
+{
+  float l = fabsf(a0);
+  float k = 1.0f / (0.2316419f * l + 1.0f);
+  float w = horner_f(k, FNCDF_P, 5);
+  w = w * ((k * INVSQRT_2PI_F) * nt2o_exp_f((-(l * l)) * 0.5f));
+  return (a0 > 0.0f) ? 1.0f - w : w;
+}
+
+/* ----------------------------------------------------------- double exp -- */
+/* exponential/functions/scalar/impl/expo/d_expo_reduction.hpp:57-82 with the
+ * selections of exponential/functions/simd/common/impl/expo/expo_base.hpp:31-45 */
+static const uint64_t EXP_D_P[5] = {0x3e66376972bea4d0ull, 0xbebbbd41c5d26bf1ull,
+                                    0x3f11566aaf25de2cull, 0xbf66c16c16bebd93ull,
+                                    0x3fc555555555553eull};
+
+EXPORT double nt2o_exp_d(double a0)
+{
+  if (isnan(a0)) return a0;
+  if (a0 >= MAXLOG_D) return INFINITY;
+  if (a0 <= MINLOG_D) return 0.0;
+  double k = r2e_d(INVLOG_2_D * a0);
+  double hi = a0 - k * LOG_2HI_D;
+  double lo = k * LOG_2LO_D;
+  double x = hi - lo;
+  double t = x * x;
+  double c = x - t * horner_d(t, EXP_D_P, 5);
+  c = 1.0 - ((lo - (x * c) / (2.0 - c)) - hi);
+  return scale_d(c, k);
+}
+
+/* ----------------------------------------------------------- double log -- */
+/* exponential/functions/simd/common/impl/logs/d_log.hpp:57-98 + finalize :124-137 */
+static const uint64_t LOG_D_T1[3] = {0x3fc39a09d078c69full, 0x3fcc71c51d8e78afull, 0x3fd999999997fa04ull};
+static const uint64_t LOG_D_T2[4] = {0x3fc2f112df3e5244ull, 0x3fc7466496cb03deull,
+                                     0x3fd2492494229359ull, 0x3fe5555555555593ull};
+
+EXPORT double nt2o_log_d(double a0)
+{
+  int64_t k;
+  double x = frexp_d(a0, &k);
+  int lt = SQRT_2O_2_D > x;
+  k = k + (lt ? -1 : 0);
+  double f = (x + (lt ? x : 0.0)) - 1.0;
+  double dk = (double)k;
+  double s = f / (2.0 + f);
+  double z = s * s;
+  double w = z * z;
+  double t1 = w * horner_d(w, LOG_D_T1, 3);
+  double t2 = z * horner_d(w, LOG_D_T2, 4);
+  double R = t2 + t1;
+  double hfsq = 0.5 * (f * f);
+  double y = dk * LOG_2HI_D - ((hfsq - (s * (hfsq + R) + dk * LOG_2LO_D)) - f);
+  if (a0 < 0.0 || isnan(a0)) y = NAN;
+  if (a0 == INFINITY) y = a0;
+  if (a0 == 0.0) y = -INFINITY;
+  return y;
+}
+
+/* ---------------------------------------------------------- double erfc -- */
+/* euler/functions/simd/common/erfc.hpp:46-89, kernels
+ * euler/functions/details/erf_kernel.hpp:101-163 (rational 5/5, 7/7, 7/7) */
+static const uint64_t ERF1_D_P[5] = {0x3f110512d5b20332ull, 0x3f53b7664358865aull, 0x3fa4a59a4f02579cull,
+                                     0x3fc16500f106c0a5ull, 0x3ff20dd750429b61ull};
+static const uint64_t ERF1_D_Q[5] = {0x3f37ea4332348252ull, 0x3f8166f75999dbd1ull, 0x3fb64536ca92ea2full,
+                                     0x3fdd0a84eb1ca867ull, 0x3ff0000000000000ull};
+static const uint64_t ERFC2_D_P[7] = {0x0ull, 0x3f7cf4cfe0aacbb4ull, 0x3fb2488a6b5cb5e5ull, 0x3fd53dd7a67c7e9full,
+                                      0x3fec1986509e687bull, 0x3ff54dfe9b258a60ull, 0x3feffffffbbb552bull};
+static const uint64_t ERFC2_D_Q[7] = {0x3f89a996639b0d00ull, 0x3fc033c113a7deeeull, 0x3fe307622fcff772ull,
+                                      0x3ff9e677c2777c3cull, 0x40053b1052dca8bdull, 0x4003adeae79b9708ull,
+                                      0x3ff0000000000000ull};
+static const uint64_t ERFC3_D_P[7] = {0x0ull, 0x3f971d0907ea7a92ull, 0x3fc42210f88b9d43ull, 0x3fe29be1cff90d94ull,
+                                      0x3ff44744306832aeull, 0x3ff9fa202deb88e5ull, 0x3fefff5a9e697ae2ull};
+static const uint64_t ERFC3_D_Q[7] = {0x3fa47bd61bbb3843ull, 0x3fd1d7ab774bb837ull, 0x3ff0cfd4cb6cde9full,
+                                      0x400315ffdfd5ce91ull, 0x400afd487397568full, 0x400602f24bf3fdb6ull,
+                                      0x3ff0000000000000ull};
+
+static inline double erfc_abs_d(double x)
+{
+  double xx = x * x;
+  double r1;
+  if (x < 0.65) {
+    r1 = 1.0 - x * (horner_d(xx, ERF1_D_P, 5) / horner_d(xx, ERF1_D_Q, 5));
+  } else {
+    double ex = nt2o_exp_d(-xx);
+    if (x < 2.2) r1 = ex * (horner_d(x, ERFC2_D_P, 7) / horner_d(x, ERFC2_D_Q, 7));
+    else         r1 = ex * (horner_d(x, ERFC3_D_P, 7) / horner_d(x, ERFC3_D_Q, 7));
+  }
+  if (x == INFINITY) r1 = 0.0;
+  return r1;
+}
+
+EXPORT double nt2o_erfc_d(double a0)
+{
+  double r1 = erfc_abs_d(fabs(a0));
+  return (a0 < 0.0) ? 2.0 - r1 : r1;
+}
+
+EXPORT double nt2o_normcdf_d(double a0)
+{
+  return 0.5 * nt2o_erfc_d((-SQRT_2O_2_D) * a0);
+}
+
+/* ------------------------------------------------- scalar-tail variants -- */
+/* NT2's transform runs the SIMD body on N-lane packs and the scalar functor
+ * on the n%N tail (core/functions/simd/transform.hpp:46-56).  The scalar
+ * erfc forms differ from the SIMD ones; they are restated here so tests can
+ * show where the two agree.  euler/functions/scalar/erfc.hpp:38-96. */
+EXPORT float nt2o_erfc_f_scalar(float a0)
+{
+  float x = fabsf(a0);
+  float r1 = 0.0f;
+  float z = x / (1.0f + x);
+  if (x < TWOTHIRD_F) r1 = (1.0f - z) * horner_f(z, ERFC3_F_P, 9);
+  else if (x == INFINITY) r1 = 0.0f;
+  else { z -= 0.4f; r1 = nt2o_exp_f(-(x * x)) * horner_f(z, ERFC2_F_P, 11); }
+  return (a0 < 0.0f) ? 2.0f - r1 : r1;
+}
+
+EXPORT double nt2o_erfc_d_scalar(double a0)
+{
+  if (isnan(a0)) return a0;
+  double x = fabs(a0), xx = x * x, z = 0.0;
+  if (x <= 0.0000000001) z = 1.0 - x * 2.0 / sqrt(3.14159265358979323846);
+  else if (x < 0.65) z = 1.0 - x * (horner_d(xx, ERF1_D_P, 5) / horner_d(xx, ERF1_D_Q, 5));
+  else if (x < 2.2) z = nt2o_exp_d(-xx) * (horner_d(x, ERFC2_D_P, 7) / horner_d(x, ERFC2_D_Q, 7));
+  else if (x < 6.0) z = nt2o_exp_d(-xx) * (horner_d(x, ERFC3_D_P, 7) / horner_d(x, ERFC3_D_Q, 7));
+  return (a0 < 0.0) ? 2.0 - z : z;
+}
+
+/* ------------------------------------------------------------- maps ------ */
+enum { OP_EXP = 0, OP_LOG = 1, OP_ERFC = 2, OP_NORMCDF = 3, OP_FASTNORMCDF = 4, OP_SQRT = 5,
+       OP_ERFC_SCALAR = 6 };
+
+EXPORT int nt2o_map_f(int op, const float* x, float* y, size_t n)
+{
+  for (size_t i = 0; i < n; ++i) {
+    float a = x[i];
+    switch (op) {
+      case OP_EXP: y[i] = nt2o_exp_f(a); break;
+      case OP_LOG: y[i] = nt2o_log_f(a); break;
+      case OP_ERFC: y[i] = nt2o_erfc_f(a); break;
+      case OP_NORMCDF: y[i] = nt2o_normcdf_f(a); break;
+      case OP_FASTNORMCDF: y[i] = nt2o_fastnormcdf_f(a); break;
+      case OP_SQRT: y[i] = sqrtf(a); break;
+      case OP_ERFC_SCALAR: y[i] = nt2o_erfc_f_scalar(a); break;
+      default: return 1;
+    }
+  }
+  return 0;
+}
+
+EXPORT int nt2o_map_d(int op, const double* x, double* y, size_t n)
+{
+  for (size_t i = 0; i < n; ++i) {
+    double a = x[i];
+    switch (op) {
+      case OP_EXP: y[i] = nt2o_exp_d(a); break;
+      case OP_LOG: y[i] = nt2o_log_d(a); break;
+      case OP_ERFC: y[i] = nt2o_erfc_d(a); break;
+      case OP_NORMCDF: y[i] = nt2o_normcdf_d(a); break;
+      case OP_SQRT: y[i] = sqrt(a); break;
+      case OP_ERFC_SCALAR: y[i] = nt2o_erfc_d_scalar(a); break;
+      default: return 1;
+    }
+  }
+  return 0;
+}
+
+/* --------------------------------------------- OpenMP chunking (NT2) ----- */
+/* Transform grain = L2 bytes / sizeof(T); the spawner runs only when
+ * sz > 8*grain (shared_memory/transform.hpp:38-48); static schedule over
+ * chunks of `grain`, the last chunk taking the leftover
+ * (openmp/spawner/transform.hpp:47-58).  `threads` <= 0 keeps OpenMP's default. */
+static size_t l2_bytes(void)
+{
+  long v = -1;
+#ifdef _SC_LEVEL2_CACHE_SIZE
+  v = sysconf(_SC_LEVEL2_CACHE_SIZE);
+#endif
+  return v > 0 ? (size_t)v : (size_t)1 << 20;
+}
+
+EXPORT size_t nt2o_l2_bytes(void) { return l2_bytes(); }
+
+EXPORT int nt2o_max_threads(void)
+{
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+#ifdef _OPENMP
+#define NT2_SPAWN(n, elem_size, threads, ...)                                    \
+  do {                                                                           \
+    size_t grain_ = l2_bytes() / (elem_size);                                    \
+    if (!grain_) grain_ = 1;                                                     \
+    if ((n) > 8 * grain_) {                                                      \
+      ptrdiff_t nb_ = (ptrdiff_t)((n) / grain_);                                 \
+      size_t left_ = (n) % grain_;                                               \
+      int th_ = (threads) > 0 ? (threads) : omp_get_max_threads();              \
+      _Pragma("omp parallel for schedule(static) num_threads(th_)")              \
+      for (ptrdiff_t c_ = 0; c_ < nb_; ++c_) {                                   \
+        size_t lo_ = (size_t)c_ * grain_;                                        \
+        size_t hi_ = lo_ + ((c_ < nb_ - 1) ? grain_ : grain_ + left_);           \
+        for (size_t i = lo_; i < hi_; ++i) { __VA_ARGS__; }                             \
+      }                                                                          \
+    } else {                                                                     \
+      for (size_t i = 0; i < (n); ++i) { __VA_ARGS__; }                                 \
+    }                                                                            \
+  } while (0)
+#else
+#define NT2_SPAWN(n, elem_size, threads, ...) \
+  do { for (size_t i = 0; i < (n); ++i) { __VA_ARGS__; } } while (0)
+#endif
+
+/* ------------------------------------------------------------ configs ---- */
+/* saxpy: Y = alpha*X + Y (demo/saxpy/nt2/saxpy_nt2.cpp:39-42).  The proto
+ * optimizer rewrites a*b+c to fma (boost/simd/operator/functions/optimize/plus.hpp),
+ * which the generic fma evaluates unfused. */
+EXPORT void nt2o_saxpy_f(float a, const float* x, float* y, size_t n, int threads)
+{
+  NT2_SPAWN(n, sizeof(float), threads, y[i] = a * x[i] + y[i]);
+}
+
+EXPORT void nt2o_saxpy_d(double a, const double* x, double* y, size_t n, int threads)
+{
+  NT2_SPAWN(n, sizeof(double), threads, y[i] = a * x[i] + y[i]);
+}
+
+/* rgb2grey: gr = 0.3*r + 0.59*g + 0.11*b (demo/rgb2grey/nt2/rgb2grey_nt2.cpp:42-45) */
+EXPORT void nt2o_rgb2grey_f(const float* r, const float* g, const float* b, float* gr,
+                            size_t n, int threads)
+{
+  NT2_SPAWN(n, sizeof(float), threads,
+            gr[i] = (0.3f * r[i] + 0.59f * g[i]) + 0.11f * b[i]);
+}
+
+/* Black-Scholes call and put, written as the NT2 table expression
+ *   da = sqrt(T); vda = v*da;
+ *   d1 = (log(S/K) + fma(sqr(v),0.5,r)*T) / vda;   d2 = d1 - vda;
+ *   e  = K*exp(-r*T);
+ *   tie(call,put) = tie(fnms(e,cdf(d2),S*cdf(d1)), fnms(S,cdf(-d1),e*cdf(-d2)));
+ * cdf = normcdf (cdf_kind 0) or fastnormcdf (cdf_kind 1, float only). */
+static inline void bs_one_f(float S, float K, float T, float r, float v, int cdf,
+                            float* call, float* put)
+{
+  float da = sqrtf(T);
+  float vda = v * da;
+  float d1 = (nt2o_log_f(S / K) + ((v * v) * 0.5f + r) * T) / vda;
+  float d2 = d1 - vda;
+  float e = K * nt2o_exp_f((-r) * T);
+  float n1, n2, m1, m2;
+  if (cdf == 0) {
+    n1 = nt2o_normcdf_f(d1); n2 = nt2o_normcdf_f(d2);
+    m1 = nt2o_normcdf_f(-d1); m2 = nt2o_normcdf_f(-d2);
+  } else {
+    n1 = nt2o_fastnormcdf_f(d1); n2 = nt2o_fastnormcdf_f(d2);
+    m1 = nt2o_fastnormcdf_f(-d1); m2 = nt2o_fastnormcdf_f(-d2);
+  }
+  *call = S * n1 - e * n2;
+  *put = e * m2 - S * m1;
+}
+
+EXPORT void nt2o_bs_f(const float* S, const float* K, const float* T, float r, float v,
+                      float* call, float* put, size_t n, int cdf, int threads)
+{
+  NT2_SPAWN(n, sizeof(float), threads, bs_one_f(S[i], K[i], T[i], r, v, cdf, &call[i], &put[i]));
+}
+
+static inline void bs_one_d(double S, double K, double T, double r, double v,
+                            double* call, double* put)
+{
+  double da = sqrt(T);
+  double vda = v * da;
+  double d1 = (nt2o_log_d(S / K) + ((v * v) * 0.5 + r) * T) / vda;
+  double d2 = d1 - vda;
+  double e = K * nt2o_exp_d((-r) * T);
+  *call = S * nt2o_normcdf_d(d1) - e * nt2o_normcdf_d(d2);
+  *put = e * nt2o_normcdf_d(-d2) - S * nt2o_normcdf_d(-d1);
+}
+
+EXPORT void nt2o_bs_d(const double* S, const double* K, const double* T, double r, double v,
+                      double* call, double* put, size_t n, int threads)
+{
+  NT2_SPAWN(n, sizeof(double), threads, bs_one_d(S[i], K[i], T[i], r, v, &call[i], &put[i]));
+}
+
+/* Demo form, verbatim (demo/blackscholes/nt2/blackandscholes_nt2.cpp:55-59):
+ *   da = sqrt(Ta); d1 = log(Sa/Xa) + (fma(sqr(va),0.5,ra)*Ta)/(va*da);
+ *   d2 = fnms(va,da,d1); R = fnms(Xa*exp(-ra*Ta), fastnormcdf(d2), Sa*fastnormcdf(d1)); */
+EXPORT void nt2o_bs_demo_f(const float* S, const float* X, const float* T, const float* r,
+                           const float* v, float* R, size_t n, int threads)
+{
+  NT2_SPAWN(n, sizeof(float), threads, {
+    float da = sqrtf(T[i]);
+    float d1 = nt2o_log_f(S[i] / X[i]) + (((v[i] * v[i]) * 0.5f + r[i]) * T[i]) / (v[i] * da);
+    float d2 = d1 - v[i] * da;
+    R[i] = S[i] * nt2o_fastnormcdf_f(d1) - (X[i] * nt2o_exp_f((-r[i]) * T[i])) * nt2o_fastnormcdf_f(d2);
+  });
+}
+
+/* sigmadelta, NT2 form (demo/sigmadelta/nt2/sigmadelta_nt2.cpp:37-58) with
+ * saturating adds on uint8.  For each pixel of each of `nframes` frames
+ * starting at frame `first`: update bkg and var in place, write the label. */
+static inline void sd_pixel(uint8_t* bkg, uint8_t fr, uint8_t* var, uint8_t* out)
+{
+  uint8_t b = *bkg, v = *var;
+  b = (b < fr) ? (uint8_t)(b + 1) : ((b > fr) ? (uint8_t)(b - 1) : b);
+  uint8_t d = (uint8_t)((b > fr ? b : fr) - (b < fr ? b : fr));
+  unsigned s2 = (unsigned)d + d; if (s2 > 255) s2 = 255;
+  unsigned s3 = s2 + d; if (s3 > 255) s3 = 255;
+  uint8_t m = (uint8_t)s3;
+  if (d != 0) v = (v < m) ? (uint8_t)(v + 1) : ((v > m) ? (uint8_t)(v - 1) : v);
+  *out = (d < v) ? 0 : 1;
+  *bkg = b; *var = v;
+}
+
+/* frames: nframes planes of npix bytes, `frame_stride` bytes apart.
+ * If init != 0: bkg = frame 0, var = 1, then frames 1..nframes-1 are processed
+ * (the demo's setup and loop, sigmadelta_nt2.cpp:85-106); labels gets
+ * nframes-1 planes.  Else all nframes frames are processed from the given
+ * bkg/var and labels gets nframes planes.  Labels planes are npix apart. */
+EXPORT void nt2o_sigmadelta_u8(const uint8_t* frames, size_t frame_stride, size_t npix, int nframes,
+                               uint8_t* bkg, uint8_t* var, uint8_t* labels, int init, int threads)
+{
+  int first = init ? 1 : 0;
+  NT2_SPAWN(npix, 1, threads, {
+    uint8_t b, v;
+    if (init) { b = frames[i]; v = 1; } else { b = bkg[i]; v = var[i]; }
+    for (int k = first; k < nframes; ++k)
+      sd_pixel(&b, frames[(size_t)k * frame_stride + i], &v, &labels[(size_t)(k - first) * npix + i]);
+    bkg[i] = b; var[i] = v;
+  });
+}
+
+/* -------------------------------------------------------------- folds ---- */
+/* Neumaier-compensated double sum of float terms; the FP64 oracle for the
+ * FP32 folds. */
+typedef struct { double s, c; } nsum_t;
+static inline void nadd(nsum_t* a, double x)
+{
+  double t = a->s + x;
+  if (fabs(a->s) >= fabs(x)) a->c += (a->s - t) + x; else a->c += (x - t) + a->s;
+  a->s = t;
+}
+
+EXPORT double nt2o_sum_fp64_f(const float* x, size_t n, double* abs_sum)
+{
+  nsum_t a = {0, 0}, b = {0, 0};
+  for (size_t i = 0; i < n; ++i) { nadd(&a, (double)x[i]); nadd(&b, fabs((double)x[i])); }
+  if (abs_sum) *abs_sum = b.s + b.c;
+  return a.s + a.c;
+}
+
+/* sum over i of x[i]*y[i], products exact in double */
+EXPORT double nt2o_dot_fp64_f(const float* x, const float* y, size_t n, double* abs_sum)
+{
+  nsum_t a = {0, 0}, b = {0, 0};
+  for (size_t i = 0; i < n; ++i) {
+    double p = (double)x[i] * (double)y[i];
+    nadd(&a, p); nadd(&b, fabs(p));
+  }
+  if (abs_sum) *abs_sum = b.s + b.c;
+  return a.s + a.c;
+}
+
+EXPORT double nt2o_sum_fp64_d(const double* x, size_t n, double* abs_sum)
+{
+  nsum_t a = {0, 0}, b = {0, 0};
+  for (size_t i = 0; i < n; ++i) { nadd(&a, x[i]); nadd(&b, fabs(x[i])); }
+  if (abs_sum) *abs_sum = b.s + b.c;
+  return a.s + a.c;
+}
+
+/* NT2's single-thread FP32 inner fold of one contiguous column: N-lane
+ * accumulators over the nb_vec*N body, horizontal sum of the lanes in lane
+ * order, then the scalar tail (core/functions/simd/inner_fold.hpp:49-63).
+ * `prod` = y != NULL folds x[i]*y[i] (globalsum(X*Y), demo/sdot/nt2/sdot_nt2.cpp:35-38). */
+static float fold_nt2_f(const float* x, const float* y, size_t n, int lanes)
+{
+  float acc[64];
+  if (lanes < 1) lanes = 1;
+  if (lanes > 64) lanes = 64;
+  for (int l = 0; l < lanes; ++l) acc[l] = 0.0f;
+  size_t nb = n / (size_t)lanes, body = nb * (size_t)lanes;
+  for (size_t v = 0; v < nb; ++v)
+    for (int l = 0; l < lanes; ++l) {
+      size_t i = v * (size_t)lanes + (size_t)l;
+      acc[l] = acc[l] + (y ? x[i] * y[i] : x[i]);
+    }
+  float s = acc[0];
+  for (int l = 1; l < lanes; ++l) s = s + acc[l];
+  for (size_t i = body; i < n; ++i) s = s + (y ? x[i] * y[i] : x[i]);
+  return s;
+}
+
+EXPORT float nt2o_globalsum_nt2_f(const float* x, size_t n, int lanes) { return fold_nt2_f(x, NULL, n, lanes); }
+EXPORT float nt2o_dot_nt2_f(const float* x, const float* y, size_t n, int lanes) { return fold_nt2_f(x, y, n, lanes); }
+
+/* Column sums of a column-major rows x cols table (sum(A,1), inner_fold).
+ * out32 gets NT2's FP32 lane order, out64 the compensated FP64 sums and
+ * abs64 the sums of |a| (for error bounds); any may be NULL. */
+EXPORT void nt2o_inner_fold_f(const float* A, size_t rows, size_t cols, int lanes,
+                              float* out32, double* out64, double* abs64, int threads)
+{
+  (void)threads;
+#ifdef _OPENMP
+  int th = threads > 0 ? threads : omp_get_max_threads();
+  #pragma omp parallel for schedule(static) num_threads(th)
+#endif
+  for (ptrdiff_t j = 0; j < (ptrdiff_t)cols; ++j) {
+    const float* c = A + (size_t)j * rows;
+    if (out32) out32[j] = fold_nt2_f(c, NULL, rows, lanes);
+    if (out64 || abs64) {
+      double ab;
+      double s = nt2o_sum_fp64_f(c, rows, &ab);
+      if (out64) out64[j] = s;
+      if (abs64) abs64[j] = ab;
+    }
+  }
+}
+
+/* Row sums of a column-major rows x cols table (sum(A,2), outer_fold): NT2
+ * walks the columns in order and accumulates each row
+ * (core/functions/details/outer_fold_step.hpp:49-66), so its FP32 result is
+ * the plain sequential sum per row. */
+EXPORT void nt2o_outer_fold_f(const float* A, size_t rows, size_t cols,
+                              float* out32, double* out64, double* abs64, int threads)
+{
+  (void)threads;
+#ifdef _OPENMP
+  int th = threads > 0 ? threads : omp_get_max_threads();
+  #pragma omp parallel for schedule(static) num_threads(th)
+#endif
+  for (ptrdiff_t i = 0; i < (ptrdiff_t)rows; ++i) {
+    float s = 0.0f;
+    nsum_t a = {0, 0}, b = {0, 0};
+    for (size_t m = 0; m < cols; ++m) {
+      float x = A[m * rows + (size_t)i];
+      s = s + x;
+      nadd(&a, x); nadd(&b, fabs((double)x));
+    }
+    if (out32) out32[i] = s;
+    if (out64) out64[i] = a.s + a.c;
+    if (abs64) abs64[i] = b.s + b.c;
+  }
+}
+
+/* Timed CPU baseline for the folds: NT2's OpenMP fold spawner splits the
+ * vectorised part into blocks of one L2 cache line's worth of elements
+ * (shared_memory/worker/inner_fold.hpp:53-56, openmp/spawner/fold.hpp:49-66)
+ * and combines the per-block partials in arrival order.  Arrival order is
+ * what makes NT2's FP32 sums vary run to run; here the combine is an OpenMP
+ * reduction, the same class of order. */
+EXPORT float nt2o_dot_omp_f(const float* x, const float* y, size_t n, int lanes, int threads)
+{
+  (void)lanes;
+  float s = 0.0f;
+#ifdef _OPENMP
+  int th = threads > 0 ? threads : omp_get_max_threads();
+  #pragma omp parallel for schedule(static) reduction(+ : s) num_threads(th)
+#endif
+  for (ptrdiff_t i = 0; i < (ptrdiff_t)n; ++i) s = s + (y ? x[i] * y[i] : x[i]);
+  return s;
+}

@@ -1,0 +1,151 @@
+"""ctypes binding of the CPU oracle (oracle/nt2_oracle.c) for the tests.
+
+The oracle is the checker: tests compare the CUDA path against it.  It is
+built on first use by oracle/build_oracle.py.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import build_oracle  # noqa: E402
+
+_libs = {}
+
+f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+sz = C.c_size_t
+
+SIGS = {
+    "nt2o_ulpdist_f": (C.c_double, [C.c_float, C.c_float]),
+    "nt2o_ulpdist_d": (C.c_double, [C.c_double, C.c_double]),
+    "nt2o_max_ulp_f": (C.c_double, [f32p, f32p, sz, C.POINTER(sz)]),
+    "nt2o_max_ulp_d": (C.c_double, [f64p, f64p, sz, C.POINTER(sz)]),
+    "nt2o_exp_f": (C.c_float, [C.c_float]),
+    "nt2o_log_f": (C.c_float, [C.c_float]),
+    "nt2o_erfc_f": (C.c_float, [C.c_float]),
+    "nt2o_erfc_f_scalar": (C.c_float, [C.c_float]),
+    "nt2o_normcdf_f": (C.c_float, [C.c_float]),
+    "nt2o_fastnormcdf_f": (C.c_float, [C.c_float]),
+    "nt2o_exp_d": (C.c_double, [C.c_double]),
+    "nt2o_log_d": (C.c_double, [C.c_double]),
+    "nt2o_erfc_d": (C.c_double, [C.c_double]),
+    "nt2o_erfc_d_scalar": (C.c_double, [C.c_double]),
+    "nt2o_normcdf_d": (C.c_double, [C.c_double]),
+    "nt2o_map_f": (C.c_int, [C.c_int, f32p, f32p, sz]),
+    "nt2o_map_d": (C.c_int, [C.c_int, f64p, f64p, sz]),
+    "nt2o_saxpy_f": (None, [C.c_float, f32p, f32p, sz, C.c_int]),
+    "nt2o_saxpy_d": (None, [C.c_double, f64p, f64p, sz, C.c_int]),
+    "nt2o_rgb2grey_f": (None, [f32p, f32p, f32p, f32p, sz, C.c_int]),
+    "nt2o_bs_f": (None, [f32p, f32p, f32p, C.c_float, C.c_float, f32p, f32p, sz, C.c_int, C.c_int]),
+    "nt2o_bs_d": (None, [f64p, f64p, f64p, C.c_double, C.c_double, f64p, f64p, sz, C.c_int]),
+    "nt2o_bs_demo_f": (None, [f32p, f32p, f32p, f32p, f32p, f32p, sz, C.c_int]),
+    "nt2o_sigmadelta_u8": (None, [u8p, sz, sz, C.c_int, u8p, u8p, u8p, C.c_int, C.c_int]),
+    "nt2o_sum_fp64_f": (C.c_double, [f32p, sz, C.POINTER(C.c_double)]),
+    "nt2o_dot_fp64_f": (C.c_double, [f32p, f32p, sz, C.POINTER(C.c_double)]),
+    "nt2o_sum_fp64_d": (C.c_double, [f64p, sz, C.POINTER(C.c_double)]),
+    "nt2o_globalsum_nt2_f": (C.c_float, [f32p, sz, C.c_int]),
+    "nt2o_dot_nt2_f": (C.c_float, [f32p, f32p, sz, C.c_int]),
+    "nt2o_inner_fold_f": (None, [f32p, sz, sz, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "nt2o_outer_fold_f": (None, [f32p, sz, sz, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "nt2o_dot_omp_f": (C.c_float, [f32p, C.c_void_p, sz, C.c_int, C.c_int]),
+    "nt2o_l2_bytes": (sz, []),
+    "nt2o_max_threads": (C.c_int, []),
+}
+
+OP = {"exp": 0, "log": 1, "erfc": 2, "normcdf": 3, "fastnormcdf": 4, "sqrt": 5, "erfc_scalar": 6}
+
+
+def load(variant: str = "libnt2oracle.so"):
+    if variant in _libs:
+        return _libs[variant]
+    paths = build_oracle.build()
+    L = C.CDLL(paths[variant])
+    for name, (res, args) in SIGS.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _libs[variant] = L
+    return L
+
+
+def max_ulp(a: np.ndarray, b: np.ndarray):
+    L = load()
+    w = sz()
+    if a.dtype == np.float32:
+        m = L.nt2o_max_ulp_f(np.ascontiguousarray(a), np.ascontiguousarray(b), a.size, C.byref(w))
+    else:
+        m = L.nt2o_max_ulp_d(np.ascontiguousarray(a), np.ascontiguousarray(b), a.size, C.byref(w))
+    return m, w.value
+
+
+def map_(op: str, x: np.ndarray) -> np.ndarray:
+    L = load()
+    y = np.empty_like(x)
+    fn = L.nt2o_map_f if x.dtype == np.float32 else L.nt2o_map_d
+    assert fn(OP[op], x, y, x.size) == 0
+    return y
+
+
+def bs(S, K, T, r, v, cdf: int = 0, threads: int = 0):
+    L = load()
+    call = np.empty_like(S)
+    put = np.empty_like(S)
+    if S.dtype == np.float32:
+        L.nt2o_bs_f(S, K, T, r, v, call, put, S.size, cdf, threads)
+    else:
+        L.nt2o_bs_d(S, K, T, r, v, call, put, S.size, threads)
+    return call, put
+
+
+def bs_demo(S, X, T, r, v, threads: int = 0):
+    R = np.empty_like(S)
+    load().nt2o_bs_demo_f(S, X, T, r, v, R, S.size, threads)
+    return R
+
+
+def sigmadelta(frames: np.ndarray, frame_stride: int, npix: int, nframes: int, bkg=None, var=None,
+               init: bool = True, threads: int = 0):
+    bkg = np.zeros(npix, np.uint8) if bkg is None else bkg.copy()
+    var = np.zeros(npix, np.uint8) if var is None else var.copy()
+    nl = nframes - 1 if init else nframes
+    labels = np.zeros(max(nl, 1) * npix, np.uint8)
+    load().nt2o_sigmadelta_u8(frames, frame_stride, npix, nframes, bkg, var, labels, int(init), threads)
+    return bkg, var, labels[: nl * npix]
+
+
+def inner_fold(A, rows, cols, lanes=8):
+    out32 = np.empty(cols, np.float32)
+    out64 = np.empty(cols, np.float64)
+    abs64 = np.empty(cols, np.float64)
+    load().nt2o_inner_fold_f(A, rows, cols, lanes, out32.ctypes.data, out64.ctypes.data, abs64.ctypes.data, 0)
+    return out32, out64, abs64
+
+
+def outer_fold(A, rows, cols):
+    out32 = np.empty(rows, np.float32)
+    out64 = np.empty(rows, np.float64)
+    abs64 = np.empty(rows, np.float64)
+    load().nt2o_outer_fold_f(A, rows, cols, out32.ctypes.data, out64.ctypes.data, abs64.ctypes.data, 0)
+    return out32, out64, abs64
+
+
+def sum_fp64(x):
+    a = C.c_double()
+    if x.dtype == np.float32:
+        s = load().nt2o_sum_fp64_f(x, x.size, C.byref(a))
+    else:
+        s = load().nt2o_sum_fp64_d(x, x.size, C.byref(a))
+    return s, a.value
+
+
+def dot_fp64(x, y):
+    a = C.c_double()
+    s = load().nt2o_dot_fp64_f(x, y, x.size, C.byref(a))
+    return s, a.value

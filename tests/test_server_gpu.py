@@ -1,0 +1,128 @@
+"""The continuous-batching request server: each result is the same alone and in
+the mix (bit-identical to the single-statement entry point and the oracle),
+admission respects the device-memory budget, and waits are bounded."""
+import threading
+import time
+
+import numpy as np
+import pytest
+import torch
+
+from nt2_gb300.server import Server, copy_out
+
+pytestmark = pytest.mark.gpu
+
+
+def pool(n, seed=0):
+    S = torch.empty(n, dtype=torch.float32, device="cuda")
+    K = torch.empty(n, dtype=torch.float32, device="cuda")
+    T = torch.empty(n, dtype=torch.float32, device="cuda")
+    import nt2_gb300.api as api
+    api.fill_uniform(S, 5, 30, seed + 1)
+    api.fill_uniform(K, 1, 100, seed + 2)
+    api.fill_uniform(T, 0.25, 10, seed + 3)
+    torch.cuda.synchronize()
+    return S, K, T
+
+
+def requests(total, sizes_seed, lo=256, hi=1 << 16, count=200):
+    rng = np.random.default_rng(sizes_seed)
+    sizes = np.exp(rng.uniform(np.log(lo), np.log(hi), count)).astype(int)
+    offs = rng.integers(0, total - hi, count)
+    return list(zip(offs.tolist(), sizes.tolist()))
+
+
+@pytest.mark.parametrize("coalesce", [True, False])
+def test_mix_equals_alone(gpu, oracle, coalesce):
+    S, K, T = pool(1 << 20)
+    reqs = requests(1 << 20, 1)
+    with Server(budget_bytes=256 << 20, max_batch_requests=64, max_inflight_batches=3, coalesce=coalesce) as srv:
+        tickets = [srv.submit_ptr(S.data_ptr() + 4 * o, K.data_ptr() + 4 * o, T.data_ptr() + 4 * o, 0.02, 0.30, n)
+                   for o, n in reqs]
+        outs = []
+        for t, (o, n) in zip(tickets, reqs):
+            c, p = srv.wait(t, 30000)
+            outs.append((copy_out(c, n), copy_out(p, n)))
+            assert srv.latency_ns(t) > 0
+            srv.release(t)
+        st = srv.stats()
+    assert st["completed"] == len(reqs)
+    if coalesce:
+        assert st["launches"] < len(reqs)
+    else:
+        assert st["launches"] == len(reqs)
+    Sn, Kn, Tn = (a.cpu().numpy() for a in (S, K, T))
+    for (o, n), (c, p) in zip(reqs, outs):
+        # alone: the plain entry point on the same sub-range
+        ca, pa = gpu.blackscholes(S[o:o + n], K[o:o + n], T[o:o + n], 0.02, 0.30)
+        assert torch.equal(c, ca) and torch.equal(p, pa)
+        rc, rp = oracle.bs(Sn[o:o + n].copy(), Kn[o:o + n].copy(), Tn[o:o + n].copy(), 0.02, 0.30)
+        assert oracle.max_ulp(c.cpu().numpy(), rc)[0] == 0.0
+        assert oracle.max_ulp(p.cpu().numpy(), rp)[0] == 0.0
+
+
+def test_budget_admission_and_release(gpu):
+    S, K, T = pool(1 << 20, seed=5)
+    n = 1 << 16                                          # 512 KiB of outputs per request
+    with Server(budget_bytes=2 << 20, max_batch_requests=16, max_inflight_batches=2) as srv:
+        ts = [srv.submit(S[:n], K[:n], T[:n], 0.02, 0.30) for _ in range(12)]
+        done = 0
+        for t in ts:
+            srv.wait(t, 30000)
+            st = srv.stats()
+            assert st["reserved_bytes"] <= 2 << 20
+            srv.release(t)
+            done += 1
+        st = srv.stats()
+        assert st["peak_reserved_bytes"] <= 2 << 20
+        assert st["admission_waits"] > 0                 # later requests had to wait for memory
+        assert st["completed"] == 12
+
+
+def test_request_over_budget_rejected(gpu):
+    import nt2_gb300
+    S, K, T = pool(1 << 16)
+    with Server(budget_bytes=64 << 10, max_batch_requests=4, max_inflight_batches=1) as srv:
+        with pytest.raises(nt2_gb300.NT2CudaError) as ei:
+            srv.submit(S, K, T, 0.02, 0.30)
+        assert ei.value.status == 3                      # NT2CUDA_ERR_BUDGET
+
+
+def test_wait_is_bounded(gpu):
+    import nt2_gb300
+    S, K, T = pool(1 << 16)
+    n = 1 << 14
+    with Server(budget_bytes=160 << 10, max_batch_requests=4, max_inflight_batches=1) as srv:
+        t1 = srv.submit(S[:n], K[:n], T[:n], 0.02, 0.30)   # 128 KiB: admitted
+        t2 = srv.submit(S[:n], K[:n], T[:n], 0.02, 0.30)   # waits for t1's memory
+        srv.wait(t1, 30000)
+        with pytest.raises(nt2_gb300.NT2CudaError) as ei:
+            srv.wait(t2, 50)                              # t1 is never released: t2 cannot be admitted
+        assert ei.value.status == 5                      # NT2CUDA_ERR_TIMEOUT
+        assert srv.poll(t2) is None
+        srv.release(t1)
+        srv.wait(t2, 30000)
+        srv.release(t2)
+
+
+def test_concurrent_submitters(gpu, oracle):
+    S, K, T = pool(1 << 20, seed=9)
+    reqs = requests(1 << 20, 7, count=120)
+    results = {}
+    with Server(budget_bytes=128 << 20, max_batch_requests=32, max_inflight_batches=3) as srv:
+        def client(part):
+            for o, n in part:
+                t = srv.submit_ptr(S.data_ptr() + 4 * o, K.data_ptr() + 4 * o, T.data_ptr() + 4 * o, 0.02, 0.30, n)
+                c, p = srv.wait(t, 30000)
+                results[(o, n)] = (copy_out(c, n), copy_out(p, n))
+                torch.cuda.synchronize()
+                srv.release(t)
+        ths = [threading.Thread(target=client, args=(reqs[i::4],)) for i in range(4)]
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+        srv.drain(30000)
+    for (o, n), (c, p) in results.items():
+        ca, pa = gpu.blackscholes(S[o:o + n], K[o:o + n], T[o:o + n], 0.02, 0.30)
+        assert torch.equal(c, ca) and torch.equal(p, pa)

@@ -1,0 +1,210 @@
+"""Elementwise statements on the GPU against the CPU oracle.
+
+With fused = 0 the device evaluates NT2's arithmetic with the same
+roundings as the oracle, so every float32/float64 result must be
+bit-identical (ulpdist 0; NaNs compare equal).  fused = 1 (hardware FMA) is
+held to the stated ULP bounds below.
+"""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [0, 1, 3, 7, 31, 33, 1000, 4097, (1 << 16) + 5]
+# fused-FMA bounds (NT2 ulpdist units) against the unfused oracle
+FUSED_BOUND = {"exp": 1.0, "log": 1.0, "erfc": 4.0, "normcdf": 4.0, "fastnormcdf": 2.0, "sqrt": 0.0}
+
+
+def to_dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def inputs(op, n, dtype, seed=0):
+    rng = np.random.default_rng(seed)
+    if op in ("log", "sqrt"):
+        x = rng.uniform(0, 100, n)
+    elif op == "exp":
+        x = rng.uniform(-100, 100, n)
+    else:
+        x = rng.uniform(-10, 10, n)
+    x = x.astype(dtype)
+    specials = np.array([0.0, -0.0, 1.0, -1.0, np.inf, -np.inf, np.nan, 88.5, -88.5, 1e-40, -3.0], dtype)
+    if n >= len(specials):
+        x[: len(specials)] = specials
+    return x
+
+
+@pytest.mark.parametrize("op", ["exp", "log", "erfc", "normcdf", "fastnormcdf", "sqrt"])
+@pytest.mark.parametrize("n", SIZES)
+def test_map_f32_bit_exact(gpu, oracle, op, n):
+    x = inputs(op, n, np.float32, seed=n)
+    y = host(gpu.map_(op, to_dev(x)))
+    ref = oracle.map_(op, x)
+    m, w = oracle.max_ulp(y, ref)
+    assert m == 0.0, (op, n, w, x[w] if n else None, y[w] if n else None, ref[w] if n else None)
+
+
+@pytest.mark.parametrize("op", ["exp", "log", "erfc", "normcdf", "sqrt"])
+@pytest.mark.parametrize("n", [1, 7, 4097, (1 << 16) + 3])
+def test_map_f64_bit_exact(gpu, oracle, op, n):
+    x = inputs(op, n, np.float64, seed=n + 1)
+    y = host(gpu.map_(op, to_dev(x)))
+    ref = oracle.map_(op, x)
+    m, w = oracle.max_ulp(y, ref)
+    assert m == 0.0, (op, n, w)
+
+
+@pytest.mark.parametrize("op", ["exp", "log", "erfc", "normcdf", "fastnormcdf"])
+def test_map_f32_fused_within_bound(gpu, oracle, op):
+    x = inputs(op, 1 << 16, np.float32, seed=5)
+    y = host(gpu.map_(op, to_dev(x), fused=True))
+    m, _ = oracle.max_ulp(y, oracle.map_(op, x))
+    assert m <= FUSED_BOUND[op], (op, m)
+
+
+def test_map_misaligned_views(gpu, oracle):
+    x = inputs("erfc", 1000, np.float32)
+    xd = to_dev(x)
+    out = torch.empty(1001, dtype=torch.float32, device="cuda")
+    for off in (1, 2, 3):
+        xv = xd[off:]
+        yv = out[off:]
+        gpu.map_("erfc", xv, out=yv)
+        m, _ = oracle.max_ulp(host(yv), oracle.map_("erfc", x[off:]))
+        assert m == 0.0
+
+
+@pytest.mark.parametrize("n", SIZES)
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_saxpy_bit_exact(gpu, oracle, n, dtype):
+    rng = np.random.default_rng(n)
+    x = rng.uniform(-1, 1, n).astype(dtype)
+    y = rng.uniform(-1, 1, n).astype(dtype)
+    yd = to_dev(y)
+    gpu.saxpy(2.5, to_dev(x), yd)
+    ref = y.copy()
+    (oracle.load().nt2o_saxpy_f if dtype == np.float32 else oracle.load().nt2o_saxpy_d)(2.5, x, ref, n, 1)
+    assert np.array_equal(host(yd).view(np.uint8), ref.view(np.uint8))
+
+
+def test_rgb2grey_bit_exact(gpu, oracle):
+    n = 1920 * 1080 + 3
+    rng = np.random.default_rng(9)
+    r, g, b = (rng.uniform(0, 255, n).astype(np.float32) for _ in range(3))
+    out = host(gpu.rgb2grey(to_dev(r), to_dev(g), to_dev(b)))
+    ref = np.empty_like(r)
+    oracle.load().nt2o_rgb2grey_f(r, g, b, ref, n, 1)
+    assert np.array_equal(out.view(np.uint32), ref.view(np.uint32))
+
+
+def bs_inputs(n, dtype, seed=42):
+    rng = np.random.default_rng(seed)
+    S = rng.uniform(5, 30, n).astype(dtype)
+    K = rng.uniform(1, 100, n).astype(dtype)
+    T = rng.uniform(0.25, 10, n).astype(dtype)
+    return S, K, T
+
+
+@pytest.mark.parametrize("cdf", ["normcdf", "fastnormcdf"])
+@pytest.mark.parametrize("n", [1, 5, 1023, 4099, 1 << 20])
+def test_blackscholes_f32_bit_exact(gpu, oracle, cdf, n):
+    S, K, T = bs_inputs(n, np.float32, seed=n)
+    c, p = gpu.blackscholes(to_dev(S), to_dev(K), to_dev(T), 0.02, 0.30, cdf=cdf)
+    rc, rp = oracle.bs(S, K, T, 0.02, 0.30, cdf=0 if cdf == "normcdf" else 1)
+    for got, ref in ((host(c), rc), (host(p), rp)):
+        m, w = oracle.max_ulp(got, ref)
+        assert m == 0.0, (cdf, n, w, S[w], K[w], T[w], got[w], ref[w])
+
+
+@pytest.mark.parametrize("n", [1, 3, 4099, 1 << 18])
+def test_blackscholes_f64_bit_exact(gpu, oracle, n):
+    S, K, T = bs_inputs(n, np.float64, seed=n + 7)
+    c, p = gpu.blackscholes(to_dev(S), to_dev(K), to_dev(T), 0.02, 0.30)
+    rc, rp = oracle.bs(S, K, T, 0.02, 0.30)
+    assert oracle.max_ulp(host(c), rc)[0] == 0.0
+    assert oracle.max_ulp(host(p), rp)[0] == 0.0
+
+
+def test_blackscholes_f32_full_size_and_fp64_error(gpu, oracle):
+    """2^24 options: bit-exact against the oracle; error against the FP64 evaluation reported."""
+    n = 1 << 24
+    S, K, T = bs_inputs(n, np.float32, seed=2024)
+    c, p = gpu.blackscholes(to_dev(S), to_dev(K), to_dev(T), 0.02, 0.30)
+    gc, gp = host(c), host(p)
+    rc, rp = oracle.bs(S, K, T, 0.02, 0.30, threads=0)
+    assert oracle.max_ulp(gc, rc)[0] == 0.0
+    assert oracle.max_ulp(gp, rp)[0] == 0.0
+    c64, p64 = oracle.bs(S.astype(np.float64), K.astype(np.float64), T.astype(np.float64), 0.02, 0.30)
+    scale = np.maximum(np.abs(c64), 1.0)
+    err = np.max(np.abs(gc - c64) / scale)
+    assert err < 1e-4           # absolute error per unit of price, FP32 vs FP64 evaluation of the statement
+    # put-call parity as a size-independent property
+    parity = np.abs((gc.astype(np.float64) - gp) - (S - K * np.exp(-0.02 * T.astype(np.float64))))
+    assert np.max(parity / (1 + K)) < 5e-5
+
+
+def test_blackscholes_fused_within_bound(gpu, oracle):
+    n = 1 << 18
+    S, K, T = bs_inputs(n, np.float32, seed=3)
+    c, p = gpu.blackscholes(to_dev(S), to_dev(K), to_dev(T), 0.02, 0.30, fused=True)
+    rc, rp = oracle.bs(S, K, T, 0.02, 0.30)
+    c64, _ = oracle.bs(S.astype(np.float64), K.astype(np.float64), T.astype(np.float64), 0.02, 0.30)
+    # fused and unfused FP32 both within 1e-4 absolute of the FP64 evaluation (prices up to ~30)
+    assert np.max(np.abs(host(c) - c64) / np.maximum(np.abs(c64), 1)) < 1e-4
+    assert np.max(np.abs(rc - c64) / np.maximum(np.abs(c64), 1)) < 1e-4
+
+
+def test_blackscholes_demo_bit_exact(gpu, oracle):
+    n = 100003
+    rng = np.random.default_rng(11)
+    S = rng.uniform(5, 30, n).astype(np.float32)
+    X = rng.uniform(1, 100, n).astype(np.float32)
+    T = rng.uniform(0.25, 10, n).astype(np.float32)
+    r = rng.uniform(0.0, 0.05, n).astype(np.float32)
+    v = rng.uniform(0.1, 0.5, n).astype(np.float32)
+    R = host(gpu.blackscholes_demo(*(to_dev(a) for a in (S, X, T, r, v))))
+    ref = oracle.bs_demo(S, X, T, r, v)
+    m, w = oracle.max_ulp(R, ref)
+    assert m == 0.0, (w, R[w], ref[w])
+
+
+def test_blackscholes_host_entry(gpu, oracle):
+    n = (1 << 21) * 3 + 17   # several pipeline chunks and a ragged tail
+    S, K, T = bs_inputs(n, np.float32, seed=77)
+    ts = [torch.from_numpy(a).pin_memory() for a in (S, K, T)]
+    call = torch.empty(n, dtype=torch.float32).pin_memory()
+    put = torch.empty(n, dtype=torch.float32).pin_memory()
+    gpu.blackscholes_host(*ts, 0.02, 0.30, call, put)
+    rc, rp = oracle.bs(S, K, T, 0.02, 0.30)
+    assert oracle.max_ulp(call.numpy(), rc)[0] == 0.0
+    assert oracle.max_ulp(put.numpy(), rp)[0] == 0.0
+
+
+def test_alias_rules(gpu):
+    import nt2_gb300
+    x = torch.ones(1024, device="cuda")
+    # y aliases x with an offset: partial overlap is rejected
+    with pytest.raises(nt2_gb300.NT2CudaError):
+        gpu.saxpy(2.0, x[1:513], x[0:512])
+    # exact aliasing Y = a*Y + Y is allowed and elementwise
+    y = torch.full((1000,), 3.0, device="cuda")
+    gpu.saxpy(2.0, y, y)
+    assert torch.all(y == 9.0)
+
+
+def test_autotune_and_tuning_roundtrip(gpu, oracle):
+    u, w, ms = gpu.autotune("bs_f32", 1 << 20)
+    assert u in (1, 2, 4) and w in (1, 2, 4) and ms > 0
+    text = gpu.tuning_export()
+    assert "bs_f32@20" in text
+    assert gpu.tuning_import(text) >= 1
+    S, K, T = bs_inputs(1 << 20, np.float32, seed=1)
+    c, p = gpu.blackscholes(to_dev(S), to_dev(K), to_dev(T), 0.02, 0.30)
+    rc, _ = oracle.bs(S, K, T, 0.02, 0.30)
+    assert oracle.max_ulp(host(c), rc)[0] == 0.0
