@@ -1,0 +1,444 @@
+// nt2cuda/table.hpp -- NT2's table / expression front end, evaluated on the GPU.
+//
+// User code written against nt2::table compiles unchanged against this
+// header (compiled by nvcc, -std=c++17, with include/ and nt2_gb300/csrc/ on
+// the include path) once `nt2` is aliased to `nt2cuda`:
+//
+//     nt2cuda::table<float> X(nt2cuda::of_size(n)), Y(nt2cuda::of_size(n));
+//     for (std::size_t i = 1; i <= n; ++i) X(i) = Y(i) = float(i - 1);
+//     Y = alpha * X + Y;                          // one fused kernel
+//     float s = nt2cuda::globalsum(X * Y);        // fused fold
+//     nt2cuda::tie(call, put) = nt2cuda::tie(e1, e2);
+//
+// Mirrors (paths relative to the NT2 source tree):
+//   table container      modules/core/container/table/include/nt2/core/container/table/table.hpp:26-121
+//   assignment           modules/core/sdk/include/nt2/core/container/dsl/expression.hpp:161-191
+//   tie()                modules/core/container/table/include/nt2/core/functions/expr/tie.hpp:40-182
+//   globalsum / sum      modules/core/reduction/include/nt2/core/functions/globalsum.hpp:75-88,
+//                        modules/core/reduction/include/nt2/dsl/functions/reduction/run.hpp:30-104
+//
+// Residency: a table owns a device buffer in HBM and a host mirror that is
+// created on first element access.  Element access (1-based, column-major,
+// as NT2) moves the data to the host once and marks the device copy stale;
+// the next evaluation that reads the table uploads it once.  Evaluations run
+// on the table's stream (nt2cuda::set_stream) and, like NT2's operator=,
+// return with the results ready unless nt2cuda::set_synchronous(false).
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+#include <stdexcept>
+#include <string>
+#include <tuple>
+#include <type_traits>
+#include <utility>
+#include <vector>
+#include "nt2cuda/expr.cuh"
+#include "nt2cuda/fold_launch.cuh"
+#include "nt2cuda/launch.cuh"
+
+namespace nt2cuda {
+
+// ------------------------------------------------------------ settings
+struct eval_settings {
+  cudaStream_t stream = nullptr;
+  bool synchronous = true;
+  bool fused = false;       // hardware FMA for NT2's fma/fnms/horner steps
+  bool compensated = true;  // compensated FP32 folds
+};
+inline eval_settings& settings() { static thread_local eval_settings s; return s; }
+inline void set_stream(cudaStream_t s) { settings().stream = s; }
+inline void set_synchronous(bool b) { settings().synchronous = b; }
+inline void set_fused(bool b) { settings().fused = b; }
+inline void set_compensated(bool b) { settings().compensated = b; }
+
+struct error : std::runtime_error {
+  explicit error(const std::string& w, cudaError_t e)
+      : std::runtime_error(w + ": " + cudaGetErrorString(e)), code(e) {}
+  cudaError_t code;
+};
+inline void check(cudaError_t e, const char* where)
+{
+  if (e != cudaSuccess) throw error(where, e);
+}
+
+// ------------------------------------------------------------ of_size
+struct of_size_ {
+  size_t d[2] = {0, 1};
+  size_t numel() const { return d[0] * d[1]; }
+};
+inline of_size_ of_size(size_t n) { of_size_ s; s.d[0] = n; s.d[1] = 1; return s; }
+inline of_size_ of_size(size_t h, size_t w) { of_size_ s; s.d[0] = h; s.d[1] = w; return s; }
+
+template <class E> struct xpr;   // lazy expression
+template <class T> class table;
+
+// ------------------------------------------------------------- table
+template <class T> class table {
+ public:
+  using value_type = T;
+  table() = default;
+  explicit table(of_size_ s) { resize(s); }
+  table(const table& o) { *this = o; }
+  table(table&& o) noexcept { swap(o); }
+  template <class E> table(const xpr<E>& x) { *this = x; }
+  ~table() { release(); }
+
+  table& operator=(table&& o) noexcept { swap(o); return *this; }
+  table& operator=(const table& o)
+  {
+    if (this == &o) return *this;
+    resize(o.extent());
+    if (!numel()) return *this;
+    o.sync_device();
+    check(cudaMemcpyAsync(d_, o.d_, numel() * sizeof(T), cudaMemcpyDeviceToDevice, settings().stream),
+          "table copy");
+    dev_valid_ = true;
+    host_valid_ = false;
+    finish();
+    return *this;
+  }
+  template <class E> table& operator=(const xpr<E>& x);
+
+  void resize(of_size_ s)
+  {
+    if (s.d[0] == sz_.d[0] && s.d[1] == sz_.d[1]) return;
+    release();
+    sz_ = s;
+    if (numel()) check(cudaMalloc(&d_, numel() * sizeof(T)), "table alloc");
+    dev_valid_ = true;
+    host_valid_ = false;
+  }
+
+  size_t numel() const { return sz_.numel(); }
+  of_size_ extent() const { return sz_; }
+  size_t height() const { return sz_.d[0]; }
+  size_t width() const { return sz_.d[1]; }
+
+  // 1-based element access (host mirror)
+  T& operator()(size_t i) { sync_host(); dev_valid_ = false; return h_[i - 1]; }
+  T& operator()(size_t i, size_t j) { return (*this)(i + (j - 1) * sz_.d[0]); }
+  T operator()(size_t i) const { sync_host(); return h_[i - 1]; }
+  T operator()(size_t i, size_t j) const { return (*this)(i + (j - 1) * sz_.d[0]); }
+
+  // device pointer with the device copy current
+  T* device() { sync_device(); host_valid_ = false; return d_; }
+  const T* device() const { sync_device(); return d_; }
+  void mark_device_written() { dev_valid_ = true; host_valid_ = false; }
+
+  void sync_host() const
+  {
+    if (host_valid_) return;
+    h_.resize(numel());
+    if (numel()) {
+      check(cudaMemcpyAsync(h_.data(), d_, numel() * sizeof(T), cudaMemcpyDeviceToHost, settings().stream), "d2h");
+      check(cudaStreamSynchronize(settings().stream), "d2h sync");
+    }
+    host_valid_ = true;
+  }
+  void sync_device() const
+  {
+    if (dev_valid_) return;
+    if (numel())
+      check(cudaMemcpyAsync(d_, h_.data(), numel() * sizeof(T), cudaMemcpyHostToDevice, settings().stream), "h2d");
+    // h2d from pageable memory is staged before return; the host mirror stays valid
+    dev_valid_ = true;
+  }
+
+ private:
+  void release()
+  {
+    if (d_) cudaFree(d_);
+    d_ = nullptr;
+    h_.clear();
+    sz_ = of_size_{};
+    dev_valid_ = true;
+    host_valid_ = false;
+  }
+  void swap(table& o) noexcept
+  {
+    std::swap(d_, o.d_);
+    std::swap(sz_, o.sz_);
+    h_.swap(o.h_);
+    std::swap(dev_valid_, o.dev_valid_);
+    std::swap(host_valid_, o.host_valid_);
+  }
+  static void finish()
+  {
+    if (settings().synchronous) check(cudaStreamSynchronize(settings().stream), "evaluation");
+  }
+
+  T* d_ = nullptr;
+  of_size_ sz_{};
+  mutable std::vector<T> h_;
+  mutable bool dev_valid_ = true;
+  mutable bool host_valid_ = false;
+  template <class> friend class table;
+  friend struct detail_front;
+};
+
+// ----------------------------------------------------------- expressions
+// xpr<E> holds the device tree E plus the element count it evaluates over.
+template <class E> struct xpr {
+  E e;
+  of_size_ size;
+  using value_type = typename value_of<E>::type;
+};
+
+template <class X> struct is_table : std::false_type {};
+template <class T> struct is_table<table<T>> : std::true_type {};
+template <class X> struct is_xpr : std::false_type {};
+template <class E> struct is_xpr<xpr<E>> : std::true_type {};
+template <class X> constexpr bool is_operand_v =
+    is_table<std::decay_t<X>>::value || is_xpr<std::decay_t<X>>::value;
+
+// operand -> (tree, size)
+template <class T> inline term<T> tree_of(const table<T>& t) { return term<T>{t.device()}; }
+template <class E> inline E tree_of(const xpr<E>& x) { return x.e; }
+template <class T> inline of_size_ size_of(const table<T>& t) { return t.extent(); }
+template <class E> inline of_size_ size_of(const xpr<E>& x) { return x.size; }
+template <class X> struct elem_of;
+template <class T> struct elem_of<table<T>> { using type = T; };
+template <class E> struct elem_of<xpr<E>> { using type = typename value_of<E>::type; };
+
+inline of_size_ common_size(of_size_ a, of_size_ b)
+{
+  if (a.numel() != b.numel()) throw std::invalid_argument("nt2cuda: operand sizes differ");
+  return a;
+}
+
+// scalar operand, converted to the element type of the other side
+template <class V, class S> inline scal<V> scalar_as(S s) { return scal<V>{(V)s}; }
+
+template <class Tag, class A> inline auto make_unary(const A& a)
+{
+  auto t = tree_of(a);
+  return xpr<node<Tag, decltype(t)>>{node<Tag, decltype(t)>{t}, size_of(a)};
+}
+
+template <class Tag, class A, class B> inline auto make_binary(const A& a, const B& b)
+{
+  if constexpr (is_operand_v<A> && is_operand_v<B>) {
+    auto ta = tree_of(a);
+    auto tb = tree_of(b);
+    return xpr<node<Tag, decltype(ta), decltype(tb)>>{node<Tag, decltype(ta), decltype(tb)>{ta, tb},
+                                                      common_size(size_of(a), size_of(b))};
+  } else if constexpr (is_operand_v<A>) {
+    using V = typename elem_of<std::decay_t<A>>::type;
+    auto ta = tree_of(a);
+    auto tb = scalar_as<V>(b);
+    return xpr<node<Tag, decltype(ta), decltype(tb)>>{node<Tag, decltype(ta), decltype(tb)>{ta, tb}, size_of(a)};
+  } else {
+    using V = typename elem_of<std::decay_t<B>>::type;
+    auto ta = scalar_as<V>(a);
+    auto tb = tree_of(b);
+    return xpr<node<Tag, decltype(ta), decltype(tb)>>{node<Tag, decltype(ta), decltype(tb)>{ta, tb}, size_of(b)};
+  }
+}
+
+template <class X, class V> inline auto tree_or_scalar(const X& x)
+{
+  if constexpr (is_operand_v<X>) return tree_of(x); else return scal<V>{(V)x};
+}
+
+template <class Tag, class A, class B, class C> inline auto make_ternary(const A& a, const B& b, const C& c)
+{
+  // element type: first table/expression operand among a, b, c
+  using V = typename std::conditional_t<is_operand_v<A>, elem_of<std::decay_t<A>>,
+            std::conditional_t<is_operand_v<B>, elem_of<std::decay_t<B>>, elem_of<std::decay_t<C>>>>::type;
+  auto ta = tree_or_scalar<A, V>(a);
+  auto tb = tree_or_scalar<B, V>(b);
+  auto tc = tree_or_scalar<C, V>(c);
+  of_size_ sz{};
+  bool have = false;
+  auto take = [&](const auto& x) {
+    if constexpr (is_operand_v<std::decay_t<decltype(x)>>) {
+      sz = have ? common_size(sz, size_of(x)) : size_of(x);
+      have = true;
+    }
+  };
+  take(a); take(b); take(c);
+  using N = node<Tag, decltype(ta), decltype(tb), decltype(tc)>;
+  return xpr<N>{N{ta, tb, tc}, sz};
+}
+
+#define NT2CUDA_BINOP(OP, TAG)                                                          \
+  template <class A, class B, std::enable_if_t<is_operand_v<A> || is_operand_v<B>, int> = 0> \
+  inline auto operator OP(const A& a, const B& b) { return make_binary<tag::TAG>(a, b); }
+NT2CUDA_BINOP(+, plus_)
+NT2CUDA_BINOP(-, minus_)
+NT2CUDA_BINOP(*, multiplies_)
+NT2CUDA_BINOP(/, divides_)
+NT2CUDA_BINOP(<, is_less_)
+NT2CUDA_BINOP(>, is_greater_)
+NT2CUDA_BINOP(<=, is_less_equal_)
+NT2CUDA_BINOP(>=, is_greater_equal_)
+NT2CUDA_BINOP(==, is_equal_)
+NT2CUDA_BINOP(!=, is_not_equal_)
+#undef NT2CUDA_BINOP
+
+template <class A, std::enable_if_t<is_operand_v<A>, int> = 0>
+inline auto operator-(const A& a) { return make_unary<tag::unary_minus_>(a); }
+
+#define NT2CUDA_FN1(NAME, TAG)                                                          \
+  template <class A, std::enable_if_t<is_operand_v<A>, int> = 0>                        \
+  inline auto NAME(const A& a) { return make_unary<tag::TAG>(a); }
+NT2CUDA_FN1(exp, exp_)
+NT2CUDA_FN1(log, log_)
+NT2CUDA_FN1(sqrt, sqrt_)
+NT2CUDA_FN1(sqr, sqr_)
+NT2CUDA_FN1(erfc, erfc_)
+NT2CUDA_FN1(normcdf, normcdf_)
+NT2CUDA_FN1(fastnormcdf, fastnormcdf_)
+NT2CUDA_FN1(abs, abs_)
+NT2CUDA_FN1(rec, rec_)
+NT2CUDA_FN1(oneminus, oneminus_)
+NT2CUDA_FN1(minusone, minusone_)
+#undef NT2CUDA_FN1
+
+#define NT2CUDA_FN2(NAME, TAG)                                                          \
+  template <class A, class B, std::enable_if_t<is_operand_v<A> || is_operand_v<B>, int> = 0> \
+  inline auto NAME(const A& a, const B& b) { return make_binary<tag::TAG>(a, b); }
+NT2CUDA_FN2(max, max_)
+NT2CUDA_FN2(min, min_)
+NT2CUDA_FN2(adds, adds_)
+NT2CUDA_FN2(subs, subs_)
+NT2CUDA_FN2(selinc, selinc_)
+NT2CUDA_FN2(seldec, seldec_)
+#undef NT2CUDA_FN2
+
+#define NT2CUDA_FN3(NAME, TAG)                                                          \
+  template <class A, class B, class C,                                                  \
+            std::enable_if_t<is_operand_v<A> || is_operand_v<B> || is_operand_v<C>, int> = 0> \
+  inline auto NAME(const A& a, const B& b, const C& c) { return make_ternary<tag::TAG>(a, b, c); }
+NT2CUDA_FN3(fma, fma_)
+NT2CUDA_FN3(fnms, fnms_)
+NT2CUDA_FN3(if_else, if_else_)
+#undef NT2CUDA_FN3
+
+// if_zero_else_one(c): the result has the element type of the compared operands.
+template <class E> inline auto if_zero_else_one(const xpr<E>& c)
+{
+  using R = typename value_of<std::decay_t<decltype(c.e.a)>>::type;
+  using N = node<tag::if_zero_else_one_, E, scal<R>>;
+  return xpr<N>{N{c.e, scal<R>{R(0)}}, c.size};
+}
+
+// ------------------------------------------------------- evaluation
+template <class T> template <class E> table<T>& table<T>::operator=(const xpr<E>& x)
+{
+  // resize: inputs were captured as device pointers when the tree was built
+  if (x.size.numel() != numel()) {
+    if (numel()) throw std::invalid_argument("nt2cuda: assignment to a table of another size");
+    resize(x.size);
+  }
+  T* out = device();
+  auto p = make_prog(assign<T, E>{out, x.e});
+  cudaError_t e = settings().fused ? transform<true>(p, numel(), settings().stream)
+                                   : transform<false>(p, numel(), settings().stream);
+  check(e, "transform");
+  check(cudaGetLastError(), "transform launch");
+  mark_device_written();
+  finish();
+  return *this;
+}
+
+// ------------------------------------------------------------------ tie
+template <class... Ts> struct tie_lhs {
+  std::tuple<table<Ts>&...> outs;
+
+  template <class... Es> tie_lhs& operator=(const std::tuple<xpr<Es>...>& rhs)
+  {
+    static_assert(sizeof...(Es) == sizeof...(Ts), "tie: arity mismatch");
+    assign_all(rhs, std::index_sequence_for<Ts...>{});
+    return *this;
+  }
+
+ private:
+  template <class R, size_t... I> void assign_all(const R& rhs, std::index_sequence<I...>)
+  {
+    const size_t n = std::get<0>(rhs).size.numel();
+    // outputs are sized first; their device pointers are the assign targets
+    int dummy[] = {(prepare(std::get<I>(outs), n), 0)...};
+    (void)dummy;
+    auto p = make_prog(assign<typename std::remove_reference_t<decltype(std::get<I>(outs))>::value_type,
+                              std::decay_t<decltype(std::get<I>(rhs).e)>>{std::get<I>(outs).device(),
+                                                                          std::get<I>(rhs).e}...);
+    cudaError_t e = settings().fused ? transform<true>(p, n, settings().stream)
+                                     : transform<false>(p, n, settings().stream);
+    check(e, "tie transform");
+    check(cudaGetLastError(), "tie launch");
+    int dummy2[] = {(std::get<I>(outs).mark_device_written(), 0)...};
+    (void)dummy2;
+    if (settings().synchronous) check(cudaStreamSynchronize(settings().stream), "tie");
+  }
+  template <class T> static void prepare(table<T>& t, size_t n)
+  {
+    if (t.numel() != n) t.resize(of_size(n));
+  }
+};
+
+template <class... Ts> inline tie_lhs<Ts...> tie(table<Ts>&... ts) { return tie_lhs<Ts...>{{ts...}}; }
+template <class... Es> inline std::tuple<xpr<Es>...> tie(const xpr<Es>&... xs) { return std::tuple<xpr<Es>...>(xs...); }
+
+// ------------------------------------------------------------ reductions
+template <class X> inline auto as_xpr(const X& x)
+{
+  if constexpr (is_table<std::decay_t<X>>::value) {
+    using T = typename std::decay_t<X>::value_type;
+    return xpr<term<T>>{term<T>{x.device()}, x.extent()};
+  } else {
+    return x;
+  }
+}
+
+// globalsum(X): the sum of every element, on the host
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto globalsum(const X& x)
+{
+  auto e = as_xpr(x);
+  using V = typename decltype(e)::value_type;
+  using A = std::conditional_t<std::is_floating_point<V>::value, V, double>;
+  static_assert(std::is_same<A, float>::value || std::is_same<A, double>::value, "globalsum: float or double");
+  A* d = nullptr;
+  check(cudaMalloc(&d, sizeof(A)), "globalsum alloc");
+  cudaStream_t s = settings().stream;
+  cudaError_t err = (std::is_same<A, float>::value && settings().compensated)
+                        ? fold::inner_fold<true, A>(e.e, e.size.numel(), 1, d, s)
+                        : fold::inner_fold<false, A>(e.e, e.size.numel(), 1, d, s);
+  A r = 0;
+  if (err == cudaSuccess) err = cudaMemcpyAsync(&r, d, sizeof(A), cudaMemcpyDeviceToHost, s);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+  cudaFree(d);
+  check(err, "globalsum");
+  return (V)r;
+}
+
+// sum(A, dim) for a 2-D table (dim 1: column sums, dim 2: row sums), as NT2's
+// reduction run_assign picks inner_fold or outer_fold.
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto sum(const X& x, int dim = 1)
+{
+  auto e = as_xpr(x);
+  using V = typename decltype(e)::value_type;
+  const size_t rows = e.size.d[0], cols = e.size.d[1];
+  cudaStream_t s = settings().stream;
+  if (dim == 1) {
+    table<V> out(of_size(1, cols));
+    cudaError_t err = settings().compensated && std::is_same<V, float>::value
+                          ? fold::inner_fold<true, V>(e.e, rows, cols, out.device(), s)
+                          : fold::inner_fold<false, V>(e.e, rows, cols, out.device(), s);
+    check(err, "sum(A,1)");
+    out.mark_device_written();
+    if (settings().synchronous) check(cudaStreamSynchronize(s), "sum");
+    return out;
+  }
+  table<V> out(of_size(rows, 1));
+  cudaError_t err = settings().compensated && std::is_same<V, float>::value
+                        ? fold::outer_fold<true, V>(e.e, rows, cols, out.device(), s)
+                        : fold::outer_fold<false, V>(e.e, rows, cols, out.device(), s);
+  check(err, "sum(A,2)");
+  out.mark_device_written();
+  if (settings().synchronous) check(cudaStreamSynchronize(s), "sum");
+  return out;
+}
+
+}  // namespace nt2cuda

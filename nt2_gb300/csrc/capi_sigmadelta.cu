@@ -223,7 +223,7 @@ nt2cuda_status nt2cuda_sigmadelta_batch_u8(const nt2cuda_sd_stream* streams, int
   if (st != NT2CUDA_OK) return st;
   cudaStream_t s = as_stream(stream);
   void* dev = nullptr;
-  st = stream_scratch(s, batch_bytes(nstreams), &dev, 1);
+  st = detail_capi::stream_scratch(s, batch_bytes(nstreams), &dev, 1);
   if (st != NT2CUDA_OK) return st;
   sd_desc* dd;
   uint64_t* dt;

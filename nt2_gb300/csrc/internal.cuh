@@ -4,6 +4,7 @@
 #include <mutex>
 #include <unordered_map>
 #include "../../include/nt2cuda.h"
+#include "nt2cuda/scratch.cuh"
 
 namespace nt2cuda {
 namespace detail_capi {
@@ -30,43 +31,9 @@ inline nt2cuda_status launch_status(cudaError_t e)
   return from_cuda(e, NT2CUDA_ERR_LAUNCH);
 }
 
-// Per-stream scratch for the multi-block folds.  Each stream gets its own
-// buffer so folds enqueued on different streams never share partials;
-// calls on one stream are ordered, so they can reuse it.  The buffer only
-// grows; growing synchronises the stream first.
-struct scratch_pool {
-  struct entry { void* p = nullptr; size_t bytes = 0; };
-  std::mutex m;
-  std::unordered_map<uintptr_t, entry> by_stream;
-};
-inline scratch_pool& pool() { static scratch_pool p; return p; }
-
-// slot 0: fold partials and counters; slot 1: batched-launch descriptors.
 inline nt2cuda_status stream_scratch(cudaStream_t s, size_t bytes, void** out, int slot = 0)
 {
-  int dev = 0;
-  cudaGetDevice(&dev);
-  uintptr_t key = (reinterpret_cast<uintptr_t>(s) * 64u + (uintptr_t)dev) * 4u + (uintptr_t)slot;
-  scratch_pool& P = pool();
-  std::lock_guard<std::mutex> g(P.m);
-  scratch_pool::entry& e = P.by_stream[key];
-  if (e.bytes < bytes) {
-    if (e.p) {
-      cudaStreamSynchronize(s);
-      cudaFree(e.p);
-      e.p = nullptr;
-      e.bytes = 0;
-    }
-    size_t want = bytes < 4096 ? 4096 : bytes;
-    cudaError_t err = cudaMalloc(&e.p, want);
-    if (err != cudaSuccess) { e.p = nullptr; return from_cuda(err); }
-    // counters at the front of the scratch start (and are left) at zero
-    err = cudaMemsetAsync(e.p, 0, want, s);
-    if (err != cudaSuccess) return from_cuda(err);
-    e.bytes = want;
-  }
-  *out = e.p;
-  return NT2CUDA_OK;
+  return from_cuda(nt2cuda::stream_scratch(s, bytes, out, slot));
 }
 
 }  // namespace detail_capi

@@ -152,8 +152,27 @@ template <bool F> struct fn<tag::if_else_, F> {
 template <class E> struct value_of;
 template <class T> struct value_of<term<T>> { using type = T; };
 template <class T> struct value_of<scal<T>> { using type = T; };
+// Result type of a functor from its argument types (spelled out rather than
+// deduced from fn::apply, which is device code): comparisons give bool,
+// selinc/seldec/if_else give their second argument's type, everything else
+// its first argument's type.
+template <class Tag, class... A> struct tag_result;
+template <class Tag, class A, class... R> struct tag_result<Tag, A, R...> { using type = A; };
+#define NT2CUDA_BOOL_RESULT(TAG) \
+  template <class A, class B> struct tag_result<tag::TAG, A, B> { using type = bool; };
+NT2CUDA_BOOL_RESULT(is_less_)
+NT2CUDA_BOOL_RESULT(is_greater_)
+NT2CUDA_BOOL_RESULT(is_less_equal_)
+NT2CUDA_BOOL_RESULT(is_greater_equal_)
+NT2CUDA_BOOL_RESULT(is_equal_)
+NT2CUDA_BOOL_RESULT(is_not_equal_)
+#undef NT2CUDA_BOOL_RESULT
+template <class A, class B> struct tag_result<tag::selinc_, A, B> { using type = B; };
+template <class A, class B> struct tag_result<tag::seldec_, A, B> { using type = B; };
+template <class A, class B, class C> struct tag_result<tag::if_else_, A, B, C> { using type = B; };
+
 template <class Tag, class... C> struct value_of<node<Tag, C...>> {
-  using type = decltype(fn<Tag, false>::apply(std::declval<typename value_of<C>::type>()...));
+  using type = typename tag_result<Tag, typename value_of<C>::type...>::type;
 };
 // if_zero_else_one carries its result type in a scal<R> second child that is never read.
 template <class A, class R> struct value_of<node<tag::if_zero_else_one_, A, scal<R>>> { using type = R; };
@@ -258,7 +277,6 @@ template <class P, int V> struct pregs;
 template <int V> struct pregs<prog<>, V> {
   template <bool S> __device__ __forceinline__ void load(const prog<>&, size_t) {}
   template <bool F> __device__ __forceinline__ void compute_store(const prog<>&, size_t) {}
-  template <bool F> __device__ __forceinline__ void ordered(const prog<>&, size_t) {}
 };
 template <class T, class E, class... As, int V> struct pregs<prog<assign<T, E>, As...>, V> {
   using P = prog<assign<T, E>, As...>;
@@ -268,30 +286,22 @@ template <class T, class E, class... As, int V> struct pregs<prog<assign<T, E>, 
     r.template load<S>(p.head.e, i);
     rest.template load<S>(p.tail, i);
   }
-  template <bool F> __device__ __forceinline__ void store_head(const P& p, size_t i) {
+  template <bool F> __device__ __forceinline__ void compute_store(const P& p, size_t i) {
     T out[V];
 #pragma unroll
     for (int l = 0; l < V; ++l) out[l] = (T)r.template get<F>(p.head.e, l);
     mem::store_vec<T, V>(p.head.out, i, out);
-  }
-  template <bool F> __device__ __forceinline__ void compute_store(const P& p, size_t i) {
-    store_head<F>(p, i);
     rest.template compute_store<F>(p.tail, i);
-  }
-  // Load, compute and store each assign in turn with coherent loads, so an
-  // assign reads the outputs that earlier assigns of the statement wrote.
-  template <bool F> __device__ __forceinline__ void ordered(const P& p, size_t i) {
-    r.template load<false>(p.head.e, i);
-    store_head<F>(p, i);
-    rest.template ordered<F>(p.tail, i);
   }
 };
 
 // ---------------------------------------------------------- the kernel
 // Persistent grid-stride transform.  Each thread owns groups of V contiguous
-// elements and keeps U groups in flight per trip; the n % V tail is done one
-// element per thread by the first threads of the grid.
-template <bool F, bool Ordered, int V, int U, class P>
+// elements and keeps U groups in flight per trip: all terminals of all
+// assigns of a group are loaded before any of its outputs is stored, which
+// is NT2's order for tie() statements.  The n % V tail is done one element
+// per thread by the first threads of the grid.
+template <bool F, int V, int U, class P>
 __global__ void __launch_bounds__(256) k_transform(P p, size_t n)
 {
   const size_t ngroups = n / V;
@@ -300,25 +310,21 @@ __global__ void __launch_bounds__(256) k_transform(P p, size_t n)
   size_t g = tid;
   for (; g + (size_t)(U - 1) * T < ngroups; g += (size_t)U * T) {
     pregs<P, V> r[U];
-    if constexpr (!Ordered) {
 #pragma unroll
-      for (int u = 0; u < U; ++u) r[u].template load<true>(p, (g + (size_t)u * T) * V);
+    for (int u = 0; u < U; ++u) r[u].template load<true>(p, (g + (size_t)u * T) * V);
 #pragma unroll
-      for (int u = 0; u < U; ++u) r[u].template compute_store<F>(p, (g + (size_t)u * T) * V);
-    } else {
-#pragma unroll
-      for (int u = 0; u < U; ++u) r[u].template ordered<F>(p, (g + (size_t)u * T) * V);
-    }
+    for (int u = 0; u < U; ++u) r[u].template compute_store<F>(p, (g + (size_t)u * T) * V);
   }
   for (; g < ngroups; g += T) {
     pregs<P, V> r;
-    if constexpr (!Ordered) { r.template load<true>(p, g * V); r.template compute_store<F>(p, g * V); }
-    else r.template ordered<F>(p, g * V);
+    r.template load<true>(p, g * V);
+    r.template compute_store<F>(p, g * V);
   }
   const size_t tail0 = ngroups * V;
   if (tid < n - tail0) {
     pregs<P, 1> r;
-    r.template ordered<F>(p, tail0 + tid);
+    r.template load<false>(p, tail0 + tid);
+    r.template compute_store<F>(p, tail0 + tid);
   }
 }
 

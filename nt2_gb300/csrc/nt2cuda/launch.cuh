@@ -40,18 +40,22 @@ inline void visit_prog(const prog<assign<T, E>, As...>& p, F&& f, int a = 0)
   visit_prog(p.tail, f, a + 1);
 }
 
-enum class alias_kind { none, ordered, bad };
+enum class alias_kind { none, bad };
 
 // Classify how the inputs of a statement alias its outputs over n elements.
-// An input equal to an output of its own assign is fine in either order (each
-// element is read before it is written, by the same thread); an input that
-// is another assign's output needs the ordered evaluation; any partial
-// overlap is rejected.
+// An input that is exactly one of the statement's outputs is fine: NT2
+// evaluates every right-hand side of a statement (all members of a tie())
+// at an index before it stores any output
+// (modules/core/container/table/include/nt2/core/functions/expr/tie.hpp:70-95),
+// and the kernel does the same, each element read by the thread that later
+// writes it.  Partial overlaps, and one table bound to two outputs, are
+// rejected.
 template <class P> inline alias_kind classify_alias(const P& p, size_t n)
 {
   ptr_span spans[64]; int ns = 0;
-  visit_prog(p, [&](ptr_span s) { if (ns < 64) spans[ns++] = s; });
-  alias_kind k = alias_kind::none;
+  bool overflow = false;
+  visit_prog(p, [&](ptr_span s) { if (ns < 64) spans[ns++] = s; else overflow = true; });
+  if (overflow) return alias_kind::bad;
   for (int i = 0; i < ns; ++i) {
     if (!spans[i].out) continue;
     const char* o0 = (const char*)spans[i].p; const char* o1 = o0 + n * spans[i].bytes;
@@ -61,10 +65,9 @@ template <class P> inline alias_kind classify_alias(const P& p, size_t n)
       if (a1 <= o0 || o1 <= a0) continue;                      // disjoint
       if (a0 != o0 || spans[j].bytes != spans[i].bytes) return alias_kind::bad;
       if (spans[j].out) return alias_kind::bad;                // two outputs on one table
-      if (spans[j].assign != spans[i].assign) k = alias_kind::ordered;
     }
   }
-  return k;
+  return alias_kind::none;
 }
 
 template <class P> inline bool all_aligned(const P& p, unsigned align)
@@ -121,17 +124,12 @@ inline cudaError_t transform(const P& p, size_t n, cudaStream_t s, const char* t
   size_t nn = n;
   void* args[] = {&pc, &nn};
   const bool vec = all_aligned(p, 16u);
-  if (!vec) {
-    if (ak == alias_kind::ordered) return launch_persistent(k_transform<F, true, 1, 1, P>, n, 256, W, s, args);
-    return launch_persistent(k_transform<F, false, 1, 1, P>, n, 256, W, s, args);
-  }
+  if (!vec) return launch_persistent(k_transform<F, 1, 1, P>, n, 256, W, s, args);
   const size_t groups = n / V;
-  if (ak == alias_kind::ordered)
-    return launch_persistent(k_transform<F, true, V, 1, P>, groups, 256, W, s, args);
   switch (U) {
-    case 1: return launch_persistent(k_transform<F, false, V, 1, P>, groups, 256, W, s, args);
-    case 4: return launch_persistent(k_transform<F, false, V, 4, P>, groups, 256, W, s, args);
-    default: return launch_persistent(k_transform<F, false, V, 2, P>, groups, 256, W, s, args);
+    case 1: return launch_persistent(k_transform<F, V, 1, P>, groups, 256, W, s, args);
+    case 4: return launch_persistent(k_transform<F, V, 4, P>, groups, 256, W, s, args);
+    default: return launch_persistent(k_transform<F, V, 2, P>, groups, 256, W, s, args);
   }
 }
 

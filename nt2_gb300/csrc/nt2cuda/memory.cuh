@@ -1,10 +1,12 @@
 // nt2cuda/memory.cuh -- 16-byte global loads and stores for streaming tables.
 //
 // Tables on the evaluator's path are read once and written once per
-// evaluation, so inputs that the kernel does not also write are read through
-// the non-coherent path without L1 allocation, and outputs are stored with
-// the evict-first (.cs) policy.  Inputs that alias an output of the same
-// multi-output assignment are read with plain coherent loads instead.
+// evaluation, so inputs are read through the non-coherent path without L1
+// allocation and outputs are stored with the evict-first (.cs) policy.  An
+// input may be the same table as an output of its statement (Y = a*X + Y):
+// every element is then read, before it is written, by the one thread that
+// writes it, and never read again, so no stale line can be observed.
+// ld_plain is the coherent load used for single elements.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>

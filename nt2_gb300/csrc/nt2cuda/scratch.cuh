@@ -1,0 +1,53 @@
+// nt2cuda/scratch.cuh -- per-stream device scratch for multi-block kernels.
+//
+// The folds keep per-block partials and arrival counters in global memory.
+// Each (stream, device, slot) gets its own buffer, so kernels enqueued on
+// different streams never share scratch; calls on one stream are ordered and
+// reuse it.  A buffer only grows; growing synchronises its stream first.  The
+// first call on a stream allocates (cudaMalloc), so make it before capturing
+// that stream into a CUDA graph.  Counters at the front of a fold's scratch
+// start at zero (the buffer is cleared when allocated) and every fold leaves
+// them at zero.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <mutex>
+#include <unordered_map>
+
+namespace nt2cuda {
+
+struct scratch_pool {
+  struct entry { void* p = nullptr; size_t bytes = 0; };
+  std::mutex m;
+  std::unordered_map<uintptr_t, entry> by_key;
+};
+inline scratch_pool& global_scratch_pool() { static scratch_pool p; return p; }
+
+// slot 0: fold partials and counters; slot 1: batched-launch descriptors.
+inline cudaError_t stream_scratch(cudaStream_t s, size_t bytes, void** out, int slot = 0)
+{
+  int dev = 0;
+  cudaGetDevice(&dev);
+  uintptr_t key = (reinterpret_cast<uintptr_t>(s) * 64u + (uintptr_t)dev) * 4u + (uintptr_t)slot;
+  scratch_pool& P = global_scratch_pool();
+  std::lock_guard<std::mutex> g(P.m);
+  scratch_pool::entry& e = P.by_key[key];
+  if (e.bytes < bytes) {
+    if (e.p) {
+      cudaStreamSynchronize(s);
+      cudaFree(e.p);
+      e.p = nullptr;
+      e.bytes = 0;
+    }
+    size_t want = bytes < 4096 ? 4096 : bytes;
+    cudaError_t err = cudaMalloc(&e.p, want);
+    if (err != cudaSuccess) { e.p = nullptr; return err; }
+    err = cudaMemsetAsync(e.p, 0, want, s);
+    if (err != cudaSuccess) return err;
+    e.bytes = want;
+  }
+  *out = e.p;
+  return cudaSuccess;
+}
+
+}  // namespace nt2cuda

@@ -1,0 +1,33 @@
+"""Compile demos.cu (NT2's demo statements as NT2 user code) with nvcc for sm_103a."""
+from __future__ import annotations
+
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(HERE)
+ROOT = os.path.dirname(PKG)
+OUT = os.path.join(HERE, "_build", "demos")
+
+
+def build(verbose: bool = False) -> str:
+    src = os.path.join(HERE, "demos.cu")
+    deps = [src]
+    for d in (os.path.join(ROOT, "include"), os.path.join(PKG, "csrc", "nt2cuda")):
+        for base, _, files in os.walk(d):
+            deps += [os.path.join(base, f) for f in files]
+    if os.path.exists(OUT) and all(os.path.getmtime(OUT) > os.path.getmtime(d) for d in deps):
+        return OUT
+    os.makedirs(os.path.dirname(OUT), exist_ok=True)
+    cmd = [os.environ.get("NVCC", "nvcc"), "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
+           "-lineinfo", "-I", os.path.join(ROOT, "include"), "-I", os.path.join(PKG, "csrc"), src, "-o", OUT]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"demo build failed:\n{r.stdout}\n{r.stderr}")
+    return OUT
+
+
+if __name__ == "__main__":
+    print(build(verbose=True))

@@ -1,0 +1,130 @@
+// demos.cu -- NT2's demo statements, written as NT2 user code against the
+// nt2cuda table front end (namespace nt2 = nt2cuda).  Each subcommand reads
+// its input tables from raw binary files, evaluates the reference demo's
+// statements and writes the result tables, so a test can compare them with
+// the oracle:
+//   saxpy      demo/saxpy/nt2/saxpy_nt2.cpp:39-42
+//   sdot       demo/sdot/nt2/sdot_nt2.cpp:35-38
+//   bs         demo/blackscholes/nt2/blackandscholes_nt2.cpp:53-60
+//   bs_merged  demo/blackscholes/nt2_merged/blackandscholes_nt2_merged.cpp:57-64
+//   rgb2grey   demo/rgb2grey/nt2/rgb2grey_nt2.cpp:42-45
+//   sigmadelta demo/sigmadelta/nt2/sigmadelta_nt2.cpp:37-58, 100-106
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+#include "nt2cuda/table.hpp"
+
+namespace nt2 = nt2cuda;
+
+template <class T> static std::vector<T> read_file(const char* path, size_t n)
+{
+  std::vector<T> v(n);
+  FILE* f = std::fopen(path, "rb");
+  if (!f || std::fread(v.data(), sizeof(T), n, f) != n) { std::fprintf(stderr, "cannot read %s\n", path); std::exit(2); }
+  std::fclose(f);
+  return v;
+}
+
+template <class T> static void load(nt2::table<T>& t, const std::vector<T>& v)
+{
+  for (std::size_t i = 1; i <= t.numel(); ++i) t(i) = v[i - 1];
+}
+
+template <class T> static void write_table(const char* path, const nt2::table<T>& t)
+{
+  FILE* f = std::fopen(path, "wb");
+  for (std::size_t i = 1; i <= t.numel(); ++i) { T x = t(i); std::fwrite(&x, sizeof(T), 1, f); }
+  std::fclose(f);
+}
+
+// the five statements of the demo's do_work, one table assignment each
+template <class Pixel>
+static void do_work(Pixel& bkg, const Pixel& fr, Pixel& var, Pixel& diff_img, Pixel& mul_img, Pixel& out)
+{
+  typename Pixel::value_type zero = 0;
+  bkg = nt2::selinc(bkg < fr, nt2::seldec(bkg > fr, bkg));
+  diff_img = nt2::max(bkg, fr) - nt2::min(bkg, fr);
+  mul_img = nt2::adds(nt2::adds(diff_img, diff_img), diff_img);
+  var = nt2::if_else(diff_img != zero, nt2::selinc(var < mul_img, nt2::seldec(var > mul_img, var)), var);
+  out = nt2::if_zero_else_one(diff_img < var);
+}
+
+int main(int argc, char** argv)
+{
+  if (argc < 3) { std::fprintf(stderr, "usage: demos <cmd> <n> files...\n"); return 2; }
+  std::string cmd = argv[1];
+  const std::size_t n = std::strtoull(argv[2], nullptr, 10);
+  if (cmd == "saxpy") {                                   // in: x y ; out: y
+    typedef float T;
+    T alpha = 2.5f;
+    nt2::table<T> X(nt2::of_size(n)), Y(nt2::of_size(n));
+    load(X, read_file<T>(argv[3], n));
+    load(Y, read_file<T>(argv[4], n));
+    Y = alpha * X + Y;
+    write_table(argv[5], Y);
+  } else if (cmd == "sdot") {                             // in: x y ; prints the sum
+    typedef float T;
+    nt2::table<T> X(nt2::of_size(n)), Y(nt2::of_size(n));
+    load(X, read_file<T>(argv[3], n));
+    load(Y, read_file<T>(argv[4], n));
+    T res = nt2::globalsum(X * Y);
+    std::printf("%.9e\n", (double)res);
+  } else if (cmd == "bs" || cmd == "bs_merged") {         // in: S X T r v ; out: R
+    typedef float T;
+    nt2::table<T> Sa(nt2::of_size(n)), Xa(nt2::of_size(n)), Ta(nt2::of_size(n)), ra(nt2::of_size(n)),
+        va(nt2::of_size(n)), R(nt2::of_size(n));
+    load(Sa, read_file<T>(argv[3], n));
+    load(Xa, read_file<T>(argv[4], n));
+    load(Ta, read_file<T>(argv[5], n));
+    load(ra, read_file<T>(argv[6], n));
+    load(va, read_file<T>(argv[7], n));
+    if (cmd == "bs") {
+      nt2::table<T> da = nt2::sqrt(Ta);
+      nt2::table<T> d1 = nt2::log(Sa / Xa) + (nt2::fma(nt2::sqr(va), T(0.5), ra) * Ta) / (va * da);
+      nt2::table<T> d2 = nt2::fnms(va, da, d1);
+      R = nt2::fnms(Xa * nt2::exp(-ra * Ta), nt2::fastnormcdf(d2), Sa * nt2::fastnormcdf(d1));
+    } else {
+      nt2::table<T> da(nt2::of_size(n)), d1(nt2::of_size(n)), d2(nt2::of_size(n));
+      // every right-hand side reads the tables as they were before the statement, so the
+      // results settle on the second evaluation (the demo calls its operator() repeatedly)
+      for (int rep = 0; rep < 3; ++rep)
+        nt2::tie(da, d1, d2, R) = nt2::tie(nt2::sqrt(Ta),
+                                           nt2::log(Sa / Xa) + (nt2::fma(nt2::sqr(va), T(0.5), ra) * Ta) / (va * da),
+                                           nt2::fnms(va, da, d1),
+                                           nt2::fnms(Xa * nt2::exp(-ra * Ta), nt2::fastnormcdf(d2),
+                                                     Sa * nt2::fastnormcdf(d1)));
+    }
+    write_table(argv[8], R);
+  } else if (cmd == "rgb2grey") {                         // in: r g b ; out: gr
+    typedef float T;
+    nt2::table<T> r(nt2::of_size(n)), g(nt2::of_size(n)), b(nt2::of_size(n)), gr(nt2::of_size(n));
+    load(r, read_file<T>(argv[3], n));
+    load(g, read_file<T>(argv[4], n));
+    load(b, read_file<T>(argv[5], n));
+    gr = T(0.3) * r + T(0.59) * g + T(0.11) * b;
+    write_table(argv[6], gr);
+  } else if (cmd == "sigmadelta") {                       // n = pixels; argv[3] = frames; in: frames ; out: bkg var label
+    typedef unsigned char T;
+    const int nb_frames = std::atoi(argv[3]);
+    std::vector<T> all = read_file<T>(argv[4], n * (std::size_t)nb_frames);
+    std::vector<nt2::table<T>> frames((std::size_t)nb_frames);
+    for (int k = 0; k < nb_frames; ++k) {
+      frames[(std::size_t)k].resize(nt2::of_size(n));
+      for (std::size_t i = 1; i <= n; ++i) frames[(std::size_t)k](i) = all[(std::size_t)k * n + i - 1];
+    }
+    nt2::table<T> image_variance(nt2::of_size(n)), diff_img(nt2::of_size(n)), mul_img(nt2::of_size(n)),
+        background_img(nt2::of_size(n)), binary_label(nt2::of_size(n));
+    for (std::size_t i = 1; i <= n; ++i) { image_variance(i) = 1; background_img(i) = frames[0](i); }
+    for (int k = 1; k < nb_frames; ++k)
+      do_work(background_img, frames[(std::size_t)k], image_variance, diff_img, mul_img, binary_label);
+    write_table(argv[5], background_img);
+    write_table(argv[6], image_variance);
+    write_table(argv[7], binary_label);
+  } else {
+    std::fprintf(stderr, "unknown demo %s\n", cmd.c_str());
+    return 2;
+  }
+  return 0;
+}

@@ -1,0 +1,91 @@
+"""NT2's demo programs, written as NT2 user code against the nt2cuda table front
+end (nt2_gb300/demo/demos.cu), produce the oracle's results bit for bit."""
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def demos(gpu):
+    sys.path.insert(0, os.path.join(ROOT, "nt2_gb300", "demo"))
+    import build_demos
+    return build_demos.build()
+
+
+def run(demos, tmp_path, cmd, n, arrays, outs, extra=()):
+    files = []
+    for i, a in enumerate(arrays):
+        p = tmp_path / f"in{i}.bin"
+        np.ascontiguousarray(a).tofile(p)
+        files.append(str(p))
+    out_files = [str(tmp_path / f"out{i}.bin") for i in range(outs)]
+    r = subprocess.run([demos, cmd, str(n), *extra, *files, *out_files], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr
+    return r.stdout, out_files
+
+
+def test_saxpy_demo(demos, oracle, tmp_path):
+    n = 100003
+    rng = np.random.default_rng(1)
+    x = rng.uniform(-1, 1, n).astype(np.float32)
+    y = rng.uniform(-1, 1, n).astype(np.float32)
+    _, (o,) = run(demos, tmp_path, "saxpy", n, [x, y], 1)
+    ref = y.copy()
+    oracle.load().nt2o_saxpy_f(2.5, x, ref, n, 1)
+    assert np.array_equal(np.fromfile(o, np.float32).view(np.uint32), ref.view(np.uint32))
+
+
+def test_sdot_demo(demos, oracle, tmp_path):
+    n = 1 << 20
+    rng = np.random.default_rng(2)
+    x = rng.standard_normal(n).astype(np.float32)
+    y = rng.standard_normal(n).astype(np.float32)
+    out, _ = run(demos, tmp_path, "sdot", n, [x, y], 0)
+    ref, ab = oracle.dot_fp64(x, y)
+    assert abs(float(out) - ref) <= 2 ** -22 * ab
+
+
+@pytest.mark.parametrize("form", ["bs", "bs_merged"])
+def test_blackscholes_demo(demos, oracle, tmp_path, form):
+    n = 50001
+    rng = np.random.default_rng(3)
+    S = rng.uniform(5, 30, n).astype(np.float32)
+    X = rng.uniform(1, 100, n).astype(np.float32)
+    T = rng.uniform(0.25, 10, n).astype(np.float32)
+    r = rng.uniform(0, 0.05, n).astype(np.float32)
+    v = rng.uniform(0.1, 0.5, n).astype(np.float32)
+    _, (o,) = run(demos, tmp_path, form, n, [S, X, T, r, v], 1)
+    ref = oracle.bs_demo(S, X, T, r, v)
+    m, w = oracle.max_ulp(np.fromfile(o, np.float32), ref)
+    assert m == 0.0, (form, w)
+
+
+def test_rgb2grey_demo(demos, oracle, tmp_path):
+    n = 640 * 480
+    rng = np.random.default_rng(4)
+    r, g, b = (rng.uniform(0, 255, n).astype(np.float32) for _ in range(3))
+    _, (o,) = run(demos, tmp_path, "rgb2grey", n, [r, g, b], 1)
+    ref = np.empty_like(r)
+    oracle.load().nt2o_rgb2grey_f(r, g, b, ref, n, 1)
+    assert np.array_equal(np.fromfile(o, np.float32).view(np.uint32), ref.view(np.uint32))
+
+
+def test_sigmadelta_demo(demos, oracle, tmp_path):
+    npix, nf = 333 * 97, 6
+    rng = np.random.default_rng(5)
+    bg = rng.integers(16, 240, npix)
+    frames = np.concatenate([np.clip(bg + rng.integers(-8, 9, npix), 0, 255) for _ in range(nf)]).astype(np.uint8)
+    frames[3 * npix + 100:3 * npix + 400] = 255
+    _, (ob, ov, ol) = run(demos, tmp_path, "sigmadelta", npix, [frames], 3, extra=(str(nf),))
+    rb, rv, rl = oracle.sigmadelta(frames, npix, npix, nf, init=True)
+    assert np.array_equal(np.fromfile(ob, np.uint8), rb)
+    assert np.array_equal(np.fromfile(ov, np.uint8), rv)
+    assert np.array_equal(np.fromfile(ol, np.uint8), rl[(nf - 2) * npix:])    # the demo keeps the last label

@@ -12,8 +12,9 @@ import torch
 pytestmark = pytest.mark.gpu
 
 SIZES = [0, 1, 3, 7, 31, 33, 1000, 4097, (1 << 16) + 5]
-# fused-FMA bounds (NT2 ulpdist units) against the unfused oracle
-FUSED_BOUND = {"exp": 1.0, "log": 1.0, "erfc": 4.0, "normcdf": 4.0, "fastnormcdf": 2.0, "sqrt": 0.0}
+# fused-FMA bounds (NT2 ulpdist units) against the unfused oracle; erfc and normcdf stay within
+# the 16 ULP that NT2 states for its float erfc (erf_kernel.hpp:50-52)
+FUSED_BOUND = {"exp": 1.0, "log": 1.0, "erfc": 16.0, "normcdf": 16.0, "fastnormcdf": 2.0, "sqrt": 0.0}
 
 
 def to_dev(a):
