@@ -140,6 +140,20 @@ nt2cuda_status nt2cuda_blackscholes_f32_host(const float* S, const float* K, con
 nt2cuda_status nt2cuda_globalsum_f32(const float* x, size_t n, float* out, int compensated, nt2cuda_stream stream);
 nt2cuda_status nt2cuda_dot_f32(const float* x, const float* y, size_t n, float* out, int compensated,
                                nt2cuda_stream stream);
+/* No counterpart in the reference: NT2 has no device code.  The same result
+ * as nt2cuda_dot_f32, for callers that cannot allocate device memory (their
+ * device memory belongs to another allocator, or cudaMalloc's device-wide
+ * synchronisation is not acceptable in their loop).  It allocates nothing:
+ * its scratch is a fixed 512.25 KiB array in device memory, held by every GPU
+ * that loads the library until the process exits.  n may not exceed
+ * NT2CUDA_DOT_NOALLOC_MAX_N (larger n returns NT2CUDA_ERR_ARG).  The first
+ * call on a device looks up the array's address on that device; make that
+ * first call before any stream capture.  All calls share the array, so calls
+ * whose kernels overlap on the GPU (other streams, other threads) race;
+ * calls on one stream are safe.  *out is a DEVICE scalar. */
+#define NT2CUDA_DOT_NOALLOC_MAX_N ((size_t)1 << 30)
+nt2cuda_status nt2cuda_dot_f32_noalloc(const float* x, const float* y, size_t n, float* out, int compensated,
+                                       nt2cuda_stream stream);
 nt2cuda_status nt2cuda_globalsum_f64(const double* x, size_t n, double* out, nt2cuda_stream stream);
 nt2cuda_status nt2cuda_dot_f64(const double* x, const double* y, size_t n, double* out, nt2cuda_stream stream);
 

@@ -83,6 +83,7 @@ _SIGS = {
     "nt2cuda_blackscholes_f32_host": (c_int, [c_vp, c_vp, c_vp, c_f, c_f, c_vp, c_vp, c_size, c_int, c_int]),
     "nt2cuda_globalsum_f32": (c_int, [c_vp, c_size, c_vp, c_int, c_vp]),
     "nt2cuda_dot_f32": (c_int, [c_vp, c_vp, c_size, c_vp, c_int, c_vp]),
+    "nt2cuda_dot_f32_noalloc": (c_int, [c_vp, c_vp, c_size, c_vp, c_int, c_vp]),
     "nt2cuda_globalsum_f64": (c_int, [c_vp, c_size, c_vp, c_vp]),
     "nt2cuda_dot_f64": (c_int, [c_vp, c_vp, c_size, c_vp, c_vp]),
     "nt2cuda_sum_inner_f32": (c_int, [c_vp, c_size, c_size, c_vp, c_int, c_vp]),

@@ -23,6 +23,7 @@ SOURCES = [
     "capi_fold.cu",
     "capi_sigmadelta.cu",
     "server.cu",
+    "capi_noalloc.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
