@@ -309,14 +309,28 @@ def run_ours(args):
     stream = torch.cuda.current_stream().cuda_stream
     sp, kp, tp, cp, pp = S.data_ptr(), K.data_ptr(), T.data_ptr(), call.data_ptr(), put.data_ptr()
 
-    def step():
-        st = L.nt2cuda_blackscholes_f32(sp, kp, tp, R, SIGMA, cp, pp, n, 0, 0, stream)
-        if st:
-            raise RuntimeError(f"blackscholes status {st}")
+    # the project's autotuner picks unroll and grid waves per precision mode (outside the timed region)
+    tuned = {}
+    for key in ("bs_f32", "bs_f32_fused", "bs_f32_fast"):
+        u, w, tms = api.autotune(key, n)
+        tuned[key] = {"unroll": u, "waves": w, "ms": tms}
 
+    def make_step(prec):
+        def step():
+            st = L.nt2cuda_blackscholes_f32(sp, kp, tp, R, SIGMA, cp, pp, n, 0, prec, stream)
+            if st:
+                raise RuntimeError(f"blackscholes status {st}")
+        return step
+
+    step = make_step(0)
     sampler = ClockSampler(torch.cuda.current_device()).start()
     time.sleep(0.3)
     ms, t0, t1 = time_device(step, args.steps, max(args.warmup, 3), ws)
+    modes = {}
+    for name, prec in (("fused", 1), ("fast", 2)):
+        mms, _, _ = time_device(make_step(prec), min(args.steps, 500), max(args.warmup, 3), ws)
+        gbs = BYTES_PER_OPTION * n / (mms * 1e-3) / 1e9
+        modes[name] = {"ms_per_step": mms, "options_per_s": ws * n / (mms * 1e-3), "gb_per_s": gbs}
     value = ws * n / (ms * 1e-3)
     peak, peak_kind = peaks()
     achieved = BYTES_PER_OPTION * n / (ms * 1e-3) / 1e9
@@ -336,13 +350,26 @@ def run_ours(args):
     for _ in range(3):
         e2e_step()
     e2e_steps = max(3, min(args.steps, 200))
+    # the staged copy pipeline, for comparison (pageable host tables take it automatically)
+    Sp, Kp, Tp, cpg, ppg = (torch.empty(n, dtype=torch.float32) for _ in range(5))
+    Sp.copy_(Sh); Kp.copy_(Kh); Tp.copy_(Th)
+    hsp = [a.data_ptr() for a in (Sp, Kp, Tp, cpg, ppg)]
+    st = L.nt2cuda_blackscholes_f32_host(hsp[0], hsp[1], hsp[2], R, SIGMA, hsp[3], hsp[4], n, 0, 0)
+    tp0 = time.perf_counter()
+    for _ in range(min(e2e_steps, 20)):
+        st |= L.nt2cuda_blackscholes_f32_host(hsp[0], hsp[1], hsp[2], R, SIGMA, hsp[3], hsp[4], n, 0, 0)
+    staged_pageable_ms = (time.perf_counter() - tp0) * 1e3 / min(e2e_steps, 20)
+    if st:
+        raise RuntimeError(f"blackscholes_host (pageable) status {st}")
+    del Sp, Kp, Tp, cpg, ppg
     barrier(ws)
     te0 = time.perf_counter()
     for _ in range(e2e_steps):
         e2e_step()
     te1 = time.perf_counter()
     e2e_ms = max_over_ranks((te1 - te0) * 1e3 / e2e_steps, ws)
-    # results of the e2e path equal the device path's
+    # results of the e2e path equal the device path's (recomputed: the mode timings reuse call/put)
+    step()
     torch.cuda.synchronize()
     same = bool(torch.equal(ch, call.cpu()) and torch.equal(ph, put.cpu()))
     sampler.stop()
@@ -364,10 +391,18 @@ def run_ours(args):
                      "algorithmic_bytes_per_launch": BYTES_PER_OPTION * n},
         "e2e": {"value": ws * n / (e2e_ms * 1e-3), "unit": "options/s", "h2d_bytes_per_step": 12 * n,
                 "d2h_bytes_per_step": 8 * n, "ms_per_step": e2e_ms, "steps": e2e_steps,
-                "results_equal_device_path": same},
+                "results_equal_device_path": same,
+                "path": "pinned host tables read and written in place by the kernel over NVLink-C2C",
+                "pageable_host_tables_ms_per_step": staged_pageable_ms},
         "gpu_launches": args.steps,
         "clocks": clocks,
+        "precision_modes": modes,
+        "autotune": tuned,
     }
+    peak_v = peak
+    for m in modes.values():
+        m["hbm_frac_measured"] = m["gb_per_s"] / peak_v
+        m["hbm_frac_nominal"] = m["gb_per_s"] / NOMINAL_HBM_GBS
     if rank == 0 and ws == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline()
     if rank == 0 and ws == 1 and not args.no_serving:
@@ -385,8 +420,22 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def suite(ws: int):
-    """One line per other configuration (device time, inputs resident, > L2 or flushed)."""
+CASES = ("bs_exact", "bs_fused", "bs_fast", "bs_fastnormcdf", "bs_f64", "saxpy", "sdot", "sdot_plain",
+         "inner", "outer", "sigmadelta")
+
+
+def run_case(name: str, steps: int, warmup: int):
+    """One configuration alone, for profiling: prints one JSON line."""
+    import torch
+    torch.cuda.set_device(0)
+    import nt2_gb300.api as api
+    api.init(0)
+    for line in suite(1, only=name, steps=steps, warmup=warmup):
+        print(json.dumps(line), flush=True)
+
+
+def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: int = 3):
+    """One line per configuration (device time, inputs resident, > L2 or flushed)."""
     import torch
     import nt2_gb300.api as api
     from nt2_gb300 import video
@@ -398,23 +447,52 @@ def suite(ws: int):
         return {"config": name, "ms": ms, "gb_per_s": gbs, "hbm_frac_measured": gbs / peak,
                 "hbm_frac_nominal": gbs / NOMINAL_HBM_GBS, "value": units / (ms * 1e-3), "unit": unit}
 
-    n = 1 << 24
-    x = torch.empty(n, device="cuda")
-    y = torch.empty(n, device="cuda")
-    api.fill_uniform(x, -1, 1, 1)
-    api.fill_uniform(y, -1, 1, 2)
-    ms, _, _ = time_device(lambda: api.saxpy(2.5, x, y), 200, 5, ws)
-    out.append(line("saxpy f32 2^24", ms, 12 * n, n, "elements/s"))
-    n = 1 << 26
-    x = torch.empty(n, device="cuda")
-    y = torch.empty(n, device="cuda")
-    api.fill_normal(x, 1)
-    api.fill_normal(y, 2)
-    o = torch.empty(1, device="cuda")
-    ms, _, _ = time_device(lambda: api.dot(x, y, out=o), 100, 5, ws)
-    out.append(line("sdot f32 2^26 compensated", ms, 8 * n, n, "elements/s"))
-    ms, _, _ = time_device(lambda: api.dot(x, y, compensated=False, out=o), 100, 5, ws)
-    out.append(line("sdot f32 2^26 plain", ms, 8 * n, n, "elements/s"))
+    def want(name):
+        return only is None or only == name
+
+    flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def flushed(fn):
+        def f():
+            flush_buf.zero_()
+            fn()
+        return f
+
+    def flush_only_ms():
+        m, _, _ = time_device(lambda: flush_buf.zero_(), 50, 3, ws)
+        return m
+
+    def K(default):
+        return steps if steps is not None else default
+
+    if want("saxpy"):
+        n = 1 << 24
+        x = torch.empty(n, device="cuda")
+        y = torch.empty(n, device="cuda")
+        api.fill_uniform(x, -1, 1, 1)
+        api.fill_uniform(y, -1, 1, 2)
+        api.autotune("saxpy_f32", n)
+        fm0 = flush_only_ms()
+        ms, _, _ = time_device(flushed(lambda: api.saxpy(2.5, x, y)), K(200), warmup, ws)
+        out.append(line("saxpy f32 2^24 (L2 flushed)", ms - fm0, 12 * n, n, "elements/s"))
+        del x, y
+    if want("sdot") or want("sdot_plain"):
+        n = 1 << 26
+        x = torch.empty(n, device="cuda")
+        y = torch.empty(n, device="cuda")
+        api.fill_normal(x, 1)
+        api.fill_normal(y, 2)
+        o = torch.empty(1, device="cuda")
+        if want("sdot"):
+            ms, _, _ = time_device(lambda: api.dot(x, y, out=o), K(100), warmup, ws)
+            out.append(line("sdot f32 2^26 compensated", ms, 8 * n, n, "elements/s"))
+        if want("sdot_plain"):
+            ms, _, _ = time_device(lambda: api.dot(x, y, compensated=False, out=o), K(100), warmup, ws)
+            out.append(line("sdot f32 2^26 plain", ms, 8 * n, n, "elements/s"))
+        del x, y
+    if not (want("inner") or want("outer") or want("bs_f64") or want("bs_fused") or want("bs_fast")
+            or want("bs_exact") or want("bs_fastnormcdf") or want("sigmadelta")):
+        return out
     rows, cols = 8192, 4096
     A = torch.empty(rows * cols, device="cuda")
     api.fill_normal(A, 3)
@@ -432,42 +510,55 @@ def suite(ws: int):
         m, _, _ = time_device(lambda: flush.zero_(), 50, 3, ws)
         return m
 
-    fm = flush_ms()
-    ms, _, _ = time_device(with_flush(lambda: api.sum_colmajor(A, rows, cols, 1, out=oc)), 50, 3, ws)
-    out.append(line("inner_fold column sums 8192x4096 f32 compensated (L2 flushed)", ms - fm,
-                    4 * rows * cols + 4 * cols, rows * cols, "elements/s"))
-    ms, _, _ = time_device(with_flush(lambda: api.sum_colmajor(A, rows, cols, 2, out=orow)), 50, 3, ws)
-    out.append(line("outer_fold row sums 8192x4096 f32 compensated (L2 flushed)", ms - fm,
-                    4 * rows * cols + 4 * rows, rows * cols, "elements/s"))
-    n = 1 << 24
-    S = torch.empty(n, dtype=torch.float64, device="cuda")
-    K = torch.empty(n, dtype=torch.float64, device="cuda")
-    T = torch.empty(n, dtype=torch.float64, device="cuda")
-    api.fill_uniform(S, 5, 30, 1)
-    api.fill_uniform(K, 1, 100, 2)
-    api.fill_uniform(T, 0.25, 10, 3)
-    c = torch.empty_like(S)
-    p = torch.empty_like(S)
-    ms, _, _ = time_device(lambda: api.blackscholes(S, K, T, R, SIGMA, call=c, put=p), 20, 3, ws)
-    out.append(line("Black-Scholes f64 2^24 (FP64-issue bound)", ms, 40 * n, n, "options/s"))
-    del S, K, T, c, p
-    S, K, T = bs_tables(1 << 24, 5)
-    c = torch.empty_like(S)
-    p = torch.empty_like(S)
-    ms, _, _ = time_device(lambda: api.blackscholes(S, K, T, R, SIGMA, call=c, put=p, fused=True), 200, 5, ws)
-    out.append(line("Black-Scholes f32 2^24 fused FMA", ms, 20 * (1 << 24), 1 << 24, "options/s"))
-    ms, _, _ = time_device(lambda: api.blackscholes(S, K, T, R, SIGMA, call=c, put=p, cdf="fastnormcdf"), 200, 5,
-                           ws)
-    out.append(line("Black-Scholes f32 2^24 fastnormcdf", ms, 20 * (1 << 24), 1 << 24, "options/s"))
-    del S, K, T, c, p
-    batch = video.make_batch(256, 8, seed=11)
-    torch.cuda.synchronize()
-    plan = api.SigmaDeltaPlan(batch, 8, init=True)
-    ms, _, _ = time_device(plan.launch, 20, 3, ws)
-    pf = video.pixel_frames(batch, 8, True)
-    out.append(line("sigmadelta 256 streams x 8 frames uint8 (graph)", ms, video.bytes_moved(batch, 8, True), pf,
-                    "pixel-frames/s"))
-    plan.close()
+    if want("inner") or want("outer"):
+        fm = flush_ms()
+        if want("inner"):
+            ms, _, _ = time_device(with_flush(lambda: api.sum_colmajor(A, rows, cols, 1, out=oc)), K(50), warmup, ws)
+            out.append(line("inner_fold column sums 8192x4096 f32 compensated (L2 flushed)", ms - fm,
+                            4 * rows * cols + 4 * cols, rows * cols, "elements/s"))
+        if want("outer"):
+            ms, _, _ = time_device(with_flush(lambda: api.sum_colmajor(A, rows, cols, 2, out=orow)), K(50), warmup,
+                                   ws)
+            out.append(line("outer_fold row sums 8192x4096 f32 compensated (L2 flushed)", ms - fm,
+                            4 * rows * cols + 4 * rows, rows * cols, "elements/s"))
+    del A, flush
+    if want("bs_f64"):
+        n = 1 << 24
+        S = torch.empty(n, dtype=torch.float64, device="cuda")
+        Kt = torch.empty(n, dtype=torch.float64, device="cuda")
+        T = torch.empty(n, dtype=torch.float64, device="cuda")
+        api.fill_uniform(S, 5, 30, 1)
+        api.fill_uniform(Kt, 1, 100, 2)
+        api.fill_uniform(T, 0.25, 10, 3)
+        c = torch.empty_like(S)
+        p = torch.empty_like(S)
+        ms, _, _ = time_device(lambda: api.blackscholes(S, Kt, T, R, SIGMA, call=c, put=p), K(20), warmup, ws)
+        out.append(line("Black-Scholes f64 2^24 (FP64-issue bound)", ms, 40 * n, n, "options/s"))
+        del S, Kt, T, c, p
+    bs_cases = [("bs_exact", "exact", "normcdf"), ("bs_fused", "fused", "normcdf"), ("bs_fast", "fast", "normcdf"),
+                ("bs_fastnormcdf", "exact", "fastnormcdf")]
+    if any(want(cn) for cn, _, _ in bs_cases):
+        S, Kt, T = bs_tables(1 << 24, 5)
+        c = torch.empty_like(S)
+        p = torch.empty_like(S)
+        for key in ("bs_f32", "bs_f32_fused", "bs_f32_fast"):
+            api.autotune(key, 1 << 24)
+        for cn, prec, cdf in bs_cases:
+            if not want(cn) or (only is None and cn == "bs_exact"):
+                continue
+            ms, _, _ = time_device(lambda: api.blackscholes(S, Kt, T, R, SIGMA, call=c, put=p, precision=prec,
+                                                            cdf=cdf), K(200), warmup, ws)
+            out.append(line(f"Black-Scholes f32 2^24 {prec} {cdf}", ms, 20 * (1 << 24), 1 << 24, "options/s"))
+        del S, Kt, T, c, p
+    if want("sigmadelta"):
+        batch = video.make_batch(256, 8, seed=11)
+        torch.cuda.synchronize()
+        plan = api.SigmaDeltaPlan(batch, 8, init=True)
+        ms, _, _ = time_device(plan.launch, K(20), warmup, ws)
+        pf = video.pixel_frames(batch, 8, True)
+        out.append(line("sigmadelta 256 streams x 8 frames uint8 (graph)", ms, video.bytes_moved(batch, 8, True),
+                        pf, "pixel-frames/s"))
+        plan.close()
     return out
 
 
@@ -520,8 +611,11 @@ def main():
     ap.add_argument("--suite", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--case", choices=CASES, help="run one configuration alone (for profiling)")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.case:
+        run_case(args.case, args.steps, max(args.warmup, 3))
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -18,6 +18,10 @@
  *   - Every entry point returns an nt2cuda_status; none calls exit() or traps.
  *   - `fused` = 0 evaluates NT2's fma/fnms/Horner steps unfused (bit-exact
  *     with NT2 built without FMA contraction); 1 uses hardware FMA.
+ *   - `precision` (Black-Scholes entry points and the server) takes those two
+ *     values and 2 = fast: hardware FMA, the special-function unit for exp and
+ *     log, and reciprocal division inside erfc (float only; its distance to the
+ *     exact results and to FP64 is stated in the tests).
  */
 #ifndef NT2CUDA_H_INCLUDED
 #define NT2CUDA_H_INCLUDED
@@ -30,6 +34,9 @@ extern "C" {
 #endif
 
 typedef void* nt2cuda_stream;
+
+/* precision modes (see the conventions above) */
+enum { NT2CUDA_PREC_EXACT = 0, NT2CUDA_PREC_FUSED = 1, NT2CUDA_PREC_FAST = 2 };
 
 /* Status codes.  NT2's OpenMP spawners capture worker exceptions and drop
  * them (modules/arch/openmp/include/nt2/sdk/openmp/spawner/transform.hpp:40-69);
@@ -108,10 +115,10 @@ nt2cuda_status nt2cuda_rgb2grey_f32(const float* r, const float* g, const float*
  * in one pass (a tie() assignment, modules/core/container/table/include/nt2/core/functions/expr/tie.hpp:40-74).
  * cdf_kind 0 = normcdf via erfc, 1 = fastnormcdf (float only). */
 nt2cuda_status nt2cuda_blackscholes_f32(const float* S, const float* K, const float* T, float r, float sigma,
-                                        float* call, float* put, size_t n, int cdf_kind, int fused,
+                                        float* call, float* put, size_t n, int cdf_kind, int precision,
                                         nt2cuda_stream stream);
 nt2cuda_status nt2cuda_blackscholes_f64(const double* S, const double* K, const double* T, double r,
-                                        double sigma, double* call, double* put, size_t n, int fused,
+                                        double sigma, double* call, double* put, size_t n, int precision,
                                         nt2cuda_stream stream);
 
 /* The Black-Scholes demo statement, verbatim
@@ -128,7 +135,7 @@ nt2cuda_status nt2cuda_blackscholes_demo_f32(const float* S, const float* X, con
  * the results.  Host buffers should be pinned for full copy bandwidth. */
 nt2cuda_status nt2cuda_blackscholes_f32_host(const float* S, const float* K, const float* T, float r,
                                              float sigma, float* call, float* put, size_t n, int cdf_kind,
-                                             int fused);
+                                             int precision);
 
 /* ------------------------------------------------------------- folds ---- */
 /* globalsum(X) and globalsum(X*Y) (modules/core/reduction/include/nt2/core/functions/globalsum.hpp:75-88,
@@ -218,7 +225,7 @@ typedef struct {
   int max_batch_requests;     /* requests coalesced into one launch         */
   int max_inflight_batches;   /* launches on the device at once (streams)   */
   int coalesce;               /* 1 = batched work-list, 0 = launch per request */
-  int fused;
+  int fused;                  /* precision mode: 0 exact, 1 fused, 2 fast   */
   int cdf_kind;               /* 0 = normcdf, 1 = fastnormcdf               */
   int wait_timeout_ms;        /* default bound of waits (<= 0: 60000)       */
 } nt2cuda_server_config;
@@ -250,9 +257,10 @@ nt2cuda_status nt2cuda_server_drain(nt2cuda_server* server, int timeout_ms);
 nt2cuda_status nt2cuda_server_get_stats(nt2cuda_server* server, nt2cuda_server_stats* stats);
 
 /* ------------------------------------------------------------ tuning ---- */
-/* Times the transform variants of one entry point at size n on scratch
- * tables and records the fastest for n's size bucket.  kernel: "saxpy_f32",
- * "bs_f32", "bs_f64", "map_f32". */
+/* Times the launch variants of one entry point at size n on scratch tables
+ * and records the fastest for n's size bucket.  kernel: "saxpy_f32",
+ * "saxpy_f64", "bs_f32", "bs_f32_fused", "bs_f32_fast", "bs_f64",
+ * "bs_f64_fused" (the Black-Scholes keys are per precision mode). */
 nt2cuda_status nt2cuda_autotune(const char* kernel, size_t n, int* best_unroll, int* best_waves, float* best_ms);
 /* Tuning table as text ("key@bucket unroll waves" lines). */
 nt2cuda_status nt2cuda_tuning_export(char* buf, size_t cap, size_t* needed);

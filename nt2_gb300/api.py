@@ -73,10 +73,21 @@ def rgb2grey(r: torch.Tensor, g: torch.Tensor, b: torch.Tensor, out: torch.Tenso
     return out
 
 
+PRECISION = {"exact": 0, "fused": 1, "fast": 2}
+
+
+def _prec(fused, precision):
+    if precision is not None:
+        return PRECISION[precision]
+    return 1 if fused else 0
+
+
 def blackscholes(S: torch.Tensor, K: torch.Tensor, T: torch.Tensor, r: float, sigma: float,
                  call: torch.Tensor | None = None, put: torch.Tensor | None = None,
-                 cdf: str = "normcdf", fused: bool = False):
-    """(call, put) prices for n options; float32 or float64 tables."""
+                 cdf: str = "normcdf", fused: bool = False, precision: str | None = None):
+    """(call, put) prices for n options; float32 or float64 tables.
+
+    precision: "exact" (bit-exact NT2 arithmetic, default), "fused" (hardware FMA) or "fast"."""
     n = S.numel()
     if K.numel() != n or T.numel() != n:
         raise ValueError("S, K, T must have the same size")
@@ -86,13 +97,13 @@ def blackscholes(S: torch.Tensor, K: torch.Tensor, T: torch.Tensor, r: float, si
     if S.dtype == torch.float32:
         st = L.nt2cuda_blackscholes_f32(_dev(S), _dev(K, torch.float32), _dev(T, torch.float32), r, sigma,
                                         _dev(call, torch.float32), _dev(put, torch.float32), n, CDF[cdf],
-                                        int(fused), _stream())
+                                        _prec(fused, precision), _stream())
     elif S.dtype == torch.float64:
         if cdf != "normcdf":
             raise ValueError("fastnormcdf is float32 only")
         st = L.nt2cuda_blackscholes_f64(_dev(S), _dev(K, torch.float64), _dev(T, torch.float64), r, sigma,
-                                        _dev(call, torch.float64), _dev(put, torch.float64), n, int(fused),
-                                        _stream())
+                                        _dev(call, torch.float64), _dev(put, torch.float64), n,
+                                        _prec(fused, precision), _stream())
     else:
         raise TypeError("blackscholes takes float32 or float64 tables")
     check(st, "blackscholes")
@@ -109,13 +120,14 @@ def blackscholes_demo(S, X, T, r, v, out=None, fused: bool = False) -> torch.Ten
     return out
 
 
-def blackscholes_host(S, K, T, r: float, sigma: float, call, put, cdf: str = "normcdf", fused: bool = False):
+def blackscholes_host(S, K, T, r: float, sigma: float, call, put, cdf: str = "normcdf", fused: bool = False,
+                      precision: str | None = None):
     """Host-buffer form: S, K, T, call, put are CPU float32 tensors (pinned for best speed)."""
     for t in (S, K, T, call, put):
         if t.is_cuda or not t.is_contiguous() or t.dtype != torch.float32:
             raise ValueError("host tables must be contiguous CPU float32 tensors")
     check(lib().nt2cuda_blackscholes_f32_host(S.data_ptr(), K.data_ptr(), T.data_ptr(), r, sigma, call.data_ptr(),
-                                              put.data_ptr(), S.numel(), CDF[cdf], int(fused)),
+                                              put.data_ptr(), S.numel(), CDF[cdf], _prec(fused, precision)),
           "blackscholes_host")
     return call, put
 

@@ -6,13 +6,14 @@
 // the image with the diff and mul temporaries materialised.  Here the five
 // statements are fused per pixel, every frame of a stream is processed while
 // bkg/var stay in registers, and all streams share one launch driven by a
-// (stream, tile) work-list.  Pixels are handled four to a 32-bit word with
-// CUDA's byte-SIMD intrinsics; the arithmetic is NT2's:
+// (stream, tile) work-list.  Pixels are handled two to a __half2 on the FMA
+// pipe (exact small-integer arithmetic); the arithmetic is NT2's:
 //   bkg  = selinc(bkg < fr, seldec(bkg > fr, bkg))
 //   diff = max(bkg, fr) - min(bkg, fr)
 //   mul  = adds(adds(diff, diff), diff)                (saturating uint8)
 //   var  = if_else(diff != 0, selinc(var < mul, seldec(var > mul, var)), var)
 //   out  = if_zero_else_one(diff < var)
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <vector>
@@ -41,20 +42,39 @@ struct sd_desc {
   uint32_t pad;
 };
 
-// One frame step for four pixels packed in a word.
-__device__ __forceinline__ uint32_t sd_step4(uint32_t& b, uint32_t f, uint32_t& v)
+// Two pixels per __half2 on the FMA pipe.  Pixel values, their differences,
+// 3*diff (<= 765) and the biased values 1024 + x are all integers below 2048,
+// so every half-precision operation below is exact.  A byte x becomes the half
+// 1024 + x by placing it under the exponent byte 0x64 (one PRMT), and the low
+// byte of such a half is x again.
+__device__ __forceinline__ void unpack_bytes(uint32_t w, __half2& lo, __half2& hi)
 {
-  const uint32_t ones = 0x01010101u;
-  uint32_t inc = __vcmpltu4(b, f) & ones;
-  uint32_t dec = __vcmpgtu4(b, f) & ones;
-  b = __vsub4(__vadd4(b, inc), dec);
-  uint32_t d = __vabsdiffu4(b, f);
-  uint32_t m = __vaddus4(__vaddus4(d, d), d);
-  uint32_t nz = __vcmpne4(d, 0u);
-  uint32_t vinc = __vcmpltu4(v, m) & nz & ones;
-  uint32_t vdec = __vcmpgtu4(v, m) & nz & ones;
-  v = __vsub4(__vadd4(v, vinc), vdec);
-  return (~__vcmpltu4(d, v)) & ones;
+  uint32_t a = __byte_perm(w, 0x64646464u, 0x4140);   // [0x64 x1 0x64 x0]
+  uint32_t b = __byte_perm(w, 0x64646464u, 0x4342);   // [0x64 x3 0x64 x2]
+  lo = *reinterpret_cast<__half2*>(&a);
+  hi = *reinterpret_cast<__half2*>(&b);
+}
+
+__device__ __forceinline__ uint32_t pack_bytes(__half2 lo, __half2 hi)
+{
+  uint32_t a = *reinterpret_cast<uint32_t*>(&lo);
+  uint32_t b = *reinterpret_cast<uint32_t*>(&hi);
+  return __byte_perm(a, b, 0x6420);                  // low bytes of the four halves
+}
+
+// One frame step: b and f biased (1024 + x), v plain; returns the biased label.
+__device__ __forceinline__ __half2 sd_step_h2(__half2& b, __half2 f, __half2& v)
+{
+  const __half2 one = __float2half2_rn(1.0f), mone = __float2half2_rn(-1.0f);
+  const __half2 zero = __float2half2_rn(0.0f), c255 = __float2half2_rn(255.0f);
+  const __half2 three = __float2half2_rn(3.0f);
+  const __half2 l1024 = __float2half2_rn(1024.0f), l1025 = __float2half2_rn(1025.0f);
+  b = __hadd2(b, __hmax2(__hmin2(__hsub2(f, b), one), mone));          // bkg one step toward fr
+  const __half2 d = __habs2(__hsub2(f, b));                           // |bkg - fr|
+  const __half2 m = __hmin2(__hmul2(d, three), c255);                 // adds(adds(d,d),d)
+  const __half2 nz = __hmin2(d, one);                                 // d != 0
+  v = __hfma2(nz, __hmax2(__hmin2(__hsub2(m, v), one), mone), v);     // var one step toward m
+  return __hmax2(__hmin2(__hadd2(__hsub2(d, v), l1025), l1025), l1024);  // 1024 + (d >= var)
 }
 
 __device__ __forceinline__ void sd_step1(uint8_t& b, uint8_t f, uint8_t& v, uint8_t& out)
@@ -91,15 +111,33 @@ __global__ void __launch_bounds__(SD_THREADS) k_sigmadelta(const sd_desc* __rest
     const uint64_t p = (t - t0) * SD_TILE + (uint64_t)threadIdx.x * SD_PIX;
     if (p >= d.npix) continue;
     if (d.vec_ok && p + SD_PIX <= d.npix) {
-      uint4 b, v;
+      // state for 16 pixels: 8 biased bkg pairs, 8 var pairs
+      __half2 b[8], v[8];
       if (init) {
-        b = __ldcs(reinterpret_cast<const uint4*>(d.frames + p));
-        v = make_uint4(0x01010101u, 0x01010101u, 0x01010101u, 0x01010101u);
+        const uint4 w = __ldcs(reinterpret_cast<const uint4*>(d.frames + p));
+        unpack_bytes(w.x, b[0], b[1]);
+        unpack_bytes(w.y, b[2], b[3]);
+        unpack_bytes(w.z, b[4], b[5]);
+        unpack_bytes(w.w, b[6], b[7]);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[q] = __float2half2_rn(1.0f);
       } else {
-        b = __ldcs(reinterpret_cast<const uint4*>(d.bkg + p));
-        v = __ldcs(reinterpret_cast<const uint4*>(d.var + p));
+        const uint4 wb = __ldcs(reinterpret_cast<const uint4*>(d.bkg + p));
+        const uint4 wv = __ldcs(reinterpret_cast<const uint4*>(d.var + p));
+        unpack_bytes(wb.x, b[0], b[1]);
+        unpack_bytes(wb.y, b[2], b[3]);
+        unpack_bytes(wb.z, b[4], b[5]);
+        unpack_bytes(wb.w, b[6], b[7]);
+        const __half2 l1024 = __float2half2_rn(1024.0f);
+        unpack_bytes(wv.x, v[0], v[1]);
+        unpack_bytes(wv.y, v[2], v[3]);
+        unpack_bytes(wv.z, v[4], v[5]);
+        unpack_bytes(wv.w, v[6], v[7]);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[q] = __hsub2(v[q], l1024);
       }
       int k = first;
+#pragma unroll 1
       for (; k + 4 <= nframes; k += 4) {
         uint4 f[4];
 #pragma unroll
@@ -107,25 +145,45 @@ __global__ void __launch_bounds__(SD_THREADS) k_sigmadelta(const sd_desc* __rest
           f[q] = __ldcs(reinterpret_cast<const uint4*>(d.frames + (uint64_t)(k + q) * d.frame_stride + p));
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-          uint4 o;
-          o.x = sd_step4(b.x, f[q].x, v.x);
-          o.y = sd_step4(b.y, f[q].y, v.y);
-          o.z = sd_step4(b.z, f[q].z, v.z);
-          o.w = sd_step4(b.w, f[q].w, v.w);
-          __stcs(reinterpret_cast<uint4*>(d.labels + (uint64_t)(k + q - first) * d.label_stride + p), o);
+          const uint32_t fw[4] = {f[q].x, f[q].y, f[q].z, f[q].w};
+          uint32_t ow[4];
+#pragma unroll
+          for (int w = 0; w < 4; ++w) {
+            __half2 flo, fhi;
+            unpack_bytes(fw[w], flo, fhi);
+            const __half2 llo = sd_step_h2(b[2 * w], flo, v[2 * w]);
+            const __half2 lhi = sd_step_h2(b[2 * w + 1], fhi, v[2 * w + 1]);
+            ow[w] = pack_bytes(llo, lhi);
+          }
+          __stcs(reinterpret_cast<uint4*>(d.labels + (uint64_t)(k + q - first) * d.label_stride + p),
+                 make_uint4(ow[0], ow[1], ow[2], ow[3]));
         }
       }
+#pragma unroll 1
       for (; k < nframes; ++k) {
-        uint4 f = __ldcs(reinterpret_cast<const uint4*>(d.frames + (uint64_t)k * d.frame_stride + p));
-        uint4 o;
-        o.x = sd_step4(b.x, f.x, v.x);
-        o.y = sd_step4(b.y, f.y, v.y);
-        o.z = sd_step4(b.z, f.z, v.z);
-        o.w = sd_step4(b.w, f.w, v.w);
-        __stcs(reinterpret_cast<uint4*>(d.labels + (uint64_t)(k - first) * d.label_stride + p), o);
+        const uint4 fq = __ldcs(reinterpret_cast<const uint4*>(d.frames + (uint64_t)k * d.frame_stride + p));
+        const uint32_t fw[4] = {fq.x, fq.y, fq.z, fq.w};
+        uint32_t ow[4];
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+          __half2 flo, fhi;
+          unpack_bytes(fw[w], flo, fhi);
+          const __half2 llo = sd_step_h2(b[2 * w], flo, v[2 * w]);
+          const __half2 lhi = sd_step_h2(b[2 * w + 1], fhi, v[2 * w + 1]);
+          ow[w] = pack_bytes(llo, lhi);
+        }
+        __stcs(reinterpret_cast<uint4*>(d.labels + (uint64_t)(k - first) * d.label_stride + p),
+               make_uint4(ow[0], ow[1], ow[2], ow[3]));
       }
-      __stcs(reinterpret_cast<uint4*>(d.bkg + p), b);
-      __stcs(reinterpret_cast<uint4*>(d.var + p), v);
+      const __half2 l1024 = __float2half2_rn(1024.0f);
+      uint32_t bw[4], vw[4];
+#pragma unroll
+      for (int w = 0; w < 4; ++w) {
+        bw[w] = pack_bytes(b[2 * w], b[2 * w + 1]);
+        vw[w] = pack_bytes(__hadd2(v[2 * w], l1024), __hadd2(v[2 * w + 1], l1024));
+      }
+      __stcs(reinterpret_cast<uint4*>(d.bkg + p), make_uint4(bw[0], bw[1], bw[2], bw[3]));
+      __stcs(reinterpret_cast<uint4*>(d.var + p), make_uint4(vw[0], vw[1], vw[2], vw[3]));
     } else {
       const uint64_t end = (p + SD_PIX < d.npix) ? p + SD_PIX : d.npix;
       for (uint64_t q = p; q < end; ++q) {

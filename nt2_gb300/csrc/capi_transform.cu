@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <mutex>
+#include <stdlib.h>
+#include <string.h>
 #include <vector>
 #include "internal.cuh"
 #include "nt2cuda/blackscholes.cuh"
@@ -76,7 +78,7 @@ template <bool F> nt2cuda_status bs_demo_impl(const float* S, const float* X, co
 
 template <class T> bool aligned16(const T* p) { return ((uintptr_t)p & 15u) == 0; }
 
-template <class T, int CDF, bool F>
+template <class T, int CDF, int P>
 nt2cuda_status bs_launch(const T* S, const T* K, const T* Tm, T r, T v, T* call, T* put, size_t n,
                          cudaStream_t s, int unroll, int waves)
 {
@@ -84,36 +86,50 @@ nt2cuda_status bs_launch(const T* S, const T* K, const T* Tm, T r, T v, T* call,
   size_t nn = n;
   void* args[] = {(void*)&S, (void*)&K, (void*)&Tm, (void*)&r, (void*)&v, (void*)&call, (void*)&put, (void*)&nn};
   if (!(aligned16(S) && aligned16(K) && aligned16(Tm) && aligned16(call) && aligned16(put)))
-    return launch_status(launch_persistent(k_blackscholes_scalar<T, CDF, F>, n, 256, waves, s, args));
+    return launch_status(launch_persistent(k_blackscholes_scalar<T, CDF, P>, n, 256, waves, s, args));
   constexpr int V = 16 / (int)sizeof(T);
   size_t groups = n / V;
   switch (unroll) {
-    case 1: return launch_status(launch_persistent(k_blackscholes<T, CDF, F, 1>, groups, 256, waves, s, args));
-    case 4: return launch_status(launch_persistent(k_blackscholes<T, CDF, F, 4>, groups, 256, waves, s, args));
-    default: return launch_status(launch_persistent(k_blackscholes<T, CDF, F, 2>, groups, 256, waves, s, args));
+    case 1: return launch_status(launch_persistent(k_blackscholes<T, CDF, P, 1>, groups, 256, waves, s, args));
+    case 4: return launch_status(launch_persistent(k_blackscholes<T, CDF, P, 4>, groups, 256, waves, s, args));
+    default: return launch_status(launch_persistent(k_blackscholes<T, CDF, P, 2>, groups, 256, waves, s, args));
+  }
+}
+
+template <class T, int CDF>
+nt2cuda_status bs_prec(const T* S, const T* K, const T* Tm, T r, T v, T* call, T* put, size_t n, int prec,
+                       cudaStream_t s, int unroll, int waves)
+{
+  switch (prec) {
+    case PREC_EXACT: return bs_launch<T, CDF, PREC_EXACT>(S, K, Tm, r, v, call, put, n, s, unroll, waves);
+    case PREC_FUSED: return bs_launch<T, CDF, PREC_FUSED>(S, K, Tm, r, v, call, put, n, s, unroll, waves);
+    case PREC_FAST:
+      if constexpr (sizeof(T) == 4) return bs_launch<T, CDF, PREC_FAST>(S, K, Tm, r, v, call, put, n, s, unroll, waves);
+      else return NT2CUDA_ERR_ARG;
+    default: return NT2CUDA_ERR_ARG;
   }
 }
 
 template <class T>
 nt2cuda_status bs_dispatch(const T* S, const T* K, const T* Tm, T r, T v, T* call, T* put, size_t n,
-                           int cdf, int fused, cudaStream_t s, int unroll, int waves)
+                           int cdf, int prec, cudaStream_t s, int unroll, int waves)
 {
   if (n && (!S || !K || !Tm || !call || !put)) return NT2CUDA_ERR_ARG;
   if (cdf != CDF_NORMCDF && cdf != CDF_FASTNORMCDF) return NT2CUDA_ERR_ARG;
   if constexpr (sizeof(T) == 8) {
     if (cdf != CDF_NORMCDF) return NT2CUDA_ERR_ARG;
-    return fused ? bs_launch<T, CDF_NORMCDF, true>(S, K, Tm, r, v, call, put, n, s, unroll, waves)
-                 : bs_launch<T, CDF_NORMCDF, false>(S, K, Tm, r, v, call, put, n, s, unroll, waves);
+    return bs_prec<T, CDF_NORMCDF>(S, K, Tm, r, v, call, put, n, prec, s, unroll, waves);
   } else {
-    if (cdf == CDF_FASTNORMCDF)
-      return fused ? bs_launch<T, CDF_FASTNORMCDF, true>(S, K, Tm, r, v, call, put, n, s, unroll, waves)
-                   : bs_launch<T, CDF_FASTNORMCDF, false>(S, K, Tm, r, v, call, put, n, s, unroll, waves);
-    return fused ? bs_launch<T, CDF_NORMCDF, true>(S, K, Tm, r, v, call, put, n, s, unroll, waves)
-                 : bs_launch<T, CDF_NORMCDF, false>(S, K, Tm, r, v, call, put, n, s, unroll, waves);
+    if (cdf == CDF_FASTNORMCDF) return bs_prec<T, CDF_FASTNORMCDF>(S, K, Tm, r, v, call, put, n, prec, s, unroll, waves);
+    return bs_prec<T, CDF_NORMCDF>(S, K, Tm, r, v, call, put, n, prec, s, unroll, waves);
   }
 }
 
-const char* bs_key(size_t bytes) { return bytes == 4 ? "bs_f32" : "bs_f64"; }
+const char* bs_key(size_t bytes, int prec = 0)
+{
+  if (bytes != 4) return prec == PREC_FUSED ? "bs_f64_fused" : "bs_f64";
+  return prec == PREC_FAST ? "bs_f32_fast" : (prec == PREC_FUSED ? "bs_f32_fused" : "bs_f32");
+}
 
 // ---------------------------------------------- host-buffer pipeline state
 struct host_pipeline {
@@ -172,7 +188,7 @@ nt2cuda_status nt2cuda_blackscholes_f32(const float* S, const float* K, const fl
                                         float* call, float* put, size_t n, int cdf_kind, int fused,
                                         nt2cuda_stream s)
 {
-  tuning::params p = tuning::lookup(bs_key(4), n);
+  tuning::params p = tuning::lookup(bs_key(4, fused), n);
   return bs_dispatch<float>(S, K, T, r, sigma, call, put, n, cdf_kind, fused, as_stream(s), p.unroll, p.waves);
 }
 
@@ -180,10 +196,42 @@ nt2cuda_status nt2cuda_blackscholes_f64(const double* S, const double* K, const 
                                         double sigma, double* call, double* put, size_t n, int fused,
                                         nt2cuda_stream s)
 {
-  tuning::params p = tuning::lookup(bs_key(8), n);
+  tuning::params p = tuning::lookup(bs_key(8, fused), n);
   return bs_dispatch<double>(S, K, T, r, sigma, call, put, n, CDF_NORMCDF, fused, as_stream(s), p.unroll,
                              p.waves);
 }
+
+}  // extern "C"
+
+namespace {
+
+// Device-side address of a pinned (page-locked, mapped) host buffer, or null.
+template <class T> T* mapped_ptr(T* p)
+{
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+  if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr || a.hostPointer == nullptr) return nullptr;
+  return (T*)((char*)a.devicePointer + ((const char*)p - (const char*)a.hostPointer));
+}
+
+// Which host path to take: 0 = automatic (mapped when every table is pinned),
+// 1 = always staged copies, 2 = mapped whenever possible.  Read once from
+// NT2CUDA_HOST_PATH ("auto", "staged", "mapped").
+int host_path_policy()
+{
+  static int policy = [] {
+    const char* e = getenv("NT2CUDA_HOST_PATH");
+    if (!e) return 0;
+    if (!strcmp(e, "staged")) return 1;
+    if (!strcmp(e, "mapped")) return 2;
+    return 0;
+  }();
+  return policy;
+}
+
+}  // namespace
+
+extern "C" {
 
 nt2cuda_status nt2cuda_blackscholes_f32_host(const float* S, const float* K, const float* T, float r,
                                              float sigma, float* call, float* put, size_t n, int cdf_kind,
@@ -195,6 +243,25 @@ nt2cuda_status nt2cuda_blackscholes_f32_host(const float* S, const float* K, con
   std::lock_guard<std::mutex> g(P.m);
   int dev = 0;
   cudaGetDevice(&dev);
+  const int policy = host_path_policy();
+  // Mapped path: pinned host tables are read and written by the kernel in place over
+  // NVLink-C2C (no staging copies, no HBM round trip).
+  const float *mS = nullptr, *mK = nullptr, *mT = nullptr;
+  float *mc = nullptr, *mp = nullptr;
+  if (policy != 1) {
+    mS = mapped_ptr(S); mK = mapped_ptr(K); mT = mapped_ptr(T); mc = mapped_ptr(call); mp = mapped_ptr(put);
+  }
+  if (mS && mK && mT && mc && mp) {
+    if (!P.st[0]) {
+      cudaError_t e = cudaStreamCreateWithFlags(&P.st[0], cudaStreamNonBlocking);
+      if (e != cudaSuccess) return from_cuda(e);
+    }
+    tuning::params tp = tuning::lookup(fused == PREC_FAST ? "bs_f32_fast_mapped" : "bs_f32_mapped", n);
+    nt2cuda_status rs = bs_dispatch<float>(mS, mK, mT, r, sigma, mc, mp, n, cdf_kind, fused, P.st[0], tp.unroll,
+                                           tp.waves);
+    if (rs != NT2CUDA_OK) return rs;
+    return from_cuda(cudaStreamSynchronize(P.st[0]));
+  }
   const size_t chunk = (size_t)1 << 21;   // options per pipeline stage (8 MiB per table)
   if (P.dev != dev || P.chunk < chunk) {
     for (int i = 0; i < host_pipeline::NS; ++i) {
@@ -215,7 +282,7 @@ nt2cuda_status nt2cuda_blackscholes_f32_host(const float* S, const float* K, con
     P.chunk = chunk;
     P.dev = dev;
   }
-  tuning::params tp = tuning::lookup(bs_key(4), chunk);
+  tuning::params tp = tuning::lookup(bs_key(4, fused), chunk);
   size_t nchunks = (n + chunk - 1) / chunk;
   for (size_t c = 0; c < nchunks; ++c) {
     int i = (int)(c % host_pipeline::NS);
@@ -245,9 +312,14 @@ nt2cuda_status nt2cuda_autotune(const char* kernel, size_t n, int* best_unroll, 
 {
   if (!kernel || n == 0) return NT2CUDA_ERR_ARG;
   std::string k(kernel);
-  const bool f64 = (k == "bs_f64" || k == "saxpy_f64");
+  const bool f64 = (k == "bs_f64" || k == "bs_f64_fused" || k == "saxpy_f64");
   const size_t es = f64 ? 8 : 4;
-  if (!(k == "bs_f32" || k == "bs_f64" || k == "saxpy_f32" || k == "saxpy_f64")) return NT2CUDA_ERR_ARG;
+  int prec = PREC_EXACT;
+  if (k == "bs_f32_fused" || k == "bs_f64_fused") prec = PREC_FUSED;
+  if (k == "bs_f32_fast") prec = PREC_FAST;
+  const bool bs32 = (k == "bs_f32" || k == "bs_f32_fused" || k == "bs_f32_fast");
+  const bool bs64 = (k == "bs_f64" || k == "bs_f64_fused");
+  if (!(bs32 || bs64 || k == "saxpy_f32" || k == "saxpy_f64")) return NT2CUDA_ERR_ARG;
   void* buf[5] = {};
   for (int j = 0; j < 5; ++j) {
     cudaError_t e = cudaMalloc(&buf[j], n * es);
@@ -275,12 +347,12 @@ nt2cuda_status nt2cuda_autotune(const char* kernel, size_t n, int* best_unroll, 
   for (int ui = 0; ui < 3 && st == NT2CUDA_OK; ++ui)
     for (int wi = 0; wi < 3 && st == NT2CUDA_OK; ++wi) {
       auto once = [&]() -> nt2cuda_status {
-        if (k == "bs_f32")
+        if (bs32)
           return bs_dispatch<float>((float*)buf[0], (float*)buf[1], (float*)buf[2], 0.02f, 0.30f, (float*)buf[3],
-                                    (float*)buf[4], n, CDF_NORMCDF, 0, s, unrolls[ui], wavesv[wi]);
-        if (k == "bs_f64")
+                                    (float*)buf[4], n, CDF_NORMCDF, prec, s, unrolls[ui], wavesv[wi]);
+        if (bs64)
           return bs_dispatch<double>((double*)buf[0], (double*)buf[1], (double*)buf[2], 0.02, 0.30,
-                                     (double*)buf[3], (double*)buf[4], n, CDF_NORMCDF, 0, s, unrolls[ui],
+                                     (double*)buf[3], (double*)buf[4], n, CDF_NORMCDF, prec, s, unrolls[ui],
                                      wavesv[wi]);
         tuning::set(k.c_str(), n, tuning::params{unrolls[ui], wavesv[wi]});
         if (k == "saxpy_f32") return nt2cuda_saxpy_f32(2.5f, (float*)buf[0], (float*)buf[1], n, 0, s);

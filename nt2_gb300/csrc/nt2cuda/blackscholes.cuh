@@ -25,11 +25,36 @@
 namespace nt2cuda {
 
 enum { CDF_NORMCDF = 0, CDF_FASTNORMCDF = 1 };
+// Precision modes: 0 = NT2's arithmetic unfused (bit-exact), 1 = each NT2
+// fma/fnms/Horner step as one hardware FMA, 2 = fast (FMA, and the
+// special-function unit for exp, log, rsqrt and reciprocals; NT2's erfc and
+// fastnormcdf polynomials; float only).
+enum { PREC_EXACT = 0, PREC_FUSED = 1, PREC_FAST = 2 };
 
-template <class T, int CDF, bool F>
+template <class T, int CDF, int P>
 __device__ __forceinline__ void bs_lane(T S, T K, T Tm, T r, T v, T c, T& call, T& put)
 {
   using namespace math;
+  constexpr bool F = P != PREC_EXACT;
+  if constexpr (P == PREC_FAST && sizeof(T) == 4) {
+    // sqrt(T) = T * rsqrt(T) and the divisions by reciprocal on the special-function unit
+    const float rs = rsqrtf(Tm);
+    const float vda = __fmul_rn(v, __fmul_rn(Tm, rs));
+    const float d1 = __fdividef(__fmaf_rn(c, Tm, fast::log(__fdividef(S, K))), vda);
+    const float d2 = __fsub_rn(d1, vda);
+    const float e = __fmul_rn(K, fast::exp_small(__fmul_rn(-r, Tm)));
+    float n1, m1, n2, m2;
+    if constexpr (CDF == CDF_FASTNORMCDF) {
+      fast::fastnormcdf_pair(d1, n1, m1);
+      fast::fastnormcdf_pair(d2, n2, m2);
+    } else {
+      fast::normcdf_pair(d1, n1, m1);
+      fast::normcdf_pair(d2, n2, m2);
+    }
+    call = __fmaf_rn(-e, n2, __fmul_rn(S, n1));
+    put = __fmaf_rn(-S, m1, __fmul_rn(e, m2));
+    return;
+  }
   T da = sqrt_(Tm);
   T vda = mul(v, da);
   T d1 = div(madd<F>(c, Tm, log<F>(div(S, K))), vda);
@@ -49,17 +74,18 @@ __device__ __forceinline__ void bs_lane(T S, T K, T Tm, T r, T v, T c, T& call, 
 
 // V options per thread per group (16 bytes of each input), U groups in
 // flight per grid-stride trip.
-template <class T, int CDF, bool F, int U>
+template <class T, int CDF, int P, int U>
 __global__ void __launch_bounds__(256) k_blackscholes(const T* __restrict__ S, const T* __restrict__ K,
                                                       const T* __restrict__ Tm, T r, T v,
                                                       T* __restrict__ call, T* __restrict__ put, size_t n)
 {
   constexpr int V = 16 / (int)sizeof(T);
-  const T c = math::madd<F>(math::mul(v, v), T(0.5), r);
+  const T c = math::madd<(P != PREC_EXACT)>(math::mul(v, v), T(0.5), r);
   const size_t ngroups = n / V;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   size_t g = tid;
+#pragma unroll 1
   for (; g + (size_t)(U - 1) * stride < ngroups; g += (size_t)U * stride) {
     T s[U][V], k[U][V], t[U][V];
 #pragma unroll
@@ -73,12 +99,13 @@ __global__ void __launch_bounds__(256) k_blackscholes(const T* __restrict__ S, c
     for (int u = 0; u < U; ++u) {
       T oc[V], op[V];
 #pragma unroll
-      for (int l = 0; l < V; ++l) bs_lane<T, CDF, F>(s[u][l], k[u][l], t[u][l], r, v, c, oc[l], op[l]);
+      for (int l = 0; l < V; ++l) bs_lane<T, CDF, P>(s[u][l], k[u][l], t[u][l], r, v, c, oc[l], op[l]);
       size_t i = (g + (size_t)u * stride) * V;
       mem::store_vec<T, V>(call, i, oc);
       mem::store_vec<T, V>(put, i, op);
     }
   }
+#pragma unroll 1
   for (; g < ngroups; g += stride) {
     T s[V], k[V], t[V], oc[V], op[V];
     size_t i = g * V;
@@ -86,25 +113,25 @@ __global__ void __launch_bounds__(256) k_blackscholes(const T* __restrict__ S, c
     mem::load_vec<T, V, true>(K, i, k);
     mem::load_vec<T, V, true>(Tm, i, t);
 #pragma unroll
-    for (int l = 0; l < V; ++l) bs_lane<T, CDF, F>(s[l], k[l], t[l], r, v, c, oc[l], op[l]);
+    for (int l = 0; l < V; ++l) bs_lane<T, CDF, P>(s[l], k[l], t[l], r, v, c, oc[l], op[l]);
     mem::store_vec<T, V>(call, i, oc);
     mem::store_vec<T, V>(put, i, op);
   }
   const size_t tail0 = ngroups * V;
   if (tid < n - tail0) {
     size_t i = tail0 + tid;
-    bs_lane<T, CDF, F>(S[i], K[i], Tm[i], r, v, c, call[i], put[i]);
+    bs_lane<T, CDF, P>(S[i], K[i], Tm[i], r, v, c, call[i], put[i]);
   }
 }
 
 // Misaligned tables: one option per thread per trip.
-template <class T, int CDF, bool F>
+template <class T, int CDF, int P>
 __global__ void __launch_bounds__(256) k_blackscholes_scalar(const T* S, const T* K, const T* Tm, T r, T v,
                                                              T* call, T* put, size_t n)
 {
-  const T c = math::madd<F>(math::mul(v, v), T(0.5), r);
+  const T c = math::madd<(P != PREC_EXACT)>(math::mul(v, v), T(0.5), r);
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    bs_lane<T, CDF, F>(S[i], K[i], Tm[i], r, v, c, call[i], put[i]);
+    bs_lane<T, CDF, P>(S[i], K[i], Tm[i], r, v, c, call[i], put[i]);
 }
 
 }  // namespace nt2cuda

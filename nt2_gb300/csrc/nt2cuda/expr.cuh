@@ -301,13 +301,18 @@ template <class T, class E, class... As, int V> struct pregs<prog<assign<T, E>, 
 // assigns of a group are loaded before any of its outputs is stored, which
 // is NT2's order for tie() statements.  The n % V tail is done one element
 // per thread by the first threads of the grid.
+// Unrolled variants ask the compiler for enough resident blocks that the
+// extra groups in flight are not paid for with occupancy.
+template <int U> struct transform_min_blocks { static constexpr int value = U == 1 ? 1 : (U == 2 ? 4 : 3); };
+
 template <bool F, int V, int U, class P>
-__global__ void __launch_bounds__(256) k_transform(P p, size_t n)
+__global__ void __launch_bounds__(256, transform_min_blocks<U>::value) k_transform(P p, size_t n)
 {
   const size_t ngroups = n / V;
   const size_t T = (size_t)gridDim.x * blockDim.x;
   const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   size_t g = tid;
+#pragma unroll 1
   for (; g + (size_t)(U - 1) * T < ngroups; g += (size_t)U * T) {
     pregs<P, V> r[U];
 #pragma unroll
@@ -315,6 +320,7 @@ __global__ void __launch_bounds__(256) k_transform(P p, size_t n)
 #pragma unroll
     for (int u = 0; u < U; ++u) r[u].template compute_store<F>(p, (g + (size_t)u * T) * V);
   }
+#pragma unroll 1
   for (; g < ngroups; g += T) {
     pregs<P, V> r;
     r.template load<true>(p, g * V);

@@ -310,3 +310,108 @@ __device__ __forceinline__ void normcdf_pair(double a0, double& pos, double& neg
 
 }  // namespace math
 }  // namespace nt2cuda
+
+// ---------------------------------------------------------------------------
+// Fast variants (precision mode 2): NT2's reductions and polynomials with
+// hardware FMA, the GB300 special-function unit for 2^x and log2 x (PTX
+// ex2.approx / lg2.approx), and the reciprocal-based division where the
+// divisor is known to lie in [1, 12].  Their distance to the exact NT2 forms and
+// to FP64 is measured by the parity tests; they are not bit-exact.
+namespace nt2cuda {
+namespace math {
+namespace fast {
+
+__device__ __forceinline__ float ex2(float x)
+{
+  float r;
+  asm("ex2.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ float lg2(float x)
+{
+  float r;
+  asm("lg2.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// exp(x): NT2's Cody-Waite reduction x = k*ln2 + f (FMA form), then 2^(f*log2e)
+// on the special-function unit and the exponent scale by integer add; the
+// reduced argument keeps ex2.approx's error at a few ulp over the whole range.
+__device__ __forceinline__ float exp(float a0)
+{
+  const float k = rintf(__fmul_rn(fbits(cf::invlog_2), a0));
+  float f = __fmaf_rn(-k, fbits(cf::log_2hi), a0);
+  f = __fmaf_rn(-k, fbits(cf::log_2lo), f);
+  const float p = ex2(__fmul_rn(f, fbits(cf::invlog_2)));
+  const int ik = (int)k;
+  // 2^k in two halves so that k down to -149 and up to 127 scale exactly
+  const float s1 = __int_as_float((unsigned)((ik >> 1) + 127) << 23);
+  const float s2 = __int_as_float((unsigned)((ik - (ik >> 1)) + 127) << 23);
+  float r = __fmul_rn(__fmul_rn(p, s1), s2);
+  r = (a0 <= fbits(cf::minlog)) ? 0.0f : r;
+  r = (a0 >= fbits(cf::maxlog)) ? __int_as_float(0x7f800000) : r;
+  return (a0 != a0) ? a0 : r;
+}
+
+// exp(x) for moderate |x| (exp(-r*T), exp(-x^2) inside erfc): 2^(x*log2e) on
+// the special-function unit; the rounding of x*log2e adds |x|*2^-24*log2e of
+// relative error (about 1e-6 at |x| = 10, where exp(-x) is 4.5e-5).
+__device__ __forceinline__ float exp_small(float x)
+{
+  return ex2(__fmul_rn(x, 1.4426950408889634f));
+}
+
+// log(x) = log2(x) * ln2 on the special-function unit (absolute error of a few
+// 1e-8 near 1, relative error of a few ulp elsewhere); NT2's special values.
+__device__ __forceinline__ float log(float a0)
+{
+  float r = __fmul_rn(lg2(a0), 0.69314718055994530942f);
+  r = (a0 < 0.0f || a0 != a0) ? __int_as_float(0x7fffffff) : r;
+  r = (a0 == __int_as_float(0x7f800000)) ? a0 : r;
+  return (a0 == 0.0f) ? __int_as_float(0xff800000) : r;
+}
+
+// erfc(|a|) with NT2's two polynomials (erf_kernel.hpp:48-85) in FMA form;
+// x/(1+x) by reciprocal (1+x >= 1).
+__device__ __forceinline__ float erfc_abs(float x)
+{
+  constexpr uint32_t P2[11] = {0xc0283611u, 0x40d67e3bu, 0xc0cd1a85u, 0x4050b063u,
+                               0xbfaea865u, 0x3e2006f0u, 0x3e1175c7u, 0x3ec4ca6eu,
+                               0x3e243828u, 0xbf918a62u, 0x3f0a0e8bu};
+  constexpr uint32_t P3[9] = {0x41aa8e55u, 0x401b5680u, 0xc010d956u, 0x3f2cff3bu,
+                              0xc016c985u, 0xbffc9284u, 0xbfa11698u, 0xbe036d7eu, 0x3f7ffffeu};
+  const float z = __fdividef(x, __fadd_rn(1.0f, x));
+  float r1;
+  if (x < fbits(cf::twothird)) {
+    r1 = __fmul_rn(__fsub_rn(1.0f, z), horner<true>(z, P3));
+  } else {
+    r1 = __fmul_rn(exp_small(-__fmul_rn(x, x)), horner<true>(__fsub_rn(z, 0.4f), P2));
+  }
+  return (x == __int_as_float(0x7f800000)) ? 0.0f : r1;
+}
+
+__device__ __forceinline__ void normcdf_pair(float a0, float& pos, float& neg)
+{
+  const float y = __fmul_rn(-fbits(cf::sqrt_2o_2), a0);
+  const float r1 = erfc_abs(fabsf(y));
+  const float two_m = __fsub_rn(2.0f, r1);
+  pos = __fmul_rn(0.5f, (y < 0.0f) ? two_m : r1);
+  neg = __fmul_rn(0.5f, (-y < 0.0f) ? two_m : r1);
+}
+
+__device__ __forceinline__ void fastnormcdf_pair(float a0, float& pos, float& neg)
+{
+  constexpr uint32_t P[5] = {0x3faa466fu, 0xbfe91eeau, 0x3fe40778u, 0xbeb68f87u, 0x3ea385fau};
+  const float l = fabsf(a0);
+  const float k = __fdividef(1.0f, __fmaf_rn(0.2316419f, l, 1.0f));
+  float w = horner<true>(k, P);
+  w = __fmul_rn(w, __fmul_rn(__fmul_rn(k, fbits(cf::invsqrt_2pi)), exp_small(__fmul_rn(-__fmul_rn(l, l), 0.5f))));
+  const float om = __fsub_rn(1.0f, w);
+  pos = (a0 > 0.0f) ? om : w;
+  neg = (-a0 > 0.0f) ? om : w;
+}
+
+}  // namespace fast
+}  // namespace math
+}  // namespace nt2cuda

@@ -55,7 +55,7 @@ struct req_desc {
 // work-list; tile_start[i] is the first tile of request i.  The per-option
 // arithmetic is bs_lane, the same function the single-request kernel uses,
 // so a request's results do not depend on what it was batched with.
-template <int CDF, bool F>
+template <int CDF, int P>
 __global__ void __launch_bounds__(256) k_bs_batch(const req_desc* __restrict__ desc,
                                                   const uint64_t* __restrict__ tile_start, int nreq)
 {
@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(256) k_bs_batch(const req_desc* __restrict__ d
     const req_desc d = desc[ri];
     const uint64_t t0 = tile_start[ri];
     __syncthreads();
-    const float c = math::madd<F>(math::mul(d.sigma, d.sigma), 0.5f, d.r);
+    const float c = math::madd<(P != PREC_EXACT)>(math::mul(d.sigma, d.sigma), 0.5f, d.r);
     const uint64_t base = (t - t0) * BS_TILE;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
@@ -87,13 +87,13 @@ __global__ void __launch_bounds__(256) k_bs_batch(const req_desc* __restrict__ d
         mem::load_vec<float, 4, true>(d.K, i, k);
         mem::load_vec<float, 4, true>(d.T, i, tt);
 #pragma unroll
-        for (int l = 0; l < 4; ++l) bs_lane<float, CDF, F>(s[l], k[l], tt[l], d.r, d.sigma, c, oc[l], op[l]);
+        for (int l = 0; l < 4; ++l) bs_lane<float, CDF, P>(s[l], k[l], tt[l], d.r, d.sigma, c, oc[l], op[l]);
         mem::store_vec<float, 4>(d.call, i, oc);
         mem::store_vec<float, 4>(d.put, i, op);
       } else {
         const uint64_t e = (i + 4 < d.n) ? i + 4 : d.n;
         for (uint64_t q = i; q < e; ++q)
-          bs_lane<float, CDF, F>(d.S[q], d.K[q], d.T[q], d.r, d.sigma, c, d.call[q], d.put[q]);
+          bs_lane<float, CDF, P>(d.S[q], d.K[q], d.T[q], d.r, d.sigma, c, d.call[q], d.put[q]);
       }
     }
   }
@@ -157,12 +157,19 @@ struct request {
 
 struct batch;
 
+// One launch slot: a stream, an event, and the work-list of the batch it
+// carries (descriptors then tile starts, in one pinned buffer copied to the
+// device in one transfer).
 struct slot {
   cudaStream_t stream = nullptr;
-  req_desc* h_desc = nullptr;     // pinned
-  uint64_t* h_tiles = nullptr;    // pinned
+  cudaEvent_t done = nullptr;
+  char* h_buf = nullptr;          // pinned
+  char* d_buf = nullptr;
+  req_desc* h_desc = nullptr;
+  uint64_t* h_tiles = nullptr;
   req_desc* d_desc = nullptr;
   uint64_t* d_tiles = nullptr;
+  size_t bytes = 0;
   bool busy = false;
 };
 
@@ -183,6 +190,9 @@ struct nt2cuda_server {
   size_t reserved = 0;
   bool stop = false;
   std::thread worker;
+  std::thread reaper;
+  std::deque<struct batch*> inflight;   // launched batches, in launch order
+  std::condition_variable cv_inflight;  // reaper: a batch was launched or stop
   nt2cuda_server_stats st{};
   nt2cuda_status worker_error = NT2CUDA_OK;
 };
@@ -213,10 +223,10 @@ void admit_locked(nt2cuda_server* s)
   }
 }
 
-void CUDART_CB on_batch_done(void* p)
+// Completion: the reaper waits for each launched batch's event in launch
+// order, stamps its requests done and frees its slot.
+void complete_batch(nt2cuda_server* s, batch* b, cudaError_t err)
 {
-  batch* b = (batch*)p;
-  nt2cuda_server* s = b->srv;
   uint64_t t = now_ns();
   {
     std::lock_guard<std::mutex> g(s->m);
@@ -227,6 +237,7 @@ void CUDART_CB on_batch_done(void* p)
       it->second.t_done = t;
       s->st.completed++;
     }
+    if (err != cudaSuccess && s->worker_error == NT2CUDA_OK) s->worker_error = from_cuda(err, NT2CUDA_ERR_LAUNCH);
     s->slots[(size_t)b->slot].busy = false;
   }
   s->cv_done.notify_all();
@@ -234,20 +245,36 @@ void CUDART_CB on_batch_done(void* p)
   delete b;
 }
 
-template <int CDF, bool F>
+void reaper_loop(nt2cuda_server* s)
+{
+  cudaSetDevice(s->device);
+  for (;;) {
+    batch* b = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(s->m);
+      s->cv_inflight.wait(lk, [&] { return s->stop || !s->inflight.empty(); });
+      if (s->inflight.empty()) return;   // stop requested and nothing left
+      b = s->inflight.front();
+      s->inflight.pop_front();
+    }
+    cudaError_t e = cudaEventSynchronize(s->slots[(size_t)b->slot].done);
+    complete_batch(s, b, e);
+  }
+}
+
+template <int CDF, int P>
 nt2cuda_status launch_batch(nt2cuda_server* s, slot& sl, int nreq)
 {
-  cudaError_t e = cudaMemcpyAsync(sl.d_desc, sl.h_desc, (size_t)nreq * sizeof(req_desc), cudaMemcpyHostToDevice,
-                                  sl.stream);
-  if (e != cudaSuccess) return from_cuda(e);
-  e = cudaMemcpyAsync(sl.d_tiles, sl.h_tiles, ((size_t)nreq + 1) * 8, cudaMemcpyHostToDevice, sl.stream);
+  // descriptors [0, nreq) and tile starts [0, nreq] sit at fixed offsets of one buffer
+  const size_t used = (size_t)((char*)(sl.h_tiles + nreq + 1) - sl.h_buf);
+  cudaError_t e = cudaMemcpyAsync(sl.d_buf, sl.h_buf, used, cudaMemcpyHostToDevice, sl.stream);
   if (e != cudaSuccess) return from_cuda(e);
   uint64_t tiles = sl.h_tiles[nreq];
-  int per_sm = resident_blocks(k_bs_batch<CDF, F>, 256);
+  int per_sm = resident_blocks(k_bs_batch<CDF, P>, 256);
   uint64_t grid = (uint64_t)sm_count() * (uint64_t)per_sm;
   if (grid > tiles) grid = tiles;
   if (grid < 1) grid = 1;
-  k_bs_batch<CDF, F><<<(unsigned)grid, 256, 0, sl.stream>>>(sl.d_desc, sl.d_tiles, nreq);
+  k_bs_batch<CDF, P><<<(unsigned)grid, 256, 0, sl.stream>>>(sl.d_desc, sl.d_tiles, nreq);
   (void)s;
   return launch_status(cudaSuccess);
 }
@@ -296,11 +323,15 @@ void worker_loop(nt2cuda_server* s)
 
     nt2cuda_status rs = NT2CUDA_OK;
     if (s->cfg.coalesce) {
-      const bool F = s->cfg.fused != 0;
+      const int P = s->cfg.fused;
       if (s->cfg.cdf_kind == CDF_FASTNORMCDF)
-        rs = F ? launch_batch<CDF_FASTNORMCDF, true>(s, sl, nreq) : launch_batch<CDF_FASTNORMCDF, false>(s, sl, nreq);
+        rs = P == PREC_FAST ? launch_batch<CDF_FASTNORMCDF, PREC_FAST>(s, sl, nreq)
+           : P == PREC_FUSED ? launch_batch<CDF_FASTNORMCDF, PREC_FUSED>(s, sl, nreq)
+                             : launch_batch<CDF_FASTNORMCDF, PREC_EXACT>(s, sl, nreq);
       else
-        rs = F ? launch_batch<CDF_NORMCDF, true>(s, sl, nreq) : launch_batch<CDF_NORMCDF, false>(s, sl, nreq);
+        rs = P == PREC_FAST ? launch_batch<CDF_NORMCDF, PREC_FAST>(s, sl, nreq)
+           : P == PREC_FUSED ? launch_batch<CDF_NORMCDF, PREC_FUSED>(s, sl, nreq)
+                             : launch_batch<CDF_NORMCDF, PREC_EXACT>(s, sl, nreq);
       lk.lock();
       s->st.launches++;
       lk.unlock();
@@ -310,7 +341,7 @@ void worker_loop(nt2cuda_server* s)
       s->st.launches += (uint64_t)nreq;
       lk.unlock();
     }
-    if (rs == NT2CUDA_OK) rs = from_cuda(cudaLaunchHostFunc(sl.stream, on_batch_done, b));
+    if (rs == NT2CUDA_OK) rs = from_cuda(cudaEventRecord(sl.done, sl.stream));
     if (rs != NT2CUDA_OK) {
       lk.lock();
       s->worker_error = rs;
@@ -319,7 +350,12 @@ void worker_loop(nt2cuda_server* s)
       lk.unlock();
       s->cv_done.notify_all();
       delete b;
+      continue;
     }
+    lk.lock();
+    s->inflight.push_back(b);
+    lk.unlock();
+    s->cv_inflight.notify_one();
   }
 }
 
@@ -348,7 +384,7 @@ nt2cuda_status nt2cuda_server_create(const nt2cuda_server_config* cfg, nt2cuda_s
   *out = nullptr;
   if (cfg->budget_bytes < 4096 || cfg->max_inflight_batches < 1 || cfg->max_inflight_batches > 16 ||
       cfg->max_batch_requests < 1 || cfg->max_batch_requests > (1 << 20) ||
-      (cfg->cdf_kind != CDF_NORMCDF && cfg->cdf_kind != CDF_FASTNORMCDF))
+      (cfg->cdf_kind != CDF_NORMCDF && cfg->cdf_kind != CDF_FASTNORMCDF) || cfg->fused < 0 || cfg->fused > 2)
     return NT2CUDA_ERR_ARG;
   nt2cuda_server* s = new nt2cuda_server();
   s->cfg = *cfg;
@@ -357,15 +393,22 @@ nt2cuda_status nt2cuda_server_create(const nt2cuda_server_config* cfg, nt2cuda_s
   if (!s->mem.init(cfg->budget_bytes)) { delete s; return NT2CUDA_ERR_OOM; }
   s->slots.resize((size_t)cfg->max_inflight_batches);
   const int maxb = cfg->coalesce ? cfg->max_batch_requests : 1;
+  const size_t desc_bytes = ((size_t)maxb * sizeof(req_desc) + 255) / 256 * 256;
+  const size_t slot_bytes = desc_bytes + ((size_t)maxb + 1) * 8;
   for (slot& sl : s->slots) {
     bool ok = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) == cudaSuccess &&
-              cudaMallocHost(&sl.h_desc, (size_t)maxb * sizeof(req_desc)) == cudaSuccess &&
-              cudaMallocHost(&sl.h_tiles, ((size_t)maxb + 1) * 8) == cudaSuccess &&
-              cudaMalloc(&sl.d_desc, (size_t)maxb * sizeof(req_desc)) == cudaSuccess &&
-              cudaMalloc(&sl.d_tiles, ((size_t)maxb + 1) * 8) == cudaSuccess;
+              cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) == cudaSuccess &&
+              cudaMallocHost(&sl.h_buf, slot_bytes) == cudaSuccess &&
+              cudaMalloc(&sl.d_buf, slot_bytes) == cudaSuccess;
     if (!ok) { nt2cuda_server_destroy(s); return NT2CUDA_ERR_OOM; }
+    sl.bytes = slot_bytes;
+    sl.h_desc = (req_desc*)sl.h_buf;
+    sl.h_tiles = (uint64_t*)(sl.h_buf + desc_bytes);
+    sl.d_desc = (req_desc*)sl.d_buf;
+    sl.d_tiles = (uint64_t*)(sl.d_buf + desc_bytes);
   }
   s->worker = std::thread(worker_loop, s);
+  s->reaper = std::thread(reaper_loop, s);
   *out = s;
   return NT2CUDA_OK;
 }
@@ -379,13 +422,14 @@ nt2cuda_status nt2cuda_server_destroy(nt2cuda_server* s)
   }
   s->cv_work.notify_all();
   if (s->worker.joinable()) s->worker.join();
+  s->cv_inflight.notify_all();
+  if (s->reaper.joinable()) s->reaper.join();   // drains every launched batch first
   for (slot& sl : s->slots) if (sl.stream) cudaStreamSynchronize(sl.stream);
   for (slot& sl : s->slots) {
+    if (sl.done) cudaEventDestroy(sl.done);
     if (sl.stream) cudaStreamDestroy(sl.stream);
-    if (sl.h_desc) cudaFreeHost(sl.h_desc);
-    if (sl.h_tiles) cudaFreeHost(sl.h_tiles);
-    if (sl.d_desc) cudaFree(sl.d_desc);
-    if (sl.d_tiles) cudaFree(sl.d_tiles);
+    if (sl.h_buf) cudaFreeHost(sl.h_buf);
+    if (sl.d_buf) cudaFree(sl.d_buf);
   }
   delete s;
   return NT2CUDA_OK;

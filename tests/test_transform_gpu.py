@@ -161,6 +161,32 @@ def test_blackscholes_fused_within_bound(gpu, oracle):
     assert np.max(np.abs(rc - c64) / np.maximum(np.abs(c64), 1)) < 1e-4
 
 
+@pytest.mark.parametrize("cdf", ["normcdf", "fastnormcdf"])
+def test_blackscholes_fast_mode_bounds(gpu, oracle, cdf):
+    """precision="fast": stated bounds against the FP64 evaluation and the exact oracle.
+
+    Against FP64: |fast - fp64| <= 2e-5 * max(1, |fp64|) for call and put (the exact FP32
+    path's own error is of the same order).  Against the exact oracle: 99% of prices above
+    0.01 within 64 ULP (NT2 ulpdist units)."""
+    n = 1 << 20
+    S, K, T = bs_inputs(n, np.float32, seed=91)
+    c, p = gpu.blackscholes(to_dev(S), to_dev(K), to_dev(T), 0.02, 0.30, cdf=cdf, precision="fast")
+    gc, gp = host(c), host(p)
+    kind = 0 if cdf == "normcdf" else 1
+    rc, rp = oracle.bs(S, K, T, 0.02, 0.30, cdf=kind)
+    if kind == 0:
+        c64, p64 = oracle.bs(S.astype(np.float64), K.astype(np.float64), T.astype(np.float64), 0.02, 0.30)
+    else:
+        c64, p64 = rc.astype(np.float64), rp.astype(np.float64)    # fastnormcdf exists in float only
+    for got, ref32, ref64 in ((gc, rc, c64), (gp, rp, p64)):
+        err = np.abs(got.astype(np.float64) - ref64) / np.maximum(1.0, np.abs(ref64))
+        assert err.max() <= 2e-5, err.max()
+        big = np.abs(ref32) > 0.01
+        L = oracle.load()
+        u = np.array([L.nt2o_ulpdist_f(float(a), float(b)) for a, b in zip(got[big][:20000], ref32[big][:20000])])
+        assert np.percentile(u, 99) <= 64, np.percentile(u, 99)
+
+
 def test_blackscholes_demo_bit_exact(gpu, oracle):
     n = 100003
     rng = np.random.default_rng(11)
