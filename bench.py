@@ -450,32 +450,28 @@ def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: in
     def want(name):
         return only is None or only == name
 
-    flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-
-    def flushed(fn):
-        def f():
-            flush_buf.zero_()
-            fn()
-        return f
-
-    def flush_only_ms():
-        m, _, _ = time_device(lambda: flush_buf.zero_(), 50, 3, ws)
-        return m
 
     def K(default):
         return steps if steps is not None else default
 
     if want("saxpy"):
+        # four (x, y) pairs (536 MB) visited in turn: every step reads from DRAM, no flush traffic
         n = 1 << 24
-        x = torch.empty(n, device="cuda")
-        y = torch.empty(n, device="cuda")
-        api.fill_uniform(x, -1, 1, 1)
-        api.fill_uniform(y, -1, 1, 2)
+        xs = [torch.empty(n, device="cuda") for _ in range(4)]
+        ys = [torch.empty(n, device="cuda") for _ in range(4)]
+        for i in range(4):
+            api.fill_uniform(xs[i], -1, 1, 1 + i)
+            api.fill_uniform(ys[i], -1, 1, 11 + i)
         api.autotune("saxpy_f32", n)
-        fm0 = flush_only_ms()
-        ms, _, _ = time_device(flushed(lambda: api.saxpy(2.5, x, y)), K(200), warmup, ws)
-        out.append(line("saxpy f32 2^24 (L2 flushed)", ms - fm0, 12 * n, n, "elements/s"))
-        del x, y
+        it = [0]
+
+        def saxpy_step():
+            i = it[0] & 3
+            it[0] += 1
+            api.saxpy(2.5, xs[i], ys[i])
+        ms, _, _ = time_device(saxpy_step, K(200), warmup, ws)
+        out.append(line("saxpy f32 2^24 (4 rotating copies, 536 MB > L2)", ms, 12 * n, n, "elements/s"))
+        del xs, ys
     if want("sdot") or want("sdot_plain"):
         n = 1 << 26
         x = torch.empty(n, device="cuda")
@@ -494,34 +490,30 @@ def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: in
             or want("bs_exact") or want("bs_fastnormcdf") or want("sigmadelta")):
         return out
     rows, cols = 8192, 4096
-    A = torch.empty(rows * cols, device="cuda")
-    api.fill_normal(A, 3)
-    oc = torch.empty(cols, device="cuda")
-    orow = torch.empty(rows, device="cuda")
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-
-    def with_flush(fn):
-        def f():
-            flush.zero_()
-            fn()
-        return f
-
-    def flush_ms():
-        m, _, _ = time_device(lambda: flush.zero_(), 50, 3, ws)
-        return m
-
     if want("inner") or want("outer"):
-        fm = flush_ms()
+        # four 134 MB tables visited in turn (536 MB > L2): every step reads from DRAM
+        As = [torch.empty(rows * cols, device="cuda") for _ in range(4)]
+        for i in range(4):
+            api.fill_normal(As[i], 3 + i)
+        oc = torch.empty(cols, device="cuda")
+        orow = torch.empty(rows, device="cuda")
+        it = [0]
+
+        def fold_step(dim, o):
+            def f():
+                i = it[0] & 3
+                it[0] += 1
+                api.sum_colmajor(As[i], rows, cols, dim, out=o)
+            return f
         if want("inner"):
-            ms, _, _ = time_device(with_flush(lambda: api.sum_colmajor(A, rows, cols, 1, out=oc)), K(50), warmup, ws)
-            out.append(line("inner_fold column sums 8192x4096 f32 compensated (L2 flushed)", ms - fm,
+            ms, _, _ = time_device(fold_step(1, oc), K(100), warmup, ws)
+            out.append(line("inner_fold column sums 8192x4096 f32 compensated (4 rotating tables)", ms,
                             4 * rows * cols + 4 * cols, rows * cols, "elements/s"))
         if want("outer"):
-            ms, _, _ = time_device(with_flush(lambda: api.sum_colmajor(A, rows, cols, 2, out=orow)), K(50), warmup,
-                                   ws)
-            out.append(line("outer_fold row sums 8192x4096 f32 compensated (L2 flushed)", ms - fm,
+            ms, _, _ = time_device(fold_step(2, orow), K(100), warmup, ws)
+            out.append(line("outer_fold row sums 8192x4096 f32 compensated (4 rotating tables)", ms,
                             4 * rows * cols + 4 * rows, rows * cols, "elements/s"))
-    del A, flush
+        del As
     if want("bs_f64"):
         n = 1 << 24
         S = torch.empty(n, dtype=torch.float64, device="cuda")

@@ -179,6 +179,12 @@ nt2cuda_status nt2cuda_sum_outer_f32(const float* A, size_t rows, size_t cols, f
 nt2cuda_status nt2cuda_sum_outer_f64(const double* A, size_t rows, size_t cols, double* out,
                                      nt2cuda_stream stream);
 
+/* Kernel family for the folds: 0 = automatic (TMA-staged tiles for long
+ * columns, register-pipelined kernels otherwise), 1 = register-pipelined
+ * only, 2 = TMA-staged wherever the tables allow it.  Results of every family
+ * are within the same bounds; each family is bitwise reproducible.  Process-wide. */
+nt2cuda_status nt2cuda_set_fold_path(int path);
+
 /* --------------------------------------------------------- sigmadelta ---- */
 /* One grey video stream for the batched sigma-delta background subtraction
  * (demo/sigmadelta/nt2/sigmadelta_nt2.cpp:37-58, 85-106).  frames holds

@@ -90,6 +90,7 @@ _SIGS = {
     "nt2cuda_sum_inner_f64": (c_int, [c_vp, c_size, c_size, c_vp, c_vp]),
     "nt2cuda_sum_outer_f32": (c_int, [c_vp, c_size, c_size, c_vp, c_int, c_vp]),
     "nt2cuda_sum_outer_f64": (c_int, [c_vp, c_size, c_size, c_vp, c_vp]),
+    "nt2cuda_set_fold_path": (c_int, [c_int]),
     "nt2cuda_sigmadelta_batch_u8": (c_int, [C.POINTER(SdStream), c_int, c_int, c_int, c_vp]),
     "nt2cuda_sigmadelta_plan_create": (c_int, [C.POINTER(SdStream), c_int, c_int, c_int, c_vp, C.POINTER(c_vp)]),
     "nt2cuda_sigmadelta_plan_launch": (c_int, [c_vp, c_vp]),

@@ -74,4 +74,11 @@ nt2cuda_status nt2cuda_sum_outer_f64(const double* A, size_t rows, size_t cols, 
   return launch_status(nt2cuda::fold::outer_fold<false, double>(term<double>{A}, rows, cols, out, as_stream(s)));
 }
 
+nt2cuda_status nt2cuda_set_fold_path(int path)
+{
+  if (path < 0 || path > 2) return NT2CUDA_ERR_ARG;
+  nt2cuda::fold::fold_path().store(path);
+  return NT2CUDA_OK;
+}
+
 }  // extern "C"

@@ -255,10 +255,20 @@ __global__ void __launch_bounds__(256) k_outer(E e, outer_shape sh, T* __restric
       __threadfence();
       if (threadIdx.x < STRIP && row < sh.rows) {
         acc<T> c{T(0), T(0)};
-        for (size_t q = 0; q < sh.splits; ++q) {
+        size_t q = 0;
+        for (; q + 8 <= sh.splits; q += 8) {
+          acc<T> v[8];
+#pragma unroll
+          for (int k = 0; k < 8; ++k) {
+            const acc<T>* p = partials + (strip * sh.splits + q + k) * STRIP + threadIdx.x;
+            v[k] = acc<T>{__ldcg(&p->s), __ldcg(&p->c)};
+          }
+#pragma unroll
+          for (int k = 0; k < 8; ++k) c = merge<COMP>(c, v[k]);
+        }
+        for (; q < sh.splits; ++q) {
           const acc<T>* p = partials + (strip * sh.splits + q) * STRIP + threadIdx.x;
-          acc<T> v{__ldcg(&p->s), __ldcg(&p->c)};
-          c = merge<COMP>(c, v);
+          c = merge<COMP>(c, acc<T>{__ldcg(&p->s), __ldcg(&p->c)});
         }
         out[row] = result<COMP>(c);
       }

@@ -11,6 +11,10 @@
 #include "fold.cuh"
 #include "launch.cuh"
 #include "scratch.cuh"
+#include "fold_tma.cuh"
+#include <stdlib.h>
+#include <string.h>
+#include <atomic>
 
 namespace nt2cuda {
 namespace fold {
@@ -27,9 +31,45 @@ template <class E> bool expr_aligned(const E& e)
 // Segment length of one warp's share of a column: 128 vector groups per lane.
 template <class T> constexpr size_t inner_seg() { return (size_t)32 * (16 / sizeof(T)) * 128; }
 
+// Which kernels serve the folds of a table or of a product of two tables:
+//   0 (auto): TMA-staged for long columns (inner_fold, rows >= 2^16), the
+//             register-pipelined kernels otherwise;
+//   1 (simt): always the register-pipelined kernels;
+//   2 (tma):  TMA-staged wherever the tables allow it (16-byte aligned, whole
+//             vectors long; outer_fold from 256 rows).
+// The initial value comes from NT2CUDA_FOLD_PATH ("auto", "simt", "tma").
+inline std::atomic<int>& fold_path()
+{
+  static std::atomic<int> p([] {
+    const char* e = getenv("NT2CUDA_FOLD_PATH");
+    if (e && !strcmp(e, "simt")) return 1;
+    if (e && !strcmp(e, "tma")) return 2;
+    return 0;
+  }());
+  return p;
+}
+
+template <class T> struct tma_terms { static constexpr int n = 0; };
+template <class T> struct tma_terms<term<T>> { static constexpr int n = 1; };
+template <class T> struct tma_terms<node<tag::multiplies_, term<T>, term<T>>> { static constexpr int n = 2; };
+
+template <class T> inline const T* first_term(const term<T>& t) { return t.p; }
+template <class T> inline const T* first_term(const node<tag::multiplies_, term<T>, term<T>>& n) { return n.a.p; }
+template <class T> inline const T* second_term(const term<T>&) { return nullptr; }
+template <class T> inline const T* second_term(const node<tag::multiplies_, term<T>, term<T>>& n) { return n.b.p; }
+
 template <bool COMP, class T, class E>
 cudaError_t inner_fold(const E& e, size_t rows, size_t cols, T* out, cudaStream_t s)
 {
+  if constexpr (tma_terms<E>::n > 0) {
+    constexpr size_t VV = 16 / sizeof(T);
+    // auto: long columns only; a short column's tiles are too few to amortise the block barriers
+    const int path = fold_path().load(std::memory_order_relaxed);
+    const size_t min_rows = path == 2 ? 32 : ((size_t)1 << 16);
+    if (path != 1 && rows >= min_rows && cols > 0 && out && rows % VV == 0 && expr_aligned(e) &&
+        std::is_same<typename value_of<E>::type, T>::value)
+      return inner_fold_tma<COMP, T>(first_term(e), second_term(e), rows, cols, out, s);
+  }
   if (cols == 0) return cudaSuccess;
   if (!out) return cudaErrorInvalidValue;
   if (rows == 0) return (cudaMemsetAsync(out, 0, cols * sizeof(T), s));
@@ -63,13 +103,21 @@ cudaError_t inner_fold(const E& e, size_t rows, size_t cols, T* out, cudaStream_
   T* o = out;
   void* args[] = {&ec, &sh, &o, &partials, &counters};
   // launch_persistent counts threads; a unit is one warp
-  if (vec) return (launch_persistent(k_inner<COMP, VV, 4, T, E>, units * 32, 256, 4, s, args));
+  if (vec) return (launch_persistent(k_inner<COMP, VV, 8, T, E>, units * 32, 256, 4, s, args));
   return (launch_persistent(k_inner<COMP, 1, 4, T, E>, units * 32, 256, 4, s, args));
 }
 
 template <bool COMP, class T, class E>
 cudaError_t outer_fold(const E& e, size_t rows, size_t cols, T* out, cudaStream_t s)
 {
+  if constexpr (tma_terms<E>::n == 1) {
+    constexpr size_t VV = 16 / sizeof(T);
+    if (fold_path().load(std::memory_order_relaxed) == 2 && rows >= 256 && cols > 0 && out && rows % VV == 0 &&
+        expr_aligned(e) && rows < ((size_t)1 << 31) && cols < ((size_t)1 << 31)) {
+      cudaError_t r = outer_fold_tma<COMP, T>(first_term(e), rows, cols, out, s);
+      if (r != cudaErrorNotSupported) return r;
+    }
+  }
   if (rows == 0) return cudaSuccess;
   if (!out) return cudaErrorInvalidValue;
   if (cols == 0) return (cudaMemsetAsync(out, 0, rows * sizeof(T), s));
@@ -80,9 +128,16 @@ cudaError_t outer_fold(const E& e, size_t rows, size_t cols, T* out, cudaStream_
   outer_shape sh;
   sh.rows = rows;
   sh.cols = cols;
-  sh.cchunk = 256;
-  sh.splits = (cols + sh.cchunk - 1) / sh.cchunk;
   sh.strips = (rows + STRIP - 1) / STRIP;
+  // about 512 blocks in all, so the grid fits in one wave of resident blocks
+  // (the split depends only on the shape, so results stay reproducible)
+  {
+    const size_t want_splits = (512 + sh.strips - 1) / sh.strips;
+    size_t cchunk = (cols + want_splits - 1) / want_splits;
+    cchunk = (cchunk + 63) / 64 * 64;
+    sh.cchunk = cchunk < 64 ? 64 : cchunk;
+  }
+  sh.splits = (cols + sh.cchunk - 1) / sh.cchunk;
   acc<T>* partials = nullptr;
   unsigned* counters = nullptr;
   if (sh.splits > 1) {
@@ -98,7 +153,7 @@ cudaError_t outer_fold(const E& e, size_t rows, size_t cols, T* out, cudaStream_
   E ec = e;
   T* o = out;
   void* args[] = {&ec, &sh, &o, &partials, &counters};
-  if (vec) return (launch_persistent(k_outer<COMP, VV, 4, T, E>, units * 256, 256, 4, s, args));
+  if (vec) return (launch_persistent(k_outer<COMP, VV, 8, T, E>, units * 256, 256, 4, s, args));
   return (launch_persistent(k_outer<COMP, 1, 4, T, E>, units * 256, 256, 4, s, args));
 }
 

@@ -1,0 +1,432 @@
+// nt2cuda/fold_tma.cuh -- inner_fold and outer_fold with TMA-staged tiles.
+//
+// Same results contract as fold.cuh (compensated or plain accumulation,
+// partials merged in index order, decomposition fixed by the table's shape),
+// but the input tiles reach shared memory through the Tensor Memory
+// Accelerator, so each block keeps several 16 KB tiles in flight without
+// holding them in registers:
+//   inner_fold (sum(A,1), globalsum, globalsum(X*Y)): a unit is one segment of
+//     one column; its tiles are contiguous, one 1-D cp.async.bulk per term.
+//   outer_fold (sum(A,2)): a unit is a strip of 256 rows by a chunk of columns;
+//     each tile is a 256-row x 16-column box loaded through a 2-D tensor map,
+//     which also zero-fills the ragged edges of the table.
+// NT2's counterparts: modules/arch/shared_memory/include/nt2/sdk/shared_memory/worker/inner_fold.hpp:53-108
+// and .../worker/outer_fold.hpp:31-155.
+//
+// A block whose barrier wait runs out (tma::mbar_wait) writes NaN for the
+// unit it was working on, waits (bounded) for the copies it still has in
+// flight and leaves.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+#include <stdint.h>
+#include <mutex>
+#include "fold.cuh"
+#include "launch.cuh"
+#include "scratch.cuh"
+#include "tma.cuh"
+
+namespace nt2cuda {
+namespace fold {
+
+constexpr int kTmaTileBytes = 16384;
+
+template <class T> __device__ __forceinline__ T quiet_nan()
+{
+  if constexpr (sizeof(T) == 4) return __int_as_float(0x7fc00000);
+  else return __longlong_as_double(0x7ff8000000000000ll);
+}
+
+// Merge n partials p[0], p[stride], ... in index order, with 8 loads in
+// flight at a time (the merge is at the tail of the kernel, where serial L2
+// round trips would show).
+template <bool COMP, class T>
+__device__ __forceinline__ acc<T> merge_partials(const acc<T>* p, size_t n, size_t stride)
+{
+  acc<T> m{T(0), T(0)};
+  size_t q = 0;
+  for (; q + 8 <= n; q += 8) {
+    acc<T> v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const acc<T>* e = p + (q + k) * stride;
+      v[k] = acc<T>{__ldcg(&e->s), __ldcg(&e->c)};
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) m = merge<COMP>(m, v[k]);
+  }
+  for (; q < n; ++q) {
+    const acc<T>* e = p + q * stride;
+    m = merge<COMP>(m, acc<T>{__ldcg(&e->s), __ldcg(&e->c)});
+  }
+  return m;
+}
+
+// Merge v[threadIdx.x] over the block in a fixed order; thread 0 gets the result.
+template <bool COMP, class T>
+__device__ __forceinline__ acc<T> block_merge(acc<T> v, acc<T>* red)
+{
+  v = warp_merge<COMP>(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  acc<T> r = red[0];
+  if (threadIdx.x == 0)
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r = merge<COMP>(r, red[w]);
+  __syncthreads();
+  return r;
+}
+
+// ------------------------------------------------------------ inner fold
+struct inner_tma_shape {
+  size_t rows, cols, seg, splits, units;
+};
+
+template <class T> __host__ __device__ constexpr int inner_tile() { return kTmaTileBytes / (int)sizeof(T); }
+
+template <class T>
+__device__ __forceinline__ size_t inner_unit_tiles(const inner_tma_shape& sh, size_t u)
+{
+  const size_t r0 = (u % sh.splits) * sh.seg;
+  const size_t r1 = (r0 + sh.seg < sh.rows) ? r0 + sh.seg : sh.rows;
+  return (r1 - r0 + inner_tile<T>() - 1) / inner_tile<T>();
+}
+
+// NT = 1 folds x; NT = 2 folds x*y (float product rounded, as NT2's X*Y).
+template <bool COMP, class T, int NT, int STAGES>
+__global__ void __launch_bounds__(256) k_inner_tma(const T* __restrict__ x, const T* __restrict__ y,
+                                                   inner_tma_shape sh, T* __restrict__ out,
+                                                   acc<T>* __restrict__ partials, unsigned* __restrict__ counters)
+{
+  constexpr int TILE = inner_tile<T>();
+  constexpr int V = 16 / (int)sizeof(T);
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  T* buf = reinterpret_cast<T*>(smem_raw);          // [STAGES][NT][TILE]
+  __shared__ __align__(8) uint64_t bar[STAGES];
+  __shared__ acc<T> red[8];
+  __shared__ unsigned s_last;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) tma::mbar_init(&bar[s], 1);
+    tma::fence_barrier_init();
+  }
+  __syncthreads();
+
+  // producer state (thread 0): next tile to issue
+  size_t pu = blockIdx.x, pt = 0;
+  uint32_t issued = 0;
+  auto produce = [&](int s) {
+    const size_t j = pu / sh.splits, r0 = (pu % sh.splits) * sh.seg + pt * (size_t)TILE;
+    const size_t rend = ((pu % sh.splits) * sh.seg + sh.seg < sh.rows) ? (pu % sh.splits) * sh.seg + sh.seg : sh.rows;
+    const uint32_t cnt = (uint32_t)((rend - r0) < (size_t)TILE ? (rend - r0) : (size_t)TILE);
+    const uint32_t bytes = cnt * (uint32_t)sizeof(T);
+    tma::mbar_arrive_expect_tx(&bar[s], bytes * NT);
+    tma::bulk_g2s(buf + (size_t)(s * NT) * TILE, x + j * sh.rows + r0, bytes, &bar[s]);
+    if constexpr (NT == 2) tma::bulk_g2s(buf + (size_t)(s * NT + 1) * TILE, y + j * sh.rows + r0, bytes, &bar[s]);
+    ++issued;
+    if (++pt == inner_unit_tiles<T>(sh, pu)) { pt = 0; pu += gridDim.x; }
+  };
+  if (threadIdx.x == 0)
+    for (int s = 0; s < STAGES && pu < sh.units; ++s) produce(s);
+
+  size_t cu = blockIdx.x, ct = 0;
+  uint32_t iter = 0;
+  acc<T> a[V];
+#pragma unroll
+  for (int l = 0; l < V; ++l) a[l] = acc<T>{T(0), T(0)};
+  while (cu < sh.units) {
+    const int s = (int)(iter % STAGES);
+    const bool ok = tma::mbar_wait(&bar[s], (iter / STAGES) & 1u);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        out[cu / sh.splits] = quiet_nan<T>();
+        for (uint32_t k = iter; k < issued; ++k) tma::mbar_wait(&bar[k % STAGES], (k / STAGES) & 1u);
+      }
+      __syncthreads();
+      return;
+    }
+    const size_t j = cu / sh.splits;
+    const size_t seg0 = (cu % sh.splits) * sh.seg;
+    const size_t rend = (seg0 + sh.seg < sh.rows) ? seg0 + sh.seg : sh.rows;
+    const size_t r0 = seg0 + ct * (size_t)TILE;
+    const int cnt = (int)((rend - r0) < (size_t)TILE ? (rend - r0) : (size_t)TILE);
+    const T* tx = buf + (size_t)(s * NT) * TILE;
+    const T* ty = buf + (size_t)(s * NT + (NT == 2 ? 1 : 0)) * TILE;
+    for (int e = threadIdx.x * V; e < cnt; e += 256 * V) {
+      T xv[V];
+      *reinterpret_cast<uint4*>(xv) = *reinterpret_cast<const uint4*>(tx + e);
+      if constexpr (NT == 2) {
+        T yv[V];
+        *reinterpret_cast<uint4*>(yv) = *reinterpret_cast<const uint4*>(ty + e);
+#pragma unroll
+        for (int l = 0; l < V; ++l) add<COMP>(a[l], math::mul(xv[l], yv[l]));
+      } else {
+#pragma unroll
+        for (int l = 0; l < V; ++l) add<COMP>(a[l], xv[l]);
+      }
+    }
+    __syncthreads();                                   // every thread is done with stage s
+    if (threadIdx.x == 0 && pu < sh.units) {
+      tma::fence_proxy_async();
+      produce(s);
+    }
+    if (++ct == inner_unit_tiles<T>(sh, cu)) {         // unit complete: merge and emit
+      acc<T> t = a[0];
+#pragma unroll
+      for (int l = 1; l < V; ++l) t = merge<COMP>(t, a[l]);
+      t = block_merge<COMP>(t, red);
+      if (sh.splits == 1) {
+        if (threadIdx.x == 0) out[j] = result<COMP>(t);
+      } else {
+        if (threadIdx.x == 0) {
+          partials[cu] = t;
+          __threadfence();
+          const unsigned prev = atomicAdd(&counters[j], 1u);
+          s_last = (prev == (unsigned)sh.splits - 1u);
+          if (s_last) counters[j] = 0u;
+        }
+        __syncthreads();
+        if (s_last) {
+          __threadfence();
+          acc<T> m{T(0), T(0)};
+          for (size_t q = threadIdx.x; q < sh.splits; q += blockDim.x) {
+            const acc<T>* p = partials + j * sh.splits + q;
+            m = merge<COMP>(m, acc<T>{__ldcg(&p->s), __ldcg(&p->c)});
+          }
+          m = block_merge<COMP>(m, red);
+          if (threadIdx.x == 0) out[j] = result<COMP>(m);
+        }
+      }
+#pragma unroll
+      for (int l = 0; l < V; ++l) a[l] = acc<T>{T(0), T(0)};
+      ct = 0;
+      cu += gridDim.x;
+    }
+    ++iter;
+  }
+}
+
+// ------------------------------------------------------------ outer fold
+struct outer_tma_shape {
+  size_t rows, cols, cchunk, splits, strips, units;
+};
+
+constexpr int kOuterRows = 256;   // box rows (and threads per block)
+template <class T> __host__ __device__ constexpr int outer_cols() { return kTmaTileBytes / (kOuterRows * (int)sizeof(T)); }
+
+template <bool COMP, class T, int STAGES>
+__global__ void __launch_bounds__(256) k_outer_tma(const __grid_constant__ CUtensorMap map, outer_tma_shape sh,
+                                                   T* __restrict__ out, acc<T>* __restrict__ partials,
+                                                   unsigned* __restrict__ counters)
+{
+  constexpr int BR = kOuterRows, BC = outer_cols<T>();
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  T* buf = reinterpret_cast<T*>(smem_raw);          // [STAGES][BC][BR]
+  __shared__ __align__(8) uint64_t bar[STAGES];
+  __shared__ unsigned s_last;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) tma::mbar_init(&bar[s], 1);
+    tma::fence_barrier_init();
+  }
+  __syncthreads();
+
+  auto unit_tiles = [&](size_t u) {
+    const size_t c0 = (u % sh.splits) * sh.cchunk;
+    const size_t c1 = (c0 + sh.cchunk < sh.cols) ? c0 + sh.cchunk : sh.cols;
+    return (c1 - c0 + BC - 1) / BC;
+  };
+  size_t pu = blockIdx.x, pt = 0;
+  uint32_t issued = 0;
+  auto produce = [&](int s) {
+    const int xr = (int)((pu / sh.splits) * BR);
+    const int yc = (int)((pu % sh.splits) * sh.cchunk + pt * BC);
+    tma::mbar_arrive_expect_tx(&bar[s], (uint32_t)(BR * BC * sizeof(T)));
+    tma::tensor_g2s_2d(buf + (size_t)s * BC * BR, &map, xr, yc, &bar[s]);
+    ++issued;
+    if (++pt == unit_tiles(pu)) { pt = 0; pu += gridDim.x; }
+  };
+  if (threadIdx.x == 0)
+    for (int s = 0; s < STAGES && pu < sh.units; ++s) produce(s);
+
+  size_t cu = blockIdx.x, ct = 0;
+  uint32_t iter = 0;
+  acc<T> a0{T(0), T(0)}, a1{T(0), T(0)};
+  while (cu < sh.units) {
+    const int s = (int)(iter % STAGES);
+    const bool ok = tma::mbar_wait(&bar[s], (iter / STAGES) & 1u);
+    if (__syncthreads_or(!ok)) {
+      const size_t row = (cu / sh.splits) * BR + threadIdx.x;
+      if (row < sh.rows) out[row] = quiet_nan<T>();
+      if (threadIdx.x == 0)
+        for (uint32_t k = iter; k < issued; ++k) tma::mbar_wait(&bar[k % STAGES], (k / STAGES) & 1u);
+      __syncthreads();
+      return;
+    }
+    const T* tile = buf + (size_t)s * BC * BR;
+    // columns past the table are zero-filled by the copy; chunks are whole tiles wide
+#pragma unroll
+    for (int c = 0; c < BC; c += 2) {
+      add<COMP>(a0, tile[c * BR + threadIdx.x]);
+      add<COMP>(a1, tile[(c + 1) * BR + threadIdx.x]);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && pu < sh.units) {
+      tma::fence_proxy_async();
+      produce(s);
+    }
+    if (++ct == unit_tiles(cu)) {
+      const size_t strip = cu / sh.splits;
+      const size_t row = strip * BR + threadIdx.x;
+      const acc<T> t = merge<COMP>(a0, a1);
+      if (sh.splits == 1) {
+        if (row < sh.rows) out[row] = result<COMP>(t);
+      } else {
+        partials[cu * BR + threadIdx.x] = t;
+        __syncthreads();                    // the block's partials, then one device-scope fence
+        if (threadIdx.x == 0) {
+          __threadfence();
+          const unsigned prev = atomicAdd(&counters[strip], 1u);
+          s_last = (prev == (unsigned)sh.splits - 1u);
+          if (s_last) counters[strip] = 0u;
+        }
+        __syncthreads();
+        if (s_last) {
+          __threadfence();
+          acc<T> m = merge_partials<COMP, T>(partials + strip * sh.splits * BR + threadIdx.x, sh.splits, BR);
+          if (row < sh.rows) out[row] = result<COMP>(m);
+        }
+      }
+      a0 = acc<T>{T(0), T(0)};
+      a1 = acc<T>{T(0), T(0)};
+      ct = 0;
+      cu += gridDim.x;
+    }
+    ++iter;
+  }
+}
+
+// ------------------------------------------------------------- launchers
+inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
+template <class K> inline cudaError_t set_smem(K kernel, int bytes)
+{
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+// x (and y when not null) are 16-byte aligned and rows % (16/sizeof(T)) == 0.
+template <bool COMP, class T>
+cudaError_t inner_fold_tma(const T* x, const T* y, size_t rows, size_t cols, T* out, cudaStream_t s)
+{
+  constexpr int TILE = inner_tile<T>();
+  inner_tma_shape sh;
+  sh.rows = rows;
+  sh.cols = cols;
+  sh.seg = (size_t)TILE * 16;
+  sh.splits = (rows + sh.seg - 1) / sh.seg;
+  sh.units = cols * sh.splits;
+  if (sh.units == 0) return cudaSuccess;
+  acc<T>* partials = nullptr;
+  unsigned* counters = nullptr;
+  if (sh.splits > 1) {
+    const size_t cbytes = (cols * sizeof(unsigned) + 255) / 256 * 256;
+    void* scratch = nullptr;
+    cudaError_t e = stream_scratch(s, cbytes + sh.units * sizeof(acc<T>), &scratch);
+    if (e != cudaSuccess) return e;
+    counters = (unsigned*)scratch;
+    partials = (acc<T>*)((char*)scratch + cbytes);
+  }
+  size_t grid;
+  cudaError_t e;
+  if (y) {
+    constexpr int ST = 3;
+    auto k = k_inner_tma<COMP, T, 2, ST>;
+    const int smem = ST * 2 * kTmaTileBytes;
+    if ((e = set_smem(k, smem)) != cudaSuccess) return e;
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, 256, smem);
+    grid = (size_t)sm_count() * (size_t)(per > 0 ? per : 1);
+    if (grid > sh.units) grid = sh.units;
+    k<<<(unsigned)grid, 256, smem, s>>>(x, y, sh, out, partials, counters);
+  } else {
+    constexpr int ST = 4;
+    auto k = k_inner_tma<COMP, T, 1, ST>;
+    const int smem = ST * kTmaTileBytes;
+    if ((e = set_smem(k, smem)) != cudaSuccess) return e;
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, 256, smem);
+    grid = (size_t)sm_count() * (size_t)(per > 0 ? per : 1);
+    if (grid > sh.units) grid = sh.units;
+    k<<<(unsigned)grid, 256, smem, s>>>(x, y, sh, out, partials, counters);
+  }
+  return cudaGetLastError();
+}
+
+// A is 16-byte aligned and rows % (16/sizeof(T)) == 0; rows, cols < 2^31.
+template <bool COMP, class T>
+cudaError_t outer_fold_tma(const T* A, size_t rows, size_t cols, T* out, cudaStream_t s)
+{
+  constexpr int BR = kOuterRows, BC = outer_cols<T>();
+  if (rows == 0 || cols == 0) return cudaSuccess;
+  if (rows >= ((size_t)1 << 31) || cols >= ((size_t)1 << 31)) return cudaErrorNotSupported;
+  PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+  if (!encode) return cudaErrorNotSupported;
+  CUtensorMap map;
+  const cuuint64_t gdim[2] = {(cuuint64_t)rows, (cuuint64_t)cols};
+  const cuuint64_t gstride[1] = {(cuuint64_t)rows * sizeof(T)};
+  const cuuint32_t box[2] = {(cuuint32_t)BR, (cuuint32_t)BC};
+  const cuuint32_t estride[2] = {1, 1};
+  CUresult r = encode(&map, sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2,
+                      (void*)A, gdim, gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+  outer_tma_shape sh;
+  sh.rows = rows;
+  sh.cols = cols;
+  sh.strips = (rows + BR - 1) / BR;
+  // about 2048 units so blocks stay balanced; a chunk is a whole number of tiles
+  size_t want = (cols * sh.strips + 2047) / 2048;
+  sh.cchunk = ((want + BC - 1) / BC) * BC;
+  if (sh.cchunk < (size_t)BC) sh.cchunk = BC;
+  sh.splits = (cols + sh.cchunk - 1) / sh.cchunk;
+  sh.units = sh.strips * sh.splits;
+  acc<T>* partials = nullptr;
+  unsigned* counters = nullptr;
+  if (sh.splits > 1) {
+    const size_t cbytes = (sh.strips * sizeof(unsigned) + 255) / 256 * 256;
+    void* scratch = nullptr;
+    cudaError_t e = stream_scratch(s, cbytes + sh.units * BR * sizeof(acc<T>), &scratch);
+    if (e != cudaSuccess) return e;
+    counters = (unsigned*)scratch;
+    partials = (acc<T>*)((char*)scratch + cbytes);
+  }
+  constexpr int ST = 4;
+  auto k = k_outer_tma<COMP, T, ST>;
+  const int smem = ST * kTmaTileBytes;
+  cudaError_t e = set_smem(k, smem);
+  if (e != cudaSuccess) return e;
+  int per = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, 256, smem);
+  size_t grid = (size_t)sm_count() * (size_t)(per > 0 ? per : 1);
+  if (grid > sh.units) grid = sh.units;
+  k<<<(unsigned)grid, 256, smem, s>>>(map, sh, out, partials, counters);
+  return cudaGetLastError();
+}
+
+}  // namespace fold
+}  // namespace nt2cuda

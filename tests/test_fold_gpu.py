@@ -24,6 +24,15 @@ def to_dev(a):
     return torch.from_numpy(np.ascontiguousarray(a)).cuda()
 
 
+@pytest.fixture(params=["auto", "simt", "tma"], autouse=True)
+def fold_path(request, cuda_lib):
+    """Every fold test runs on each kernel family (nt2cuda_set_fold_path)."""
+    code = {"auto": 0, "simt": 1, "tma": 2}[request.param]
+    assert cuda_lib.nt2cuda_set_fold_path(code) == 0
+    yield request.param
+    cuda_lib.nt2cuda_set_fold_path(0)
+
+
 def host(t):
     torch.cuda.synchronize()
     return t.cpu().numpy()
