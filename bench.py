@@ -337,6 +337,7 @@ def run_ours(args):
     traffic = profiled_traffic("k_blackscholes_f32_n16777216")
 
     # e2e: host (pinned) buffers through the C ABI, copies inside the timed region
+    api.autotune("bs_f32_mapped", n)
     Sh, Kh, Th = (a.cpu().pin_memory() for a in (S, K, T))
     ch = torch.empty(n, dtype=torch.float32).pin_memory()
     ph = torch.empty(n, dtype=torch.float32).pin_memory()
@@ -424,17 +425,17 @@ CASES = ("bs_exact", "bs_fused", "bs_fast", "bs_fastnormcdf", "bs_f64", "saxpy",
          "inner", "outer", "sigmadelta")
 
 
-def run_case(name: str, steps: int, warmup: int):
+def run_case(name: str, steps: int, warmup: int, autotune: bool = True):
     """One configuration alone, for profiling: prints one JSON line."""
     import torch
     torch.cuda.set_device(0)
     import nt2_gb300.api as api
     api.init(0)
-    for line in suite(1, only=name, steps=steps, warmup=warmup):
+    for line in suite(1, only=name, steps=steps, warmup=warmup, autotune=autotune):
         print(json.dumps(line), flush=True)
 
 
-def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: int = 3):
+def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: int = 3, autotune: bool = True):
     """One line per configuration (device time, inputs resident, > L2 or flushed)."""
     import torch
     import nt2_gb300.api as api
@@ -462,7 +463,8 @@ def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: in
         for i in range(4):
             api.fill_uniform(xs[i], -1, 1, 1 + i)
             api.fill_uniform(ys[i], -1, 1, 11 + i)
-        api.autotune("saxpy_f32", n)
+        if autotune:
+            api.autotune("saxpy_f32", n)
         it = [0]
 
         def saxpy_step():
@@ -534,7 +536,8 @@ def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: in
         c = torch.empty_like(S)
         p = torch.empty_like(S)
         for key in ("bs_f32", "bs_f32_fused", "bs_f32_fast"):
-            api.autotune(key, 1 << 24)
+            if autotune:
+                api.autotune(key, 1 << 24)
         for cn, prec, cdf in bs_cases:
             if not want(cn) or (only is None and cn == "bs_exact"):
                 continue
@@ -604,9 +607,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--case", choices=CASES, help="run one configuration alone (for profiling)")
+    ap.add_argument("--no-autotune", action="store_true", help="with --case: default launch shapes")
     args = ap.parse_args()
     if args.case:
-        run_case(args.case, args.steps, max(args.warmup, 3))
+        run_case(args.case, args.steps, max(args.warmup, 3), autotune=not args.no_autotune)
     elif args.impl == "reference":
         run_reference(args)
     else:

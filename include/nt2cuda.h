@@ -266,7 +266,9 @@ nt2cuda_status nt2cuda_server_get_stats(nt2cuda_server* server, nt2cuda_server_s
 /* Times the launch variants of one entry point at size n on scratch tables
  * and records the fastest for n's size bucket.  kernel: "saxpy_f32",
  * "saxpy_f64", "bs_f32", "bs_f32_fused", "bs_f32_fast", "bs_f64",
- * "bs_f64_fused" (the Black-Scholes keys are per precision mode). */
+ * "bs_f64_fused" (the Black-Scholes keys are per precision mode), and
+ * "bs_f32_mapped", "bs_f32_fast_mapped" (the kernel on pinned host tables,
+ * as nt2cuda_blackscholes_f32_host runs it). */
 nt2cuda_status nt2cuda_autotune(const char* kernel, size_t n, int* best_unroll, int* best_waves, float* best_ms);
 /* Tuning table as text ("key@bucket unroll waves" lines). */
 nt2cuda_status nt2cuda_tuning_export(char* buf, size_t cap, size_t* needed);

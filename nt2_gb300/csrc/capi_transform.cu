@@ -316,14 +316,19 @@ nt2cuda_status nt2cuda_autotune(const char* kernel, size_t n, int* best_unroll, 
   const size_t es = f64 ? 8 : 4;
   int prec = PREC_EXACT;
   if (k == "bs_f32_fused" || k == "bs_f64_fused") prec = PREC_FUSED;
-  if (k == "bs_f32_fast") prec = PREC_FAST;
-  const bool bs32 = (k == "bs_f32" || k == "bs_f32_fused" || k == "bs_f32_fast");
+  if (k == "bs_f32_fast" || k == "bs_f32_fast_mapped") prec = PREC_FAST;
+  // *_mapped keys tune the kernel on pinned host tables (the zero-copy host path)
+  const bool mapped = (k == "bs_f32_mapped" || k == "bs_f32_fast_mapped");
+  const bool bs32 = (k == "bs_f32" || k == "bs_f32_fused" || k == "bs_f32_fast" || mapped);
   const bool bs64 = (k == "bs_f64" || k == "bs_f64_fused");
   if (!(bs32 || bs64 || k == "saxpy_f32" || k == "saxpy_f64")) return NT2CUDA_ERR_ARG;
   void* buf[5] = {};
   for (int j = 0; j < 5; ++j) {
-    cudaError_t e = cudaMalloc(&buf[j], n * es);
-    if (e != cudaSuccess) { for (int q = 0; q < j; ++q) cudaFree(buf[q]); return from_cuda(e); }
+    cudaError_t e = mapped ? cudaMallocHost(&buf[j], n * es) : cudaMalloc(&buf[j], n * es);
+    if (e != cudaSuccess) {
+      for (int q = 0; q < j; ++q) { if (mapped) cudaFreeHost(buf[q]); else cudaFree(buf[q]); }
+      return from_cuda(e);
+    }
   }
   cudaStream_t s;
   cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
@@ -340,12 +345,12 @@ nt2cuda_status nt2cuda_autotune(const char* kernel, size_t n, int* best_unroll, 
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   const int unrolls[3] = {1, 2, 4};
-  const int wavesv[3] = {1, 2, 4};
+  const int wavesv[4] = {1, 2, 4, 8};
   float best = 1e30f;
   tuning::params bp;
   nt2cuda_status st = NT2CUDA_OK;
   for (int ui = 0; ui < 3 && st == NT2CUDA_OK; ++ui)
-    for (int wi = 0; wi < 3 && st == NT2CUDA_OK; ++wi) {
+    for (int wi = 0; wi < 4 && st == NT2CUDA_OK; ++wi) {
       auto once = [&]() -> nt2cuda_status {
         if (bs32)
           return bs_dispatch<float>((float*)buf[0], (float*)buf[1], (float*)buf[2], 0.02f, 0.30f, (float*)buf[3],
@@ -374,7 +379,7 @@ nt2cuda_status nt2cuda_autotune(const char* kernel, size_t n, int* best_unroll, 
   cudaEventDestroy(e1);
   cudaStreamSynchronize(s);
   cudaStreamDestroy(s);
-  for (int j = 0; j < 5; ++j) cudaFree(buf[j]);
+  for (int j = 0; j < 5; ++j) { if (mapped) cudaFreeHost(buf[j]); else cudaFree(buf[j]); }
   if (st != NT2CUDA_OK) return st;
   if (best_unroll) *best_unroll = bp.unroll;
   if (best_waves) *best_waves = bp.waves;
