@@ -116,26 +116,18 @@ class ClockSampler:
 
 # --------------------------------------------------------------- helpers
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    from nt2_gb300 import replicas
+    return replicas.env()
 
 
 def max_over_ranks(x: float, ws: int):
-    if ws == 1:
-        return x
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    from nt2_gb300 import replicas
+    return replicas.max_over_ranks(x, ws)
 
 
 def barrier(ws: int):
-    if ws > 1:
-        import torch.distributed as dist
-        dist.barrier()
+    from nt2_gb300 import replicas
+    replicas.barrier(ws)
 
 
 def bs_tables(n: int, seed: int):
@@ -331,7 +323,8 @@ def run_ours(args):
         mms, _, _ = time_device(make_step(prec), min(args.steps, 500), max(args.warmup, 3), ws)
         gbs = BYTES_PER_OPTION * n / (mms * 1e-3) / 1e9
         modes[name] = {"ms_per_step": mms, "options_per_s": ws * n / (mms * 1e-3), "gb_per_s": gbs}
-    value = ws * n / (ms * 1e-3)
+    from nt2_gb300 import replicas
+    value = replicas.job_throughput(n, ws, ms * 1e-3)
     peak, peak_kind = peaks()
     achieved = BYTES_PER_OPTION * n / (ms * 1e-3) / 1e9
     traffic = profiled_traffic("k_blackscholes_f32_n16777216")
@@ -608,7 +601,11 @@ def main():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--case", choices=CASES, help="run one configuration alone (for profiling)")
     ap.add_argument("--no-autotune", action="store_true", help="with --case: default launch shapes")
+    ap.add_argument("--tuning", default=None, help="tuning-table text to import first (\"key@bucket unroll waves\" lines)")
     args = ap.parse_args()
+    if args.tuning:
+        import nt2_gb300.api as api
+        api.tuning_import(args.tuning.replace(";", "\n"))
     if args.case:
         run_case(args.case, args.steps, max(args.warmup, 3), autotune=not args.no_autotune)
     elif args.impl == "reference":

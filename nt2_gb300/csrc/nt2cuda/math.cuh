@@ -128,23 +128,34 @@ __device__ __forceinline__ float log(float a0)
 // kernels: modules/core/euler/include/nt2/euler/functions/details/erf_kernel.hpp:48-85
 // erfc_abs(x) is the |a0| part, shared by erfc(a) and erfc(-a):
 // erfc(a) = a < 0 ? 2 - erfc_abs(|a|) : erfc_abs(|a|).
+// The two regions of NT2's float erfc, given x = |a| and z = x/(1+x).
 template <bool F = false>
-__device__ __forceinline__ float erfc_abs(float x)
+__device__ __forceinline__ float erfc_small(float z)
+{
+  constexpr uint32_t P3[9] = {0x41aa8e55u, 0x401b5680u, 0xc010d956u, 0x3f2cff3bu,
+                              0xc016c985u, 0xbffc9284u, 0xbfa11698u, 0xbe036d7eu, 0x3f7ffffeu};
+  return mul(sub(1.0f, z), horner<F>(z, P3));
+}
+template <bool F = false>
+__device__ __forceinline__ float erfc_large(float x, float z)
 {
   constexpr uint32_t P2[11] = {0xc0283611u, 0x40d67e3bu, 0xc0cd1a85u, 0x4050b063u,
                                0xbfaea865u, 0x3e2006f0u, 0x3e1175c7u, 0x3ec4ca6eu,
                                0x3e243828u, 0xbf918a62u, 0x3f0a0e8bu};
-  constexpr uint32_t P3[9] = {0x41aa8e55u, 0x401b5680u, 0xc010d956u, 0x3f2cff3bu,
-                              0xc016c985u, 0xbffc9284u, 0xbfa11698u, 0xbe036d7eu, 0x3f7ffffeu};
-  float z = div(x, add(1.0f, x));
-  float r1;
-  if (x < fbits(cf::twothird)) {
-    r1 = mul(sub(1.0f, z), horner<F>(z, P3));
-  } else {
-    float zz = sub(z, 0.4f);
-    r1 = mul(exp<F>(-mul(x, x)), horner<F>(zz, P2));
-  }
+  return mul(exp<F>(-mul(x, x)), horner<F>(sub(z, 0.4f), P2));
+}
+__device__ __forceinline__ bool erfc_is_small(float x) { return x < fbits(cf::twothird); }
+__device__ __forceinline__ float erfc_finish(float x, float r1)
+{
   return (x == __int_as_float(0x7f800000)) ? 0.0f : r1;
+}
+
+template <bool F = false>
+__device__ __forceinline__ float erfc_abs(float x)
+{
+  float z = div(x, add(1.0f, x));
+  float r1 = erfc_is_small(x) ? erfc_small<F>(z) : erfc_large<F>(x, z);
+  return erfc_finish(x, r1);
 }
 
 template <bool F = false>
