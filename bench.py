@@ -213,7 +213,18 @@ def serving_bench(seconds: float = 1.0, rates=(1000, 10000, 50000), seed: int = 
     torch.cuda.synchronize()
     rng = np.random.default_rng(seed)
     out = {}
+    # The arrival loop busy-waits in Python while the client thread collects and releases
+    # results; with the default 5 ms GIL switch interval the client would get the
+    # interpreter about once per 5 ms, release outputs late and let the 40 GB budget fill.
+    switch = sys.getswitchinterval()
+    sys.setswitchinterval(2e-5)
+    try:
+        return _serving(np, Server, S, K, T, pool_n, rng, out, seconds, rates, seed)
+    finally:
+        sys.setswitchinterval(switch)
 
+
+def _serving(np, Server, S, K, T, pool_n, rng, out, seconds, rates, seed):
     def run(mode, rate, dur):
         coalesce = mode == "batched"
         srv = Server(budget_bytes=40 << 30, max_batch_requests=4096, max_inflight_batches=3 if coalesce else 1,
@@ -256,7 +267,9 @@ def serving_bench(seconds: float = 1.0, rates=(1000, 10000, 50000), seed: int = 
         lat_us = np.array(lat) / 1e3
         return {"requests": nreq, "options_per_s": float(sizes.sum() / (t1 - t0)),
                 "p50_us": float(np.percentile(lat_us, 50)), "p99_us": float(np.percentile(lat_us, 99)),
-                "launches": int(st["launches"]), "batches": int(st["batches"])}
+                "launches": int(st["launches"]), "batches": int(st["batches"]),
+                "admission_waits": int(st["admission_waits"]),
+                "peak_reserved_gb": round(st["peak_reserved_bytes"] / 1e9, 2)}
 
     for rate in rates:
         out[f"{rate}_req_s"] = {m: run(m, rate, seconds) for m in ("batched", "launch_per_request")}
@@ -425,6 +438,7 @@ def run_ours(args):
 
 
 CASES = ("bs_exact", "bs_fused", "bs_fast", "bs_fastnormcdf", "bs_f64", "saxpy", "sdot", "sdot_plain",
+         "rgb2grey_u8", "rgb2yuv", "mandelbrot",
          "inner", "outer", "sigmadelta")
 
 
@@ -491,6 +505,48 @@ def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: in
             ms, _, _ = time_device(lambda: api.dot(x, y, compensated=False, out=o), K(100), warmup, ws)
             out.append(line("sdot f32 2^26 plain", ms, 8 * n, n, "elements/s"))
         del x, y
+    if want("rgb2grey_u8"):
+        # two sets of uint8 planes (2 x 268 MB > L2) visited in turn
+        n = 1 << 26
+        gen = torch.Generator(device="cuda")
+        gen.manual_seed(5)
+        sets = [[torch.randint(0, 256, (n,), dtype=torch.uint8, device="cuda", generator=gen) for _ in range(4)]
+                for _ in range(2)]
+        it = [0]
+
+        def grey_step():
+            r, g, b, o = sets[it[0] & 1]
+            it[0] += 1
+            api.rgb2grey(r, g, b, out=o)
+        ms, _, _ = time_device(grey_step, K(200), warmup, ws)
+        out.append(line("rgb2grey u8 2^26 pixels (2 rotating sets, 536 MB > L2)", ms, 4 * n, n, "pixels/s"))
+        del sets
+    if want("rgb2yuv"):
+        n = 1 << 24
+        sets = []
+        for k in range(2):
+            planes = [torch.empty(n, device="cuda") for _ in range(3)]
+            for j, t in enumerate(planes):
+                api.fill_uniform(t, 0, 255, 31 + 3 * k + j)
+            sets.append(planes)
+        it = [0]
+
+        def yuv_step():
+            r, g, b = sets[it[0] & 1]
+            it[0] += 1
+            api.rgb2yuv(r, g, b)
+        ms, _, _ = time_device(yuv_step, K(200), warmup, ws)
+        out.append(line("rgb2yuv f32 2^24 pixels (2 rotating sets)", ms, 24 * n, n, "pixels/s"))
+        del sets
+    if want("mandelbrot"):
+        h = w = 1600
+        C = torch.empty(h * w, dtype=torch.int32, device="cuda")
+        ms, _, _ = time_device(lambda: api.mandelbrot_grid(-1.5, 1.5, -1.5, 1.5, h, w, pack=8, out=C), K(50),
+                               warmup, ws)
+        counts = C.to(torch.int64).sum().item()
+        out.append({"config": "mandelbrot 1600x1600 over [-1.5,1.5]^2, pack 8 (FP32 issue-bound)", "ms": ms,
+                    "value": h * w / (ms * 1e-3), "unit": "pixels/s",
+                    "counted_trips_per_s": counts / (ms * 1e-3), "mean_count": counts / (h * w)})
     if not (want("inner") or want("outer") or want("bs_f64") or want("bs_fused") or want("bs_fast")
             or want("bs_exact") or want("bs_fastnormcdf") or want("sigmadelta")):
         return out

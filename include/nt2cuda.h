@@ -107,6 +107,39 @@ nt2cuda_status nt2cuda_saxpy_f64(double alpha, const double* x, double* y, size_
 nt2cuda_status nt2cuda_rgb2grey_f32(const float* r, const float* g, const float* b, float* gr, size_t n,
                                     int fused, nt2cuda_stream stream);
 
+/* The same statement over uint8 planes, spelled in NT2 as
+ *   gr = cast<uint8_t>(0.3f*cast<float>(r) + 0.59f*cast<float>(g) + 0.11f*cast<float>(b))
+ * (nt2/operator/functions/container/cast.hpp:133-150: tofloat on the way in, touint and
+ * narrowing on the way out, i.e. truncation toward zero; the sum stays in [0, 255]). */
+nt2cuda_status nt2cuda_rgb2grey_u8(const uint8_t* r, const uint8_t* g, const uint8_t* b, uint8_t* gr, size_t n,
+                                   int fused, nt2cuda_stream stream);
+
+/* The rgb2yuv demo's three statements (demo/rgb2yuv/nt2/rgb2yuv_nt2.cpp:28-33)
+ *   y = 0.299f*r + 0.587f*g + 0.114f*b;  u = 0.492f*(b - y);  v = 0.877f*(r - y);
+ * in one pass: u and v use the y value the first statement stores, so the
+ * result is the one of the three NT2 passes.  The outputs may not overlap the
+ * inputs or each other (NT2CUDA_ERR_ALIAS). */
+nt2cuda_status nt2cuda_rgb2yuv_f32(const float* r, const float* g, const float* b, float* y, float* u, float* v,
+                                   size_t n, int fused, nt2cuda_stream stream);
+
+/* C = arrayfun(step, A, B) of the mandelbrot demo (demo/mandelbrot/nt2/mandelbrot_nt2.cpp:41-83,120-123):
+ * per element the escape-time loop z <- z^2 + (a + ib) from z = 0, at most 256
+ * trips, counting the trips on which |z|^2 < 4 held before the update.  NT2
+ * runs the functor on SIMD packs: a pack keeps iterating while any of its
+ * lanes has not escaped, and elements past the last whole pack run alone.
+ * `pack` is that cardinality (1, 2, 4, 8, 16 or 32; 8 is AVX float, 1 the
+ * scalar build); it changes results only where an escaped orbit re-enters
+ * the disc.  Element i of C is an int32 count. */
+nt2cuda_status nt2cuda_mandelbrot_f32(const float* A, const float* B, int32_t* C, size_t n, int pack,
+                                      nt2cuda_stream stream);
+/* The demo's complete program: A = expand_to(linspace(a0,a1,w),h,w) and
+ * B = expand_to(colvect(linspace(b0,b1,h)),h,w) generated in the kernel (no
+ * input tables; linspace as nt2/core/functions/details/linspace.hpp:33-45), then
+ * C (h x w, column-major) = arrayfun(step, A, B).  NT2 accepts the demo's
+ * expand_to only for h == w; other shapes follow the same formulas. */
+nt2cuda_status nt2cuda_mandelbrot_grid_f32(float a0, float a1, float b0, float b1, size_t h, size_t w,
+                                           int32_t* C, int pack, nt2cuda_stream stream);
+
 /* Black-Scholes call and put over n options with scalar rate r and
  * volatility sigma, as the NT2 statement
  *   tie(call,put) = tie(fnms(e,cdf(d2),S*cdf(d1)), fnms(S,cdf(-d1),e*cdf(-d2)))
@@ -234,6 +267,8 @@ typedef struct {
   int fused;                  /* precision mode: 0 exact, 1 fused, 2 fast   */
   int cdf_kind;               /* 0 = normcdf, 1 = fastnormcdf               */
   int wait_timeout_ms;        /* default bound of waits (<= 0: 60000)       */
+  int spin_us;                /* the launch thread polls this long for new
+                                 requests before it sleeps (< 0: 0; 0: 50)   */
 } nt2cuda_server_config;
 
 typedef struct {

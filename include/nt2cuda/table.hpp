@@ -316,6 +316,15 @@ NT2CUDA_FN3(fnms, fnms_)
 NT2CUDA_FN3(if_else, if_else_)
 #undef NT2CUDA_FN3
 
+// cast<R>(x): the elements of x converted to R, as nt2::cast
+// (nt2/operator/functions/container/cast.hpp:133-150).
+template <class R, class A, std::enable_if_t<is_operand_v<A>, int> = 0> inline auto cast(const A& a)
+{
+  auto t = tree_of(a);
+  using N = node<tag::cast_, decltype(t), scal<R>>;
+  return xpr<N>{N{t, scal<R>{R(0)}}, size_of(a)};
+}
+
 // if_zero_else_one(c): the result has the element type of the compared operands.
 template <class E> inline auto if_zero_else_one(const xpr<E>& c)
 {

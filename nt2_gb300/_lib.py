@@ -43,6 +43,7 @@ class ServerConfig(C.Structure):
     _fields_ = [
         ("budget_bytes", c_size), ("max_batch_requests", c_int), ("max_inflight_batches", c_int),
         ("coalesce", c_int), ("fused", c_int), ("cdf_kind", c_int), ("wait_timeout_ms", c_int),
+        ("spin_us", c_int),
     ]
 
 
@@ -77,6 +78,10 @@ _SIGS = {
     "nt2cuda_saxpy_f32": (c_int, [c_f, c_vp, c_vp, c_size, c_int, c_vp]),
     "nt2cuda_saxpy_f64": (c_int, [c_d, c_vp, c_vp, c_size, c_int, c_vp]),
     "nt2cuda_rgb2grey_f32": (c_int, [c_vp, c_vp, c_vp, c_vp, c_size, c_int, c_vp]),
+    "nt2cuda_rgb2grey_u8": (c_int, [c_vp, c_vp, c_vp, c_vp, c_size, c_int, c_vp]),
+    "nt2cuda_rgb2yuv_f32": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_size, c_int, c_vp]),
+    "nt2cuda_mandelbrot_f32": (c_int, [c_vp, c_vp, c_vp, c_size, c_int, c_vp]),
+    "nt2cuda_mandelbrot_grid_f32": (c_int, [c_f, c_f, c_f, c_f, c_size, c_size, c_vp, c_int, c_vp]),
     "nt2cuda_blackscholes_f32": (c_int, [c_vp, c_vp, c_vp, c_f, c_f, c_vp, c_vp, c_size, c_int, c_int, c_vp]),
     "nt2cuda_blackscholes_f64": (c_int, [c_vp, c_vp, c_vp, c_d, c_d, c_vp, c_vp, c_size, c_int, c_vp]),
     "nt2cuda_blackscholes_demo_f32": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_size, c_int, c_vp]),

@@ -67,9 +67,45 @@ def saxpy(alpha: float, x: torch.Tensor, y: torch.Tensor, fused: bool = False) -
 
 def rgb2grey(r: torch.Tensor, g: torch.Tensor, b: torch.Tensor, out: torch.Tensor | None = None,
              fused: bool = False) -> torch.Tensor:
+    """gr = 0.3*r + 0.59*g + 0.11*b over float32 planes, or over uint8 planes with the
+    float statement between cast<float> and cast<uint8_t>."""
     out = torch.empty_like(r) if out is None else out
-    check(lib().nt2cuda_rgb2grey_f32(_dev(r, torch.float32), _dev(g, torch.float32), _dev(b, torch.float32),
-                                     _dev(out, torch.float32), r.numel(), int(fused), _stream()), "rgb2grey")
+    if r.dtype == torch.uint8:
+        st = lib().nt2cuda_rgb2grey_u8(_dev(r, torch.uint8), _dev(g, torch.uint8), _dev(b, torch.uint8),
+                                       _dev(out, torch.uint8), r.numel(), int(fused), _stream())
+    else:
+        st = lib().nt2cuda_rgb2grey_f32(_dev(r, torch.float32), _dev(g, torch.float32), _dev(b, torch.float32),
+                                        _dev(out, torch.float32), r.numel(), int(fused), _stream())
+    check(st, "rgb2grey")
+    return out
+
+
+def rgb2yuv(r: torch.Tensor, g: torch.Tensor, b: torch.Tensor, fused: bool = False):
+    """(y, u, v) of the rgb2yuv demo over float32 planes, in one pass."""
+    y, u, v = (torch.empty_like(r) for _ in range(3))
+    check(lib().nt2cuda_rgb2yuv_f32(_dev(r, torch.float32), _dev(g, torch.float32), _dev(b, torch.float32),
+                                    _dev(y), _dev(u), _dev(v), r.numel(), int(fused), _stream()), "rgb2yuv")
+    return y, u, v
+
+
+def mandelbrot(A: torch.Tensor, B: torch.Tensor, pack: int = 8, out: torch.Tensor | None = None) -> torch.Tensor:
+    """C = arrayfun(step, A, B) of the mandelbrot demo: int32 escape counts (at most 256)."""
+    if A.numel() != B.numel():
+        raise ValueError("A and B must have the same size")
+    out = torch.empty(A.shape, dtype=torch.int32, device=A.device) if out is None else out
+    check(lib().nt2cuda_mandelbrot_f32(_dev(A, torch.float32), _dev(B, torch.float32), _dev(out, torch.int32),
+                                       A.numel(), int(pack), _stream()), "mandelbrot")
+    return out
+
+
+def mandelbrot_grid(a0: float, a1: float, b0: float, b1: float, h: int, w: int, pack: int = 8,
+                    out: torch.Tensor | None = None) -> torch.Tensor:
+    """The demo's whole program over an h x w grid (column-major, returned as a flat int32 table)."""
+    out = torch.empty(h * w, dtype=torch.int32, device="cuda") if out is None else out
+    if out.numel() != h * w:
+        raise ValueError("out must hold h*w counts")
+    check(lib().nt2cuda_mandelbrot_grid_f32(a0, a1, b0, b1, h, w, _dev(out, torch.int32), int(pack), _stream()),
+          "mandelbrot_grid")
     return out
 
 

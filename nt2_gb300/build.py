@@ -22,6 +22,7 @@ SOURCES = [
     "capi_transform.cu",
     "capi_fold.cu",
     "capi_sigmadelta.cu",
+    "capi_mandelbrot.cu",
     "server.cu",
     "capi_noalloc.cu",
 ]

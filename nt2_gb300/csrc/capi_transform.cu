@@ -59,6 +59,90 @@ template <bool F> nt2cuda_status rgb2grey_impl(const float* r, const float* g, c
   return run<F>(make_prog(asg(gr, e)), n, s, "rgb2grey");
 }
 
+// gr = cast<uint8_t>(T(0.3)*cast<float>(r) + T(0.59)*cast<float>(g) + T(0.11)*cast<float>(b)),
+// the float statement's tree between the two casts.
+template <bool F> nt2cuda_status rgb2grey_u8_impl(const uint8_t* r, const uint8_t* g, const uint8_t* b,
+                                                  uint8_t* gr, size_t n, nt2cuda_stream s)
+{
+  auto fr = nd<tag::cast_>(tm(r), sc(0.0f));
+  auto fg = nd<tag::cast_>(tm(g), sc(0.0f));
+  auto fb = nd<tag::cast_>(tm(b), sc(0.0f));
+  auto e = nd<tag::fma_>(sc(0.11f), fb, nd<tag::fma_>(sc(0.3f), fr, nd<tag::multiplies_>(sc(0.59f), fg)));
+  // 0.3f + 0.59f + 0.11f < 1 and every term is >= 0, so the sum stays in [0, 255]
+  return run<F>(make_prog(asg(gr, nd<tag::trunc_u8_>(e))), n, s, "rgb2grey_u8");
+}
+
+// rgb2yuv: the three statements of one pixel, with u and v reading the y that
+// the first statement stores (the proto optimizer gives y the tree
+// fma(0.114, b, fma(0.299, r, 0.587*g)), as for rgb2grey).
+template <bool F> struct yuv {
+  __device__ __forceinline__ static void px(float r, float g, float b, float& y, float& u, float& v)
+  {
+    y = math::madd<F>(0.114f, b, math::madd<F>(0.299f, r, math::mul(0.587f, g)));
+    u = math::mul(0.492f, math::sub(b, y));
+    v = math::mul(0.877f, math::sub(r, y));
+  }
+};
+
+template <bool F>
+__global__ void __launch_bounds__(256) k_rgb2yuv(const float* __restrict__ r, const float* __restrict__ g,
+                                                 const float* __restrict__ b, float* __restrict__ y,
+                                                 float* __restrict__ u, float* __restrict__ v, size_t n)
+{
+  constexpr int V = 4;
+  const size_t groups = n / V;
+  const size_t T = (size_t)gridDim.x * blockDim.x;
+  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+#pragma unroll 1
+  for (size_t i = t; i < groups; i += T) {
+    float R[V], G[V], B[V], Y[V], Uo[V], Vo[V];
+    mem::load_vec<float, V, true>(r, i * V, R);
+    mem::load_vec<float, V, true>(g, i * V, G);
+    mem::load_vec<float, V, true>(b, i * V, B);
+#pragma unroll
+    for (int l = 0; l < V; ++l) yuv<F>::px(R[l], G[l], B[l], Y[l], Uo[l], Vo[l]);
+    mem::store_vec<float, V>(y, i * V, Y);
+    mem::store_vec<float, V>(u, i * V, Uo);
+    mem::store_vec<float, V>(v, i * V, Vo);
+  }
+  const size_t k = groups * V + t;
+  if (k < n) yuv<F>::px(r[k], g[k], b[k], y[k], u[k], v[k]);
+}
+
+template <bool F>
+__global__ void __launch_bounds__(256) k_rgb2yuv_scalar(const float* r, const float* g, const float* b, float* y,
+                                                        float* u, float* v, size_t n)
+{
+  const size_t T = (size_t)gridDim.x * blockDim.x;
+#pragma unroll 1
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += T)
+    yuv<F>::px(r[k], g[k], b[k], y[k], u[k], v[k]);
+}
+
+inline bool overlap(const void* a, const void* b, size_t bytes)
+{
+  const uintptr_t x = (uintptr_t)a, z = (uintptr_t)b;
+  return x < z + bytes && z < x + bytes;
+}
+
+template <bool F> nt2cuda_status rgb2yuv_impl(const float* r, const float* g, const float* b, float* y,
+                                              float* u, float* v, size_t n, cudaStream_t s)
+{
+  if (!n) return NT2CUDA_OK;
+  // one fused pass reads every input before writing: outputs may overlap nothing
+  const size_t bytes = n * sizeof(float);
+  const void* outs[3] = {y, u, v};
+  const void* all[6] = {r, g, b, y, u, v};
+  for (int o = 0; o < 3; ++o)
+    for (int k = 0; k < 6; ++k)
+      if (k != o + 3 && overlap(outs[o], all[k], bytes)) return NT2CUDA_ERR_ALIAS;
+  void* args[] = {(void*)&r, (void*)&g, (void*)&b, (void*)&y, (void*)&u, (void*)&v, (void*)&n};
+  const uintptr_t bits = (uintptr_t)r | (uintptr_t)g | (uintptr_t)b | (uintptr_t)y | (uintptr_t)u | (uintptr_t)v;
+  if (bits & 15u)       // a misaligned view: one element per thread
+    return launch_status(launch_persistent(k_rgb2yuv_scalar<F>, n, 256, 2, s, args));
+  return launch_status(launch_persistent(k_rgb2yuv<F>, n / 4 + 1, 256, 2, s, args));
+}
+
 // The demo statement, lowered through the generic expression engine.
 template <bool F> nt2cuda_status bs_demo_impl(const float* S, const float* X, const float* T, const float* r,
                                               const float* v, float* R, size_t n, nt2cuda_stream s)
@@ -125,6 +209,14 @@ nt2cuda_status bs_dispatch(const T* S, const T* K, const T* Tm, T r, T v, T* cal
   }
 }
 
+template <int CDF, int P> void warm_bs()
+{
+  (void)resident_blocks(k_blackscholes<float, CDF, P, 1>, 256);
+  (void)resident_blocks(k_blackscholes<float, CDF, P, 2>, 256);
+  (void)resident_blocks(k_blackscholes<float, CDF, P, 4>, 256);
+  (void)resident_blocks(k_blackscholes_scalar<float, CDF, P>, 256);
+}
+
 const char* bs_key(size_t bytes, int prec = 0)
 {
   if (bytes != 4) return prec == PREC_FUSED ? "bs_f64_fused" : "bs_f64";
@@ -143,6 +235,16 @@ struct host_pipeline {
 host_pipeline& hp() { static host_pipeline p; return p; }
 
 }  // namespace
+
+void nt2cuda::detail_capi::warm_blackscholes_f32(int cdf, int prec)
+{
+  if (cdf == CDF_FASTNORMCDF)
+    prec == PREC_FAST ? warm_bs<CDF_FASTNORMCDF, PREC_FAST>()
+    : prec == PREC_FUSED ? warm_bs<CDF_FASTNORMCDF, PREC_FUSED>() : warm_bs<CDF_FASTNORMCDF, PREC_EXACT>();
+  else
+    prec == PREC_FAST ? warm_bs<CDF_NORMCDF, PREC_FAST>()
+    : prec == PREC_FUSED ? warm_bs<CDF_NORMCDF, PREC_FUSED>() : warm_bs<CDF_NORMCDF, PREC_EXACT>();
+}
 
 extern "C" {
 
@@ -175,6 +277,21 @@ nt2cuda_status nt2cuda_rgb2grey_f32(const float* r, const float* g, const float*
 {
   if (n && (!r || !g || !b || !gr)) return NT2CUDA_ERR_ARG;
   return fused ? rgb2grey_impl<true>(r, g, b, gr, n, s) : rgb2grey_impl<false>(r, g, b, gr, n, s);
+}
+
+nt2cuda_status nt2cuda_rgb2grey_u8(const uint8_t* r, const uint8_t* g, const uint8_t* b, uint8_t* gr, size_t n,
+                                   int fused, nt2cuda_stream s)
+{
+  if (n && (!r || !g || !b || !gr)) return NT2CUDA_ERR_ARG;
+  return fused ? rgb2grey_u8_impl<true>(r, g, b, gr, n, s) : rgb2grey_u8_impl<false>(r, g, b, gr, n, s);
+}
+
+nt2cuda_status nt2cuda_rgb2yuv_f32(const float* r, const float* g, const float* b, float* y, float* u, float* v,
+                                   size_t n, int fused, nt2cuda_stream s)
+{
+  if (n && (!r || !g || !b || !y || !u || !v)) return NT2CUDA_ERR_ARG;
+  return fused ? rgb2yuv_impl<true>(r, g, b, y, u, v, n, as_stream(s))
+               : rgb2yuv_impl<false>(r, g, b, y, u, v, n, as_stream(s));
 }
 
 nt2cuda_status nt2cuda_blackscholes_demo_f32(const float* S, const float* X, const float* T, const float* r,

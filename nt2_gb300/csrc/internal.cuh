@@ -36,5 +36,9 @@ inline nt2cuda_status stream_scratch(cudaStream_t s, size_t bytes, void** out, i
   return from_cuda(nt2cuda::stream_scratch(s, bytes, out, slot));
 }
 
+// Load the single-request FP32 Black-Scholes kernels of one (cdf, precision)
+// pair ahead of their first launch (capi_transform.cu).
+void warm_blackscholes_f32(int cdf_kind, int precision);
+
 }  // namespace detail_capi
 }  // namespace nt2cuda

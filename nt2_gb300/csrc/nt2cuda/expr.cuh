@@ -38,7 +38,9 @@ struct normcdf_ {}; struct fastnormcdf_ {}; struct max_ {}; struct min_ {};
 struct adds_ {}; struct subs_ {}; struct selinc_ {}; struct seldec_ {}; struct if_else_ {};
 struct if_zero_else_one_ {}; struct is_less_ {}; struct is_greater_ {};
 struct is_less_equal_ {}; struct is_greater_equal_ {}; struct is_equal_ {};
-struct is_not_equal_ {}; struct oneminus_ {}; struct minusone_ {};
+struct is_not_equal_ {}; struct oneminus_ {}; struct minusone_ {}; struct cast_ {};
+// cast<uint8_t> of a float the statement keeps in [0, 256) (see trunc_u8 below)
+struct trunc_u8_ {};
 }  // namespace tag
 
 // ------------------------------------------------------------ tree nodes
@@ -130,6 +132,11 @@ NT2CUDA_UN(log_, math::log<F>(a))
 NT2CUDA_UN(erfc_, math::erfc<F>(a))
 NT2CUDA_UN(normcdf_, math::normcdf<F>(a))
 NT2CUDA_UN(fastnormcdf_, math::fastnormcdf<F>(a))
+// trunc_u8(y) = cast<uint8_t>(y) for a float y in [0, 256), where the cast truncates toward
+// zero: 2^23 + y rounded toward zero is 2^23 + floor(y), whose low byte is the result.
+// Used where the statement bounds y (rgb2grey's weights sum below 1); a full-rate add in
+// place of the quarter-rate float-to-integer conversion.
+NT2CUDA_UN(trunc_u8_, (uint8_t)(__float_as_uint(__fadd_rz((float)a, 8388608.0f)) & 0xFFu))
 // if_zero_else_one(c) = c ? 0 : 1 (boost/simd/boolean/functions/scalar/if_zero_else_one.hpp:28-50);
 // the result type is the caller's element type, carried by the node.
 #undef NT2CUDA_BIN
@@ -174,8 +181,28 @@ template <class A, class B, class C> struct tag_result<tag::if_else_, A, B, C> {
 template <class Tag, class... C> struct value_of<node<Tag, C...>> {
   using type = typename tag_result<Tag, typename value_of<C>::type...>::type;
 };
-// if_zero_else_one carries its result type in a scal<R> second child that is never read.
+// if_zero_else_one and cast carry their result type in a scal<R> second child that is never read.
 template <class A, class R> struct value_of<node<tag::if_zero_else_one_, A, scal<R>>> { using type = R; };
+template <class A, class R> struct value_of<node<tag::cast_, A, scal<R>>> { using type = R; };
+template <class A> struct tag_result<tag::trunc_u8_, A> { using type = uint8_t; };
+
+// nt2::cast<R>(x) (nt2/operator/functions/container/cast.hpp:133-150): integer -> floating goes
+// through tofloat, floating -> unsigned through touint then narrowing groups, floating -> signed
+// through toint; each of those is a plain C conversion of the scalar
+// (boost/simd/arithmetic/functions/scalar/touint.hpp:31-36, swar/functions/scalar/group.hpp:20-27).
+// Defined for values the target type (or its 32-bit widening) represents, as in NT2.
+template <class R, class A> __device__ __forceinline__ R cast_value(A a)
+{
+  if constexpr (std::is_same<R, float>::value && std::is_unsigned<A>::value && sizeof(A) < 4) {
+    // exact: 2^23 + a is a float whose low mantissa bits are a; subtracting 2^23 leaves a.
+    // An integer add and a float add instead of the quarter-rate integer-to-float conversion.
+    return __fsub_rn(__uint_as_float(0x4B000000u | (uint32_t)a), 8388608.0f);
+  } else if constexpr (std::is_floating_point<A>::value && std::is_integral<R>::value && sizeof(R) < 4) {
+    if constexpr (std::is_unsigned<R>::value) return (R)(uint32_t)a; else return (R)(int32_t)a;
+  } else {
+    return (R)a;
+  }
+}
 
 // Smallest element size among the terminals (drives the lane count).
 template <class E> struct min_elem;
@@ -228,6 +255,9 @@ template <class Tag, class A, class B, int V> struct regs<node<Tag, A, B>, V> {
     if constexpr (std::is_same<Tag, tag::if_zero_else_one_>::value) {
       using R = typename value_of<node<Tag, A, B>>::type;
       return ra.template get<F>(n.a, l) ? R(0) : R(1);
+    } else if constexpr (std::is_same<Tag, tag::cast_>::value) {
+      using R = typename value_of<node<Tag, A, B>>::type;
+      return cast_value<R>(ra.template get<F>(n.a, l));
     } else {
       return fn<Tag, F>::apply(ra.template get<F>(n.a, l), rb.template get<F>(n.b, l));
     }

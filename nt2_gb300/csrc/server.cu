@@ -51,13 +51,20 @@ struct req_desc {
   uint32_t pad;
 };
 
+// Small batches travel in the kernel's parameter block (no descriptor copy
+// before the launch); larger ones in a device buffer filled by one copy.
+constexpr int kInline = 16;
+struct inline_list {
+  req_desc d[kInline];
+  uint64_t tile_start[kInline + 1];
+};
+
 // One launch over all requests of a batch.  Each block takes tiles from the
 // work-list; tile_start[i] is the first tile of request i.  The per-option
 // arithmetic is bs_lane, the same function the single-request kernel uses,
 // so a request's results do not depend on what it was batched with.
 template <int CDF, int P>
-__global__ void __launch_bounds__(256) k_bs_batch(const req_desc* __restrict__ desc,
-                                                  const uint64_t* __restrict__ tile_start, int nreq)
+__device__ __forceinline__ void bs_batch_body(const req_desc* desc, const uint64_t* tile_start, int nreq)
 {
   __shared__ int s_req;
   const uint64_t total = tile_start[nreq];
@@ -97,6 +104,28 @@ __global__ void __launch_bounds__(256) k_bs_batch(const req_desc* __restrict__ d
       }
     }
   }
+}
+
+template <int CDF, int P>
+__global__ void __launch_bounds__(256) k_bs_batch(const req_desc* __restrict__ desc,
+                                                  const uint64_t* __restrict__ tile_start, int nreq)
+{
+  bs_batch_body<CDF, P>(desc, tile_start, nreq);
+}
+
+template <int CDF, int P>
+__global__ void __launch_bounds__(256) k_bs_batch_inline(const __grid_constant__ inline_list list, int nreq)
+{
+  bs_batch_body<CDF, P>(list.d, list.tile_start, nreq);
+}
+
+// Persistent grid of a batch kernel: resident blocks per SM x SMs, computed
+// once per instantiation (this also loads the kernel, so the first request
+// does not pay for lazy module loading).
+template <class K> int batch_grid(K kernel)
+{
+  static const int g = sm_count() * resident_blocks(kernel, 256);
+  return g;
 }
 
 // ------------------------------------------------------- device arena
@@ -195,6 +224,8 @@ struct nt2cuda_server {
   std::condition_variable cv_inflight;  // reaper: a batch was launched or stop
   nt2cuda_server_stats st{};
   nt2cuda_status worker_error = NT2CUDA_OK;
+  std::atomic<int> n_admitted{0};    // admitted.size(), readable without the lock
+  uint64_t spin_ns = 0;
 };
 
 namespace {
@@ -219,6 +250,7 @@ void admit_locked(nt2cuda_server* s)
     s->st.reserved_bytes = s->reserved;
     if (s->reserved > s->st.peak_reserved_bytes) s->st.peak_reserved_bytes = s->reserved;
     s->admitted.push_back(r.id);
+    s->n_admitted.store((int)s->admitted.size(), std::memory_order_release);
     s->waiting.pop_front();
   }
 }
@@ -265,18 +297,48 @@ void reaper_loop(nt2cuda_server* s)
 template <int CDF, int P>
 nt2cuda_status launch_batch(nt2cuda_server* s, slot& sl, int nreq)
 {
+  uint64_t tiles = sl.h_tiles[nreq];
+  if (nreq <= kInline) {
+    inline_list list;
+    for (int i = 0; i < nreq; ++i) { list.d[i] = sl.h_desc[i]; list.tile_start[i] = sl.h_tiles[i]; }
+    list.tile_start[nreq] = tiles;
+    uint64_t grid = (uint64_t)batch_grid(k_bs_batch_inline<CDF, P>);
+    if (grid > tiles) grid = tiles;
+    if (grid < 1) grid = 1;
+    k_bs_batch_inline<CDF, P><<<(unsigned)grid, 256, 0, sl.stream>>>(list, nreq);
+    (void)s;
+    return launch_status(cudaGetLastError());
+  }
   // descriptors [0, nreq) and tile starts [0, nreq] sit at fixed offsets of one buffer
   const size_t used = (size_t)((char*)(sl.h_tiles + nreq + 1) - sl.h_buf);
   cudaError_t e = cudaMemcpyAsync(sl.d_buf, sl.h_buf, used, cudaMemcpyHostToDevice, sl.stream);
   if (e != cudaSuccess) return from_cuda(e);
-  uint64_t tiles = sl.h_tiles[nreq];
-  int per_sm = resident_blocks(k_bs_batch<CDF, P>, 256);
-  uint64_t grid = (uint64_t)sm_count() * (uint64_t)per_sm;
+  uint64_t grid = (uint64_t)batch_grid(k_bs_batch<CDF, P>);
   if (grid > tiles) grid = tiles;
   if (grid < 1) grid = 1;
   k_bs_batch<CDF, P><<<(unsigned)grid, 256, 0, sl.stream>>>(sl.d_desc, sl.d_tiles, nreq);
-  (void)s;
-  return launch_status(cudaSuccess);
+  return launch_status(cudaGetLastError());
+}
+
+// Load (and size) the kernels this server will launch before the first request.
+template <int CDF, int P> void warm_batch()
+{
+  (void)batch_grid(k_bs_batch_inline<CDF, P>);
+  (void)batch_grid(k_bs_batch<CDF, P>);
+}
+
+void warm(const nt2cuda_server_config& c)
+{
+  if (c.coalesce) {
+    if (c.cdf_kind == CDF_FASTNORMCDF)
+      c.fused == PREC_FAST ? warm_batch<CDF_FASTNORMCDF, PREC_FAST>()
+      : c.fused == PREC_FUSED ? warm_batch<CDF_FASTNORMCDF, PREC_FUSED>() : warm_batch<CDF_FASTNORMCDF, PREC_EXACT>();
+    else
+      c.fused == PREC_FAST ? warm_batch<CDF_NORMCDF, PREC_FAST>()
+      : c.fused == PREC_FUSED ? warm_batch<CDF_NORMCDF, PREC_FUSED>() : warm_batch<CDF_NORMCDF, PREC_EXACT>();
+  } else {
+    warm_blackscholes_f32(c.cdf_kind, c.fused);
+  }
 }
 
 nt2cuda_status launch_single(nt2cuda_server* s, slot& sl, const req_desc& d)
@@ -292,6 +354,13 @@ void worker_loop(nt2cuda_server* s)
   cudaSetDevice(s->device);
   const int maxb = s->cfg.coalesce ? std::max(1, s->cfg.max_batch_requests) : 1;
   for (;;) {
+    // poll briefly before sleeping: a request that arrives within spin_ns is
+    // launched without waiting for the thread to be woken
+    if (s->spin_ns && s->n_admitted.load(std::memory_order_acquire) == 0) {
+      const uint64_t until = now_ns() + s->spin_ns;
+      while (s->n_admitted.load(std::memory_order_acquire) == 0 && now_ns() < until) {
+      }
+    }
     std::unique_lock<std::mutex> lk(s->m);
     int si = -1;
     s->cv_work.wait(lk, [&] {
@@ -316,6 +385,7 @@ void worker_loop(nt2cuda_server* s)
       b->ids.push_back(r.id);
       ++nreq;
     }
+    s->n_admitted.store((int)s->admitted.size(), std::memory_order_release);
     sl.h_tiles[nreq] = tiles;
     sl.busy = true;
     s->st.batches++;
@@ -384,11 +454,13 @@ nt2cuda_status nt2cuda_server_create(const nt2cuda_server_config* cfg, nt2cuda_s
   *out = nullptr;
   if (cfg->budget_bytes < 4096 || cfg->max_inflight_batches < 1 || cfg->max_inflight_batches > 16 ||
       cfg->max_batch_requests < 1 || cfg->max_batch_requests > (1 << 20) ||
-      (cfg->cdf_kind != CDF_NORMCDF && cfg->cdf_kind != CDF_FASTNORMCDF) || cfg->fused < 0 || cfg->fused > 2)
+      (cfg->cdf_kind != CDF_NORMCDF && cfg->cdf_kind != CDF_FASTNORMCDF) || cfg->fused < 0 || cfg->fused > 2 ||
+      cfg->spin_us > 100000)
     return NT2CUDA_ERR_ARG;
   nt2cuda_server* s = new nt2cuda_server();
   s->cfg = *cfg;
   if (s->cfg.wait_timeout_ms <= 0) s->cfg.wait_timeout_ms = 60000;
+  s->spin_ns = cfg->spin_us < 0 ? 0 : (uint64_t)(cfg->spin_us == 0 ? 50 : cfg->spin_us) * 1000;
   cudaGetDevice(&s->device);
   if (!s->mem.init(cfg->budget_bytes)) { delete s; return NT2CUDA_ERR_OOM; }
   s->slots.resize((size_t)cfg->max_inflight_batches);
@@ -407,6 +479,7 @@ nt2cuda_status nt2cuda_server_create(const nt2cuda_server_config* cfg, nt2cuda_s
     sl.d_desc = (req_desc*)sl.d_buf;
     sl.d_tiles = (uint64_t*)(sl.d_buf + desc_bytes);
   }
+  warm(s->cfg);
   s->worker = std::thread(worker_loop, s);
   s->reaper = std::thread(reaper_loop, s);
   *out = s;

@@ -7,7 +7,8 @@
 //   sdot       demo/sdot/nt2/sdot_nt2.cpp:35-38
 //   bs         demo/blackscholes/nt2/blackandscholes_nt2.cpp:53-60
 //   bs_merged  demo/blackscholes/nt2_merged/blackandscholes_nt2_merged.cpp:57-64
-//   rgb2grey   demo/rgb2grey/nt2/rgb2grey_nt2.cpp:42-45
+//   rgb2grey   demo/rgb2grey/nt2/rgb2grey_nt2.cpp:42-45 (float, and uint8 planes through nt2::cast)
+//   rgb2yuv    demo/rgb2yuv/nt2/rgb2yuv_nt2.cpp:28-33
 //   sigmadelta demo/sigmadelta/nt2/sigmadelta_nt2.cpp:37-58, 100-106
 #include <cstdio>
 #include <cstdlib>
@@ -106,6 +107,27 @@ int main(int argc, char** argv)
     load(b, read_file<T>(argv[5], n));
     gr = T(0.3) * r + T(0.59) * g + T(0.11) * b;
     write_table(argv[6], gr);
+  } else if (cmd == "rgb2grey_u8") {                      // in: r g b (uint8) ; out: gr (uint8)
+    typedef unsigned char T;
+    nt2::table<T> r(nt2::of_size(n)), g(nt2::of_size(n)), b(nt2::of_size(n)), gr(nt2::of_size(n));
+    load(r, read_file<T>(argv[3], n));
+    load(g, read_file<T>(argv[4], n));
+    load(b, read_file<T>(argv[5], n));
+    gr = nt2::cast<T>(0.3f * nt2::cast<float>(r) + 0.59f * nt2::cast<float>(g) + 0.11f * nt2::cast<float>(b));
+    write_table(argv[6], gr);
+  } else if (cmd == "rgb2yuv") {                          // in: r g b ; out: y u v
+    typedef float K;
+    nt2::table<K> r(nt2::of_size(n)), g(nt2::of_size(n)), b(nt2::of_size(n));
+    nt2::table<K> y(nt2::of_size(n)), u(nt2::of_size(n)), v(nt2::of_size(n));
+    load(r, read_file<K>(argv[3], n));
+    load(g, read_file<K>(argv[4], n));
+    load(b, read_file<K>(argv[5], n));
+    y = K(0.299f) * r + K(0.587f) * g + K(0.114f) * b;
+    u = K(0.492f) * (b - y);
+    v = K(0.877f) * (r - y);
+    write_table(argv[6], y);
+    write_table(argv[7], u);
+    write_table(argv[8], v);
   } else if (cmd == "sigmadelta") {                       // n = pixels; argv[3] = frames; in: frames ; out: bkg var label
     typedef unsigned char T;
     const int nb_frames = std::atoi(argv[3]);

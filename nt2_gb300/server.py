@@ -16,10 +16,11 @@ class Server:
 
     def __init__(self, budget_bytes: int = 40 << 30, max_batch_requests: int = 4096,
                  max_inflight_batches: int = 3, coalesce: bool = True, fused: bool = False,
-                 cdf: str = "normcdf", wait_timeout_ms: int = 60000, precision: str | None = None):
+                 cdf: str = "normcdf", wait_timeout_ms: int = 60000, precision: str | None = None,
+                 spin_us: int = 0):
         prec = {"exact": 0, "fused": 1, "fast": 2}[precision] if precision else int(fused)
         cfg = ServerConfig(budget_bytes, max_batch_requests, max_inflight_batches, int(coalesce), prec,
-                           {"normcdf": 0, "fastnormcdf": 1}[cdf], wait_timeout_ms)
+                           {"normcdf": 0, "fastnormcdf": 1}[cdf], wait_timeout_ms, spin_us)
         self._h = C.c_void_p()
         check(lib().nt2cuda_server_create(C.byref(cfg), C.byref(self._h)), "server_create")
 

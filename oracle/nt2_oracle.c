@@ -8,7 +8,7 @@
  *
  * What it restates (paths relative to the NT2 source tree):
  *   - the Boost.SIMD / NT2 math functors used by the saxpy, sdot,
- *     Black-Scholes, rgb2grey and sigmadelta expressions, in the form that
+ *     Black-Scholes, rgb2grey, rgb2yuv, mandelbrot and sigmadelta expressions, in the form that
  *     NT2's SIMD transform body evaluates (the simd/common/... files), with
  *     the generic unfused fma/fnms (a*b+c rounded twice,
  *     modules/boost/simd/base/include/boost/simd/arithmetic/functions/generic/fma.hpp:32,
@@ -488,6 +488,103 @@ EXPORT void nt2o_rgb2grey_f(const float* r, const float* g, const float* b, floa
 {
   NT2_SPAWN(n, sizeof(float), threads,
             gr[i] = (0.3f * r[i] + 0.59f * g[i]) + 0.11f * b[i]);
+}
+
+/* rgb2grey over uint8 planes: the float statement between nt2::cast<float> and
+ * nt2::cast<uint8_t> (nt2/operator/functions/container/cast.hpp:133-150; tofloat is
+ * exact, touint and group are C conversions, so truncation toward zero on [0, 255]). */
+EXPORT void nt2o_rgb2grey_u8(const uint8_t* r, const uint8_t* g, const uint8_t* b, uint8_t* gr,
+                             size_t n, int threads)
+{
+  NT2_SPAWN(n, sizeof(uint8_t), threads,
+            gr[i] = (uint8_t)(uint32_t)((0.3f * (float)r[i] + 0.59f * (float)g[i]) + 0.11f * (float)b[i]));
+}
+
+/* rgb2yuv: three statements (demo/rgb2yuv/nt2/rgb2yuv_nt2.cpp:28-33), each a full pass
+ * as NT2 evaluates them:  y = 0.299f*r + 0.587f*g + 0.114f*b;  u = 0.492f*(b - y);
+ * v = 0.877f*(r - y). */
+EXPORT void nt2o_rgb2yuv_f(const float* r, const float* g, const float* b, float* y, float* u, float* v,
+                           size_t n, int threads)
+{
+  NT2_SPAWN(n, sizeof(float), threads, y[i] = (0.299f * r[i] + 0.587f * g[i]) + 0.114f * b[i]);
+  NT2_SPAWN(n, sizeof(float), threads, u[i] = 0.492f * (b[i] - y[i]));
+  NT2_SPAWN(n, sizeof(float), threads, v[i] = 0.877f * (r[i] - y[i]));
+}
+
+/* linspace(lo, hi, n): step = (hi-lo)/float(n-1); element p is hi at p = n-1, else
+ * fma(p, step, lo) with the generic unfused fma
+ * (modules/core/generative/include/nt2/core/functions/details/linspace.hpp:27-45). */
+EXPORT void nt2o_linspace_f(float lo, float hi, size_t n, float* out)
+{
+  if (!n) return;
+  float step = (hi - lo) / (float)(n - 1);
+  for (size_t p = 0; p < n; ++p) out[p] = (p == n - 1) ? hi : (float)p * step + lo;
+}
+
+/* The mandelbrot demo's step functor (demo/mandelbrot/nt2/mandelbrot_nt2.cpp:55-81) on
+ * one pack of `w` lanes: iterate the whole pack until no lane has |z|^2 < 4 (taken
+ * before the update) or 256 trips; each lane counts the trips on which it held. */
+static void mandel_pack(const float* a, const float* b, int32_t* out, int w)
+{
+  float x[32], y[32];
+  int32_t it[32];
+  for (int l = 0; l < w; ++l) { x[l] = 0.f; y[l] = 0.f; it[l] = 0; }
+  for (int i = 0; i < 256; ++i) {
+    int any = 0;
+    for (int l = 0; l < w; ++l) {
+      float x2 = x[l] * x[l];
+      float y2 = y[l] * y[l];
+      float xy = 2.0f * x[l] * y[l];
+      x[l] = x2 - y2 + a[l];
+      y[l] = xy + b[l];
+      float m2 = x2 + y2;
+      int mask = m2 < 4.0f;
+      it[l] += mask;
+      any |= mask;
+    }
+    if (!any) break;
+  }
+  for (int l = 0; l < w; ++l) out[l] = it[l];
+}
+
+/* C = arrayfun(step, A, B) with NT2's transform skeleton: packs of `pack` elements
+ * from index 0, then the n % pack tail one element at a time
+ * (modules/core/base/include/nt2/core/functions/simd/transform.hpp:40-57). */
+EXPORT int nt2o_mandelbrot_f(const float* A, const float* B, int32_t* C, size_t n, int pack, int threads)
+{
+  if (pack < 1 || pack > 32) return -1;
+  size_t np = n / (size_t)pack, nfull = np * (size_t)pack;
+#ifdef _OPENMP
+  int th = threads > 0 ? threads : omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 16) num_threads(th)
+#endif
+  for (ptrdiff_t k = 0; k < (ptrdiff_t)np; ++k)
+    mandel_pack(A + (size_t)k * pack, B + (size_t)k * pack, C + (size_t)k * pack, pack);
+  for (size_t e = nfull; e < n; ++e) mandel_pack(A + e, B + e, C + e, 1);
+  (void)threads;
+  return 0;
+}
+
+/* The demo's program: A = expand_to(linspace(a0,a1,w),h,w), B = expand_to(colvect(linspace(b0,b1,h)),h,w)
+ * (mandelbrot_nt2.cpp:107-108), column-major, then C = arrayfun(step, A, B). */
+EXPORT int nt2o_mandelbrot_grid_f(float a0, float a1, float b0, float b1, size_t h, size_t w, int32_t* C,
+                                  int pack, int threads)
+{
+  size_t n = h * w;
+  float* la = (float*)malloc((w ? w : 1) * sizeof(float));
+  float* lb = (float*)malloc((h ? h : 1) * sizeof(float));
+  float* A = (float*)malloc((n ? n : 1) * sizeof(float));
+  float* B = (float*)malloc((n ? n : 1) * sizeof(float));
+  int rc = -1;
+  if (la && lb && A && B) {
+    nt2o_linspace_f(a0, a1, w, la);
+    nt2o_linspace_f(b0, b1, h, lb);
+    for (size_t j = 0; j < w; ++j)
+      for (size_t i = 0; i < h; ++i) { A[i + j * h] = la[j]; B[i + j * h] = lb[i]; }
+    rc = nt2o_mandelbrot_f(A, B, C, n, pack, threads);
+  }
+  free(la); free(lb); free(A); free(B);
+  return rc;
 }
 
 /* Black-Scholes call and put, written as the NT2 table expression

@@ -20,6 +20,7 @@ _libs = {}
 f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
 sz = C.c_size_t
 
 SIGS = {
@@ -43,6 +44,11 @@ SIGS = {
     "nt2o_saxpy_f": (None, [C.c_float, f32p, f32p, sz, C.c_int]),
     "nt2o_saxpy_d": (None, [C.c_double, f64p, f64p, sz, C.c_int]),
     "nt2o_rgb2grey_f": (None, [f32p, f32p, f32p, f32p, sz, C.c_int]),
+    "nt2o_rgb2grey_u8": (None, [u8p, u8p, u8p, u8p, sz, C.c_int]),
+    "nt2o_rgb2yuv_f": (None, [f32p, f32p, f32p, f32p, f32p, f32p, sz, C.c_int]),
+    "nt2o_linspace_f": (None, [C.c_float, C.c_float, sz, f32p]),
+    "nt2o_mandelbrot_f": (C.c_int, [f32p, f32p, i32p, sz, C.c_int, C.c_int]),
+    "nt2o_mandelbrot_grid_f": (C.c_int, [C.c_float, C.c_float, C.c_float, C.c_float, sz, sz, i32p, C.c_int, C.c_int]),
     "nt2o_bs_f": (None, [f32p, f32p, f32p, C.c_float, C.c_float, f32p, f32p, sz, C.c_int, C.c_int]),
     "nt2o_bs_d": (None, [f64p, f64p, f64p, C.c_double, C.c_double, f64p, f64p, sz, C.c_int]),
     "nt2o_bs_demo_f": (None, [f32p, f32p, f32p, f32p, f32p, f32p, sz, C.c_int]),
@@ -149,3 +155,27 @@ def dot_fp64(x, y):
     a = C.c_double()
     s = load().nt2o_dot_fp64_f(x, y, x.size, C.byref(a))
     return s, a.value
+
+
+def rgb2yuv(r, g, b, threads: int = 0):
+    y, u, v = (np.empty_like(r) for _ in range(3))
+    load().nt2o_rgb2yuv_f(r, g, b, y, u, v, r.size, threads)
+    return y, u, v
+
+
+def mandelbrot(A, B, pack: int = 8, threads: int = 0):
+    C_ = np.empty(A.size, np.int32)
+    assert load().nt2o_mandelbrot_f(np.ascontiguousarray(A), np.ascontiguousarray(B), C_, A.size, pack, threads) == 0
+    return C_
+
+
+def mandelbrot_grid(a0, a1, b0, b1, h, w, pack: int = 8, threads: int = 0):
+    C_ = np.empty(h * w, np.int32)
+    assert load().nt2o_mandelbrot_grid_f(a0, a1, b0, b1, h, w, C_, pack, threads) == 0
+    return C_
+
+
+def linspace(lo, hi, n):
+    out = np.empty(max(n, 1), np.float32)
+    load().nt2o_linspace_f(lo, hi, n, out)
+    return out[:n]

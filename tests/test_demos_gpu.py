@@ -78,6 +78,25 @@ def test_rgb2grey_demo(demos, oracle, tmp_path):
     assert np.array_equal(np.fromfile(o, np.float32).view(np.uint32), ref.view(np.uint32))
 
 
+def test_rgb2grey_u8_demo(demos, oracle, tmp_path):
+    n = 640 * 480 + 5
+    rng = np.random.default_rng(6)
+    r, g, b = (rng.integers(0, 256, n, dtype=np.uint8) for _ in range(3))
+    _, (o,) = run(demos, tmp_path, "rgb2grey_u8", n, [r, g, b], 1)
+    ref = np.empty_like(r)
+    oracle.load().nt2o_rgb2grey_u8(r, g, b, ref, n, 1)
+    assert np.array_equal(np.fromfile(o, np.uint8), ref)
+
+
+def test_rgb2yuv_demo(demos, oracle, tmp_path):
+    n = 128 * 128 + 3
+    rng = np.random.default_rng(7)
+    r, g, b = (rng.uniform(0, 255, n).astype(np.float32) for _ in range(3))
+    _, outs = run(demos, tmp_path, "rgb2yuv", n, [r, g, b], 3)
+    for o, ref in zip(outs, oracle.rgb2yuv(r, g, b)):
+        assert np.array_equal(np.fromfile(o, np.float32).view(np.uint32), ref.view(np.uint32))
+
+
 def test_sigmadelta_demo(demos, oracle, tmp_path):
     npix, nf = 333 * 97, 6
     rng = np.random.default_rng(5)
