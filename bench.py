@@ -204,7 +204,9 @@ def cpu_baseline(sample: int = 1 << 22, seconds: float = 3.0):
 # -------------------------------------------------------------- serving
 def serving_bench(seconds: float = 1.0, rates=(1000, 10000, 50000), seed: int = 7):
     """Poisson arrivals of Black-Scholes requests (sizes log-uniform 256..2^22 options) into the
-    continuous-batching server and into a one-launch-per-request server on the same GPU."""
+    continuous-batching server and into a one-launch-per-request server on the same GPU.  The
+    trace is replayed natively (nt2cuda_server_replay): arrivals, completion waits and releases
+    run in C++ threads, so the numbers are the server's, not a Python client's."""
     import numpy as np
     import torch
     from nt2_gb300.server import Server
@@ -212,92 +214,36 @@ def serving_bench(seconds: float = 1.0, rates=(1000, 10000, 50000), seed: int = 
     S, K, T = bs_tables(pool_n, seed=99)
     torch.cuda.synchronize()
     rng = np.random.default_rng(seed)
+    sp, kp, tp = S.data_ptr(), K.data_ptr(), T.data_ptr()
     out = {}
-    # The arrival loop busy-waits in Python while the client thread collects and releases
-    # results; with the default 5 ms GIL switch interval the client would get the
-    # interpreter about once per 5 ms, release outputs late and let the 40 GB budget fill.
-    switch = sys.getswitchinterval()
-    sys.setswitchinterval(2e-5)
-    try:
-        return _serving(np, Server, S, K, T, pool_n, rng, out, seconds, rates, seed)
-    finally:
-        sys.setswitchinterval(switch)
 
-
-def _serving(np, Server, S, K, T, pool_n, rng, out, seconds, rates, seed):
-    def run(mode, rate, dur):
+    def replay(mode, sizes, offs, arrivals):
         coalesce = mode == "batched"
         srv = Server(budget_bytes=40 << 30, max_batch_requests=4096, max_inflight_batches=3 if coalesce else 1,
                      coalesce=coalesce)
-        nreq = max(8, int(rate * dur))
-        sizes = np.exp(rng.uniform(math.log(256), math.log(1 << 22), nreq)).astype(np.int64)
-        offs = (rng.integers(0, pool_n - (1 << 22), nreq) // 4) * 4
-        gaps = rng.exponential(1.0 / rate, nreq) if rate else np.zeros(nreq)
-        tickets = []
-        lat = []
-        done = threading.Event()
-        sp, kp, tp = S.data_ptr(), K.data_ptr(), T.data_ptr()
-
-        def reaper():
-            i = 0
-            while i < nreq:
-                while i >= len(tickets):
-                    time.sleep(0)
-                t = tickets[i]
-                srv.wait(t, 120000)
-                lat.append(srv.latency_ns(t))
-                srv.release(t)
-                i += 1
-            done.set()
-
-        th = threading.Thread(target=reaper, daemon=True)
-        th.start()
-        t0 = time.perf_counter()
-        next_t = t0
-        for i in range(nreq):
-            next_t += gaps[i]
-            while time.perf_counter() < next_t:
-                pass
-            o = int(offs[i]) * 4
-            tickets.append(srv.submit_ptr(sp + o, kp + o, tp + o, R, SIGMA, int(sizes[i])))
-        done.wait(300)
-        t1 = time.perf_counter()
+        lat, elapsed = srv.replay(sp, kp, tp, R, SIGMA, offs, sizes, arrivals)
         st = srv.stats()
         srv.close()
-        lat_us = np.array(lat) / 1e3
-        return {"requests": nreq, "options_per_s": float(sizes.sum() / (t1 - t0)),
+        lat_us = lat.astype(np.float64) / 1e3
+        return {"requests": int(sizes.size), "options_per_s": float(sizes.sum() / elapsed),
                 "p50_us": float(np.percentile(lat_us, 50)), "p99_us": float(np.percentile(lat_us, 99)),
                 "launches": int(st["launches"]), "batches": int(st["batches"]),
                 "admission_waits": int(st["admission_waits"]),
                 "peak_reserved_gb": round(st["peak_reserved_bytes"] / 1e9, 2)}
 
     for rate in rates:
-        out[f"{rate}_req_s"] = {m: run(m, rate, seconds) for m in ("batched", "launch_per_request")}
-    # saturation: all requests offered at once (small requests, where launch cost dominates)
+        nreq = max(8, int(rate * seconds))
+        sizes = np.exp(rng.uniform(math.log(256), math.log(1 << 22), nreq)).astype(np.uint64)
+        offs = ((rng.integers(0, pool_n - (1 << 22), nreq) // 4) * 4).astype(np.uint64)
+        arrivals = (np.cumsum(rng.exponential(1.0 / rate, nreq)) * 1e9).astype(np.uint64)
+        out[f"{rate}_req_s"] = {m: replay(m, sizes, offs, arrivals) for m in ("batched", "launch_per_request")}
+    # saturation: every request offered at once (small requests, where launch cost dominates)
     sat_rng = np.random.default_rng(seed + 1)
-
-    def saturate(mode, nreq=20000, lo=256, hi=1 << 14):
-        coalesce = mode == "batched"
-        srv = Server(budget_bytes=40 << 30, max_batch_requests=4096, max_inflight_batches=3 if coalesce else 1,
-                     coalesce=coalesce)
-        sizes = np.exp(sat_rng.uniform(math.log(lo), math.log(hi), nreq)).astype(np.int64)
-        offs = (sat_rng.integers(0, pool_n - hi, nreq) // 4) * 4
-        sp, kp, tp = S.data_ptr(), K.data_ptr(), T.data_ptr()
-        t0 = time.perf_counter()
-        ts = [srv.submit_ptr(sp + int(o) * 4, kp + int(o) * 4, tp + int(o) * 4, R, SIGMA, int(n))
-              for o, n in zip(offs, sizes)]
-        srv.drain(300000)
-        t1 = time.perf_counter()
-        lat = np.array([srv.latency_ns(t) for t in ts]) / 1e3
-        for t in ts:
-            srv.release(t)
-        st = srv.stats()
-        srv.close()
-        return {"requests": nreq, "options_per_s": float(sizes.sum() / (t1 - t0)),
-                "p50_us": float(np.percentile(lat, 50)), "p99_us": float(np.percentile(lat, 99)),
-                "launches": int(st["launches"])}
-
-    sat = {m: saturate(m) for m in ("batched", "launch_per_request")}
+    nreq, lo, hi = 20000, 256, 1 << 14
+    sizes = np.exp(sat_rng.uniform(math.log(lo), math.log(hi), nreq)).astype(np.uint64)
+    offs = ((sat_rng.integers(0, pool_n - hi, nreq) // 4) * 4).astype(np.uint64)
+    zero = np.zeros(nreq, np.uint64)
+    sat = {m: replay(m, sizes, offs, zero) for m in ("batched", "launch_per_request")}
     sat["throughput_ratio"] = sat["batched"]["options_per_s"] / sat["launch_per_request"]["options_per_s"]
     out["saturation_small_requests"] = sat
     return out
@@ -512,6 +458,8 @@ def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: in
         gen.manual_seed(5)
         sets = [[torch.randint(0, 256, (n,), dtype=torch.uint8, device="cuda", generator=gen) for _ in range(4)]
                 for _ in range(2)]
+        if autotune:
+            api.autotune("rgb2grey_u8", n)
         it = [0]
 
         def grey_step():

@@ -296,6 +296,18 @@ nt2cuda_status nt2cuda_server_release(nt2cuda_server* server, uint64_t ticket);
 nt2cuda_status nt2cuda_server_latency_ns(nt2cuda_server* server, uint64_t ticket, uint64_t* ns);
 nt2cuda_status nt2cuda_server_drain(nt2cuda_server* server, int timeout_ms);
 nt2cuda_status nt2cuda_server_get_stats(nt2cuda_server* server, nt2cuda_server_stats* stats);
+/* Open-loop replay of a request trace, driven natively: request i (inputs
+ * S/K/T + offsets[i] elements, sizes[i] options) is submitted arrival_ns[i]
+ * after the call starts; a collector thread waits for the requests in
+ * submission order, stores each one's submit-to-completion latency in
+ * latency_ns[i] and releases it at once.  Returns when every request is
+ * released, or with the first failing status; *elapsed_ns is the time from
+ * the start to the last completion.  Measures the server without a client's
+ * own overheads (capacity planning, the serving benchmark). */
+nt2cuda_status nt2cuda_server_replay(nt2cuda_server* server, const float* S, const float* K, const float* T,
+                                     float r, float sigma, size_t nreq, const uint64_t* offsets,
+                                     const uint64_t* sizes, const uint64_t* arrival_ns, uint64_t* latency_ns,
+                                     uint64_t* elapsed_ns);
 
 /* ------------------------------------------------------------ tuning ---- */
 /* Times the launch variants of one entry point at size n on scratch tables
@@ -303,7 +315,7 @@ nt2cuda_status nt2cuda_server_get_stats(nt2cuda_server* server, nt2cuda_server_s
  * "saxpy_f64", "bs_f32", "bs_f32_fused", "bs_f32_fast", "bs_f64",
  * "bs_f64_fused" (the Black-Scholes keys are per precision mode), and
  * "bs_f32_mapped", "bs_f32_fast_mapped" (the kernel on pinned host tables,
- * as nt2cuda_blackscholes_f32_host runs it). */
+ * as nt2cuda_blackscholes_f32_host runs it), "rgb2grey_u8". */
 nt2cuda_status nt2cuda_autotune(const char* kernel, size_t n, int* best_unroll, int* best_waves, float* best_ms);
 /* Tuning table as text ("key@bucket unroll waves" lines). */
 nt2cuda_status nt2cuda_tuning_export(char* buf, size_t cap, size_t* needed);

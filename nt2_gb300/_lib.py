@@ -115,6 +115,7 @@ _SIGS = {
     "nt2cuda_server_latency_ns": (c_int, [c_vp, c_u64, C.POINTER(c_u64)]),
     "nt2cuda_server_drain": (c_int, [c_vp, c_int]),
     "nt2cuda_server_get_stats": (c_int, [c_vp, C.POINTER(ServerStats)]),
+    "nt2cuda_server_replay": (c_int, [c_vp, c_vp, c_vp, c_vp, c_f, c_f, c_size, c_vp, c_vp, c_vp, c_vp, c_vp]),
 }
 
 

@@ -430,7 +430,8 @@ nt2cuda_status nt2cuda_autotune(const char* kernel, size_t n, int* best_unroll, 
   if (!kernel || n == 0) return NT2CUDA_ERR_ARG;
   std::string k(kernel);
   const bool f64 = (k == "bs_f64" || k == "bs_f64_fused" || k == "saxpy_f64");
-  const size_t es = f64 ? 8 : 4;
+  const bool grey8 = (k == "rgb2grey_u8");
+  const size_t es = f64 ? 8 : (grey8 ? 1 : 4);
   int prec = PREC_EXACT;
   if (k == "bs_f32_fused" || k == "bs_f64_fused") prec = PREC_FUSED;
   if (k == "bs_f32_fast" || k == "bs_f32_fast_mapped") prec = PREC_FAST;
@@ -438,7 +439,7 @@ nt2cuda_status nt2cuda_autotune(const char* kernel, size_t n, int* best_unroll, 
   const bool mapped = (k == "bs_f32_mapped" || k == "bs_f32_fast_mapped");
   const bool bs32 = (k == "bs_f32" || k == "bs_f32_fused" || k == "bs_f32_fast" || mapped);
   const bool bs64 = (k == "bs_f64" || k == "bs_f64_fused");
-  if (!(bs32 || bs64 || k == "saxpy_f32" || k == "saxpy_f64")) return NT2CUDA_ERR_ARG;
+  if (!(bs32 || bs64 || grey8 || k == "saxpy_f32" || k == "saxpy_f64")) return NT2CUDA_ERR_ARG;
   void* buf[5] = {};
   for (int j = 0; j < 5; ++j) {
     cudaError_t e = mapped ? cudaMallocHost(&buf[j], n * es) : cudaMalloc(&buf[j], n * es);
@@ -449,7 +450,9 @@ nt2cuda_status nt2cuda_autotune(const char* kernel, size_t n, int* best_unroll, 
   }
   cudaStream_t s;
   cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
-  if (f64) {
+  if (grey8) {
+    for (int j = 0; j < 3; ++j) cudaMemsetAsync(buf[j], 0x5a + 40 * j, n, s);
+  } else if (f64) {
     nt2cuda_fill_uniform_f64((double*)buf[0], n, 5.0, 30.0, 1, s);
     nt2cuda_fill_uniform_f64((double*)buf[1], n, 1.0, 100.0, 2, s);
     nt2cuda_fill_uniform_f64((double*)buf[2], n, 0.25, 10.0, 3, s);
@@ -477,6 +480,9 @@ nt2cuda_status nt2cuda_autotune(const char* kernel, size_t n, int* best_unroll, 
                                      (double*)buf[3], (double*)buf[4], n, CDF_NORMCDF, prec, s, unrolls[ui],
                                      wavesv[wi]);
         tuning::set(k.c_str(), n, tuning::params{unrolls[ui], wavesv[wi]});
+        if (grey8)
+          return nt2cuda_rgb2grey_u8((const uint8_t*)buf[0], (const uint8_t*)buf[1], (const uint8_t*)buf[2],
+                                     (uint8_t*)buf[3], n, 0, s);
         if (k == "saxpy_f32") return nt2cuda_saxpy_f32(2.5f, (float*)buf[0], (float*)buf[1], n, 0, s);
         return nt2cuda_saxpy_f64(2.5, (double*)buf[0], (double*)buf[1], n, 0, s);
       };

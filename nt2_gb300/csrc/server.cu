@@ -616,4 +616,45 @@ nt2cuda_status nt2cuda_server_get_stats(nt2cuda_server* s, nt2cuda_server_stats*
   return NT2CUDA_OK;
 }
 
+nt2cuda_status nt2cuda_server_replay(nt2cuda_server* s, const float* S, const float* K, const float* T, float r,
+                                     float sigma, size_t nreq, const uint64_t* offsets, const uint64_t* sizes,
+                                     const uint64_t* arrival_ns, uint64_t* latency_ns, uint64_t* elapsed_ns)
+{
+  if (!s || !S || !K || !T || (nreq && (!offsets || !sizes || !arrival_ns || !latency_ns)) || !elapsed_ns)
+    return NT2CUDA_ERR_ARG;
+  std::vector<uint64_t> tickets(nreq);
+  std::atomic<size_t> submitted{0};
+  std::atomic<int> err{NT2CUDA_OK};
+  std::atomic<uint64_t> t_last{0};
+  const uint64_t t0 = now_ns();
+  std::thread collector([&] {
+    for (size_t i = 0; i < nreq; ++i) {
+      while (submitted.load(std::memory_order_acquire) <= i) {
+        if (err.load(std::memory_order_acquire) != NT2CUDA_OK) return;
+        std::this_thread::yield();
+      }
+      const uint64_t t = tickets[i];
+      nt2cuda_status st = nt2cuda_server_wait(s, t, -1, nullptr, nullptr);
+      if (st == NT2CUDA_OK) st = nt2cuda_server_latency_ns(s, t, &latency_ns[i]);
+      if (st == NT2CUDA_OK) st = nt2cuda_server_release(s, t);
+      if (st != NT2CUDA_OK) { int ok = NT2CUDA_OK; err.compare_exchange_strong(ok, (int)st); return; }
+      t_last.store(now_ns(), std::memory_order_release);
+    }
+  });
+  for (size_t i = 0; i < nreq && err.load(std::memory_order_acquire) == NT2CUDA_OK; ++i) {
+    const uint64_t due = t0 + arrival_ns[i];
+    while (now_ns() < due) {
+    }
+    uint64_t t = 0;
+    nt2cuda_status st = nt2cuda_server_submit(s, S + offsets[i], K + offsets[i], T + offsets[i], r, sigma,
+                                              (size_t)sizes[i], &t);
+    if (st != NT2CUDA_OK) { int ok = NT2CUDA_OK; err.compare_exchange_strong(ok, (int)st); break; }
+    tickets[i] = t;
+    submitted.store(i + 1, std::memory_order_release);
+  }
+  collector.join();
+  *elapsed_ns = t_last.load() > t0 ? t_last.load() - t0 : 0;
+  return (nt2cuda_status)err.load();
+}
+
 }  // extern "C"

@@ -60,6 +60,20 @@ class Server:
     def drain(self, timeout_ms: int = -1) -> None:
         check(lib().nt2cuda_server_drain(self._h, timeout_ms), "server_drain")
 
+    def replay(self, S: int, K: int, T: int, r: float, sigma: float, offsets, sizes, arrival_ns):
+        """Replay a trace natively (nt2cuda_server_replay): request i uses the tables at device
+        addresses S/K/T + 4*offsets[i] with sizes[i] options and arrives arrival_ns[i] after the start.
+        Returns (per-request latency in ns as a numpy array, elapsed seconds)."""
+        import numpy as np
+        off = np.ascontiguousarray(offsets, dtype=np.uint64)
+        siz = np.ascontiguousarray(sizes, dtype=np.uint64)
+        arr = np.ascontiguousarray(arrival_ns, dtype=np.uint64)
+        lat = np.zeros(off.size, dtype=np.uint64)
+        el = C.c_uint64()
+        check(lib().nt2cuda_server_replay(self._h, S, K, T, r, sigma, off.size, off.ctypes.data, siz.ctypes.data,
+                                          arr.ctypes.data, lat.ctypes.data, C.byref(el)), "server_replay")
+        return lat, el.value * 1e-9
+
     def stats(self) -> dict:
         s = ServerStats()
         check(lib().nt2cuda_server_get_stats(self._h, C.byref(s)), "server_stats")

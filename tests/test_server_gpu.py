@@ -126,3 +126,39 @@ def test_concurrent_submitters(gpu, oracle):
     for (o, n), (c, p) in results.items():
         ca, pa = gpu.blackscholes(S[o:o + n], K[o:o + n], T[o:o + n], 0.02, 0.30)
         assert torch.equal(c, ca) and torch.equal(p, pa)
+
+
+def test_replay_trace(gpu, cuda_lib):
+    """Native trace replay: every request completes, is released, and has a latency."""
+    import numpy as np
+    from nt2_gb300.server import Server
+    n = 1 << 20
+    S, K, T = (torch.empty(n, device="cuda") for _ in range(3))
+    gpu.fill_uniform(S, 5, 30, 1)
+    gpu.fill_uniform(K, 1, 100, 2)
+    gpu.fill_uniform(T, 0.25, 10, 3)
+    torch.cuda.synchronize()
+    rng = np.random.default_rng(3)
+    nreq = 500
+    sizes = rng.integers(1, 1 << 16, nreq).astype(np.uint64)
+    offs = rng.integers(0, n - (1 << 16), nreq).astype(np.uint64)
+    arrivals = np.cumsum(rng.exponential(20e3, nreq)).astype(np.uint64)   # ~50k requests/s
+    for coalesce in (True, False):
+        with Server(budget_bytes=1 << 28, coalesce=coalesce, max_inflight_batches=3 if coalesce else 1) as srv:
+            lat, elapsed = srv.replay(S.data_ptr(), K.data_ptr(), T.data_ptr(), 0.02, 0.3, offs, sizes, arrivals)
+            st = srv.stats()
+            assert st["completed"] == nreq and st["submitted"] == nreq
+            assert st["reserved_bytes"] == 0
+            assert np.all(lat > 0) and elapsed > 0
+            assert elapsed >= arrivals[-1] * 1e-9
+
+
+def test_replay_rejects_oversized_request(gpu):
+    import numpy as np
+    from nt2_gb300.server import Server
+    from nt2_gb300._lib import NT2CudaError
+    S = torch.empty(1 << 16, device="cuda")
+    with Server(budget_bytes=1 << 16) as srv:
+        with pytest.raises(NT2CudaError):
+            srv.replay(S.data_ptr(), S.data_ptr(), S.data_ptr(), 0.02, 0.3, np.zeros(2, np.uint64),
+                       np.array([16, 1 << 16], np.uint64), np.zeros(2, np.uint64))
