@@ -384,7 +384,7 @@ def run_ours(args):
 
 
 CASES = ("bs_exact", "bs_fused", "bs_fast", "bs_fastnormcdf", "bs_f64", "saxpy", "sdot", "sdot_plain",
-         "rgb2grey_u8", "rgb2yuv", "mandelbrot",
+         "rgb2grey_u8", "rgb2yuv", "mandelbrot", "reductions",
          "inner", "outer", "sigmadelta")
 
 
@@ -495,10 +495,29 @@ def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: in
         out.append({"config": "mandelbrot 1600x1600 over [-1.5,1.5]^2, pack 8 (FP32 issue-bound)", "ms": ms,
                     "value": h * w / (ms * 1e-3), "unit": "pixels/s",
                     "counted_trips_per_s": counts / (ms * 1e-3), "mean_count": counts / (h * w)})
-    if not (want("inner") or want("outer") or want("bs_f64") or want("bs_fused") or want("bs_fast")
+    if not (want("inner") or want("outer") or want("reductions") or want("bs_f64") or want("bs_fused") or want("bs_fast")
             or want("bs_exact") or want("bs_fastnormcdf") or want("sigmadelta")):
         return out
     rows, cols = 8192, 4096
+    if want("reductions"):
+        # every reduction of the 8192 x 4096 table along each dimension, four rotating tables
+        As = [torch.empty(rows * cols, device="cuda") for _ in range(4)]
+        for i in range(4):
+            api.fill_normal(As[i], 3 + i)
+        it = [0]
+        for dim in (1, 2):
+            m = cols if dim == 1 else rows
+            for op in ("sum", "asum1", "norm2", "mean", "var", "max", "prod", "all"):
+                o = torch.empty(m, dtype=torch.uint8 if op == "all" else torch.float32, device="cuda")
+
+                def red_step(op=op, dim=dim, o=o):
+                    i = it[0] & 3
+                    it[0] += 1
+                    api.reduce(op, As[i], rows, cols, dim, out=o)
+                ms, _, _ = time_device(red_step, K(50), warmup, ws)
+                out.append(line(f"{op}(A,{dim}) 8192x4096 f32 (4 rotating tables)", ms,
+                                4 * rows * cols + o.element_size() * m, rows * cols, "elements/s"))
+        del As
     if want("inner") or want("outer"):
         # four 134 MB tables visited in turn (536 MB > L2): every step reads from DRAM
         As = [torch.empty(rows * cols, device="cuda") for _ in range(4)]

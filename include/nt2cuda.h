@@ -218,6 +218,36 @@ nt2cuda_status nt2cuda_sum_outer_f64(const double* A, size_t rows, size_t cols, 
  * are within the same bounds; each family is bitwise reproducible.  Process-wide. */
 nt2cuda_status nt2cuda_set_fold_path(int path);
 
+/* ------------------------------------------------------- reductions ---- */
+/* The reductions of NT2's reduction module on the fold kernels, along
+ * dim 1 (one value per column: inner_fold, out has cols entries), dim 2
+ * (one value per row: outer_fold, out has rows entries) or dim 0 (the whole
+ * table, NT2's global* functions: out has 1 entry).
+ * (modules/core/reduction/include/nt2/core/functions/expr/{asum1,asum2,norm2,mean,var,stdev}.hpp,
+ *  modules/boost/simd/base/include/boost/simd/reduction/functions/{sum,maximum,minimum,prod}.hpp)
+ * FP32 sums accumulate compensated unless NT2CUDA_RED_PLAIN is set; var and
+ * stdev normalise by n - 1 (NT2's w = 0; by n with NT2CUDA_RED_VAR_N) and are
+ * computed in one pass (Welford updates, Chan merges).  max and min skip NaNs;
+ * a fold of zero elements gives NT2's neutral value (0, 1, -FLT_MAX, FLT_MAX). */
+enum {
+  NT2CUDA_RED_SUM = 0, NT2CUDA_RED_ASUM1 = 1, NT2CUDA_RED_ASUM2 = 2, NT2CUDA_RED_NORM2 = 3,
+  NT2CUDA_RED_MEAN = 4, NT2CUDA_RED_VAR = 5, NT2CUDA_RED_STDEV = 6, NT2CUDA_RED_MAX = 7,
+  NT2CUDA_RED_MIN = 8, NT2CUDA_RED_PROD = 9
+};
+enum { NT2CUDA_RED_PLAIN = 1, NT2CUDA_RED_VAR_N = 2 };   /* flags */
+/* logical reductions: all(A != 0), any(A != 0), none = !any; uint8_t 0/1 outputs
+ * (boost/simd/reduction/functions/{all,any,none}.hpp) */
+enum { NT2CUDA_RED_ALL = 0, NT2CUDA_RED_ANY = 1, NT2CUDA_RED_NONE = 2 };
+
+nt2cuda_status nt2cuda_reduce_f32(int op, const float* A, size_t rows, size_t cols, int dim, float* out, int flags,
+                                  nt2cuda_stream stream);
+nt2cuda_status nt2cuda_reduce_f64(int op, const double* A, size_t rows, size_t cols, int dim, double* out,
+                                  int flags, nt2cuda_stream stream);
+nt2cuda_status nt2cuda_reduce_logical_f32(int op, const float* A, size_t rows, size_t cols, int dim, uint8_t* out,
+                                          nt2cuda_stream stream);
+nt2cuda_status nt2cuda_reduce_logical_f64(int op, const double* A, size_t rows, size_t cols, int dim, uint8_t* out,
+                                          nt2cuda_stream stream);
+
 /* --------------------------------------------------------- sigmadelta ---- */
 /* One grey video stream for the batched sigma-delta background subtraction
  * (demo/sigmadelta/nt2/sigmadelta_nt2.cpp:37-58, 85-106).  frames holds

@@ -224,6 +224,41 @@ def sum_colmajor(A: torch.Tensor, rows: int, cols: int, dim: int, compensated: b
     return out
 
 
+REDUCTIONS = {"sum": 0, "asum1": 1, "asum2": 2, "norm2": 3, "mean": 4, "var": 5, "stdev": 6, "max": 7, "min": 8,
+              "prod": 9}
+LOGICAL_REDUCTIONS = {"all": 0, "any": 1, "none": 2}
+
+
+def reduce(op: str, A: torch.Tensor, rows: int, cols: int, dim: int = 1, compensated: bool = True,
+           var_by_n: bool = False, out: torch.Tensor | None = None) -> torch.Tensor:
+    """NT2's reductions of a rows x cols column-major table stored flat in A.
+
+    op: sum, asum1, asum2, norm2, mean, var, stdev, max, min, prod (values of A's type) or
+    all, any, none (uint8 0/1).  dim = 1: one value per column; 2: one per row; 0: the whole
+    table (NT2's global* functions).  var_by_n: NT2's w = 1 (normalise by n instead of n - 1).
+    """
+    if A.numel() != rows * cols:
+        raise ValueError("A must hold rows*cols elements")
+    if dim not in (0, 1, 2):
+        raise ValueError("dim must be 0, 1 or 2")
+    m = 1 if dim == 0 else (cols if dim == 1 else rows)
+    L = lib()
+    if A.dtype not in (torch.float32, torch.float64):
+        raise TypeError("reductions take float32 or float64 tables")
+    f32 = A.dtype == torch.float32
+    if op in LOGICAL_REDUCTIONS:
+        out = torch.empty(m, dtype=torch.uint8, device=A.device) if out is None else out
+        fn = L.nt2cuda_reduce_logical_f32 if f32 else L.nt2cuda_reduce_logical_f64
+        st = fn(LOGICAL_REDUCTIONS[op], _dev(A), rows, cols, dim, _dev(out, torch.uint8), _stream())
+    else:
+        out = torch.empty(m, dtype=A.dtype, device=A.device) if out is None else out
+        flags = (0 if compensated else 1) | (2 if var_by_n else 0)
+        fn = L.nt2cuda_reduce_f32 if f32 else L.nt2cuda_reduce_f64
+        st = fn(REDUCTIONS[op], _dev(A), rows, cols, dim, _dev(out, A.dtype), flags, _stream())
+    check(st, f"{op}(A,{dim})")
+    return out
+
+
 def sd_streams(entries: Sequence[dict]) -> C.Array:
     """Build an nt2cuda_sd_stream array from dicts of tensors and sizes."""
     arr = (SdStream * len(entries))()

@@ -23,6 +23,8 @@ SOURCES = [
     "capi_fold.cu",
     "capi_sigmadelta.cu",
     "capi_mandelbrot.cu",
+    "capi_reduce_f32.cu",
+    "capi_reduce_f64.cu",
     "server.cu",
     "capi_noalloc.cu",
 ]

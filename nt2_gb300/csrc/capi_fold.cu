@@ -18,8 +18,8 @@ nt2cuda_status nt2cuda_globalsum_f32(const float* x, size_t n, float* out, int c
 {
   if ((n && !x) || !out) return NT2CUDA_ERR_ARG;
   term<float> e{x};
-  return launch_status(compensated ? nt2cuda::fold::inner_fold<true, float>(e, n, 1, out, as_stream(s))
-                     : nt2cuda::fold::inner_fold<false, float>(e, n, 1, out, as_stream(s)));
+  return launch_status(compensated ? nt2cuda::fold::inner_fold<fold::op_sum<true>, float>(e, n, 1, out, as_stream(s))
+                     : nt2cuda::fold::inner_fold<fold::op_sum<false>, float>(e, n, 1, out, as_stream(s)));
 }
 
 nt2cuda_status nt2cuda_dot_f32(const float* x, const float* y, size_t n, float* out, int compensated,
@@ -27,21 +27,21 @@ nt2cuda_status nt2cuda_dot_f32(const float* x, const float* y, size_t n, float* 
 {
   if ((n && (!x || !y)) || !out) return NT2CUDA_ERR_ARG;
   node<tag::multiplies_, term<float>, term<float>> e{term<float>{x}, term<float>{y}};
-  return launch_status(compensated ? nt2cuda::fold::inner_fold<true, float>(e, n, 1, out, as_stream(s))
-                     : nt2cuda::fold::inner_fold<false, float>(e, n, 1, out, as_stream(s)));
+  return launch_status(compensated ? nt2cuda::fold::inner_fold<fold::op_sum<true>, float>(e, n, 1, out, as_stream(s))
+                     : nt2cuda::fold::inner_fold<fold::op_sum<false>, float>(e, n, 1, out, as_stream(s)));
 }
 
 nt2cuda_status nt2cuda_globalsum_f64(const double* x, size_t n, double* out, nt2cuda_stream s)
 {
   if ((n && !x) || !out) return NT2CUDA_ERR_ARG;
-  return launch_status(nt2cuda::fold::inner_fold<false, double>(term<double>{x}, n, 1, out, as_stream(s)));
+  return launch_status(nt2cuda::fold::inner_fold<fold::op_sum<false>, double>(term<double>{x}, n, 1, out, as_stream(s)));
 }
 
 nt2cuda_status nt2cuda_dot_f64(const double* x, const double* y, size_t n, double* out, nt2cuda_stream s)
 {
   if ((n && (!x || !y)) || !out) return NT2CUDA_ERR_ARG;
   node<tag::multiplies_, term<double>, term<double>> e{term<double>{x}, term<double>{y}};
-  return launch_status(nt2cuda::fold::inner_fold<false, double>(e, n, 1, out, as_stream(s)));
+  return launch_status(nt2cuda::fold::inner_fold<fold::op_sum<false>, double>(e, n, 1, out, as_stream(s)));
 }
 
 nt2cuda_status nt2cuda_sum_inner_f32(const float* A, size_t rows, size_t cols, float* out, int compensated,
@@ -49,14 +49,14 @@ nt2cuda_status nt2cuda_sum_inner_f32(const float* A, size_t rows, size_t cols, f
 {
   if ((rows && cols && !A) || !out) return NT2CUDA_ERR_ARG;
   term<float> e{A};
-  return launch_status(compensated ? nt2cuda::fold::inner_fold<true, float>(e, rows, cols, out, as_stream(s))
-                     : nt2cuda::fold::inner_fold<false, float>(e, rows, cols, out, as_stream(s)));
+  return launch_status(compensated ? nt2cuda::fold::inner_fold<fold::op_sum<true>, float>(e, rows, cols, out, as_stream(s))
+                     : nt2cuda::fold::inner_fold<fold::op_sum<false>, float>(e, rows, cols, out, as_stream(s)));
 }
 
 nt2cuda_status nt2cuda_sum_inner_f64(const double* A, size_t rows, size_t cols, double* out, nt2cuda_stream s)
 {
   if ((rows && cols && !A) || !out) return NT2CUDA_ERR_ARG;
-  return launch_status(nt2cuda::fold::inner_fold<false, double>(term<double>{A}, rows, cols, out, as_stream(s)));
+  return launch_status(nt2cuda::fold::inner_fold<fold::op_sum<false>, double>(term<double>{A}, rows, cols, out, as_stream(s)));
 }
 
 nt2cuda_status nt2cuda_sum_outer_f32(const float* A, size_t rows, size_t cols, float* out, int compensated,
@@ -64,14 +64,14 @@ nt2cuda_status nt2cuda_sum_outer_f32(const float* A, size_t rows, size_t cols, f
 {
   if ((rows && cols && !A) || !out) return NT2CUDA_ERR_ARG;
   term<float> e{A};
-  return launch_status(compensated ? nt2cuda::fold::outer_fold<true, float>(e, rows, cols, out, as_stream(s))
-                     : nt2cuda::fold::outer_fold<false, float>(e, rows, cols, out, as_stream(s)));
+  return launch_status(compensated ? nt2cuda::fold::outer_fold<fold::op_sum<true>, float>(e, rows, cols, out, as_stream(s))
+                     : nt2cuda::fold::outer_fold<fold::op_sum<false>, float>(e, rows, cols, out, as_stream(s)));
 }
 
 nt2cuda_status nt2cuda_sum_outer_f64(const double* A, size_t rows, size_t cols, double* out, nt2cuda_stream s)
 {
   if ((rows && cols && !A) || !out) return NT2CUDA_ERR_ARG;
-  return launch_status(nt2cuda::fold::outer_fold<false, double>(term<double>{A}, rows, cols, out, as_stream(s)));
+  return launch_status(nt2cuda::fold::outer_fold<fold::op_sum<false>, double>(term<double>{A}, rows, cols, out, as_stream(s)));
 }
 
 nt2cuda_status nt2cuda_set_fold_path(int path)

@@ -71,7 +71,7 @@ nt2cuda_status dot_noalloc(const float* x, const float* y, size_t n, float* out,
     size_t rows = n, cols = 1;
     float* o = out;
     void* args[] = {&e, &rows, &cols, &o};
-    return launch_status(launch_persistent(fold::k_inner_short<COMP, float, E>, 1, 256, 1, s, args));
+    return launch_status(launch_persistent(fold::k_inner_short<fold::op_sum<COMP>, float, E>, 1, 256, 1, s, args));
   }
   void* base = nullptr;
   nt2cuda_status st = scratch_address(&base);
@@ -89,8 +89,8 @@ nt2cuda_status dot_noalloc(const float* x, const float* y, size_t n, float* out,
   float* o = out;
   void* args[] = {&e, &sh, &o, &partials, &counters};
   const size_t threads = sh.splits * 32;
-  if (vec) return launch_status(launch_persistent(fold::k_inner<COMP, 4, 4, float, E>, threads, 256, 4, s, args));
-  return launch_status(launch_persistent(fold::k_inner<COMP, 1, 4, float, E>, threads, 256, 4, s, args));
+  if (vec) return launch_status(launch_persistent(fold::k_inner<fold::op_sum<COMP>, 4, 4, float, E>, threads, 256, 4, s, args));
+  return launch_status(launch_persistent(fold::k_inner<fold::op_sum<COMP>, 1, 4, float, E>, threads, 256, 4, s, args));
 }
 
 }  // namespace

@@ -61,18 +61,159 @@ template <bool COMP, class T> __device__ __forceinline__ T result(acc<T> a)
   return COMP ? nt2cuda::math::add(a.s, a.c) : a.s;
 }
 
+// ------------------------------------------------------------ operations
+// A reduction is NT2's reduction_<Tag, Bop, Neutral>
+// (boost/simd/reduction/functions/sum.hpp:26-29, maximum.hpp:30, minimum.hpp:29,
+// prod.hpp:26, all.hpp:29, any.hpp:29) applied to the elements of an expression,
+// plus the scalar step that turns the fold into mean, norm2, var or stdev
+// (nt2/core/functions/expr/mean.hpp, norm2.hpp, var.hpp, stdev.hpp).  An
+// operation supplies its accumulator (state), the neutral state, add,
+// merge (the left operand holds the lower indices), warp shuffles, uncached
+// loads of partials, and finish(state, n) -> output for a fold of n elements.
+enum fin_kind { FIN_NONE = 0, FIN_SQRT = 1, FIN_MEAN = 2 };
+
+template <bool COMP, int FIN = FIN_NONE> struct op_sum {
+  template <class T> using state = acc<T>;
+  template <class T> using out_t = T;
+  template <class T> __device__ __forceinline__ static state<T> init() { return acc<T>{T(0), T(0)}; }
+  template <class T> __device__ __forceinline__ static void add(state<T>& a, T x) { fold::add<COMP>(a, x); }
+  template <class T> __device__ __forceinline__ static state<T> merge(state<T> a, state<T> b) { return fold::merge<COMP>(a, b); }
+  template <class T> __device__ __forceinline__ static state<T> shfl(state<T> a, int off)
+  {
+    return acc<T>{__shfl_xor_sync(0xffffffffu, a.s, off), __shfl_xor_sync(0xffffffffu, a.c, off)};
+  }
+  template <class T> __device__ __forceinline__ static state<T> ldcg(const state<T>* p)
+  {
+    return acc<T>{__ldcg(&p->s), __ldcg(&p->c)};
+  }
+  template <class T> __device__ __forceinline__ static T finish(state<T> a, size_t n)
+  {
+    const T r = result<COMP>(a);
+    if constexpr (FIN == FIN_SQRT) return math::sqrt_(r);
+    if constexpr (FIN == FIN_MEAN) return math::mul(math::div(T(1), (T)n), r);   // rec(n) * sum
+    return r;
+  }
+};
+
+template <class T> struct val { T v; };
+
+// max / min / prod: one value; max and min ignore NaNs (NT2's result with NaNs
+// depends on its evaluation order), their neutral elements are NT2's Maxinit
+// (-largest finite) and Valmax (+largest finite).
+template <int KIND> struct op_val {   // 0 max, 1 min, 2 prod
+  template <class T> using state = val<T>;
+  template <class T> using out_t = T;
+  template <class T> __device__ __forceinline__ static state<T> init()
+  {
+    // largest finite value: NT2's Valmax, and -Valmax is its Maxinit (constant/constants/maxinit.hpp)
+    const T big = sizeof(T) == 4 ? (T)3.40282346638528859812e+38 : (T)1.79769313486231570815e+308;
+    if constexpr (KIND == 2) return val<T>{T(1)};
+    else return val<T>{KIND == 0 ? -big : big};
+  }
+  // a is the accumulator (never NaN), b the next element: NT2's max(a,b) = a > b ? a : b
+  // (boost/simd/arithmetic/functions/scalar/max.hpp), except that a NaN b is skipped
+  template <class T> __device__ __forceinline__ static T op(T a, T b)
+  {
+    if constexpr (KIND == 0) return (a > b || b != b) ? a : b;
+    else if constexpr (KIND == 1) return (a < b || b != b) ? a : b;
+    else return math::mul(a, b);
+  }
+  template <class T> __device__ __forceinline__ static void add(state<T>& a, T x) { a.v = op(a.v, x); }
+  template <class T> __device__ __forceinline__ static state<T> merge(state<T> a, state<T> b) { return val<T>{op(a.v, b.v)}; }
+  template <class T> __device__ __forceinline__ static state<T> shfl(state<T> a, int off)
+  {
+    return val<T>{__shfl_xor_sync(0xffffffffu, a.v, off)};
+  }
+  template <class T> __device__ __forceinline__ static state<T> ldcg(const state<T>* p) { return val<T>{__ldcg(&p->v)}; }
+  template <class T> __device__ __forceinline__ static T finish(state<T> a, size_t) { return a.v; }
+};
+
+// all / any: logical_and / logical_or of (x != 0) with neutral True / False;
+// none = !any (boost/simd/reduction/functions/scalar/none.hpp: is_eqz of the
+// element).  The output is a logical table stored as uint8_t 0/1.
+template <bool ANY, bool NOT = false> struct op_logic {
+  using flag = val<unsigned>;
+  template <class T> using state = flag;
+  template <class T> using out_t = uint8_t;
+  template <class T> __device__ __forceinline__ static flag init() { return flag{ANY ? 0u : 1u}; }
+  template <class T> __device__ __forceinline__ static void add(flag& a, T x)
+  {
+    const unsigned b = (x != T(0)) ? 1u : 0u;
+    a.v = ANY ? (a.v | b) : (a.v & b);
+  }
+  __device__ __forceinline__ static flag merge(flag a, flag b) { return flag{ANY ? (a.v | b.v) : (a.v & b.v)}; }
+  __device__ __forceinline__ static flag shfl(flag a, int off) { return flag{__shfl_xor_sync(0xffffffffu, a.v, off)}; }
+  __device__ __forceinline__ static flag ldcg(const flag* p) { return flag{__ldcg(&p->v)}; }
+  __device__ __forceinline__ static uint8_t finish(flag a, size_t) { return (uint8_t)(NOT ? (a.v ^ 1u) : a.v); }
+};
+
+// var / stdev in one pass: Welford's update per element and Chan's merge of
+// partial (count, mean, M2).  NT2 computes var(A) = f * asum2(center(A)) with
+// f = rec(n - 1) (rec(n) with w = 1, 1 when n <= 1) in two passes
+// (nt2/core/functions/expr/var.hpp); the result here is the same quantity
+// within the error bound stated in the tests.
+template <class T> struct moments { T n, mean, m2; };
+
+template <bool W1, bool STDEV> struct op_moments {
+  template <class U> using state = moments<U>;
+  template <class U> using out_t = U;
+  template <class U> __device__ __forceinline__ static state<U> init() { return moments<U>{U(0), U(0), U(0)}; }
+  template <class U> __device__ __forceinline__ static void add(state<U>& a, U x)
+  {
+    a.n = a.n + U(1);
+    const U d = x - a.mean;
+    if constexpr (sizeof(U) == 4) a.mean = __fmaf_rn(d, __frcp_rn(a.n), a.mean);
+    else a.mean = a.mean + d / a.n;
+    a.m2 = a.m2 + d * (x - a.mean);
+  }
+  template <class U> __device__ __forceinline__ static state<U> merge(state<U> a, state<U> b)
+  {
+    if (b.n == U(0)) return a;
+    if (a.n == U(0)) return b;
+    const U n = a.n + b.n;
+    const U d = b.mean - a.mean;
+    const U wb = b.n / n;
+    return moments<U>{n, a.mean + d * wb, a.m2 + b.m2 + d * d * a.n * wb};
+  }
+  template <class U> __device__ __forceinline__ static state<U> shfl(state<U> a, int off)
+  {
+    return moments<U>{__shfl_xor_sync(0xffffffffu, a.n, off), __shfl_xor_sync(0xffffffffu, a.mean, off),
+                      __shfl_xor_sync(0xffffffffu, a.m2, off)};
+  }
+  template <class U> __device__ __forceinline__ static state<U> ldcg(const state<U>* p)
+  {
+    return moments<U>{__ldcg(&p->n), __ldcg(&p->mean), __ldcg(&p->m2)};
+  }
+  template <class U> __device__ __forceinline__ static U finish(state<U> a, size_t n)
+  {
+    const U n1 = (U)n - (W1 ? U(0) : U(1));
+    const U f = (n <= 1) ? U(1) : math::div(U(1), n1);
+    const U v = math::mul(f, a.m2);
+    return STDEV ? math::sqrt_(v) : v;
+  }
+};
+
+template <class Op, class T> using state_of = typename Op::template state<T>;
+template <class Op, class T> using out_of = typename Op::template out_t<T>;
+
 // Butterfly over the warp; every lane ends with the same value.
-template <bool COMP, class T> __device__ __forceinline__ acc<T> warp_merge(acc<T> a)
+template <class Op, class T> __device__ __forceinline__ state_of<Op, T> warp_merge(state_of<Op, T> a)
 {
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
-    acc<T> o;
-    o.s = __shfl_xor_sync(0xffffffffu, a.s, off);
-    o.c = __shfl_xor_sync(0xffffffffu, a.c, off);
+    state_of<Op, T> o = Op::shfl(a, off);
     // combine in lane order so every lane computes the same value
-    a = ((threadIdx.x & 31) & off) ? merge<COMP>(o, a) : merge<COMP>(a, o);
+    a = ((threadIdx.x & 31) & off) ? Op::merge(o, a) : Op::merge(a, o);
   }
   return a;
+}
+
+// Folds of zero elements: every output is finish(neutral).
+template <class Op, class T>
+__global__ void __launch_bounds__(256) k_fold_empty(out_of<Op, T>* __restrict__ out, size_t count)
+{
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = Op::finish(Op::template init<T>(), 0);
 }
 
 // ------------------------------------------------------------ inner fold
@@ -84,9 +225,9 @@ struct inner_shape {
   size_t rows, cols, seg, splits;
 };
 
-template <bool COMP, int V, int U, class T, class E>
-__global__ void __launch_bounds__(256) k_inner(E e, inner_shape sh, T* __restrict__ out,
-                                               acc<T>* __restrict__ partials, unsigned* __restrict__ counters)
+template <class Op, int V, int U, class T, class E>
+__global__ void __launch_bounds__(256) k_inner(E e, inner_shape sh, out_of<Op, T>* __restrict__ out,
+                                               state_of<Op, T>* __restrict__ partials, unsigned* __restrict__ counters)
 {
   const int lane = threadIdx.x & 31;
   const size_t warps_total = (size_t)gridDim.x * (blockDim.x >> 5);
@@ -96,9 +237,9 @@ __global__ void __launch_bounds__(256) k_inner(E e, inner_shape sh, T* __restric
     const size_t r0 = sp * sh.seg;
     const size_t r1 = (r0 + sh.seg < sh.rows) ? r0 + sh.seg : sh.rows;
     const size_t base = j * sh.rows;
-    acc<T> a[V];
+    state_of<Op, T> a[V];
 #pragma unroll
-    for (int l = 0; l < V; ++l) a[l] = acc<T>{T(0), T(0)};
+    for (int l = 0; l < V; ++l) a[l] = Op::template init<T>();
     // full V-groups
     const size_t g0 = r0 / V, g1 = r1 / V;   // r0 is a multiple of V
     size_t g = g0 + lane;
@@ -109,26 +250,26 @@ __global__ void __launch_bounds__(256) k_inner(E e, inner_shape sh, T* __restric
 #pragma unroll
       for (int u = 0; u < U; ++u)
 #pragma unroll
-        for (int l = 0; l < V; ++l) add<COMP>(a[l], (T)rr[u].template get<false>(e, l));
+        for (int l = 0; l < V; ++l) Op::add(a[l], (T)rr[u].template get<false>(e, l));
     }
     for (; g < g1; g += 32) {
       regs<E, V> rr;
       rr.template load<true>(e, base + g * V);
 #pragma unroll
-      for (int l = 0; l < V; ++l) add<COMP>(a[l], (T)rr.template get<false>(e, l));
+      for (int l = 0; l < V; ++l) Op::add(a[l], (T)rr.template get<false>(e, l));
     }
     // ragged end of the segment (only when rows % V != 0 or V == 1)
     for (size_t r = g1 * V + lane; r < r1; r += 32) {
       regs<E, 1> rr;
       rr.template load<false>(e, base + r);
-      add<COMP>(a[0], (T)rr.template get<false>(e, 0));
+      Op::add(a[0], (T)rr.template get<false>(e, 0));
     }
-    acc<T> t = a[0];
+    state_of<Op, T> t = a[0];
 #pragma unroll
-    for (int l = 1; l < V; ++l) t = merge<COMP>(t, a[l]);
-    t = warp_merge<COMP>(t);
+    for (int l = 1; l < V; ++l) t = Op::merge(t, a[l]);
+    t = warp_merge<Op, T>(t);
     if (sh.splits == 1) {
-      if (lane == 0) out[j] = result<COMP>(t);
+      if (lane == 0) out[j] = Op::finish(t, sh.rows);
       continue;
     }
     unsigned last = 0;
@@ -144,29 +285,25 @@ __global__ void __launch_bounds__(256) k_inner(E e, inner_shape sh, T* __restric
     __threadfence();
     // combine the column's partials in segment order: lane k folds
     // segments k, k+32, ... then the butterfly merges lanes in order
-    acc<T> c{T(0), T(0)};
-    for (size_t q = lane; q < sh.splits; q += 32) {
-      const acc<T>* p = partials + j * sh.splits + q;
-      acc<T> v{__ldcg(&p->s), __ldcg(&p->c)};
-      c = merge<COMP>(c, v);
-    }
-    c = warp_merge<COMP>(c);
-    if (lane == 0) out[j] = result<COMP>(c);
+    state_of<Op, T> c = Op::template init<T>();
+    for (size_t q = lane; q < sh.splits; q += 32) c = Op::merge(c, Op::ldcg(partials + j * sh.splits + q));
+    c = warp_merge<Op, T>(c);
+    if (lane == 0) out[j] = Op::finish(c, sh.rows);
   }
 }
 
 // Short columns (rows < 32): one thread folds one whole column.
-template <bool COMP, class T, class E>
-__global__ void __launch_bounds__(256) k_inner_short(E e, size_t rows, size_t cols, T* __restrict__ out)
+template <class Op, class T, class E>
+__global__ void __launch_bounds__(256) k_inner_short(E e, size_t rows, size_t cols, out_of<Op, T>* __restrict__ out)
 {
   for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < cols; j += (size_t)gridDim.x * blockDim.x) {
-    acc<T> a{T(0), T(0)};
+    state_of<Op, T> a = Op::template init<T>();
     for (size_t r = 0; r < rows; ++r) {
       regs<E, 1> rr;
       rr.template load<false>(e, j * rows + r);
-      add<COMP>(a, (T)rr.template get<false>(e, 0));
+      Op::add(a, (T)rr.template get<false>(e, 0));
     }
-    out[j] = result<COMP>(a);
+    out[j] = Op::finish(a, rows);
   }
 }
 
@@ -181,12 +318,13 @@ struct outer_shape {
   size_t rows, cols, cchunk, splits, strips;
 };
 
-template <bool COMP, int V, int U, class T, class E>
-__global__ void __launch_bounds__(256) k_outer(E e, outer_shape sh, T* __restrict__ out,
-                                               acc<T>* __restrict__ partials, unsigned* __restrict__ counters)
+template <class Op, int V, int U, class T, class E>
+__global__ void __launch_bounds__(256) k_outer(E e, outer_shape sh, out_of<Op, T>* __restrict__ out,
+                                               state_of<Op, T>* __restrict__ partials, unsigned* __restrict__ counters)
 {
+  using S = state_of<Op, T>;
   constexpr int STRIP = 32 * V;
-  __shared__ acc<T> red[8][STRIP];
+  __shared__ S red[8][STRIP];
   __shared__ unsigned is_last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const size_t units = sh.strips * sh.splits;
@@ -196,9 +334,9 @@ __global__ void __launch_bounds__(256) k_outer(E e, outer_shape sh, T* __restric
     const size_t m0 = sp * sh.cchunk;
     const size_t m1 = (m0 + sh.cchunk < sh.cols) ? m0 + sh.cchunk : sh.cols;
     const bool full = row0 + V <= sh.rows;
-    acc<T> a[V];
+    S a[V];
 #pragma unroll
-    for (int l = 0; l < V; ++l) a[l] = acc<T>{T(0), T(0)};
+    for (int l = 0; l < V; ++l) a[l] = Op::template init<T>();
     if (full) {
       size_t m = m0 + warp;
       for (; m + (size_t)(U - 1) * 8 < m1; m += (size_t)U * 8) {
@@ -208,13 +346,13 @@ __global__ void __launch_bounds__(256) k_outer(E e, outer_shape sh, T* __restric
 #pragma unroll
         for (int u = 0; u < U; ++u)
 #pragma unroll
-          for (int l = 0; l < V; ++l) add<COMP>(a[l], (T)rr[u].template get<false>(e, l));
+          for (int l = 0; l < V; ++l) Op::add(a[l], (T)rr[u].template get<false>(e, l));
       }
       for (; m < m1; m += 8) {
         regs<E, V> rr;
         rr.template load<true>(e, m * sh.rows + row0);
 #pragma unroll
-        for (int l = 0; l < V; ++l) add<COMP>(a[l], (T)rr.template get<false>(e, l));
+        for (int l = 0; l < V; ++l) Op::add(a[l], (T)rr.template get<false>(e, l));
       }
     } else if (row0 < sh.rows) {
       for (size_t m = m0 + warp; m < m1; m += 8)
@@ -223,22 +361,22 @@ __global__ void __launch_bounds__(256) k_outer(E e, outer_shape sh, T* __restric
           if (row0 + l < sh.rows) {
             regs<E, 1> rr;
             rr.template load<false>(e, m * sh.rows + row0 + l);
-            add<COMP>(a[l], (T)rr.template get<false>(e, 0));
+            Op::add(a[l], (T)rr.template get<false>(e, 0));
           }
     }
 #pragma unroll
     for (int l = 0; l < V; ++l) red[warp][lane * V + l] = a[l];
     __syncthreads();
     // thread t < STRIP merges row t of the strip over the 8 warps in order
-    acc<T> rsum{T(0), T(0)};
+    S rsum = Op::template init<T>();
     const size_t row = strip * STRIP + threadIdx.x;
     if (threadIdx.x < STRIP) {
       rsum = red[0][threadIdx.x];
 #pragma unroll
-      for (int w = 1; w < 8; ++w) rsum = merge<COMP>(rsum, red[w][threadIdx.x]);
+      for (int w = 1; w < 8; ++w) rsum = Op::merge(rsum, red[w][threadIdx.x]);
     }
     if (sh.splits == 1) {
-      if (threadIdx.x < STRIP && row < sh.rows) out[row] = result<COMP>(rsum);
+      if (threadIdx.x < STRIP && row < sh.rows) out[row] = Op::finish(rsum, sh.cols);
       __syncthreads();
       continue;
     }
@@ -254,23 +392,17 @@ __global__ void __launch_bounds__(256) k_outer(E e, outer_shape sh, T* __restric
     if (is_last) {
       __threadfence();
       if (threadIdx.x < STRIP && row < sh.rows) {
-        acc<T> c{T(0), T(0)};
+        S c = Op::template init<T>();
         size_t q = 0;
         for (; q + 8 <= sh.splits; q += 8) {
-          acc<T> v[8];
+          S v[8];
 #pragma unroll
-          for (int k = 0; k < 8; ++k) {
-            const acc<T>* p = partials + (strip * sh.splits + q + k) * STRIP + threadIdx.x;
-            v[k] = acc<T>{__ldcg(&p->s), __ldcg(&p->c)};
-          }
+          for (int k = 0; k < 8; ++k) v[k] = Op::ldcg(partials + (strip * sh.splits + q + k) * STRIP + threadIdx.x);
 #pragma unroll
-          for (int k = 0; k < 8; ++k) c = merge<COMP>(c, v[k]);
+          for (int k = 0; k < 8; ++k) c = Op::merge(c, v[k]);
         }
-        for (; q < sh.splits; ++q) {
-          const acc<T>* p = partials + (strip * sh.splits + q) * STRIP + threadIdx.x;
-          c = merge<COMP>(c, acc<T>{__ldcg(&p->s), __ldcg(&p->c)});
-        }
-        out[row] = result<COMP>(c);
+        for (; q < sh.splits; ++q) c = Op::merge(c, Op::ldcg(partials + (strip * sh.splits + q) * STRIP + threadIdx.x));
+        out[row] = Op::finish(c, sh.cols);
       }
     }
     __syncthreads();

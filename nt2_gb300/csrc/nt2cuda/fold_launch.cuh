@@ -58,9 +58,17 @@ template <class T> inline const T* first_term(const node<tag::multiplies_, term<
 template <class T> inline const T* second_term(const term<T>&) { return nullptr; }
 template <class T> inline const T* second_term(const node<tag::multiplies_, term<T>, term<T>>& n) { return n.b.p; }
 
-template <bool COMP, class T, class E>
-cudaError_t inner_fold(const E& e, size_t rows, size_t cols, T* out, cudaStream_t s)
+template <class Op, class T> cudaError_t fold_empty(out_of<Op, T>* out, size_t count, cudaStream_t s)
 {
+  void* args[] = {&out, &count};
+  return launch_persistent(k_fold_empty<Op, T>, count, 256, 1, s, args);
+}
+
+// inner_fold with operation Op (op_sum<COMP>, op_val, op_logic, op_moments).
+template <class Op, class T, class E>
+cudaError_t inner_fold(const E& e, size_t rows, size_t cols, out_of<Op, T>* out, cudaStream_t s)
+{
+  using S = state_of<Op, T>;
   if constexpr (tma_terms<E>::n > 0) {
     constexpr size_t VV = 16 / sizeof(T);
     // auto: long columns only; a short column's tiles are too few to amortise the block barriers
@@ -68,17 +76,17 @@ cudaError_t inner_fold(const E& e, size_t rows, size_t cols, T* out, cudaStream_
     const size_t min_rows = path == 2 ? 32 : ((size_t)1 << 16);
     if (path != 1 && rows >= min_rows && cols > 0 && out && rows % VV == 0 && expr_aligned(e) &&
         std::is_same<typename value_of<E>::type, T>::value)
-      return inner_fold_tma<COMP, T>(first_term(e), second_term(e), rows, cols, out, s);
+      return inner_fold_tma<Op, T>(first_term(e), second_term(e), rows, cols, out, s);
   }
   if (cols == 0) return cudaSuccess;
   if (!out) return cudaErrorInvalidValue;
-  if (rows == 0) return (cudaMemsetAsync(out, 0, cols * sizeof(T), s));
+  if (rows == 0) return fold_empty<Op, T>(out, cols, s);
   if (rows < 32) {
     size_t ee = cols;
     E ec = e;
-    T* o = out;
+    out_of<Op, T>* o = out;
     void* args[] = {&ec, &rows, &ee, &o};
-    return (launch_persistent(k_inner_short<COMP, T, E>, cols, 256, 4, s, args));
+    return (launch_persistent(k_inner_short<Op, T, E>, cols, 256, 4, s, args));
   }
   constexpr int VV = 16 / (int)sizeof(T);
   const bool vec = expr_aligned(e) && rows % VV == 0;
@@ -87,40 +95,41 @@ cudaError_t inner_fold(const E& e, size_t rows, size_t cols, T* out, cudaStream_
   sh.cols = cols;
   sh.seg = inner_seg<T>();
   sh.splits = (rows + sh.seg - 1) / sh.seg;
-  acc<T>* partials = nullptr;
+  S* partials = nullptr;
   unsigned* counters = nullptr;
   if (sh.splits > 1) {
     size_t cbytes = round_up(cols * sizeof(unsigned), 256);
-    size_t pbytes = cols * sh.splits * sizeof(acc<T>);
+    size_t pbytes = cols * sh.splits * sizeof(S);
     void* scratch = nullptr;
     cudaError_t st = stream_scratch(s, cbytes + pbytes, &scratch);
     if (st != cudaSuccess) return st;
     counters = (unsigned*)scratch;
-    partials = (acc<T>*)((char*)scratch + cbytes);
+    partials = (S*)((char*)scratch + cbytes);
   }
   const size_t units = cols * sh.splits;
   E ec = e;
-  T* o = out;
+  out_of<Op, T>* o = out;
   void* args[] = {&ec, &sh, &o, &partials, &counters};
   // launch_persistent counts threads; a unit is one warp
-  if (vec) return (launch_persistent(k_inner<COMP, VV, 8, T, E>, units * 32, 256, 4, s, args));
-  return (launch_persistent(k_inner<COMP, 1, 4, T, E>, units * 32, 256, 4, s, args));
+  if (vec) return (launch_persistent(k_inner<Op, VV, 8, T, E>, units * 32, 256, 4, s, args));
+  return (launch_persistent(k_inner<Op, 1, 4, T, E>, units * 32, 256, 4, s, args));
 }
 
-template <bool COMP, class T, class E>
-cudaError_t outer_fold(const E& e, size_t rows, size_t cols, T* out, cudaStream_t s)
+template <class Op, class T, class E>
+cudaError_t outer_fold(const E& e, size_t rows, size_t cols, out_of<Op, T>* out, cudaStream_t s)
 {
+  using S = state_of<Op, T>;
   if constexpr (tma_terms<E>::n == 1) {
     constexpr size_t VV = 16 / sizeof(T);
     if (fold_path().load(std::memory_order_relaxed) == 2 && rows >= 256 && cols > 0 && out && rows % VV == 0 &&
         expr_aligned(e) && rows < ((size_t)1 << 31) && cols < ((size_t)1 << 31)) {
-      cudaError_t r = outer_fold_tma<COMP, T>(first_term(e), rows, cols, out, s);
+      cudaError_t r = outer_fold_tma<Op, T>(first_term(e), rows, cols, out, s);
       if (r != cudaErrorNotSupported) return r;
     }
   }
   if (rows == 0) return cudaSuccess;
   if (!out) return cudaErrorInvalidValue;
-  if (cols == 0) return (cudaMemsetAsync(out, 0, rows * sizeof(T), s));
+  if (cols == 0) return fold_empty<Op, T>(out, rows, s);
   constexpr int VV = 16 / (int)sizeof(T);
   const bool vec = expr_aligned(e) && rows % VV == 0;
   const int V = vec ? VV : 1;
@@ -138,23 +147,23 @@ cudaError_t outer_fold(const E& e, size_t rows, size_t cols, T* out, cudaStream_
     sh.cchunk = cchunk < 64 ? 64 : cchunk;
   }
   sh.splits = (cols + sh.cchunk - 1) / sh.cchunk;
-  acc<T>* partials = nullptr;
+  S* partials = nullptr;
   unsigned* counters = nullptr;
   if (sh.splits > 1) {
     size_t cbytes = round_up(sh.strips * sizeof(unsigned), 256);
-    size_t pbytes = sh.strips * sh.splits * STRIP * sizeof(acc<T>);
+    size_t pbytes = sh.strips * sh.splits * STRIP * sizeof(S);
     void* scratch = nullptr;
     cudaError_t st = stream_scratch(s, cbytes + pbytes, &scratch);
     if (st != cudaSuccess) return st;
     counters = (unsigned*)scratch;
-    partials = (acc<T>*)((char*)scratch + cbytes);
+    partials = (S*)((char*)scratch + cbytes);
   }
   const size_t units = sh.strips * sh.splits;
   E ec = e;
-  T* o = out;
+  out_of<Op, T>* o = out;
   void* args[] = {&ec, &sh, &o, &partials, &counters};
-  if (vec) return (launch_persistent(k_outer<COMP, VV, 8, T, E>, units * 256, 256, 4, s, args));
-  return (launch_persistent(k_outer<COMP, 1, 4, T, E>, units * 256, 256, 4, s, args));
+  if (vec) return (launch_persistent(k_outer<Op, VV, 8, T, E>, units * 256, 256, 4, s, args));
+  return (launch_persistent(k_outer<Op, 1, 4, T, E>, units * 256, 256, 4, s, args));
 }
 
 }  // namespace fold

@@ -1,6 +1,6 @@
 // nt2cuda/fold_tma.cuh -- inner_fold and outer_fold with TMA-staged tiles.
 //
-// Same results contract as fold.cuh (compensated or plain accumulation,
+// Same results contract as fold.cuh (any of its reduction operations,
 // partials merged in index order, decomposition fixed by the table's shape),
 // but the input tiles reach shared memory through the Tensor Memory
 // Accelerator, so each block keeps several 16 KB tiles in flight without
@@ -32,47 +32,43 @@ namespace fold {
 
 constexpr int kTmaTileBytes = 16384;
 
+// value written for a unit whose copies did not arrive: NaN, or 0xFF for a logical output
 template <class T> __device__ __forceinline__ T quiet_nan()
 {
-  if constexpr (sizeof(T) == 4) return __int_as_float(0x7fc00000);
+  if constexpr (sizeof(T) == 1) return (T)0xFF;
+  else if constexpr (sizeof(T) == 4) return __int_as_float(0x7fc00000);
   else return __longlong_as_double(0x7ff8000000000000ll);
 }
 
 // Merge n partials p[0], p[stride], ... in index order, with 8 loads in
 // flight at a time (the merge is at the tail of the kernel, where serial L2
 // round trips would show).
-template <bool COMP, class T>
-__device__ __forceinline__ acc<T> merge_partials(const acc<T>* p, size_t n, size_t stride)
+template <class Op, class T>
+__device__ __forceinline__ state_of<Op, T> merge_partials(const state_of<Op, T>* p, size_t n, size_t stride)
 {
-  acc<T> m{T(0), T(0)};
+  state_of<Op, T> m = Op::template init<T>();
   size_t q = 0;
   for (; q + 8 <= n; q += 8) {
-    acc<T> v[8];
+    state_of<Op, T> v[8];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const acc<T>* e = p + (q + k) * stride;
-      v[k] = acc<T>{__ldcg(&e->s), __ldcg(&e->c)};
-    }
+    for (int k = 0; k < 8; ++k) v[k] = Op::ldcg(p + (q + k) * stride);
 #pragma unroll
-    for (int k = 0; k < 8; ++k) m = merge<COMP>(m, v[k]);
+    for (int k = 0; k < 8; ++k) m = Op::merge(m, v[k]);
   }
-  for (; q < n; ++q) {
-    const acc<T>* e = p + q * stride;
-    m = merge<COMP>(m, acc<T>{__ldcg(&e->s), __ldcg(&e->c)});
-  }
+  for (; q < n; ++q) m = Op::merge(m, Op::ldcg(p + q * stride));
   return m;
 }
 
 // Merge v[threadIdx.x] over the block in a fixed order; thread 0 gets the result.
-template <bool COMP, class T>
-__device__ __forceinline__ acc<T> block_merge(acc<T> v, acc<T>* red)
+template <class Op, class T>
+__device__ __forceinline__ state_of<Op, T> block_merge(state_of<Op, T> v, state_of<Op, T>* red)
 {
-  v = warp_merge<COMP>(v);
+  v = warp_merge<Op, T>(v);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
   __syncthreads();
-  acc<T> r = red[0];
+  state_of<Op, T> r = red[0];
   if (threadIdx.x == 0)
-    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r = merge<COMP>(r, red[w]);
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r = Op::merge(r, red[w]);
   __syncthreads();
   return r;
 }
@@ -93,17 +89,19 @@ __device__ __forceinline__ size_t inner_unit_tiles(const inner_tma_shape& sh, si
 }
 
 // NT = 1 folds x; NT = 2 folds x*y (float product rounded, as NT2's X*Y).
-template <bool COMP, class T, int NT, int STAGES>
+template <class Op, class T, int NT, int STAGES>
 __global__ void __launch_bounds__(256) k_inner_tma(const T* __restrict__ x, const T* __restrict__ y,
-                                                   inner_tma_shape sh, T* __restrict__ out,
-                                                   acc<T>* __restrict__ partials, unsigned* __restrict__ counters)
+                                                   inner_tma_shape sh, out_of<Op, T>* __restrict__ out,
+                                                   state_of<Op, T>* __restrict__ partials,
+                                                   unsigned* __restrict__ counters)
 {
+  using S = state_of<Op, T>;
   constexpr int TILE = inner_tile<T>();
   constexpr int V = 16 / (int)sizeof(T);
   extern __shared__ __align__(128) unsigned char smem_raw[];
   T* buf = reinterpret_cast<T*>(smem_raw);          // [STAGES][NT][TILE]
   __shared__ __align__(8) uint64_t bar[STAGES];
-  __shared__ acc<T> red[8];
+  __shared__ S red[8];
   __shared__ unsigned s_last;
 
   if (threadIdx.x == 0) {
@@ -131,15 +129,15 @@ __global__ void __launch_bounds__(256) k_inner_tma(const T* __restrict__ x, cons
 
   size_t cu = blockIdx.x, ct = 0;
   uint32_t iter = 0;
-  acc<T> a[V];
+  S a[V];
 #pragma unroll
-  for (int l = 0; l < V; ++l) a[l] = acc<T>{T(0), T(0)};
+  for (int l = 0; l < V; ++l) a[l] = Op::template init<T>();
   while (cu < sh.units) {
     const int s = (int)(iter % STAGES);
     const bool ok = tma::mbar_wait(&bar[s], (iter / STAGES) & 1u);
     if (__syncthreads_or(!ok)) {
       if (threadIdx.x == 0) {
-        out[cu / sh.splits] = quiet_nan<T>();
+        out[cu / sh.splits] = quiet_nan<out_of<Op, T>>();
         for (uint32_t k = iter; k < issued; ++k) tma::mbar_wait(&bar[k % STAGES], (k / STAGES) & 1u);
       }
       __syncthreads();
@@ -159,10 +157,10 @@ __global__ void __launch_bounds__(256) k_inner_tma(const T* __restrict__ x, cons
         T yv[V];
         *reinterpret_cast<uint4*>(yv) = *reinterpret_cast<const uint4*>(ty + e);
 #pragma unroll
-        for (int l = 0; l < V; ++l) add<COMP>(a[l], math::mul(xv[l], yv[l]));
+        for (int l = 0; l < V; ++l) Op::add(a[l], math::mul(xv[l], yv[l]));
       } else {
 #pragma unroll
-        for (int l = 0; l < V; ++l) add<COMP>(a[l], xv[l]);
+        for (int l = 0; l < V; ++l) Op::add(a[l], xv[l]);
       }
     }
     __syncthreads();                                   // every thread is done with stage s
@@ -171,12 +169,12 @@ __global__ void __launch_bounds__(256) k_inner_tma(const T* __restrict__ x, cons
       produce(s);
     }
     if (++ct == inner_unit_tiles<T>(sh, cu)) {         // unit complete: merge and emit
-      acc<T> t = a[0];
+      S t = a[0];
 #pragma unroll
-      for (int l = 1; l < V; ++l) t = merge<COMP>(t, a[l]);
-      t = block_merge<COMP>(t, red);
+      for (int l = 1; l < V; ++l) t = Op::merge(t, a[l]);
+      t = block_merge<Op, T>(t, red);
       if (sh.splits == 1) {
-        if (threadIdx.x == 0) out[j] = result<COMP>(t);
+        if (threadIdx.x == 0) out[j] = Op::finish(t, sh.rows);
       } else {
         if (threadIdx.x == 0) {
           partials[cu] = t;
@@ -188,17 +186,15 @@ __global__ void __launch_bounds__(256) k_inner_tma(const T* __restrict__ x, cons
         __syncthreads();
         if (s_last) {
           __threadfence();
-          acc<T> m{T(0), T(0)};
-          for (size_t q = threadIdx.x; q < sh.splits; q += blockDim.x) {
-            const acc<T>* p = partials + j * sh.splits + q;
-            m = merge<COMP>(m, acc<T>{__ldcg(&p->s), __ldcg(&p->c)});
-          }
-          m = block_merge<COMP>(m, red);
-          if (threadIdx.x == 0) out[j] = result<COMP>(m);
+          S m = Op::template init<T>();
+          for (size_t q = threadIdx.x; q < sh.splits; q += blockDim.x)
+            m = Op::merge(m, Op::ldcg(partials + j * sh.splits + q));
+          m = block_merge<Op, T>(m, red);
+          if (threadIdx.x == 0) out[j] = Op::finish(m, sh.rows);
         }
       }
 #pragma unroll
-      for (int l = 0; l < V; ++l) a[l] = acc<T>{T(0), T(0)};
+      for (int l = 0; l < V; ++l) a[l] = Op::template init<T>();
       ct = 0;
       cu += gridDim.x;
     }
@@ -214,11 +210,13 @@ struct outer_tma_shape {
 constexpr int kOuterRows = 256;   // box rows (and threads per block)
 template <class T> __host__ __device__ constexpr int outer_cols() { return kTmaTileBytes / (kOuterRows * (int)sizeof(T)); }
 
-template <bool COMP, class T, int STAGES>
+template <class Op, class T, int STAGES>
 __global__ void __launch_bounds__(256) k_outer_tma(const __grid_constant__ CUtensorMap map, outer_tma_shape sh,
-                                                   T* __restrict__ out, acc<T>* __restrict__ partials,
+                                                   out_of<Op, T>* __restrict__ out,
+                                                   state_of<Op, T>* __restrict__ partials,
                                                    unsigned* __restrict__ counters)
 {
+  using S = state_of<Op, T>;
   constexpr int BR = kOuterRows, BC = outer_cols<T>();
   extern __shared__ __align__(128) unsigned char smem_raw[];
   T* buf = reinterpret_cast<T*>(smem_raw);          // [STAGES][BC][BR]
@@ -251,24 +249,31 @@ __global__ void __launch_bounds__(256) k_outer_tma(const __grid_constant__ CUten
 
   size_t cu = blockIdx.x, ct = 0;
   uint32_t iter = 0;
-  acc<T> a0{T(0), T(0)}, a1{T(0), T(0)};
+  S a0 = Op::template init<T>(), a1 = Op::template init<T>();
   while (cu < sh.units) {
     const int s = (int)(iter % STAGES);
     const bool ok = tma::mbar_wait(&bar[s], (iter / STAGES) & 1u);
     if (__syncthreads_or(!ok)) {
       const size_t row = (cu / sh.splits) * BR + threadIdx.x;
-      if (row < sh.rows) out[row] = quiet_nan<T>();
+      if (row < sh.rows) out[row] = quiet_nan<out_of<Op, T>>();
       if (threadIdx.x == 0)
         for (uint32_t k = iter; k < issued; ++k) tma::mbar_wait(&bar[k % STAGES], (k / STAGES) & 1u);
       __syncthreads();
       return;
     }
     const T* tile = buf + (size_t)s * BC * BR;
-    // columns past the table are zero-filled by the copy; chunks are whole tiles wide
+    // columns past the table are zero-filled by the copy and skipped (a zero is
+    // not neutral for every operation); chunks are whole tiles wide
+    const size_t cbase = (cu % sh.splits) * sh.cchunk + ct * BC;
+    if (cbase + BC <= sh.cols) {
 #pragma unroll
-    for (int c = 0; c < BC; c += 2) {
-      add<COMP>(a0, tile[c * BR + threadIdx.x]);
-      add<COMP>(a1, tile[(c + 1) * BR + threadIdx.x]);
+      for (int c = 0; c < BC; c += 2) {
+        Op::add(a0, tile[c * BR + threadIdx.x]);
+        Op::add(a1, tile[(c + 1) * BR + threadIdx.x]);
+      }
+    } else {
+      for (int c = 0; c < BC; ++c)
+        if (cbase + c < sh.cols) Op::add((c & 1) ? a1 : a0, tile[c * BR + threadIdx.x]);
     }
     __syncthreads();
     if (threadIdx.x == 0 && pu < sh.units) {
@@ -278,9 +283,9 @@ __global__ void __launch_bounds__(256) k_outer_tma(const __grid_constant__ CUten
     if (++ct == unit_tiles(cu)) {
       const size_t strip = cu / sh.splits;
       const size_t row = strip * BR + threadIdx.x;
-      const acc<T> t = merge<COMP>(a0, a1);
+      const S t = Op::merge(a0, a1);
       if (sh.splits == 1) {
-        if (row < sh.rows) out[row] = result<COMP>(t);
+        if (row < sh.rows) out[row] = Op::finish(t, sh.cols);
       } else {
         partials[cu * BR + threadIdx.x] = t;
         __syncthreads();                    // the block's partials, then one device-scope fence
@@ -293,12 +298,12 @@ __global__ void __launch_bounds__(256) k_outer_tma(const __grid_constant__ CUten
         __syncthreads();
         if (s_last) {
           __threadfence();
-          acc<T> m = merge_partials<COMP, T>(partials + strip * sh.splits * BR + threadIdx.x, sh.splits, BR);
-          if (row < sh.rows) out[row] = result<COMP>(m);
+          S m = merge_partials<Op, T>(partials + strip * sh.splits * BR + threadIdx.x, sh.splits, BR);
+          if (row < sh.rows) out[row] = Op::finish(m, sh.cols);
         }
       }
-      a0 = acc<T>{T(0), T(0)};
-      a1 = acc<T>{T(0), T(0)};
+      a0 = Op::template init<T>();
+      a1 = Op::template init<T>();
       ct = 0;
       cu += gridDim.x;
     }
@@ -330,9 +335,10 @@ template <class K> inline cudaError_t set_smem(K kernel, int bytes)
 }
 
 // x (and y when not null) are 16-byte aligned and rows % (16/sizeof(T)) == 0.
-template <bool COMP, class T>
-cudaError_t inner_fold_tma(const T* x, const T* y, size_t rows, size_t cols, T* out, cudaStream_t s)
+template <class Op, class T>
+cudaError_t inner_fold_tma(const T* x, const T* y, size_t rows, size_t cols, out_of<Op, T>* out, cudaStream_t s)
 {
+  using S = state_of<Op, T>;
   constexpr int TILE = inner_tile<T>();
   inner_tma_shape sh;
   sh.rows = rows;
@@ -341,21 +347,21 @@ cudaError_t inner_fold_tma(const T* x, const T* y, size_t rows, size_t cols, T* 
   sh.splits = (rows + sh.seg - 1) / sh.seg;
   sh.units = cols * sh.splits;
   if (sh.units == 0) return cudaSuccess;
-  acc<T>* partials = nullptr;
+  S* partials = nullptr;
   unsigned* counters = nullptr;
   if (sh.splits > 1) {
     const size_t cbytes = (cols * sizeof(unsigned) + 255) / 256 * 256;
     void* scratch = nullptr;
-    cudaError_t e = stream_scratch(s, cbytes + sh.units * sizeof(acc<T>), &scratch);
+    cudaError_t e = stream_scratch(s, cbytes + sh.units * sizeof(S), &scratch);
     if (e != cudaSuccess) return e;
     counters = (unsigned*)scratch;
-    partials = (acc<T>*)((char*)scratch + cbytes);
+    partials = (S*)((char*)scratch + cbytes);
   }
   size_t grid;
   cudaError_t e;
   if (y) {
     constexpr int ST = 3;
-    auto k = k_inner_tma<COMP, T, 2, ST>;
+    auto k = k_inner_tma<Op, T, 2, ST>;
     const int smem = ST * 2 * kTmaTileBytes;
     if ((e = set_smem(k, smem)) != cudaSuccess) return e;
     int per = 0;
@@ -365,7 +371,7 @@ cudaError_t inner_fold_tma(const T* x, const T* y, size_t rows, size_t cols, T* 
     k<<<(unsigned)grid, 256, smem, s>>>(x, y, sh, out, partials, counters);
   } else {
     constexpr int ST = 4;
-    auto k = k_inner_tma<COMP, T, 1, ST>;
+    auto k = k_inner_tma<Op, T, 1, ST>;
     const int smem = ST * kTmaTileBytes;
     if ((e = set_smem(k, smem)) != cudaSuccess) return e;
     int per = 0;
@@ -378,9 +384,10 @@ cudaError_t inner_fold_tma(const T* x, const T* y, size_t rows, size_t cols, T* 
 }
 
 // A is 16-byte aligned and rows % (16/sizeof(T)) == 0; rows, cols < 2^31.
-template <bool COMP, class T>
-cudaError_t outer_fold_tma(const T* A, size_t rows, size_t cols, T* out, cudaStream_t s)
+template <class Op, class T>
+cudaError_t outer_fold_tma(const T* A, size_t rows, size_t cols, out_of<Op, T>* out, cudaStream_t s)
 {
+  using S = state_of<Op, T>;
   constexpr int BR = kOuterRows, BC = outer_cols<T>();
   if (rows == 0 || cols == 0) return cudaSuccess;
   if (rows >= ((size_t)1 << 31) || cols >= ((size_t)1 << 31)) return cudaErrorNotSupported;
@@ -405,18 +412,18 @@ cudaError_t outer_fold_tma(const T* A, size_t rows, size_t cols, T* out, cudaStr
   if (sh.cchunk < (size_t)BC) sh.cchunk = BC;
   sh.splits = (cols + sh.cchunk - 1) / sh.cchunk;
   sh.units = sh.strips * sh.splits;
-  acc<T>* partials = nullptr;
+  S* partials = nullptr;
   unsigned* counters = nullptr;
   if (sh.splits > 1) {
     const size_t cbytes = (sh.strips * sizeof(unsigned) + 255) / 256 * 256;
     void* scratch = nullptr;
-    cudaError_t e = stream_scratch(s, cbytes + sh.units * BR * sizeof(acc<T>), &scratch);
+    cudaError_t e = stream_scratch(s, cbytes + sh.units * BR * sizeof(S), &scratch);
     if (e != cudaSuccess) return e;
     counters = (unsigned*)scratch;
-    partials = (acc<T>*)((char*)scratch + cbytes);
+    partials = (S*)((char*)scratch + cbytes);
   }
   constexpr int ST = 4;
-  auto k = k_outer_tma<COMP, T, ST>;
+  auto k = k_outer_tma<Op, T, ST>;
   const int smem = ST * kTmaTileBytes;
   cudaError_t e = set_smem(k, smem);
   if (e != cudaSuccess) return e;
