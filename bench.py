@@ -384,7 +384,7 @@ def run_ours(args):
 
 
 CASES = ("bs_exact", "bs_fused", "bs_fast", "bs_fastnormcdf", "bs_f64", "saxpy", "sdot", "sdot_plain",
-         "rgb2grey_u8", "rgb2yuv", "mandelbrot", "reductions",
+         "rgb2grey_u8", "rgb2yuv", "mandelbrot", "reductions", "scans",
          "inner", "outer", "sigmadelta")
 
 
@@ -495,10 +495,33 @@ def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: in
         out.append({"config": "mandelbrot 1600x1600 over [-1.5,1.5]^2, pack 8 (FP32 issue-bound)", "ms": ms,
                     "value": h * w / (ms * 1e-3), "unit": "pixels/s",
                     "counted_trips_per_s": counts / (ms * 1e-3), "mean_count": counts / (h * w)})
-    if not (want("inner") or want("outer") or want("reductions") or want("bs_f64") or want("bs_fused") or want("bs_fast")
+    if not (want("inner") or want("outer") or want("reductions") or want("scans") or want("bs_f64") or want("bs_fused") or want("bs_fast")
             or want("bs_exact") or want("bs_fastnormcdf") or want("sigmadelta")):
         return out
     rows, cols = 8192, 4096
+    if want("scans"):
+        n = 1 << 26
+        x = torch.empty(n, device="cuda")
+        api.fill_normal(x, 21)
+        y = torch.empty(n, device="cuda")
+        ms, _, _ = time_device(lambda: api.cumulative("cumsum", x, n, 1, 1, out=y), K(50), warmup, ws)
+        out.append(line("cumsum f32 2^26 vector, compensated (64 KB tiles: aggregate, look-back, rescan from L2)", ms, 8 * n, n,
+                        "elements/s"))
+        del x, y
+        Ts = [torch.empty(rows * cols, device="cuda") for _ in range(2)]
+        for i in range(2):
+            api.fill_normal(Ts[i], 23 + i)
+        o = torch.empty(rows * cols, device="cuda")
+        it = [0]
+        for dim, note in ((1, "one 32 KB tile per column, single pass"), (2, "two passes: chunk totals, then rescan")):
+            def scan_step(dim=dim):
+                i = it[0] & 1
+                it[0] += 1
+                api.cumulative("cumsum", Ts[i], rows, cols, dim, out=o)
+            ms, _, _ = time_device(scan_step, K(50), warmup, ws)
+            out.append(line(f"cumsum(A,{dim}) 8192x4096 f32 ({note}; 8 B/element algorithmic)", ms,
+                            8 * rows * cols, rows * cols, "elements/s"))
+        del Ts, o
     if want("reductions"):
         # every reduction of the 8192 x 4096 table along each dimension, four rotating tables
         As = [torch.empty(rows * cols, device="cuda") for _ in range(4)]

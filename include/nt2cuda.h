@@ -248,6 +248,20 @@ nt2cuda_status nt2cuda_reduce_logical_f32(int op, const float* A, size_t rows, s
 nt2cuda_status nt2cuda_reduce_logical_f64(int op, const double* A, size_t rows, size_t cols, int dim, uint8_t* out,
                                           nt2cuda_stream stream);
 
+/* ------------------------------------------------------------- scans ---- */
+/* cumsum, cumprod, cummax, cummin of a rows x cols column-major table along
+ * dim 1 (down each column: inner_scan) or dim 2 (along each row: outer_scan)
+ * (modules/core/swar/include/nt2/dsl/functions/cumulative/run.hpp:27-75,
+ *  modules/boost/simd/base/include/boost/simd/swar/functions/{cumsum,cumprod,cummax,cummin}.hpp).
+ * out may be A itself (in place) but no other overlap.  FP32 cumsum carries
+ * compensated partial sums unless NT2CUDA_RED_PLAIN is set; cummax and cummin
+ * skip NaNs.  Results are bitwise reproducible from run to run. */
+enum { NT2CUDA_SCAN_SUM = 0, NT2CUDA_SCAN_PROD = 1, NT2CUDA_SCAN_MAX = 2, NT2CUDA_SCAN_MIN = 3 };
+nt2cuda_status nt2cuda_scan_f32(int op, const float* A, size_t rows, size_t cols, int dim, float* out, int flags,
+                                nt2cuda_stream stream);
+nt2cuda_status nt2cuda_scan_f64(int op, const double* A, size_t rows, size_t cols, int dim, double* out, int flags,
+                                nt2cuda_stream stream);
+
 /* --------------------------------------------------------- sigmadelta ---- */
 /* One grey video stream for the batched sigma-delta background subtraction
  * (demo/sigmadelta/nt2/sigmadelta_nt2.cpp:37-58, 85-106).  frames holds

@@ -259,6 +259,30 @@ def reduce(op: str, A: torch.Tensor, rows: int, cols: int, dim: int = 1, compens
     return out
 
 
+SCANS = {"cumsum": 0, "cumprod": 1, "cummax": 2, "cummin": 3}
+
+
+def cumulative(op: str, A: torch.Tensor, rows: int, cols: int, dim: int = 1, compensated: bool = True,
+               out: torch.Tensor | None = None) -> torch.Tensor:
+    """cumsum / cumprod / cummax / cummin of a rows x cols column-major table stored flat in A,
+    down each column (dim 1) or along each row (dim 2); out may be A (in place)."""
+    if A.numel() != rows * cols:
+        raise ValueError("A must hold rows*cols elements")
+    if dim not in (1, 2):
+        raise ValueError("dim must be 1 or 2")
+    out = torch.empty_like(A) if out is None else out
+    L = lib()
+    if A.dtype == torch.float32:
+        fn = L.nt2cuda_scan_f32
+    elif A.dtype == torch.float64:
+        fn = L.nt2cuda_scan_f64
+    else:
+        raise TypeError("cumulative functions take float32 or float64 tables")
+    check(fn(SCANS[op], _dev(A), rows, cols, dim, _dev(out, A.dtype), 0 if compensated else 1, _stream()),
+          f"{op}(A,{dim})")
+    return out
+
+
 def sd_streams(entries: Sequence[dict]) -> C.Array:
     """Build an nt2cuda_sd_stream array from dicts of tensors and sizes."""
     arr = (SdStream * len(entries))()

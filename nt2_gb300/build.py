@@ -25,6 +25,7 @@ SOURCES = [
     "capi_mandelbrot.cu",
     "capi_reduce_f32.cu",
     "capi_reduce_f64.cu",
+    "capi_scan.cu",
     "server.cu",
     "capi_noalloc.cu",
 ]

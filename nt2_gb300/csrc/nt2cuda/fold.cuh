@@ -86,6 +86,10 @@ template <bool COMP, int FIN = FIN_NONE> struct op_sum {
   {
     return acc<T>{__ldcg(&p->s), __ldcg(&p->c)};
   }
+  template <class T> __device__ __forceinline__ static state<T> shfl_from(state<T> a, int src)
+  {
+    return acc<T>{__shfl_sync(0xffffffffu, a.s, src), __shfl_sync(0xffffffffu, a.c, src)};
+  }
   template <class T> __device__ __forceinline__ static T finish(state<T> a, size_t n)
   {
     const T r = result<COMP>(a);
@@ -99,23 +103,28 @@ template <class T> struct val { T v; };
 
 // max / min / prod: one value; max and min ignore NaNs (NT2's result with NaNs
 // depends on its evaluation order), their neutral elements are NT2's Maxinit
-// (-largest finite) and Valmax (+largest finite).
-template <int KIND> struct op_val {   // 0 max, 1 min, 2 prod
+// (-largest finite) and Valmax (+largest finite).  KIND 3 and 4 are max and min
+// with the neutral elements of cummax and cummin, Minf and Inf
+// (boost/simd/swar/functions/cummax.hpp, cummin.hpp).
+template <int KIND> struct op_val {   // 0 max, 1 min, 2 prod, 3 cummax, 4 cummin
   template <class T> using state = val<T>;
   template <class T> using out_t = T;
   template <class T> __device__ __forceinline__ static state<T> init()
   {
     // largest finite value: NT2's Valmax, and -Valmax is its Maxinit (constant/constants/maxinit.hpp)
     const T big = sizeof(T) == 4 ? (T)3.40282346638528859812e+38 : (T)1.79769313486231570815e+308;
+    const T inf = sizeof(T) == 4 ? (T)__int_as_float(0x7f800000) : (T)__longlong_as_double(0x7ff0000000000000ll);
     if constexpr (KIND == 2) return val<T>{T(1)};
+    else if constexpr (KIND == 3) return val<T>{-inf};
+    else if constexpr (KIND == 4) return val<T>{inf};
     else return val<T>{KIND == 0 ? -big : big};
   }
   // a is the accumulator (never NaN), b the next element: NT2's max(a,b) = a > b ? a : b
   // (boost/simd/arithmetic/functions/scalar/max.hpp), except that a NaN b is skipped
   template <class T> __device__ __forceinline__ static T op(T a, T b)
   {
-    if constexpr (KIND == 0) return (a > b || b != b) ? a : b;
-    else if constexpr (KIND == 1) return (a < b || b != b) ? a : b;
+    if constexpr (KIND == 0 || KIND == 3) return (a > b || b != b) ? a : b;
+    else if constexpr (KIND == 1 || KIND == 4) return (a < b || b != b) ? a : b;
     else return math::mul(a, b);
   }
   template <class T> __device__ __forceinline__ static void add(state<T>& a, T x) { a.v = op(a.v, x); }
@@ -125,6 +134,10 @@ template <int KIND> struct op_val {   // 0 max, 1 min, 2 prod
     return val<T>{__shfl_xor_sync(0xffffffffu, a.v, off)};
   }
   template <class T> __device__ __forceinline__ static state<T> ldcg(const state<T>* p) { return val<T>{__ldcg(&p->v)}; }
+  template <class T> __device__ __forceinline__ static state<T> shfl_from(state<T> a, int src)
+  {
+    return val<T>{__shfl_sync(0xffffffffu, a.v, src)};
+  }
   template <class T> __device__ __forceinline__ static T finish(state<T> a, size_t) { return a.v; }
 };
 
