@@ -388,17 +388,19 @@ CASES = ("bs_exact", "bs_fused", "bs_fast", "bs_fastnormcdf", "bs_f64", "saxpy",
          "inner", "outer", "sigmadelta")
 
 
-def run_case(name: str, steps: int, warmup: int, autotune: bool = True):
-    """One configuration alone, for profiling: prints one JSON line."""
+def run_case(name: str, steps: int, warmup: int, autotune: bool = True, part: str | None = None):
+    """One configuration alone, for profiling: prints one JSON line (one per part of the
+    reductions and scans cases; `part` keeps only the parts whose label contains it)."""
     import torch
     torch.cuda.set_device(0)
     import nt2_gb300.api as api
     api.init(0)
-    for line in suite(1, only=name, steps=steps, warmup=warmup, autotune=autotune):
+    for line in suite(1, only=name, steps=steps, warmup=warmup, autotune=autotune, part=part):
         print(json.dumps(line), flush=True)
 
 
-def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: int = 3, autotune: bool = True):
+def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: int = 3, autotune: bool = True,
+          part: str | None = None):
     """One line per configuration (device time, inputs resident, > L2 or flushed)."""
     import torch
     import nt2_gb300.api as api
@@ -504,9 +506,10 @@ def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: in
         x = torch.empty(n, device="cuda")
         api.fill_normal(x, 21)
         y = torch.empty(n, device="cuda")
-        ms, _, _ = time_device(lambda: api.cumulative("cumsum", x, n, 1, 1, out=y), K(50), warmup, ws)
-        out.append(line("cumsum f32 2^26 vector, compensated (64 KB tiles: aggregate, look-back, rescan from L2)", ms, 8 * n, n,
-                        "elements/s"))
+        if part is None or part in "cumsum(x) 2^26":
+            ms, _, _ = time_device(lambda: api.cumulative("cumsum", x, n, 1, 1, out=y), K(50), warmup, ws)
+            out.append(line("cumsum(x) f32 2^26 vector, compensated (64 KB tiles: aggregate, look-back, rescan from L2)",
+                            ms, 8 * n, n, "elements/s"))
         del x, y
         Ts = [torch.empty(rows * cols, device="cuda") for _ in range(2)]
         for i in range(2):
@@ -514,6 +517,9 @@ def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: in
         o = torch.empty(rows * cols, device="cuda")
         it = [0]
         for dim, note in ((1, "one 32 KB tile per column, single pass"), (2, "two passes: chunk totals, then rescan")):
+            if part is not None and part not in f"cumsum(A,{dim})":
+                continue
+
             def scan_step(dim=dim):
                 i = it[0] & 1
                 it[0] += 1
@@ -531,6 +537,8 @@ def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: in
         for dim in (1, 2):
             m = cols if dim == 1 else rows
             for op in ("sum", "asum1", "norm2", "mean", "var", "max", "prod", "all"):
+                if part is not None and part != f"{op}(A,{dim})":
+                    continue
                 o = torch.empty(m, dtype=torch.uint8 if op == "all" else torch.float32, device="cuda")
 
                 def red_step(op=op, dim=dim, o=o):
@@ -658,12 +666,13 @@ def main():
     ap.add_argument("--case", choices=CASES, help="run one configuration alone (for profiling)")
     ap.add_argument("--no-autotune", action="store_true", help="with --case: default launch shapes")
     ap.add_argument("--tuning", default=None, help="tuning-table text to import first (\"key@bucket unroll waves\" lines)")
+    ap.add_argument("--part", default=None, help="with --case reductions/scans: one part, e.g. 'var(A,1)'")
     args = ap.parse_args()
     if args.tuning:
         import nt2_gb300.api as api
         api.tuning_import(args.tuning.replace(";", "\n"))
     if args.case:
-        run_case(args.case, args.steps, max(args.warmup, 3), autotune=not args.no_autotune)
+        run_case(args.case, args.steps, max(args.warmup, 3), autotune=not args.no_autotune, part=args.part)
     elif args.impl == "reference":
         run_reference(args)
     else:
