@@ -84,14 +84,21 @@ nt2cuda_status nt2cuda_stream_sync(nt2cuda_stream stream);
  * fastnormcdf/sqrt (modules/core/exponential/include/nt2/exponential/functions/generic/exp.hpp:19-32,
  * generic/log.hpp:20-31, modules/core/euler/include/nt2/euler/functions/simd/common/erfc.hpp:46-123,
  * modules/core/statistics/include/nt2/statistics/functions/generic/normcdf.hpp:28-34,
- * generic/fastnormcdf.hpp:33-55, boost/simd/arithmetic/functions/scalar/sqrt.hpp:21-62). */
+ * generic/fastnormcdf.hpp:33-55, boost/simd/arithmetic/functions/scalar/sqrt.hpp:21-62)
+ * and exp2/exp10/log2/log10
+ * (modules/core/exponential/include/nt2/exponential/functions/scalar/impl/expo/{f,d}_expo_reduction.hpp,
+ * simd/common/impl/logs/{f,d}_log.hpp). */
 enum {
   NT2CUDA_OP_EXP = 0,
   NT2CUDA_OP_LOG = 1,
   NT2CUDA_OP_ERFC = 2,
   NT2CUDA_OP_NORMCDF = 3,
   NT2CUDA_OP_FASTNORMCDF = 4, /* float only, as in NT2 */
-  NT2CUDA_OP_SQRT = 5
+  NT2CUDA_OP_SQRT = 5,
+  NT2CUDA_OP_EXP2 = 6,
+  NT2CUDA_OP_EXP10 = 7,
+  NT2CUDA_OP_LOG2 = 8,
+  NT2CUDA_OP_LOG10 = 9
 };
 
 /* y = op(x).  Replaces `y = nt2::op(x)` evaluated by transform_

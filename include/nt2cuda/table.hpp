@@ -285,6 +285,10 @@ inline auto operator-(const A& a) { return make_unary<tag::unary_minus_>(a); }
   inline auto NAME(const A& a) { return make_unary<tag::TAG>(a); }
 NT2CUDA_FN1(exp, exp_)
 NT2CUDA_FN1(log, log_)
+NT2CUDA_FN1(exp2, exp2_)
+NT2CUDA_FN1(exp10, exp10_)
+NT2CUDA_FN1(log2, log2_)
+NT2CUDA_FN1(log10, log10_)
 NT2CUDA_FN1(sqrt, sqrt_)
 NT2CUDA_FN1(sqr, sqr_)
 NT2CUDA_FN1(erfc, erfc_)
@@ -412,8 +416,8 @@ template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto globa
   check(cudaMalloc(&d, sizeof(A)), "globalsum alloc");
   cudaStream_t s = settings().stream;
   cudaError_t err = (std::is_same<A, float>::value && settings().compensated)
-                        ? fold::inner_fold<true, A>(e.e, e.size.numel(), 1, d, s)
-                        : fold::inner_fold<false, A>(e.e, e.size.numel(), 1, d, s);
+                        ? fold::inner_fold<fold::op_sum<true>, A>(e.e, e.size.numel(), 1, d, s)
+                        : fold::inner_fold<fold::op_sum<false>, A>(e.e, e.size.numel(), 1, d, s);
   A r = 0;
   if (err == cudaSuccess) err = cudaMemcpyAsync(&r, d, sizeof(A), cudaMemcpyDeviceToHost, s);
   if (err == cudaSuccess) err = cudaStreamSynchronize(s);
@@ -433,8 +437,8 @@ template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto sum(c
   if (dim == 1) {
     table<V> out(of_size(1, cols));
     cudaError_t err = settings().compensated && std::is_same<V, float>::value
-                          ? fold::inner_fold<true, V>(e.e, rows, cols, out.device(), s)
-                          : fold::inner_fold<false, V>(e.e, rows, cols, out.device(), s);
+                          ? fold::inner_fold<fold::op_sum<true>, V>(e.e, rows, cols, out.device(), s)
+                          : fold::inner_fold<fold::op_sum<false>, V>(e.e, rows, cols, out.device(), s);
     check(err, "sum(A,1)");
     out.mark_device_written();
     if (settings().synchronous) check(cudaStreamSynchronize(s), "sum");
@@ -442,8 +446,8 @@ template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto sum(c
   }
   table<V> out(of_size(rows, 1));
   cudaError_t err = settings().compensated && std::is_same<V, float>::value
-                        ? fold::outer_fold<true, V>(e.e, rows, cols, out.device(), s)
-                        : fold::outer_fold<false, V>(e.e, rows, cols, out.device(), s);
+                        ? fold::outer_fold<fold::op_sum<true>, V>(e.e, rows, cols, out.device(), s)
+                        : fold::outer_fold<fold::op_sum<false>, V>(e.e, rows, cols, out.device(), s);
   check(err, "sum(A,2)");
   out.mark_device_written();
   if (settings().synchronous) check(cudaStreamSynchronize(s), "sum");

@@ -123,6 +123,102 @@ __device__ __forceinline__ float log(float a0)
   return (a0 == 0.0f) ? __int_as_float(0xff800000) : r;
 }
 
+// ----------------------------------------------- exp2, exp10, log2, log10
+// The exp and log skeletons with NT2's other reductions and recombinations:
+// exp2/exp10 float: modules/core/exponential/include/nt2/exponential/functions/scalar/impl/expo/f_expo_reduction.hpp:88-143,
+// log2/log10 float: .../functions/simd/common/impl/logs/f_log.hpp:126-170 (constants: exponential/constants/*.hpp).
+struct cf2 {
+  static constexpr uint32_t maxlog2 = 0x42fe0000u, minlog2 = 0xc2fe0000u, maxlog10 = 0x4218ec59u,
+                            minlog10 = 0xc2179999u, invlog10_2 = 0x40549a78u, log10_2hi = 0x3e9a0000u,
+                            log10_2lo = 0x39826a14u, log_2 = 0x3f317218u, log2_em1 = 0x3ee2a8edu,
+                            log10_elo = 0x3a37b152u, log10_ehi = 0x3ede0000u, mlog2two2nmb = 0xc1b80000u,
+                            mlog10two2nmb = 0xc0dd8edeu;
+};
+
+// expo_base selections (simd/common/impl/expo/expo_base.hpp:48-62) and the
+// exponent-bit scale by 2^k (scalar/impl/expo/expo_scale.hpp:26-35)
+__device__ __forceinline__ float expo_select(float a0, float c, float k, float minl, float maxl)
+{
+  unsigned ik = (unsigned)((int)k + 127);
+  float r = mul(c, __uint_as_float(ik << 23));
+  r = (a0 <= minl) ? 0.0f : r;
+  r = (a0 >= maxl) ? __int_as_float(0x7f800000) : r;
+  return (a0 != a0) ? a0 : r;
+}
+
+template <bool F = false>
+__device__ __forceinline__ float exp2(float a0)
+{
+  constexpr uint32_t P[5] = {0x3922c8c4u, 0x3ab01218u, 0x3c1d9422u, 0x3d6356ebu, 0x3e75fdf1u};
+  float k = rintf(a0);
+  float x = sub(a0, k);
+  float y = horner<F>(x, P);
+  float c = add(madd<F>(y, mul(x, x), mul(x, fbits(cf2::log_2))), 1.0f);   // inc(fma(y, sqr(x), x*Log_2))
+  return expo_select(a0, c, k, fbits(cf2::minlog2), fbits(cf2::maxlog2));
+}
+
+template <bool F = false>
+__device__ __forceinline__ float exp10(float a0)
+{
+  constexpr uint32_t P[6] = {0x3e54dff1u, 0x3f0aacefu, 0x3f95eb4cu, 0x400237dau, 0x4029a926u, 0x40135d8eu};
+  float k = rintf(mul(fbits(cf2::invlog10_2), a0));
+  float x = nmsub<F>(k, fbits(cf2::log10_2hi), a0);
+  x = nmsub<F>(k, fbits(cf2::log10_2lo), x);
+  float c = madd<F>(horner<F>(x, P), x, 1.0f);                               // inc(horner(x)*x)
+  return expo_select(a0, c, k, fbits(cf2::minlog10), fbits(cf2::maxlog10));
+}
+
+// the float log kernel (scalar/impl/logs/f_kernel.hpp:43-73) after f_log.hpp's denormal rescale
+struct logparts { float fe, x, x2, y, t; };
+template <bool F>
+__device__ __forceinline__ logparts log_kernel(float a0, float mtwo2nmb)
+{
+  constexpr uint32_t P[8] = {0xbda5dff0u, 0x3e0229f9u, 0xbe04d6b7u, 0x3e116e80u,
+                             0xbe2a6aa0u, 0x3e4cd0a3u, 0xbe800064u, 0x3eaaaaa9u};
+  logparts p;
+  float z = a0;
+  p.t = 0.0f;
+  if (fabsf(z) < fbits(cf::smallestposval)) { z = mul(z, fbits(cf::twotonmb)); p.t = mtwo2nmb; }
+  uint32_t u = __float_as_uint(z);
+  int e = (int)((u & 0x7f800000u) >> 23) - 126;
+  float x = __uint_as_float((u & ~0x7f800000u) | 0x3f000000u);   // fast_frexp
+  bool lt = x < fbits(cf::sqrt_2o_2);
+  p.fe = lt ? add((float)e, -1.0f) : (float)e;
+  p.x = sub(lt ? add(x, x) : x, 1.0f);
+  p.x2 = mul(p.x, p.x);
+  p.y = mul(mul(horner<F>(p.x, P), p.x), p.x2);
+  return p;
+}
+
+// f_log.hpp finalize (:173-186)
+__device__ __forceinline__ float log_finalize(float a0, float r)
+{
+  r = (a0 < 0.0f || a0 != a0) ? __int_as_float(0x7fffffff) : r;
+  r = (a0 == __int_as_float(0x7f800000)) ? a0 : r;
+  return (a0 == 0.0f) ? __int_as_float(0xff800000) : r;
+}
+
+template <bool F = false>
+__device__ __forceinline__ float log2(float a0)
+{
+  logparts p = log_kernel<F>(a0, fbits(cf2::mlog2two2nmb));
+  float y = madd<F>(-0.5f, p.x2, p.y);
+  float z = madd<F>(p.x, fbits(cf2::log2_em1), mul(y, fbits(cf2::log2_em1)));
+  return log_finalize(a0, add(add(add(add(z, y), p.x), p.fe), p.t));
+}
+
+template <bool F = false>
+__device__ __forceinline__ float log10(float a0)
+{
+  logparts p = log_kernel<F>(a0, fbits(cf2::mlog10two2nmb));
+  float y = madd<F>(-0.5f, p.x2, p.y);                       // amul(y, Mhalf, x2)
+  float z = mul(add(p.x, y), fbits(cf2::log10_elo));
+  z = madd<F>(y, fbits(cf2::log10_ehi), z);                  // amul(z, y, Log10_ehi)
+  z = madd<F>(p.x, fbits(cf2::log10_ehi), z);
+  z = madd<F>(p.fe, fbits(cf2::log10_2hi), z);
+  return log_finalize(a0, madd<F>(p.fe, fbits(cf2::log10_2lo), add(z, p.t)));
+}
+
 // --------------------------------------------------------------- float erfc
 // modules/core/euler/include/nt2/euler/functions/simd/common/erfc.hpp:92-121
 // kernels: modules/core/euler/include/nt2/euler/functions/details/erf_kernel.hpp:48-85
@@ -262,6 +358,101 @@ __device__ __forceinline__ double log(double a0)
   y = (a0 < 0.0 || a0 != a0) ? __longlong_as_double(0x7fffffffffffffffll) : y;
   y = (a0 == __longlong_as_double(0x7ff0000000000000ll)) ? a0 : y;
   return (a0 == 0.0) ? __longlong_as_double((long long)0xfff0000000000000ull) : y;
+}
+
+// ------------------------------------ double exp2, exp10, log2, log10
+// exp2/exp10: .../scalar/impl/expo/d_expo_reduction.hpp:85-160 with expo_base.hpp:26-45;
+// log2/log10: .../simd/common/impl/logs/d_log.hpp:99-121.
+struct cd2 {
+  static constexpr uint64_t maxlog2 = 0x408ff80000000000ull, minlog2 = 0xc08ff00000000000ull,
+                            maxlog10 = 0x40734413509f79feull, minlog10 = 0xc0734413509f79feull,
+                            invlog10_2 = 0x400a934f0979a372ull, log10_2hi = 0x3fd3440000000000ull,
+                            log10_2lo = 0x3ed3509f79fef312ull, log_2 = 0x3fe62e42fefa39efull,
+                            invlog_10 = 0x3fdbcb7b1526e50dull, log_2olog_10 = 0x3fd34413509f79ffull;
+};
+
+__device__ __forceinline__ double expo_select(double a0, double c, double k, double minl, double maxl)
+{
+  unsigned long long ik = (unsigned long long)((long long)k + 1023);
+  double r = mul(c, __longlong_as_double((long long)(ik << 52)));
+  r = (a0 <= minl) ? 0.0 : r;
+  r = (a0 >= maxl) ? __longlong_as_double(0x7ff0000000000000ll) : r;
+  return (a0 != a0) ? a0 : r;
+}
+
+template <bool F = false>
+__device__ __forceinline__ double exp2(double a0)
+{
+  constexpr uint64_t P[5] = {0x3e66376972bea4d0ull, 0xbebbbd41c5d26bf1ull, 0x3f11566aaf25de2cull,
+                             0xbf66c16c16bebd93ull, 0x3fc555555555553eull};
+  double k = rint(a0);
+  double x = mul(sub(a0, k), dbits(cd2::log_2));
+  double t = mul(x, x);
+  double c = nmsub<F>(t, horner<F>(t, P), x);
+  c = sub(1.0, sub(div(-mul(x, c), sub(2.0, c)), x));       // oneminus(((-(x*c)/(2-c))-x))
+  return expo_select(a0, c, k, dbits(cd2::minlog2), dbits(cd2::maxlog2));
+}
+
+template <bool F = false>
+__device__ __forceinline__ double exp10(double a0)
+{
+  constexpr uint64_t P[4] = {0x3fa4fd75f3062dd4ull, 0x40277d9474c55934ull, 0x40796b7a050349e4ull,
+                             0x40a2b4798e134a01ull};
+  constexpr uint64_t Q[4] = {0x3ff0000000000000ull, 0x405545fdce51ca08ull, 0x4093e05eefd67782ull,
+                             0x40a03f37650df6e2ull};
+  double k = rint(mul(dbits(cd2::invlog10_2), a0));
+  double x = nmsub<F>(k, dbits(cd2::log10_2hi), a0);
+  x = nmsub<F>(k, dbits(cd2::log10_2lo), x);
+  double xx = mul(x, x);
+  double px = mul(x, horner<F>(xx, P));
+  double x2 = div(px, sub(horner<F>(xx, Q), px));
+  double c = add(add(x2, x2), 1.0);                         // oneplus(x2+x2)
+  return expo_select(a0, c, k, dbits(cd2::minlog10), dbits(cd2::maxlog10));
+}
+
+// d_log.hpp kernel_log (:57-87): returns -(hfsq - s*(hfsq+R) - f), the log of the mantissa
+template <bool F>
+__device__ __forceinline__ double log_mantissa(double a0, double& dk)
+{
+  constexpr uint64_t T1[3] = {0x3fc39a09d078c69full, 0x3fcc71c51d8e78afull, 0x3fd999999997fa04ull};
+  constexpr uint64_t T2[4] = {0x3fc2f112df3e5244ull, 0x3fc7466496cb03deull, 0x3fd2492494229359ull,
+                              0x3fe5555555555593ull};
+  unsigned long long u = (unsigned long long)__double_as_longlong(a0);
+  long long k = (long long)((u & 0x7ff0000000000000ull) >> 52) - 1022;
+  double x = __longlong_as_double((long long)((u & ~0x7ff0000000000000ull) | 0x3fe0000000000000ull));
+  bool lt = dbits(cd::sqrt_2o_2) > x;
+  k = k + (lt ? -1 : 0);
+  double f = sub(add(x, lt ? x : 0.0), 1.0);
+  dk = (double)k;
+  double s = div(f, add(2.0, f));
+  double z = mul(s, s);
+  double w = mul(z, z);
+  double R = add(mul(z, horner<F>(w, T2)), mul(w, horner<F>(w, T1)));
+  double hfsq = mul(0.5, mul(f, f));
+  return -sub(sub(hfsq, mul(s, add(hfsq, R))), f);
+}
+
+__device__ __forceinline__ double log_finalize(double a0, double y)
+{
+  y = (a0 < 0.0 || a0 != a0) ? __longlong_as_double(0x7fffffffffffffffll) : y;
+  y = (a0 == __longlong_as_double(0x7ff0000000000000ll)) ? a0 : y;
+  return (a0 == 0.0) ? __longlong_as_double((long long)0xfff0000000000000ull) : y;
+}
+
+template <bool F = false>
+__device__ __forceinline__ double log2(double a0)
+{
+  double dk;
+  const double m = log_mantissa<F>(a0, dk);
+  return log_finalize(a0, madd<F>(m, dbits(cd::invlog_2), dk));
+}
+
+template <bool F = false>
+__device__ __forceinline__ double log10(double a0)
+{
+  double dk;
+  const double m = log_mantissa<F>(a0, dk);
+  return log_finalize(a0, madd<F>(m, dbits(cd2::invlog_10), mul(dk, dbits(cd2::log_2olog_10))));
 }
 
 // -------------------------------------------------------------- double erfc

@@ -309,6 +309,185 @@ EXPORT double nt2o_log_d(double a0)
   return y;
 }
 
+/* ------------------------------------------- exp2, exp10, log2, log10 -- */
+/* Same skeletons as exp and log with NT2's other reductions and recombinations:
+ * exp2/exp10 float: exponential/functions/scalar/impl/expo/f_expo_reduction.hpp:88-143,
+ * double: d_expo_reduction.hpp:85-160, selections simd/common/impl/expo/expo_base.hpp:26-65;
+ * log2/log10 float: simd/common/impl/logs/f_log.hpp:126-170, double:
+ * simd/common/impl/logs/d_log.hpp:99-121.  Constants: exponential/constants/*.hpp. */
+#define MAXLOG2_F     fb(0x42fe0000u)
+#define MINLOG2_F     fb(0xc2fe0000u)
+#define MAXLOG10_F    fb(0x4218ec59u)
+#define MINLOG10_F    fb(0xc2179999u)
+#define INVLOG10_2_F  fb(0x40549a78u)
+#define LOG10_2HI_F   fb(0x3e9a0000u)
+#define LOG10_2LO_F   fb(0x39826a14u)
+#define LOG_2_F       fb(0x3f317218u)
+#define LOG2_EM1_F    fb(0x3ee2a8edu)
+#define LOG10_ELO_F   fb(0x3a37b152u)
+#define LOG10_EHI_F   fb(0x3ede0000u)
+#define MLOG2TWO2NMB_F  fb(0xc1b80000u)
+#define MLOG10TWO2NMB_F fb(0xc0dd8edeu)
+#define MAXLOG2_D     db(0x408ff80000000000ull)
+#define MINLOG2_D     db(0xc08ff00000000000ull)
+#define MAXLOG10_D    db(0x40734413509f79feull)
+#define MINLOG10_D    db(0xc0734413509f79feull)
+#define INVLOG10_2_D  db(0x400a934f0979a372ull)
+#define LOG10_2HI_D   db(0x3fd3440000000000ull)
+#define LOG10_2LO_D   db(0x3ed3509f79fef312ull)
+#define LOG_2_D       db(0x3fe62e42fefa39efull)
+#define INVLOG_10_D   db(0x3fdbcb7b1526e50dull)
+#define LOG_2OLOG_10_D db(0x3fd34413509f79ffull)
+
+static const uint32_t EXP2_F_P[5] = {0x3922c8c4u, 0x3ab01218u, 0x3c1d9422u, 0x3d6356ebu, 0x3e75fdf1u};
+static const uint32_t EXP10_F_P[6] = {0x3e54dff1u, 0x3f0aacefu, 0x3f95eb4cu, 0x400237dau, 0x4029a926u, 0x40135d8eu};
+static const uint64_t EXP10_D_P[4] = {0x3fa4fd75f3062dd4ull, 0x40277d9474c55934ull, 0x40796b7a050349e4ull,
+                                      0x40a2b4798e134a01ull};
+static const uint64_t EXP10_D_Q[4] = {0x3ff0000000000000ull, 0x405545fdce51ca08ull, 0x4093e05eefd67782ull,
+                                      0x40a03f37650df6e2ull};
+
+/* the guards of expo_base: NaN -> NaN, >= maxlog -> Inf, <= minlog -> 0, else scale(c, k) */
+static inline float expo_select_f(float a0, float c, float k, float minl, float maxl)
+{
+  if (isnan(a0)) return a0;
+  if (a0 >= maxl) return INFINITY;
+  if (a0 <= minl) return 0.0f;
+  return scale_f(c, k);
+}
+static inline double expo_select_d(double a0, double c, double k, double minl, double maxl)
+{
+  if (isnan(a0)) return a0;
+  if (a0 >= maxl) return INFINITY;
+  if (a0 <= minl) return 0.0;
+  return scale_d(c, k);
+}
+
+EXPORT float nt2o_exp2_f(float a0)
+{
+  float k = r2e_f(a0);
+  float x = a0 - k;
+  float y = horner_f(x, EXP2_F_P, 5);
+  float c = (y * (x * x) + x * LOG_2_F) + 1.0f;           /* inc(fma(y, sqr(x), x*Log_2)) */
+  return expo_select_f(a0, c, k, MINLOG2_F, MAXLOG2_F);
+}
+
+EXPORT float nt2o_exp10_f(float a0)
+{
+  float k = r2e_f(INVLOG10_2_F * a0);
+  float x = a0 - k * LOG10_2HI_F;                          /* fnms(k, Log10_2hi, a0) */
+  x = x - k * LOG10_2LO_F;
+  float c = horner_f(x, EXP10_F_P, 6) * x + 1.0f;          /* inc(horner(x)*x) */
+  return expo_select_f(a0, c, k, MINLOG10_F, MAXLOG10_F);
+}
+
+EXPORT double nt2o_exp2_d(double a0)
+{
+  double k = r2e_d(a0);
+  double x = (a0 - k) * LOG_2_D;
+  double t = x * x;
+  double c = x - t * horner_d(t, EXP_D_P, 5);             /* approx: fnms(t, horner(t), x) */
+  c = 1.0 - ((-(x * c) / (2.0 - c)) - x);                  /* finalize: oneminus(...) */
+  return expo_select_d(a0, c, k, MINLOG2_D, MAXLOG2_D);
+}
+
+EXPORT double nt2o_exp10_d(double a0)
+{
+  double k = r2e_d(INVLOG10_2_D * a0);
+  double x = a0 - k * LOG10_2HI_D;
+  x = x - k * LOG10_2LO_D;
+  double xx = x * x;
+  double px = x * horner_d(xx, EXP10_D_P, 4);
+  double x2 = px / (horner_d(xx, EXP10_D_Q, 4) - px);
+  double c = (x2 + x2) + 1.0;                              /* oneplus(x2+x2) */
+  return expo_select_d(a0, c, k, MINLOG10_D, MAXLOG10_D);
+}
+
+/* the float log kernel (f_kernel.hpp:43-73) after the denormal rescale of f_log.hpp */
+static inline void log_kernel_f(float a0, float mtwo2nmb, float* fe, float* x, float* x2, float* y, float* t)
+{
+  float z = a0;
+  *t = 0.0f;
+  if (fabsf(z) < SMALLESTPOSVAL_F) { z = z * TWOTONMB_F; *t = mtwo2nmb; }
+  int32_t e;
+  float m = frexp_f(z, &e);
+  int lt = m < SQRT_2O_2_F;
+  *fe = lt ? ((float)e + -1.0f) : (float)e;
+  *x = (lt ? m + m : m) - 1.0f;
+  *x2 = *x * *x;
+  *y = (horner_f(*x, LOG_F_P, 8) * *x) * *x2;
+}
+
+static inline float log_finalize_f(float a0, float r)
+{
+  if (a0 < 0.0f || isnan(a0)) r = NAN;
+  if (a0 == INFINITY) r = a0;
+  if (a0 == 0.0f) r = -INFINITY;
+  return r;
+}
+
+EXPORT float nt2o_log2_f(float a0)
+{
+  float fe, x, x2, y, t;
+  log_kernel_f(a0, MLOG2TWO2NMB_F, &fe, &x, &x2, &y, &t);
+  y = -0.5f * x2 + y;                                      /* fma(Mhalf, x2, y) */
+  float z = x * LOG2_EM1_F + y * LOG2_EM1_F;               /* fma(x, Log2_em1, y*Log2_em1) */
+  return log_finalize_f(a0, (((z + y) + x) + fe) + t);
+}
+
+EXPORT float nt2o_log10_f(float a0)
+{
+  float fe, x, x2, y, t;
+  log_kernel_f(a0, MLOG10TWO2NMB_F, &fe, &x, &x2, &y, &t);
+  y = -0.5f * x2 + y;                                      /* amul(y, Mhalf, x2) */
+  float z = (x + y) * LOG10_ELO_F;
+  z = y * LOG10_EHI_F + z;                                 /* amul(z, y, Log10_ehi) */
+  z = x * LOG10_EHI_F + z;
+  z = fe * LOG10_2HI_F + z;
+  return log_finalize_f(a0, fe * LOG10_2LO_F + (z + t));   /* amul(z+t, fe, Log10_2lo) */
+}
+
+/* the double log kernel of d_log.hpp:57-87 */
+static inline void log_kernel_d(double a0, double* dk, double* hfsq, double* s, double* R, double* f)
+{
+  int64_t k;
+  double x = frexp_d(a0, &k);
+  int lt = SQRT_2O_2_D > x;
+  k = k + (lt ? -1 : 0);
+  *f = (x + (lt ? x : 0.0)) - 1.0;
+  *dk = (double)k;
+  *s = *f / (2.0 + *f);
+  double z = *s * *s;
+  double w = z * z;
+  double t1 = w * horner_d(w, LOG_D_T1, 3);
+  double t2 = z * horner_d(w, LOG_D_T2, 4);
+  *R = t2 + t1;
+  *hfsq = 0.5 * (*f * *f);
+}
+
+static inline double log_finalize_d(double a0, double y)
+{
+  if (a0 < 0.0 || isnan(a0)) y = NAN;
+  if (a0 == INFINITY) y = a0;
+  if (a0 == 0.0) y = -INFINITY;
+  return y;
+}
+
+EXPORT double nt2o_log2_d(double a0)
+{
+  double dk, hfsq, s, R, f;
+  log_kernel_d(a0, &dk, &hfsq, &s, &R, &f);
+  double y = (-((hfsq - s * (hfsq + R)) - f)) * INVLOG_2_D + dk;
+  return log_finalize_d(a0, y);
+}
+
+EXPORT double nt2o_log10_d(double a0)
+{
+  double dk, hfsq, s, R, f;
+  log_kernel_d(a0, &dk, &hfsq, &s, &R, &f);
+  double y = (-((hfsq - s * (hfsq + R)) - f)) * INVLOG_10_D + dk * LOG_2OLOG_10_D;
+  return log_finalize_d(a0, y);
+}
+
 /* ---------------------------------------------------------- double erfc -- */
 /* euler/functions/simd/common/erfc.hpp:46-89, kernels
  * euler/functions/details/erf_kernel.hpp:101-163 (rational 5/5, 7/7, 7/7) */
@@ -382,7 +561,7 @@ EXPORT double nt2o_erfc_d_scalar(double a0)
 
 /* ------------------------------------------------------------- maps ------ */
 enum { OP_EXP = 0, OP_LOG = 1, OP_ERFC = 2, OP_NORMCDF = 3, OP_FASTNORMCDF = 4, OP_SQRT = 5,
-       OP_ERFC_SCALAR = 6 };
+       OP_ERFC_SCALAR = 6, OP_EXP2 = 7, OP_EXP10 = 8, OP_LOG2 = 9, OP_LOG10 = 10 };
 
 EXPORT int nt2o_map_f(int op, const float* x, float* y, size_t n)
 {
@@ -396,6 +575,10 @@ EXPORT int nt2o_map_f(int op, const float* x, float* y, size_t n)
       case OP_FASTNORMCDF: y[i] = nt2o_fastnormcdf_f(a); break;
       case OP_SQRT: y[i] = sqrtf(a); break;
       case OP_ERFC_SCALAR: y[i] = nt2o_erfc_f_scalar(a); break;
+      case OP_EXP2: y[i] = nt2o_exp2_f(a); break;
+      case OP_EXP10: y[i] = nt2o_exp10_f(a); break;
+      case OP_LOG2: y[i] = nt2o_log2_f(a); break;
+      case OP_LOG10: y[i] = nt2o_log10_f(a); break;
       default: return 1;
     }
   }
@@ -413,6 +596,10 @@ EXPORT int nt2o_map_d(int op, const double* x, double* y, size_t n)
       case OP_NORMCDF: y[i] = nt2o_normcdf_d(a); break;
       case OP_SQRT: y[i] = sqrt(a); break;
       case OP_ERFC_SCALAR: y[i] = nt2o_erfc_d_scalar(a); break;
+      case OP_EXP2: y[i] = nt2o_exp2_d(a); break;
+      case OP_EXP10: y[i] = nt2o_exp10_d(a); break;
+      case OP_LOG2: y[i] = nt2o_log2_d(a); break;
+      case OP_LOG10: y[i] = nt2o_log10_d(a); break;
       default: return 1;
     }
   }

@@ -22,7 +22,8 @@ SPECIALS = [0.0, -0.0, 1.0, -1.0, 0.5, 2.0, np.inf, -np.inf, np.nan, 88.5, -88.5
 
 def inputs(op, n, dtype, seed):
     rng = np.random.default_rng(seed)
-    lo, hi = {"exp": (-100, 100), "log": (0, 100), "sqrt": (0, 100)}.get(op, (-10, 10))
+    lo, hi = {"exp": (-100, 100), "log": (0, 100), "sqrt": (0, 100), "exp2": (-150, 150), "exp10": (-45, 45),
+              "log2": (0, 100), "log10": (0, 100)}.get(op, (-10, 10))
     x = rng.uniform(lo, hi, n).astype(dtype)
     sp = np.array(SPECIALS, dtype)
     x[: len(sp)] = sp
@@ -31,11 +32,11 @@ def inputs(op, n, dtype, seed):
 
 def main():
     out = {}
-    for i, op in enumerate(["exp", "log", "erfc", "normcdf", "fastnormcdf", "sqrt"]):
+    for i, op in enumerate(["exp", "log", "erfc", "normcdf", "fastnormcdf", "sqrt", "exp2", "exp10", "log2", "log10"]):
         x = inputs(op, 2048, np.float32, 100 + i)
         out[f"map_f32_{op}_x"] = x
         out[f"map_f32_{op}_y"] = oracle_lib.map_(op, x)
-    for i, op in enumerate(["exp", "log", "erfc", "normcdf", "sqrt"]):
+    for i, op in enumerate(["exp", "log", "erfc", "normcdf", "sqrt", "exp2", "exp10", "log2", "log10"]):
         x = inputs(op, 2048, np.float64, 200 + i)
         out[f"map_f64_{op}_x"] = x
         out[f"map_f64_{op}_y"] = oracle_lib.map_(op, x)
@@ -66,6 +67,16 @@ def main():
     frames[2 * npix + 100:2 * npix + 700] = 255
     b, vv, lab = oracle_lib.sigmadelta(frames, npix, npix, nf, init=True)
     out.update(sd_frames=frames, sd_bkg=b, sd_var=vv, sd_labels=lab, sd_npix=np.array(npix), sd_nframes=np.array(nf))
+    # image statements: uint8 rgb2grey, rgb2yuv, and the mandelbrot program at pack widths 1 and 8
+    r8, g8, b8 = (rng.integers(0, 256, 5000, dtype=np.uint8) for _ in range(3))
+    gr8 = np.empty_like(r8)
+    oracle_lib.load().nt2o_rgb2grey_u8(r8, g8, b8, gr8, r8.size, 1)
+    out.update(grey8_r=r8, grey8_g=g8, grey8_b=b8, grey8_out=gr8)
+    rf, gf, bf = (rng.uniform(0, 255, 5000).astype(np.float32) for _ in range(3))
+    yy_, uu_, vv_ = oracle_lib.rgb2yuv(rf, gf, bf)
+    out.update(yuv_r=rf, yuv_g=gf, yuv_b=bf, yuv_y=yy_, yuv_u=uu_, yuv_v=vv_)
+    for pack in (1, 8):
+        out[f"mandel_p{pack}"] = oracle_lib.mandelbrot_grid(-1.5, 1.5, -1.5, 1.5, 160, 160, pack=pack)
     np.savez_compressed(os.path.join(HERE, "nt2_golden.npz"), **out)
     print("wrote", os.path.join(HERE, "nt2_golden.npz"), sum(a.nbytes for a in out.values()), "bytes raw")
 

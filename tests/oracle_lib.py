@@ -35,6 +35,14 @@ SIGS = {
     "nt2o_normcdf_f": (C.c_float, [C.c_float]),
     "nt2o_fastnormcdf_f": (C.c_float, [C.c_float]),
     "nt2o_exp_d": (C.c_double, [C.c_double]),
+    "nt2o_exp2_f": (C.c_float, [C.c_float]),
+    "nt2o_exp10_f": (C.c_float, [C.c_float]),
+    "nt2o_log2_f": (C.c_float, [C.c_float]),
+    "nt2o_log10_f": (C.c_float, [C.c_float]),
+    "nt2o_exp2_d": (C.c_double, [C.c_double]),
+    "nt2o_exp10_d": (C.c_double, [C.c_double]),
+    "nt2o_log2_d": (C.c_double, [C.c_double]),
+    "nt2o_log10_d": (C.c_double, [C.c_double]),
     "nt2o_log_d": (C.c_double, [C.c_double]),
     "nt2o_erfc_d": (C.c_double, [C.c_double]),
     "nt2o_erfc_d_scalar": (C.c_double, [C.c_double]),
@@ -65,7 +73,8 @@ SIGS = {
     "nt2o_max_threads": (C.c_int, []),
 }
 
-OP = {"exp": 0, "log": 1, "erfc": 2, "normcdf": 3, "fastnormcdf": 4, "sqrt": 5, "erfc_scalar": 6}
+OP = {"exp": 0, "log": 1, "erfc": 2, "normcdf": 3, "fastnormcdf": 4, "sqrt": 5, "erfc_scalar": 6,
+      "exp2": 7, "exp10": 8, "log2": 9, "log10": 10}
 
 
 def load(variant: str = "libnt2oracle.so"):

@@ -67,3 +67,12 @@ def test_tuning_table_roundtrip(cuda_lib):
     assert "bs_f32@24 4 2" in text and "saxpy_f32@24 1 1" in text and "bogus" not in text
     small = C.create_string_buffer(4)
     assert L.nt2cuda_tuning_export(small, 4, C.byref(need)) == 1
+
+
+def test_demo_programs_compile():
+    """NT2's demo statements written against the C++ front end compile (nvcc cross-compiles
+    for sm_103a without a GPU), so a change to the kernels' templates cannot break them unseen."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "nt2_gb300", "demo"))
+    import build_demos
+    assert os.path.exists(build_demos.build())

@@ -20,8 +20,8 @@ def same(a, b):
     return bool(np.array_equal(a, b))
 
 
-OPS32 = ["exp", "log", "erfc", "normcdf", "fastnormcdf", "sqrt"]
-OPS64 = ["exp", "log", "erfc", "normcdf", "sqrt"]
+OPS32 = ["exp", "log", "erfc", "normcdf", "fastnormcdf", "sqrt", "exp2", "exp10", "log2", "log10"]
+OPS64 = ["exp", "log", "erfc", "normcdf", "sqrt", "exp2", "exp10", "log2", "log10"]
 
 
 @pytest.mark.parametrize("op", OPS32)
@@ -88,3 +88,25 @@ def test_device_reproduces_golden_statements(gpu):
     gpu.sigmadelta_batch([e], nf, init=True)
     assert same(host(e["bkg"]), G["sd_bkg"]) and same(host(e["var"]), G["sd_var"])
     assert same(host(e["labels"])[: (nf - 1) * npix], G["sd_labels"])
+
+
+def test_oracle_reproduces_golden_images(oracle):
+    gr = np.empty_like(G["grey8_r"])
+    oracle.load().nt2o_rgb2grey_u8(G["grey8_r"], G["grey8_g"], G["grey8_b"], gr, gr.size, 1)
+    assert same(gr, G["grey8_out"])
+    for got, key in zip(oracle.rgb2yuv(G["yuv_r"], G["yuv_g"], G["yuv_b"]), ("yuv_y", "yuv_u", "yuv_v")):
+        assert same(got, G[key])
+    for pack in (1, 8):
+        assert same(oracle.mandelbrot_grid(-1.5, 1.5, -1.5, 1.5, 160, 160, pack=pack), G[f"mandel_p{pack}"])
+
+
+@pytest.mark.gpu
+def test_gpu_reproduces_golden_images(gpu):
+    import torch
+    d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    h = lambda t: (torch.cuda.synchronize(), t.cpu().numpy())[1]
+    assert same(h(gpu.rgb2grey(d(G["grey8_r"]), d(G["grey8_g"]), d(G["grey8_b"]))), G["grey8_out"])
+    for got, key in zip(gpu.rgb2yuv(d(G["yuv_r"]), d(G["yuv_g"]), d(G["yuv_b"])), ("yuv_y", "yuv_u", "yuv_v")):
+        assert same(h(got), G[key])
+    for pack in (1, 8):
+        assert same(h(gpu.mandelbrot_grid(-1.5, 1.5, -1.5, 1.5, 160, 160, pack=pack)), G[f"mandel_p{pack}"])

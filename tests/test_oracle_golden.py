@@ -226,3 +226,55 @@ def test_blackscholes_oracle_sane(oracle):
     assert np.max(np.abs(lhs - rhs) / (1 + np.abs(K))) < 2e-5
     c64, p64 = oracle.bs(S.astype(np.float64), K.astype(np.float64), T.astype(np.float64), 0.02, 0.30)
     assert np.max(np.abs(call - c64) / (1 + np.abs(c64))) < 1e-4
+
+
+# ---------------------------------------------------------- exp2, exp10, log2, log10
+# special values: modules/core/exponential/unit/scalar/{exp2,exp10,log2,log10}.cpp (0 ULP)
+EXPLOG_SPECIALS = {
+    "exp2": [(INF, INF), (-INF, 0.0), (NAN, NAN), (-1.0, 0.5), (1.0, 2.0), (0.0, 1.0)],
+    "exp10": [(INF, INF), (-INF, 0.0), (NAN, NAN), (-1.0, 0.1), (1.0, 10.0), (0.0, 1.0)],
+    "log2": [(INF, INF), (-INF, NAN), (NAN, NAN), (-1.0, NAN), (0.0, -INF), (1.0, 0.0), (2.0, 1.0),
+             (8.0, 3.0), (64.0, 6.0)],
+    "log10": [(INF, INF), (-INF, NAN), (NAN, NAN), (-1.0, NAN), (0.0, -INF), (1.0, 0.0), (10.0, 1.0),
+              (100.0, 2.0)],
+}
+
+
+@pytest.mark.parametrize("fn", sorted(EXPLOG_SPECIALS))
+@pytest.mark.parametrize("prec", ["f", "d"])
+def test_explog_special_values(oracle, fn, prec):
+    L = oracle.load()
+    f = getattr(L, f"nt2o_{fn}_{prec}")
+    u = ulp_f if prec == "f" else ulp_d
+    cast = f32 if prec == "f" else float
+    for x, r in EXPLOG_SPECIALS[fn]:
+        assert u(L, f(x), cast(r)) == 0.0, (fn, prec, x)
+
+
+# cover tests: modules/core/exponential/cover/scalar/{exp2,exp10,log2,log10}.cpp -- the range and the
+# ulp bound against a high-precision reference (cephes long double there, FP64 / mpmath here)
+EXPLOG_COVER = {"exp2": (-100.0, 100.0, 7.0), "exp10": (-37.0, 37.0, 0.5), "log2": (0.0, 100.0, 2.0),
+                "log10": (0.0, 100.0, 1.0)}
+
+
+@pytest.mark.parametrize("fn", sorted(EXPLOG_COVER))
+def test_explog_cover_f32(oracle, fn):
+    lo, hi, bound = EXPLOG_COVER[fn]
+    x = np.random.default_rng(3).uniform(lo, hi, 200000).astype(np.float32)
+    ref = {"exp2": np.exp2, "exp10": lambda v: np.power(10.0, v), "log2": np.log2, "log10": np.log10}[fn](
+        x.astype(np.float64)).astype(np.float32)
+    m, w = oracle.max_ulp(oracle.map_(fn, x), ref)
+    assert m <= bound, (fn, m, x[w])
+
+
+@pytest.mark.parametrize("fn", sorted(EXPLOG_COVER))
+def test_explog_cover_f64(oracle, fn):
+    mpmath = pytest.importorskip("mpmath")
+    mpmath.mp.dps = 40
+    lo, hi, bound = EXPLOG_COVER[fn]
+    x = np.random.default_rng(4).uniform(lo, hi, 3000)
+    mf = {"exp2": lambda v: mpmath.power(2, v), "exp10": lambda v: mpmath.power(10, v),
+          "log2": lambda v: mpmath.log(v, 2), "log10": lambda v: mpmath.log10(v)}[fn]
+    ref = np.array([float(mf(mpmath.mpf(float(v)))) for v in x])
+    m, w = oracle.max_ulp(oracle.map_(fn, x), ref)
+    assert m <= bound, (fn, m, x[w])
