@@ -35,6 +35,7 @@
 #include <vector>
 #include "nt2cuda/expr.cuh"
 #include "nt2cuda/fold_launch.cuh"
+#include "nt2cuda/scan_launch.cuh"
 #include "nt2cuda/launch.cuh"
 
 namespace nt2cuda {
@@ -453,5 +454,145 @@ template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto sum(c
   if (settings().synchronous) check(cudaStreamSynchronize(s), "sum");
   return out;
 }
+
+// ------------------------------------------- the other reductions and scans
+// NT2's reductions along a dimension (1: one value per column, 2: one per row)
+// or over every element (the global* forms), on the fold kernels with the
+// operation policies of nt2cuda/fold.cuh
+// (nt2/core/functions/expr/{asum1,asum2,norm2,mean,var,stdev}.hpp,
+//  boost/simd/reduction/functions/{maximum,minimum,prod,all,any,none}.hpp),
+// and the cumulative functions on the scan kernels of nt2cuda/scan.cuh
+// (boost/simd/swar/functions/{cumsum,cumprod,cummax,cummin}.hpp).
+namespace detail_table {
+template <class X> using value_t = typename decltype(as_xpr(std::declval<X>()))::value_type;
+template <class V, int FIN = fold::FIN_NONE>
+using sum_op = std::conditional_t<std::is_same<V, float>::value, fold::op_sum<true, FIN>, fold::op_sum<false, FIN>>;
+
+template <class Op, class X> inline auto reduce_dim(const X& x, int dim, const char* what)
+{
+  auto e = as_xpr(x);
+  using V = typename decltype(e)::value_type;
+  using O = fold::out_of<Op, V>;
+  const size_t rows = e.size.d[0], cols = e.size.d[1];
+  cudaStream_t s = settings().stream;
+  table<O> out(dim == 1 ? of_size(1, cols) : of_size(rows, 1));
+  cudaError_t err = dim == 1 ? fold::inner_fold<Op, V>(e.e, rows, cols, out.device(), s)
+                             : fold::outer_fold<Op, V>(e.e, rows, cols, out.device(), s);
+  check(err, what);
+  out.mark_device_written();
+  if (settings().synchronous) check(cudaStreamSynchronize(s), what);
+  return out;
+}
+
+template <class Op, class X> inline auto reduce_all(const X& x, const char* what)
+{
+  auto e = as_xpr(x);
+  using V = typename decltype(e)::value_type;
+  using O = fold::out_of<Op, V>;
+  O* d = nullptr;
+  check(cudaMalloc(&d, sizeof(O)), what);
+  cudaStream_t s = settings().stream;
+  cudaError_t err = fold::inner_fold<Op, V>(e.e, e.size.numel(), 1, d, s);
+  O r{};
+  if (err == cudaSuccess) err = cudaMemcpyAsync(&r, d, sizeof(O), cudaMemcpyDeviceToHost, s);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+  cudaFree(d);
+  check(err, what);
+  return r;
+}
+
+template <class Op, class X> inline auto scan_dim(const X& x, int dim, const char* what)
+{
+  using V = value_t<X>;
+  table<V> in;
+  const V* src;
+  of_size_ sz;
+  if constexpr (is_table<std::decay_t<X>>::value) {
+    src = x.device();
+    sz = x.extent();
+  } else {                    // an expression is evaluated into a table first, as NT2's scan reads it
+    in = x;
+    src = in.device();
+    sz = in.extent();
+  }
+  table<V> out(sz);
+  cudaStream_t s = settings().stream;
+  check(scan::scan_dim<Op, V>(src, out.device(), sz.d[0], sz.numel() / (sz.d[0] ? sz.d[0] : 1), dim, s), what);
+  out.mark_device_written();
+  if (settings().synchronous) check(cudaStreamSynchronize(s), what);
+  return out;
+}
+}  // namespace detail_table
+
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto asum1(const X& x, int dim = 1)
+{ return detail_table::reduce_dim<detail_table::sum_op<detail_table::value_t<X>>>(abs(x), dim, "asum1"); }
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto globalasum1(const X& x)
+{ return detail_table::reduce_all<detail_table::sum_op<detail_table::value_t<X>>>(abs(x), "globalasum1"); }
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto asum2(const X& x, int dim = 1)
+{ return detail_table::reduce_dim<detail_table::sum_op<detail_table::value_t<X>>>(sqr(x), dim, "asum2"); }
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto globalasum2(const X& x)
+{ return detail_table::reduce_all<detail_table::sum_op<detail_table::value_t<X>>>(sqr(x), "globalasum2"); }
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto norm2(const X& x, int dim = 1)
+{ return detail_table::reduce_dim<detail_table::sum_op<detail_table::value_t<X>, fold::FIN_SQRT>>(sqr(x), dim, "norm2"); }
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto globalnorm2(const X& x)
+{ return detail_table::reduce_all<detail_table::sum_op<detail_table::value_t<X>, fold::FIN_SQRT>>(sqr(x), "globalnorm2"); }
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto mean(const X& x, int dim = 1)
+{ return detail_table::reduce_dim<detail_table::sum_op<detail_table::value_t<X>, fold::FIN_MEAN>>(x, dim, "mean"); }
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto globalmean(const X& x)
+{ return detail_table::reduce_all<detail_table::sum_op<detail_table::value_t<X>, fold::FIN_MEAN>>(x, "globalmean"); }
+// var(A, w, dim) / stdev(A, w, dim): w = 0 normalises by n - 1, w = 1 by n
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto var(const X& x, int w = 0, int dim = 1)
+{
+  return w ? detail_table::reduce_dim<fold::op_moments<true, false>>(x, dim, "var")
+           : detail_table::reduce_dim<fold::op_moments<false, false>>(x, dim, "var");
+}
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto stdev(const X& x, int w = 0, int dim = 1)
+{
+  return w ? detail_table::reduce_dim<fold::op_moments<true, true>>(x, dim, "stdev")
+           : detail_table::reduce_dim<fold::op_moments<false, true>>(x, dim, "stdev");
+}
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto globalvar(const X& x, int w = 0)
+{
+  return w ? detail_table::reduce_all<fold::op_moments<true, false>>(x, "globalvar")
+           : detail_table::reduce_all<fold::op_moments<false, false>>(x, "globalvar");
+}
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto globalstdev(const X& x, int w = 0)
+{
+  return w ? detail_table::reduce_all<fold::op_moments<true, true>>(x, "globalstdev")
+           : detail_table::reduce_all<fold::op_moments<false, true>>(x, "globalstdev");
+}
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto maximum(const X& x, int dim = 1)
+{ return detail_table::reduce_dim<fold::op_val<0>>(x, dim, "maximum"); }
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto globalmax(const X& x)
+{ return detail_table::reduce_all<fold::op_val<0>>(x, "globalmax"); }
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto minimum(const X& x, int dim = 1)
+{ return detail_table::reduce_dim<fold::op_val<1>>(x, dim, "minimum"); }
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto globalmin(const X& x)
+{ return detail_table::reduce_all<fold::op_val<1>>(x, "globalmin"); }
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto prod(const X& x, int dim = 1)
+{ return detail_table::reduce_dim<fold::op_val<2>>(x, dim, "prod"); }
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto globalprod(const X& x)
+{ return detail_table::reduce_all<fold::op_val<2>>(x, "globalprod"); }
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto all(const X& x, int dim = 1)
+{ return detail_table::reduce_dim<fold::op_logic<false>>(x, dim, "all"); }
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline bool globalall(const X& x)
+{ return detail_table::reduce_all<fold::op_logic<false>>(x, "globalall") != 0; }
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto any(const X& x, int dim = 1)
+{ return detail_table::reduce_dim<fold::op_logic<true>>(x, dim, "any"); }
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline bool globalany(const X& x)
+{ return detail_table::reduce_all<fold::op_logic<true>>(x, "globalany") != 0; }
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto none(const X& x, int dim = 1)
+{ return detail_table::reduce_dim<fold::op_logic<true, true>>(x, dim, "none"); }
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline bool globalnone(const X& x)
+{ return detail_table::reduce_all<fold::op_logic<true, true>>(x, "globalnone") != 0; }
+
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto cumsum(const X& x, int dim = 1)
+{ return detail_table::scan_dim<detail_table::sum_op<detail_table::value_t<X>>>(x, dim, "cumsum"); }
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto cumprod(const X& x, int dim = 1)
+{ return detail_table::scan_dim<fold::op_val<2>>(x, dim, "cumprod"); }
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto cummax(const X& x, int dim = 1)
+{ return detail_table::scan_dim<fold::op_val<3>>(x, dim, "cummax"); }
+template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto cummin(const X& x, int dim = 1)
+{ return detail_table::scan_dim<fold::op_val<4>>(x, dim, "cummin"); }
 
 }  // namespace nt2cuda

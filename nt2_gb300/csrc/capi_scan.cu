@@ -4,103 +4,13 @@
 #include <stdint.h>
 #include "internal.cuh"
 #include "nt2cuda/launch.cuh"
-#include "nt2cuda/scan.cuh"
-#include "nt2cuda/scratch.cuh"
+#include "nt2cuda/scan_launch.cuh"
 
 using namespace nt2cuda;
 using namespace nt2cuda::detail_capi;
 using nt2cuda::fold::state_of;
 
 namespace {
-
-inline size_t align256(size_t b) { return (b + 255) / 256 * 256; }
-
-template <class Op, class T>
-cudaError_t inner_scan(const T* x, T* y, size_t rows, size_t cols, cudaStream_t s)
-{
-  using S = state_of<Op, T>;
-  if (!rows || !cols) return cudaSuccess;
-  if (rows <= 64) {
-    void* args[] = {(void*)&x, (void*)&y, (void*)&rows, (void*)&cols};
-    return launch_persistent(scan::k_scan_inner_short<Op, T>, cols, 256, 2, s, args);
-  }
-  // columns of one 32 KB tile: a single pass without look-back; longer ones:
-  // 64 KB tiles chained by the look-back, aggregate then rescan from L2
-  const bool one_pass = rows <= (size_t)scan::tile<T>();
-  const size_t TILE = one_pass ? (size_t)scan::tile<T>() : scan::scan_tiles<Op, T>::TILE;
-  scan::inner_shape sh;
-  sh.rows = rows;
-  sh.cols = cols;
-  sh.tiles_per_col = (rows + TILE - 1) / TILE;
-  sh.tiles = sh.tiles_per_col * cols;
-  // scratch: ticket, error word, flags | aggregates | inclusive prefixes
-  const size_t head = 256, fbytes = align256(sh.tiles * sizeof(unsigned));
-  const size_t sbytes = align256(sh.tiles * scan::carry_bytes<Op, T>());
-  void* scratch = nullptr;
-  cudaError_t e = nt2cuda::stream_scratch(s, head + fbytes + 2 * sbytes, &scratch, 1);
-  if (e != cudaSuccess) return e;
-  char* b = (char*)scratch;
-  unsigned long long* ticket = (unsigned long long*)b;
-  unsigned* err = (unsigned*)(b + 8);
-  unsigned* flags = (unsigned*)(b + head);
-  void* agg = b + head + fbytes;
-  void* incl = b + head + fbytes + sbytes;
-  if ((e = cudaMemsetAsync(b, 0, head + fbytes, s)) != cudaSuccess) return e;
-  int vec = ((((uintptr_t)x | (uintptr_t)y) & 15u) == 0 && (rows * sizeof(T)) % 16 == 0) ? 1 : 0;
-  auto k = one_pass ? scan::k_scan_inner_1p<Op, T, false> : scan::k_scan_inner<Op, T>;
-  size_t grid = (size_t)sm_count() * (size_t)resident_blocks(k, 256);
-  if (grid > sh.tiles) grid = sh.tiles;
-  k<<<(unsigned)grid, 256, 0, s>>>(x, y, sh, vec, ticket, flags, agg, incl, err);
-  return cudaGetLastError();
-}
-
-template <class Op, class T, int V>
-cudaError_t outer_scan_v(const T* x, T* y, size_t rows, size_t cols, cudaStream_t s)
-{
-  using S = state_of<Op, T>;
-  constexpr size_t ROWS = 256 * (size_t)V;
-  scan::outer_shape sh;
-  sh.rows = rows;
-  sh.cols = cols;
-  sh.strips = (rows + ROWS - 1) / ROWS;
-  // about two blocks per SM in all; a chunk is a whole number of 8-column groups
-  const size_t want = (2 * (size_t)sm_count() + sh.strips - 1) / sh.strips;
-  size_t cchunk = (cols + want - 1) / want;
-  cchunk = (cchunk + 7) / 8 * 8;
-  sh.cchunk = cchunk < 8 ? 8 : cchunk;
-  sh.chunks = (cols + sh.cchunk - 1) / sh.cchunk;
-  const size_t units = sh.strips * sh.chunks;
-  S* totals = nullptr;
-  cudaError_t e;
-  if (sh.chunks > 1) {
-    void* scratch = nullptr;
-    if ((e = nt2cuda::stream_scratch(s, units * ROWS * sizeof(S), &scratch, 1)) != cudaSuccess) return e;
-    totals = (S*)scratch;
-    void* a1[] = {(void*)&x, (void*)&y, (void*)&sh, (void*)&totals};
-    if ((e = launch_persistent(scan::k_scan_outer<Op, T, V, false>, units * 256, 256, 2, s, a1)) != cudaSuccess)
-      return e;
-    void* a2[] = {(void*)&sh, (void*)&totals};
-    if ((e = launch_persistent(scan::k_scan_outer_prefix<Op, T, V>, sh.strips * ROWS, 256, 2, s, a2)) != cudaSuccess)
-      return e;
-  }
-  void* a3[] = {(void*)&x, (void*)&y, (void*)&sh, (void*)&totals};
-  return launch_persistent(scan::k_scan_outer<Op, T, V, true>, units * 256, 256, 2, s, a3);
-}
-
-template <class Op, class T>
-cudaError_t outer_scan(const T* x, T* y, size_t rows, size_t cols, cudaStream_t s)
-{
-  if (!rows || !cols) return cudaSuccess;
-  constexpr int V = 16 / (int)sizeof(T);
-  if ((((uintptr_t)x | (uintptr_t)y) & 15u) == 0 && rows % V == 0) return outer_scan_v<Op, T, V>(x, y, rows, cols, s);
-  return outer_scan_v<Op, T, 1>(x, y, rows, cols, s);
-}
-
-template <class Op, class T>
-cudaError_t scan_dim(const T* x, T* y, size_t rows, size_t cols, int dim, cudaStream_t s)
-{
-  return dim == 1 ? inner_scan<Op, T>(x, y, rows, cols, s) : outer_scan<Op, T>(x, y, rows, cols, s);
-}
 
 template <class T>
 nt2cuda_status scan_impl(int op, const T* A, size_t rows, size_t cols, int dim, T* out, int flags, cudaStream_t s)
@@ -114,11 +24,11 @@ nt2cuda_status scan_impl(int op, const T* A, size_t rows, size_t cols, int dim, 
   cudaError_t e;
   switch (op) {
     case NT2CUDA_SCAN_SUM:
-      e = comp ? scan_dim<op_sum<true>, T>(A, out, rows, cols, dim, s) : scan_dim<op_sum<false>, T>(A, out, rows, cols, dim, s);
+      e = comp ? scan::scan_dim<op_sum<true>, T>(A, out, rows, cols, dim, s) : scan::scan_dim<op_sum<false>, T>(A, out, rows, cols, dim, s);
       break;
-    case NT2CUDA_SCAN_PROD: e = scan_dim<op_val<2>, T>(A, out, rows, cols, dim, s); break;
-    case NT2CUDA_SCAN_MAX: e = scan_dim<op_val<3>, T>(A, out, rows, cols, dim, s); break;
-    case NT2CUDA_SCAN_MIN: e = scan_dim<op_val<4>, T>(A, out, rows, cols, dim, s); break;
+    case NT2CUDA_SCAN_PROD: e = scan::scan_dim<op_val<2>, T>(A, out, rows, cols, dim, s); break;
+    case NT2CUDA_SCAN_MAX: e = scan::scan_dim<op_val<3>, T>(A, out, rows, cols, dim, s); break;
+    case NT2CUDA_SCAN_MIN: e = scan::scan_dim<op_val<4>, T>(A, out, rows, cols, dim, s); break;
     default: return NT2CUDA_ERR_ARG;
   }
   return launch_status(e);

@@ -58,6 +58,11 @@ template <class T> inline const T* first_term(const node<tag::multiplies_, term<
 template <class T> inline const T* second_term(const term<T>&) { return nullptr; }
 template <class T> inline const T* second_term(const node<tag::multiplies_, term<T>, term<T>>& n) { return n.b.p; }
 
+// Loads in flight per lane in the register-pipelined kernels: 8, or 4 for the
+// three-value var/stdev state (8 would cost residency for no more bandwidth).
+template <class Op> struct fold_unroll { static constexpr int value = 8; };
+template <bool W1, bool SD> struct fold_unroll<op_moments<W1, SD>> { static constexpr int value = 4; };
+
 template <class Op, class T> cudaError_t fold_empty(out_of<Op, T>* out, size_t count, cudaStream_t s)
 {
   void* args[] = {&out, &count};
@@ -111,7 +116,7 @@ cudaError_t inner_fold(const E& e, size_t rows, size_t cols, out_of<Op, T>* out,
   out_of<Op, T>* o = out;
   void* args[] = {&ec, &sh, &o, &partials, &counters};
   // launch_persistent counts threads; a unit is one warp
-  if (vec) return (launch_persistent(k_inner<Op, VV, 8, T, E>, units * 32, 256, 4, s, args));
+  if (vec) return (launch_persistent(k_inner<Op, VV, fold_unroll<Op>::value, T, E>, units * 32, 256, 4, s, args));
   return (launch_persistent(k_inner<Op, 1, 4, T, E>, units * 32, 256, 4, s, args));
 }
 
@@ -162,7 +167,7 @@ cudaError_t outer_fold(const E& e, size_t rows, size_t cols, out_of<Op, T>* out,
   E ec = e;
   out_of<Op, T>* o = out;
   void* args[] = {&ec, &sh, &o, &partials, &counters};
-  if (vec) return (launch_persistent(k_outer<Op, VV, 8, T, E>, units * 256, 256, 4, s, args));
+  if (vec) return (launch_persistent(k_outer<Op, VV, fold_unroll<Op>::value, T, E>, units * 256, 256, 4, s, args));
   return (launch_persistent(k_outer<Op, 1, 4, T, E>, units * 256, 256, 4, s, args));
 }
 

@@ -10,6 +10,8 @@
 //   rgb2grey   demo/rgb2grey/nt2/rgb2grey_nt2.cpp:42-45 (float, and uint8 planes through nt2::cast)
 //   rgb2yuv    demo/rgb2yuv/nt2/rgb2yuv_nt2.cpp:28-33
 //   sigmadelta demo/sigmadelta/nt2/sigmadelta_nt2.cpp:37-58, 100-106
+//   stats      NT2 reductions and cumulative functions of a table (mean, var,
+//              maximum, asum1, cumsum along both dimensions, global* forms)
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -128,6 +130,29 @@ int main(int argc, char** argv)
     write_table(argv[6], y);
     write_table(argv[7], u);
     write_table(argv[8], v);
+  } else if (cmd == "stats") {                            // n = rows; argv[3] = cols; in: A ; out: 7 tables
+    typedef float T;
+    const std::size_t cols = std::strtoull(argv[3], nullptr, 10);
+    nt2::table<T> A(nt2::of_size(n, cols));
+    load(A, read_file<T>(argv[4], n * cols));
+    nt2::table<T> m1 = nt2::mean(A, 1);
+    nt2::table<T> v2 = nt2::var(A, 0, 2);
+    nt2::table<T> x1 = nt2::maximum(A, 1);
+    nt2::table<T> a2 = nt2::asum1(A, 2);
+    nt2::table<T> c1 = nt2::cumsum(A, 1);
+    nt2::table<T> c2 = nt2::cumsum(A, 2);
+    nt2::table<T> g(nt2::of_size(4));
+    g(1) = nt2::globalsum(A);
+    g(2) = nt2::globalnorm2(A);
+    g(3) = nt2::globalmax(A);
+    g(4) = nt2::globalstdev(A);
+    write_table(argv[5], m1);
+    write_table(argv[6], v2);
+    write_table(argv[7], x1);
+    write_table(argv[8], a2);
+    write_table(argv[9], c1);
+    write_table(argv[10], c2);
+    write_table(argv[11], g);
   } else if (cmd == "sigmadelta") {                       // n = pixels; argv[3] = frames; in: frames ; out: bkg var label
     typedef unsigned char T;
     const int nb_frames = std::atoi(argv[3]);

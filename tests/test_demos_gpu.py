@@ -108,3 +108,22 @@ def test_sigmadelta_demo(demos, oracle, tmp_path):
     assert np.array_equal(np.fromfile(ob, np.uint8), rb)
     assert np.array_equal(np.fromfile(ov, np.uint8), rv)
     assert np.array_equal(np.fromfile(ol, np.uint8), rl[(nf - 2) * npix:])    # the demo keeps the last label
+
+
+def test_stats_demo(demos, gpu, tmp_path):
+    """NT2-spelled reductions and cumulative functions give the C-ABI results bit for bit."""
+    import torch
+    rows, cols = 1000, 37
+    rng = np.random.default_rng(9)
+    A = (rng.standard_normal(rows * cols) * 2 + 1).astype(np.float32)
+    _, outs = run(demos, tmp_path, "stats", rows, [A], 7, extra=(str(cols),))
+    got = [np.fromfile(o, np.float32) for o in outs]
+    Ad = torch.from_numpy(A).cuda()
+    h = lambda t: (torch.cuda.synchronize(), t.cpu().numpy())[1]
+    expect = [h(gpu.reduce("mean", Ad, rows, cols, 1)), h(gpu.reduce("var", Ad, rows, cols, 2)),
+              h(gpu.reduce("max", Ad, rows, cols, 1)), h(gpu.reduce("asum1", Ad, rows, cols, 2)),
+              h(gpu.cumulative("cumsum", Ad, rows, cols, 1)), h(gpu.cumulative("cumsum", Ad, rows, cols, 2))]
+    for g, e in zip(got[:6], expect):
+        assert np.array_equal(g.view(np.uint32), e.view(np.uint32))
+    gl = [h(gpu.reduce(op, Ad, rows, cols, 0))[0] for op in ("sum", "norm2", "max", "stdev")]
+    assert np.array_equal(got[6].view(np.uint32), np.array(gl, np.float32).view(np.uint32))
