@@ -85,9 +85,9 @@ nt2cuda_status nt2cuda_stream_sync(nt2cuda_stream stream);
  * generic/log.hpp:20-31, modules/core/euler/include/nt2/euler/functions/simd/common/erfc.hpp:46-123,
  * modules/core/statistics/include/nt2/statistics/functions/generic/normcdf.hpp:28-34,
  * generic/fastnormcdf.hpp:33-55, boost/simd/arithmetic/functions/scalar/sqrt.hpp:21-62)
- * and exp2/exp10/log2/log10
+ * and exp2/exp10/log2/log10/expm1/log1p
  * (modules/core/exponential/include/nt2/exponential/functions/scalar/impl/expo/{f,d}_expo_reduction.hpp,
- * simd/common/impl/logs/{f,d}_log.hpp). */
+ * simd/common/impl/logs/{f,d}_log.hpp, details/expm1_kernel.hpp, simd/common/log1p.hpp). */
 enum {
   NT2CUDA_OP_EXP = 0,
   NT2CUDA_OP_LOG = 1,
@@ -98,7 +98,9 @@ enum {
   NT2CUDA_OP_EXP2 = 6,
   NT2CUDA_OP_EXP10 = 7,
   NT2CUDA_OP_LOG2 = 8,
-  NT2CUDA_OP_LOG10 = 9
+  NT2CUDA_OP_LOG10 = 9,
+  NT2CUDA_OP_EXPM1 = 10,
+  NT2CUDA_OP_LOG1P = 11
 };
 
 /* y = op(x).  Replaces `y = nt2::op(x)` evaluated by transform_

@@ -290,6 +290,8 @@ NT2CUDA_FN1(exp2, exp2_)
 NT2CUDA_FN1(exp10, exp10_)
 NT2CUDA_FN1(log2, log2_)
 NT2CUDA_FN1(log10, log10_)
+NT2CUDA_FN1(expm1, expm1_)
+NT2CUDA_FN1(log1p, log1p_)
 NT2CUDA_FN1(sqrt, sqrt_)
 NT2CUDA_FN1(sqr, sqr_)
 NT2CUDA_FN1(erfc, erfc_)

@@ -15,7 +15,7 @@ import torch
 from ._lib import SdStream, check, lib
 
 OPS = {"exp": 0, "log": 1, "erfc": 2, "normcdf": 3, "fastnormcdf": 4, "sqrt": 5, "exp2": 6, "exp10": 7, "log2": 8,
-       "log10": 9}
+       "log10": 9, "expm1": 10, "log1p": 11}
 CDF = {"normcdf": 0, "fastnormcdf": 1}
 
 
@@ -38,7 +38,8 @@ def init(device: int = 0) -> None:
 
 
 def map_(op: str, x: torch.Tensor, out: torch.Tensor | None = None, fused: bool = False) -> torch.Tensor:
-    """out = nt2::op(x) for op in exp, log, erfc, normcdf, fastnormcdf, sqrt, exp2, exp10, log2, log10."""
+    """out = nt2::op(x) for op in exp, log, erfc, normcdf, fastnormcdf, sqrt, exp2, exp10, log2, log10, expm1,
+    log1p."""
     out = torch.empty_like(x) if out is None else out
     L = lib()
     if x.dtype == torch.float32:

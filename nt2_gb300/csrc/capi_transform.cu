@@ -39,6 +39,8 @@ template <bool F, class T> nt2cuda_status map_impl(int op, const T* x, T* y, siz
     case NT2CUDA_OP_EXP10: return run<F>(make_prog(asg(y, nd<tag::exp10_>(X))), n, s, "map");
     case NT2CUDA_OP_LOG2: return run<F>(make_prog(asg(y, nd<tag::log2_>(X))), n, s, "map");
     case NT2CUDA_OP_LOG10: return run<F>(make_prog(asg(y, nd<tag::log10_>(X))), n, s, "map");
+    case NT2CUDA_OP_EXPM1: return run<F>(make_prog(asg(y, nd<tag::expm1_>(X))), n, s, "map");
+    case NT2CUDA_OP_LOG1P: return run<F>(make_prog(asg(y, nd<tag::log1p_>(X))), n, s, "map");
     case NT2CUDA_OP_FASTNORMCDF:
       if constexpr (sizeof(T) == 4) return run<F>(make_prog(asg(y, nd<tag::fastnormcdf_>(X))), n, s, "map");
       else return NT2CUDA_ERR_ARG;

@@ -34,7 +34,7 @@ namespace tag {
 struct plus_ {}; struct minus_ {}; struct multiplies_ {}; struct divides_ {};
 struct unary_minus_ {}; struct fma_ {}; struct fnms_ {}; struct sqr_ {}; struct sqrt_ {};
 struct rec_ {}; struct abs_ {}; struct exp_ {}; struct log_ {}; struct erfc_ {};
-struct exp2_ {}; struct exp10_ {}; struct log2_ {}; struct log10_ {};
+struct exp2_ {}; struct exp10_ {}; struct log2_ {}; struct log10_ {}; struct expm1_ {}; struct log1p_ {};
 struct normcdf_ {}; struct fastnormcdf_ {}; struct max_ {}; struct min_ {};
 struct adds_ {}; struct subs_ {}; struct selinc_ {}; struct seldec_ {}; struct if_else_ {};
 struct if_zero_else_one_ {}; struct is_less_ {}; struct is_greater_ {};
@@ -134,6 +134,8 @@ NT2CUDA_UN(exp2_, math::exp2<F>(a))
 NT2CUDA_UN(exp10_, math::exp10<F>(a))
 NT2CUDA_UN(log2_, math::log2<F>(a))
 NT2CUDA_UN(log10_, math::log10<F>(a))
+NT2CUDA_UN(expm1_, math::expm1<F>(a))
+NT2CUDA_UN(log1p_, math::log1p<F>(a))
 NT2CUDA_UN(erfc_, math::erfc<F>(a))
 NT2CUDA_UN(normcdf_, math::normcdf<F>(a))
 NT2CUDA_UN(fastnormcdf_, math::fastnormcdf<F>(a))

@@ -219,6 +219,40 @@ __device__ __forceinline__ float log10(float a0)
   return log_finalize(a0, madd<F>(p.fe, fbits(cf2::log10_2lo), add(z, p.t)));
 }
 
+// ---------------------------------------------------------- expm1, log1p
+// expm1: modules/core/exponential/include/nt2/exponential/functions/details/expm1_kernel.hpp:24-80,
+// selections simd/common/expm1.hpp:35-41, fast_ldexp by exponent bits;
+// log1p: .../functions/simd/common/log1p.hpp:29-38.
+template <bool F = false>
+__device__ __forceinline__ float expm1(float a0)
+{
+  constexpr uint32_t P[3] = {0x3acf6db4u, 0xbd08887fu, 0x3f800000u};
+  float k = rintf(mul(fbits(cf::invlog_2), a0));
+  float x = nmsub<F>(k, fbits(cf::log_2hi), a0);
+  x = nmsub<F>(k, fbits(cf::log_2lo), x);
+  float hx = mul(x, 0.5f);
+  float hxs = mul(x, hx);
+  float r1 = horner<F>(hxs, P);
+  float t = nmsub<F>(r1, hx, 3.0f);                          // fnms(r1, hx, Three)
+  float e = mul(hxs, div(sub(r1, t), nmsub<F>(x, t, 6.0f)));
+  e = F ? __fmaf_rn(x, e, -hxs) : sub(mul(x, e), hxs);      // fms(x, e, hxs)
+  int ik = (int)k;
+  float two2mk = __uint_as_float((unsigned)(127 - ik) << 23);
+  float y = sub(sub(1.0f, two2mk), sub(e, x));
+  float r = mul(y, __uint_as_float((unsigned)(ik + 127) << 23));
+  r = (a0 > fbits(cf::maxlog)) ? __int_as_float(0x7f800000) : r;
+  return (a0 < __uint_as_float(0xc17f1402u)) ? -1.0f : r;    // Logeps
+}
+
+template <bool F = false>
+__device__ __forceinline__ float log1p(float a0)
+{
+  float u = add(1.0f, a0);
+  float r = log<F>(u);
+  r = (u != 0.0f) ? add(r, div(sub(a0, sub(u, 1.0f)), u)) : r;
+  return (u == __int_as_float(0x7f800000)) ? u : r;
+}
+
 // --------------------------------------------------------------- float erfc
 // modules/core/euler/include/nt2/euler/functions/simd/common/erfc.hpp:92-121
 // kernels: modules/core/euler/include/nt2/euler/functions/details/erf_kernel.hpp:48-85
@@ -453,6 +487,41 @@ __device__ __forceinline__ double log10(double a0)
   double dk;
   const double m = log_mantissa<F>(a0, dk);
   return log_finalize(a0, madd<F>(m, dbits(cd2::invlog_10), mul(dk, dbits(cd2::log_2olog_10))));
+}
+
+// --------------------------------------------------- double expm1, log1p
+template <bool F = false>
+__device__ __forceinline__ double expm1(double a0)
+{
+  constexpr uint64_t P[6] = {0xBE8AFDB76E09C32Dull, 0x3ED0CFCA86E65239ull, 0xBF14CE199EAADBB7ull,
+                             0x3F5A01A019FE5585ull, 0xBFA11111111110F4ull, 0x3ff0000000000000ull};
+  double k = rint(mul(dbits(cd::invlog_2), a0));
+  double hi = nmsub<F>(k, dbits(cd::log_2hi), a0);
+  double lo = mul(k, dbits(cd::log_2lo));
+  double x = sub(hi, lo);
+  double hxs = mul(mul(x, x), 0.5);
+  double r1 = horner<F>(hxs, P);
+  double t = nmsub<F>(mul(r1, 0.5), x, 3.0);                 // Three - r1*Half*x
+  double e = mul(hxs, div(sub(r1, t), nmsub<F>(x, t, 6.0)));
+  double c = sub(sub(hi, x), lo);
+  e = sub(sub(mul(x, sub(e, c)), c), hxs);
+  long long ik = (long long)k;
+  double two2mk = __longlong_as_double((long long)((unsigned long long)(1023 - ik) << 52));
+  double ct1 = sub(sub(1.0, two2mk), sub(e, x));
+  double ct2 = add(sub(x, add(e, two2mk)), 1.0);
+  double y = (k < 20.0) ? ct1 : ct2;
+  double r = mul(y, __longlong_as_double((long long)((unsigned long long)(ik + 1023) << 52)));
+  r = (a0 > dbits(cd::maxlog)) ? __longlong_as_double(0x7ff0000000000000ll) : r;
+  return (a0 < __longlong_as_double(0xc04205966f2b4f19ll)) ? -1.0 : r;   // Logeps
+}
+
+template <bool F = false>
+__device__ __forceinline__ double log1p(double a0)
+{
+  double u = add(1.0, a0);
+  double r = log<F>(u);
+  r = (u != 0.0) ? add(r, div(sub(a0, sub(u, 1.0)), u)) : r;
+  return (u == __longlong_as_double(0x7ff0000000000000ll)) ? u : r;
 }
 
 // -------------------------------------------------------------- double erfc

@@ -488,6 +488,75 @@ EXPORT double nt2o_log10_d(double a0)
   return log_finalize_d(a0, y);
 }
 
+/* ------------------------------------------------------- expm1, log1p -- */
+/* expm1: exponential/functions/details/expm1_kernel.hpp:24-80 with the
+ * selections of simd/common/expm1.hpp:35-41 (below Logeps: -1, above Maxlog:
+ * Inf); fast_ldexp multiplies by 2^ik built in the exponent bits
+ * (boost/simd/ieee/functions/simd/common/fast_ldexp.hpp).
+ * log1p: simd/common/log1p.hpp:29-38, u = 1+a0, log(u) corrected by (a0-(u-1))/u. */
+#define LOGEPS_F fb(0xc17f1402u)
+#define LOGEPS_D db(0xc04205966f2b4f19ull)
+static const uint32_t EXPM1_F_P[3] = {0x3acf6db4u, 0xbd08887fu, 0x3f800000u};
+static const uint64_t EXPM1_D_P[6] = {0xBE8AFDB76E09C32Dull, 0x3ED0CFCA86E65239ull, 0xBF14CE199EAADBB7ull,
+                                      0x3F5A01A019FE5585ull, 0xBFA11111111110F4ull, 0x3ff0000000000000ull};
+
+EXPORT float nt2o_expm1_f(float a0)
+{
+  if (a0 < LOGEPS_F) return -1.0f;
+  if (a0 > MAXLOG_F) return INFINITY;
+  float k = r2e_f(INVLOG_2_F * a0);
+  float x = a0 - k * LOG_2HI_F;
+  x = x - k * LOG_2LO_F;
+  float hx = x * 0.5f;
+  float hxs = x * hx;
+  float r1 = horner_f(hxs, EXPM1_F_P, 3);
+  float t = 3.0f - r1 * hx;                                 /* fnms(r1, hx, Three) */
+  float e = hxs * ((r1 - t) / (6.0f - x * t));
+  e = x * e - hxs;                                          /* fms(x, e, hxs) */
+  uint32_t ik = (uint32_t)(int32_t)k;                       /* k is integral (NaN only when a0 is) */
+  float two2mk = fb((127u - ik) << 23);
+  float y = (1.0f - two2mk) - (e - x);
+  return y * fb((ik + 127u) << 23);
+}
+
+EXPORT double nt2o_expm1_d(double a0)
+{
+  if (a0 < LOGEPS_D) return -1.0;
+  if (a0 > MAXLOG_D) return INFINITY;
+  double k = r2e_d(INVLOG_2_D * a0);
+  double hi = a0 - k * LOG_2HI_D;
+  double lo = k * LOG_2LO_D;
+  double x = hi - lo;
+  double hxs = (x * x) * 0.5;
+  double r1 = horner_d(hxs, EXPM1_D_P, 6);
+  double t = 3.0 - (r1 * 0.5) * x;
+  double e = hxs * ((r1 - t) / (6.0 - x * t));
+  double c = (hi - x) - lo;
+  e = (x * (e - c) - c) - hxs;
+  uint64_t ik = (uint64_t)(int64_t)k;
+  double two2mk = db((1023ull - ik) << 52);
+  double ct1 = (1.0 - two2mk) - (e - x);
+  double ct2 = (x - (e + two2mk)) + 1.0;
+  double y = (k < 20.0) ? ct1 : ct2;
+  return y * db((ik + 1023ull) << 52);
+}
+
+EXPORT float nt2o_log1p_f(float a0)
+{
+  float u = 1.0f + a0;
+  float r = nt2o_log_f(u);
+  if (u != 0.0f) r = r + (a0 - (u - 1.0f)) / u;
+  return (u == INFINITY) ? u : r;
+}
+
+EXPORT double nt2o_log1p_d(double a0)
+{
+  double u = 1.0 + a0;
+  double r = nt2o_log_d(u);
+  if (u != 0.0) r = r + (a0 - (u - 1.0)) / u;
+  return (u == INFINITY) ? u : r;
+}
+
 /* ---------------------------------------------------------- double erfc -- */
 /* euler/functions/simd/common/erfc.hpp:46-89, kernels
  * euler/functions/details/erf_kernel.hpp:101-163 (rational 5/5, 7/7, 7/7) */
@@ -561,7 +630,8 @@ EXPORT double nt2o_erfc_d_scalar(double a0)
 
 /* ------------------------------------------------------------- maps ------ */
 enum { OP_EXP = 0, OP_LOG = 1, OP_ERFC = 2, OP_NORMCDF = 3, OP_FASTNORMCDF = 4, OP_SQRT = 5,
-       OP_ERFC_SCALAR = 6, OP_EXP2 = 7, OP_EXP10 = 8, OP_LOG2 = 9, OP_LOG10 = 10 };
+       OP_ERFC_SCALAR = 6, OP_EXP2 = 7, OP_EXP10 = 8, OP_LOG2 = 9, OP_LOG10 = 10, OP_EXPM1 = 11,
+       OP_LOG1P = 12 };
 
 EXPORT int nt2o_map_f(int op, const float* x, float* y, size_t n)
 {
@@ -579,6 +649,8 @@ EXPORT int nt2o_map_f(int op, const float* x, float* y, size_t n)
       case OP_EXP10: y[i] = nt2o_exp10_f(a); break;
       case OP_LOG2: y[i] = nt2o_log2_f(a); break;
       case OP_LOG10: y[i] = nt2o_log10_f(a); break;
+      case OP_EXPM1: y[i] = nt2o_expm1_f(a); break;
+      case OP_LOG1P: y[i] = nt2o_log1p_f(a); break;
       default: return 1;
     }
   }
@@ -600,6 +672,8 @@ EXPORT int nt2o_map_d(int op, const double* x, double* y, size_t n)
       case OP_EXP10: y[i] = nt2o_exp10_d(a); break;
       case OP_LOG2: y[i] = nt2o_log2_d(a); break;
       case OP_LOG10: y[i] = nt2o_log10_d(a); break;
+      case OP_EXPM1: y[i] = nt2o_expm1_d(a); break;
+      case OP_LOG1P: y[i] = nt2o_log1p_d(a); break;
       default: return 1;
     }
   }

@@ -23,7 +23,7 @@ SPECIALS = [0.0, -0.0, 1.0, -1.0, 0.5, 2.0, np.inf, -np.inf, np.nan, 88.5, -88.5
 def inputs(op, n, dtype, seed):
     rng = np.random.default_rng(seed)
     lo, hi = {"exp": (-100, 100), "log": (0, 100), "sqrt": (0, 100), "exp2": (-150, 150), "exp10": (-45, 45),
-              "log2": (0, 100), "log10": (0, 100)}.get(op, (-10, 10))
+              "log2": (0, 100), "log10": (0, 100), "expm1": (-100, 100), "log1p": (-1, 100)}.get(op, (-10, 10))
     x = rng.uniform(lo, hi, n).astype(dtype)
     sp = np.array(SPECIALS, dtype)
     x[: len(sp)] = sp
@@ -32,11 +32,13 @@ def inputs(op, n, dtype, seed):
 
 def main():
     out = {}
-    for i, op in enumerate(["exp", "log", "erfc", "normcdf", "fastnormcdf", "sqrt", "exp2", "exp10", "log2", "log10"]):
+    for i, op in enumerate(["exp", "log", "erfc", "normcdf", "fastnormcdf", "sqrt", "exp2", "exp10", "log2", "log10",
+                            "expm1", "log1p"]):
         x = inputs(op, 2048, np.float32, 100 + i)
         out[f"map_f32_{op}_x"] = x
         out[f"map_f32_{op}_y"] = oracle_lib.map_(op, x)
-    for i, op in enumerate(["exp", "log", "erfc", "normcdf", "sqrt", "exp2", "exp10", "log2", "log10"]):
+    for i, op in enumerate(["exp", "log", "erfc", "normcdf", "sqrt", "exp2", "exp10", "log2", "log10", "expm1",
+                            "log1p"]):
         x = inputs(op, 2048, np.float64, 200 + i)
         out[f"map_f64_{op}_x"] = x
         out[f"map_f64_{op}_y"] = oracle_lib.map_(op, x)

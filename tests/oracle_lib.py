@@ -36,6 +36,10 @@ SIGS = {
     "nt2o_fastnormcdf_f": (C.c_float, [C.c_float]),
     "nt2o_exp_d": (C.c_double, [C.c_double]),
     "nt2o_exp2_f": (C.c_float, [C.c_float]),
+    "nt2o_expm1_f": (C.c_float, [C.c_float]),
+    "nt2o_log1p_f": (C.c_float, [C.c_float]),
+    "nt2o_expm1_d": (C.c_double, [C.c_double]),
+    "nt2o_log1p_d": (C.c_double, [C.c_double]),
     "nt2o_exp10_f": (C.c_float, [C.c_float]),
     "nt2o_log2_f": (C.c_float, [C.c_float]),
     "nt2o_log10_f": (C.c_float, [C.c_float]),
@@ -74,7 +78,7 @@ SIGS = {
 }
 
 OP = {"exp": 0, "log": 1, "erfc": 2, "normcdf": 3, "fastnormcdf": 4, "sqrt": 5, "erfc_scalar": 6,
-      "exp2": 7, "exp10": 8, "log2": 9, "log10": 10}
+      "exp2": 7, "exp10": 8, "log2": 9, "log10": 10, "expm1": 11, "log1p": 12}
 
 
 def load(variant: str = "libnt2oracle.so"):

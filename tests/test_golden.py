@@ -20,8 +20,8 @@ def same(a, b):
     return bool(np.array_equal(a, b))
 
 
-OPS32 = ["exp", "log", "erfc", "normcdf", "fastnormcdf", "sqrt", "exp2", "exp10", "log2", "log10"]
-OPS64 = ["exp", "log", "erfc", "normcdf", "sqrt", "exp2", "exp10", "log2", "log10"]
+OPS32 = ["exp", "log", "erfc", "normcdf", "fastnormcdf", "sqrt", "exp2", "exp10", "log2", "log10", "expm1", "log1p"]
+OPS64 = ["exp", "log", "erfc", "normcdf", "sqrt", "exp2", "exp10", "log2", "log10", "expm1", "log1p"]
 
 
 @pytest.mark.parametrize("op", OPS32)

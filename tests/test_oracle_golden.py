@@ -278,3 +278,40 @@ def test_explog_cover_f64(oracle, fn):
     ref = np.array([float(mf(mpmath.mpf(float(v)))) for v in x])
     m, w = oracle.max_ulp(oracle.map_(fn, x), ref)
     assert m <= bound, (fn, m, x[w])
+
+
+# expm1, log1p: modules/core/exponential/unit/scalar/{expm1,log1p}.cpp (specials) and
+# cover/scalar/{expm1,log1p}.cpp ([-0.5, 0.5], 1 ulp)
+E1 = math.e
+
+
+@pytest.mark.parametrize("prec", ["f", "d"])
+def test_expm1_log1p_special_values(oracle, prec):
+    L = oracle.load()
+    u = ulp_f if prec == "f" else ulp_d
+    cast = f32 if prec == "f" else float
+    em1 = getattr(L, f"nt2o_expm1_{prec}")
+    l1p = getattr(L, f"nt2o_log1p_{prec}")
+    for x, r, tol in [(INF, INF, 1.0), (-INF, -1.0, 1.0), (NAN, NAN, 1.0), (-1.0, 1 / E1 - 1, 1.0),
+                      (1.0, E1 - 1, 1.0), (0.0, 0.0, 1.0)]:
+        assert u(L, em1(x), cast(r)) <= tol, ("expm1", prec, x)
+    eps = float(np.finfo(np.float32 if prec == "f" else np.float64).eps)
+    tiny = float(np.finfo(np.float32 if prec == "f" else np.float64).tiny)
+    for x, r in [(NAN, NAN), (-INF, NAN), (-1.0, -INF), (eps, eps), (1.0, math.log(2.0)), (0.0, 0.0),
+                 (tiny, tiny)]:
+        assert u(L, l1p(x), cast(r)) <= 0.5, ("log1p", prec, x)
+
+
+@pytest.mark.parametrize("fn", ["expm1", "log1p"])
+def test_expm1_log1p_cover(oracle, fn):
+    x = np.random.default_rng(6).uniform(-0.5, 0.5, 200000).astype(np.float32)
+    ref = (np.expm1 if fn == "expm1" else np.log1p)(x.astype(np.float64)).astype(np.float32)
+    m, w = oracle.max_ulp(oracle.map_(fn, x), ref)
+    assert m <= 1.0, (fn, m, x[w])
+    mpmath = pytest.importorskip("mpmath")
+    mpmath.mp.dps = 40
+    xd = np.random.default_rng(7).uniform(-0.5, 0.5, 2000)
+    mf = mpmath.expm1 if fn == "expm1" else mpmath.log1p
+    refd = np.array([float(mf(mpmath.mpf(float(v)))) for v in xd])
+    m, w = oracle.max_ulp(oracle.map_(fn, xd), refd)
+    assert m <= 1.0, (fn, "f64", m, xd[w])
