@@ -14,6 +14,7 @@
 #include "fold_tma.cuh"
 #include <stdlib.h>
 #include <string.h>
+#include <algorithm>
 #include <atomic>
 
 namespace nt2cuda {
@@ -103,13 +104,10 @@ cudaError_t inner_fold(const E& e, size_t rows, size_t cols, out_of<Op, T>* out,
   S* partials = nullptr;
   unsigned* counters = nullptr;
   if (sh.splits > 1) {
-    size_t cbytes = round_up(cols * sizeof(unsigned), 256);
-    size_t pbytes = cols * sh.splits * sizeof(S);
-    void* scratch = nullptr;
-    cudaError_t st = stream_scratch(s, cbytes + pbytes, &scratch);
+    void* p = nullptr;
+    cudaError_t st = fold_scratch(s, cols, cols * sh.splits, sizeof(S), &counters, &p);
     if (st != cudaSuccess) return st;
-    counters = (unsigned*)scratch;
-    partials = (S*)((char*)scratch + cbytes);
+    partials = (S*)p;
   }
   const size_t units = cols * sh.splits;
   E ec = e;
@@ -155,13 +153,10 @@ cudaError_t outer_fold(const E& e, size_t rows, size_t cols, out_of<Op, T>* out,
   S* partials = nullptr;
   unsigned* counters = nullptr;
   if (sh.splits > 1) {
-    size_t cbytes = round_up(sh.strips * sizeof(unsigned), 256);
-    size_t pbytes = sh.strips * sh.splits * STRIP * sizeof(S);
-    void* scratch = nullptr;
-    cudaError_t st = stream_scratch(s, cbytes + pbytes, &scratch);
+    void* p = nullptr;
+    cudaError_t st = fold_scratch(s, sh.strips, sh.strips * sh.splits * STRIP, sizeof(S), &counters, &p);
     if (st != cudaSuccess) return st;
-    counters = (unsigned*)scratch;
-    partials = (S*)((char*)scratch + cbytes);
+    partials = (S*)p;
   }
   const size_t units = sh.strips * sh.splits;
   E ec = e;

@@ -350,12 +350,10 @@ cudaError_t inner_fold_tma(const T* x, const T* y, size_t rows, size_t cols, out
   S* partials = nullptr;
   unsigned* counters = nullptr;
   if (sh.splits > 1) {
-    const size_t cbytes = (cols * sizeof(unsigned) + 255) / 256 * 256;
-    void* scratch = nullptr;
-    cudaError_t e = stream_scratch(s, cbytes + sh.units * sizeof(S), &scratch);
+    void* p = nullptr;
+    cudaError_t e = fold_scratch(s, cols, sh.units, sizeof(S), &counters, &p);
     if (e != cudaSuccess) return e;
-    counters = (unsigned*)scratch;
-    partials = (S*)((char*)scratch + cbytes);
+    partials = (S*)p;
   }
   size_t grid;
   cudaError_t e;
@@ -415,12 +413,10 @@ cudaError_t outer_fold_tma(const T* A, size_t rows, size_t cols, out_of<Op, T>* 
   S* partials = nullptr;
   unsigned* counters = nullptr;
   if (sh.splits > 1) {
-    const size_t cbytes = (sh.strips * sizeof(unsigned) + 255) / 256 * 256;
-    void* scratch = nullptr;
-    cudaError_t e = stream_scratch(s, cbytes + sh.units * BR * sizeof(S), &scratch);
+    void* p = nullptr;
+    cudaError_t e = fold_scratch(s, sh.strips, sh.units * BR, sizeof(S), &counters, &p);
     if (e != cudaSuccess) return e;
-    counters = (unsigned*)scratch;
-    partials = (S*)((char*)scratch + cbytes);
+    partials = (S*)p;
   }
   constexpr int ST = 4;
   auto k = k_outer_tma<Op, T, ST>;

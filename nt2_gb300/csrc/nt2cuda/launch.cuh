@@ -109,6 +109,14 @@ inline cudaError_t launch_persistent(K kernel, size_t work_items, int block, int
   return cudaLaunchKernel((const void*)kernel, dim3((unsigned)grid), dim3(block), args, 0, s);
 }
 
+// Launch with an explicit grid (at least one block).
+template <class K>
+inline cudaError_t launch_grid(K kernel, size_t grid, int block, cudaStream_t s, void** args)
+{
+  if (grid < 1) grid = 1;
+  return cudaLaunchKernel((const void*)kernel, dim3((unsigned)grid), dim3(block), args, 0, s);
+}
+
 // Evaluate statement p over [0,n).  Returns cudaErrorInvalidValue when the
 // statement's tables partially overlap.
 template <bool F, class P>

@@ -5,9 +5,10 @@
 // different streams never share scratch; calls on one stream are ordered and
 // reuse it.  A buffer only grows; growing synchronises its stream first.  The
 // first call on a stream allocates (cudaMalloc), so make it before capturing
-// that stream into a CUDA graph.  Counters at the front of a fold's scratch
-// start at zero (the buffer is cleared when allocated) and every fold leaves
-// them at zero.
+// that stream into a CUDA graph.  The folds' arrival counters have a slot of
+// their own: they start at zero (a buffer is cleared when allocated), every
+// fold leaves the ones it used at zero, and nothing else is written there --
+// partials, which other kernels overwrite freely, live in another slot.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -23,8 +24,24 @@ struct scratch_pool {
 };
 inline scratch_pool& global_scratch_pool() { static scratch_pool p; return p; }
 
-// slot 0: fold partials and counters; slot 1: batched-launch descriptors.
-inline cudaError_t stream_scratch(cudaStream_t s, size_t bytes, void** out, int slot = 0)
+// slot 0: fold arrival counters only; slot 1: per-call data (batched-launch
+// descriptors, scan flags and carries); slot 2: fold partials.
+inline cudaError_t stream_scratch(cudaStream_t s, size_t bytes, void** out, int slot = 0);
+
+// The two buffers of a fold: ncounters zero-valued arrival counters and room
+// for npartials partial states of `partial_bytes` each.
+inline cudaError_t fold_scratch(cudaStream_t s, size_t ncounters, size_t npartials, size_t partial_bytes,
+                                unsigned** counters, void** partials)
+{
+  void* c = nullptr;
+  cudaError_t e = stream_scratch(s, ncounters * sizeof(unsigned), &c, 0);
+  if (e != cudaSuccess) return e;
+  e = stream_scratch(s, npartials * partial_bytes, partials, 2);
+  *counters = (unsigned*)c;
+  return e;
+}
+
+inline cudaError_t stream_scratch(cudaStream_t s, size_t bytes, void** out, int slot)
 {
   int dev = 0;
   cudaGetDevice(&dev);
