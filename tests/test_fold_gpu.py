@@ -154,3 +154,17 @@ def test_f64_folds(gpu, oracle, n):
     M = A.reshape(300, 256)
     assert np.allclose(cs, M.sum(axis=1), rtol=0, atol=1e-12)
     assert np.allclose(rs, M.sum(axis=0), rtol=0, atol=1e-12)
+
+
+def test_fold_after_fold_shares_scratch_safely(gpu, oracle):
+    """A row-sum fold with split columns, then a column-sum fold with split rows on the same
+    stream: the second fold's arrival counters must not see the first fold's partials."""
+    rng = np.random.default_rng(12)
+    B = rng.standard_normal(2048 * 3000).astype(np.float32)
+    host(gpu.sum_colmajor(to_dev(B), 2048, 3000, 2))          # outer fold, partials in scratch
+    rows, cols = 40000, 100                                  # inner fold: 3 segments per column
+    A = rng.standard_normal(rows * cols).astype(np.float32)
+    got = host(gpu.sum_colmajor(to_dev(A), rows, cols, 1))
+    _, r64, a64 = oracle.inner_fold(A, rows, cols)
+    for j in range(cols):
+        assert abs(float(got[j]) - r64[j]) <= bound(True, rows, r64[j], a64[j]), j
