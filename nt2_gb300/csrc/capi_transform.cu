@@ -95,6 +95,7 @@ __global__ void __launch_bounds__(256) k_rgb2yuv(const float* __restrict__ r, co
                                                  const float* __restrict__ b, float* __restrict__ y,
                                                  float* __restrict__ u, float* __restrict__ v, size_t n)
 {
+  nt2cuda::mem::pdl_begin();
   constexpr int V = 4;
   const size_t groups = n / V;
   const size_t T = (size_t)gridDim.x * blockDim.x;
@@ -119,6 +120,7 @@ template <bool F>
 __global__ void __launch_bounds__(256) k_rgb2yuv_scalar(const float* r, const float* g, const float* b, float* y,
                                                         float* u, float* v, size_t n)
 {
+  nt2cuda::mem::pdl_begin();
   const size_t T = (size_t)gridDim.x * blockDim.x;
 #pragma unroll 1
   for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += T)

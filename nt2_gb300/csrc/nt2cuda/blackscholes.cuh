@@ -79,6 +79,7 @@ __global__ void __launch_bounds__(256) k_blackscholes(const T* __restrict__ S, c
                                                       const T* __restrict__ Tm, T r, T v,
                                                       T* __restrict__ call, T* __restrict__ put, size_t n)
 {
+  nt2cuda::mem::pdl_begin();
   constexpr int V = 16 / (int)sizeof(T);
   const T c = math::madd<(P != PREC_EXACT)>(math::mul(v, v), T(0.5), r);
   const size_t ngroups = n / V;
@@ -129,6 +130,7 @@ template <class T, int CDF, int P>
 __global__ void __launch_bounds__(256) k_blackscholes_scalar(const T* S, const T* K, const T* Tm, T r, T v,
                                                              T* call, T* put, size_t n)
 {
+  nt2cuda::mem::pdl_begin();
   const T c = math::madd<(P != PREC_EXACT)>(math::mul(v, v), T(0.5), r);
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     bs_lane<T, CDF, P>(S[i], K[i], Tm[i], r, v, c, call[i], put[i]);

@@ -345,6 +345,7 @@ template <int U> struct transform_min_blocks { static constexpr int value = U ==
 template <bool F, int V, int U, class P>
 __global__ void __launch_bounds__(256, transform_min_blocks<U>::value) k_transform(P p, size_t n)
 {
+  nt2cuda::mem::pdl_begin();
   const size_t ngroups = n / V;
   const size_t T = (size_t)gridDim.x * blockDim.x;
   const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;

@@ -225,6 +225,7 @@ template <class Op, class T> __device__ __forceinline__ state_of<Op, T> warp_mer
 template <class Op, class T>
 __global__ void __launch_bounds__(256) k_fold_empty(out_of<Op, T>* __restrict__ out, size_t count)
 {
+  nt2cuda::mem::pdl_begin();
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
     out[i] = Op::finish(Op::template init<T>(), 0);
 }
@@ -242,6 +243,7 @@ template <class Op, int V, int U, class T, class E>
 __global__ void __launch_bounds__(256) k_inner(E e, inner_shape sh, out_of<Op, T>* __restrict__ out,
                                                state_of<Op, T>* __restrict__ partials, unsigned* __restrict__ counters)
 {
+  nt2cuda::mem::pdl_begin();
   const int lane = threadIdx.x & 31;
   const size_t warps_total = (size_t)gridDim.x * (blockDim.x >> 5);
   const size_t units = sh.cols * sh.splits;
@@ -309,6 +311,7 @@ __global__ void __launch_bounds__(256) k_inner(E e, inner_shape sh, out_of<Op, T
 template <class Op, class T, class E>
 __global__ void __launch_bounds__(256) k_inner_short(E e, size_t rows, size_t cols, out_of<Op, T>* __restrict__ out)
 {
+  nt2cuda::mem::pdl_begin();
   for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < cols; j += (size_t)gridDim.x * blockDim.x) {
     state_of<Op, T> a = Op::template init<T>();
     for (size_t r = 0; r < rows; ++r) {
@@ -335,6 +338,7 @@ template <class Op, int V, int U, class T, class E>
 __global__ void __launch_bounds__(256) k_outer(E e, outer_shape sh, out_of<Op, T>* __restrict__ out,
                                                state_of<Op, T>* __restrict__ partials, unsigned* __restrict__ counters)
 {
+  nt2cuda::mem::pdl_begin();
   using S = state_of<Op, T>;
   constexpr int STRIP = 32 * V;
   __shared__ S red[8][STRIP];

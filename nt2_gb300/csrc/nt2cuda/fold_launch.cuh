@@ -115,7 +115,7 @@ cudaError_t inner_fold(const E& e, size_t rows, size_t cols, out_of<Op, T>* out,
   out_of<Op, T>* o = out;
   void* args[] = {&ec, &sh, &o, &partials, &counters};
   // launch_persistent counts threads; a unit is one warp
-  if (vec) return (launch_persistent(k_inner<Op, VV, fold_unroll<Op>::value, T, E>, units * 32, 256, 4, s, args));
+  if (vec) return (launch_persistent(k_inner<Op, VV, fold_unroll<Op>::value, T, E>, units * 32, 128, 4, s, args));
   return (launch_persistent(k_inner<Op, 1, 4, T, E>, units * 32, 256, 4, s, args));
 }
 

@@ -97,6 +97,27 @@ template <class K> inline int resident_blocks(K kernel, int block)
   return nb;
 }
 
+// Launch as a programmatic dependent of the previous kernel on the stream:
+// the grid may be scheduled while its predecessor finishes, and waits in
+// pdl_begin() until the predecessor has completed and its writes are visible.
+// Every kernel launched this way starts with pdl_begin().
+template <class K>
+inline cudaError_t launch_dependent(K kernel, size_t grid, int block, cudaStream_t s, void** args)
+{
+  if (grid < 1) grid = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelExC(&cfg, (const void*)kernel, args);
+}
+
 template <class K>
 inline cudaError_t launch_persistent(K kernel, size_t work_items, int block, int waves,
                                      cudaStream_t s, void** args)
@@ -105,16 +126,14 @@ inline cudaError_t launch_persistent(K kernel, size_t work_items, int block, int
   size_t full = (size_t)sm_count() * (size_t)per_sm * (size_t)(waves > 0 ? waves : 1);
   size_t need = (work_items + (size_t)block - 1) / (size_t)block;
   size_t grid = need < full ? need : full;
-  if (grid < 1) grid = 1;
-  return cudaLaunchKernel((const void*)kernel, dim3((unsigned)grid), dim3(block), args, 0, s);
+  return launch_dependent(kernel, grid, block, s, args);
 }
 
 // Launch with an explicit grid (at least one block).
 template <class K>
 inline cudaError_t launch_grid(K kernel, size_t grid, int block, cudaStream_t s, void** args)
 {
-  if (grid < 1) grid = 1;
-  return cudaLaunchKernel((const void*)kernel, dim3((unsigned)grid), dim3(block), args, 0, s);
+  return launch_dependent(kernel, grid, block, s, args);
 }
 
 // Evaluate statement p over [0,n).  Returns cudaErrorInvalidValue when the

@@ -151,5 +151,13 @@ __device__ __forceinline__ void store_vec(T* base, size_t i, const T (&in)[V])
   }
 }
 
+// Kernels launched as programmatic dependents (launch.cuh) begin here: wait
+// until the previous grid on the stream has completed and its writes are
+// visible, then let the next grid be scheduled.
+__device__ __forceinline__ void pdl_begin()
+{
+  asm volatile("griddepcontrol.wait;\n\tgriddepcontrol.launch_dependents;" ::: "memory");
+}
+
 }  // namespace mem
 }  // namespace nt2cuda

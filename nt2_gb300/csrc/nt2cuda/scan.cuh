@@ -735,6 +735,7 @@ template <class Op, class T>
 __global__ void __launch_bounds__(256) k_scan_inner_short(const T* __restrict__ x, T* __restrict__ y, size_t rows,
                                                           size_t cols)
 {
+  nt2cuda::mem::pdl_begin();
   for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < cols; j += (size_t)gridDim.x * blockDim.x) {
     state_of<Op, T> st = Op::template init<T>();
     for (size_t r = 0; r < rows; ++r) {
@@ -758,6 +759,7 @@ template <class Op, class T, int V, bool WRITE>
 __global__ void __launch_bounds__(256) k_scan_outer(const T* __restrict__ x, T* __restrict__ y, outer_shape sh,
                                                     state_of<Op, T>* __restrict__ totals)
 {
+  nt2cuda::mem::pdl_begin();
   using S = state_of<Op, T>;
   constexpr int ROWS = 256 * V;
   const size_t units = sh.strips * sh.chunks;
@@ -817,6 +819,7 @@ __global__ void __launch_bounds__(256) k_scan_outer(const T* __restrict__ x, T* 
 template <class Op, class T, int V>
 __global__ void __launch_bounds__(256) k_scan_outer_prefix(outer_shape sh, state_of<Op, T>* __restrict__ totals)
 {
+  nt2cuda::mem::pdl_begin();
   using S = state_of<Op, T>;
   constexpr size_t ROWS = 256 * (size_t)V;
   const size_t n = sh.strips * ROWS;
