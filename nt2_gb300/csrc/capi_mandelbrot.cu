@@ -46,6 +46,7 @@ __global__ void __launch_bounds__(256) k_mandelbrot(const float* __restrict__ A,
                                                     grid gr, int32_t* __restrict__ C, uint64_t n,
                                                     uint64_t nfull)
 {
+  nt2cuda::mem::pdl_begin();
   const uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned lane = threadIdx.x & 31u;
   const bool in = e < n;
@@ -92,16 +93,18 @@ nt2cuda_status launch(const float* A, const float* B, const grid& g, int32_t* C,
   const uint64_t nfull = n - n % (uint64_t)pack;
   const uint64_t blocks = (n + 255) / 256;
   if (blocks > 0x7fffffffULL) return NT2CUDA_ERR_ARG;
-  const dim3 gd((unsigned)blocks), bd(256);
+  void* args[] = {(void*)&A, (void*)&B, (void*)&g, (void*)&C, (void*)&n, (void*)&nfull};
+  cudaError_t e;
   switch (pack) {
-    case 1: k_mandelbrot<1, GRID><<<gd, bd, 0, s>>>(A, B, g, C, n, nfull); break;
-    case 2: k_mandelbrot<2, GRID><<<gd, bd, 0, s>>>(A, B, g, C, n, nfull); break;
-    case 4: k_mandelbrot<4, GRID><<<gd, bd, 0, s>>>(A, B, g, C, n, nfull); break;
-    case 8: k_mandelbrot<8, GRID><<<gd, bd, 0, s>>>(A, B, g, C, n, nfull); break;
-    case 16: k_mandelbrot<16, GRID><<<gd, bd, 0, s>>>(A, B, g, C, n, nfull); break;
-    case 32: k_mandelbrot<32, GRID><<<gd, bd, 0, s>>>(A, B, g, C, n, nfull); break;
+    case 1: e = launch_grid(k_mandelbrot<1, GRID>, blocks, 256, s, args); break;
+    case 2: e = launch_grid(k_mandelbrot<2, GRID>, blocks, 256, s, args); break;
+    case 4: e = launch_grid(k_mandelbrot<4, GRID>, blocks, 256, s, args); break;
+    case 8: e = launch_grid(k_mandelbrot<8, GRID>, blocks, 256, s, args); break;
+    case 16: e = launch_grid(k_mandelbrot<16, GRID>, blocks, 256, s, args); break;
+    case 32: e = launch_grid(k_mandelbrot<32, GRID>, blocks, 256, s, args); break;
     default: return NT2CUDA_ERR_ARG;
   }
+  if (e != cudaSuccess) return launch_status(e);
   return launch_status(cudaGetLastError());
 }
 

@@ -95,6 +95,7 @@ __global__ void __launch_bounds__(256) k_inner_tma(const T* __restrict__ x, cons
                                                    state_of<Op, T>* __restrict__ partials,
                                                    unsigned* __restrict__ counters)
 {
+  nt2cuda::mem::pdl_begin();
   using S = state_of<Op, T>;
   constexpr int TILE = inner_tile<T>();
   constexpr int V = 16 / (int)sizeof(T);
@@ -216,6 +217,7 @@ __global__ void __launch_bounds__(256) k_outer_tma(const __grid_constant__ CUten
                                                    state_of<Op, T>* __restrict__ partials,
                                                    unsigned* __restrict__ counters)
 {
+  nt2cuda::mem::pdl_begin();
   using S = state_of<Op, T>;
   constexpr int BR = kOuterRows, BC = outer_cols<T>();
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -366,7 +368,9 @@ cudaError_t inner_fold_tma(const T* x, const T* y, size_t rows, size_t cols, out
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, 256, smem);
     grid = (size_t)sm_count() * (size_t)(per > 0 ? per : 1);
     if (grid > sh.units) grid = sh.units;
-    k<<<(unsigned)grid, 256, smem, s>>>(x, y, sh, out, partials, counters);
+    void* args[] = {(void*)&x, (void*)&y, (void*)&sh, (void*)&out, (void*)&partials, (void*)&counters};
+    e = launch_dependent(k, grid, 256, s, args, smem);
+    if (e != cudaSuccess) return e;
   } else {
     constexpr int ST = 4;
     auto k = k_inner_tma<Op, T, 1, ST>;
@@ -376,7 +380,9 @@ cudaError_t inner_fold_tma(const T* x, const T* y, size_t rows, size_t cols, out
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, 256, smem);
     grid = (size_t)sm_count() * (size_t)(per > 0 ? per : 1);
     if (grid > sh.units) grid = sh.units;
-    k<<<(unsigned)grid, 256, smem, s>>>(x, y, sh, out, partials, counters);
+    void* args[] = {(void*)&x, (void*)&y, (void*)&sh, (void*)&out, (void*)&partials, (void*)&counters};
+    e = launch_dependent(k, grid, 256, s, args, smem);
+    if (e != cudaSuccess) return e;
   }
   return cudaGetLastError();
 }
@@ -427,7 +433,9 @@ cudaError_t outer_fold_tma(const T* A, size_t rows, size_t cols, out_of<Op, T>* 
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, 256, smem);
   size_t grid = (size_t)sm_count() * (size_t)(per > 0 ? per : 1);
   if (grid > sh.units) grid = sh.units;
-  k<<<(unsigned)grid, 256, smem, s>>>(map, sh, out, partials, counters);
+  void* args[] = {(void*)&map, (void*)&sh, (void*)&out, (void*)&partials, (void*)&counters};
+  e = launch_dependent(k, grid, 256, s, args, smem);
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 

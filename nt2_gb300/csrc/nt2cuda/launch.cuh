@@ -102,13 +102,14 @@ template <class K> inline int resident_blocks(K kernel, int block)
 // pdl_begin() until the predecessor has completed and its writes are visible.
 // Every kernel launched this way starts with pdl_begin().
 template <class K>
-inline cudaError_t launch_dependent(K kernel, size_t grid, int block, cudaStream_t s, void** args)
+inline cudaError_t launch_dependent(K kernel, size_t grid, int block, cudaStream_t s, void** args,
+                                    size_t smem = 0)
 {
   if (grid < 1) grid = 1;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
   cfg.blockDim = dim3(block);
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;

@@ -522,6 +522,7 @@ __global__ void __launch_bounds__(256) k_scan_inner(const T* __restrict__ x, T* 
                                                     unsigned* __restrict__ flags, void* __restrict__ aggv,
                                                     void* __restrict__ inclv, unsigned* __restrict__ err)
 {
+  nt2cuda::mem::pdl_begin();
   using K = scan_tiles<Op, T>;
   using S = typename K::S;
   S* agg = reinterpret_cast<S*>(aggv);
@@ -589,6 +590,7 @@ __global__ void __launch_bounds__(256) k_scan_inner_1p(const T* __restrict__ x, 
                                                        unsigned* __restrict__ flags, void* __restrict__ aggv,
                                                        void* __restrict__ inclv, unsigned* __restrict__ err)
 {
+  nt2cuda::mem::pdl_begin();
   using K = scan_tiles<Op, T>;
   using S = typename K::S;
   constexpr int CK = carry_of<Op, T>::value;

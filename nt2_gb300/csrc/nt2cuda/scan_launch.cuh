@@ -49,8 +49,9 @@ cudaError_t inner_scan(const T* x, T* y, size_t rows, size_t cols, cudaStream_t 
   auto k = one_pass ? k_scan_inner_1p<Op, T, false> : k_scan_inner<Op, T>;
   size_t grid = (size_t)sm_count() * (size_t)resident_blocks(k, 256);
   if (grid > sh.tiles) grid = sh.tiles;
-  k<<<(unsigned)grid, 256, 0, s>>>(x, y, sh, vec, ticket, flags, agg, incl, err);
-  return cudaGetLastError();
+  void* args[] = {(void*)&x, (void*)&y, (void*)&sh, (void*)&vec, (void*)&ticket, (void*)&flags, (void*)&agg,
+                  (void*)&incl, (void*)&err};
+  return launch_dependent(k, grid, 256, s, args);
 }
 
 template <class Op, class T, int V>
