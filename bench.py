@@ -384,7 +384,7 @@ def run_ours(args):
 
 
 CASES = ("bs_exact", "bs_fused", "bs_fast", "bs_fastnormcdf", "bs_f64", "saxpy", "sdot", "sdot_plain",
-         "rgb2grey_u8", "rgb2yuv", "mandelbrot", "reductions", "scans",
+         "rgb2grey_u8", "rgb2yuv", "mandelbrot", "trig", "reductions", "scans",
          "inner", "outer", "sigmadelta")
 
 
@@ -497,6 +497,29 @@ def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: in
         out.append({"config": "mandelbrot 1600x1600 over [-1.5,1.5]^2, pack 8 (FP32 issue-bound)", "ms": ms,
                     "value": h * w / (ms * 1e-3), "unit": "pixels/s",
                     "counted_trips_per_s": counts / (ms * 1e-3), "mean_count": counts / (h * w)})
+    if want("trig"):
+        # y = op(x) over 2^24 elements of [-60, 60] (NT2's cover range; packs at the cephes level),
+        # 2 rotating inputs of 64/128 MB; 8 (float) or 16 (double) bytes per element
+        for dt, tname in ((torch.float32, "f32"), (torch.float64, "f64")):
+            n = 1 << 24
+            xs = [torch.empty(n, dtype=dt, device="cuda") for _ in range(2)]
+            for k, t in enumerate(xs):
+                api.fill_uniform(t, -60.0, 60.0, 41 + k)
+            y = torch.empty(n, dtype=dt, device="cuda")
+            for op in ("sin", "cos", "tan"):
+                for simd in (False, True):
+                    label = f"{op} {tname} 2^24 [-60,60]{' simd128' if simd else ''}"
+                    if part and part not in label:
+                        continue
+                    it = [0]
+
+                    def trig_step(op=op, simd=simd):
+                        x = xs[it[0] & 1]
+                        it[0] += 1
+                        api.map_(op, x, out=y, simd128=simd)
+                    ms, _, _ = time_device(trig_step, K(100), warmup, ws)
+                    out.append(line(label, ms, 2 * n * xs[0].element_size(), n, "elements/s"))
+            del xs, y
     if not (want("inner") or want("outer") or want("reductions") or want("scans") or want("bs_f64") or want("bs_fused") or want("bs_fast")
             or want("bs_exact") or want("bs_fastnormcdf") or want("sigmadelta")):
         return out

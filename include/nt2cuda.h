@@ -87,7 +87,18 @@ nt2cuda_status nt2cuda_stream_sync(nt2cuda_stream stream);
  * generic/fastnormcdf.hpp:33-55, boost/simd/arithmetic/functions/scalar/sqrt.hpp:21-62)
  * and exp2/exp10/log2/log10/expm1/log1p
  * (modules/core/exponential/include/nt2/exponential/functions/scalar/impl/expo/{f,d}_expo_reduction.hpp,
- * simd/common/impl/logs/{f,d}_log.hpp, details/expm1_kernel.hpp, simd/common/log1p.hpp). */
+ * simd/common/impl/logs/{f,d}_log.hpp, details/expm1_kernel.hpp, simd/common/log1p.hpp)
+ * and sin/cos/tan/sinpi/cospi
+ * (modules/core/trigonometric/include/nt2/trigonometric/functions/generic/{sin,cos,tan,sinpi,cospi}.hpp
+ * over scalar/impl/trigo/trig_base.hpp and simd/common/impl/trigo/trig_base.hpp).
+ * NT2's SIMD code reduces the arguments of a whole pack with the method it
+ * picks for the pack's largest |x|
+ * (functions/scalar/impl/trigo/trig_reduction.hpp:46-183), so its results
+ * depend on the pack width.  By default each element is reduced on its own,
+ * as NT2's scalar code does (NT2 without a SIMD extension, e.g. on aarch64);
+ * with NT2CUDA_MAP_SIMD128 each 16-byte pack (4 floats, 2 doubles, from index
+ * 0) is reduced together, as NT2 on a 128-bit SIMD extension does, with the
+ * n % pack tail scalar (tables not 16-byte aligned: scalar throughout). */
 enum {
   NT2CUDA_OP_EXP = 0,
   NT2CUDA_OP_LOG = 1,
@@ -100,13 +111,23 @@ enum {
   NT2CUDA_OP_LOG2 = 8,
   NT2CUDA_OP_LOG10 = 9,
   NT2CUDA_OP_EXPM1 = 10,
-  NT2CUDA_OP_LOG1P = 11
+  NT2CUDA_OP_LOG1P = 11,
+  NT2CUDA_OP_SIN = 12,
+  NT2CUDA_OP_COS = 13,
+  NT2CUDA_OP_TAN = 14,
+  NT2CUDA_OP_SINPI = 15,
+  NT2CUDA_OP_COSPI = 16
 };
 
+/* Flags of nt2cuda_map_*. */
+#define NT2CUDA_MAP_FUSED 1     /* hardware FMA (the `fused` convention above) */
+#define NT2CUDA_MAP_SIMD128 2   /* trigonometric ops: 128-bit pack reductions  */
+
 /* y = op(x).  Replaces `y = nt2::op(x)` evaluated by transform_
- * (modules/core/base/include/nt2/core/functions/transform.hpp:23-69). */
-nt2cuda_status nt2cuda_map_f32(int op, const float* x, float* y, size_t n, int fused, nt2cuda_stream stream);
-nt2cuda_status nt2cuda_map_f64(int op, const double* x, double* y, size_t n, int fused, nt2cuda_stream stream);
+ * (modules/core/base/include/nt2/core/functions/transform.hpp:23-69).
+ * `flags`: NT2CUDA_MAP_FUSED | NT2CUDA_MAP_SIMD128 (0 = exact, scalar packs). */
+nt2cuda_status nt2cuda_map_f32(int op, const float* x, float* y, size_t n, int flags, nt2cuda_stream stream);
+nt2cuda_status nt2cuda_map_f64(int op, const double* x, double* y, size_t n, int flags, nt2cuda_stream stream);
 
 /* Y = alpha*X + Y (demo/saxpy/nt2/saxpy_nt2.cpp:39-42). */
 nt2cuda_status nt2cuda_saxpy_f32(float alpha, const float* x, float* y, size_t n, int fused, nt2cuda_stream stream);

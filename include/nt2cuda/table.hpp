@@ -292,6 +292,11 @@ NT2CUDA_FN1(log2, log2_)
 NT2CUDA_FN1(log10, log10_)
 NT2CUDA_FN1(expm1, expm1_)
 NT2CUDA_FN1(log1p, log1p_)
+NT2CUDA_FN1(sin, sin_)
+NT2CUDA_FN1(cos, cos_)
+NT2CUDA_FN1(tan, tan_)
+NT2CUDA_FN1(sinpi, sinpi_)
+NT2CUDA_FN1(cospi, cospi_)
 NT2CUDA_FN1(sqrt, sqrt_)
 NT2CUDA_FN1(sqr, sqr_)
 NT2CUDA_FN1(erfc, erfc_)

@@ -15,7 +15,7 @@ import torch
 from ._lib import SdStream, check, lib
 
 OPS = {"exp": 0, "log": 1, "erfc": 2, "normcdf": 3, "fastnormcdf": 4, "sqrt": 5, "exp2": 6, "exp10": 7, "log2": 8,
-       "log10": 9, "expm1": 10, "log1p": 11}
+       "log10": 9, "expm1": 10, "log1p": 11, "sin": 12, "cos": 13, "tan": 14, "sinpi": 15, "cospi": 16}
 CDF = {"normcdf": 0, "fastnormcdf": 1}
 
 
@@ -37,15 +37,22 @@ def init(device: int = 0) -> None:
     check(lib().nt2cuda_init(device), "init")
 
 
-def map_(op: str, x: torch.Tensor, out: torch.Tensor | None = None, fused: bool = False) -> torch.Tensor:
+MAP_FUSED, MAP_SIMD128 = 1, 2
+
+
+def map_(op: str, x: torch.Tensor, out: torch.Tensor | None = None, fused: bool = False,
+         simd128: bool = False) -> torch.Tensor:
     """out = nt2::op(x) for op in exp, log, erfc, normcdf, fastnormcdf, sqrt, exp2, exp10, log2, log10, expm1,
-    log1p."""
+    log1p, sin, cos, tan, sinpi, cospi.  The trigonometric ops reduce each element on its own (NT2's scalar
+    code); with simd128 they reduce each 16-byte pack of x with the method NT2's 128-bit SIMD code picks for
+    the pack's largest |x| (tables that are not 16-byte aligned: scalar code throughout)."""
     out = torch.empty_like(x) if out is None else out
     L = lib()
+    flags = (MAP_FUSED if fused else 0) | (MAP_SIMD128 if simd128 else 0)
     if x.dtype == torch.float32:
-        st = L.nt2cuda_map_f32(OPS[op], _dev(x), _dev(out, torch.float32), x.numel(), int(fused), _stream())
+        st = L.nt2cuda_map_f32(OPS[op], _dev(x), _dev(out, torch.float32), x.numel(), flags, _stream())
     elif x.dtype == torch.float64:
-        st = L.nt2cuda_map_f64(OPS[op], _dev(x), _dev(out, torch.float64), x.numel(), int(fused), _stream())
+        st = L.nt2cuda_map_f64(OPS[op], _dev(x), _dev(out, torch.float64), x.numel(), flags, _stream())
     else:
         raise TypeError("map_ takes float32 or float64 tables")
     check(st, f"map_({op})")

@@ -28,6 +28,8 @@ SOURCES = [
     "capi_scan.cu",
     "server.cu",
     "capi_noalloc.cu",
+    "capi_trig_f32.cu",
+    "capi_trig_f64.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

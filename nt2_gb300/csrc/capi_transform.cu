@@ -256,15 +256,23 @@ void nt2cuda::detail_capi::warm_blackscholes_f32(int cdf, int prec)
 
 extern "C" {
 
-nt2cuda_status nt2cuda_map_f32(int op, const float* x, float* y, size_t n, int fused, nt2cuda_stream s)
+nt2cuda_status nt2cuda_map_f32(int op, const float* x, float* y, size_t n, int flags, nt2cuda_stream s)
 {
   if (n && (!x || !y)) return NT2CUDA_ERR_ARG;
+  if (flags & ~(NT2CUDA_MAP_FUSED | NT2CUDA_MAP_SIMD128)) return NT2CUDA_ERR_ARG;
+  const bool fused = (flags & NT2CUDA_MAP_FUSED) != 0;
+  if (op >= NT2CUDA_OP_SIN && op <= NT2CUDA_OP_COSPI)
+    return map_trig(op, x, y, n, fused, (flags & NT2CUDA_MAP_SIMD128) != 0, s);
   return fused ? map_impl<true>(op, x, y, n, s) : map_impl<false>(op, x, y, n, s);
 }
 
-nt2cuda_status nt2cuda_map_f64(int op, const double* x, double* y, size_t n, int fused, nt2cuda_stream s)
+nt2cuda_status nt2cuda_map_f64(int op, const double* x, double* y, size_t n, int flags, nt2cuda_stream s)
 {
   if (n && (!x || !y)) return NT2CUDA_ERR_ARG;
+  if (flags & ~(NT2CUDA_MAP_FUSED | NT2CUDA_MAP_SIMD128)) return NT2CUDA_ERR_ARG;
+  const bool fused = (flags & NT2CUDA_MAP_FUSED) != 0;
+  if (op >= NT2CUDA_OP_SIN && op <= NT2CUDA_OP_COSPI)
+    return map_trig(op, x, y, n, fused, (flags & NT2CUDA_MAP_SIMD128) != 0, s);
   return fused ? map_impl<true>(op, x, y, n, s) : map_impl<false>(op, x, y, n, s);
 }
 

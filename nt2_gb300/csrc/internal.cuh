@@ -40,5 +40,11 @@ inline nt2cuda_status stream_scratch(cudaStream_t s, size_t bytes, void** out, i
 // pair ahead of their first launch (capi_transform.cu).
 void warm_blackscholes_f32(int cdf_kind, int precision);
 
+// y = op(x) for the trigonometric ops of nt2cuda_map_*, reduced element by
+// element or (simd128) over 16-byte packs (capi_trig.cu, a translation unit of
+// its own so that the build compiles it in parallel).
+nt2cuda_status map_trig(int op, const float* x, float* y, size_t n, bool fused, bool simd128, nt2cuda_stream s);
+nt2cuda_status map_trig(int op, const double* x, double* y, size_t n, bool fused, bool simd128, nt2cuda_stream s);
+
 }  // namespace detail_capi
 }  // namespace nt2cuda

@@ -24,6 +24,7 @@
 #include <limits>
 #include <type_traits>
 #include "math.cuh"
+#include "trig.cuh"
 #include "memory.cuh"
 
 namespace nt2cuda {
@@ -42,6 +43,11 @@ struct is_less_equal_ {}; struct is_greater_equal_ {}; struct is_equal_ {};
 struct is_not_equal_ {}; struct oneminus_ {}; struct minusone_ {}; struct cast_ {};
 // cast<uint8_t> of a float the statement keeps in [0, 256) (see trunc_u8 below)
 struct trunc_u8_ {};
+// trigonometric functors, reduced element by element as NT2's scalar code does;
+// simd128_<T> evaluates T over 16-byte packs as NT2's 128-bit SIMD code does
+// (see regs<node<simd128_<...>>> below)
+struct sin_ {}; struct cos_ {}; struct tan_ {}; struct sinpi_ {}; struct cospi_ {};
+template <class T> struct simd128_ {};
 }  // namespace tag
 
 // ------------------------------------------------------------ tree nodes
@@ -139,6 +145,11 @@ NT2CUDA_UN(log1p_, math::log1p<F>(a))
 NT2CUDA_UN(erfc_, math::erfc<F>(a))
 NT2CUDA_UN(normcdf_, math::normcdf<F>(a))
 NT2CUDA_UN(fastnormcdf_, math::fastnormcdf<F>(a))
+NT2CUDA_UN(sin_, (trig::one<trig::SIN, F>(a)))
+NT2CUDA_UN(cos_, (trig::one<trig::COS, F>(a)))
+NT2CUDA_UN(tan_, (trig::one<trig::TAN, F>(a)))
+NT2CUDA_UN(sinpi_, (trig::one<trig::SINPI, F>(a)))
+NT2CUDA_UN(cospi_, (trig::one<trig::COSPI, F>(a)))
 // trunc_u8(y) = cast<uint8_t>(y) for a float y in [0, 256), where the cast truncates toward
 // zero: 2^23 + y rounded toward zero is 2^23 + floor(y), whose low byte is the result.
 // Used where the statement bounds y (rgb2grey's weights sum below 1); a full-rate add in
@@ -281,6 +292,44 @@ template <class Tag, class A, class B, class C, int V> struct regs<node<Tag, A, 
   }
   template <bool F> __device__ __forceinline__ auto get(const node<Tag, A, B, C>& n, int l) const {
     return fn<Tag, F>::apply(ra.template get<F>(n.a, l), rb.template get<F>(n.b, l), rc.template get<F>(n.c, l));
+  }
+};
+
+// 128-bit SIMD form of a trigonometric node.  NT2's SIMD code reduces the
+// arguments of a whole pack with one method chosen from the pack's largest |x|
+// (nt2cuda/trig.cuh), so a lane's value depends on its neighbours: the node
+// computes all lanes of a pack when asked for the pack's first lane and hands
+// out the rest from `res`.  The kernels ask for lanes 0..V-1 in order.  A pack
+// is 16 bytes of the argument type; groups of fewer lanes (the scalar tail,
+// misaligned tables) are NT2's scalar code.
+template <class Tag> struct trig_kind;
+template <> struct trig_kind<tag::sin_> { static constexpr int value = trig::SIN; };
+template <> struct trig_kind<tag::cos_> { static constexpr int value = trig::COS; };
+template <> struct trig_kind<tag::tan_> { static constexpr int value = trig::TAN; };
+template <> struct trig_kind<tag::sinpi_> { static constexpr int value = trig::SINPI; };
+template <> struct trig_kind<tag::cospi_> { static constexpr int value = trig::COSPI; };
+
+template <class Tag, class A, int V> struct regs<node<tag::simd128_<Tag>, A>, V> {
+  using N = node<tag::simd128_<Tag>, A>;
+  using T = typename value_of<A>::type;
+  static_assert(std::is_same<T, float>::value || std::is_same<T, double>::value,
+                "trigonometric functors take float or double tables");
+  static constexpr int PW = 16 / (int)sizeof(T);
+  static constexpr int P = (V % PW == 0) ? PW : 1;
+  regs<A, V> ra;
+  mutable T res[V];
+  template <bool S> __device__ __forceinline__ void load(const N& n, size_t i) { ra.template load<S>(n.a, i); }
+  template <bool S> __device__ __forceinline__ void load_one(const N& n, size_t i, int l) { ra.template load_one<S>(n.a, i, l); }
+  template <bool F> __device__ __forceinline__ T get(const N& n, int l) const {
+    if (l % P == 0) {
+      T a[P], y[P];
+#pragma unroll
+      for (int p = 0; p < P; ++p) a[p] = (T)ra.template get<F>(n.a, l + p);
+      trig::pack<trig_kind<Tag>::value, F, P>(a, y);
+#pragma unroll
+      for (int p = 0; p < P; ++p) res[l + p] = y[p];
+    }
+    return res[l];
   }
 };
 

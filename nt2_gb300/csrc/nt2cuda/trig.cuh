@@ -1,0 +1,565 @@
+// nt2cuda/trig.cuh -- NT2's sin, cos, tan (radians) and sinpi, cospi for
+// float and double, evaluated over packs of lanes the way NT2's SIMD
+// transform evaluates them.
+//
+// Paths are relative to NT2's modules/core/trigonometric/include/nt2/trigonometric/.
+//
+// NT2 reduces a whole pack with one method, chosen from the pack's largest
+// |x| (functions/scalar/impl/trigo/trig_reduction.hpp:46-183, mode big_ of
+// functions/scalar/impl/selection_tags.hpp:55-61):
+//   level 0  all |x| <= pi/4       no reduction
+//   level 1  all |x| <= pi/2       rem_pio2_straight   (functions/generic/rem_pio2_straight.hpp)
+//   level 2  all |x| <= 20 pi      rem_pio2_cephes     (functions/generic/rem_pio2_cephes.hpp)
+//   level 3  all |x| <= Medium_pi  rem_pio2_medium     (functions/generic/rem_pio2_medium.hpp);
+//                                  Medium_pi = 2^6 pi (float), 2^18 pi (double)
+//   level 4  float, all |x| <= 2^18 pi: each half pack converted to double and
+//            reduced by the double chain
+//   level 5  rem_pio2 lane by lane (functions/scalar/rem_pio2.hpp, fdlibm)
+// one() is NT2's scalar code (each element its own pack); pack<P>() is NT2's
+// SIMD code over P lanes, used with P = one 16-byte group of a thread (4
+// floats, 2 doubles: NT2 on a 128-bit SIMD extension).
+// Lanes that reach fdlibm's __kernel_rem_pio2(f) (float |x| > 2^7 pi/2 at level
+// 5, double |x| > 2^19 pi/2) use an exact Payne-Hanek reduction rounded once.
+// The polynomials are functions/simd/common/impl/trigo/{f,d}_trig_evaluation.hpp
+// with NT2's unfused fma; F (fused) contracts them.
+#pragma once
+#include <stdint.h>
+#include "math.cuh"
+
+namespace nt2cuda {
+namespace trig {
+
+using math::fbits;
+using math::dbits;
+
+enum kind { SIN = 0, COS = 1, TAN = 2, SINPI = 3, COSPI = 4 };
+
+// Bit patterns of the BOOST_SIMD_CONSTANT_REGISTER lines in constants/*.hpp.
+struct tf {
+  static constexpr uint32_t pio4 = 0x3f490fdbu, pio2 = 0x3fc90fdbu, p20pi = 0x427b53d1u,
+                            medpi = 0x43490fdbu, dmpi = 0x49490fdbu, pi = 0x40490fdbu,
+                            twoopi = 0x3f22f983u, invpio2 = 0x3f22f984u, pio2_1 = 0x3fc90f80u,
+                            pio2_2 = 0x37354400u, pio2_3 = 0x2e85a300u, pio2_1t = 0x37354443u,
+                            pio2_2t = 0x2e85a308u, pio2_3t = 0x248d3132u;
+};
+struct td {
+  static constexpr uint64_t pio4 = 0x3fe921fb54442d18ull, pio2 = 0x3ff921fb54442d18ull,
+                            p20pi = 0x404f6a7a2955385eull, medpi = 0x412921fb54442d18ull,
+                            pi = 0x400921fb54442d18ull, twoopi = 0x3fe45f306dc9c883ull,
+                            invpio2 = 0x3fe45f306dc9c883ull, pio2_1 = 0x3ff921fb54400000ull,
+                            pio2_2 = 0x3dd0b4611a600000ull, pio2_3 = 0x3ba3198a2e000000ull,
+                            pio2_1t = 0x3dd0b4611a626331ull, pio2_2t = 0x3ba3198a2e037073ull,
+                            pio2_3t = 0x397b839a252049c1ull;
+};
+
+// High bits of n*pi/2, n = 1..32 (float: pattern with the low 8 bits
+// cleared; double: high word): the cancellation test of fdlibm's medium branch.
+__device__ __constant__ const uint32_t kNpio2F[32] = {
+  0x3fc90f00u, 0x40490f00u, 0x4096cb00u, 0x40c90f00u, 0x40fb5300u, 0x4116cb00u, 0x412fed00u, 0x41490f00u,
+  0x41623100u, 0x417b5300u, 0x418a3a00u, 0x4196cb00u, 0x41a35c00u, 0x41afed00u, 0x41bc7e00u, 0x41c90f00u,
+  0x41d5a000u, 0x41e23100u, 0x41eec200u, 0x41fb5300u, 0x4203f200u, 0x420a3a00u, 0x42108300u, 0x4216cb00u,
+  0x421d1400u, 0x42235c00u, 0x4229a500u, 0x422fed00u, 0x42363600u, 0x423c7e00u, 0x4242c700u, 0x42490f00u};
+__device__ __constant__ const uint32_t kNpio2D[32] = {
+  0x3ff921fbu, 0x400921fbu, 0x4012d97cu, 0x401921fbu, 0x401f6a7au, 0x4022d97cu, 0x4025fdbbu, 0x402921fbu,
+  0x402c463au, 0x402f6a7au, 0x4031475cu, 0x4032d97cu, 0x40346b9cu, 0x4035fdbbu, 0x40378fdbu, 0x403921fbu,
+  0x403ab41bu, 0x403c463au, 0x403dd85au, 0x403f6a7au, 0x40407e4cu, 0x4041475cu, 0x4042106cu, 0x4042d97cu,
+  0x4043a28cu, 0x40446b9cu, 0x404534acu, 0x4045fdbbu, 0x4046c6cbu, 0x40478fdbu, 0x404858ebu, 0x404921fbu};
+
+// 2/pi, bits after the binary point, 32 per word.
+__device__ __constant__ const uint32_t kTwoOverPi[40] = {
+  0xa2f9836eu, 0x4e441529u, 0xfc2757d1u, 0xf534ddc0u, 0xdb629599u, 0x3c439041u, 0xfe5163abu, 0xdebbc561u,
+  0xb7246e3au, 0x424dd2e0u, 0x06492eeau, 0x09d1921cu, 0xfe1deb1cu, 0xb129a73eu, 0xe88235f5u, 0x2ebb4484u,
+  0xe99c7026u, 0xb45f7e41u, 0x3991d639u, 0x835339f4u, 0x9c845f8bu, 0xbdf9283bu, 0x1ff897ffu, 0xde05980fu,
+  0xef2f118bu, 0x5a0a6d1fu, 0x6d367ecfu, 0x27cb09b7u, 0x4f463f66u, 0x9e5fea2du, 0x7527bac7u, 0xebe5f17bu,
+  0x3d0739f7u, 0x8a5292eau, 0x6bfb5fb1u, 0x1f8d5d08u, 0x56033046u, 0xfc7b6babu, 0xf0cfbc20u, 0x9af4361du};
+
+// ------------------------------------------------ exact Payne-Hanek reduction
+// 64-bit limbs, little-endian.
+template <int N> __device__ __forceinline__ int lbit(const uint64_t (&p)[N], int k)
+{
+  return (k < 0 || k >= 64 * N) ? 0 : (int)((p[k >> 6] >> (k & 63)) & 1ull);
+}
+template <int N> __device__ __forceinline__ uint64_t lword(const uint64_t (&p)[N], int i)
+{
+  return (i < 0 || i >= N) ? 0ull : p[i];
+}
+// bits [k, k + 64)
+template <int N> __device__ __forceinline__ uint64_t lbits64(const uint64_t (&p)[N], int k)
+{
+  const int i = k >= 0 ? (k >> 6) : -((-k + 63) >> 6);
+  const int s = k - 64 * i;
+  const uint64_t lo = lword(p, i), hi = lword(p, i + 1);
+  return s == 0 ? lo : ((lo >> s) | (hi << (64 - s)));
+}
+// any bit in [0, k)
+template <int N> __device__ __forceinline__ bool lany_below(const uint64_t (&p)[N], int k)
+{
+  for (int i = 0; i < N; ++i) {
+    const int lo = 64 * i;
+    if (lo >= k) break;
+    const uint64_t m = (k - lo >= 64) ? ~0ull : ((1ull << (k - lo)) - 1ull);
+    if (p[i] & m) return true;
+  }
+  return false;
+}
+
+// x = m * 2^q (m < 2^53, x > 0 finite): n = round(x * 2/pi) mod 4 and
+// r = x - n*pi/2, rounded once to `prec` bits.  A 256-bit window of 2/pi
+// starting at the first word that can reach the integer part mod 4.
+static __device__ __noinline__ int exact_rem_pio2(uint64_t m, int q, int prec, double* r)
+{
+  const int i0 = q >= 2 ? (q - 2) / 32 : 0;
+  uint64_t nw[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+    nw[3 - j] = ((uint64_t)kTwoOverPi[i0 + 2 * j] << 32) | kTwoOverPi[i0 + 2 * j + 1];
+  uint64_t p[5];
+  uint64_t c = 0;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    uint64_t lo = m * nw[j];
+    uint64_t hi = __umul64hi(m, nw[j]);
+    lo += c;
+    hi += (lo < c) ? 1ull : 0ull;
+    p[j] = lo;
+    c = hi;
+  }
+  p[4] = c;
+  const int sh = 32 * (i0 + 8) - q;          // fraction bits of p (223..301)
+  int n = lbit(p, sh) | (lbit(p, sh + 1) << 1);
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {               // keep the fraction
+    const int lo = 64 * i;
+    p[i] = lo >= sh ? 0ull : ((sh - lo >= 64) ? p[i] : (p[i] & ((1ull << (sh - lo)) - 1ull)));
+  }
+  const bool neg = lbit(p, sh - 1) != 0;
+  if (neg) {                                  // p = 2^sh - p = (-p) mod 2^sh, n = n + 1
+    n += 1;
+    uint64_t cc = 1;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      const int lo = 64 * i;
+      const uint64_t mask = lo >= sh ? 0ull : ((sh - lo >= 64) ? ~0ull : ((1ull << (sh - lo)) - 1ull));
+      const uint64_t v = ~p[i] + cc;
+      cc = (cc != 0ull && v == 0ull) ? 1ull : 0ull;
+      p[i] = v & mask;
+    }
+  }
+  int top = -1;
+  for (int i = 4; i >= 0; --i)
+    if (p[i]) { top = 64 * i + 63 - __clzll((long long)p[i]); break; }
+  if (top < 0) { *r = 0.0; return n & 3; }
+  const uint64_t mh = lbits64(p, top - 63), ml = lbits64(p, top - 127);
+  const bool sticky_f = lany_below(p, top - 127);
+  // Q = M * floor(pi/2 * 2^126)
+  const uint64_t ph = 0x6487ed5110b4611aull, pl = 0x62633145c06e0e68ull;
+  uint64_t Q[4];
+  {
+    const uint64_t a0 = ml * pl, a1 = __umul64hi(ml, pl);
+    const uint64_t b0 = ml * ph, b1 = __umul64hi(ml, ph);
+    const uint64_t c0 = mh * pl, c1 = __umul64hi(mh, pl);
+    const uint64_t d0 = mh * ph, d1 = __umul64hi(mh, ph);
+    Q[0] = a0;
+    uint64_t s1 = a1 + b0;
+    uint64_t k1 = s1 < a1 ? 1ull : 0ull;
+    const uint64_t t1 = s1 + c0;
+    k1 += t1 < s1 ? 1ull : 0ull;
+    Q[1] = t1;
+    uint64_t s2 = b1 + c1;
+    uint64_t k2 = s2 < b1 ? 1ull : 0ull;
+    const uint64_t t2 = s2 + d0;
+    k2 += t2 < s2 ? 1ull : 0ull;
+    const uint64_t u2 = t2 + k1;
+    k2 += u2 < t2 ? 1ull : 0ull;
+    Q[2] = u2;
+    Q[3] = d1 + k2;
+  }
+  const int T = lbit(Q, 254) ? 254 : 253;
+  const uint64_t mant = lbits64(Q, T - 63);
+  const bool sticky = sticky_f || lany_below(Q, T - 63);
+  const int drop = 64 - prec;
+  uint64_t mm = mant >> drop;
+  const uint64_t rem = mant & ((1ull << drop) - 1ull), half = 1ull << (drop - 1);
+  int e = (T - 63) + (top - 253 - sh) + drop;
+  if (rem > half || (rem == half && (sticky || (mm & 1ull)))) ++mm;
+  if (mm >> prec) { mm >>= 1; ++e; }
+  // mm * 2^e, a normal double: |r| lies in [2^-70, pi/4]
+  const int be = e + prec - 1 + 1023;
+  const uint64_t bits = ((uint64_t)be << 52) | ((mm << (53 - prec)) & 0xfffffffffffffull);
+  const double v = __longlong_as_double((long long)bits);
+  *r = neg ? -v : v;
+  return n & 3;
+}
+
+// -------------------------------------------------------------- reductions
+// cvttps2dq / cvttpd2dq: NaN or out of range gives INT32_MIN
+__device__ __forceinline__ int toint32(double a)
+{
+  return (a != a || a >= 2147483648.0 || a < -2147483648.0) ? (int)0x80000000 : (int)a;
+}
+__device__ __forceinline__ long long toint64(double a)
+{
+  return (a != a || a >= 9223372036854775808.0 || a < -9223372036854775808.0) ? (long long)0x8000000000000000ull
+                                                                               : (long long)a;
+}
+
+__device__ __forceinline__ int straight(float x, float& xr)
+{
+  float r = __fsub_rn(x, fbits(tf::pio2_1));
+  r = __fsub_rn(r, fbits(tf::pio2_2));
+  xr = __fsub_rn(r, fbits(tf::pio2_3));
+  return 1;
+}
+__device__ __forceinline__ int straight(double x, double& xr)
+{
+  double r = __dsub_rn(x, dbits(td::pio2_1));
+  r = __dsub_rn(r, dbits(td::pio2_2));
+  xr = __dsub_rn(r, dbits(td::pio2_3));
+  return 1;
+}
+__device__ __forceinline__ int cephes(float x, float& xr)
+{
+  const float xi = rintf(__fmul_rn(x, fbits(tf::twoopi)));
+  float r = __fsub_rn(x, __fmul_rn(xi, fbits(tf::pio2_1)));
+  r = __fsub_rn(r, __fmul_rn(xi, fbits(tf::pio2_2)));
+  xr = __fsub_rn(r, __fmul_rn(xi, fbits(tf::pio2_3)));
+  return toint32(xi) & 3;
+}
+__device__ __forceinline__ int cephes(double x, double& xr)
+{
+  const double xi = rint(__dmul_rn(x, dbits(td::twoopi)));
+  double r = __dsub_rn(x, __dmul_rn(xi, dbits(td::pio2_1)));
+  r = __dsub_rn(r, __dmul_rn(xi, dbits(td::pio2_2)));
+  xr = __dsub_rn(r, __dmul_rn(xi, dbits(td::pio2_3)));
+  return (int)(toint64(xi) & 3);
+}
+template <class T, class C> __device__ __forceinline__ int medium_impl(T t, T& xr, T invpio2, T p1, T p2, T p2t, T p3, T p3t)
+{
+  using math::add; using math::sub; using math::mul;
+  const T fn = C::round(mul(t, invpio2));
+  T r = sub(t, mul(fn, p1));
+  T t2 = r, w = mul(fn, p2);
+  r = sub(t2, w);
+  w = sub(mul(fn, p2t), sub(sub(t2, r), w));
+  t2 = r;
+  w = mul(fn, p3);
+  r = sub(t2, w);
+  w = sub(mul(fn, p3t), sub(sub(t2, r), w));
+  xr = sub(r, w);
+  return C::toint(fn) & 3;
+}
+struct cvt_f { __device__ static float round(float a) { return rintf(a); } __device__ static int toint(float a) { return toint32(a); } };
+struct cvt_d { __device__ static double round(double a) { return rint(a); } __device__ static int toint(double a) { return (int)(toint64(a) & 3); } };
+__device__ __forceinline__ int medium(float t, float& xr)
+{
+  return medium_impl<float, cvt_f>(t, xr, fbits(tf::invpio2), fbits(tf::pio2_1), fbits(tf::pio2_2), fbits(tf::pio2_2t),
+                                   fbits(tf::pio2_3), fbits(tf::pio2_3t));
+}
+__device__ __forceinline__ int medium(double t, double& xr)
+{
+  return medium_impl<double, cvt_d>(t, xr, dbits(td::invpio2), dbits(td::pio2_1), dbits(td::pio2_2), dbits(td::pio2_2t),
+                                    dbits(td::pio2_3), dbits(td::pio2_3t));
+}
+
+// fdlibm __ieee754_rem_pio2f for x >= 0 (functions/scalar/rem_pio2.hpp:148-231)
+static __device__ __noinline__ int fdlibm(float x, float* xrp)
+{
+  const uint32_t ix = __float_as_uint(x) & 0x7fffffffu;
+  float xr;
+  int n;
+  if (ix <= 0x3f490fd8u) {
+    xr = x; n = 0;
+  } else if (ix < 0x4016cbe4u) {
+    float z = __fsub_rn(x, fbits(tf::pio2_1));
+    if ((ix & 0xfffffff0u) != 0x3fc90fd0u) {
+      xr = __fsub_rn(z, fbits(tf::pio2_1t));
+    } else {
+      z = __fsub_rn(z, fbits(tf::pio2_2));
+      xr = __fsub_rn(z, fbits(tf::pio2_2t));
+    }
+    n = 1;
+  } else if (ix <= 0x43490f80u) {
+    const int ni = (int)__fadd_rn(__fmul_rn(x, fbits(tf::invpio2)), 0.5f);
+    const float fn = (float)ni;
+    float r = __fsub_rn(x, __fmul_rn(fn, fbits(tf::pio2_1)));
+    float w = __fmul_rn(fn, fbits(tf::pio2_1t));
+    float y0 = __fsub_rn(r, w);
+    if (!(ni < 32 && (ix & 0xffffff00u) != kNpio2F[ni - 1])) {
+      const int j = (int)(ix >> 23);
+      int i = j - (int)((__float_as_uint(y0) >> 23) & 0xffu);
+      if (i > 8) {
+        float t = r;
+        w = __fmul_rn(fn, fbits(tf::pio2_2));
+        r = __fsub_rn(t, w);
+        w = __fsub_rn(__fmul_rn(fn, fbits(tf::pio2_2t)), __fsub_rn(__fsub_rn(t, r), w));
+        y0 = __fsub_rn(r, w);
+        i = j - (int)((__float_as_uint(y0) >> 23) & 0xffu);
+        if (i > 25) {
+          t = r;
+          w = __fmul_rn(fn, fbits(tf::pio2_3));
+          r = __fsub_rn(t, w);
+          w = __fsub_rn(__fmul_rn(fn, fbits(tf::pio2_3t)), __fsub_rn(__fsub_rn(t, r), w));
+          y0 = __fsub_rn(r, w);
+        }
+      }
+    }
+    xr = y0;
+    n = ni & 3;
+  } else if (ix >= 0x7f800000u) {
+    xr = __fsub_rn(x, x); n = 0;
+  } else {
+    double rd;
+    n = exact_rem_pio2((uint64_t)((ix & 0x7fffffu) | 0x800000u), (int)(ix >> 23) - 150, 24, &rd);
+    xr = (float)rd;
+  }
+  *xrp = xr;
+  return n;
+}
+
+// NT2's double rem_pio2 (functions/scalar/rem_pio2.hpp:413-427) over fdlibm
+// __ieee754_rem_pio2 for x >= 0 (:536-621)
+static __device__ __noinline__ int fdlibm(double x, double* xrp)
+{
+  const uint64_t b = (uint64_t)__double_as_longlong(x);
+  const uint32_t ix = (uint32_t)(b >> 32) & 0x7fffffffu;
+  double xr;
+  int n;
+  if (b == 0x7ff0000000000000ull) {
+    xr = __longlong_as_double(0x7ff8000000000000ll); n = 0;
+  } else if (ix <= 0x3fe921fbu) {
+    xr = x; n = 0;
+  } else if (ix < 0x4002d97cu) {
+    double z = __dsub_rn(x, dbits(td::pio2_1));
+    if (ix != 0x3ff921fbu) {
+      xr = __dsub_rn(z, dbits(td::pio2_1t));
+    } else {
+      z = __dsub_rn(z, dbits(td::pio2_2));
+      xr = __dsub_rn(z, dbits(td::pio2_2t));
+    }
+    n = 1;
+  } else if (ix <= 0x413921fbu) {
+    const int ni = (int)__dadd_rn(__dmul_rn(x, dbits(td::invpio2)), 0.5);
+    const double fn = (double)ni;
+    double r = __dsub_rn(x, __dmul_rn(fn, dbits(td::pio2_1)));
+    double w = __dmul_rn(fn, dbits(td::pio2_1t));
+    double y0 = __dsub_rn(r, w);
+    if (!(ni < 32 && ni > 0 && ix != kNpio2D[ni - 1])) {
+      const int j = (int)(ix >> 20);
+      int i = j - (int)(((uint64_t)__double_as_longlong(y0) >> 52) & 0x7ffu);
+      if (i > 16) {
+        double t = r;
+        w = __dmul_rn(fn, dbits(td::pio2_2));
+        r = __dsub_rn(t, w);
+        w = __dsub_rn(__dmul_rn(fn, dbits(td::pio2_2t)), __dsub_rn(__dsub_rn(t, r), w));
+        y0 = __dsub_rn(r, w);
+        i = j - (int)(((uint64_t)__double_as_longlong(y0) >> 52) & 0x7ffu);
+        if (i > 49) {
+          t = r;
+          w = __dmul_rn(fn, dbits(td::pio2_3));
+          r = __dsub_rn(t, w);
+          w = __dsub_rn(__dmul_rn(fn, dbits(td::pio2_3t)), __dsub_rn(__dsub_rn(t, r), w));
+          y0 = __dsub_rn(r, w);
+        }
+      }
+    }
+    xr = y0;
+    n = ni & 3;
+  } else if (ix >= 0x7ff00000u) {
+    xr = __dsub_rn(x, x); n = 0;
+  } else {
+    n = exact_rem_pio2((b & 0xfffffffffffffull) | (1ull << 52), (int)((b >> 52) & 0x7ffu) - 1075, 53, &xr);
+  }
+  *xrp = xr;
+  return n;
+}
+
+// Level of a lane: how many thresholds |x| exceeds (NaN: 0).
+__device__ __forceinline__ int level(float x)
+{
+  return (x > fbits(tf::pio4)) + (x > fbits(tf::pio2)) + (x > fbits(tf::p20pi)) + (x > fbits(tf::medpi)) +
+         (x > fbits(tf::dmpi));
+}
+__device__ __forceinline__ int level(double x)
+{
+  return (x > dbits(td::pio4)) + (x > dbits(td::pio2)) + (x > dbits(td::p20pi)) + (x > dbits(td::medpi));
+}
+
+// The double chain over one pack of P lanes.
+template <int P> __device__ __forceinline__ void reduce_pack(const double (&x)[P], double (&xr)[P], int (&n)[P])
+{
+  int lv = 0;
+#pragma unroll
+  for (int l = 0; l < P; ++l) lv = max(lv, level(x[l]));
+  if (lv == 0) {
+#pragma unroll
+    for (int l = 0; l < P; ++l) { xr[l] = x[l]; n[l] = 0; }
+  } else if (lv == 1) {
+#pragma unroll
+    for (int l = 0; l < P; ++l) n[l] = straight(x[l], xr[l]);
+  } else if (lv == 2) {
+#pragma unroll
+    for (int l = 0; l < P; ++l) n[l] = cephes(x[l], xr[l]);
+  } else if (lv == 3) {
+#pragma unroll
+    for (int l = 0; l < P; ++l) n[l] = medium(x[l], xr[l]);
+  } else {
+#pragma unroll
+    for (int l = 0; l < P; ++l) n[l] = fdlibm(x[l], &xr[l]);
+  }
+}
+
+// The float chain over one pack of P lanes.
+template <int P> __device__ __forceinline__ void reduce_pack(const float (&x)[P], float (&xr)[P], int (&n)[P])
+{
+  int lv = 0;
+#pragma unroll
+  for (int l = 0; l < P; ++l) lv = max(lv, level(x[l]));
+  if (lv == 0) {
+#pragma unroll
+    for (int l = 0; l < P; ++l) { xr[l] = x[l]; n[l] = 0; }
+  } else if (lv == 1) {
+#pragma unroll
+    for (int l = 0; l < P; ++l) n[l] = straight(x[l], xr[l]);
+  } else if (lv == 2) {
+#pragma unroll
+    for (int l = 0; l < P; ++l) n[l] = cephes(x[l], xr[l]);
+  } else if (lv == 3) {
+#pragma unroll
+    for (int l = 0; l < P; ++l) n[l] = medium(x[l], xr[l]);
+  } else if (lv == 4) {
+    // halves of the pack through the double chain
+    constexpr int H = P > 1 ? P / 2 : 1;
+#pragma unroll
+    for (int s = 0; s < P; s += H) {
+      double xd[H], rd[H];
+      int nd[H];
+#pragma unroll
+      for (int l = 0; l < H; ++l) xd[l] = (double)x[s + l];
+      reduce_pack<H>(xd, rd, nd);
+#pragma unroll
+      for (int l = 0; l < H; ++l) { xr[s + l] = (float)rd[l]; n[s + l] = nd[l]; }
+    }
+  } else {
+#pragma unroll
+    for (int l = 0; l < P; ++l) n[l] = fdlibm(x[l], &xr[l]);
+  }
+}
+
+// pi_tag reduction (trig_reduction.hpp:216-229): xi = round2even(2x),
+// xr = (x - xi/2) * pi, n = fast_toint(xi).
+__device__ __forceinline__ int reduce_pi(float x, float& xr, bool)
+{
+  const float xi = rintf(__fmul_rn(x, 2.0f));
+  xr = __fmul_rn(__fsub_rn(x, __fmul_rn(xi, 0.5f)), fbits(tf::pi));
+  return toint32(xi) & 3;
+}
+__device__ __forceinline__ int reduce_pi(double x, double& xr, bool simd)
+{
+  const double xi = rint(__dmul_rn(x, 2.0));
+  xr = __dmul_rn(__dsub_rn(x, __dmul_rn(xi, 0.5)), dbits(td::pi));
+  // SSE2 converts packed doubles through int32 (cvttpd2dq); scalar code casts to int64
+  return simd ? (toint32(xi) & 3) : (int)(toint64(xi) & 3);
+}
+
+// ------------------------------------------------------------- evaluation
+// functions/simd/common/impl/trigo/f_trig_evaluation.hpp:25-56
+template <bool F> __device__ __forceinline__ float cos_eval(float z)
+{
+  constexpr uint32_t C[3] = {0x37ccf5ceu, 0xbab60619u, 0x3d2aaaa5u};
+  const float y = math::horner<F>(z, C);
+  return __fadd_rn(1.0f, math::madd<F>(z, -0.5f, __fmul_rn(y, __fmul_rn(z, z))));
+}
+template <bool F> __device__ __forceinline__ float sin_eval(float z, float x)
+{
+  constexpr uint32_t C[3] = {0xb94ca1f9u, 0x3c08839du, 0xbe2aaaa2u};
+  return math::madd<F>(__fmul_rn(math::horner<F>(z, C), z), x, x);
+}
+template <bool F> __device__ __forceinline__ float tan_eval(float x)
+{
+  constexpr uint32_t C[6] = {0x3c19c53bu, 0x3b4c779cu, 0x3cc821b5u, 0x3d5ac5c9u, 0x3e0896ddu, 0x3eaaaa6fu};
+  const float zz = __fmul_rn(x, x);
+  return math::madd<F>(__fmul_rn(math::horner<F>(zz, C), zz), x, x);
+}
+// functions/simd/common/impl/trigo/d_trig_evaluation.hpp:25-66
+template <bool F> __device__ __forceinline__ double cos_eval(double z)
+{
+  constexpr uint64_t C[7] = {0x3da8ff831ad9b219ull, 0xbe21eea7c1e514d4ull, 0x3e927e4f8e06d9a5ull,
+                             0xbefa01a019ddbcd9ull, 0x3f56c16c16c15d47ull, 0xbfa5555555555551ull,
+                             0x3fe0000000000000ull};
+  return math::nmsub<F>(math::horner<F>(z, C), z, 1.0);
+}
+template <bool F> __device__ __forceinline__ double sin_eval(double z, double x)
+{
+  constexpr uint64_t C[6] = {0x3de5d8fd1fcf0ec1ull, 0xbe5ae5e5a9291691ull, 0x3ec71de3567d4896ull,
+                             0xbf2a01a019bfdf03ull, 0x3f8111111110f7d0ull, 0xbfc5555555555548ull};
+  return math::madd<F>(__dmul_rn(math::horner<F>(z, C), z), x, x);
+}
+template <bool F> __device__ __forceinline__ double tan_eval(double x)
+{
+  constexpr uint64_t N[3] = {0xc0c992d8d24f3f38ull, 0x413199eca5fc9dddull, 0xc1711fead3299176ull};
+  constexpr uint64_t D[5] = {0x3ff0000000000000ull, 0x40cab8a5eeb36572ull, 0xc13427bc582abc96ull,
+                             0x4177d98fc2ead8efull, 0xc189afe03cbe5a31ull};
+  const double zz = __dmul_rn(x, x);
+  const double q = __ddiv_rn(math::horner<F>(zz, N), math::horner<F>(zz, D));
+  return math::madd<F>(x, __dmul_rn(zz, q), x);
+}
+
+__device__ __forceinline__ float flip(float v, uint32_t s) { return __uint_as_float(__float_as_uint(v) ^ s); }
+__device__ __forceinline__ double flip(double v, uint64_t s)
+{
+  return __longlong_as_double((long long)((uint64_t)__double_as_longlong(v) ^ s));
+}
+__device__ __forceinline__ uint32_t sign_of(float a) { return __float_as_uint(a) & 0x80000000u; }
+__device__ __forceinline__ uint64_t sign_of(double a) { return (uint64_t)__double_as_longlong(a) & 0x8000000000000000ull; }
+template <class T> struct bits_of;
+template <> struct bits_of<float> { using type = uint32_t; static constexpr int top = 31; };
+template <> struct bits_of<double> { using type = uint64_t; static constexpr int top = 63; };
+
+// trig_base sina / cosa / tana (functions/simd/common/impl/trigo/trig_base.hpp:49-92)
+template <int K, bool F, class T> __device__ __forceinline__ T finish(T a0, T xr, int n)
+{
+  using U = typename bits_of<T>::type;
+  constexpr int top = bits_of<T>::top;
+  if constexpr (K == TAN) {
+    T y = tan_eval<F>(xr);
+    if (n & 1) y = -math::div(T(1), y);
+    return flip(y, sign_of(a0));
+  } else {
+    const T z = math::mul(xr, xr);
+    if constexpr (K == SIN || K == SINPI) {
+      const T v = (n & 1) ? cos_eval<F>(z) : sin_eval<F>(z, xr);
+      return flip(v, sign_of(a0) ^ ((U)(n & 2) << (top - 1)));
+    } else {
+      const T v = (n & 1) ? sin_eval<F>(z, xr) : cos_eval<F>(z);
+      return flip(v, (U)((n ^ (n >> 1)) & 1) << top);
+    }
+  }
+}
+
+// y[l] = f(a[l]) for one pack of P lanes.
+template <int K, bool F, int P, class T> __device__ __forceinline__ void pack(const T (&a)[P], T (&y)[P])
+{
+  T x[P], xr[P];
+  int n[P];
+#pragma unroll
+  for (int l = 0; l < P; ++l) x[l] = fabs(a[l]);
+  if constexpr (K == SINPI || K == COSPI) {
+#pragma unroll
+    for (int l = 0; l < P; ++l) n[l] = reduce_pi(x[l], xr[l], P > 1);
+  } else {
+    reduce_pack<P>(x, xr, n);
+  }
+#pragma unroll
+  for (int l = 0; l < P; ++l) y[l] = finish<K, F>(a[l], xr[l], n[l]);
+}
+
+// One element, NT2's scalar code (a pack of one).
+template <int K, bool F, class T> __device__ __forceinline__ T one(T a)
+{
+  T in[1] = {a}, out[1];
+  pack<K, F, 1>(in, out);
+  return out[0];
+}
+
+}  // namespace trig
+}  // namespace nt2cuda

@@ -16,7 +16,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_build")
-SRC = os.path.join(HERE, "nt2_oracle.c")
+SRCS = [os.path.join(HERE, "nt2_oracle.c"), os.path.join(HERE, "nt2_oracle_trig.c")]
 
 VARIANTS = {
     "libnt2oracle.so": ["-O2", "-fno-tree-vectorize"],
@@ -31,10 +31,10 @@ def build(verbose: bool = False) -> dict[str, str]:
     for name, opt in VARIANTS.items():
         lib = os.path.join(OUT, name)
         out[name] = lib
-        if os.path.exists(lib) and os.path.getmtime(lib) > os.path.getmtime(SRC):
+        if os.path.exists(lib) and all(os.path.getmtime(lib) > os.path.getmtime(src) for src in SRCS):
             continue
         cmd = [cc, *opt, "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC",
-               "-shared", SRC, "-o", lib, "-lm"]
+               "-shared", *SRCS, "-o", lib, "-lm"]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

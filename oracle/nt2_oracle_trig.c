@@ -1,0 +1,572 @@
+/*
+ * nt2_oracle_trig.c -- CPU restatement of NT2's sine, cosine and tangent
+ * (sin, cos, tan in radians; sinpi, cospi) for float and double.
+ *
+ * TEST INFRASTRUCTURE ONLY, like nt2_oracle.c: the parity checker of the
+ * CUDA evaluator, never called by the product path.
+ *
+ * Paths are relative to NT2's modules/core/trigonometric/include/nt2/trigonometric/.
+ *
+ * NT2 evaluates a transform in packs of N lanes from the start of the range
+ * and finishes the last n % N elements one at a time
+ * (modules/core/base/include/nt2/core/functions/simd/transform.hpp:40-48).
+ * Its radian reduction picks ONE method for a whole pack from the pack's
+ * largest |x| (functions/scalar/impl/trigo/trig_reduction.hpp:46-160; the
+ * `big_` mode of functions/scalar/impl/selection_tags.hpp:55-61):
+ *   level 0  all |x| <= pi/4        no reduction
+ *   level 1  all |x| <= pi/2        rem_pio2_straight (functions/generic/rem_pio2_straight.hpp)
+ *   level 2  all |x| <= 20 pi       rem_pio2_cephes   (functions/generic/rem_pio2_cephes.hpp)
+ *   level 3  all |x| <= Medium_pi   rem_pio2_medium   (functions/generic/rem_pio2_medium.hpp);
+ *                                   Medium_pi is 2^6 pi for float, 2^18 pi for double
+ *   level 4  float, all |x| <= 2^18 pi: each half of the pack is converted to
+ *            double and reduced by the double chain (trig_reduction.hpp:161-183)
+ *   level 5  rem_pio2 lane by lane (functions/scalar/rem_pio2.hpp: fdlibm's
+ *            __ieee754_rem_pio2f :83-232 and __ieee754_rem_pio2 :484-622)
+ * so a lane's result depends on the other lanes of its pack.  `pack` below
+ * is N (1 = NT2's scalar code, 4 floats / 2 doubles = 128-bit SIMD).
+ *
+ * Lanes that reach fdlibm's __kernel_rem_pio2f / __kernel_rem_pio2 (float
+ * |x| > 2^7 pi/2 at level 5, double |x| > 2^19 pi/2) are reduced here by an
+ * exact Payne-Hanek reduction (224 bits of 2/pi, one rounding).  fdlibm's
+ * kernels sum their partial products in float/double and may differ in the
+ * last bit of the reduced argument: parity for those lanes is unpinned to
+ * that bit.  Everything else follows NT2 operation by operation; the
+ * polynomials are functions/simd/common/impl/trigo/{f,d}_trig_evaluation.hpp
+ * with NT2's unfused fma (the file is built with -ffp-contract=off).
+ */
+#include <math.h>
+#include <stddef.h>
+#include <stdint.h>
+#include <string.h>
+
+#define EXPORT __attribute__((visibility("default")))
+
+static inline float tfb(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
+static inline uint32_t tbf(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
+static inline double tdb(uint64_t u) { double d; memcpy(&d, &u, 8); return d; }
+static inline uint64_t tbd(double d) { uint64_t u; memcpy(&u, &d, 8); return u; }
+
+/* ------------------------------------------------------------ constants -- */
+/* Bit patterns of the BOOST_SIMD_CONSTANT_REGISTER lines in constants/*.hpp. */
+#define F_PIO4    0x3f490fdbu
+#define F_PIO2    0x3fc90fdbu
+#define F_20PI    0x427b53d1u
+#define F_MEDPI   0x43490fdbu   /* 2^6 pi */
+#define F_DMPI    0x49490fdbu   /* 2^18 pi */
+#define F_PI      0x40490fdbu
+#define F_TWOOPI  0x3f22f983u
+#define F_INVPIO2 0x3f22f984u
+#define F_PIO2_1  0x3fc90f80u
+#define F_PIO2_2  0x37354400u
+#define F_PIO2_3  0x2e85a300u
+#define F_PIO2_1T 0x37354443u
+#define F_PIO2_2T 0x2e85a308u
+#define F_PIO2_3T 0x248d3132u
+
+#define D_PIO4    0x3fe921fb54442d18ull
+#define D_PIO2    0x3ff921fb54442d18ull
+#define D_20PI    0x404f6a7a2955385eull
+#define D_MEDPI   0x412921fb54442d18ull   /* 2^18 pi */
+#define D_PI      0x400921fb54442d18ull
+#define D_TWOOPI  0x3fe45f306dc9c883ull
+#define D_INVPIO2 0x3fe45f306dc9c883ull
+#define D_PIO2_1  0x3ff921fb54400000ull
+#define D_PIO2_2  0x3dd0b4611a600000ull
+#define D_PIO2_3  0x3ba3198a2e000000ull
+#define D_PIO2_1T 0x3dd0b4611a626331ull
+#define D_PIO2_2T 0x3ba3198a2e037073ull
+#define D_PIO2_3T 0x397b839a252049c1ull
+
+/* High bits of n*pi/2, n = 1..32 (float: bit pattern with the low 8 bits
+ * cleared; double: high word), the "no cancellation" test of fdlibm's
+ * medium branch. */
+static const uint32_t NPIO2_HW_F[32] = {
+  0x3fc90f00u, 0x40490f00u, 0x4096cb00u, 0x40c90f00u, 0x40fb5300u, 0x4116cb00u, 0x412fed00u, 0x41490f00u,
+  0x41623100u, 0x417b5300u, 0x418a3a00u, 0x4196cb00u, 0x41a35c00u, 0x41afed00u, 0x41bc7e00u, 0x41c90f00u,
+  0x41d5a000u, 0x41e23100u, 0x41eec200u, 0x41fb5300u, 0x4203f200u, 0x420a3a00u, 0x42108300u, 0x4216cb00u,
+  0x421d1400u, 0x42235c00u, 0x4229a500u, 0x422fed00u, 0x42363600u, 0x423c7e00u, 0x4242c700u, 0x42490f00u};
+static const uint32_t NPIO2_HW_D[32] = {
+  0x3ff921fbu, 0x400921fbu, 0x4012d97cu, 0x401921fbu, 0x401f6a7au, 0x4022d97cu, 0x4025fdbbu, 0x402921fbu,
+  0x402c463au, 0x402f6a7au, 0x4031475cu, 0x4032d97cu, 0x40346b9cu, 0x4035fdbbu, 0x40378fdbu, 0x403921fbu,
+  0x403ab41bu, 0x403c463au, 0x403dd85au, 0x403f6a7au, 0x40407e4cu, 0x4041475cu, 0x4042106cu, 0x4042d97cu,
+  0x4043a28cu, 0x40446b9cu, 0x404534acu, 0x4045fdbbu, 0x4046c6cbu, 0x40478fdbu, 0x404858ebu, 0x404921fbu};
+
+/* 2/pi: bits after the binary point, 32 per word (1280 bits). */
+static const uint32_t TWO_OVER_PI[40] = {
+  0xa2f9836eu, 0x4e441529u, 0xfc2757d1u, 0xf534ddc0u, 0xdb629599u, 0x3c439041u, 0xfe5163abu, 0xdebbc561u,
+  0xb7246e3au, 0x424dd2e0u, 0x06492eeau, 0x09d1921cu, 0xfe1deb1cu, 0xb129a73eu, 0xe88235f5u, 0x2ebb4484u,
+  0xe99c7026u, 0xb45f7e41u, 0x3991d639u, 0x835339f4u, 0x9c845f8bu, 0xbdf9283bu, 0x1ff897ffu, 0xde05980fu,
+  0xef2f118bu, 0x5a0a6d1fu, 0x6d367ecfu, 0x27cb09b7u, 0x4f463f66u, 0x9e5fea2du, 0x7527bac7u, 0xebe5f17bu,
+  0x3d0739f7u, 0x8a5292eau, 0x6bfb5fb1u, 0x1f8d5d08u, 0x56033046u, 0xfc7b6babu, 0xf0cfbc20u, 0x9af4361du};
+/* floor(pi/2 * 2^126), little-endian 32-bit limbs. */
+static const uint32_t PIO2_126[4] = {0xc06e0e68u, 0x62633145u, 0x10b4611au, 0x6487ed51u};
+
+/* ------------------------------------------- exact Payne-Hanek reduction -- */
+static inline int wbit(const uint32_t* p, int nw, int k)
+{
+  if (k < 0 || k >= 32 * nw) return 0;
+  return (int)((p[k >> 5] >> (k & 31)) & 1u);
+}
+static uint64_t wbits64(const uint32_t* p, int nw, int k)   /* bits [k, k+64) */
+{
+  uint64_t r = 0;
+  for (int i = 63; i >= 0; --i) r = (r << 1) | (uint64_t)wbit(p, nw, k + i);
+  return r;
+}
+static int wany_below(const uint32_t* p, int nw, int k)      /* any bit in [0, k) */
+{
+  for (int i = 0; i < k && i < 32 * nw; ++i)
+    if (wbit(p, nw, i)) return 1;
+  return 0;
+}
+
+/* x = m * 2^q (m < 2^53, x > 0 finite).  n = round(x * 2/pi) mod 4 and
+ * r = x - n*pi/2 rounded once to `prec` bits. */
+static int exact_rem_pio2(uint64_t m, int q, int prec, double* r)
+{
+  enum { K = 7 };
+  const int i0 = q >= 2 ? (q - 2) / 32 : 0;   /* earlier words only add multiples of 4 */
+  uint32_t nw[K], p[K + 2];
+  memset(p, 0, sizeof p);
+  for (int b = 0; b < K; ++b) nw[b] = TWO_OVER_PI[i0 + K - 1 - b];
+  const uint32_t ma[2] = {(uint32_t)m, (uint32_t)(m >> 32)};
+  for (int a = 0; a < 2; ++a) {
+    uint64_t c = 0;
+    for (int b = 0; b < K; ++b) {
+      uint64_t t = (uint64_t)ma[a] * nw[b] + p[a + b] + c;
+      p[a + b] = (uint32_t)t;
+      c = t >> 32;
+    }
+    p[a + K] = (uint32_t)c;
+  }
+  const int sh = 32 * (i0 + K) - q;           /* fraction bits of p */
+  int n = wbit(p, K + 2, sh) | (wbit(p, K + 2, sh + 1) << 1);
+  uint32_t f[K + 2];
+  for (int k = 0; k < K + 2; ++k) {
+    const int lo = 32 * k;
+    f[k] = lo >= sh ? 0u : (lo + 32 > sh ? (p[k] & ((1u << (sh - lo)) - 1u)) : p[k]);
+  }
+  const int neg = wbit(f, K + 2, sh - 1);
+  if (neg) {                                   /* f = 2^sh - f, n = n + 1 */
+    n += 1;
+    uint64_t c = 1;
+    for (int k = 0; k < K + 2; ++k) {
+      const int lo = 32 * k;
+      const uint32_t mask = lo >= sh ? 0u : (lo + 32 > sh ? ((1u << (sh - lo)) - 1u) : 0xffffffffu);
+      uint64_t t = (uint64_t)(~f[k] & mask) + c;
+      f[k] = (uint32_t)t & mask;
+      c = t >> 32;
+    }
+  }
+  int top = -1;
+  for (int k = 32 * (K + 2) - 1; k >= 0; --k)
+    if (wbit(f, K + 2, k)) { top = k; break; }
+  if (top < 0) { *r = 0.0; return n & 3; }
+  uint32_t M[4];
+  for (int j = 0; j < 4; ++j) M[j] = (uint32_t)wbits64(f, K + 2, top - 127 + 32 * j);
+  const int sticky_f = wany_below(f, K + 2, top - 127);
+  uint32_t Q[8];
+  memset(Q, 0, sizeof Q);
+  for (int a = 0; a < 4; ++a) {
+    uint64_t c = 0;
+    for (int b = 0; b < 4; ++b) {
+      uint64_t t = (uint64_t)M[a] * PIO2_126[b] + Q[a + b] + c;
+      Q[a + b] = (uint32_t)t;
+      c = t >> 32;
+    }
+    Q[a + 4] = (uint32_t)c;
+  }
+  /* |r| = Q * 2^(top - 127 - sh - 126) */
+  const int T = wbit(Q, 8, 254) ? 254 : 253;
+  const uint64_t mant = wbits64(Q, 8, T - 63);
+  const int sticky = sticky_f || wany_below(Q, 8, T - 63);
+  const int drop = 64 - prec;
+  uint64_t mm = mant >> drop;
+  const uint64_t rem = mant & ((1ull << drop) - 1u), half = 1ull << (drop - 1);
+  int e = (T - 63) + (top - 253 - sh) + drop;
+  if (rem > half || (rem == half && (sticky || (mm & 1u)))) ++mm;
+  if (mm >> prec) { mm >>= 1; ++e; }
+  const double v = ldexp((double)mm, e);
+  *r = neg ? -v : v;
+  return n & 3;
+}
+
+/* ------------------------------------------------- float reductions ------ */
+static inline float r2e_tf(float a) { return rintf(a); }
+static inline double r2e_td(double a) { return rint(a); }
+/* cvttps2dq / cvttpd2dq: out of range or NaN gives INT32_MIN */
+static inline int32_t toint32(double a)
+{
+  return (a != a || a >= 2147483648.0 || a < -2147483648.0) ? INT32_MIN : (int32_t)a;
+}
+static inline int64_t toint64(double a)
+{
+  return (a != a || a >= 9223372036854775808.0 || a < -9223372036854775808.0) ? INT64_MIN : (int64_t)a;
+}
+
+static int straight_f(float x, float* xr)
+{
+  float r = x - tfb(F_PIO2_1);
+  r -= tfb(F_PIO2_2);
+  r -= tfb(F_PIO2_3);
+  *xr = r;
+  return 1;
+}
+static int cephes_f(float x, float* xr)
+{
+  const float xi = r2e_tf(x * tfb(F_TWOOPI));
+  float r = x - xi * tfb(F_PIO2_1);
+  r -= xi * tfb(F_PIO2_2);
+  r -= xi * tfb(F_PIO2_3);
+  *xr = r;
+  return toint32(xi) & 3;
+}
+static int medium_f(float t, float* xr)
+{
+  const float fn = r2e_tf(t * tfb(F_INVPIO2));
+  float r = t - fn * tfb(F_PIO2_1);
+  float t2 = r, w = fn * tfb(F_PIO2_2);
+  r = t2 - w;
+  w = fn * tfb(F_PIO2_2T) - ((t2 - r) - w);
+  t2 = r;
+  w = fn * tfb(F_PIO2_3);
+  r = t2 - w;
+  w = fn * tfb(F_PIO2_3T) - ((t2 - r) - w);
+  *xr = r - w;
+  return toint32(fn) & 3;
+}
+/* fdlibm __ieee754_rem_pio2f for x >= 0 (scalar/rem_pio2.hpp:148-231) */
+static int fdlibm_f(float x, float* xr)
+{
+  const uint32_t ix = tbf(x) & 0x7fffffffu;
+  if (ix <= 0x3f490fd8u) { *xr = x; return 0; }
+  if (ix < 0x4016cbe4u) {
+    float z = x - tfb(F_PIO2_1);
+    if ((ix & 0xfffffff0u) != 0x3fc90fd0u) *xr = z - tfb(F_PIO2_1T);
+    else { z -= tfb(F_PIO2_2); *xr = z - tfb(F_PIO2_2T); }
+    return 1;
+  }
+  if (ix <= 0x43490f80u) {
+    const int32_t n = (int32_t)(x * tfb(F_INVPIO2) + 0.5f);
+    const float fn = (float)n;
+    float r = x - fn * tfb(F_PIO2_1), w = fn * tfb(F_PIO2_1T), y0;
+    if (n < 32 && (ix & 0xffffff00u) != NPIO2_HW_F[n - 1]) {
+      y0 = r - w;
+    } else {
+      const int j = (int)(ix >> 23);
+      y0 = r - w;
+      int i = j - (int)((tbf(y0) >> 23) & 0xffu);
+      if (i > 8) {
+        float t = r;
+        w = fn * tfb(F_PIO2_2);
+        r = t - w;
+        w = fn * tfb(F_PIO2_2T) - ((t - r) - w);
+        y0 = r - w;
+        i = j - (int)((tbf(y0) >> 23) & 0xffu);
+        if (i > 25) {
+          t = r;
+          w = fn * tfb(F_PIO2_3);
+          r = t - w;
+          w = fn * tfb(F_PIO2_3T) - ((t - r) - w);
+          y0 = r - w;
+        }
+      }
+    }
+    *xr = y0;
+    return n & 3;
+  }
+  if (ix >= 0x7f800000u) { *xr = x - x; return 0; }
+  double r;
+  const int n = exact_rem_pio2((uint64_t)((ix & 0x7fffffu) | 0x800000u), (int)(ix >> 23) - 150, 24, &r);
+  *xr = (float)r;
+  return n;
+}
+
+/* ------------------------------------------------ double reductions ------ */
+static int straight_d(double x, double* xr)
+{
+  double r = x - tdb(D_PIO2_1);
+  r -= tdb(D_PIO2_2);
+  r -= tdb(D_PIO2_3);
+  *xr = r;
+  return 1;
+}
+static int cephes_d(double x, double* xr)
+{
+  const double xi = r2e_td(x * tdb(D_TWOOPI));
+  double r = x - xi * tdb(D_PIO2_1);
+  r -= xi * tdb(D_PIO2_2);
+  r -= xi * tdb(D_PIO2_3);
+  *xr = r;
+  return (int)(toint64(xi) & 3);
+}
+static int medium_d(double t, double* xr)
+{
+  const double fn = r2e_td(t * tdb(D_INVPIO2));
+  double r = t - fn * tdb(D_PIO2_1);
+  double t2 = r, w = fn * tdb(D_PIO2_2);
+  r = t2 - w;
+  w = fn * tdb(D_PIO2_2T) - ((t2 - r) - w);
+  t2 = r;
+  w = fn * tdb(D_PIO2_3);
+  r = t2 - w;
+  w = fn * tdb(D_PIO2_3T) - ((t2 - r) - w);
+  *xr = r - w;
+  return (int)(toint64(fn) & 3);
+}
+/* NT2's double rem_pio2 (scalar/rem_pio2.hpp:413-427) over fdlibm
+ * __ieee754_rem_pio2 for x >= 0 (:536-621) */
+static int fdlibm_d(double x, double* xr)
+{
+  if (x == INFINITY) { *xr = NAN; return 0; }
+  const uint32_t ix = (uint32_t)(tbd(x) >> 32) & 0x7fffffffu;
+  if (ix <= 0x3fe921fbu) { *xr = x; return 0; }
+  if (ix < 0x4002d97cu) {
+    double z = x - tdb(D_PIO2_1);
+    if (ix != 0x3ff921fbu) *xr = z - tdb(D_PIO2_1T);
+    else { z -= tdb(D_PIO2_2); *xr = z - tdb(D_PIO2_2T); }
+    return 1;
+  }
+  if (ix <= 0x413921fbu) {
+    const int32_t n = (int32_t)(x * tdb(D_INVPIO2) + 0.5);
+    const double fn = (double)n;
+    double r = x - fn * tdb(D_PIO2_1), w = fn * tdb(D_PIO2_1T), y0;
+    if (n < 32 && n > 0 && ix != NPIO2_HW_D[n - 1]) {
+      y0 = r - w;
+    } else {
+      const int j = (int)(ix >> 20);
+      y0 = r - w;
+      int i = j - (int)((tbd(y0) >> 52) & 0x7ffu);
+      if (i > 16) {
+        double t = r;
+        w = fn * tdb(D_PIO2_2);
+        r = t - w;
+        w = fn * tdb(D_PIO2_2T) - ((t - r) - w);
+        y0 = r - w;
+        i = j - (int)((tbd(y0) >> 52) & 0x7ffu);
+        if (i > 49) {
+          t = r;
+          w = fn * tdb(D_PIO2_3);
+          r = t - w;
+          w = fn * tdb(D_PIO2_3T) - ((t - r) - w);
+          y0 = r - w;
+        }
+      }
+    }
+    *xr = y0;
+    return n & 3;
+  }
+  if (ix >= 0x7ff00000u) { *xr = x - x; return 0; }
+  const uint64_t b = tbd(x);
+  return exact_rem_pio2((b & 0xfffffffffffffull) | (1ull << 52), (int)((b >> 52) & 0x7ffu) - 1075, 53, xr);
+}
+
+/* Level of one lane (number of thresholds |x| exceeds; NaN is level 0). */
+static inline int level_f(float x)
+{
+  return (x > tfb(F_PIO4)) + (x > tfb(F_PIO2)) + (x > tfb(F_20PI)) + (x > tfb(F_MEDPI)) + (x > tfb(F_DMPI));
+}
+static inline int level_d(double x)
+{
+  return (x > tdb(D_PIO4)) + (x > tdb(D_PIO2)) + (x > tdb(D_20PI)) + (x > tdb(D_MEDPI));
+}
+
+/* The double chain over lanes x[0..k) (one SIMD pack of doubles). */
+static void reduce_pack_d(const double* x, int k, double* xr, int* n)
+{
+  int lv = 0;
+  for (int l = 0; l < k; ++l) { const int v = level_d(x[l]); lv = v > lv ? v : lv; }
+  for (int l = 0; l < k; ++l) {
+    switch (lv) {
+      case 0: xr[l] = x[l]; n[l] = 0; break;
+      case 1: n[l] = straight_d(x[l], &xr[l]); break;
+      case 2: n[l] = cephes_d(x[l], &xr[l]); break;
+      case 3: n[l] = medium_d(x[l], &xr[l]); break;
+      default: n[l] = fdlibm_d(x[l], &xr[l]); break;
+    }
+  }
+}
+
+/* The float chain over one pack of k lanes. */
+static void reduce_pack_f(const float* x, int k, float* xr, int* n)
+{
+  int lv = 0;
+  for (int l = 0; l < k; ++l) { const int v = level_f(x[l]); lv = v > lv ? v : lv; }
+  if (lv == 4) {                     /* halves of the pack through the double chain */
+    const int h = k > 1 ? k / 2 : 1;
+    for (int s = 0; s < k; s += h) {
+      double xd[8], rd[8];
+      for (int l = 0; l < h; ++l) xd[l] = (double)x[s + l];
+      reduce_pack_d(xd, h, rd, n + s);
+      for (int l = 0; l < h; ++l) xr[s + l] = (float)rd[l];
+    }
+    return;
+  }
+  for (int l = 0; l < k; ++l) {
+    switch (lv) {
+      case 0: xr[l] = x[l]; n[l] = 0; break;
+      case 1: n[l] = straight_f(x[l], &xr[l]); break;
+      case 2: n[l] = cephes_f(x[l], &xr[l]); break;
+      case 3: n[l] = medium_f(x[l], &xr[l]); break;
+      default: n[l] = fdlibm_f(x[l], &xr[l]); break;
+    }
+  }
+}
+
+/* --------------------------------------------------------- evaluation ---- */
+/* simd/common/impl/trigo/f_trig_evaluation.hpp:25-56 */
+static inline float hornerf(float x, const uint32_t* c, int k)
+{
+  float a = tfb(c[0]);
+  for (int i = 1; i < k; ++i) a = x * a + tfb(c[i]);
+  return a;
+}
+static inline double hornerd(double x, const uint64_t* c, int k)
+{
+  double a = tdb(c[0]);
+  for (int i = 1; i < k; ++i) a = x * a + tdb(c[i]);
+  return a;
+}
+static const uint32_t COS_F[3] = {0x37ccf5ceu, 0xbab60619u, 0x3d2aaaa5u};
+static const uint32_t SIN_F[3] = {0xb94ca1f9u, 0x3c08839du, 0xbe2aaaa2u};
+static const uint32_t TAN_F[6] = {0x3c19c53bu, 0x3b4c779cu, 0x3cc821b5u, 0x3d5ac5c9u, 0x3e0896ddu, 0x3eaaaa6fu};
+static const uint64_t COS_D[7] = {0x3da8ff831ad9b219ull, 0xbe21eea7c1e514d4ull, 0x3e927e4f8e06d9a5ull,
+                                  0xbefa01a019ddbcd9ull, 0x3f56c16c16c15d47ull, 0xbfa5555555555551ull,
+                                  0x3fe0000000000000ull};
+static const uint64_t SIN_D[6] = {0x3de5d8fd1fcf0ec1ull, 0xbe5ae5e5a9291691ull, 0x3ec71de3567d4896ull,
+                                  0xbf2a01a019bfdf03ull, 0x3f8111111110f7d0ull, 0xbfc5555555555548ull};
+static const uint64_t TAN_DN[3] = {0xc0c992d8d24f3f38ull, 0x413199eca5fc9dddull, 0xc1711fead3299176ull};
+static const uint64_t TAN_DD[5] = {0x3ff0000000000000ull, 0x40cab8a5eeb36572ull, 0xc13427bc582abc96ull,
+                                   0x4177d98fc2ead8efull, 0xc189afe03cbe5a31ull};
+
+static inline float cos_eval_f(float z)
+{
+  const float y = hornerf(z, COS_F, 3);
+  return 1.0f + (z * -0.5f + y * (z * z));
+}
+static inline float sin_eval_f(float z, float x) { return (hornerf(z, SIN_F, 3) * z) * x + x; }
+static inline float tan_eval_f(float x)
+{
+  const float zz = x * x;
+  return (hornerf(zz, TAN_F, 6) * zz) * x + x;
+}
+static inline double cos_eval_d(double z) { return 1.0 - hornerd(z, COS_D, 7) * z; }
+static inline double sin_eval_d(double z, double x) { return (hornerd(z, SIN_D, 6) * z) * x + x; }
+static inline double tan_eval_d(double x)
+{
+  const double zz = x * x;
+  return x + x * (zz * (hornerd(zz, TAN_DN, 3) / hornerd(zz, TAN_DD, 5)));
+}
+
+enum { TRIG_SIN = 0, TRIG_COS = 1, TRIG_TAN = 2, TRIG_SINPI = 3, TRIG_COSPI = 4 };
+
+/* trig_base sina / cosa / tana (simd/common/impl/trigo/trig_base.hpp:49-92) */
+static inline float finish_f(int kind, float a0, float xr, int n)
+{
+  const uint32_t sgn = tbf(a0) & 0x80000000u;
+  if (kind == TRIG_TAN) {
+    float y = tan_eval_f(xr);
+    if (n & 1) y = -(1.0f / y);
+    return tfb(tbf(y) ^ sgn);
+  }
+  const float z = xr * xr;
+  const int swap = n & 1;
+  if (kind == TRIG_SIN || kind == TRIG_SINPI) {
+    const float v = swap ? cos_eval_f(z) : sin_eval_f(z, xr);
+    return tfb(tbf(v) ^ sgn ^ ((uint32_t)(n & 2) << 30));
+  }
+  const float v = swap ? sin_eval_f(z, xr) : cos_eval_f(z);
+  return tfb(tbf(v) ^ ((uint32_t)((n ^ (n >> 1)) & 1) << 31));
+}
+static inline double finish_d(int kind, double a0, double xr, int n)
+{
+  const uint64_t sgn = tbd(a0) & 0x8000000000000000ull;
+  if (kind == TRIG_TAN) {
+    double y = tan_eval_d(xr);
+    if (n & 1) y = -(1.0 / y);
+    return tdb(tbd(y) ^ sgn);
+  }
+  const double z = xr * xr;
+  const int swap = n & 1;
+  if (kind == TRIG_SIN || kind == TRIG_SINPI) {
+    const double v = swap ? cos_eval_d(z) : sin_eval_d(z, xr);
+    return tdb(tbd(v) ^ sgn ^ ((uint64_t)(n & 2) << 62));
+  }
+  const double v = swap ? sin_eval_d(z, xr) : cos_eval_d(z);
+  return tdb(tbd(v) ^ ((uint64_t)((n ^ (n >> 1)) & 1) << 63));
+}
+
+/* pi_tag reduction (trig_reduction.hpp:216-229): xi = round2even(2x),
+ * xr = (x - xi/2) * pi, n = fast_toint(xi). */
+static inline int reduce_pi_f(float x, float* xr)
+{
+  const float xi = r2e_tf(x * 2.0f);
+  *xr = (x - xi * 0.5f) * tfb(F_PI);
+  return toint32(xi) & 3;
+}
+static inline int reduce_pi_d(double x, double* xr, int simd)
+{
+  const double xi = r2e_td(x * 2.0);
+  *xr = (x - xi * 0.5) * tdb(D_PI);
+  /* SSE2 converts packed doubles through int32 (cvttpd2dq); scalar code casts to int64 */
+  return simd ? (toint32(xi) & 3) : (int)(toint64(xi) & 3);
+}
+
+static void trig_pack_f(int kind, const float* a, float* y, int k)
+{
+  float x[8], xr[8];
+  int n[8];
+  for (int l = 0; l < k; ++l) x[l] = fabsf(a[l]);
+  if (kind == TRIG_SINPI || kind == TRIG_COSPI) {
+    for (int l = 0; l < k; ++l) n[l] = reduce_pi_f(x[l], &xr[l]);
+  } else {
+    reduce_pack_f(x, k, xr, n);
+  }
+  for (int l = 0; l < k; ++l) y[l] = finish_f(kind, a[l], xr[l], n[l]);
+}
+static void trig_pack_d(int kind, const double* a, double* y, int k)
+{
+  double x[8], xr[8];
+  int n[8];
+  for (int l = 0; l < k; ++l) x[l] = fabs(a[l]);
+  if (kind == TRIG_SINPI || kind == TRIG_COSPI) {
+    for (int l = 0; l < k; ++l) n[l] = reduce_pi_d(x[l], &xr[l], k > 1);
+  } else {
+    reduce_pack_d(x, k, xr, n);
+  }
+  for (int l = 0; l < k; ++l) y[l] = finish_d(kind, a[l], xr[l], n[l]);
+}
+
+/* y[i] = f(x[i]) over [0, n): packs of `pack` lanes from index 0, then the
+ * n % pack tail one element at a time (NT2's scalar code). */
+EXPORT int nt2o_trig_f(int kind, const float* x, float* y, size_t n, int pack)
+{
+  if (kind < 0 || kind > TRIG_COSPI || pack < 1 || pack > 8) return 1;
+  size_t i = 0;
+  for (; i + (size_t)pack <= n; i += (size_t)pack) trig_pack_f(kind, x + i, y + i, pack);
+  for (; i < n; ++i) trig_pack_f(kind, x + i, y + i, 1);
+  return 0;
+}
+EXPORT int nt2o_trig_d(int kind, const double* x, double* y, size_t n, int pack)
+{
+  if (kind < 0 || kind > TRIG_COSPI || pack < 1 || pack > 8) return 1;
+  size_t i = 0;
+  for (; i + (size_t)pack <= n; i += (size_t)pack) trig_pack_d(kind, x + i, y + i, pack);
+  for (; i < n; ++i) trig_pack_d(kind, x + i, y + i, 1);
+  return 0;
+}
+
+/* The reduction alone, for checking it: returns n, writes xr. */
+EXPORT int nt2o_rem_pio2_exact_d(double x, double* xr)
+{
+  const uint64_t b = tbd(x);
+  return exact_rem_pio2((b & 0xfffffffffffffull) | (1ull << 52), (int)((b >> 52) & 0x7ffu) - 1075, 53, xr);
+}
+EXPORT int nt2o_rem_pio2_exact_f(float x, float* xr)
+{
+  double r;
+  const uint32_t b = tbf(x);
+  const int n = exact_rem_pio2((uint64_t)((b & 0x7fffffu) | 0x800000u), (int)((b >> 23) & 0xffu) - 150, 24, &r);
+  *xr = (float)r;
+  return n;
+}

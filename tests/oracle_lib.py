@@ -40,6 +40,10 @@ SIGS = {
     "nt2o_log1p_f": (C.c_float, [C.c_float]),
     "nt2o_expm1_d": (C.c_double, [C.c_double]),
     "nt2o_log1p_d": (C.c_double, [C.c_double]),
+    "nt2o_trig_f": (C.c_int, [C.c_int, f32p, f32p, sz, C.c_int]),
+    "nt2o_trig_d": (C.c_int, [C.c_int, f64p, f64p, sz, C.c_int]),
+    "nt2o_rem_pio2_exact_f": (C.c_int, [C.c_float, C.POINTER(C.c_float)]),
+    "nt2o_rem_pio2_exact_d": (C.c_int, [C.c_double, C.POINTER(C.c_double)]),
     "nt2o_exp10_f": (C.c_float, [C.c_float]),
     "nt2o_log2_f": (C.c_float, [C.c_float]),
     "nt2o_log10_f": (C.c_float, [C.c_float]),
@@ -104,7 +108,23 @@ def max_ulp(a: np.ndarray, b: np.ndarray):
     return m, w.value
 
 
+TRIG = {"sin": 0, "cos": 1, "tan": 2, "sinpi": 3, "cospi": 4}
+
+
+def trig(op: str, x: np.ndarray, pack: int = 1) -> np.ndarray:
+    """NT2's op over x in packs of `pack` lanes from index 0 and a scalar tail; pack 1 is NT2's
+    scalar code, 16 // itemsize its 128-bit SIMD code."""
+    L = load()
+    x = np.ascontiguousarray(x)
+    y = np.empty_like(x)
+    fn = L.nt2o_trig_f if x.dtype == np.float32 else L.nt2o_trig_d
+    assert fn(TRIG[op], x, y, x.size, pack) == 0
+    return y
+
+
 def map_(op: str, x: np.ndarray) -> np.ndarray:
+    if op in TRIG:
+        return trig(op, x)
     L = load()
     y = np.empty_like(x)
     fn = L.nt2o_map_f if x.dtype == np.float32 else L.nt2o_map_d

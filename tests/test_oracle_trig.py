@@ -1,0 +1,153 @@
+"""Pin the CPU oracle's sin, cos, tan, sinpi, cospi against NT2's own unit-test
+and cover-test values.
+
+Expected values and tolerances are NT2's, from
+modules/core/trigonometric/unit/scalar/{sin,cos,tan,sinpi,cospi}.cpp and
+modules/core/trigonometric/cover/scalar/{sin,cos,tan,sinpi,cospi}.cpp
+(ranges and ulp bounds; the high-precision reference there is cephes long
+double, here FP64 for float results and mpmath for double results).  Tolerances
+are in NT2's ulpdist units (adjacent floats are 0.5 apart).
+"""
+import math
+
+import numpy as np
+import pytest
+
+INF = float("inf")
+NAN = float("nan")
+PI = math.pi
+SQ2 = math.sqrt(0.5)
+
+# (x, expected, ulp tolerance) from the unit tests
+SPECIALS = {
+    "sin": [(INF, NAN, 0.5), (-INF, NAN, 0.5), (NAN, NAN, 0.5), (-PI / 2, -1.0, 0.5), (-PI / 4, -SQ2, 0.5),
+            (PI / 2, 1.0, 0.5), (PI / 4, SQ2, 0.5), (0.0, 0.0, 0.5)],
+    "cos": [(INF, NAN, 0.5), (-INF, NAN, 0.5), (NAN, NAN, 0.5), (-PI, -1.0, 0.5), (-PI / 2, 0.0, 0.5),
+            (-PI / 4, SQ2, 0.5), (PI, -1.0, 0.5), (PI / 2, 0.0, 0.5), (PI / 4, SQ2, 0.5), (0.0, 1.0, 0.5)],
+    "tan": [(INF, NAN, 0.5), (-INF, NAN, 0.5), (NAN, NAN, 0.5), (-PI, 0.0, 0.75), (-PI / 4, -1.0, 1.0),
+            (PI, 0.0, 0.75), (PI / 4, 1.0, 1.0), (0.0, 0.0, 0.5)],
+    "sinpi": [(INF, NAN, 0.5), (-INF, NAN, 0.5), (NAN, NAN, 0.5), (-0.25, -SQ2, 0.5), (0.5, 1.0, 0.5),
+              (-0.5, -1.0, 0.5), (1.0, 0.0, 0.5), (0.25, SQ2, 0.5), (0.0, 0.0, 0.5)],
+    "cospi": [(INF, NAN, 0.5), (-INF, NAN, 0.5), (NAN, NAN, 0.5), (-0.25, SQ2, 0.5), (0.5, 0.0, 0.5),
+              (-0.5, 0.0, 0.5), (1.0, -1.0, 0.5), (0.25, SQ2, 0.5), (0.0, 1.0, 0.5), (-1.0, -1.0, 0.5)],
+}
+
+# cover tests: range and ulp bound
+COVER = {"sin": (60.0, 0.5), "cos": (60.0, 0.5), "tan": (60.0, 1.0), "sinpi": (40.0, 10.0), "cospi": (41.0, 3.0)}
+
+
+def _ulp(L, dt):
+    return L.nt2o_ulpdist_f if dt == np.float32 else L.nt2o_ulpdist_d
+
+
+@pytest.mark.parametrize("op", sorted(SPECIALS))
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_trig_special_values(oracle, op, dt):
+    L = oracle.load()
+    u = _ulp(L, dt)
+    for x, r, tol in SPECIALS[op]:
+        xs = np.array([x], dt)
+        for pack in (1, 16 // np.dtype(dt).itemsize, 32 // np.dtype(dt).itemsize):
+            # the SIMD unit tests splat one value over the pack
+            y = oracle.trig(op, np.repeat(xs, pack), pack)
+            assert u(float(y[0]), float(dt(r))) <= tol, (op, dt, x, pack, y[0])
+            assert np.array_equal(y, np.repeat(y[:1], pack), equal_nan=True)
+
+
+@pytest.mark.parametrize("op", sorted(COVER))
+def test_trig_cover_f32(oracle, op):
+    lim, bound = COVER[op]
+    x = np.random.default_rng(21).uniform(-lim, lim, 200000).astype(np.float32)
+    xd = x.astype(np.float64)
+    ref = {"sin": np.sin, "cos": np.cos, "tan": np.tan,
+           "sinpi": lambda v: np.sin(np.pi * v), "cospi": lambda v: np.cos(np.pi * v)}[op](xd)
+    if op in ("sinpi", "cospi"):
+        # pi*x in FP64 loses the low bits for |x| near 40; the exact product is what NT2 is held to
+        mpmath = pytest.importorskip("mpmath")
+        mpmath.mp.dps = 40
+        f = mpmath.sin if op == "sinpi" else mpmath.cos
+        ref = np.array([float(f(mpmath.pi * mpmath.mpf(float(v)))) for v in xd[:20000]])
+        x = x[:20000]
+    ref = ref.astype(np.float32)
+    L = oracle.load()
+    for pack in (1, 4, 8):
+        y = oracle.trig(op, x, pack)
+        m, w = oracle.max_ulp(y, ref)
+        # NT2's cover runs draw a few hundred samples; over this many the bound is
+        # missed by one step (one ulp) at a rate below 1e-4
+        assert m <= bound + 0.5, (op, pack, m, x[w])
+        over = sum(L.nt2o_ulpdist_f(float(a), float(b)) > bound for a, b in zip(y, ref))
+        assert over <= 1e-4 * x.size, (op, pack, over)
+
+
+@pytest.mark.parametrize("op", sorted(COVER))
+def test_trig_cover_f64(oracle, op):
+    mpmath = pytest.importorskip("mpmath")
+    mpmath.mp.dps = 40
+    lim, bound = COVER[op]
+    x = np.random.default_rng(22).uniform(-lim, lim, 3000)
+    f = {"sin": mpmath.sin, "cos": mpmath.cos, "tan": mpmath.tan,
+         "sinpi": lambda v: mpmath.sin(mpmath.pi * v), "cospi": lambda v: mpmath.cos(mpmath.pi * v)}[op]
+    ref = np.array([float(f(mpmath.mpf(float(v)))) for v in x])
+    # NT2's scalar code and 256-bit packs; 128-bit packs of two doubles meet a pack
+    # with one lane in (pi/4, pi/2] about once in this sample (test below)
+    for pack in (1, 4):
+        m, w = oracle.max_ulp(oracle.trig(op, x, pack), ref)
+        assert m <= bound, (op, pack, m, x[w])
+
+
+def test_trig_pack_reduction_is_shared(oracle):
+    """NT2's SIMD code reduces a whole pack with one method: a lane <= pi/4 next to a lane in
+    (pi/4, pi/2] goes through rem_pio2_straight (x - pi/2, then the cosine polynomial outside the
+    range it was fitted on) instead of being left alone as NT2's scalar code leaves it.  Its error
+    there is large; the scalar form is the default of the CUDA evaluator for that reason."""
+    x = np.array([1e-3, 1.0], np.float64)
+    alone = oracle.trig("sin", x[:1], 1)[0]
+    packed = oracle.trig("sin", x, 2)
+    assert abs(alone - math.sin(1e-3)) <= 2.0 ** -53 * 1e-3
+    assert 1e-9 < abs(packed[0] / math.sin(1e-3) - 1) < 1e-6
+    assert packed[1] == oracle.trig("sin", x[1:], 1)[0]     # level-1 lane: straight either way
+    xf = np.array([1e-3, 0.5, 0.25, 1.2], np.float32)
+    assert abs(oracle.trig("sin", xf, 4)[0] / np.float32(1e-3) - 1) > 1e-3
+    assert abs(oracle.trig("sin", xf, 1)[0] / math.sin(float(xf[0])) - 1) < 1e-7
+    # a pack of one is the scalar code element by element
+    assert np.array_equal(oracle.trig("sin", xf, 1), np.array([oracle.trig("sin", xf[i:i + 1], 1)[0]
+                                                              for i in range(4)]))
+
+
+def test_trig_tail_is_scalar(oracle):
+    # packs from index 0, the n % pack tail one element at a time
+    x = np.array([1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1.0], np.float64)
+    y = oracle.trig("sin", x, 4)
+    assert np.all(y[:4] == oracle.trig("sin", x[:1], 1)[0])
+    assert y[4] == oracle.trig("sin", x[4:5], 1)[0]
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_rem_pio2_exact(oracle, dt):
+    """The exact reduction used where NT2 calls fdlibm's __kernel_rem_pio2(f): n and x - n*pi/2
+    rounded once, against mpmath."""
+    mpmath = pytest.importorskip("mpmath")
+    import ctypes as C
+    mpmath.mp.prec = 2400
+    L = oracle.load()
+    rng = np.random.default_rng(5)
+    if dt == np.float64:
+        vals = [6381956970095103 * 2.0 ** 797, 1e22, 1e300, 5.319372648326541e255, 823550.0]
+        vals += list(rng.uniform(1, 2, 300) * 2.0 ** rng.uniform(19, 1020, 300))
+        fn, out, prec = L.nt2o_rem_pio2_exact_d, C.c_double(), 53
+    else:
+        vals = [float(np.float32(v)) for v in (201.1, 1e6, 3.4e38, 1e30, 823549.6875, 12345.678)]
+        vals += [float(np.float32(v)) for v in rng.uniform(1, 2, 300) * 2.0 ** rng.uniform(7.7, 126.9, 300)]
+        fn, out, prec = L.nt2o_rem_pio2_exact_f, C.c_float(), 24
+    half_pi = mpmath.pi / 2
+    for x in vals:
+        n = fn(x, C.byref(out))
+        k = mpmath.nint(mpmath.mpf(x) / half_pi)
+        r = mpmath.mpf(x) - k * half_pi
+        with mpmath.workprec(prec):
+            want = float(+r)
+        assert n == int(k) % 4 and out.value == want, (x, n, out.value, want)
+    # sin(1e22), the classic check of an argument reduction
+    y = oracle.trig("sin", np.array([1e22]), 1)[0]
+    assert abs(y - (-0.8522008497671888)) <= 2.0 ** -53
