@@ -145,11 +145,6 @@ NT2CUDA_UN(log1p_, math::log1p<F>(a))
 NT2CUDA_UN(erfc_, math::erfc<F>(a))
 NT2CUDA_UN(normcdf_, math::normcdf<F>(a))
 NT2CUDA_UN(fastnormcdf_, math::fastnormcdf<F>(a))
-NT2CUDA_UN(sin_, (trig::one<trig::SIN, F>(a)))
-NT2CUDA_UN(cos_, (trig::one<trig::COS, F>(a)))
-NT2CUDA_UN(tan_, (trig::one<trig::TAN, F>(a)))
-NT2CUDA_UN(sinpi_, (trig::one<trig::SINPI, F>(a)))
-NT2CUDA_UN(cospi_, (trig::one<trig::COSPI, F>(a)))
 // trunc_u8(y) = cast<uint8_t>(y) for a float y in [0, 256), where the cast truncates toward
 // zero: 2^23 + y rounded toward zero is 2^23 + floor(y), whose low byte is the result.
 // Used where the statement bounds y (rgb2grey's weights sum below 1); a full-rate add in
@@ -295,13 +290,16 @@ template <class Tag, class A, class B, class C, int V> struct regs<node<Tag, A, 
   }
 };
 
-// 128-bit SIMD form of a trigonometric node.  NT2's SIMD code reduces the
-// arguments of a whole pack with one method chosen from the pack's largest |x|
-// (nt2cuda/trig.cuh), so a lane's value depends on its neighbours: the node
-// computes all lanes of a pack when asked for the pack's first lane and hands
-// out the rest from `res`.  The kernels ask for lanes 0..V-1 in order.  A pack
-// is 16 bytes of the argument type; groups of fewer lanes (the scalar tail,
-// misaligned tables) are NT2's scalar code.
+// Trigonometric nodes.  NT2's SIMD code reduces the arguments of a whole pack
+// with one method chosen from the pack's largest |x| (nt2cuda/trig.cuh), so in
+// the simd128_ form a lane's value depends on its neighbours; the plain tags
+// are NT2's scalar code, each element on its own.  Either way the node
+// computes all lanes of a group when asked for the group's first lane and
+// hands out the rest from `res` (the kernels ask for lanes 0..V-1 in order).
+// simd128_ groups are 16-byte packs of the argument type (groups of fewer
+// lanes, the scalar tail and misaligned tables, are scalar code); the scalar
+// form takes the thread's whole group, reduced in one pass when its elements
+// share a reduction level.
 template <class Tag> struct trig_kind;
 template <> struct trig_kind<tag::sin_> { static constexpr int value = trig::SIN; };
 template <> struct trig_kind<tag::cos_> { static constexpr int value = trig::COS; };
@@ -309,13 +307,13 @@ template <> struct trig_kind<tag::tan_> { static constexpr int value = trig::TAN
 template <> struct trig_kind<tag::sinpi_> { static constexpr int value = trig::SINPI; };
 template <> struct trig_kind<tag::cospi_> { static constexpr int value = trig::COSPI; };
 
-template <class Tag, class A, int V> struct regs<node<tag::simd128_<Tag>, A>, V> {
-  using N = node<tag::simd128_<Tag>, A>;
+template <class NodeTag, class Tag, bool SIMD, class A, int V> struct trig_regs {
+  using N = node<NodeTag, A>;
   using T = typename value_of<A>::type;
   static_assert(std::is_same<T, float>::value || std::is_same<T, double>::value,
                 "trigonometric functors take float or double tables");
   static constexpr int PW = 16 / (int)sizeof(T);
-  static constexpr int P = (V % PW == 0) ? PW : 1;
+  static constexpr int P = SIMD ? ((V % PW == 0) ? PW : 1) : V;
   regs<A, V> ra;
   mutable T res[V];
   template <bool S> __device__ __forceinline__ void load(const N& n, size_t i) { ra.template load<S>(n.a, i); }
@@ -325,13 +323,24 @@ template <class Tag, class A, int V> struct regs<node<tag::simd128_<Tag>, A>, V>
       T a[P], y[P];
 #pragma unroll
       for (int p = 0; p < P; ++p) a[p] = (T)ra.template get<F>(n.a, l + p);
-      trig::pack<trig_kind<Tag>::value, F, P>(a, y);
+      if constexpr (SIMD) trig::pack<trig_kind<Tag>::value, F, P>(a, y);
+      else trig::scalar_group<trig_kind<Tag>::value, F, P>(a, y);
 #pragma unroll
       for (int p = 0; p < P; ++p) res[l + p] = y[p];
     }
     return res[l];
   }
 };
+#define NT2CUDA_TRIG_REGS(TAG)                                                                     \
+  template <class A, int V> struct regs<node<tag::TAG, A>, V> : trig_regs<tag::TAG, tag::TAG, false, A, V> {}; \
+  template <class A, int V>                                                                        \
+  struct regs<node<tag::simd128_<tag::TAG>, A>, V> : trig_regs<tag::simd128_<tag::TAG>, tag::TAG, true, A, V> {};
+NT2CUDA_TRIG_REGS(sin_)
+NT2CUDA_TRIG_REGS(cos_)
+NT2CUDA_TRIG_REGS(tan_)
+NT2CUDA_TRIG_REGS(sinpi_)
+NT2CUDA_TRIG_REGS(cospi_)
+#undef NT2CUDA_TRIG_REGS
 
 // ------------------------------------------------------------- programs
 // prog<A0, A...>: the assigns of one statement, evaluated per index in order.

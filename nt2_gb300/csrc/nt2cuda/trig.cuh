@@ -192,7 +192,12 @@ static __device__ __noinline__ int exact_rem_pio2(uint64_t m, int q, int prec, d
 }
 
 // -------------------------------------------------------------- reductions
-// cvttps2dq / cvttpd2dq: NaN or out of range gives INT32_MIN
+// cvttps2dq / cvttpd2dq: NaN or out of range gives INT32_MIN (a plain cast
+// saturates instead).  A float overload keeps float code off the FP64 pipe.
+__device__ __forceinline__ int toint32(float a)
+{
+  return (a != a || a >= 2147483648.0f || a < -2147483648.0f) ? (int)0x80000000 : (int)a;
+}
 __device__ __forceinline__ int toint32(double a)
 {
   return (a != a || a >= 2147483648.0 || a < -2147483648.0) ? (int)0x80000000 : (int)a;
@@ -223,7 +228,7 @@ __device__ __forceinline__ int cephes(float x, float& xr)
   float r = __fsub_rn(x, __fmul_rn(xi, fbits(tf::pio2_1)));
   r = __fsub_rn(r, __fmul_rn(xi, fbits(tf::pio2_2)));
   xr = __fsub_rn(r, __fmul_rn(xi, fbits(tf::pio2_3)));
-  return toint32(xi) & 3;
+  return (int)xi & 3;     // |xi| <= 40 (or NaN, whose xr is NaN whatever n is)
 }
 __device__ __forceinline__ int cephes(double x, double& xr)
 {
@@ -231,7 +236,7 @@ __device__ __forceinline__ int cephes(double x, double& xr)
   double r = __dsub_rn(x, __dmul_rn(xi, dbits(td::pio2_1)));
   r = __dsub_rn(r, __dmul_rn(xi, dbits(td::pio2_2)));
   xr = __dsub_rn(r, __dmul_rn(xi, dbits(td::pio2_3)));
-  return (int)(toint64(xi) & 3);
+  return (int)xi & 3;     // |xi| <= 40 (or NaN, whose xr is NaN whatever n is)
 }
 template <class T, class C> __device__ __forceinline__ int medium_impl(T t, T& xr, T invpio2, T p1, T p2, T p2t, T p3, T p3t)
 {
@@ -248,8 +253,9 @@ template <class T, class C> __device__ __forceinline__ int medium_impl(T t, T& x
   xr = sub(r, w);
   return C::toint(fn) & 3;
 }
-struct cvt_f { __device__ static float round(float a) { return rintf(a); } __device__ static int toint(float a) { return toint32(a); } };
-struct cvt_d { __device__ static double round(double a) { return rint(a); } __device__ static int toint(double a) { return (int)(toint64(a) & 3); } };
+// medium's quotients are below 2^7 (float) and 2^19 (double), or NaN
+struct cvt_f { __device__ static float round(float a) { return rintf(a); } __device__ static int toint(float a) { return (int)a; } };
+struct cvt_d { __device__ static double round(double a) { return rint(a); } __device__ static int toint(double a) { return (int)a; } };
 __device__ __forceinline__ int medium(float t, float& xr)
 {
   return medium_impl<float, cvt_f>(t, xr, fbits(tf::invpio2), fbits(tf::pio2_1), fbits(tf::pio2_2), fbits(tf::pio2_2t),
@@ -384,12 +390,19 @@ __device__ __forceinline__ int level(double x)
   return (x > dbits(td::pio4)) + (x > dbits(td::pio2)) + (x > dbits(td::p20pi)) + (x > dbits(td::medpi));
 }
 
-// The double chain over one pack of P lanes.
-template <int P> __device__ __forceinline__ void reduce_pack(const double (&x)[P], double (&xr)[P], int (&n)[P])
+// Largest |x| of a pack (NaN lanes ignored, as their level is 0); level() is
+// monotone, so the pack's level is the level of its largest lane.
+template <int P, class T> __device__ __forceinline__ T pack_max(const T (&x)[P])
 {
-  int lv = 0;
+  T m = x[0];
 #pragma unroll
-  for (int l = 0; l < P; ++l) lv = max(lv, level(x[l]));
+  for (int l = 1; l < P; ++l) m = fmax(m, x[l]);
+  return m;
+}
+
+// The double chain over one pack of P lanes at level lv.
+template <int P> __device__ __forceinline__ void reduce_at(int lv, const double (&x)[P], double (&xr)[P], int (&n)[P])
+{
   if (lv == 0) {
 #pragma unroll
     for (int l = 0; l < P; ++l) { xr[l] = x[l]; n[l] = 0; }
@@ -407,13 +420,14 @@ template <int P> __device__ __forceinline__ void reduce_pack(const double (&x)[P
     for (int l = 0; l < P; ++l) n[l] = fdlibm(x[l], &xr[l]);
   }
 }
-
-// The float chain over one pack of P lanes.
-template <int P> __device__ __forceinline__ void reduce_pack(const float (&x)[P], float (&xr)[P], int (&n)[P])
+template <int P> __device__ __forceinline__ void reduce_pack(const double (&x)[P], double (&xr)[P], int (&n)[P])
 {
-  int lv = 0;
-#pragma unroll
-  for (int l = 0; l < P; ++l) lv = max(lv, level(x[l]));
+  reduce_at<P>(level(pack_max<P>(x)), x, xr, n);
+}
+
+// The float chain over one pack of P lanes at level lv.
+template <int P> __device__ __forceinline__ void reduce_at(int lv, const float (&x)[P], float (&xr)[P], int (&n)[P])
+{
   if (lv == 0) {
 #pragma unroll
     for (int l = 0; l < P; ++l) { xr[l] = x[l]; n[l] = 0; }
@@ -443,6 +457,10 @@ template <int P> __device__ __forceinline__ void reduce_pack(const float (&x)[P]
 #pragma unroll
     for (int l = 0; l < P; ++l) n[l] = fdlibm(x[l], &xr[l]);
   }
+}
+template <int P> __device__ __forceinline__ void reduce_pack(const float (&x)[P], float (&xr)[P], int (&n)[P])
+{
+  reduce_at<P>(level(pack_max<P>(x)), x, xr, n);
 }
 
 // pi_tag reduction (trig_reduction.hpp:216-229): xi = round2even(2x),
@@ -536,8 +554,11 @@ template <int K, bool F, class T> __device__ __forceinline__ T finish(T a0, T xr
   }
 }
 
-// y[l] = f(a[l]) for one pack of P lanes.
-template <int K, bool F, int P, class T> __device__ __forceinline__ void pack(const T (&a)[P], T (&y)[P])
+// NT2's SIMD code over one pack of P lanes: y[l] = f(a[l]), one reduction
+// method for the pack.  SIMD selects the packed-double conversion of the pi
+// reduction (P > 1).
+template <int K, bool F, int P, bool SIMD, class T>
+__device__ __forceinline__ void pack_impl(const T (&a)[P], T (&y)[P])
 {
   T x[P], xr[P];
   int n[P];
@@ -545,20 +566,62 @@ template <int K, bool F, int P, class T> __device__ __forceinline__ void pack(co
   for (int l = 0; l < P; ++l) x[l] = fabs(a[l]);
   if constexpr (K == SINPI || K == COSPI) {
 #pragma unroll
-    for (int l = 0; l < P; ++l) n[l] = reduce_pi(x[l], xr[l], P > 1);
+    for (int l = 0; l < P; ++l) n[l] = reduce_pi(x[l], xr[l], SIMD);
   } else {
     reduce_pack<P>(x, xr, n);
   }
 #pragma unroll
   for (int l = 0; l < P; ++l) y[l] = finish<K, F>(a[l], xr[l], n[l]);
 }
+template <int K, bool F, int P, class T> __device__ __forceinline__ void pack(const T (&a)[P], T (&y)[P])
+{
+  pack_impl<K, F, P, (P > 1)>(a, y);
+}
 
 // One element, NT2's scalar code (a pack of one).
 template <int K, bool F, class T> __device__ __forceinline__ T one(T a)
 {
   T in[1] = {a}, out[1];
-  pack<K, F, 1>(in, out);
+  pack_impl<K, F, 1, false>(in, out);
   return out[0];
+}
+
+// NT2's scalar code on the P elements of a thread's group, each reduced on its
+// own.  Levels 0-2 (|x| <= 20 pi) are computed without branches: the cephes
+// and straight reductions are both evaluated and the element's level picks
+// between them and x itself, so a warp whose elements mix these levels runs
+// one path.  Larger levels branch per element.
+template <class T> __device__ __forceinline__ int reduce_low(int lv, T x, T& xr)
+{
+  T xs, xc;
+  straight(x, xs);
+  const int nc = cephes(x, xc);
+  xr = lv == 0 ? x : (lv == 1 ? xs : xc);
+  return lv == 0 ? 0 : (lv == 1 ? 1 : nc);
+}
+template <int K, bool F, int P, class T> __device__ __forceinline__ void scalar_group(const T (&a)[P], T (&y)[P])
+{
+  if constexpr (K == SINPI || K == COSPI) {
+    pack_impl<K, F, P, false>(a, y);
+  } else {
+    T xr[P];
+    int n[P];
+#pragma unroll
+    for (int l = 0; l < P; ++l) {
+      T x1[1] = {fabs(a[l])}, r1[1];
+      int n1[1];
+      const int lv = level(x1[0]);
+      if (lv <= 2) {
+        n1[0] = reduce_low(lv, x1[0], r1[0]);
+      } else {
+        reduce_at<1>(lv, x1, r1, n1);
+      }
+      xr[l] = r1[0];
+      n[l] = n1[0];
+    }
+#pragma unroll
+    for (int l = 0; l < P; ++l) y[l] = finish<K, F>(a[l], xr[l], n[l]);
+  }
 }
 
 }  // namespace trig
