@@ -138,15 +138,17 @@ inline cudaError_t launch_grid(K kernel, size_t grid, int block, cudaStream_t s,
 }
 
 // Evaluate statement p over [0,n).  Returns cudaErrorInvalidValue when the
-// statement's tables partially overlap.
+// statement's tables partially overlap.  `def` is used when the tuning table
+// has no entry for tune_key at this size.
 template <bool F, class P>
-inline cudaError_t transform(const P& p, size_t n, cudaStream_t s, const char* tune_key = nullptr)
+inline cudaError_t transform(const P& p, size_t n, cudaStream_t s, const char* tune_key = nullptr,
+                             tuning::params def = tuning::params{})
 {
   if (n == 0) return cudaSuccess;
   alias_kind ak = classify_alias(p, n);
   if (ak == alias_kind::bad) return cudaErrorInvalidValue;
   constexpr int V = base_lanes<P>::value;
-  const tuning::params tp = tuning::lookup(tune_key, n);
+  const tuning::params tp = tuning::lookup(tune_key, n, def);
   const int U = tp.unroll, W = tp.waves;
   P pc = p;
   size_t nn = n;

@@ -73,6 +73,10 @@ __device__ __constant__ const uint32_t kTwoOverPi[40] = {
   0xef2f118bu, 0x5a0a6d1fu, 0x6d367ecfu, 0x27cb09b7u, 0x4f463f66u, 0x9e5fea2du, 0x7527bac7u, 0xebe5f17bu,
   0x3d0739f7u, 0x8a5292eau, 0x6bfb5fb1u, 0x1f8d5d08u, 0x56033046u, 0xfc7b6babu, 0xf0cfbc20u, 0x9af4361du};
 
+// A reduced argument: x - n*pi/2 and n mod 4.  Returned by value, so that the
+// out-of-line reductions below take no address of the caller's registers.
+template <class T> struct reduced { T xr; int n; };
+
 // ------------------------------------------------ exact Payne-Hanek reduction
 // 64-bit limbs, little-endian.
 template <int N> __device__ __forceinline__ int lbit(const uint64_t (&p)[N], int k)
@@ -106,7 +110,7 @@ template <int N> __device__ __forceinline__ bool lany_below(const uint64_t (&p)[
 // x = m * 2^q (m < 2^53, x > 0 finite): n = round(x * 2/pi) mod 4 and
 // r = x - n*pi/2, rounded once to `prec` bits.  A 256-bit window of 2/pi
 // starting at the first word that can reach the integer part mod 4.
-static __device__ __noinline__ int exact_rem_pio2(uint64_t m, int q, int prec, double* r)
+static __device__ __noinline__ reduced<double> exact_rem_pio2(uint64_t m, int q, int prec)
 {
   const int i0 = q >= 2 ? (q - 2) / 32 : 0;
   uint64_t nw[4];
@@ -148,7 +152,7 @@ static __device__ __noinline__ int exact_rem_pio2(uint64_t m, int q, int prec, d
   int top = -1;
   for (int i = 4; i >= 0; --i)
     if (p[i]) { top = 64 * i + 63 - __clzll((long long)p[i]); break; }
-  if (top < 0) { *r = 0.0; return n & 3; }
+  if (top < 0) return reduced<double>{0.0, n & 3};
   const uint64_t mh = lbits64(p, top - 63), ml = lbits64(p, top - 127);
   const bool sticky_f = lany_below(p, top - 127);
   // Q = M * floor(pi/2 * 2^126)
@@ -187,8 +191,7 @@ static __device__ __noinline__ int exact_rem_pio2(uint64_t m, int q, int prec, d
   const int be = e + prec - 1 + 1023;
   const uint64_t bits = ((uint64_t)be << 52) | ((mm << (53 - prec)) & 0xfffffffffffffull);
   const double v = __longlong_as_double((long long)bits);
-  *r = neg ? -v : v;
-  return n & 3;
+  return reduced<double>{neg ? -v : v, n & 3};
 }
 
 // -------------------------------------------------------------- reductions
@@ -268,7 +271,7 @@ __device__ __forceinline__ int medium(double t, double& xr)
 }
 
 // fdlibm __ieee754_rem_pio2f for x >= 0 (functions/scalar/rem_pio2.hpp:148-231)
-static __device__ __noinline__ int fdlibm(float x, float* xrp)
+static __device__ __noinline__ reduced<float> fdlibm(float x)
 {
   const uint32_t ix = __float_as_uint(x) & 0x7fffffffu;
   float xr;
@@ -314,17 +317,16 @@ static __device__ __noinline__ int fdlibm(float x, float* xrp)
   } else if (ix >= 0x7f800000u) {
     xr = __fsub_rn(x, x); n = 0;
   } else {
-    double rd;
-    n = exact_rem_pio2((uint64_t)((ix & 0x7fffffu) | 0x800000u), (int)(ix >> 23) - 150, 24, &rd);
-    xr = (float)rd;
+    const reduced<double> e = exact_rem_pio2((uint64_t)((ix & 0x7fffffu) | 0x800000u), (int)(ix >> 23) - 150, 24);
+    xr = (float)e.xr;
+    n = e.n;
   }
-  *xrp = xr;
-  return n;
+  return {xr, n};
 }
 
 // NT2's double rem_pio2 (functions/scalar/rem_pio2.hpp:413-427) over fdlibm
 // __ieee754_rem_pio2 for x >= 0 (:536-621)
-static __device__ __noinline__ int fdlibm(double x, double* xrp)
+static __device__ __noinline__ reduced<double> fdlibm(double x)
 {
   const uint64_t b = (uint64_t)__double_as_longlong(x);
   const uint32_t ix = (uint32_t)(b >> 32) & 0x7fffffffu;
@@ -373,10 +375,11 @@ static __device__ __noinline__ int fdlibm(double x, double* xrp)
   } else if (ix >= 0x7ff00000u) {
     xr = __dsub_rn(x, x); n = 0;
   } else {
-    n = exact_rem_pio2((b & 0xfffffffffffffull) | (1ull << 52), (int)((b >> 52) & 0x7ffu) - 1075, 53, &xr);
+    const reduced<double> e = exact_rem_pio2((b & 0xfffffffffffffull) | (1ull << 52), (int)((b >> 52) & 0x7ffu) - 1075, 53);
+    xr = e.xr;
+    n = e.n;
   }
-  *xrp = xr;
-  return n;
+  return {xr, n};
 }
 
 // Level of a lane: how many thresholds |x| exceeds (NaN: 0).
@@ -417,7 +420,7 @@ template <int P> __device__ __forceinline__ void reduce_at(int lv, const double 
     for (int l = 0; l < P; ++l) n[l] = medium(x[l], xr[l]);
   } else {
 #pragma unroll
-    for (int l = 0; l < P; ++l) n[l] = fdlibm(x[l], &xr[l]);
+    for (int l = 0; l < P; ++l) { const auto r = fdlibm(x[l]); xr[l] = r.xr; n[l] = r.n; }
   }
 }
 template <int P> __device__ __forceinline__ void reduce_pack(const double (&x)[P], double (&xr)[P], int (&n)[P])
@@ -455,7 +458,7 @@ template <int P> __device__ __forceinline__ void reduce_at(int lv, const float (
     }
   } else {
 #pragma unroll
-    for (int l = 0; l < P; ++l) n[l] = fdlibm(x[l], &xr[l]);
+    for (int l = 0; l < P; ++l) { const auto r = fdlibm(x[l]); xr[l] = r.xr; n[l] = r.n; }
   }
 }
 template <int P> __device__ __forceinline__ void reduce_pack(const float (&x)[P], float (&xr)[P], int (&n)[P])

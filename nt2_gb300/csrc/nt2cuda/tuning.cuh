@@ -36,12 +36,13 @@ inline std::string make_key(const char* key, size_t n)
   return k;
 }
 
-inline params lookup(const char* key, size_t n)
+// The entry for (key, size bucket of n), or `def` when there is none.
+inline params lookup(const char* key, size_t n, params def = params{})
 {
-  if (!key) return params{};
+  if (!key) return def;
   std::lock_guard<std::mutex> g(table_mutex());
   auto it = table().find(make_key(key, n));
-  return it == table().end() ? params{} : it->second;
+  return it == table().end() ? def : it->second;
 }
 
 inline int unroll_for(const char* key, size_t n) { return lookup(key, n).unroll; }
