@@ -27,6 +27,9 @@
 #include <cuda_runtime.h>
 #include <stddef.h>
 #include <stdint.h>
+#include <cstring>
+#include <istream>
+#include <ostream>
 #include <stdexcept>
 #include <string>
 #include <tuple>
@@ -126,6 +129,17 @@ template <class T> class table {
   T* device() { sync_device(); host_valid_ = false; return d_; }
   const T* device() const { sync_device(); return d_; }
   void mark_device_written() { dev_valid_ = true; host_valid_ = false; }
+  // replace the contents from host data (numel() elements, column-major);
+  // the device copy is refreshed by the next sync_device()
+  void assign_host(std::vector<T>&& data)
+  {
+    if (data.size() != numel()) throw std::invalid_argument("assign_host: element count differs from numel()");
+    h_ = std::move(data);
+    host_valid_ = true;
+    dev_valid_ = numel() == 0;
+  }
+  // the host mirror, current after sync_host()
+  const std::vector<T>& host() const { sync_host(); return h_; }
 
   void sync_host() const
   {
@@ -601,5 +615,84 @@ template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto cumma
 { return detail_table::scan_dim<fold::op_val<3>>(x, dim, "cummax"); }
 template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto cummin(const X& x, int dim = 1)
 { return detail_table::scan_dim<fold::op_val<4>>(x, dim, "cummin"); }
+
+// ----------------------------------------------------------- table I/O
+// NT2 serializes a table as its extent followed by its numel() elements
+// (modules/core/container/table/include/nt2/core/container/io/serialization.hpp:48-83,
+// written through a Boost.Serialization archive).  save/load write the same two
+// fields in a fixed little-endian layout that needs no Boost:
+//   8 bytes   "NT2TABLE"
+//   4 bytes   element size in bytes      4 bytes  element kind: 'f', 'i' or 'u'
+//   8 bytes   extent 1 (rows)            8 bytes  extent 2 (columns)
+//   rows * columns elements, column-major
+// save is a host<->device sync point: the device copy is brought to the host
+// mirror first.  load fills the host mirror and marks the device copy stale,
+// so the first evaluation that reads the table copies it up.
+namespace detail_table {
+template <class T> constexpr uint32_t kind_of()
+{
+  return std::is_floating_point<T>::value ? 'f' : (std::is_signed<T>::value ? 'i' : 'u');
+}
+inline void put64(std::ostream& os, uint64_t v)
+{
+  unsigned char b[8];
+  for (int i = 0; i < 8; ++i) b[i] = (unsigned char)(v >> (8 * i));
+  os.write((const char*)b, 8);
+}
+inline void put32(std::ostream& os, uint32_t v)
+{
+  unsigned char b[4];
+  for (int i = 0; i < 4; ++i) b[i] = (unsigned char)(v >> (8 * i));
+  os.write((const char*)b, 4);
+}
+inline uint64_t get64(std::istream& is)
+{
+  unsigned char b[8] = {};
+  is.read((char*)b, 8);
+  uint64_t v = 0;
+  for (int i = 7; i >= 0; --i) v = (v << 8) | b[i];
+  return v;
+}
+inline uint32_t get32(std::istream& is)
+{
+  unsigned char b[4] = {};
+  is.read((char*)b, 4);
+  uint32_t v = 0;
+  for (int i = 3; i >= 0; --i) v = (v << 8) | b[i];
+  return v;
+}
+}  // namespace detail_table
+
+template <class T> void save(std::ostream& os, const table<T>& t)
+{
+  static_assert(std::is_arithmetic<T>::value, "save: tables of numbers");
+  const std::vector<T>& h = t.host();
+  os.write("NT2TABLE", 8);
+  detail_table::put32(os, (uint32_t)sizeof(T));
+  detail_table::put32(os, detail_table::kind_of<T>());
+  detail_table::put64(os, t.height());
+  detail_table::put64(os, t.width());
+  // elements in the host's byte order: little-endian on x86-64 and aarch64
+  if (!h.empty()) os.write((const char*)h.data(), (std::streamsize)(h.size() * sizeof(T)));
+  if (!os) throw std::runtime_error("nt2cuda::save: write failed");
+}
+
+template <class T> void load(std::istream& is, table<T>& t)
+{
+  static_assert(std::is_arithmetic<T>::value, "load: tables of numbers");
+  char magic[8] = {};
+  is.read(magic, 8);
+  if (!is || std::memcmp(magic, "NT2TABLE", 8) != 0) throw std::runtime_error("nt2cuda::load: not a table file");
+  const uint32_t size = detail_table::get32(is), kind = detail_table::get32(is);
+  if (size != sizeof(T) || kind != detail_table::kind_of<T>())
+    throw std::runtime_error("nt2cuda::load: element type differs from the table's");
+  const uint64_t rows = detail_table::get64(is), cols = detail_table::get64(is);
+  if (!is || (cols && rows > ~(uint64_t)0 / cols)) throw std::runtime_error("nt2cuda::load: bad extent");
+  std::vector<T> data((size_t)(rows * cols));
+  if (!data.empty()) is.read((char*)data.data(), (std::streamsize)(data.size() * sizeof(T)));
+  if (!is) throw std::runtime_error("nt2cuda::load: file ends early");
+  t.resize(of_size((size_t)rows, (size_t)cols));
+  t.assign_host(std::move(data));
+}
 
 }  // namespace nt2cuda

@@ -12,9 +12,13 @@
 //   sigmadelta demo/sigmadelta/nt2/sigmadelta_nt2.cpp:37-58, 100-106
 //   stats      NT2 reductions and cumulative functions of a table (mean, var,
 //              maximum, asum1, cumsum along both dimensions, global* forms)
+//   io         table files (nt2cuda::load / save): B = A*2 + 1 of a loaded table, saved
+//   trig       trigonometric functors inside one statement and a fold:
+//              y = sin(x) + cos(x)*tan(x*0.25f) + cospi(x)*sinpi(x), globalsum(sin(x))
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <string>
 #include <vector>
 #include "nt2cuda/table.hpp"
@@ -153,6 +157,25 @@ int main(int argc, char** argv)
     write_table(argv[9], c1);
     write_table(argv[10], c2);
     write_table(argv[11], g);
+  } else if (cmd == "io") {                               // n unused; in: table file ; out: table file
+    typedef double T;
+    nt2::table<T> A, B;
+    {
+      std::ifstream in(argv[3], std::ios::binary);
+      nt2::load(in, A);
+    }
+    B = A * T(2) + T(1);
+    std::ofstream out(argv[4], std::ios::binary);
+    nt2::save(out, B);
+    std::printf("%zu %zu\n", B.height(), B.width());
+  } else if (cmd == "trig") {                             // n; in: x ; out: y, [globalsum(sin(x))]
+    typedef float T;
+    nt2::table<T> x, y, g(nt2::of_size(1));
+    load(x, read_file<T>(argv[3], n));
+    y = nt2::sin(x) + nt2::cos(x) * nt2::tan(x * T(0.25)) + nt2::cospi(x) * nt2::sinpi(x);
+    g(1) = nt2::globalsum(nt2::sin(x));
+    write_table(argv[4], y);
+    write_table(argv[5], g);
   } else if (cmd == "sigmadelta") {                       // n = pixels; argv[3] = frames; in: frames ; out: bkg var label
     typedef unsigned char T;
     const int nb_frames = std::atoi(argv[3]);

@@ -127,3 +127,38 @@ def test_stats_demo(demos, gpu, tmp_path):
         assert np.array_equal(g.view(np.uint32), e.view(np.uint32))
     gl = [h(gpu.reduce(op, Ad, rows, cols, 0))[0] for op in ("sum", "norm2", "max", "stdev")]
     assert np.array_equal(got[6].view(np.uint32), np.array(gl, np.float32).view(np.uint32))
+
+
+def test_trig_demo(demos, oracle, tmp_path):
+    """Trigonometric functors inside an NT2 statement (each node reduces its element on its own,
+    NT2's scalar code) and under a fold: the statement is bit-exact, the fold within its FP64 bound."""
+    n = 100003
+    x = np.random.default_rng(12).uniform(-60, 60, n).astype(np.float32)
+    _, (oy, og) = run(demos, tmp_path, "trig", n, [x], 2)
+    s = oracle.trig("sin", x)
+    c = oracle.trig("cos", x)
+    t = oracle.trig("tan", x * np.float32(0.25))
+    cp = oracle.trig("cospi", x)
+    sp = oracle.trig("sinpi", x)
+    want = (s + c * t) + cp * sp
+    got = np.fromfile(oy, np.float32)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    g = float(np.fromfile(og, np.float32)[0])
+    ref = float(np.sum(s.astype(np.float64)))
+    assert abs(g - ref) <= 4 * 2.0 ** -24 * float(np.sum(np.abs(s.astype(np.float64)))), (g, ref)
+
+
+def test_io_demo(demos, tmp_path):
+    """nt2cuda::load reads a table file written from Python, the statement runs on the device, and
+    nt2cuda::save writes the result back with its extent."""
+    from nt2_gb300 import tableio
+    rows, cols = 37, 1000
+    A = np.random.default_rng(4).standard_normal(rows * cols)
+    src, dst = tmp_path / "a.tbl", tmp_path / "b.tbl"
+    tableio.save(src, A, rows, cols)
+    r = subprocess.run([demos, "io", "0", str(src), str(dst)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.split() == [str(rows), str(cols)]
+    B, ext = tableio.load(dst)
+    assert ext == (rows, cols)
+    assert np.array_equal(B, A * 2.0 + 1.0)
