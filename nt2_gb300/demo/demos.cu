@@ -170,7 +170,7 @@ int main(int argc, char** argv)
     std::printf("%zu %zu\n", B.height(), B.width());
   } else if (cmd == "trig") {                             // n; in: x ; out: y, [globalsum(sin(x))]
     typedef float T;
-    nt2::table<T> x, y, g(nt2::of_size(1));
+    nt2::table<T> x(nt2::of_size(n)), y, g(nt2::of_size(1));
     load(x, read_file<T>(argv[3], n));
     y = nt2::sin(x) + nt2::cos(x) * nt2::tan(x * T(0.25)) + nt2::cospi(x) * nt2::sinpi(x);
     g(1) = nt2::globalsum(nt2::sin(x));
