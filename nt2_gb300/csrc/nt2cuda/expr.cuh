@@ -342,6 +342,17 @@ NT2CUDA_TRIG_REGS(sinpi_)
 NT2CUDA_TRIG_REGS(cospi_)
 #undef NT2CUDA_TRIG_REGS
 
+// prefetch_terms(e, i): L2 prefetch of element i of every table read by e.
+template <class T> __device__ __forceinline__ void prefetch_terms(const term<T>& t, size_t i) { mem::prefetch_l2(t.p + i); }
+template <class T> __device__ __forceinline__ void prefetch_terms(const scal<T>&, size_t) {}
+template <class Tag, class A> __device__ __forceinline__ void prefetch_terms(const node<Tag, A>& n, size_t i)
+{ prefetch_terms(n.a, i); }
+template <class Tag, class A, class B> __device__ __forceinline__ void prefetch_terms(const node<Tag, A, B>& n, size_t i)
+{ prefetch_terms(n.a, i); prefetch_terms(n.b, i); }
+template <class Tag, class A, class B, class C>
+__device__ __forceinline__ void prefetch_terms(const node<Tag, A, B, C>& n, size_t i)
+{ prefetch_terms(n.a, i); prefetch_terms(n.b, i); prefetch_terms(n.c, i); }
+
 // ------------------------------------------------------------- programs
 // prog<A0, A...>: the assigns of one statement, evaluated per index in order.
 template <class... As> struct prog;
@@ -367,6 +378,15 @@ template <class P> struct base_lanes {
   static constexpr int m = prog_min_elem<P>::value;
   static constexpr int value = m >= 16 ? 1 : 16 / m;
 };
+
+// L2 prefetch of element i of every table a program reads.
+template <class... As> __device__ __forceinline__ void prefetch_prog(const prog<As...>&, size_t) {}
+template <class T, class E, class... As>
+__device__ __forceinline__ void prefetch_prog(const prog<assign<T, E>, As...>& p, size_t i)
+{
+  prefetch_terms(p.head.e, i);
+  prefetch_prog(p.tail, i);
+}
 
 template <class P, int V> struct pregs;
 template <int V> struct pregs<prog<>, V> {
@@ -403,10 +423,14 @@ template <int U> struct transform_min_blocks { static constexpr int value = U ==
 template <bool F, int V, int U, class P>
 __global__ void __launch_bounds__(256, transform_min_blocks<U>::value) k_transform(P p, size_t n)
 {
-  nt2cuda::mem::pdl_begin();
   const size_t ngroups = n / V;
   const size_t T = (size_t)gridDim.x * blockDim.x;
   const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  // while the previous grid drains, have the L2 fetch this thread's first U groups
+#pragma unroll
+  for (int u = 0; u < U; ++u)
+    if (tid + (size_t)u * T < ngroups) prefetch_prog(p, (tid + (size_t)u * T) * V);
+  nt2cuda::mem::pdl_begin();
   size_t g = tid;
 #pragma unroll 1
   for (; g + (size_t)(U - 1) * T < ngroups; g += (size_t)U * T) {

@@ -243,10 +243,26 @@ template <class Op, int V, int U, class T, class E>
 __global__ void __launch_bounds__(256) k_inner(E e, inner_shape sh, out_of<Op, T>* __restrict__ out,
                                                state_of<Op, T>* __restrict__ partials, unsigned* __restrict__ counters)
 {
-  nt2cuda::mem::pdl_begin();
   const int lane = threadIdx.x & 31;
   const size_t warps_total = (size_t)gridDim.x * (blockDim.x >> 5);
   const size_t units = sh.cols * sh.splits;
+  {
+    // while the previous grid drains, have the L2 fetch the lines of this
+    // warp's first U loads (one prefetch per 128-byte line)
+    const size_t w = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    constexpr int LANES_PER_LINE = (V * (int)sizeof(T)) >= 128 ? 1 : 128 / (V * (int)sizeof(T));
+    if (w < units && V > 1 && lane % LANES_PER_LINE == 0) {
+      const size_t j = w / sh.splits, r0 = (w % sh.splits) * sh.seg;
+      const size_t r1 = (r0 + sh.seg < sh.rows) ? r0 + sh.seg : sh.rows;
+      const size_t g1 = r1 / V;
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const size_t g = r0 / V + lane + (size_t)u * 32;
+        if (g < g1) prefetch_terms(e, j * sh.rows + g * V);
+      }
+    }
+  }
+  nt2cuda::mem::pdl_begin();
   for (size_t w = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < units; w += warps_total) {
     const size_t j = w / sh.splits, sp = w % sh.splits;
     const size_t r0 = sp * sh.seg;
@@ -338,13 +354,31 @@ template <class Op, int V, int U, class T, class E>
 __global__ void __launch_bounds__(256) k_outer(E e, outer_shape sh, out_of<Op, T>* __restrict__ out,
                                                state_of<Op, T>* __restrict__ partials, unsigned* __restrict__ counters)
 {
-  nt2cuda::mem::pdl_begin();
   using S = state_of<Op, T>;
   constexpr int STRIP = 32 * V;
   __shared__ S red[8][STRIP];
   __shared__ unsigned is_last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const size_t units = sh.strips * sh.splits;
+  {
+    // while the previous grid drains, have the L2 fetch the lines of this
+    // warp's first U loads of its first unit (one prefetch per 128-byte line)
+    constexpr int LANES_PER_LINE = (V * (int)sizeof(T)) >= 128 ? 1 : 128 / (V * (int)sizeof(T));
+    const size_t b = blockIdx.x;
+    if (b < units && V > 1 && lane % LANES_PER_LINE == 0) {
+      const size_t strip = b / sh.splits, m0 = (b % sh.splits) * sh.cchunk;
+      const size_t row0 = strip * STRIP + (size_t)lane * V;
+      const size_t m1 = (m0 + sh.cchunk < sh.cols) ? m0 + sh.cchunk : sh.cols;
+      if (row0 + V <= sh.rows) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const size_t m = m0 + warp + (size_t)u * 8;
+          if (m < m1) prefetch_terms(e, m * sh.rows + row0);
+        }
+      }
+    }
+  }
+  nt2cuda::mem::pdl_begin();
   for (size_t b = blockIdx.x; b < units; b += gridDim.x) {
     const size_t strip = b / sh.splits, sp = b % sh.splits;
     const size_t row0 = strip * STRIP + (size_t)lane * V;   // first row of this lane

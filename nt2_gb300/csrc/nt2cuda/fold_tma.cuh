@@ -95,10 +95,22 @@ __global__ void __launch_bounds__(256) k_inner_tma(const T* __restrict__ x, cons
                                                    state_of<Op, T>* __restrict__ partials,
                                                    unsigned* __restrict__ counters)
 {
-  nt2cuda::mem::pdl_begin();
   using S = state_of<Op, T>;
   constexpr int TILE = inner_tile<T>();
   constexpr int V = 16 / (int)sizeof(T);
+  if (blockIdx.x < sh.units) {
+    // while the previous grid drains, have the L2 fetch the first STAGES tiles
+    // of this block's first unit (one prefetch per 128-byte line)
+    const size_t u = blockIdx.x, j = u / sh.splits, r0 = (u % sh.splits) * sh.seg;
+    const size_t rend = (r0 + sh.seg < sh.rows) ? r0 + sh.seg : sh.rows;
+    const size_t span = (rend - r0 < (size_t)STAGES * TILE) ? rend - r0 : (size_t)STAGES * TILE;
+    const size_t lines = (span * sizeof(T) + 127) / 128;
+    for (size_t q = threadIdx.x; q < lines; q += blockDim.x) {
+      nt2cuda::mem::prefetch_l2(reinterpret_cast<const char*>(x + j * sh.rows + r0) + q * 128);
+      if constexpr (NT == 2) nt2cuda::mem::prefetch_l2(reinterpret_cast<const char*>(y + j * sh.rows + r0) + q * 128);
+    }
+  }
+  nt2cuda::mem::pdl_begin();
   extern __shared__ __align__(128) unsigned char smem_raw[];
   T* buf = reinterpret_cast<T*>(smem_raw);          // [STAGES][NT][TILE]
   __shared__ __align__(8) uint64_t bar[STAGES];

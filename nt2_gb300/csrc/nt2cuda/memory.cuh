@@ -151,6 +151,16 @@ __device__ __forceinline__ void store_vec(T* base, size_t i, const T (&in)[V])
   }
 }
 
+// Ask the L2 for the 128-byte line holding p (no register result, no fault
+// path taken by the kernels: they only prefetch addresses they load).  It may
+// be issued before pdl_begin() for data the previous grid writes: the L2 is
+// the GPU's point of coherence for device memory, so a line fetched early is
+// updated by that grid's stores, and the loads after the wait see them.
+__device__ __forceinline__ void prefetch_l2(const void* p)
+{
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 // Kernels launched as programmatic dependents (launch.cuh) begin here: wait
 // until the previous grid on the stream has completed and its writes are
 // visible, then let the next grid be scheduled.
