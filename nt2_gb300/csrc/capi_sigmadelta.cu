@@ -87,27 +87,27 @@ __device__ __forceinline__ void sd_step1(uint8_t& b, uint8_t f, uint8_t& v, uint
   out = (d < v) ? 0 : 1;
 }
 
-__global__ void __launch_bounds__(SD_THREADS) k_sigmadelta(const sd_desc* __restrict__ desc,
+__global__ void __launch_bounds__(SD_THREADS, 4) k_sigmadelta(const sd_desc* __restrict__ desc,
                                                           const uint64_t* __restrict__ tile_start, int nstreams,
                                                           int nframes, int init)
 {
-  __shared__ int s_stream;
   const uint64_t total = tile_start[nstreams];
   const int first = init ? 1 : 0;
+  // Every thread finds its tile's stream itself (same addresses across the
+  // block, so the loads are broadcasts served by L1): tiles only move forward,
+  // so the search starts from the previous stream and needs no barrier.
+  int si = 0;
   for (uint64_t t = blockIdx.x; t < total; t += gridDim.x) {
-    if (threadIdx.x == 0) {
-      int lo = 0, hi = nstreams - 1;           // last stream with tile_start <= t
+    if (tile_start[si + 1] <= t) {
+      int lo = si + 1, hi = nstreams - 1;      // last stream with tile_start <= t
       while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
+        const int mid = (lo + hi + 1) >> 1;
         if (tile_start[mid] <= t) lo = mid; else hi = mid - 1;
       }
-      s_stream = lo;
+      si = lo;
     }
-    __syncthreads();
-    const int si = s_stream;            // read before the barrier that lets thread 0 move on
     const sd_desc d = desc[si];
     const uint64_t t0 = tile_start[si];
-    __syncthreads();
     const uint64_t p = (t - t0) * SD_TILE + (uint64_t)threadIdx.x * SD_PIX;
     if (p >= d.npix) continue;
     if (d.vec_ok && p + SD_PIX <= d.npix) {
@@ -159,21 +159,29 @@ __global__ void __launch_bounds__(SD_THREADS) k_sigmadelta(const sd_desc* __rest
                  make_uint4(ow[0], ow[1], ow[2], ow[3]));
         }
       }
-#pragma unroll 1
-      for (; k < nframes; ++k) {
-        const uint4 fq = __ldcs(reinterpret_cast<const uint4*>(d.frames + (uint64_t)k * d.frame_stride + p));
-        const uint32_t fw[4] = {fq.x, fq.y, fq.z, fq.w};
-        uint32_t ow[4];
+      if (k < nframes) {
+        // the last 1-3 frames as one batch: their loads in flight together
+        const int cnt = nframes - k;
+        uint4 f[3];
 #pragma unroll
-        for (int w = 0; w < 4; ++w) {
-          __half2 flo, fhi;
-          unpack_bytes(fw[w], flo, fhi);
-          const __half2 llo = sd_step_h2(b[2 * w], flo, v[2 * w]);
-          const __half2 lhi = sd_step_h2(b[2 * w + 1], fhi, v[2 * w + 1]);
-          ow[w] = pack_bytes(llo, lhi);
+        for (int q = 0; q < 3; ++q)
+          if (q < cnt) f[q] = __ldcs(reinterpret_cast<const uint4*>(d.frames + (uint64_t)(k + q) * d.frame_stride + p));
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          if (q >= cnt) break;
+          const uint32_t fw[4] = {f[q].x, f[q].y, f[q].z, f[q].w};
+          uint32_t ow[4];
+#pragma unroll
+          for (int w = 0; w < 4; ++w) {
+            __half2 flo, fhi;
+            unpack_bytes(fw[w], flo, fhi);
+            const __half2 llo = sd_step_h2(b[2 * w], flo, v[2 * w]);
+            const __half2 lhi = sd_step_h2(b[2 * w + 1], fhi, v[2 * w + 1]);
+            ow[w] = pack_bytes(llo, lhi);
+          }
+          __stcs(reinterpret_cast<uint4*>(d.labels + (uint64_t)(k + q - first) * d.label_stride + p),
+                 make_uint4(ow[0], ow[1], ow[2], ow[3]));
         }
-        __stcs(reinterpret_cast<uint4*>(d.labels + (uint64_t)(k - first) * d.label_stride + p),
-               make_uint4(ow[0], ow[1], ow[2], ow[3]));
       }
       const __half2 l1024 = __float2half2_rn(1024.0f);
       uint32_t bw[4], vw[4];
