@@ -116,7 +116,10 @@ enum {
   NT2CUDA_OP_COS = 13,
   NT2CUDA_OP_TAN = 14,
   NT2CUDA_OP_SINPI = 15,
-  NT2CUDA_OP_COSPI = 16
+  NT2CUDA_OP_COSPI = 16,
+  NT2CUDA_OP_ASIN = 17,       /* NT2's SIMD forms (simd/common/impl/invtrig) */
+  NT2CUDA_OP_ACOS = 18,
+  NT2CUDA_OP_ATAN = 19
 };
 
 /* Flags of nt2cuda_map_*. */

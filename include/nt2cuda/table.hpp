@@ -311,6 +311,9 @@ NT2CUDA_FN1(cos, cos_)
 NT2CUDA_FN1(tan, tan_)
 NT2CUDA_FN1(sinpi, sinpi_)
 NT2CUDA_FN1(cospi, cospi_)
+NT2CUDA_FN1(asin, asin_)
+NT2CUDA_FN1(acos, acos_)
+NT2CUDA_FN1(atan, atan_)
 NT2CUDA_FN1(sqrt, sqrt_)
 NT2CUDA_FN1(sqr, sqr_)
 NT2CUDA_FN1(erfc, erfc_)

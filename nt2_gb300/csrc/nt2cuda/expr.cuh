@@ -48,6 +48,7 @@ struct trunc_u8_ {};
 // (see regs<node<simd128_<...>>> below)
 struct sin_ {}; struct cos_ {}; struct tan_ {}; struct sinpi_ {}; struct cospi_ {};
 template <class T> struct simd128_ {};
+struct asin_ {}; struct acos_ {}; struct atan_ {};
 }  // namespace tag
 
 // ------------------------------------------------------------ tree nodes
@@ -145,6 +146,9 @@ NT2CUDA_UN(log1p_, math::log1p<F>(a))
 NT2CUDA_UN(erfc_, math::erfc<F>(a))
 NT2CUDA_UN(normcdf_, math::normcdf<F>(a))
 NT2CUDA_UN(fastnormcdf_, math::fastnormcdf<F>(a))
+NT2CUDA_UN(asin_, trig::asin<F>(a))
+NT2CUDA_UN(acos_, trig::acos<F>(a))
+NT2CUDA_UN(atan_, trig::atan<F>(a))
 // trunc_u8(y) = cast<uint8_t>(y) for a float y in [0, 256), where the cast truncates toward
 // zero: 2^23 + y rounded toward zero is 2^23 + floor(y), whose low byte is the result.
 // Used where the statement bounds y (rgb2grey's weights sum below 1); a full-rate add in

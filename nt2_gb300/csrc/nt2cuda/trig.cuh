@@ -581,6 +581,120 @@ template <int K, bool F, int P, class T> __device__ __forceinline__ void pack(co
   pack_impl<K, F, P, (P > 1)>(a, y);
 }
 
+// ------------------------------------------------- inverse functions
+// NT2's SIMD forms, element by element (no pack dependence):
+// functions/simd/common/impl/invtrig/f_invtrig.hpp:31-110 and d_invtrig.hpp:29-139.
+// seladd/ifadd/ifnotadd add a selected value (0 or c) unconditionally
+// (boost/simd/boolean/functions/simd/common/{seladd,ifnotadd}.hpp); fms(a,b,c) = a*b - c.
+struct tfi {
+  static constexpr uint32_t pio2lo = 0xb33bbd2eu, pio4lo = 0xb2bbbd2eu, tan3pio8 = 0x401a827au,
+                            tanpio8 = 0x3ed413cdu;
+};
+struct tdi {
+  static constexpr uint64_t pio2lo = 0x3c91a62633145c07ull, pio4lo = 0x3c81a62633145c07ull,
+                            tan3pio8 = 0x4003504f333f9de6ull, tanpio8 = 0x3fda827999fcef31ull,
+                            sqrteps = 0x3e50000000000000ull;
+};
+
+template <bool F> __device__ __forceinline__ float asin(float a0)
+{
+  constexpr uint32_t P[5] = {0x3d2cb352u, 0x3cc617e3u, 0x3d3a3ec7u, 0x3d9980f6u, 0x3e2aaae4u};
+  float x = fabsf(a0);
+  const bool larger = x > 0.5f;
+  float z = larger ? __fmul_rn(0.5f, __fsub_rn(1.0f, x)) : __fmul_rn(x, x);
+  x = larger ? __fsqrt_rn(z) : x;
+  float z1 = math::horner<F>(z, P);
+  z1 = math::madd<F>(z1, __fmul_rn(z, x), x);
+  z = larger ? __fsub_rn(fbits(tf::pio2), __fadd_rn(z1, z1)) : z1;
+  return flip(z, sign_of(a0));
+}
+template <bool F> __device__ __forceinline__ float acos(float a0)
+{
+  float x = fabsf(a0);
+  const bool larger = x > 0.5f;
+  x = larger ? __fsqrt_rn(math::madd<F>(-0.5f, x, 0.5f)) : a0;
+  x = asin<F>(x);
+  x = __fadd_rn(x, larger ? x : 0.0f);
+  x = (a0 < -0.5f) ? __fsub_rn(fbits(tf::pi), x) : x;
+  return larger ? x : __fsub_rn(fbits(tf::pio2), x);
+}
+template <bool F> __device__ __forceinline__ float atan(float a0)
+{
+  constexpr uint32_t P[4] = {0x3da4f0d1u, 0xbe0e1b85u, 0x3e4c925fu, 0xbeaaaa2au};
+  const float x = fabsf(a0);
+  const bool flag1 = x < fbits(tfi::tan3pio8);
+  const bool flag2 = flag1 && x >= fbits(tfi::tanpio8);
+  float yy = flag1 ? 0.0f : fbits(tf::pio2);
+  yy = flag2 ? fbits(tf::pio4) : yy;
+  float xx = flag1 ? x : -__fdiv_rn(1.0f, x);
+  xx = flag2 ? __fdiv_rn(__fsub_rn(x, 1.0f), __fadd_rn(x, 1.0f)) : xx;
+  const float z = __fmul_rn(xx, xx);
+  float z1 = math::madd<F>(xx, __fmul_rn(math::horner<F>(z, P), z), xx);
+  z1 = __fadd_rn(z1, flag2 ? fbits(tfi::pio4lo) : 0.0f);
+  z1 = __fadd_rn(z1, flag1 ? 0.0f : fbits(tfi::pio2lo));
+  return flip(__fadd_rn(yy, z1), sign_of(a0));
+}
+template <bool F> __device__ __forceinline__ double asin(double a0)
+{
+  constexpr uint64_t P1[5] = {0x3f684fc3988e9f08ull, 0xbfe2079259f9290full, 0x401bdff5baf33e6aull,
+                              0xc03991aaac01ab68ull, 0x403c896240f3081dull};
+  constexpr uint64_t Q1[5] = {0x3ff0000000000000ull, 0xc035f2a2b6bf5d8cull, 0x40626219af6a7f42ull,
+                              0xc077fe08959063eeull, 0x40756709b0b644beull};
+  constexpr uint64_t P2[6] = {0x3f716b9b0bd48ad3ull, 0xbfe34341333e5c16ull, 0x4015c74b178a2dd9ull,
+                              0xc0304331de27907bull, 0x40339007da779259ull, 0xc020656c06ceafd5ull};
+  constexpr uint64_t Q2[6] = {0x3ff0000000000000ull, 0xc02d7b590b5e0eabull, 0x40519fc025fe9054ull,
+                              0xc06265bb6d3576d7ull, 0x4061705684ffbf9dull, 0xc04898220a3607acull};
+  const double x = fabs(a0);
+  double r;
+  if (x < dbits(tdi::sqrteps)) {
+    r = x;
+  } else if (x > 0.625) {
+    double zz1 = __dsub_rn(1.0, x);
+    const double vp = __ddiv_rn(__dmul_rn(zz1, math::horner<F>(zz1, P1)), math::horner<F>(zz1, Q1));
+    zz1 = __dsqrt_rn(__dadd_rn(zz1, zz1));
+    double z = __dsub_rn(dbits(td::pio4), zz1);
+    zz1 = F ? __fma_rn(zz1, vp, -dbits(tdi::pio2lo)) : __dsub_rn(__dmul_rn(zz1, vp), dbits(tdi::pio2lo));
+    z = __dsub_rn(z, zz1);
+    r = __dadd_rn(z, dbits(td::pio4));
+  } else {
+    const double zz2 = __dmul_rn(a0, a0);
+    const double z = __ddiv_rn(__dmul_rn(zz2, math::horner<F>(zz2, P2)), math::horner<F>(zz2, Q2));
+    r = math::madd<F>(x, z, x);
+  }
+  if (x > 1.0) return __longlong_as_double(0x7ff8000000000000ll);
+  return flip(r, sign_of(a0));
+}
+template <bool F> __device__ __forceinline__ double acos(double a0)
+{
+  double x = fabs(a0);
+  const bool larger = x > 0.5;
+  x = larger ? __dsqrt_rn(math::madd<F>(-0.5, x, 0.5)) : a0;
+  x = asin<F>(x);
+  x = __dadd_rn(x, larger ? x : 0.0);
+  x = (a0 < -0.5) ? __dsub_rn(dbits(td::pi), x) : x;
+  return larger ? x : __dsub_rn(dbits(td::pio2), x);
+}
+template <bool F> __device__ __forceinline__ double atan(double a0)
+{
+  constexpr uint64_t P[5] = {0xbfec007fa1f72594ull, 0xc03028545b6b807aull, 0xc052c08c36880273ull,
+                             0xc05eb8bf2d05ba25ull, 0xc0503669fd28ec8eull};
+  constexpr uint64_t Q[6] = {0x3ff0000000000000ull, 0x4038dbc45b14603cull, 0x4064a0dd43b8fa25ull,
+                             0x407b0e18d2e2be3bull, 0x407e563f13b049eaull, 0x4068519efbbd62ecull};
+  const double x = fabs(a0);
+  const bool flag1 = x < dbits(tdi::tan3pio8);
+  const bool flag2 = flag1 && x >= dbits(tdi::tanpio8);
+  double yy = flag1 ? 0.0 : dbits(td::pio2);
+  yy = flag2 ? dbits(td::pio4) : yy;
+  double xx = flag1 ? x : -__ddiv_rn(1.0, x);
+  xx = flag2 ? __ddiv_rn(__dsub_rn(x, 1.0), __dadd_rn(x, 1.0)) : xx;
+  double z = __dmul_rn(xx, xx);
+  z = __ddiv_rn(__dmul_rn(z, math::horner<F>(z, P)), math::horner<F>(z, Q));
+  z = math::madd<F>(xx, z, xx);
+  z = __dadd_rn(z, flag2 ? dbits(tdi::pio4lo) : 0.0);
+  z = __dadd_rn(z, flag1 ? 0.0 : dbits(tdi::pio2lo));
+  return flip(__dadd_rn(yy, z), sign_of(a0));
+}
+
 // One element, NT2's scalar code (a pack of one).
 template <int K, bool F, class T> __device__ __forceinline__ T one(T a)
 {

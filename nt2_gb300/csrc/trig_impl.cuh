@@ -1,6 +1,6 @@
 // trig_impl.cuh -- the trigonometric functors of nt2cuda_map_f32/f64
-// (sin, cos, tan, sinpi, cospi), lowered onto the elementwise transform in
-// NT2's scalar form or its 128-bit SIMD form (nt2cuda/trig.cuh).  Included by
+// (sin, cos, tan, sinpi, cospi in NT2's scalar form or its 128-bit SIMD form;
+// asin, acos, atan), lowered onto the elementwise transform (nt2cuda/trig.cuh).  Included by
 // capi_trig_f32.cu and capi_trig_f64.cu, one element type each, which the
 // build compiles in parallel.
 #pragma once
@@ -33,12 +33,17 @@ template <bool F, bool SIMD, class T> nt2cuda_status trig_impl(int op, const T* 
     case NT2CUDA_OP_TAN: return run_trig<F, typename form<tag::tan_, SIMD>::type>(x, y, n, s);
     case NT2CUDA_OP_SINPI: return run_trig<F, typename form<tag::sinpi_, SIMD>::type>(x, y, n, s);
     case NT2CUDA_OP_COSPI: return run_trig<F, typename form<tag::cospi_, SIMD>::type>(x, y, n, s);
+    // the inverse functions do not depend on the pack: one form
+    case NT2CUDA_OP_ASIN: return SIMD ? NT2CUDA_ERR_ARG : run_trig<F, tag::asin_>(x, y, n, s);
+    case NT2CUDA_OP_ACOS: return SIMD ? NT2CUDA_ERR_ARG : run_trig<F, tag::acos_>(x, y, n, s);
+    case NT2CUDA_OP_ATAN: return SIMD ? NT2CUDA_ERR_ARG : run_trig<F, tag::atan_>(x, y, n, s);
     default: return NT2CUDA_ERR_ARG;
   }
 }
 
 template <class T> nt2cuda_status dispatch(int op, const T* x, T* y, size_t n, bool fused, bool simd, nt2cuda_stream s)
 {
+  if (op >= NT2CUDA_OP_ASIN) simd = false;   // no pack dependence: the flag changes nothing
   if (fused) return simd ? trig_impl<true, true>(op, x, y, n, s) : trig_impl<true, false>(op, x, y, n, s);
   return simd ? trig_impl<false, true>(op, x, y, n, s) : trig_impl<false, false>(op, x, y, n, s);
 }

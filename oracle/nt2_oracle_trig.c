@@ -1,6 +1,7 @@
 /*
  * nt2_oracle_trig.c -- CPU restatement of NT2's sine, cosine and tangent
- * (sin, cos, tan in radians; sinpi, cospi) for float and double.
+ * (sin, cos, tan in radians; sinpi, cospi) and of asin, acos, atan, for
+ * float and double.
  *
  * TEST INFRASTRUCTURE ONLY, like nt2_oracle.c: the parity checker of the
  * CUDA evaluator, never called by the product path.
@@ -458,7 +459,136 @@ static inline double tan_eval_d(double x)
   return x + x * (zz * (hornerd(zz, TAN_DN, 3) / hornerd(zz, TAN_DD, 5)));
 }
 
-enum { TRIG_SIN = 0, TRIG_COS = 1, TRIG_TAN = 2, TRIG_SINPI = 3, TRIG_COSPI = 4 };
+enum { TRIG_SIN = 0, TRIG_COS = 1, TRIG_TAN = 2, TRIG_SINPI = 3, TRIG_COSPI = 4,
+       TRIG_ASIN = 5, TRIG_ACOS = 6, TRIG_ATAN = 7 };
+
+/* ------------------------------------------------ inverse functions ----- */
+/* NT2's SIMD forms (functions/simd/common/impl/invtrig/{f,d}_invtrig.hpp), element by element
+ * (no pack dependence).  seladd/ifadd/ifnotadd are unconditional adds of a selected value
+ * (boost/simd/boolean/functions/simd/common/{seladd,ifnotadd}.hpp); fms(a,b,c) = a*b - c
+ * (boost/simd/arithmetic/functions/generic/fms.hpp).  NT2's scalar forms differ (float acos,
+ * double asin/acos/atan; functions/scalar/impl/invtrig/{f,d}_invtrig.hpp): not restated. */
+#define F_PIO2LO 0xb33bbd2eu
+#define F_PIO4LO 0xb2bbbd2eu
+#define F_TAN3PIO8 0x401a827au
+#define F_TANPIO8 0x3ed413cdu
+#define D_PIO2LO 0x3c91a62633145c07ull
+#define D_PIO4LO 0x3c81a62633145c07ull
+#define D_TAN3PIO8 0x4003504f333f9de6ull
+#define D_TANPIO8 0x3fda827999fcef31ull
+#define D_SQRTEPS 0x3e50000000000000ull
+
+static const uint32_t ASIN_F[5] = {0x3d2cb352u, 0x3cc617e3u, 0x3d3a3ec7u, 0x3d9980f6u, 0x3e2aaae4u};
+static const uint32_t ATAN_F[4] = {0x3da4f0d1u, 0xbe0e1b85u, 0x3e4c925fu, 0xbeaaaa2au};
+static const uint64_t ASIN_D_P1[5] = {0x3f684fc3988e9f08ull, 0xbfe2079259f9290full, 0x401bdff5baf33e6aull,
+                                      0xc03991aaac01ab68ull, 0x403c896240f3081dull};
+static const uint64_t ASIN_D_Q1[5] = {0x3ff0000000000000ull, 0xc035f2a2b6bf5d8cull, 0x40626219af6a7f42ull,
+                                      0xc077fe08959063eeull, 0x40756709b0b644beull};
+static const uint64_t ASIN_D_P2[6] = {0x3f716b9b0bd48ad3ull, 0xbfe34341333e5c16ull, 0x4015c74b178a2dd9ull,
+                                      0xc0304331de27907bull, 0x40339007da779259ull, 0xc020656c06ceafd5ull};
+static const uint64_t ASIN_D_Q2[6] = {0x3ff0000000000000ull, 0xc02d7b590b5e0eabull, 0x40519fc025fe9054ull,
+                                      0xc06265bb6d3576d7ull, 0x4061705684ffbf9dull, 0xc04898220a3607acull};
+static const uint64_t ATAN_D_P[5] = {0xbfec007fa1f72594ull, 0xc03028545b6b807aull, 0xc052c08c36880273ull,
+                                     0xc05eb8bf2d05ba25ull, 0xc0503669fd28ec8eull};
+static const uint64_t ATAN_D_Q[6] = {0x3ff0000000000000ull, 0x4038dbc45b14603cull, 0x4064a0dd43b8fa25ull,
+                                     0x407b0e18d2e2be3bull, 0x407e563f13b049eaull, 0x4068519efbbd62ecull};
+
+/* f_invtrig.hpp:31-57 */
+static float asin_f(float a0)
+{
+  float x = fabsf(a0);
+  const uint32_t sign = tbf(a0) & 0x80000000u;
+  const int larger = x > 0.5f;
+  float z = larger ? 0.5f * (1.0f - x) : x * x;
+  x = larger ? sqrtf(z) : x;
+  float z1 = hornerf(z, ASIN_F, 5);
+  z1 = z1 * (z * x) + x;
+  z = larger ? tfb(F_PIO2) - (z1 + z1) : z1;
+  return tfb(tbf(z) ^ sign);
+}
+/* f_invtrig.hpp:58-71 */
+static float acos_f(float a0)
+{
+  float x = fabsf(a0);
+  const int larger = x > 0.5f;
+  x = larger ? sqrtf(-0.5f * x + 0.5f) : a0;
+  x = asin_f(x);
+  x = x + (larger ? x : 0.0f);
+  x = (a0 < -0.5f) ? tfb(F_PI) - x : x;
+  return larger ? x : tfb(F_PIO2) - x;
+}
+/* f_invtrig.hpp:72-110 */
+static float atan_f(float a0)
+{
+  const float x = fabsf(a0);
+  const int flag1 = x < tfb(F_TAN3PIO8);
+  const int flag2 = x >= tfb(F_TANPIO8) && flag1;
+  float yy = flag1 ? 0.0f : tfb(F_PIO2);
+  yy = flag2 ? tfb(F_PIO4) : yy;
+  float xx = flag1 ? x : -(1.0f / x);
+  xx = flag2 ? (x - 1.0f) / (x + 1.0f) : xx;
+  const float z = xx * xx;
+  float z1 = hornerf(z, ATAN_F, 4);
+  z1 = xx * (z1 * z) + xx;
+  z1 = z1 + (flag2 ? tfb(F_PIO4LO) : 0.0f);
+  z1 = z1 + (flag1 ? 0.0f : tfb(F_PIO2LO));
+  return tfb(tbf(yy + z1) ^ (tbf(a0) & 0x80000000u));
+}
+/* d_invtrig.hpp:29-86 */
+static double asin_d(double a0)
+{
+  const double x = fabs(a0);
+  const int small = x < tdb(D_SQRTEPS);
+  double zz1 = 1.0 - x;
+  const double vp = zz1 * hornerd(zz1, ASIN_D_P1, 5) / hornerd(zz1, ASIN_D_Q1, 5);
+  zz1 = sqrt(zz1 + zz1);
+  double z = tdb(D_PIO4) - zz1;
+  zz1 = zz1 * vp - tdb(D_PIO2LO);
+  z = z - zz1;
+  zz1 = z + tdb(D_PIO4);
+  double zz2 = a0 * a0;
+  z = zz2 * hornerd(zz2, ASIN_D_P2, 6) / hornerd(zz2, ASIN_D_Q2, 6);
+  zz2 = x * z + x;
+  if (x > 1.0) return NAN;
+  const double r = small ? x : (x > 0.625 ? zz1 : zz2);
+  return tdb(tbd(r) ^ (tbd(a0) & 0x8000000000000000ull));
+}
+/* d_invtrig.hpp:87-97 */
+static double acos_d(double a0)
+{
+  double x = fabs(a0);
+  const int larger = x > 0.5;
+  x = larger ? sqrt(-0.5 * x + 0.5) : a0;
+  x = asin_d(x);
+  x = x + (larger ? x : 0.0);
+  x = (a0 < -0.5) ? tdb(D_PI) - x : x;
+  return larger ? x : tdb(D_PIO2) - x;
+}
+/* d_invtrig.hpp:98-139 */
+static double atan_d(double a0)
+{
+  const double x = fabs(a0);
+  const int flag1 = x < tdb(D_TAN3PIO8);
+  const int flag2 = x >= tdb(D_TANPIO8) && flag1;
+  double yy = flag1 ? 0.0 : tdb(D_PIO2);
+  yy = flag2 ? tdb(D_PIO4) : yy;
+  double xx = flag1 ? x : -(1.0 / x);
+  xx = flag2 ? (x - 1.0) / (x + 1.0) : xx;
+  double z = xx * xx;
+  z = z * hornerd(z, ATAN_D_P, 5) / hornerd(z, ATAN_D_Q, 6);
+  z = xx * z + xx;
+  z = z + (flag2 ? tdb(D_PIO4LO) : 0.0);
+  z = z + (flag1 ? 0.0 : tdb(D_PIO2LO));
+  return tdb(tbd(yy + z) ^ (tbd(a0) & 0x8000000000000000ull));
+}
+static inline float inv_f(int kind, float a)
+{
+  return kind == TRIG_ASIN ? asin_f(a) : (kind == TRIG_ACOS ? acos_f(a) : atan_f(a));
+}
+static inline double inv_d(int kind, double a)
+{
+  return kind == TRIG_ASIN ? asin_d(a) : (kind == TRIG_ACOS ? acos_d(a) : atan_d(a));
+}
 
 /* trig_base sina / cosa / tana (simd/common/impl/trigo/trig_base.hpp:49-92) */
 static inline float finish_f(int kind, float a0, float xr, int n)
@@ -541,7 +671,11 @@ static void trig_pack_d(int kind, const double* a, double* y, int k)
  * n % pack tail one element at a time (NT2's scalar code). */
 EXPORT int nt2o_trig_f(int kind, const float* x, float* y, size_t n, int pack)
 {
-  if (kind < 0 || kind > TRIG_COSPI || pack < 1 || pack > 8) return 1;
+  if (kind < 0 || kind > TRIG_ATAN || pack < 1 || pack > 8) return 1;
+  if (kind >= TRIG_ASIN) {
+    for (size_t i = 0; i < n; ++i) y[i] = inv_f(kind, x[i]);
+    return 0;
+  }
   size_t i = 0;
   for (; i + (size_t)pack <= n; i += (size_t)pack) trig_pack_f(kind, x + i, y + i, pack);
   for (; i < n; ++i) trig_pack_f(kind, x + i, y + i, 1);
@@ -549,7 +683,11 @@ EXPORT int nt2o_trig_f(int kind, const float* x, float* y, size_t n, int pack)
 }
 EXPORT int nt2o_trig_d(int kind, const double* x, double* y, size_t n, int pack)
 {
-  if (kind < 0 || kind > TRIG_COSPI || pack < 1 || pack > 8) return 1;
+  if (kind < 0 || kind > TRIG_ATAN || pack < 1 || pack > 8) return 1;
+  if (kind >= TRIG_ASIN) {
+    for (size_t i = 0; i < n; ++i) y[i] = inv_d(kind, x[i]);
+    return 0;
+  }
   size_t i = 0;
   for (; i + (size_t)pack <= n; i += (size_t)pack) trig_pack_d(kind, x + i, y + i, pack);
   for (; i < n; ++i) trig_pack_d(kind, x + i, y + i, 1);

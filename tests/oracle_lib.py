@@ -108,7 +108,7 @@ def max_ulp(a: np.ndarray, b: np.ndarray):
     return m, w.value
 
 
-TRIG = {"sin": 0, "cos": 1, "tan": 2, "sinpi": 3, "cospi": 4}
+TRIG = {"sin": 0, "cos": 1, "tan": 2, "sinpi": 3, "cospi": 4, "asin": 5, "acos": 6, "atan": 7}
 
 
 def trig(op: str, x: np.ndarray, pack: int = 1) -> np.ndarray:

@@ -1,9 +1,9 @@
-"""Pin the CPU oracle's sin, cos, tan, sinpi, cospi against NT2's own unit-test
-and cover-test values.
+"""Pin the CPU oracle's sin, cos, tan, sinpi, cospi, asin, acos, atan against
+NT2's own unit-test and cover-test values.
 
 Expected values and tolerances are NT2's, from
-modules/core/trigonometric/unit/scalar/{sin,cos,tan,sinpi,cospi}.cpp and
-modules/core/trigonometric/cover/scalar/{sin,cos,tan,sinpi,cospi}.cpp
+modules/core/trigonometric/unit/scalar/{sin,cos,tan,sinpi,cospi,asin,acos,atan}.cpp and
+modules/core/trigonometric/cover/scalar/{sin,cos,tan,sinpi,cospi,asin,acos,atan}.cpp
 (ranges and ulp bounds; the high-precision reference there is cephes long
 double, here FP64 for float results and mpmath for double results).  Tolerances
 are in NT2's ulpdist units (adjacent floats are 0.5 apart).
@@ -151,3 +151,40 @@ def test_rem_pio2_exact(oracle, dt):
     # sin(1e22), the classic check of an argument reduction
     y = oracle.trig("sin", np.array([1e22]), 1)[0]
     assert abs(y - (-0.8522008497671888)) <= 2.0 ** -53
+
+
+# inverse functions: modules/core/trigonometric/unit/scalar/{asin,acos,atan}.cpp
+INV_SPECIALS = {
+    "asin": [(INF, NAN, 0.5), (-INF, NAN, 0.5), (NAN, NAN, 0.5), (0.5, PI / 6, 0.5), (-0.5, -PI / 6, 0.5),
+             (-1.0, -PI / 2, 0.5), (1.0, PI / 2, 0.5), (0.0, 0.0, 0.5)],
+    "acos": [(INF, NAN, 0.0), (-INF, NAN, 0.0), (NAN, NAN, 0.0), (0.5, PI / 3, 0.5), (-0.5, 2 * PI / 3, 0.5),
+             (-1.0, PI, 0.0), (1.0, 0.0, 0.0), (0.0, PI / 2, 0.0)],
+    "atan": [(INF, PI / 2, 0.5), (-INF, -PI / 2, 0.5), (NAN, NAN, 0.5), (0.5, 4.636476090008061e-01, 0.5),
+             (-0.5, -4.636476090008061e-01, 0.5), (-1.0, -PI / 4, 0.5), (1.0, PI / 4, 0.5), (0.0, 0.0, 0.5)],
+}
+# modules/core/trigonometric/cover/scalar/{asin,acos,atan}.cpp: range and ulp bound
+INV_COVER = {"asin": (0.0, 1.0, 1.0), "acos": (0.0, 1.0, 0.5), "atan": (0.0, 100.0, 1.0)}
+
+
+@pytest.mark.parametrize("op", sorted(INV_SPECIALS))
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_invtrig_special_values(oracle, op, dt):
+    L = oracle.load()
+    u = _ulp(L, dt)
+    for x, r, tol in INV_SPECIALS[op]:
+        y = oracle.trig(op, np.array([x], dt))[0]
+        assert u(float(y), float(dt(r))) <= tol, (op, dt, x, y)
+
+
+@pytest.mark.parametrize("op", sorted(INV_COVER))
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_invtrig_cover(oracle, op, dt):
+    mpmath = pytest.importorskip("mpmath")
+    mpmath.mp.dps = 40
+    lo, hi, bound = INV_COVER[op]
+    n = 20000 if dt == np.float32 else 3000
+    x = np.random.default_rng(31).uniform(lo, hi, n).astype(dt)
+    f = {"asin": mpmath.asin, "acos": mpmath.acos, "atan": mpmath.atan}[op]
+    ref = np.array([float(f(mpmath.mpf(float(v)))) for v in x]).astype(dt)
+    m, w = oracle.max_ulp(oracle.trig(op, x), ref)
+    assert m <= bound, (op, dt, m, x[w])

@@ -121,3 +121,38 @@ def test_trig_table_sizes_large(gpu, oracle):
     xs = host(x)
     idx = np.random.default_rng(1).integers(0, n, 200000)
     assert same_bits(y[idx], oracle.trig("sin", np.ascontiguousarray(xs[idx]), 1)).size == 0
+
+
+INV = {"asin": 1.2, "acos": 1.2, "atan": 1e4}
+
+
+@pytest.mark.parametrize("op", sorted(INV))
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("n", [0, 1, 5, 97, (1 << 18) + 3])
+def test_invtrig_bit_exact(gpu, oracle, op, dtype, n):
+    """asin, acos, atan: NT2's SIMD forms element by element, bit-exact (NaN beyond [-1, 1])."""
+    rng = np.random.default_rng(n + 3)
+    lim = INV[op]
+    x = rng.uniform(-lim, lim, n)
+    if op == "atan" and n > 8:
+        x[: n // 2] = np.tan(rng.uniform(-1.5, 1.5, n // 2))
+    x = x.astype(dtype)
+    if n >= 64:
+        x[:12] = np.array([0.0, -0.0, 0.5, -0.5, 1.0, -1.0, np.inf, -np.inf, np.nan, 0.625, 0.41421356,
+                           2.4142135], dtype)
+    y = host(gpu.map_(op, to_dev(x)))
+    bad = same_bits(y, oracle.trig(op, x))
+    assert bad.size == 0, (op, dtype, bad[:5], x[bad[:5]], y[bad[:5]])
+    # the 128-bit flag changes nothing for the inverse functions
+    if n:
+        y2 = host(gpu.map_(op, to_dev(x), simd128=True))
+        assert same_bits(y2, y).size == 0
+
+
+@pytest.mark.parametrize("op", sorted(INV))
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_invtrig_fused_bound(gpu, oracle, op, dtype):
+    x = np.random.default_rng(2).uniform(-INV[op], INV[op], 100003).astype(dtype)
+    y = host(gpu.map_(op, to_dev(x), fused=True))
+    m, w = oracle.max_ulp(y, oracle.trig(op, x))
+    assert m <= 2.0, (op, dtype, m, x[w])
