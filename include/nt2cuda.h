@@ -295,6 +295,17 @@ nt2cuda_status nt2cuda_scan_f32(int op, const float* A, size_t rows, size_t cols
 nt2cuda_status nt2cuda_scan_f64(int op, const double* A, size_t rows, size_t cols, int dim, double* out, int flags,
                                 nt2cuda_stream stream);
 
+/* Scans of columns longer than one tile chain their tiles through bounded
+ * waits on each other's published prefixes.  A wait that runs out (well
+ * under a second; it means a fault) makes its tile write NaN and is counted:
+ * *count = waits that ran out since the library was loaded (synchronous). */
+nt2cuda_status nt2cuda_wait_timeouts(unsigned long long* count);
+/* Check that a wait which cannot be satisfied runs out and is reported: scans
+ * a two-tile column whose first tile no block takes.  Returns
+ * NT2CUDA_ERR_TIMEOUT when the kernel reported the timeout (the expected
+ * result, after about a second), NT2CUDA_OK if it did not. */
+nt2cuda_status nt2cuda_selftest_wait_timeout(nt2cuda_stream stream);
+
 /* --------------------------------------------------------- sigmadelta ---- */
 /* One grey video stream for the batched sigma-delta background subtraction
  * (demo/sigmadelta/nt2/sigmadelta_nt2.cpp:37-58, 85-106).  frames holds

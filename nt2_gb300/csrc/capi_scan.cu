@@ -50,4 +50,18 @@ nt2cuda_status nt2cuda_scan_f64(int op, const double* A, size_t rows, size_t col
   return scan_impl<double>(op, A, rows, cols, dim, out, flags, as_stream(s));
 }
 
+nt2cuda_status nt2cuda_wait_timeouts(unsigned long long* count)
+{
+  if (!count) return NT2CUDA_ERR_ARG;
+  return from_cuda(scan::wait_timeouts(count));
+}
+
+nt2cuda_status nt2cuda_selftest_wait_timeout(nt2cuda_stream s)
+{
+  unsigned failed = 0;
+  const nt2cuda_status st = from_cuda(scan::selftest_wait_timeout(as_stream(s), &failed));
+  if (st != NT2CUDA_OK) return st;
+  return failed ? NT2CUDA_ERR_TIMEOUT : NT2CUDA_OK;
+}
+
 }  // extern "C"

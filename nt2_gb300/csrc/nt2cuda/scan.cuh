@@ -45,7 +45,15 @@ constexpr int kWarps = 8;
 template <class T> __host__ __device__ constexpr int chunk_elems() { return 16 / (int)sizeof(T); }
 template <class T> __host__ __device__ constexpr int thread_elems() { return 8 * chunk_elems<T>(); }
 template <class T> __host__ __device__ constexpr int tile() { return kWarps * 32 * thread_elems<T>(); }
-constexpr unsigned kSpinMax = 1u << 22;          // bounded polls of one flag
+// Bounded polls of one flag: with the 64 ns sleeps and the load latency a
+// wait gives up after well under a second; a tile's predecessors are held by
+// running blocks that never wait on it, so a wait that runs out means a fault.
+constexpr unsigned kSpinMax = 1u << 20;
+
+// Look-back waits that ran out, over the life of the process (read by
+// nt2cuda_wait_timeouts); a tile whose wait runs out writes NaN and passes a
+// failure flag to its successors.
+static __device__ unsigned long long g_wait_timeouts = 0;
 
 enum : unsigned { F_NONE = 0, F_AGG = 1, F_INCL = 2, F_FAIL = 3 };
 
@@ -563,6 +571,7 @@ __global__ void __launch_bounds__(256) k_scan_inner(const T* __restrict__ x, T* 
         if (!ok && threadIdx.x == 0) {
           s_fail = 1;
           atomicOr(err, 1u);
+          atomicAdd(&g_wait_timeouts, 1ull);
         }
       }
     } else if (threadIdx.x == 0) {
@@ -694,6 +703,7 @@ __global__ void __launch_bounds__(256) k_scan_inner_1p(const T* __restrict__ x, 
         if (!ok && lane == 0) {
           s_fail = 1;
           atomicOr(err, 1u);
+          atomicAdd(&g_wait_timeouts, 1ull);
         }
       }
     } else if (threadIdx.x == 0) {

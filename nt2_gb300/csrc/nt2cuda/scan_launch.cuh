@@ -54,6 +54,54 @@ cudaError_t inner_scan(const T* x, T* y, size_t rows, size_t cols, cudaStream_t 
   return launch_dependent(k, grid, 256, s, args);
 }
 
+// Look-back waits that ran out since the library was loaded (synchronous).
+inline cudaError_t wait_timeouts(unsigned long long* count)
+{
+  return cudaMemcpyFromSymbol(count, g_wait_timeouts, sizeof(unsigned long long));
+}
+
+// A look-back wait that must run out: a two-tile column scanned with the
+// ticket counter started at 1, so the block that takes tile 1 waits for a tile
+// 0 that no block takes.  The kernel gives up after its bounded polls, writes
+// NaN over tile 1 and sets the error word, which is returned in *failed.
+inline cudaError_t selftest_wait_timeout(cudaStream_t s, unsigned* failed)
+{
+  using Op = fold::op_sum<true>;
+  using K = scan_tiles<Op, float>;
+  const size_t rows = 2 * K::TILE;
+  float* buf = nullptr;
+  char* scratch = nullptr;
+  const size_t head = 256, fbytes = 256, sbytes = align256(2 * carry_bytes<Op, float>());
+  cudaError_t e = cudaMalloc(&buf, rows * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&scratch, head + fbytes + 2 * sbytes);
+  if (e == cudaSuccess) e = cudaMemsetAsync(buf, 0, rows * sizeof(float), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(scratch, 0, head + fbytes, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(scratch, 1, 1, s);    // ticket = 1
+  if (e == cudaSuccess) {
+    inner_shape sh;
+    sh.rows = rows;
+    sh.cols = 1;
+    sh.tiles_per_col = 2;
+    sh.tiles = 2;
+    const float* x = buf;
+    float* y = buf;
+    int vec = 1;
+    unsigned long long* ticket = (unsigned long long*)scratch;
+    unsigned* err = (unsigned*)(scratch + 8);
+    unsigned* flags = (unsigned*)(scratch + head);
+    void* agg = scratch + head + fbytes;
+    void* incl = scratch + head + fbytes + sbytes;
+    void* args[] = {(void*)&x, (void*)&y, (void*)&sh, (void*)&vec, (void*)&ticket, (void*)&flags, (void*)&agg,
+                    (void*)&incl, (void*)&err};
+    e = launch_dependent(k_scan_inner<Op, float>, 2, 256, s, args);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(failed, err, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  }
+  if (buf) cudaFree(buf);
+  if (scratch) cudaFree(scratch);
+  return e;
+}
+
 template <class Op, class T, int V>
 cudaError_t outer_scan_v(const T* x, T* y, size_t rows, size_t cols, cudaStream_t s)
 {

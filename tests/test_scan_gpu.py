@@ -166,3 +166,30 @@ def test_scans_f64(gpu, dim):
     assert np.all(np.abs(got - r) <= 128 * 2.0 ** -53 * cabs)
     mx = back(np.maximum.accumulate(L, axis=1), rows, cols, dim)
     assert np.array_equal(host(gpu.cumulative("cummax", to_dev(A), rows, cols, dim)), mx)
+
+
+def test_no_wait_ran_out(cuda_lib):
+    """No look-back wait of the scans above ran out."""
+    import ctypes as C
+    c = C.c_ulonglong(99)
+    assert cuda_lib.nt2cuda_wait_timeouts(C.byref(c)) == 0
+    assert c.value == 0
+
+
+def test_wait_timeout_is_reported(gpu, cuda_lib):
+    """A wait that nothing satisfies runs out (bounded polls, under a second), the kernel
+    writes NaN over its tile and returns, the host reads NT2CUDA_ERR_TIMEOUT, and the context
+    stays usable."""
+    import ctypes as C
+    c0, c1, c2 = C.c_ulonglong(), C.c_ulonglong(), C.c_ulonglong()
+    assert cuda_lib.nt2cuda_wait_timeouts(C.byref(c0)) == 0
+    st = cuda_lib.nt2cuda_selftest_wait_timeout(torch.cuda.current_stream().cuda_stream)
+    assert st == 5                                        # NT2CUDA_ERR_TIMEOUT
+    assert cuda_lib.nt2cuda_wait_timeouts(C.byref(c1)) == 0
+    assert c1.value == c0.value + 1
+    n = 1 << 20
+    x = torch.empty(n, device="cuda")
+    gpu.fill_normal(x, 11)
+    check_cumsum(host(gpu.cumulative("cumsum", x, n, 1, 1)), host(x), n, 1, 1, True)
+    assert cuda_lib.nt2cuda_wait_timeouts(C.byref(c2)) == 0
+    assert c2.value == c1.value
