@@ -89,7 +89,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     if errs:
         raise RuntimeError("nvcc failed:\n" + "\n".join(errs))
     if _stale(LIB, objs):
-        cmd = [nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread"]
+        cmd = [nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread", "-ldl"]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

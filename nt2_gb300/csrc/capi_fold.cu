@@ -16,6 +16,7 @@ extern "C" {
 
 nt2cuda_status nt2cuda_globalsum_f32(const float* x, size_t n, float* out, int compensated, nt2cuda_stream s)
 {
+  NT2CUDA_NVTX_RANGE;
   if ((n && !x) || !out) return NT2CUDA_ERR_ARG;
   term<float> e{x};
   return launch_status(compensated ? nt2cuda::fold::inner_fold<fold::op_sum<true>, float>(e, n, 1, out, as_stream(s))
@@ -25,6 +26,7 @@ nt2cuda_status nt2cuda_globalsum_f32(const float* x, size_t n, float* out, int c
 nt2cuda_status nt2cuda_dot_f32(const float* x, const float* y, size_t n, float* out, int compensated,
                                nt2cuda_stream s)
 {
+  NT2CUDA_NVTX_RANGE;
   if ((n && (!x || !y)) || !out) return NT2CUDA_ERR_ARG;
   node<tag::multiplies_, term<float>, term<float>> e{term<float>{x}, term<float>{y}};
   return launch_status(compensated ? nt2cuda::fold::inner_fold<fold::op_sum<true>, float>(e, n, 1, out, as_stream(s))
@@ -33,12 +35,14 @@ nt2cuda_status nt2cuda_dot_f32(const float* x, const float* y, size_t n, float* 
 
 nt2cuda_status nt2cuda_globalsum_f64(const double* x, size_t n, double* out, nt2cuda_stream s)
 {
+  NT2CUDA_NVTX_RANGE;
   if ((n && !x) || !out) return NT2CUDA_ERR_ARG;
   return launch_status(nt2cuda::fold::inner_fold<fold::op_sum<false>, double>(term<double>{x}, n, 1, out, as_stream(s)));
 }
 
 nt2cuda_status nt2cuda_dot_f64(const double* x, const double* y, size_t n, double* out, nt2cuda_stream s)
 {
+  NT2CUDA_NVTX_RANGE;
   if ((n && (!x || !y)) || !out) return NT2CUDA_ERR_ARG;
   node<tag::multiplies_, term<double>, term<double>> e{term<double>{x}, term<double>{y}};
   return launch_status(nt2cuda::fold::inner_fold<fold::op_sum<false>, double>(e, n, 1, out, as_stream(s)));
@@ -47,6 +51,7 @@ nt2cuda_status nt2cuda_dot_f64(const double* x, const double* y, size_t n, doubl
 nt2cuda_status nt2cuda_sum_inner_f32(const float* A, size_t rows, size_t cols, float* out, int compensated,
                                      nt2cuda_stream s)
 {
+  NT2CUDA_NVTX_RANGE;
   if ((rows && cols && !A) || !out) return NT2CUDA_ERR_ARG;
   term<float> e{A};
   return launch_status(compensated ? nt2cuda::fold::inner_fold<fold::op_sum<true>, float>(e, rows, cols, out, as_stream(s))
@@ -55,6 +60,7 @@ nt2cuda_status nt2cuda_sum_inner_f32(const float* A, size_t rows, size_t cols, f
 
 nt2cuda_status nt2cuda_sum_inner_f64(const double* A, size_t rows, size_t cols, double* out, nt2cuda_stream s)
 {
+  NT2CUDA_NVTX_RANGE;
   if ((rows && cols && !A) || !out) return NT2CUDA_ERR_ARG;
   return launch_status(nt2cuda::fold::inner_fold<fold::op_sum<false>, double>(term<double>{A}, rows, cols, out, as_stream(s)));
 }
@@ -62,6 +68,7 @@ nt2cuda_status nt2cuda_sum_inner_f64(const double* A, size_t rows, size_t cols, 
 nt2cuda_status nt2cuda_sum_outer_f32(const float* A, size_t rows, size_t cols, float* out, int compensated,
                                      nt2cuda_stream s)
 {
+  NT2CUDA_NVTX_RANGE;
   if ((rows && cols && !A) || !out) return NT2CUDA_ERR_ARG;
   term<float> e{A};
   return launch_status(compensated ? nt2cuda::fold::outer_fold<fold::op_sum<true>, float>(e, rows, cols, out, as_stream(s))
@@ -70,6 +77,7 @@ nt2cuda_status nt2cuda_sum_outer_f32(const float* A, size_t rows, size_t cols, f
 
 nt2cuda_status nt2cuda_sum_outer_f64(const double* A, size_t rows, size_t cols, double* out, nt2cuda_stream s)
 {
+  NT2CUDA_NVTX_RANGE;
   if ((rows && cols && !A) || !out) return NT2CUDA_ERR_ARG;
   return launch_status(nt2cuda::fold::outer_fold<fold::op_sum<false>, double>(term<double>{A}, rows, cols, out, as_stream(s)));
 }

@@ -117,6 +117,7 @@ extern "C" {
 nt2cuda_status nt2cuda_mandelbrot_f32(const float* A, const float* B, int32_t* C, size_t n, int pack,
                                       nt2cuda_stream stream)
 {
+  NT2CUDA_NVTX_RANGE;
   if (!pack_ok(pack) || (n && (!A || !B || !C))) return NT2CUDA_ERR_ARG;
   const uintptr_t c0 = (uintptr_t)C, c1 = c0 + n * 4;
   for (const float* p : {A, B}) {
@@ -129,6 +130,7 @@ nt2cuda_status nt2cuda_mandelbrot_f32(const float* A, const float* B, int32_t* C
 nt2cuda_status nt2cuda_mandelbrot_grid_f32(float a0, float a1, float b0, float b1, size_t h, size_t w,
                                            int32_t* C, int pack, nt2cuda_stream stream)
 {
+  NT2CUDA_NVTX_RANGE;
   if (!pack_ok(pack) || (h && w && !C)) return NT2CUDA_ERR_ARG;
   if (!h || !w) return NT2CUDA_OK;
   grid g{};

@@ -41,12 +41,14 @@ extern "C" {
 nt2cuda_status nt2cuda_scan_f32(int op, const float* A, size_t rows, size_t cols, int dim, float* out, int flags,
                                 nt2cuda_stream s)
 {
+  NT2CUDA_NVTX_RANGE;
   return scan_impl<float>(op, A, rows, cols, dim, out, flags, as_stream(s));
 }
 
 nt2cuda_status nt2cuda_scan_f64(int op, const double* A, size_t rows, size_t cols, int dim, double* out, int flags,
                                 nt2cuda_stream s)
 {
+  NT2CUDA_NVTX_RANGE;
   return scan_impl<double>(op, A, rows, cols, dim, out, flags, as_stream(s));
 }
 

@@ -284,6 +284,7 @@ extern "C" {
 nt2cuda_status nt2cuda_sigmadelta_batch_u8(const nt2cuda_sd_stream* streams, int nstreams, int nframes, int init,
                                            nt2cuda_stream stream)
 {
+  NT2CUDA_NVTX_RANGE;
   host_batch hb;
   nt2cuda_status st = build_batch(streams, nstreams, nframes, init, hb);
   if (st != NT2CUDA_OK) return st;
@@ -341,6 +342,7 @@ nt2cuda_status nt2cuda_sigmadelta_plan_create(const nt2cuda_sd_stream* streams, 
 
 nt2cuda_status nt2cuda_sigmadelta_plan_launch(nt2cuda_sd_plan* plan, nt2cuda_stream stream)
 {
+  NT2CUDA_NVTX_RANGE;
   if (!plan || !plan->exec) return NT2CUDA_ERR_ARG;
   return from_cuda(cudaGraphLaunch(plan->exec, as_stream(stream)), NT2CUDA_ERR_LAUNCH);
 }

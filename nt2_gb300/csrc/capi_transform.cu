@@ -258,6 +258,7 @@ extern "C" {
 
 nt2cuda_status nt2cuda_map_f32(int op, const float* x, float* y, size_t n, int flags, nt2cuda_stream s)
 {
+  NT2CUDA_NVTX_RANGE;
   if (n && (!x || !y)) return NT2CUDA_ERR_ARG;
   if (flags & ~(NT2CUDA_MAP_FUSED | NT2CUDA_MAP_SIMD128)) return NT2CUDA_ERR_ARG;
   const bool fused = (flags & NT2CUDA_MAP_FUSED) != 0;
@@ -268,6 +269,7 @@ nt2cuda_status nt2cuda_map_f32(int op, const float* x, float* y, size_t n, int f
 
 nt2cuda_status nt2cuda_map_f64(int op, const double* x, double* y, size_t n, int flags, nt2cuda_stream s)
 {
+  NT2CUDA_NVTX_RANGE;
   if (n && (!x || !y)) return NT2CUDA_ERR_ARG;
   if (flags & ~(NT2CUDA_MAP_FUSED | NT2CUDA_MAP_SIMD128)) return NT2CUDA_ERR_ARG;
   const bool fused = (flags & NT2CUDA_MAP_FUSED) != 0;
@@ -278,12 +280,14 @@ nt2cuda_status nt2cuda_map_f64(int op, const double* x, double* y, size_t n, int
 
 nt2cuda_status nt2cuda_saxpy_f32(float a, const float* x, float* y, size_t n, int fused, nt2cuda_stream s)
 {
+  NT2CUDA_NVTX_RANGE;
   if (n && (!x || !y)) return NT2CUDA_ERR_ARG;
   return fused ? saxpy_impl<true>(a, x, y, n, s) : saxpy_impl<false>(a, x, y, n, s);
 }
 
 nt2cuda_status nt2cuda_saxpy_f64(double a, const double* x, double* y, size_t n, int fused, nt2cuda_stream s)
 {
+  NT2CUDA_NVTX_RANGE;
   if (n && (!x || !y)) return NT2CUDA_ERR_ARG;
   return fused ? saxpy_impl<true>(a, x, y, n, s) : saxpy_impl<false>(a, x, y, n, s);
 }
@@ -291,6 +295,7 @@ nt2cuda_status nt2cuda_saxpy_f64(double a, const double* x, double* y, size_t n,
 nt2cuda_status nt2cuda_rgb2grey_f32(const float* r, const float* g, const float* b, float* gr, size_t n,
                                     int fused, nt2cuda_stream s)
 {
+  NT2CUDA_NVTX_RANGE;
   if (n && (!r || !g || !b || !gr)) return NT2CUDA_ERR_ARG;
   return fused ? rgb2grey_impl<true>(r, g, b, gr, n, s) : rgb2grey_impl<false>(r, g, b, gr, n, s);
 }
@@ -298,6 +303,7 @@ nt2cuda_status nt2cuda_rgb2grey_f32(const float* r, const float* g, const float*
 nt2cuda_status nt2cuda_rgb2grey_u8(const uint8_t* r, const uint8_t* g, const uint8_t* b, uint8_t* gr, size_t n,
                                    int fused, nt2cuda_stream s)
 {
+  NT2CUDA_NVTX_RANGE;
   if (n && (!r || !g || !b || !gr)) return NT2CUDA_ERR_ARG;
   return fused ? rgb2grey_u8_impl<true>(r, g, b, gr, n, s) : rgb2grey_u8_impl<false>(r, g, b, gr, n, s);
 }
@@ -305,6 +311,7 @@ nt2cuda_status nt2cuda_rgb2grey_u8(const uint8_t* r, const uint8_t* g, const uin
 nt2cuda_status nt2cuda_rgb2yuv_f32(const float* r, const float* g, const float* b, float* y, float* u, float* v,
                                    size_t n, int fused, nt2cuda_stream s)
 {
+  NT2CUDA_NVTX_RANGE;
   if (n && (!r || !g || !b || !y || !u || !v)) return NT2CUDA_ERR_ARG;
   return fused ? rgb2yuv_impl<true>(r, g, b, y, u, v, n, as_stream(s))
                : rgb2yuv_impl<false>(r, g, b, y, u, v, n, as_stream(s));
@@ -313,6 +320,7 @@ nt2cuda_status nt2cuda_rgb2yuv_f32(const float* r, const float* g, const float* 
 nt2cuda_status nt2cuda_blackscholes_demo_f32(const float* S, const float* X, const float* T, const float* r,
                                              const float* v, float* R, size_t n, int fused, nt2cuda_stream s)
 {
+  NT2CUDA_NVTX_RANGE;
   if (n && (!S || !X || !T || !r || !v || !R)) return NT2CUDA_ERR_ARG;
   return fused ? bs_demo_impl<true>(S, X, T, r, v, R, n, s) : bs_demo_impl<false>(S, X, T, r, v, R, n, s);
 }
@@ -321,6 +329,7 @@ nt2cuda_status nt2cuda_blackscholes_f32(const float* S, const float* K, const fl
                                         float* call, float* put, size_t n, int cdf_kind, int fused,
                                         nt2cuda_stream s)
 {
+  NT2CUDA_NVTX_RANGE;
   tuning::params p = tuning::lookup(bs_key(4, fused), n);
   return bs_dispatch<float>(S, K, T, r, sigma, call, put, n, cdf_kind, fused, as_stream(s), p.unroll, p.waves);
 }
@@ -329,6 +338,7 @@ nt2cuda_status nt2cuda_blackscholes_f64(const double* S, const double* K, const 
                                         double sigma, double* call, double* put, size_t n, int fused,
                                         nt2cuda_stream s)
 {
+  NT2CUDA_NVTX_RANGE;
   tuning::params p = tuning::lookup(bs_key(8, fused), n);
   return bs_dispatch<double>(S, K, T, r, sigma, call, put, n, CDF_NORMCDF, fused, as_stream(s), p.unroll,
                              p.waves);
@@ -370,6 +380,7 @@ nt2cuda_status nt2cuda_blackscholes_f32_host(const float* S, const float* K, con
                                              float sigma, float* call, float* put, size_t n, int cdf_kind,
                                              int fused)
 {
+  NT2CUDA_NVTX_RANGE;
   if (n == 0) return NT2CUDA_OK;
   if (!S || !K || !T || !call || !put) return NT2CUDA_ERR_ARG;
   host_pipeline& P = hp();

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <mutex>
 #include <unordered_map>
+#include <nvtx3/nvToolsExt.h>
 #include "../../include/nt2cuda.h"
 #include "nt2cuda/scratch.cuh"
 
@@ -10,6 +11,16 @@ namespace nt2cuda {
 namespace detail_capi {
 
 inline cudaStream_t as_stream(nt2cuda_stream s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// An NVTX range named after the C-ABI entry point around its body, so that
+// Nsight tools attribute the launches to the call (no cost without a tool).
+struct nvtx_range {
+  explicit nvtx_range(const char* name) { nvtxRangePushA(name); }
+  ~nvtx_range() { nvtxRangePop(); }
+  nvtx_range(const nvtx_range&) = delete;
+  nvtx_range& operator=(const nvtx_range&) = delete;
+};
+#define NT2CUDA_NVTX_RANGE ::nt2cuda::detail_capi::nvtx_range nt2cuda_nvtx_range_(__func__)
 
 // Remember the last CUDA error code seen by an entry point.
 inline int& last_cuda_error() { static thread_local int e = 0; return e; }
