@@ -122,6 +122,14 @@ enum {
   NT2CUDA_OP_ATAN = 19
 };
 
+/* out = atan2(a0, a1) elementwise (NT2's SIMD form,
+ * modules/core/trigonometric/include/nt2/trigonometric/functions/simd/common/atan2.hpp:31-52;
+ * atan2(+-0, a1 < 0) is +pi, as there).  flags: NT2CUDA_MAP_FUSED or 0. */
+nt2cuda_status nt2cuda_atan2_f32(const float* a0, const float* a1, float* out, size_t n, int flags,
+                                 nt2cuda_stream stream);
+nt2cuda_status nt2cuda_atan2_f64(const double* a0, const double* a1, double* out, size_t n, int flags,
+                                 nt2cuda_stream stream);
+
 /* Flags of nt2cuda_map_*. */
 #define NT2CUDA_MAP_FUSED 1     /* hardware FMA (the `fused` convention above) */
 #define NT2CUDA_MAP_SIMD128 2   /* trigonometric ops: 128-bit pack reductions  */

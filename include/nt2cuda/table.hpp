@@ -329,6 +329,7 @@ NT2CUDA_FN1(minusone, minusone_)
   template <class A, class B, std::enable_if_t<is_operand_v<A> || is_operand_v<B>, int> = 0> \
   inline auto NAME(const A& a, const B& b) { return make_binary<tag::TAG>(a, b); }
 NT2CUDA_FN2(max, max_)
+NT2CUDA_FN2(atan2, atan2_)
 NT2CUDA_FN2(min, min_)
 NT2CUDA_FN2(adds, adds_)
 NT2CUDA_FN2(subs, subs_)

@@ -48,7 +48,7 @@ struct trunc_u8_ {};
 // (see regs<node<simd128_<...>>> below)
 struct sin_ {}; struct cos_ {}; struct tan_ {}; struct sinpi_ {}; struct cospi_ {};
 template <class T> struct simd128_ {};
-struct asin_ {}; struct acos_ {}; struct atan_ {};
+struct asin_ {}; struct acos_ {}; struct atan_ {}; struct atan2_ {};
 }  // namespace tag
 
 // ------------------------------------------------------------ tree nodes
@@ -128,6 +128,7 @@ NT2CUDA_BIN(is_not_equal_, (bool)(a != b))
 // (boost/simd/boolean/functions/scalar/selinc.hpp:27, seldec.hpp:27)
 NT2CUDA_BIN(selinc_, (a ? (B)(b + 1) : b))
 NT2CUDA_BIN(seldec_, (a ? (B)(b - 1) : b))
+NT2CUDA_BIN(atan2_, trig::atan2<F>(a, (A)b))
 NT2CUDA_UN(unary_minus_, (A)(-a))
 NT2CUDA_UN(sqr_, detail::mul(a, a))
 NT2CUDA_UN(sqrt_, math::sqrt_(a))

@@ -618,7 +618,8 @@ template <bool F> __device__ __forceinline__ float acos(float a0)
   x = (a0 < -0.5f) ? __fsub_rn(fbits(tf::pi), x) : x;
   return larger ? x : __fsub_rn(fbits(tf::pio2), x);
 }
-template <bool F> __device__ __forceinline__ float atan(float a0)
+// atan(|a0|)
+template <bool F> __device__ __forceinline__ float kernel_atan(float a0)
 {
   constexpr uint32_t P[4] = {0x3da4f0d1u, 0xbe0e1b85u, 0x3e4c925fu, 0xbeaaaa2au};
   const float x = fabsf(a0);
@@ -632,8 +633,9 @@ template <bool F> __device__ __forceinline__ float atan(float a0)
   float z1 = math::madd<F>(xx, __fmul_rn(math::horner<F>(z, P), z), xx);
   z1 = __fadd_rn(z1, flag2 ? fbits(tfi::pio4lo) : 0.0f);
   z1 = __fadd_rn(z1, flag1 ? 0.0f : fbits(tfi::pio2lo));
-  return flip(__fadd_rn(yy, z1), sign_of(a0));
+  return __fadd_rn(yy, z1);
 }
+template <bool F> __device__ __forceinline__ float atan(float a0) { return flip(kernel_atan<F>(a0), sign_of(a0)); }
 template <bool F> __device__ __forceinline__ double asin(double a0)
 {
   constexpr uint64_t P1[5] = {0x3f684fc3988e9f08ull, 0xbfe2079259f9290full, 0x401bdff5baf33e6aull,
@@ -674,7 +676,8 @@ template <bool F> __device__ __forceinline__ double acos(double a0)
   x = (a0 < -0.5) ? __dsub_rn(dbits(td::pi), x) : x;
   return larger ? x : __dsub_rn(dbits(td::pio2), x);
 }
-template <bool F> __device__ __forceinline__ double atan(double a0)
+// atan(|a0|)
+template <bool F> __device__ __forceinline__ double kernel_atan(double a0)
 {
   constexpr uint64_t P[5] = {0xbfec007fa1f72594ull, 0xc03028545b6b807aull, 0xc052c08c36880273ull,
                              0xc05eb8bf2d05ba25ull, 0xc0503669fd28ec8eull};
@@ -692,7 +695,26 @@ template <bool F> __device__ __forceinline__ double atan(double a0)
   z = math::madd<F>(xx, z, xx);
   z = __dadd_rn(z, flag2 ? dbits(tdi::pio4lo) : 0.0);
   z = __dadd_rn(z, flag1 ? 0.0 : dbits(tdi::pio2lo));
-  return flip(__dadd_rn(yy, z), sign_of(a0));
+  return __dadd_rn(yy, z);
+}
+template <bool F> __device__ __forceinline__ double atan(double a0) { return flip(kernel_atan<F>(a0), sign_of(a0)); }
+
+// atan2(a0, a1), NT2's SIMD form (functions/simd/common/atan2.hpp:31-52): both
+// infinite -> +-1 each; kernel_atan(a0/a1); Pi minus it unless a1 > 0; the sign
+// of a0 (negatenz: -0 counts as negative); a0 == 0 -> (a1 < 0 ? Pi : 0); NaN if
+// either argument is NaN.
+template <bool F, class T> __device__ __forceinline__ T atan2(T a0, T a1)
+{
+  const T pi = sizeof(T) == 4 ? (T)fbits(tf::pi) : (T)dbits(td::pi);
+  if (isinf(a0) && isinf(a1)) {
+    a0 = copysign(T(1), a0);
+    a1 = copysign(T(1), a1);
+  }
+  T z = kernel_atan<F>(math::div(a0, a1));
+  z = (a1 > T(0)) ? z : math::sub(pi, z);
+  z = flip(z, sign_of(a0));
+  z = (a0 == T(0)) ? ((a1 < T(0)) ? pi : T(0)) : z;
+  return (isnan(a0) || isnan(a1)) ? (T)NAN : z;
 }
 
 // One element, NT2's scalar code (a pack of one).

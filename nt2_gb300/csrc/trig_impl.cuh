@@ -48,6 +48,13 @@ template <class T> nt2cuda_status dispatch(int op, const T* x, T* y, size_t n, b
   return simd ? trig_impl<false, true>(op, x, y, n, s) : trig_impl<false, false>(op, x, y, n, s);
 }
 
+template <class T> nt2cuda_status atan2_impl(const T* a0, const T* a1, T* y, size_t n, bool fused, nt2cuda_stream s)
+{
+  using N = node<tag::atan2_, term<T>, term<T>>;
+  auto p = make_prog(assign<T, N>{y, N{term<T>{a0}, term<T>{a1}}});
+  return launch_status(fused ? transform<true>(p, n, as_stream(s), "trig") : transform<false>(p, n, as_stream(s), "trig"));
+}
+
 }  // namespace
 
 }  // namespace detail_capi

@@ -517,8 +517,8 @@ static float acos_f(float a0)
   x = (a0 < -0.5f) ? tfb(F_PI) - x : x;
   return larger ? x : tfb(F_PIO2) - x;
 }
-/* f_invtrig.hpp:72-110 */
-static float atan_f(float a0)
+/* f_invtrig.hpp:78-110: atan(|a0|) */
+static float kernel_atan_f(float a0)
 {
   const float x = fabsf(a0);
   const int flag1 = x < tfb(F_TAN3PIO8);
@@ -532,8 +532,10 @@ static float atan_f(float a0)
   z1 = xx * (z1 * z) + xx;
   z1 = z1 + (flag2 ? tfb(F_PIO4LO) : 0.0f);
   z1 = z1 + (flag1 ? 0.0f : tfb(F_PIO2LO));
-  return tfb(tbf(yy + z1) ^ (tbf(a0) & 0x80000000u));
+  return yy + z1;
 }
+/* f_invtrig.hpp:72-77 */
+static float atan_f(float a0) { return tfb(tbf(kernel_atan_f(a0)) ^ (tbf(a0) & 0x80000000u)); }
 /* d_invtrig.hpp:29-86 */
 static double asin_d(double a0)
 {
@@ -564,8 +566,8 @@ static double acos_d(double a0)
   x = (a0 < -0.5) ? tdb(D_PI) - x : x;
   return larger ? x : tdb(D_PIO2) - x;
 }
-/* d_invtrig.hpp:98-139 */
-static double atan_d(double a0)
+/* d_invtrig.hpp:104-139: atan(|a0|) */
+static double kernel_atan_d(double a0)
 {
   const double x = fabs(a0);
   const int flag1 = x < tdb(D_TAN3PIO8);
@@ -579,7 +581,39 @@ static double atan_d(double a0)
   z = xx * z + xx;
   z = z + (flag2 ? tdb(D_PIO4LO) : 0.0);
   z = z + (flag1 ? 0.0 : tdb(D_PIO2LO));
-  return tdb(tbd(yy + z) ^ (tbd(a0) & 0x8000000000000000ull));
+  return yy + z;
+}
+/* d_invtrig.hpp:98-103 */
+static double atan_d(double a0) { return tdb(tbd(kernel_atan_d(a0)) ^ (tbd(a0) & 0x8000000000000000ull)); }
+
+/* atan2(a0, a1), NT2's SIMD form (functions/simd/common/atan2.hpp:31-52): both infinite
+ * -> +-1 each; kernel_atan(a0/a1); Pi minus it unless a1 > 0; the sign of a0 (negatenz,
+ * -0 counts as negative); a0 == 0 -> (a1 < 0 ? Pi : 0); NaN if either is NaN. */
+static float atan2_f(float a0, float a1)
+{
+  if (isinf(a0) && isinf(a1)) { a0 = copysignf(1.0f, a0); a1 = copysignf(1.0f, a1); }
+  float z = kernel_atan_f(a0 / a1);
+  z = (a1 > 0.0f) ? z : tfb(F_PI) - z;
+  z = (tbf(a0) & 0x80000000u) ? -z : z;
+  z = (a0 == 0.0f) ? ((a1 < 0.0f) ? tfb(F_PI) : 0.0f) : z;
+  return (isnan(a0) || isnan(a1)) ? NAN : z;
+}
+static double atan2_d(double a0, double a1)
+{
+  if (isinf(a0) && isinf(a1)) { a0 = copysign(1.0, a0); a1 = copysign(1.0, a1); }
+  double z = kernel_atan_d(a0 / a1);
+  z = (a1 > 0.0) ? z : tdb(D_PI) - z;
+  z = (tbd(a0) & 0x8000000000000000ull) ? -z : z;
+  z = (a0 == 0.0) ? ((a1 < 0.0) ? tdb(D_PI) : 0.0) : z;
+  return (isnan(a0) || isnan(a1)) ? NAN : z;
+}
+EXPORT void nt2o_atan2_f(const float* a0, const float* a1, float* y, size_t n)
+{
+  for (size_t i = 0; i < n; ++i) y[i] = atan2_f(a0[i], a1[i]);
+}
+EXPORT void nt2o_atan2_d(const double* a0, const double* a1, double* y, size_t n)
+{
+  for (size_t i = 0; i < n; ++i) y[i] = atan2_d(a0[i], a1[i]);
 }
 static inline float inv_f(int kind, float a)
 {

@@ -188,3 +188,33 @@ def test_invtrig_cover(oracle, op, dt):
     ref = np.array([float(f(mpmath.mpf(float(v)))) for v in x]).astype(dt)
     m, w = oracle.max_ulp(oracle.trig(op, x), ref)
     assert m <= bound, (op, dt, m, x[w])
+
+
+# atan2: modules/core/trigonometric/unit/scalar/atan2.cpp (values, 0.5 ulp) and
+# cover/scalar/atan2.cpp (both arguments in [0, 1], 1 ulp)
+ATAN2_SPECIALS = [(INF, INF, PI / 4), (INF, 1.0, PI / 2), (-INF, -INF, -3 * PI / 4), (-INF, 1.0, -PI / 2),
+                  (NAN, NAN, NAN), (NAN, 0.0, NAN), (0.0, NAN, NAN), (1.0, INF, 0.0), (1.0, -INF, PI),
+                  (0.5, 0.5, PI / 4), (-0.5, -0.5, -3 * PI / 4), (-1.0, -1.0, -3 * PI / 4), (1.0, 1.0, PI / 4),
+                  (0.0, 0.0, 0.0)]
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_atan2_special_values(oracle, dt):
+    L = oracle.load()
+    u = _ulp(L, dt)
+    for a, b, r in ATAN2_SPECIALS:
+        y = oracle.atan2(np.array([a], dt), np.array([b], dt))[0]
+        assert u(float(y), float(dt(r))) <= 0.5, (dt, a, b, y)
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_atan2_cover(oracle, dt):
+    mpmath = pytest.importorskip("mpmath")
+    mpmath.mp.dps = 40
+    rng = np.random.default_rng(41)
+    n = 20000 if dt == np.float32 else 3000
+    a = rng.uniform(0, 1, n).astype(dt)
+    b = rng.uniform(0, 1, n).astype(dt)
+    ref = np.array([float(mpmath.atan2(mpmath.mpf(float(p)), mpmath.mpf(float(q)))) for p, q in zip(a, b)]).astype(dt)
+    m, w = oracle.max_ulp(oracle.atan2(a, b), ref)
+    assert m <= 1.0, (dt, m, a[w], b[w])

@@ -156,3 +156,21 @@ def test_invtrig_fused_bound(gpu, oracle, op, dtype):
     y = host(gpu.map_(op, to_dev(x), fused=True))
     m, w = oracle.max_ulp(y, oracle.trig(op, x))
     assert m <= 2.0, (op, dtype, m, x[w])
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("n", [1, 7, 100, (1 << 18) + 3])
+def test_atan2_bit_exact(gpu, oracle, dtype, n):
+    rng = np.random.default_rng(n)
+    a = rng.uniform(-3, 3, n).astype(dtype)
+    b = rng.uniform(-3, 3, n).astype(dtype)
+    if n >= 100:
+        sp = np.array([0.0, -0.0, 1.0, -1.0, np.inf, -np.inf, np.nan, 0.5, 1e-30, 3e30], dtype)
+        a[:100] = np.repeat(sp, 10)
+        b[:100] = np.tile(sp, 10)
+    y = host(gpu.atan2(to_dev(a), to_dev(b)))
+    bad = same_bits(y, oracle.atan2(a, b))
+    assert bad.size == 0, (dtype, bad[:5], a[bad[:5]], b[bad[:5]], y[bad[:5]])
+    yf = host(gpu.atan2(to_dev(a), to_dev(b), fused=True))
+    m, w = oracle.max_ulp(yf, oracle.atan2(a, b))
+    assert m <= 2.0, (dtype, m, a[w], b[w])
