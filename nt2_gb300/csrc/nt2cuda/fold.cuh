@@ -188,6 +188,24 @@ template <bool W1, bool STDEV> struct op_moments {
     const U wb = b.n / n;
     return moments<U>{n, a.mean + d * wb, a.m2 + b.m2 + d * d * a.n * wb};
   }
+  // N values at once (N a power of two): the block's own mean and sum of
+  // squared deviations in two passes over registers, then one merge, so the
+  // division of Welford's update is paid once per block instead of per value.
+  template <class U, int N> __device__ __forceinline__ static void add_block(state<U>& a, const U (&x)[N])
+  {
+    static_assert((N & (N - 1)) == 0, "add_block: N a power of two");
+    U s = x[0];
+#pragma unroll
+    for (int i = 1; i < N; ++i) s = s + x[i];
+    const U mb = s * (U(1) / U(N));               // exact scaling
+    U m2 = U(0);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      const U d = x[i] - mb;
+      m2 = m2 + d * d;
+    }
+    a = merge(a, moments<U>{U(N), mb, m2});
+  }
   template <class U> __device__ __forceinline__ static state<U> shfl(state<U> a, int off)
   {
     return moments<U>{__shfl_xor_sync(0xffffffffu, a.n, off), __shfl_xor_sync(0xffffffffu, a.mean, off),
@@ -207,6 +225,10 @@ template <bool W1, bool STDEV> struct op_moments {
 };
 
 template <class Op, class T> using state_of = typename Op::template state<T>;
+
+// Operations that take a block of values at once (add_block).
+template <class Op> struct has_block_add { static constexpr bool value = false; };
+template <bool W1, bool SD> struct has_block_add<op_moments<W1, SD>> { static constexpr bool value = true; };
 template <class Op, class T> using out_of = typename Op::template out_t<T>;
 
 // Butterfly over the warp; every lane ends with the same value.
@@ -278,10 +300,19 @@ __global__ void __launch_bounds__(256) k_inner(E e, inner_shape sh, out_of<Op, T
       regs<E, V> rr[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) rr[u].template load<true>(e, base + (g + (size_t)u * 32) * V);
+      if constexpr (has_block_add<Op>::value && ((U * V) & (U * V - 1)) == 0) {
+        T blk[U * V];
 #pragma unroll
-      for (int u = 0; u < U; ++u)
+        for (int u = 0; u < U; ++u)
 #pragma unroll
-        for (int l = 0; l < V; ++l) Op::add(a[l], (T)rr[u].template get<false>(e, l));
+          for (int l = 0; l < V; ++l) blk[u * V + l] = (T)rr[u].template get<false>(e, l);
+        Op::add_block(a[0], blk);
+      } else {
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+          for (int l = 0; l < V; ++l) Op::add(a[l], (T)rr[u].template get<false>(e, l));
+      }
     }
     for (; g < g1; g += 32) {
       regs<E, V> rr;
@@ -394,10 +425,21 @@ __global__ void __launch_bounds__(256) k_outer(E e, outer_shape sh, out_of<Op, T
         regs<E, V> rr[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) rr[u].template load<true>(e, (m + (size_t)u * 8) * sh.rows + row0);
+        if constexpr (has_block_add<Op>::value && (U & (U - 1)) == 0) {
+          // lane slot l is one row: its U values of this trip form a block
 #pragma unroll
-        for (int u = 0; u < U; ++u)
+          for (int l = 0; l < V; ++l) {
+            T blk[U];
 #pragma unroll
-          for (int l = 0; l < V; ++l) Op::add(a[l], (T)rr[u].template get<false>(e, l));
+            for (int u = 0; u < U; ++u) blk[u] = (T)rr[u].template get<false>(e, l);
+            Op::add_block(a[l], blk);
+          }
+        } else {
+#pragma unroll
+          for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int l = 0; l < V; ++l) Op::add(a[l], (T)rr[u].template get<false>(e, l));
+        }
       }
       for (; m < m1; m += 8) {
         regs<E, V> rr;

@@ -61,9 +61,13 @@ template <class T> inline const T* second_term(const node<tag::multiplies_, term
 
 // Loads in flight per lane in the register-pipelined kernels: 16 (8 left the
 // 134 MB folds at 71% of the copy peak, 16 reaches 75-77%, 32 adds nothing),
-// or 4 for the three-value var/stdev state (more would cost residency).
+// or 8 for var/stdev, whose block updates (add_block) hold the loaded values
+// until the block's mean is known.
 template <class Op> struct fold_unroll { static constexpr int value = 16; };
-template <bool W1, bool SD> struct fold_unroll<op_moments<W1, SD>> { static constexpr int value = 4; };
+template <bool W1, bool SD> struct fold_unroll<op_moments<W1, SD>> { static constexpr int value = 8; };
+// outer_fold keeps V rows' states per lane: var/stdev there take 4 columns a trip
+template <class Op> struct outer_unroll { static constexpr int value = fold_unroll<Op>::value; };
+template <bool W1, bool SD> struct outer_unroll<op_moments<W1, SD>> { static constexpr int value = 4; };
 
 template <class Op, class T> cudaError_t fold_empty(out_of<Op, T>* out, size_t count, cudaStream_t s)
 {
@@ -163,7 +167,7 @@ cudaError_t outer_fold(const E& e, size_t rows, size_t cols, out_of<Op, T>* out,
   E ec = e;
   out_of<Op, T>* o = out;
   void* args[] = {&ec, &sh, &o, &partials, &counters};
-  if (vec) return (launch_persistent(k_outer<Op, VV, fold_unroll<Op>::value, T, E>, units * 256, 256, 4, s, args));
+  if (vec) return (launch_persistent(k_outer<Op, VV, outer_unroll<Op>::value, T, E>, units * 256, 256, 4, s, args));
   return (launch_persistent(k_outer<Op, 1, 4, T, E>, units * 256, 256, 4, s, args));
 }
 
