@@ -171,6 +171,8 @@ __global__ void __launch_bounds__(256) k_inner_tma(const T* __restrict__ x, cons
         *reinterpret_cast<uint4*>(yv) = *reinterpret_cast<const uint4*>(ty + e);
 #pragma unroll
         for (int l = 0; l < V; ++l) Op::add(a[l], math::mul(xv[l], yv[l]));
+      } else if constexpr (has_block_add<Op>::value) {
+        Op::add_block(a[0], xv);                       // var/stdev: one merge per V values
       } else {
 #pragma unroll
         for (int l = 0; l < V; ++l) Op::add(a[l], xv[l]);
