@@ -119,7 +119,10 @@ enum {
   NT2CUDA_OP_COSPI = 16,
   NT2CUDA_OP_ASIN = 17,       /* NT2's SIMD forms (simd/common/impl/invtrig) */
   NT2CUDA_OP_ACOS = 18,
-  NT2CUDA_OP_ATAN = 19
+  NT2CUDA_OP_ATAN = 19,
+  NT2CUDA_OP_SINH = 20,       /* modules/core/hyperbolic: simd/common/{sinh,tanh}.hpp, generic/cosh.hpp */
+  NT2CUDA_OP_COSH = 21,
+  NT2CUDA_OP_TANH = 22
 };
 
 /* out = atan2(a0, a1) elementwise (NT2's SIMD form,

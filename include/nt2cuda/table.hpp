@@ -314,6 +314,9 @@ NT2CUDA_FN1(cospi, cospi_)
 NT2CUDA_FN1(asin, asin_)
 NT2CUDA_FN1(acos, acos_)
 NT2CUDA_FN1(atan, atan_)
+NT2CUDA_FN1(sinh, sinh_)
+NT2CUDA_FN1(cosh, cosh_)
+NT2CUDA_FN1(tanh, tanh_)
 NT2CUDA_FN1(sqrt, sqrt_)
 NT2CUDA_FN1(sqr, sqr_)
 NT2CUDA_FN1(erfc, erfc_)

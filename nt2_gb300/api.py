@@ -16,7 +16,7 @@ from ._lib import SdStream, check, lib
 
 OPS = {"exp": 0, "log": 1, "erfc": 2, "normcdf": 3, "fastnormcdf": 4, "sqrt": 5, "exp2": 6, "exp10": 7, "log2": 8,
        "log10": 9, "expm1": 10, "log1p": 11, "sin": 12, "cos": 13, "tan": 14, "sinpi": 15, "cospi": 16,
-       "asin": 17, "acos": 18, "atan": 19}
+       "asin": 17, "acos": 18, "atan": 19, "sinh": 20, "cosh": 21, "tanh": 22}
 CDF = {"normcdf": 0, "fastnormcdf": 1}
 
 
@@ -44,7 +44,8 @@ MAP_FUSED, MAP_SIMD128 = 1, 2
 def map_(op: str, x: torch.Tensor, out: torch.Tensor | None = None, fused: bool = False,
          simd128: bool = False) -> torch.Tensor:
     """out = nt2::op(x) for op in exp, log, erfc, normcdf, fastnormcdf, sqrt, exp2, exp10, log2, log10, expm1,
-    log1p, sin, cos, tan, sinpi, cospi, asin, acos, atan.  The trigonometric ops reduce each element on its own (NT2's scalar
+    log1p, sin, cos, tan, sinpi, cospi, asin, acos, atan, sinh, cosh, tanh.  The trigonometric ops reduce each
+    element on its own (NT2's scalar
     code); with simd128 they reduce each 16-byte pack of x with the method NT2's 128-bit SIMD code picks for
     the pack's largest |x| (tables that are not 16-byte aligned: scalar code throughout)."""
     out = torch.empty_like(x) if out is None else out

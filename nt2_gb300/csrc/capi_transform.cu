@@ -262,7 +262,7 @@ nt2cuda_status nt2cuda_map_f32(int op, const float* x, float* y, size_t n, int f
   if (n && (!x || !y)) return NT2CUDA_ERR_ARG;
   if (flags & ~(NT2CUDA_MAP_FUSED | NT2CUDA_MAP_SIMD128)) return NT2CUDA_ERR_ARG;
   const bool fused = (flags & NT2CUDA_MAP_FUSED) != 0;
-  if (op >= NT2CUDA_OP_SIN && op <= NT2CUDA_OP_ATAN)
+  if (op >= NT2CUDA_OP_SIN && op <= NT2CUDA_OP_TANH)
     return map_trig(op, x, y, n, fused, (flags & NT2CUDA_MAP_SIMD128) != 0, s);
   return fused ? map_impl<true>(op, x, y, n, s) : map_impl<false>(op, x, y, n, s);
 }
@@ -273,7 +273,7 @@ nt2cuda_status nt2cuda_map_f64(int op, const double* x, double* y, size_t n, int
   if (n && (!x || !y)) return NT2CUDA_ERR_ARG;
   if (flags & ~(NT2CUDA_MAP_FUSED | NT2CUDA_MAP_SIMD128)) return NT2CUDA_ERR_ARG;
   const bool fused = (flags & NT2CUDA_MAP_FUSED) != 0;
-  if (op >= NT2CUDA_OP_SIN && op <= NT2CUDA_OP_ATAN)
+  if (op >= NT2CUDA_OP_SIN && op <= NT2CUDA_OP_TANH)
     return map_trig(op, x, y, n, fused, (flags & NT2CUDA_MAP_SIMD128) != 0, s);
   return fused ? map_impl<true>(op, x, y, n, s) : map_impl<false>(op, x, y, n, s);
 }

@@ -49,6 +49,7 @@ struct trunc_u8_ {};
 struct sin_ {}; struct cos_ {}; struct tan_ {}; struct sinpi_ {}; struct cospi_ {};
 template <class T> struct simd128_ {};
 struct asin_ {}; struct acos_ {}; struct atan_ {}; struct atan2_ {};
+struct sinh_ {}; struct cosh_ {}; struct tanh_ {};
 }  // namespace tag
 
 // ------------------------------------------------------------ tree nodes
@@ -147,6 +148,9 @@ NT2CUDA_UN(log1p_, math::log1p<F>(a))
 NT2CUDA_UN(erfc_, math::erfc<F>(a))
 NT2CUDA_UN(normcdf_, math::normcdf<F>(a))
 NT2CUDA_UN(fastnormcdf_, math::fastnormcdf<F>(a))
+NT2CUDA_UN(sinh_, math::sinh<F>(a))
+NT2CUDA_UN(cosh_, math::cosh<F>(a))
+NT2CUDA_UN(tanh_, math::tanh<F>(a))
 NT2CUDA_UN(asin_, trig::asin<F>(a))
 NT2CUDA_UN(acos_, trig::acos<F>(a))
 NT2CUDA_UN(atan_, trig::atan<F>(a))

@@ -579,6 +579,102 @@ __device__ __forceinline__ void normcdf_pair(double a0, double& pos, double& neg
   neg = mul(0.5, (-y < 0.0) ? two_m : r1);
 }
 
+// ---------------------------------------------------- sinh, cosh, tanh
+// modules/core/hyperbolic/include/nt2/hyperbolic/functions/: sinh simd/common/sinh.hpp:20-45
+// (kernel details/sinh_kernel.hpp), cosh generic/cosh.hpp:20-42, tanh
+// simd/common/tanh.hpp:20-48 (kernel details/tanh_kernel.hpp).  The SIMD forms
+// select per lane (no pack dependence).  average(a, b) = fma(a, 0.5, b*0.5).
+template <class T> struct hyp;
+template <> struct hyp<float> {
+  static constexpr uint32_t log_2 = 0x3f317218u;
+  __device__ static float maxlog() { return fbits(cf::maxlog); }
+};
+template <> struct hyp<double> {
+  static constexpr uint64_t log_2 = 0x3fe62e42fefa39efull;
+  __device__ static double maxlog() { return dbits(cd::maxlog); }
+};
+__device__ __forceinline__ float bits_xor(float v, float s)
+{ return __uint_as_float(__float_as_uint(v) ^ (__float_as_uint(s) & 0x80000000u)); }
+__device__ __forceinline__ double bits_xor(double v, double s)
+{
+  return __longlong_as_double(__double_as_longlong(v) ^ (__double_as_longlong(s) & (long long)0x8000000000000000ull));
+}
+
+template <bool F, class T> __device__ __forceinline__ T sinh_kernel(T x);
+template <> __device__ __forceinline__ float sinh_kernel<false, float>(float x)
+{
+  constexpr uint32_t P[4] = {0x39559e2fu, 0x3c087bbeu, 0x3e2aaaccu, 0x3f800000u};
+  return mul(horner<false>(mul(x, x), P), x);
+}
+template <> __device__ __forceinline__ float sinh_kernel<true, float>(float x)
+{
+  constexpr uint32_t P[4] = {0x39559e2fu, 0x3c087bbeu, 0x3e2aaaccu, 0x3f800000u};
+  return mul(horner<true>(mul(x, x), P), x);
+}
+template <bool F> __device__ __forceinline__ double sinh_kernel_d(double x)
+{
+  constexpr uint64_t P[4] = {0xbfe9435fe8bb3cd6ull, 0xc064773a398ff4feull, 0xc0c694b8c71d6182ull,
+                             0xc115782bdbf6ab05ull};
+  constexpr uint64_t Q[4] = {0x3ff0000000000000ull, 0xc0715b6096e96484ull, 0x40e1a7ba7ed72245ull,
+                             0xc1401a20e4f90044ull};
+  const double x2 = mul(x, x);
+  return madd<F>(x, div(mul(x2, horner<F>(x2, P)), horner<F>(x2, Q)), x);
+}
+template <> __device__ __forceinline__ double sinh_kernel<false, double>(double x) { return sinh_kernel_d<false>(x); }
+template <> __device__ __forceinline__ double sinh_kernel<true, double>(double x) { return sinh_kernel_d<true>(x); }
+
+template <bool F = false, class T> __device__ __forceinline__ T sinh(T a0)
+{
+  const T x = fabs(a0);
+  T r;
+  if (x < T(1)) {
+    r = sinh_kernel<F, T>(x);
+  } else {
+    const bool test1 = x > sub(hyp<T>::maxlog(), (T)(sizeof(T) == 4 ? (T)fbits((uint32_t)hyp<float>::log_2)
+                                                                   : (T)dbits(hyp<double>::log_2)));
+    const T tmp = exp<F>(mul(x, test1 ? T(0.5) : T(1)));
+    const T tmp1 = mul(T(0.5), tmp);
+    r = test1 ? mul(tmp1, tmp) : sub(tmp1, mul(T(0.5), div(T(1), tmp)));
+  }
+  return bits_xor(r, a0);
+}
+template <bool F = false, class T> __device__ __forceinline__ T cosh(T a0)
+{
+  const T x = fabs(a0);
+  const bool test1 = x > sub(hyp<T>::maxlog(), (T)(sizeof(T) == 4 ? (T)fbits((uint32_t)hyp<float>::log_2)
+                                                                 : (T)dbits(hyp<double>::log_2)));
+  const T tmp = exp<F>(mul(x, test1 ? T(0.5) : T(1)));
+  return test1 ? mul(mul(T(0.5), tmp), tmp) : madd<F>(tmp, T(0.5), mul(div(T(1), tmp), T(0.5)));
+}
+template <bool F = false> __device__ __forceinline__ float tanh(float a0)
+{
+  constexpr uint32_t P[5] = {0xbbbaf0eau, 0x3ca9134eu, 0xbd5c1e2du, 0x3e088393u, 0xbeaaaa99u};
+  const float x = fabsf(a0);
+  float r;
+  if (x < 0.625f) {
+    const float x2 = mul(x, x);
+    r = madd<F>(mul(horner<F>(x2, P), x2), x, x);
+  } else {
+    r = madd<F>(-2.0f, div(1.0f, add(1.0f, exp<F>(add(x, x)))), 1.0f);
+  }
+  return bits_xor(r, a0);
+}
+template <bool F = false> __device__ __forceinline__ double tanh(double a0)
+{
+  constexpr uint64_t P[3] = {0xbfeedc5baafd6f4bull, 0xc058d26a0e26682dull, 0xc0993ac030580563ull};
+  constexpr uint64_t Q[4] = {0x3ff0000000000000ull, 0x405c33f28a581b86ull, 0x40a176fa0e5535faull,
+                             0x40b2ec102442040cull};
+  const double x = fabs(a0);
+  double r;
+  if (x < 0.625) {
+    const double x2 = mul(x, x);
+    r = madd<F>(div(mul(x2, horner<F>(x2, P)), horner<F>(x2, Q)), x, x);
+  } else {
+    r = madd<F>(-2.0, div(1.0, add(1.0, exp<F>(add(x, x)))), 1.0);
+  }
+  return bits_xor(r, a0);
+}
+
 }  // namespace math
 }  // namespace nt2cuda
 

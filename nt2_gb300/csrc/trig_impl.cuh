@@ -1,6 +1,7 @@
-// trig_impl.cuh -- the trigonometric functors of nt2cuda_map_f32/f64
-// (sin, cos, tan, sinpi, cospi in NT2's scalar form or its 128-bit SIMD form;
-// asin, acos, atan), lowered onto the elementwise transform (nt2cuda/trig.cuh).  Included by
+// trig_impl.cuh -- the trigonometric and hyperbolic functors of
+// nt2cuda_map_f32/f64 (sin, cos, tan, sinpi, cospi in NT2's scalar form or its
+// 128-bit SIMD form; asin, acos, atan; sinh, cosh, tanh), lowered onto the
+// elementwise transform (nt2cuda/trig.cuh, nt2cuda/math.cuh).  Included by
 // capi_trig_f32.cu and capi_trig_f64.cu, one element type each, which the
 // build compiles in parallel.
 #pragma once
@@ -37,6 +38,9 @@ template <bool F, bool SIMD, class T> nt2cuda_status trig_impl(int op, const T* 
     case NT2CUDA_OP_ASIN: return SIMD ? NT2CUDA_ERR_ARG : run_trig<F, tag::asin_>(x, y, n, s);
     case NT2CUDA_OP_ACOS: return SIMD ? NT2CUDA_ERR_ARG : run_trig<F, tag::acos_>(x, y, n, s);
     case NT2CUDA_OP_ATAN: return SIMD ? NT2CUDA_ERR_ARG : run_trig<F, tag::atan_>(x, y, n, s);
+    case NT2CUDA_OP_SINH: return SIMD ? NT2CUDA_ERR_ARG : run_trig<F, tag::sinh_>(x, y, n, s);
+    case NT2CUDA_OP_COSH: return SIMD ? NT2CUDA_ERR_ARG : run_trig<F, tag::cosh_>(x, y, n, s);
+    case NT2CUDA_OP_TANH: return SIMD ? NT2CUDA_ERR_ARG : run_trig<F, tag::tanh_>(x, y, n, s);
     default: return NT2CUDA_ERR_ARG;
   }
 }

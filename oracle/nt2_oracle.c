@@ -628,10 +628,100 @@ EXPORT double nt2o_erfc_d_scalar(double a0)
   return (a0 < 0.0) ? 2.0 - z : z;
 }
 
+/* ----------------------------------------------------- sinh, cosh, tanh -- */
+/* Paths relative to modules/core/hyperbolic/include/nt2/hyperbolic/functions/:
+ * sinh simd/common/sinh.hpp:20-45 (kernel details/sinh_kernel.hpp), cosh
+ * generic/cosh.hpp:20-42, tanh simd/common/tanh.hpp:20-48 (kernel
+ * details/tanh_kernel.hpp).  The SIMD forms select per lane: no pack dependence.
+ * average(a, b) = fma(a, 0.5, b*0.5) (boost/simd/arithmetic/functions/generic/average.hpp). */
+static const uint32_t SINH_F_P[4] = {0x39559e2fu, 0x3c087bbeu, 0x3e2aaaccu, 0x3f800000u};
+static const uint64_t SINH_D_P[4] = {0xbfe9435fe8bb3cd6ull, 0xc064773a398ff4feull, 0xc0c694b8c71d6182ull,
+                                     0xc115782bdbf6ab05ull};
+static const uint64_t SINH_D_Q[4] = {0x3ff0000000000000ull, 0xc0715b6096e96484ull, 0x40e1a7ba7ed72245ull,
+                                     0xc1401a20e4f90044ull};
+static const uint32_t TANH_F_P[5] = {0xbbbaf0eau, 0x3ca9134eu, 0xbd5c1e2du, 0x3e088393u, 0xbeaaaa99u};
+static const uint64_t TANH_D_P[3] = {0xbfeedc5baafd6f4bull, 0xc058d26a0e26682dull, 0xc0993ac030580563ull};
+static const uint64_t TANH_D_Q[4] = {0x3ff0000000000000ull, 0x405c33f28a581b86ull, 0x40a176fa0e5535faull,
+                                     0x40b2ec102442040cull};
+#define LOG_2_F 0x3f317218u
+#define LOG_2_D 0x3fe62e42fefa39efull
+
+EXPORT float nt2o_sinh_f(float a0)
+{
+  const float x = fabsf(a0);
+  const uint32_t bts = bf(a0) & 0x80000000u;
+  float r;
+  if (x < 1.0f) {
+    r = horner_f(x * x, SINH_F_P, 4) * x;
+  } else {
+    const int test1 = x > MAXLOG_F - fb(LOG_2_F);
+    const float tmp = nt2o_exp_f(x * (test1 ? 0.5f : 1.0f));
+    const float tmp1 = 0.5f * tmp;
+    r = test1 ? tmp1 * tmp : tmp1 - 0.5f * (1.0f / tmp);
+  }
+  return fb(bf(r) ^ bts);
+}
+EXPORT double nt2o_sinh_d(double a0)
+{
+  const double x = fabs(a0);
+  const uint64_t bts = bd(a0) & 0x8000000000000000ull;
+  double r;
+  if (x < 1.0) {
+    const double x2 = x * x;
+    r = x * (x2 * horner_d(x2, SINH_D_P, 4) / horner_d(x2, SINH_D_Q, 4)) + x;
+  } else {
+    const int test1 = x > MAXLOG_D - db(LOG_2_D);
+    const double tmp = nt2o_exp_d(x * (test1 ? 0.5 : 1.0));
+    const double tmp1 = 0.5 * tmp;
+    r = test1 ? tmp1 * tmp : tmp1 - 0.5 * (1.0 / tmp);
+  }
+  return db(bd(r) ^ bts);
+}
+EXPORT float nt2o_cosh_f(float a0)
+{
+  const float x = fabsf(a0);
+  const int test1 = x > MAXLOG_F - fb(LOG_2_F);
+  const float tmp = nt2o_exp_f(x * (test1 ? 0.5f : 1.0f));
+  return test1 ? (0.5f * tmp) * tmp : tmp * 0.5f + (1.0f / tmp) * 0.5f;
+}
+EXPORT double nt2o_cosh_d(double a0)
+{
+  const double x = fabs(a0);
+  const int test1 = x > MAXLOG_D - db(LOG_2_D);
+  const double tmp = nt2o_exp_d(x * (test1 ? 0.5 : 1.0));
+  return test1 ? (0.5 * tmp) * tmp : tmp * 0.5 + (1.0 / tmp) * 0.5;
+}
+EXPORT float nt2o_tanh_f(float a0)
+{
+  const float x = fabsf(a0);
+  const uint32_t bts = bf(a0) & 0x80000000u;
+  float r;
+  if (x < 0.625f) {
+    const float x2 = x * x;
+    r = (horner_f(x2, TANH_F_P, 5) * x2) * x + x;
+  } else {
+    r = -2.0f * (1.0f / (1.0f + nt2o_exp_f(x + x))) + 1.0f;
+  }
+  return fb(bf(r) ^ bts);
+}
+EXPORT double nt2o_tanh_d(double a0)
+{
+  const double x = fabs(a0);
+  const uint64_t bts = bd(a0) & 0x8000000000000000ull;
+  double r;
+  if (x < 0.625) {
+    const double x2 = x * x;
+    r = (x2 * horner_d(x2, TANH_D_P, 3) / horner_d(x2, TANH_D_Q, 4)) * x + x;
+  } else {
+    r = -2.0 * (1.0 / (1.0 + nt2o_exp_d(x + x))) + 1.0;
+  }
+  return db(bd(r) ^ bts);
+}
+
 /* ------------------------------------------------------------- maps ------ */
 enum { OP_EXP = 0, OP_LOG = 1, OP_ERFC = 2, OP_NORMCDF = 3, OP_FASTNORMCDF = 4, OP_SQRT = 5,
        OP_ERFC_SCALAR = 6, OP_EXP2 = 7, OP_EXP10 = 8, OP_LOG2 = 9, OP_LOG10 = 10, OP_EXPM1 = 11,
-       OP_LOG1P = 12 };
+       OP_LOG1P = 12, OP_SINH = 13, OP_COSH = 14, OP_TANH = 15 };
 
 EXPORT int nt2o_map_f(int op, const float* x, float* y, size_t n)
 {
@@ -651,6 +741,9 @@ EXPORT int nt2o_map_f(int op, const float* x, float* y, size_t n)
       case OP_LOG10: y[i] = nt2o_log10_f(a); break;
       case OP_EXPM1: y[i] = nt2o_expm1_f(a); break;
       case OP_LOG1P: y[i] = nt2o_log1p_f(a); break;
+      case OP_SINH: y[i] = nt2o_sinh_f(a); break;
+      case OP_COSH: y[i] = nt2o_cosh_f(a); break;
+      case OP_TANH: y[i] = nt2o_tanh_f(a); break;
       default: return 1;
     }
   }
@@ -674,6 +767,9 @@ EXPORT int nt2o_map_d(int op, const double* x, double* y, size_t n)
       case OP_LOG10: y[i] = nt2o_log10_d(a); break;
       case OP_EXPM1: y[i] = nt2o_expm1_d(a); break;
       case OP_LOG1P: y[i] = nt2o_log1p_d(a); break;
+      case OP_SINH: y[i] = nt2o_sinh_d(a); break;
+      case OP_COSH: y[i] = nt2o_cosh_d(a); break;
+      case OP_TANH: y[i] = nt2o_tanh_d(a); break;
       default: return 1;
     }
   }

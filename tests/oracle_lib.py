@@ -40,6 +40,12 @@ SIGS = {
     "nt2o_log1p_f": (C.c_float, [C.c_float]),
     "nt2o_expm1_d": (C.c_double, [C.c_double]),
     "nt2o_log1p_d": (C.c_double, [C.c_double]),
+    "nt2o_sinh_f": (C.c_float, [C.c_float]),
+    "nt2o_sinh_d": (C.c_double, [C.c_double]),
+    "nt2o_cosh_f": (C.c_float, [C.c_float]),
+    "nt2o_cosh_d": (C.c_double, [C.c_double]),
+    "nt2o_tanh_f": (C.c_float, [C.c_float]),
+    "nt2o_tanh_d": (C.c_double, [C.c_double]),
     "nt2o_trig_f": (C.c_int, [C.c_int, f32p, f32p, sz, C.c_int]),
     "nt2o_trig_d": (C.c_int, [C.c_int, f64p, f64p, sz, C.c_int]),
     "nt2o_atan2_f": (None, [f32p, f32p, f32p, sz]),
@@ -84,7 +90,8 @@ SIGS = {
 }
 
 OP = {"exp": 0, "log": 1, "erfc": 2, "normcdf": 3, "fastnormcdf": 4, "sqrt": 5, "erfc_scalar": 6,
-      "exp2": 7, "exp10": 8, "log2": 9, "log10": 10, "expm1": 11, "log1p": 12}
+      "exp2": 7, "exp10": 8, "log2": 9, "log10": 10, "expm1": 11, "log1p": 12, "sinh": 13, "cosh": 14,
+      "tanh": 15}
 
 
 def load(variant: str = "libnt2oracle.so"):

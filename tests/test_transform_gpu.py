@@ -15,7 +15,8 @@ SIZES = [0, 1, 3, 7, 31, 33, 1000, 4097, (1 << 16) + 5]
 # fused-FMA bounds (NT2 ulpdist units) against the unfused oracle; erfc and normcdf stay within
 # the 16 ULP that NT2 states for its float erfc (erf_kernel.hpp:50-52)
 FUSED_BOUND = {"exp": 1.0, "log": 1.0, "erfc": 16.0, "normcdf": 16.0, "fastnormcdf": 8.0, "sqrt": 0.0,
-               "exp2": 2.0, "exp10": 2.0, "log2": 2.0, "log10": 2.0, "expm1": 2.0, "log1p": 2.0}
+               "exp2": 2.0, "exp10": 2.0, "log2": 2.0, "log10": 2.0, "expm1": 2.0, "log1p": 2.0,
+               "sinh": 2.0, "cosh": 2.0, "tanh": 2.0}
 
 
 def to_dev(a):
@@ -51,7 +52,7 @@ def inputs(op, n, dtype, seed=0):
 
 
 @pytest.mark.parametrize("op", ["exp", "log", "erfc", "normcdf", "fastnormcdf", "sqrt", "exp2", "exp10", "log2",
-                                "log10", "expm1", "log1p"])
+                                "log10", "expm1", "log1p", "sinh", "cosh", "tanh"])
 @pytest.mark.parametrize("n", SIZES)
 def test_map_f32_bit_exact(gpu, oracle, op, n):
     x = inputs(op, n, np.float32, seed=n)
@@ -62,7 +63,7 @@ def test_map_f32_bit_exact(gpu, oracle, op, n):
 
 
 @pytest.mark.parametrize("op", ["exp", "log", "erfc", "normcdf", "sqrt", "exp2", "exp10", "log2", "log10", "expm1",
-                                "log1p"])
+                                "log1p", "sinh", "cosh", "tanh"])
 @pytest.mark.parametrize("n", [1, 7, 4097, (1 << 16) + 3])
 def test_map_f64_bit_exact(gpu, oracle, op, n):
     x = inputs(op, n, np.float64, seed=n + 1)
@@ -73,7 +74,7 @@ def test_map_f64_bit_exact(gpu, oracle, op, n):
 
 
 @pytest.mark.parametrize("op", ["exp", "log", "erfc", "normcdf", "fastnormcdf", "exp2", "exp10", "log2", "log10",
-                                "expm1", "log1p"])
+                                "expm1", "log1p", "sinh", "cosh", "tanh"])
 def test_map_f32_fused_within_bound(gpu, oracle, op):
     x = inputs(op, 1 << 16, np.float32, seed=5)
     y = host(gpu.map_(op, to_dev(x), fused=True))
