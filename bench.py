@@ -519,6 +519,24 @@ def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: in
                         api.map_(op, x, out=y, simd128=simd)
                     ms, _, _ = time_device(trig_step, K(100), warmup, ws)
                     out.append(line(label, ms, 2 * n * xs[0].element_size(), n, "elements/s"))
+            # z = pow(a0, a1) over NT2's cover range: a0 in [0, 100], a1 in [-10, 10];
+            # 12 (float) or 24 (double) bytes per element
+            label = f"pow {tname} 2^24 a0 in [0,100], a1 in [-10,10]"
+            if not part or part in label:
+                a1s = [torch.empty(n, dtype=dt, device="cuda") for _ in range(2)]
+                for k, t in enumerate(xs):
+                    api.fill_uniform(t, 0.0, 100.0, 51 + k)
+                for k, t in enumerate(a1s):
+                    api.fill_uniform(t, -10.0, 10.0, 61 + k)
+                it = [0]
+
+                def pow_step():
+                    k = it[0] & 1
+                    it[0] += 1
+                    api.pow(xs[k], a1s[k], out=y)
+                ms, _, _ = time_device(pow_step, K(100), warmup, ws)
+                out.append(line(label, ms, 3 * n * xs[0].element_size(), n, "elements/s"))
+                del a1s
             del xs, y
     if not (want("inner") or want("outer") or want("reductions") or want("scans") or want("bs_f64") or want("bs_fused") or want("bs_fast")
             or want("bs_exact") or want("bs_fastnormcdf") or want("sigmadelta")):

@@ -133,6 +133,15 @@ nt2cuda_status nt2cuda_atan2_f32(const float* a0, const float* a1, float* out, s
 nt2cuda_status nt2cuda_atan2_f64(const double* a0, const double* a1, double* out, size_t n, int flags,
                                  nt2cuda_stream stream);
 
+/* out = pow(a0, a1) elementwise, a1 floating (NT2's SIMD form, the cephes algorithm:
+ * modules/core/exponential/include/nt2/exponential/functions/simd/common/pow.hpp:29-37 over
+ * simd/common/pow_abs.hpp:72-131; NaN for a0 < 0 with a1 not an integer, pow(0, 0) = 1,
+ * pow(1, anything) = 1).  flags: NT2CUDA_MAP_FUSED or 0. */
+nt2cuda_status nt2cuda_pow_f32(const float* a0, const float* a1, float* out, size_t n, int flags,
+                               nt2cuda_stream stream);
+nt2cuda_status nt2cuda_pow_f64(const double* a0, const double* a1, double* out, size_t n, int flags,
+                               nt2cuda_stream stream);
+
 /* Flags of nt2cuda_map_*. */
 #define NT2CUDA_MAP_FUSED 1     /* hardware FMA (the `fused` convention above) */
 #define NT2CUDA_MAP_SIMD128 2   /* trigonometric ops: 128-bit pack reductions  */

@@ -333,6 +333,7 @@ NT2CUDA_FN1(minusone, minusone_)
   inline auto NAME(const A& a, const B& b) { return make_binary<tag::TAG>(a, b); }
 NT2CUDA_FN2(max, max_)
 NT2CUDA_FN2(atan2, atan2_)
+NT2CUDA_FN2(pow, pow_)
 NT2CUDA_FN2(min, min_)
 NT2CUDA_FN2(adds, adds_)
 NT2CUDA_FN2(subs, subs_)

@@ -61,22 +61,31 @@ def map_(op: str, x: torch.Tensor, out: torch.Tensor | None = None, fused: bool 
     return out
 
 
-def atan2(a0: torch.Tensor, a1: torch.Tensor, out: torch.Tensor | None = None, fused: bool = False) -> torch.Tensor:
-    """out = nt2::atan2(a0, a1) elementwise (NT2's SIMD form)."""
+def _binary(name: str, a0: torch.Tensor, a1: torch.Tensor, out: torch.Tensor | None, fused: bool) -> torch.Tensor:
     if a0.numel() != a1.numel():
         raise ValueError("a0 and a1 must have the same size")
     out = torch.empty_like(a0) if out is None else out
     L = lib()
     if a0.dtype == torch.float32:
-        st = L.nt2cuda_atan2_f32(_dev(a0), _dev(a1, torch.float32), _dev(out, torch.float32), a0.numel(),
-                                 MAP_FUSED if fused else 0, _stream())
+        st = getattr(L, f"nt2cuda_{name}_f32")(_dev(a0), _dev(a1, torch.float32), _dev(out, torch.float32),
+                                               a0.numel(), MAP_FUSED if fused else 0, _stream())
     elif a0.dtype == torch.float64:
-        st = L.nt2cuda_atan2_f64(_dev(a0), _dev(a1, torch.float64), _dev(out, torch.float64), a0.numel(),
-                                 MAP_FUSED if fused else 0, _stream())
+        st = getattr(L, f"nt2cuda_{name}_f64")(_dev(a0), _dev(a1, torch.float64), _dev(out, torch.float64),
+                                               a0.numel(), MAP_FUSED if fused else 0, _stream())
     else:
-        raise TypeError("atan2 takes float32 or float64 tables")
-    check(st, "atan2")
+        raise TypeError(f"{name} takes float32 or float64 tables")
+    check(st, name)
     return out
+
+
+def atan2(a0: torch.Tensor, a1: torch.Tensor, out: torch.Tensor | None = None, fused: bool = False) -> torch.Tensor:
+    """out = nt2::atan2(a0, a1) elementwise (NT2's SIMD form)."""
+    return _binary("atan2", a0, a1, out, fused)
+
+
+def pow(a0: torch.Tensor, a1: torch.Tensor, out: torch.Tensor | None = None, fused: bool = False) -> torch.Tensor:
+    """out = nt2::pow(a0, a1) elementwise for a floating exponent table (NT2's SIMD form)."""
+    return _binary("pow", a0, a1, out, fused)
 
 
 def saxpy(alpha: float, x: torch.Tensor, y: torch.Tensor, fused: bool = False) -> torch.Tensor:

@@ -1,4 +1,4 @@
-// capi_trig_f64.cu -- nt2cuda_map_f64's trigonometric ops and nt2cuda_atan2_f64 (double tables).
+// capi_trig_f64.cu -- nt2cuda_map_f64's trigonometric ops, nt2cuda_atan2_f64 and nt2cuda_pow_f64 (double tables).
 #include "trig_impl.cuh"
 
 namespace nt2cuda {
@@ -18,5 +18,14 @@ extern "C" nt2cuda_status nt2cuda_atan2_f64(const double* a0, const double* a1, 
   NT2CUDA_NVTX_RANGE;
   if (n && (!a0 || !a1 || !out)) return NT2CUDA_ERR_ARG;
   if (flags & ~NT2CUDA_MAP_FUSED) return NT2CUDA_ERR_ARG;
-  return nt2cuda::detail_capi::atan2_impl(a0, a1, out, n, (flags & NT2CUDA_MAP_FUSED) != 0, s);
+  return nt2cuda::detail_capi::binary_impl<nt2cuda::tag::atan2_>(a0, a1, out, n, (flags & NT2CUDA_MAP_FUSED) != 0, s);
+}
+
+extern "C" nt2cuda_status nt2cuda_pow_f64(const double* a0, const double* a1, double* out, size_t n, int flags,
+                                           nt2cuda_stream s)
+{
+  NT2CUDA_NVTX_RANGE;
+  if (n && (!a0 || !a1 || !out)) return NT2CUDA_ERR_ARG;
+  if (flags & ~NT2CUDA_MAP_FUSED) return NT2CUDA_ERR_ARG;
+  return nt2cuda::detail_capi::binary_impl<nt2cuda::tag::pow_>(a0, a1, out, n, (flags & NT2CUDA_MAP_FUSED) != 0, s);
 }

@@ -50,6 +50,7 @@ struct sin_ {}; struct cos_ {}; struct tan_ {}; struct sinpi_ {}; struct cospi_ 
 template <class T> struct simd128_ {};
 struct asin_ {}; struct acos_ {}; struct atan_ {}; struct atan2_ {};
 struct sinh_ {}; struct cosh_ {}; struct tanh_ {};
+struct pow_ {};
 }  // namespace tag
 
 // ------------------------------------------------------------ tree nodes
@@ -130,6 +131,7 @@ NT2CUDA_BIN(is_not_equal_, (bool)(a != b))
 NT2CUDA_BIN(selinc_, (a ? (B)(b + 1) : b))
 NT2CUDA_BIN(seldec_, (a ? (B)(b - 1) : b))
 NT2CUDA_BIN(atan2_, trig::atan2<F>(a, (A)b))
+NT2CUDA_BIN(pow_, math::pow<F>(a, (A)b))
 NT2CUDA_UN(unary_minus_, (A)(-a))
 NT2CUDA_UN(sqr_, detail::mul(a, a))
 NT2CUDA_UN(sqrt_, math::sqrt_(a))

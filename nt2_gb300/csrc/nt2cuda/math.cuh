@@ -675,6 +675,196 @@ template <bool F = false> __device__ __forceinline__ double tanh(double a0)
   return bits_xor(r, a0);
 }
 
+// -------------------------------------------------------------------- pow
+// pow(a0, a1) for floating a0 and a1, NT2's SIMD form:
+// modules/core/exponential/include/nt2/exponential/functions/simd/common/pow.hpp:29-37 over
+// pow_abs (simd/common/pow_abs.hpp:72-131), the cephes algorithm: log2|a0| from a 2^(-i/16)
+// table and a rational (double) or polynomial (float) correction, the product with a1 split
+// into multiples of 1/16 to keep it exact, and 2^(product) back through the same table
+// (details/pow_kernel.hpp).  The scalar form (scalar/pow.hpp, scalar/pow_abs.hpp) runs the
+// same kernel and returns the same values for the same special cases.  frexp and ldexp are
+// Boost.SIMD's (boost/simd/ieee/functions/simd/common/frexp.hpp:42-67, ldexp.hpp:55-70).
+// The tables are 2^(-i/16) rounded to the type (A) and, for even i, the rounding residual
+// 2^(-i/16) - A[i] (B, indexed by i/2); they are read through the L1 (a warp's indices fall
+// in one or two 128-byte lines).
+static __device__ const uint32_t kPowAf[17] = {
+    0x3f800000u, 0x3f75257du, 0x3f6ac0c7u, 0x3f60ccdfu, 0x3f5744fdu, 0x3f4e248cu, 0x3f45672au, 0x3f3d08a4u, 0x3f3504f3u,
+    0x3f2d583fu, 0x3f25fed7u, 0x3f1ef532u, 0x3f1837f0u, 0x3f11c3d3u, 0x3f0b95c2u, 0x3f05aac3u, 0x3f000000u};
+static __device__ const uint32_t kPowBf[9] = {0x00000000u, 0xb1c116deu, 0xb254a58au, 0x318aa837u, 0x324fe77au,
+                                              0xb2ac9d5eu, 0x32a31b71u, 0xb1e0aba1u, 0x00000000u};
+static __device__ const uint64_t kPowAd[17] = {
+    0x3ff0000000000000ull, 0x3feea4afa2a490daull, 0x3fed5818dcfba487ull, 0x3fec199bdd85529cull, 0x3feae89f995ad3adull,
+    0x3fe9c49182a3f090ull, 0x3fe8ace5422aa0dbull, 0x3fe7a11473eb0187ull, 0x3fe6a09e667f3bcdull, 0x3fe5ab07dd485429ull,
+    0x3fe4bfdad5362a27ull, 0x3fe3dea64c123422ull, 0x3fe306fe0a31b715ull, 0x3fe2387a6e756238ull, 0x3fe172b83c7d517bull,
+    0x3fe0b5586cf9890full, 0x3fe0000000000000ull};
+static __device__ const uint64_t kPowBd[9] = {0x0000000000000000ull, 0x3c72ed02d75b3707ull, 0x3c87a1cd345dcc81ull,
+                                              0x3c86e9f156864b27ull, 0xbc8bdd3413b26456ull, 0x3c6d4397afec42e2ull,
+                                              0x3c76f46ad23182e4ull, 0xbc719041b9d78a76ull, 0x0000000000000000ull};
+
+__device__ __forceinline__ float pow_a(float, int i) { return __uint_as_float(__ldg(&kPowAf[i])); }
+__device__ __forceinline__ float pow_b(float, int i) { return __uint_as_float(__ldg(&kPowBf[i])); }
+__device__ __forceinline__ double pow_a(double, int i)
+{ return __longlong_as_double((long long)__ldg(reinterpret_cast<const unsigned long long*>(&kPowAd[i]))); }
+__device__ __forceinline__ double pow_b(double, int i)
+{ return __longlong_as_double((long long)__ldg(reinterpret_cast<const unsigned long long*>(&kPowBd[i]))); }
+
+template <class T> struct powc;
+template <> struct powc<float> {
+  using U = uint32_t;
+  static constexpr int nbm = 23, maxe = 127, mine = -126, lime = 128;
+  static constexpr U expmask = 0x7f800000u, half = 0x3f000000u, smallest = 0x00800000u;
+  static constexpr U log2_em1 = 0x3ee2a8edu, large = 0x44ffe000u, low = 0xc5160000u;
+  __device__ static float bits(U u) { return __uint_as_float(u); }
+  __device__ static U ubits(float v) { return __float_as_uint(v); }
+  __device__ static float twotonmb() { return 8388608.0f; }
+};
+template <> struct powc<double> {
+  using U = uint64_t;
+  static constexpr int nbm = 52, maxe = 1023, mine = -1022, lime = 1024;
+  static constexpr U expmask = 0x7ff0000000000000ull, half = 0x3fe0000000000000ull,
+                     smallest = 0x0010000000000000ull;
+  static constexpr U log2_em1 = 0x3fdc551d94ae0bf8ull, large = 0x40cfff8000000000ull, low = 0xc0d0c7c000000000ull;
+  __device__ static double bits(U u) { return __longlong_as_double((long long)u); }
+  __device__ static U ubits(double v) { return (U)__double_as_longlong(v); }
+  __device__ static double twotonmb() { return 4503599627370496.0; }
+};
+
+// Boost.SIMD frexp: mantissa in [0.5, 1), denormals scaled by 2^nbm first; Inf/NaN keep a
+// mantissa that is not finite (r0 + a0) and exponent 0.
+template <class T> __device__ __forceinline__ T pow_frexp(T a0, int& e)
+{
+  using C = powc<T>;
+  const bool den = fabs(a0) < C::bits(C::smallest) && a0 != T(0);
+  const T aa0 = den ? mul(C::twotonmb(), a0) : a0;
+  const typename C::U b = C::ubits(aa0);
+  int r1 = (int)((b & C::expmask) >> C::nbm) - (C::maxe - 1);
+  const T r0 = C::bits((b & ~C::expmask) | C::half);
+  const bool test0 = aa0 != T(0), test1 = r1 > C::lime;
+  r1 = (!test1 && test0) ? r1 : 0;
+  e = r1 - (den ? C::nbm : 0);
+  return test0 ? (test1 ? add(r0, aa0) : r0) : T(0);
+}
+// Boost.SIMD ldexp: (a0 * 2^e) * f with f = 2^mine for exponents below mine and 2 for e = lime.
+// The exponent bits are built with an unsigned shift (e stays in [-2000, 1100] for the results
+// that pow keeps).
+template <class T> __device__ __forceinline__ T pow_ldexp(T a0, int e)
+{
+  using C = powc<T>;
+  const bool den = e < C::mine;
+  e = den ? e - C::mine : e;
+  T f = den ? C::bits(C::smallest) : T(1);
+  const bool test = e == C::lime;
+  f = test ? add(f, T(1)) : f;
+  e = test ? e - 1 : e;
+  const T s = C::bits((typename C::U)(unsigned)(e + C::maxe) << C::nbm);
+  return mul(mul(a0, s), f);
+}
+template <class T> __device__ __forceinline__ T pow_reduc(T x) { return mul(T(0.0625), floor(mul(T(16), x))); }
+
+// pow_kernel::select: i in 0..16 from x in [0.5, 1); x <- (x - A[i] - B[i/2]) / A[i].  The
+// indices it reads are 9, 13, 3..15 (odd), 1 and i itself, all inside the table.
+template <class T> __device__ __forceinline__ int pow_select(T& x)
+{
+  int i = 1;
+  i = (x <= pow_a(x, 9)) ? 9 : i;
+  i = (x <= pow_a(x, i + 4)) ? i + 4 : i;
+  i = (x <= pow_a(x, i + 2)) ? i + 2 : i;
+  i = (x >= pow_a(x, 1)) ? -1 : i;
+  i = i + 1;
+  const T tmp = pow_a(x, i);
+  x = sub(x, tmp);
+  x = sub(x, pow_b(x, i >> 1));
+  x = div(x, tmp);
+  return i;
+}
+
+template <bool F> __device__ __forceinline__ float pow1(float x, float z)
+{
+  constexpr uint32_t P[4] = {0xbe2a61b2u, 0x3e4d2fa3u, 0xbe800015u, 0x3eaaaaa3u};
+  return mul(mul(z, x), horner<F>(x, P));
+}
+template <bool F> __device__ __forceinline__ double pow1(double x, double z)
+{
+  constexpr uint64_t P[4] = {0x3fdfdb997f5b5cf0ull, 0x400dddefea9edf15ull, 0x401eccbd7f78eb6full, 0x4012aa83b65c9b74ull};
+  constexpr uint64_t Q[5] = {0x3ff0000000000000ull, 0x4022aab49b20914eull, 0x403bffff41c1c9f5ull,
+                             0x4040ccbc1b176402ull, 0x402bffc5918ae92eull};
+  return mul(x, div(mul(z, horner<F>(x, P)), horner<F>(x, Q)));
+}
+template <bool F> __device__ __forceinline__ float pow2(float x)
+{
+  constexpr uint32_t P[4] = {0x3c1a49bcu, 0x3d634d38u, 0x3e75fde1u, 0x3f317218u};
+  return horner<F>(x, P);
+}
+template <bool F> __device__ __forceinline__ double pow2(double x)
+{
+  constexpr uint64_t P[7] = {0x3eef6307d7f2937full, 0x3f242fbe60fc9259ull, 0x3f55d87ec84aef1dull,
+                             0x3f83b2ab6ef133b7ull, 0x3fac6b08d7041a92ull, 0x3fcebfbdff82c56dull,
+                             0x3fe62e42fefa39efull};
+  return horner<F>(x, P);
+}
+
+template <bool F = false, class T> __device__ __forceinline__ T pow_abs(T a0, T a1)
+{
+  using C = powc<T>;
+  const T ax = fabs(a0);
+  int e;
+  T x = pow_frexp(ax, e);
+  int i = pow_select(x);
+  T z = mul(x, x);
+  T w = pow1<F>(x, z);
+  w = madd<F>(T(-0.5), z, w);
+  w = madd<F>(C::bits(C::log2_em1), w, w);
+  z = madd<F>(C::bits(C::log2_em1), x, w);
+  z = add(z, x);
+  w = madd<F>((T)(-i), T(0.0625), (T)e);
+  const T ya = pow_reduc(a1);
+  const T yb = sub(a1, ya);
+  T W = madd<F>(z, a1, mul(w, yb));
+  T Wa = pow_reduc(W);
+  T Wb = sub(W, Wa);
+  W = madd<F>(w, ya, Wa);
+  Wa = pow_reduc(W);
+  const T u = sub(W, Wa);
+  W = add(Wb, u);
+  Wb = pow_reduc(W);
+  w = mul(T(16), add(Wa, Wb));
+  const bool inf_ret = w > C::bits(C::large), zer_ret = w < C::bits(C::low);
+  // toint(w): every w outside [low, large] (NaN aside) is replaced below, so the
+  // conversion is clamped to keep the integer steps defined; in range it truncates as NT2's.
+  e = (int)fmin(fmax(w, T(-32768)), T(32768));
+  Wb = sub(W, Wb);
+  const bool test = Wb > T(0);
+  e = test ? e + 1 : e;
+  Wb = test ? sub(Wb, T(0.0625)) : Wb;
+  z = mul(pow2<F>(Wb), Wb);
+  i = (e > 0) ? e / 16 + 1 : e / 16;
+  e = i * 16 - e;  // 0..16 for every w that is kept
+  w = pow_a(z, min(max(e, 0), 16));
+  z = madd<F>(w, z, w);
+  z = pow_ldexp(z, i);
+  const bool gtax1 = ax > T(1);
+  const T inf = C::bits(C::expmask);
+  if (a1 == inf) z = gtax1 ? inf : T(0);
+  if (a1 == -inf) z = gtax1 ? T(0) : inf;
+  if (ax == inf) z = a1 > T(0) ? inf : (a1 < T(0) ? T(0) : T(1));
+  if (zer_ret) z = T(0);
+  if (inf_ret) z = inf;
+  if (ax == T(1)) z = ax;
+  return a0 == T(0) ? (a1 == T(0) ? T(1) : T(0)) : z;
+}
+
+// Boost.SIMD is_flint (frac(x) == 0, frac = x - trunc(x), NaN for Inf and NaN) and is_odd
+// (is_flint((x - 1) / 2)): boost/simd/predicates/functions/simd/common/{is_flint,is_odd,is_even}.hpp.
+template <class T> __device__ __forceinline__ bool is_flint(T x) { return isfinite(x) && sub(x, trunc(x)) == T(0); }
+
+template <bool F = false, class T> __device__ __forceinline__ T pow(T a0, T a1)
+{
+  const bool ltz = a0 < T(0);
+  T z = pow_abs<F>(a0, a1);
+  if (ltz && is_flint(mul(sub(a1, T(1)), T(0.5)))) z = -z;
+  return (ltz && !is_flint(a1)) ? T(NAN) : z;
+}
+
 }  // namespace math
 }  // namespace nt2cuda
 

@@ -1,7 +1,8 @@
 // trig_impl.cuh -- the trigonometric and hyperbolic functors of
 // nt2cuda_map_f32/f64 (sin, cos, tan, sinpi, cospi in NT2's scalar form or its
-// 128-bit SIMD form; asin, acos, atan; sinh, cosh, tanh), lowered onto the
-// elementwise transform (nt2cuda/trig.cuh, nt2cuda/math.cuh).  Included by
+// 128-bit SIMD form; asin, acos, atan; sinh, cosh, tanh) and the binary
+// atan2 and pow, lowered onto the elementwise transform (nt2cuda/trig.cuh,
+// nt2cuda/math.cuh).  Included by
 // capi_trig_f32.cu and capi_trig_f64.cu, one element type each, which the
 // build compiles in parallel.
 #pragma once
@@ -52,9 +53,10 @@ template <class T> nt2cuda_status dispatch(int op, const T* x, T* y, size_t n, b
   return simd ? trig_impl<false, true>(op, x, y, n, s) : trig_impl<false, false>(op, x, y, n, s);
 }
 
-template <class T> nt2cuda_status atan2_impl(const T* a0, const T* a1, T* y, size_t n, bool fused, nt2cuda_stream s)
+template <class Tag, class T>
+nt2cuda_status binary_impl(const T* a0, const T* a1, T* y, size_t n, bool fused, nt2cuda_stream s)
 {
-  using N = node<tag::atan2_, term<T>, term<T>>;
+  using N = node<Tag, term<T>, term<T>>;
   auto p = make_prog(assign<T, N>{y, N{term<T>{a0}, term<T>{a1}}});
   return launch_status(fused ? transform<true>(p, n, as_stream(s), "trig") : transform<false>(p, n, as_stream(s), "trig"));
 }

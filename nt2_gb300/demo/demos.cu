@@ -15,6 +15,7 @@
 //   io         table files (nt2cuda::load / save): B = A*2 + 1 of a loaded table, saved
 //   trig       trigonometric functors inside one statement and a fold:
 //              y = sin(x) + cos(x)*tan(x*0.25f) + cospi(x)*sinpi(x), globalsum(sin(x))
+//   pow        z = pow(x, y) + pow(y, 2.0f): pow with a table and with a scalar exponent
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -176,6 +177,13 @@ int main(int argc, char** argv)
     g(1) = nt2::globalsum(nt2::sin(x));
     write_table(argv[4], y);
     write_table(argv[5], g);
+  } else if (cmd == "pow") {                              // n; in: x y ; out: z
+    typedef float T;
+    nt2::table<T> x(nt2::of_size(n)), y(nt2::of_size(n)), z;
+    load(x, read_file<T>(argv[3], n));
+    load(y, read_file<T>(argv[4], n));
+    z = nt2::pow(x, y) + nt2::pow(y, T(2));
+    write_table(argv[5], z);
   } else if (cmd == "sigmadelta") {                       // n = pixels; argv[3] = frames; in: frames ; out: bkg var label
     typedef unsigned char T;
     const int nb_frames = std::atoi(argv[3]);

@@ -718,6 +718,257 @@ EXPORT double nt2o_tanh_d(double a0)
   return db(bd(r) ^ bts);
 }
 
+/* ------------------------------------------------------------------ pow -- */
+/* pow(a0, a1) for floating a1, NT2's SIMD form: exponential/functions/simd/common/pow.hpp:20-29
+ * over pow_abs (simd/common/pow_abs.hpp:23-79, the cephes algorithm with 2^(-i/16) tables in
+ * details/pow_kernel.hpp), frexp and ldexp of Boost.SIMD
+ * (boost/simd/ieee/functions/simd/common/{frexp,ldexp}.hpp).  POW_A* are 2^(-i/16) rounded
+ * to the type, POW_B* the rounding residuals of the even entries (2^(-2k/16) - A[2k]). */
+static const uint32_t POW_AF[17] = {0x3f800000u, 0x3f75257du, 0x3f6ac0c7u, 0x3f60ccdfu, 0x3f5744fdu, 0x3f4e248cu,
+                                    0x3f45672au, 0x3f3d08a4u, 0x3f3504f3u, 0x3f2d583fu, 0x3f25fed7u, 0x3f1ef532u,
+                                    0x3f1837f0u, 0x3f11c3d3u, 0x3f0b95c2u, 0x3f05aac3u, 0x3f000000u};
+static const uint32_t POW_BF[9] = {0x00000000u, 0xb1c116deu, 0xb254a58au, 0x318aa837u, 0x324fe77au, 0xb2ac9d5eu,
+                                   0x32a31b71u, 0xb1e0aba1u, 0x00000000u};
+static const uint64_t POW_AD[17] = {0x3ff0000000000000ull, 0x3feea4afa2a490daull, 0x3fed5818dcfba487ull,
+                                    0x3fec199bdd85529cull, 0x3feae89f995ad3adull, 0x3fe9c49182a3f090ull,
+                                    0x3fe8ace5422aa0dbull, 0x3fe7a11473eb0187ull, 0x3fe6a09e667f3bcdull,
+                                    0x3fe5ab07dd485429ull, 0x3fe4bfdad5362a27ull, 0x3fe3dea64c123422ull,
+                                    0x3fe306fe0a31b715ull, 0x3fe2387a6e756238ull, 0x3fe172b83c7d517bull,
+                                    0x3fe0b5586cf9890full, 0x3fe0000000000000ull};
+static const uint64_t POW_BD[9] = {0x0000000000000000ull, 0x3c72ed02d75b3707ull, 0x3c87a1cd345dcc81ull,
+                                   0x3c86e9f156864b27ull, 0xbc8bdd3413b26456ull, 0x3c6d4397afec42e2ull,
+                                   0x3c76f46ad23182e4ull, 0xbc719041b9d78a76ull, 0x0000000000000000ull};
+static const uint32_t POW1_F[4] = {0xbe2a61b2u, 0x3e4d2fa3u, 0xbe800015u, 0x3eaaaaa3u};
+static const uint32_t POW2_F[4] = {0x3c1a49bcu, 0x3d634d38u, 0x3e75fde1u, 0x3f317218u};
+static const uint64_t POW1_DP[4] = {0x3fdfdb997f5b5cf0ull, 0x400dddefea9edf15ull, 0x401eccbd7f78eb6full,
+                                    0x4012aa83b65c9b74ull};
+static const uint64_t POW1_DQ[5] = {0x3ff0000000000000ull, 0x4022aab49b20914eull, 0x403bffff41c1c9f5ull,
+                                    0x4040ccbc1b176402ull, 0x402bffc5918ae92eull};
+static const uint64_t POW2_D[7] = {0x3eef6307d7f2937full, 0x3f242fbe60fc9259ull, 0x3f55d87ec84aef1dull,
+                                   0x3f83b2ab6ef133b7ull, 0x3fac6b08d7041a92ull, 0x3fcebfbdff82c56dull,
+                                   0x3fe62e42fefa39efull};
+#define LOG2_EM1_F 0x3ee2a8edu
+#define LOG2_EM1_D 0x3fdc551d94ae0bf8ull
+#define POWLARGE_F 0x44ffe000u
+#define POWLOW_F   0xc5160000u
+#define POWLARGE_D 0x40cfff8000000000ull
+#define POWLOW_D   0xc0d0c7c000000000ull
+
+static inline int clamp16(int64_t i) { return i < 0 ? 0 : (i > 16 ? 16 : (int)i); }
+static inline int32_t sat_i32(double w) { return (w != w) ? 0 : (w >= 2147483647.0 ? INT32_MAX : (w <= -2147483648.0 ? INT32_MIN : (int32_t)w)); }
+static inline int64_t sat_i64(double w)
+{
+  return (w != w) ? 0 : (w >= 9.2e18 ? INT64_MAX : (w <= -9.2e18 ? INT64_MIN : (int64_t)w));
+}
+
+static float pow_frexp_f(float a0, int32_t* e)
+{
+  const int den = fabsf(a0) < fb(0x00800000u) && a0 != 0.0f;
+  const float aa0 = den ? 8388608.0f * a0 : a0;
+  const int32_t t = den ? 23 : 0;
+  const uint32_t b = bf(aa0);
+  int32_t r1 = (int32_t)((b & 0x7f800000u) >> 23) - 126;
+  float r0 = fb((b & ~0x7f800000u) | 0x3f000000u);
+  const int test0 = aa0 != 0.0f, test1 = r1 > 128;
+  r1 = (!test1 && test0) ? r1 : 0;
+  r1 -= t;
+  r0 = test0 ? r0 + (test1 ? aa0 : 0.0f) : 0.0f;
+  *e = r1;
+  return r0;
+}
+static float pow_ldexp_f(float a0, int32_t e)
+{
+  float f = 1.0f;
+  const int den = e < -126;
+  e = den ? e + 126 : e;
+  f = den ? fb(0x00800000u) : 1.0f;
+  const int test = e == 128;
+  f = f + (test ? 1.0f : 0.0f);
+  e = e - (test ? 1 : 0);
+  const uint32_t bits = ((uint32_t)(e + 127)) << 23;
+  return (a0 * fb(bits)) * f;
+}
+static double pow_frexp_d(double a0, int64_t* e)
+{
+  const int den = fabs(a0) < db(0x0010000000000000ull) && a0 != 0.0;
+  const double aa0 = den ? 4503599627370496.0 * a0 : a0;
+  const int64_t t = den ? 52 : 0;
+  const uint64_t b = bd(aa0);
+  int64_t r1 = (int64_t)((b & 0x7ff0000000000000ull) >> 52) - 1022;
+  double r0 = db((b & ~0x7ff0000000000000ull) | 0x3fe0000000000000ull);
+  const int test0 = aa0 != 0.0, test1 = r1 > 1024;
+  r1 = (!test1 && test0) ? r1 : 0;
+  r1 -= t;
+  r0 = test0 ? r0 + (test1 ? aa0 : 0.0) : 0.0;
+  *e = r1;
+  return r0;
+}
+static double pow_ldexp_d(double a0, int64_t e)
+{
+  double f = 1.0;
+  const int den = e < -1022;
+  e = den ? e + 1022 : e;
+  f = den ? db(0x0010000000000000ull) : 1.0;
+  const int test = e == 1024;
+  f = f + (test ? 1.0 : 0.0);
+  e = e - (test ? 1 : 0);
+  const uint64_t bits = ((uint64_t)(e + 1023)) << 52;
+  return (a0 * db(bits)) * f;
+}
+static inline float reduc_f(float x) { return 0.0625f * floorf(16.0f * x); }
+static inline double reduc_d(double x) { return 0.0625 * floor(16.0 * x); }
+
+/* pow_kernel<float>::select: x <- (x - A[i] - B[i/2]) / A[i] */
+static int pow_select_f(float* xp)
+{
+  float x = *xp;
+  int i = 1;
+  i = (x <= fb(POW_AF[9])) ? 9 : i;
+  i = i + ((x <= fb(POW_AF[clamp16(i + 4)])) ? 4 : 0);
+  i = i + ((x <= fb(POW_AF[clamp16(i + 2)])) ? 2 : 0);
+  i = (x >= fb(POW_AF[1])) ? -1 : i;
+  i = i + 1;
+  const float tmp = fb(POW_AF[i]);
+  x -= tmp;
+  x -= fb(POW_BF[i >> 1]);
+  x /= tmp;
+  *xp = x;
+  return i;
+}
+static int pow_select_d(double* xp)
+{
+  double x = *xp;
+  int i = 1;
+  i = (x <= db(POW_AD[9])) ? 9 : i;
+  i = i + ((x <= db(POW_AD[clamp16(i + 4)])) ? 4 : 0);
+  i = i + ((x <= db(POW_AD[clamp16(i + 2)])) ? 2 : 0);
+  i = (x >= db(POW_AD[1])) ? -1 : i;
+  i = i + 1;
+  const double tmp = db(POW_AD[i]);
+  x -= tmp;
+  x -= db(POW_BD[i >> 1]);
+  x /= tmp;
+  *xp = x;
+  return i;
+}
+
+static float pow_abs_f(float a0, float a1)
+{
+  int32_t e;
+  const float ax = fabsf(a0);
+  float x = pow_frexp_f(ax, &e);
+  int32_t i = pow_select_f(&x);
+  float z = x * x;
+  float w = (z * x) * horner_f(x, POW1_F, 4);
+  w = -0.5f * z + w;
+  w = fb(LOG2_EM1_F) * w + w;
+  z = fb(LOG2_EM1_F) * x + w;
+  z += x;
+  w = (float)(-i) * 0.0625f + (float)e;
+  const float ya = reduc_f(a1);
+  const float yb = a1 - ya;
+  float W = z * a1 + w * yb;
+  float Wa = reduc_f(W);
+  float Wb = W - Wa;
+  W = w * ya + Wa;
+  Wa = reduc_f(W);
+  const float u = W - Wa;
+  W = Wb + u;
+  Wb = reduc_f(W);
+  w = 16.0f * (Wa + Wb);
+  const int inf_ret = w > fb(POWLARGE_F), zer_ret = w < fb(POWLOW_F);
+  e = sat_i32(w);
+  Wb = W - Wb;
+  const int test = Wb > 0.0f;
+  e = test ? e + 1 : e;
+  Wb = Wb - (test ? 0.0625f : 0.0f);
+  z = horner_f(Wb, POW2_F, 4) * Wb;
+  i = (e > 0) ? e / 16 + 1 : e / 16;
+  e = i * 16 - e;
+  w = fb(POW_AF[clamp16(e)]);
+  z = w * z + w;
+  z = pow_ldexp_f(z, i);
+  const int gtax1 = ax > 1.0f;
+  z = (a1 == INFINITY) ? (gtax1 ? INFINITY : 0.0f) : z;
+  z = (a1 == -INFINITY) ? (gtax1 ? 0.0f : INFINITY) : z;
+  z = (ax == INFINITY) ? (a1 > 0.0f ? INFINITY : (a1 < 0.0f ? 0.0f : 1.0f)) : z;
+  z = zer_ret ? 0.0f : z;
+  z = inf_ret ? INFINITY : z;
+  z = (ax == 1.0f) ? ax : z;
+  return (a0 == 0.0f) ? (a1 == 0.0f ? 1.0f : 0.0f) : z;
+}
+static double pow_abs_d(double a0, double a1)
+{
+  int64_t e;
+  const double ax = fabs(a0);
+  double x = pow_frexp_d(ax, &e);
+  int64_t i = pow_select_d(&x);
+  double z = x * x;
+  double w = x * (z * horner_d(x, POW1_DP, 4) / horner_d(x, POW1_DQ, 5));
+  w = -0.5 * z + w;
+  w = db(LOG2_EM1_D) * w + w;
+  z = db(LOG2_EM1_D) * x + w;
+  z += x;
+  w = (double)(-i) * 0.0625 + (double)e;
+  const double ya = reduc_d(a1);
+  const double yb = a1 - ya;
+  double W = z * a1 + w * yb;
+  double Wa = reduc_d(W);
+  double Wb = W - Wa;
+  W = w * ya + Wa;
+  Wa = reduc_d(W);
+  const double u = W - Wa;
+  W = Wb + u;
+  Wb = reduc_d(W);
+  w = 16.0 * (Wa + Wb);
+  const int inf_ret = w > db(POWLARGE_D), zer_ret = w < db(POWLOW_D);
+  e = sat_i64(w);
+  Wb = W - Wb;
+  const int test = Wb > 0.0;
+  e = test ? e + 1 : e;
+  Wb = Wb - (test ? 0.0625 : 0.0);
+  z = horner_d(Wb, POW2_D, 7) * Wb;
+  i = (e > 0) ? e / 16 + 1 : e / 16;
+  e = i * 16 - e;
+  w = db(POW_AD[clamp16(e)]);
+  z = w * z + w;
+  z = pow_ldexp_d(z, i);
+  const int gtax1 = ax > 1.0;
+  z = (a1 == INFINITY) ? (gtax1 ? INFINITY : 0.0) : z;
+  z = (a1 == -INFINITY) ? (gtax1 ? 0.0 : INFINITY) : z;
+  z = (ax == INFINITY) ? (a1 > 0.0 ? INFINITY : (a1 < 0.0 ? 0.0 : 1.0)) : z;
+  z = zer_ret ? 0.0 : z;
+  z = inf_ret ? INFINITY : z;
+  z = (ax == 1.0) ? ax : z;
+  return (a0 == 0.0) ? (a1 == 0.0 ? 1.0 : 0.0) : z;
+}
+/* is_flint(x) = frac(x) == 0 with frac = x - trunc(x) (NaN for Inf/NaN); is_odd(x) =
+ * is_flint((x - 1) / 2) (boost/simd/predicates/functions/simd/common/{is_flint,is_even,is_odd}.hpp) */
+static inline int is_flint_f(float x) { return isfinite(x) && (x - truncf(x)) == 0.0f; }
+static inline int is_flint_d(double x) { return isfinite(x) && (x - trunc(x)) == 0.0; }
+EXPORT float nt2o_pow_f(float a0, float a1)
+{
+  const int ltz = a0 < 0.0f;
+  float z = pow_abs_f(a0, a1);
+  z = (is_flint_f((a1 - 1.0f) * 0.5f) && ltz) ? -z : z;
+  return (ltz && !is_flint_f(a1)) ? NAN : z;
+}
+EXPORT double nt2o_pow_d(double a0, double a1)
+{
+  const int ltz = a0 < 0.0;
+  double z = pow_abs_d(a0, a1);
+  z = (is_flint_d((a1 - 1.0) * 0.5) && ltz) ? -z : z;
+  return (ltz && !is_flint_d(a1)) ? NAN : z;
+}
+EXPORT void nt2o_pow2_f(const float* a0, const float* a1, float* y, size_t n)
+{
+  for (size_t i = 0; i < n; ++i) y[i] = nt2o_pow_f(a0[i], a1[i]);
+}
+EXPORT void nt2o_pow2_d(const double* a0, const double* a1, double* y, size_t n)
+{
+  for (size_t i = 0; i < n; ++i) y[i] = nt2o_pow_d(a0[i], a1[i]);
+}
+
 /* ------------------------------------------------------------- maps ------ */
 enum { OP_EXP = 0, OP_LOG = 1, OP_ERFC = 2, OP_NORMCDF = 3, OP_FASTNORMCDF = 4, OP_SQRT = 5,
        OP_ERFC_SCALAR = 6, OP_EXP2 = 7, OP_EXP10 = 8, OP_LOG2 = 9, OP_LOG10 = 10, OP_EXPM1 = 11,

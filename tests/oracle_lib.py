@@ -50,6 +50,10 @@ SIGS = {
     "nt2o_trig_d": (C.c_int, [C.c_int, f64p, f64p, sz, C.c_int]),
     "nt2o_atan2_f": (None, [f32p, f32p, f32p, sz]),
     "nt2o_atan2_d": (None, [f64p, f64p, f64p, sz]),
+    "nt2o_pow_f": (C.c_float, [C.c_float, C.c_float]),
+    "nt2o_pow_d": (C.c_double, [C.c_double, C.c_double]),
+    "nt2o_pow2_f": (None, [f32p, f32p, f32p, sz]),
+    "nt2o_pow2_d": (None, [f64p, f64p, f64p, sz]),
     "nt2o_rem_pio2_exact_f": (C.c_int, [C.c_float, C.POINTER(C.c_float)]),
     "nt2o_rem_pio2_exact_d": (C.c_int, [C.c_double, C.POINTER(C.c_double)]),
     "nt2o_exp10_f": (C.c_float, [C.c_float]),
@@ -138,6 +142,16 @@ def atan2(a0: np.ndarray, a1: np.ndarray) -> np.ndarray:
     a1 = np.ascontiguousarray(a1, dtype=a0.dtype)
     y = np.empty_like(a0)
     (L.nt2o_atan2_f if a0.dtype == np.float32 else L.nt2o_atan2_d)(a0, a1, y, a0.size)
+    return y
+
+
+def pow_(a0: np.ndarray, a1: np.ndarray) -> np.ndarray:
+    """NT2's pow(a0, a1) for floating a1 (SIMD form), elementwise."""
+    L = load()
+    a0 = np.ascontiguousarray(a0)
+    a1 = np.ascontiguousarray(a1, dtype=a0.dtype)
+    y = np.empty_like(a0)
+    (L.nt2o_pow2_f if a0.dtype == np.float32 else L.nt2o_pow2_d)(a0, a1, y, a0.size)
     return y
 
 

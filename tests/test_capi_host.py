@@ -54,6 +54,8 @@ def test_argument_validation_without_device(cuda_lib):
     assert L.nt2cuda_map_f32(42, None, None, 0, 0, None) in (0, 1)
     assert L.nt2cuda_map_f32(12, None, None, 0, 4, None) == 1     # unknown flag bit
     assert L.nt2cuda_map_f64(14, None, None, 5, 2, None) == 1     # null tables
+    assert L.nt2cuda_pow_f32(None, None, None, 5, 0, None) == 1   # null tables
+    assert L.nt2cuda_pow_f64(None, None, None, 0, 2, None) == 1   # SIMD128 is not a pow flag
 
 
 def test_tuning_table_roundtrip(cuda_lib):

@@ -87,10 +87,12 @@ def test_elementwise_statements(gpu, cuda_lib, shift):
         assert st == 0
         at = Guarded(n, torch.float32, shift)
         gpu.atan2(x, r, out=at.view)
+        pw = Guarded(n, torch.float32, shift)
+        gpu.pow(r, x, out=pw.view)
         cm = Guarded(n, torch.int32, shift)
         gpu.mandelbrot(rand(n, torch.float32, -1.5, 1.5, 9), rand(n, torch.float32, -1.5, 1.5, 10), out=cm.view)
         sync()
-        for t in (y, gr, gr8, yy, uu, vv, at, cm):
+        for t in (y, gr, gr8, yy, uu, vv, at, pw, cm):
             assert t.intact(), n
     h, w = 37, 41
     grid = Guarded(h * w, torch.int32, shift)

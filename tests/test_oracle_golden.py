@@ -360,3 +360,49 @@ def test_hyperbolic_cover(oracle, fn, dt):
         assert m <= bound + 0.5, (fn, dt, lo, hi, m, x[w])
         over = sum(u(float(a), float(b)) > bound for a, b in zip(y, ref))
         assert over <= 2e-3 * x.size, (fn, dt, lo, hi, over)
+
+
+# pow(a0, a1), floating a1: modules/core/exponential/unit/scalar/pow.cpp:14-24 and
+# unit/simd/pow.cpp (specials, 0 ulp), pow_real_int (pow(2, -3) = 1/8, +-Inf and NaN bases with odd
+# and even exponents); cover/scalar/pow.cpp: a0 in [0, 100], a1 in [-10, 10], 2 ulp against cephes
+# long-double pow (the reference here is mpmath at 40 digits, or a float64/long double pow)
+POW_SPECIALS = [
+    (INF, INF, INF), (-INF, -INF, NAN), (INF, -INF, 0.0), (NAN, NAN, NAN),
+    (-1.0, -1.0, -1.0), (1.0, 1.0, 1.0), (0.0, 0.0, 1.0), (-1.0, 5.0, -1.0), (-1.0, 6.0, 1.0),
+    (0.0, 1.0, 0.0), (INF, 3.0, INF), (-INF, 3.0, -INF), (NAN, 3.0, NAN), (INF, 4.0, INF),
+    (-INF, 4.0, INF), (NAN, 4.0, NAN), (2.0, -3.0, 0.125), (-1.0, 3.0, -1.0), (-1.0, 4.0, 1.0),
+    (1.0, 3.0, 1.0), (2.0, 3.0, 8.0), (0.0, 3.0, 0.0), (1.0, 4.0, 1.0), (0.0, 4.0, 0.0),
+    (4.0, 3.0, 64.0), (4.0, -3.0, 0.015625), (7.0, 4.0, 2401.0),
+]
+
+
+@pytest.mark.parametrize("prec", ["f", "d"])
+def test_pow_special_values(oracle, prec):
+    L = oracle.load()
+    f = getattr(L, f"nt2o_pow_{prec}")
+    u = ulp_f if prec == "f" else ulp_d
+    cast = f32 if prec == "f" else float
+    for a0, a1, r in POW_SPECIALS:
+        assert u(L, f(a0, a1), cast(r)) == 0.0, (prec, a0, a1, f(a0, a1))
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_pow_cover(oracle, dt):
+    rng = np.random.default_rng(17)
+    n = 20000
+    a0 = rng.uniform(0, 100, n).astype(dt)
+    a1 = rng.uniform(-10, 10, n).astype(dt)
+    a1[::4] = np.round(a1[::4])                    # cover/simd/pow.cpp draws integer exponents
+    if dt == np.float32:
+        ref = np.power(a0.astype(np.float64), a1.astype(np.float64)).astype(dt)
+    else:
+        mpmath = pytest.importorskip("mpmath")
+        mpmath.mp.dps = 40
+        ref = np.array([float(mpmath.power(mpmath.mpf(float(x)), mpmath.mpf(float(y)))) for x, y in zip(a0, a1)])
+    m, w = oracle.max_ulp(oracle.pow_(a0, a1), ref)
+    assert m <= 2.0, (dt, m, a0[w], a1[w])
+    # negative bases with integer exponents: the sign of the odd powers, the same magnitudes
+    b = -a0[::4]
+    m, w = oracle.max_ulp(oracle.pow_(b, a1[::4]), (np.where(a1[::4] % 2 == 1, -1, 1) * np.abs(ref[::4])).astype(dt))
+    assert m <= 2.0, (dt, m, b[w])
+    assert np.isnan(oracle.pow_(-a0[1::4] - 1, a1[1::4] + np.float32(0.5) * (a1[1::4] == np.round(a1[1::4])))).all()
