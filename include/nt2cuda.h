@@ -122,7 +122,14 @@ enum {
   NT2CUDA_OP_ATAN = 19,
   NT2CUDA_OP_SINH = 20,       /* modules/core/hyperbolic: simd/common/{sinh,tanh}.hpp, generic/cosh.hpp */
   NT2CUDA_OP_COSH = 21,
-  NT2CUDA_OP_TANH = 22
+  NT2CUDA_OP_TANH = 22,
+  NT2CUDA_OP_CBRT = 23,       /* modules/core/exponential: simd/common/cbrt.hpp (SIMD form) */
+  NT2CUDA_OP_SQRT1PM1 = 24,   /* generic/sqrt1pm1.hpp: sqrt(1+x)-1 */
+  NT2CUDA_OP_EXPRECNEG = 25,  /* generic/exprecneg.hpp: exp(-1/x) */
+  NT2CUDA_OP_EXPRECNEGC = 26, /* generic/exprecnegc.hpp: -expm1(-1/x) */
+  NT2CUDA_OP_EXPX2 = 27,      /* simd/common/expx2.hpp: exp(x*x) */
+  NT2CUDA_OP_REALSQRT = 28,   /* generic/realsqrt.hpp: sqrt (NT2 asserts x >= 0) */
+  NT2CUDA_OP_REALLOG = 29     /* generic/reallog.hpp: log (NT2 asserts x >= 0) */
 };
 
 /* out = atan2(a0, a1) elementwise (NT2's SIMD form,
@@ -141,6 +148,24 @@ nt2cuda_status nt2cuda_pow_f32(const float* a0, const float* a1, float* out, siz
                                nt2cuda_stream stream);
 nt2cuda_status nt2cuda_pow_f64(const double* a0, const double* a1, double* out, size_t n, int flags,
                                nt2cuda_stream stream);
+
+/* Binary functors of nt2cuda_map2_*, NT2's SIMD forms (paths under
+ * modules/core/exponential/include/nt2/exponential/functions/ unless noted). */
+enum {
+  NT2CUDA_OP2_ATAN2 = 0,        /* as nt2cuda_atan2_* */
+  NT2CUDA_OP2_POW = 1,          /* as nt2cuda_pow_* */
+  NT2CUDA_OP2_POW_ABS = 2,      /* simd/common/pow_abs.hpp: |a0|^a1 */
+  NT2CUDA_OP2_REALPOW = 3,      /* simd/common/realpow.hpp: pow (NT2 asserts a0 >= 0 or a1 integral) */
+  NT2CUDA_OP2_LOGSPACE_ADD = 4, /* simd/common/logspace_add.hpp: log(exp(a0) + exp(a1)) */
+  NT2CUDA_OP2_LOGSPACE_SUB = 5, /* simd/common/logspace_sub.hpp: log(exp(a0) - exp(a1)) */
+  NT2CUDA_OP2_EXPX2 = 6         /* simd/common/expx2.hpp:52-74: exp(sign(a1) * a0^2) */
+};
+/* out = op(a0, a1) elementwise.  Replaces `z = nt2::op(x, y)` over two tables of one
+ * floating type, evaluated by transform_.  flags: NT2CUDA_MAP_FUSED or 0. */
+nt2cuda_status nt2cuda_map2_f32(int op, const float* a0, const float* a1, float* out, size_t n, int flags,
+                                nt2cuda_stream stream);
+nt2cuda_status nt2cuda_map2_f64(int op, const double* a0, const double* a1, double* out, size_t n, int flags,
+                                nt2cuda_stream stream);
 
 /* Flags of nt2cuda_map_*. */
 #define NT2CUDA_MAP_FUSED 1     /* hardware FMA (the `fused` convention above) */

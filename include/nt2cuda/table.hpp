@@ -317,6 +317,13 @@ NT2CUDA_FN1(atan, atan_)
 NT2CUDA_FN1(sinh, sinh_)
 NT2CUDA_FN1(cosh, cosh_)
 NT2CUDA_FN1(tanh, tanh_)
+NT2CUDA_FN1(cbrt, cbrt_)
+NT2CUDA_FN1(sqrt1pm1, sqrt1pm1_)
+NT2CUDA_FN1(exprecneg, exprecneg_)
+NT2CUDA_FN1(exprecnegc, exprecnegc_)
+NT2CUDA_FN1(expx2, expx2_)
+NT2CUDA_FN1(realsqrt, sqrt_)
+NT2CUDA_FN1(reallog, log_)
 NT2CUDA_FN1(sqrt, sqrt_)
 NT2CUDA_FN1(sqr, sqr_)
 NT2CUDA_FN1(erfc, erfc_)
@@ -334,6 +341,11 @@ NT2CUDA_FN1(minusone, minusone_)
 NT2CUDA_FN2(max, max_)
 NT2CUDA_FN2(atan2, atan2_)
 NT2CUDA_FN2(pow, pow_)
+NT2CUDA_FN2(realpow, pow_)
+NT2CUDA_FN2(pow_abs, pow_abs_)
+NT2CUDA_FN2(logspace_add, logspace_add_)
+NT2CUDA_FN2(logspace_sub, logspace_sub_)
+NT2CUDA_FN2(expx2, expx2s_)
 NT2CUDA_FN2(min, min_)
 NT2CUDA_FN2(adds, adds_)
 NT2CUDA_FN2(subs, subs_)

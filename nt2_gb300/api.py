@@ -16,7 +16,10 @@ from ._lib import SdStream, check, lib
 
 OPS = {"exp": 0, "log": 1, "erfc": 2, "normcdf": 3, "fastnormcdf": 4, "sqrt": 5, "exp2": 6, "exp10": 7, "log2": 8,
        "log10": 9, "expm1": 10, "log1p": 11, "sin": 12, "cos": 13, "tan": 14, "sinpi": 15, "cospi": 16,
-       "asin": 17, "acos": 18, "atan": 19, "sinh": 20, "cosh": 21, "tanh": 22}
+       "asin": 17, "acos": 18, "atan": 19, "sinh": 20, "cosh": 21, "tanh": 22, "cbrt": 23, "sqrt1pm1": 24,
+       "exprecneg": 25, "exprecnegc": 26, "expx2": 27, "realsqrt": 28, "reallog": 29}
+# binary functors of nt2cuda_map2_f32/f64
+OPS2 = {"atan2": 0, "pow": 1, "pow_abs": 2, "realpow": 3, "logspace_add": 4, "logspace_sub": 5, "expx2": 6}
 CDF = {"normcdf": 0, "fastnormcdf": 1}
 
 
@@ -44,7 +47,8 @@ MAP_FUSED, MAP_SIMD128 = 1, 2
 def map_(op: str, x: torch.Tensor, out: torch.Tensor | None = None, fused: bool = False,
          simd128: bool = False) -> torch.Tensor:
     """out = nt2::op(x) for op in exp, log, erfc, normcdf, fastnormcdf, sqrt, exp2, exp10, log2, log10, expm1,
-    log1p, sin, cos, tan, sinpi, cospi, asin, acos, atan, sinh, cosh, tanh.  The trigonometric ops reduce each
+    log1p, sin, cos, tan, sinpi, cospi, asin, acos, atan, sinh, cosh, tanh, cbrt, sqrt1pm1, exprecneg, exprecnegc,
+    expx2, realsqrt, reallog.  The trigonometric ops reduce each
     element on its own (NT2's scalar
     code); with simd128 they reduce each 16-byte pack of x with the method NT2's 128-bit SIMD code picks for
     the pack's largest |x| (tables that are not 16-byte aligned: scalar code throughout)."""
@@ -75,6 +79,25 @@ def _binary(name: str, a0: torch.Tensor, a1: torch.Tensor, out: torch.Tensor | N
     else:
         raise TypeError(f"{name} takes float32 or float64 tables")
     check(st, name)
+    return out
+
+
+def map2(op: str, a0: torch.Tensor, a1: torch.Tensor, out: torch.Tensor | None = None,
+         fused: bool = False) -> torch.Tensor:
+    """out = nt2::op(a0, a1) elementwise over two tables of one floating type, op in OPS2."""
+    if a0.numel() != a1.numel():
+        raise ValueError("a0 and a1 must have the same size")
+    out = torch.empty_like(a0) if out is None else out
+    L = lib()
+    if a0.dtype == torch.float32:
+        st = L.nt2cuda_map2_f32(OPS2[op], _dev(a0), _dev(a1, torch.float32), _dev(out, torch.float32),
+                                a0.numel(), MAP_FUSED if fused else 0, _stream())
+    elif a0.dtype == torch.float64:
+        st = L.nt2cuda_map2_f64(OPS2[op], _dev(a0), _dev(a1, torch.float64), _dev(out, torch.float64),
+                                a0.numel(), MAP_FUSED if fused else 0, _stream())
+    else:
+        raise TypeError(f"{op} takes float32 or float64 tables")
+    check(st, f"map2({op})")
     return out
 
 

@@ -51,6 +51,9 @@ template <class T> struct simd128_ {};
 struct asin_ {}; struct acos_ {}; struct atan_ {}; struct atan2_ {};
 struct sinh_ {}; struct cosh_ {}; struct tanh_ {};
 struct pow_ {};
+// the rest of NT2's exponential family (expx2s_ is the two-argument expx2)
+struct cbrt_ {}; struct sqrt1pm1_ {}; struct exprecneg_ {}; struct exprecnegc_ {}; struct expx2_ {};
+struct expx2s_ {}; struct pow_abs_ {}; struct logspace_add_ {}; struct logspace_sub_ {};
 }  // namespace tag
 
 // ------------------------------------------------------------ tree nodes
@@ -132,6 +135,15 @@ NT2CUDA_BIN(selinc_, (a ? (B)(b + 1) : b))
 NT2CUDA_BIN(seldec_, (a ? (B)(b - 1) : b))
 NT2CUDA_BIN(atan2_, trig::atan2<F>(a, (A)b))
 NT2CUDA_BIN(pow_, math::pow<F>(a, (A)b))
+NT2CUDA_BIN(pow_abs_, math::pow_abs<F>(a, (A)b))
+NT2CUDA_BIN(logspace_add_, math::logspace_add<F>(a, (A)b))
+NT2CUDA_BIN(logspace_sub_, math::logspace_sub<F>(a, (A)b))
+NT2CUDA_BIN(expx2s_, math::expx2<F>(a, (A)b))
+NT2CUDA_UN(cbrt_, math::cbrt<F>(a))
+NT2CUDA_UN(sqrt1pm1_, math::sqrt1pm1<F>(a))
+NT2CUDA_UN(exprecneg_, math::exprecneg<F>(a))
+NT2CUDA_UN(exprecnegc_, math::exprecnegc<F>(a))
+NT2CUDA_UN(expx2_, math::expx2<F>(a))
 NT2CUDA_UN(unary_minus_, (A)(-a))
 NT2CUDA_UN(sqr_, detail::mul(a, a))
 NT2CUDA_UN(sqrt_, math::sqrt_(a))

@@ -865,6 +865,120 @@ template <bool F = false, class T> __device__ __forceinline__ T pow(T a0, T a1)
   return (ltz && !is_flint(a1)) ? T(NAN) : z;
 }
 
+// ------------------------------------------------- rest of the exp family
+// cbrt, NT2's SIMD forms (modules/core/exponential/include/nt2/exponential/functions/simd/
+// common/cbrt.hpp:36-89 double, :91-142 float): Boost.SIMD fast_frexp (no special cases), a
+// degree-4 polynomial, the exponent divided by 3 with 2^(1/3) or 2^(2/3) for the remainder,
+// fast_ldexp, then Newton steps (two in double, one in float); zeros and infinities are
+// returned as they are.
+__device__ __forceinline__ int cbrt_split(int e, int& rem)
+{
+  int e1 = e < 0 ? -e : e;
+  rem = e1 - (e1 / 3) * 3;
+  e1 /= 3;
+  return e > 0 ? e1 : (e < 0 ? -e1 : 0);  // negate(e1, e): e1 with the sign of e, 0 for 0
+}
+template <bool F = false> __device__ __forceinline__ float cbrt(float a0)
+{
+  constexpr uint32_t P[5] = {0xbe09e49au, 0x3f0bf0feu, 0xbf745265u, 0x3f91eb77u, 0x3ece0609u};
+  float z = fabsf(a0);
+  const bool den = z < fbits(0x00800000u);
+  z = den ? mul(z, 8388608.0f) : z;
+  const float f = den ? fbits(0x3ba14518u) : 1.0f;  // 2^(-23/3)
+  const uint32_t b = __float_as_uint(z);
+  int e = (int)((b & 0x7f800000u) >> 23) - 126;    // e <= 129 (Inf/NaN): e / 3 stays small
+  float x = fbits((b & ~0x7f800000u) | 0x3f000000u);
+  x = horner<F>(x, P);
+  const bool flag = e >= 0;
+  int rem;
+  e = cbrt_split(e, rem);
+  float fact = rem == 1 ? (flag ? fbits(0x3fa14518u) : fbits(0x3f4b2ff5u)) : 1.0f;
+  fact = rem == 2 ? (flag ? fbits(0x3fcb2ff5u) : fbits(0x3f214518u)) : fact;
+  x = mul(mul(x, fact), fbits((uint32_t)(e + 127) << 23));
+  x = sub(x, mul(sub(x, div(z, mul(x, x))), fbits(0x3eaaaaabu)));
+  x = mul(__uint_as_float(__float_as_uint(x) | (__float_as_uint(a0) & 0x80000000u)), f);
+  return (a0 == 0.0f || isinf(a0)) ? a0 : x;
+}
+template <bool F = false> __device__ __forceinline__ double cbrt(double a0)
+{
+  constexpr uint64_t P[5] = {0xbfc13c93386fdff6ull, 0x3fe17e1fc7e59d58ull, 0xbfee8a4ca3ba37b8ull,
+                             0x3ff23d6ee505873aull, 0x3fd9c0c12122a4feull};
+  double z = fabs(a0);
+  const bool den = z < dbits(0x0010000000000000ull);
+  z = den ? mul(z, 4503599627370496.0) : z;
+  const double f = den ? dbits(0x3ed428a2f98d7286ull) : 1.0;  // 2^(-52/3)
+  const uint64_t b = (uint64_t)__double_as_longlong(z);
+  int e = (int)((b & 0x7ff0000000000000ull) >> 52) - 1022;
+  double x = dbits((b & ~0x7ff0000000000000ull) | 0x3fe0000000000000ull);
+  x = horner<F>(x, P);
+  const bool flag = e >= 0;
+  int rem;
+  e = cbrt_split(e, rem);
+  double fact = rem == 1 ? (flag ? dbits(0x3ff428a2f98d728bull) : dbits(0x3fe965fea53d6e3dull)) : 1.0;
+  fact = rem == 2 ? (flag ? dbits(0x3ff965fea53d6e3dull) : dbits(0x3fe428a2f98d728bull)) : fact;
+  x = mul(mul(x, fact), dbits((uint64_t)(e + 1023) << 52));
+  const double third = dbits(0x3fd5555555555555ull);
+  x = sub(x, mul(sub(x, div(z, mul(x, x))), third));
+  x = sub(x, mul(sub(x, div(z, mul(x, x))), third));
+  x = mul(dbits((uint64_t)__double_as_longlong(x) | ((uint64_t)__double_as_longlong(a0) & 0x8000000000000000ull)), f);
+  return (a0 == 0.0 || isinf(a0)) ? a0 : x;
+}
+
+// sqrt1pm1(x) = sqrt(1+x) - 1 (generic/sqrt1pm1.hpp:27-33)
+template <bool F = false, class T> __device__ __forceinline__ T sqrt1pm1(T a0)
+{
+  const T t = sqrt_(add(a0, T(1)));
+  return fabs(a0) < T(0.5) ? div(a0, add(t, T(1))) : sub(t, T(1));
+}
+// exprecneg(x) = exp(-1/x), exprecnegc(x) = -expm1(-1/x) (generic/exprecneg.hpp:27,
+// generic/exprecnegc.hpp:27; rec is the IEEE quotient 1/x)
+template <bool F = false, class T> __device__ __forceinline__ T exprecneg(T a0) { return exp<F>(-div(T(1), a0)); }
+template <bool F = false, class T> __device__ __forceinline__ T exprecnegc(T a0) { return -expm1<F>(-div(T(1), a0)); }
+
+// expx2(x) = exp(x^2) and expx2(x, s) = exp(sign(s) x^2) (simd/common/expx2.hpp:31-50, :52-74):
+// x^2 = u + u1 with u = m^2, m a multiple of Expx2c1 (32 float, 128 double) near |x|.
+template <class T> __device__ __forceinline__ T expx2_c1() { return sizeof(T) == 4 ? T(32) : T(128); }
+template <bool F = false, class T> __device__ __forceinline__ T expx2(T a0)
+{
+  const T x = fabs(a0);
+  const T m = mul(expx2_c1<T>(), floor(madd<F>(div(T(1), expx2_c1<T>()), x, T(0.5))));
+  const T f = sub(x, m);
+  const T u = mul(m, m);
+  const T u1 = madd<F>(add(m, m), f, mul(f, f));
+  const T inf = T(INFINITY);
+  const T r = add(u, u1) > hyp<T>::maxlog() ? inf : mul(exp<F>(u), exp<F>(u1));
+  return x == inf ? x : r;
+}
+template <bool F = false, class T> __device__ __forceinline__ T expx2(T a0, T s)
+{
+  const T sgn = signbit(s) ? T(-1) : T(1);  // signnz: -1 for -0
+  const T x = mul(a0, sgn);
+  const T m = mul(expx2_c1<T>(), floor(madd<F>(div(T(1), expx2_c1<T>()), x, T(0.5))));
+  const T f = sub(x, m);
+  const T u = mul(sgn, mul(m, m));
+  const T u1 = mul(sgn, madd<F>(add(m, m), f, mul(f, f)));
+  const T inf = T(INFINITY);
+  const T r = add(u, u1) > hyp<T>::maxlog() ? inf : mul(exp<F>(u), exp<F>(u1));
+  return x == inf ? x : r;
+}
+
+// logspace_add(a, b) = log(exp(a) + exp(b)), logspace_sub(a, b) = log(exp(a) - exp(b))
+// (simd/common/logspace_add.hpp:27-36, logspace_sub.hpp:27-35; the SIMD forms evaluate both
+// branches of logspace_sub and select, the value is the selected one's)
+template <bool F = false, class T> __device__ __forceinline__ T logspace_add(T a0, T a1)
+{
+  const T t = -fabs(sub(a0, a1));
+  const T r = add(a0 > a1 ? a0 : a1, log1p<F>(exp<F>(t)));
+  return isnan(t) ? add(a0, a1) : r;
+}
+template <bool F = false, class T> __device__ __forceinline__ T logspace_sub(T a0, T a1)
+{
+  const T x = sub(a1, a0);
+  const T log_2 = sizeof(T) == 4 ? (T)fbits(0x3f317218u) : (T)dbits(0x3fe62e42fefa39efull);
+  const T t = x > -log_2 ? log<F>(-expm1<F>(x)) : log1p<F>(-exp<F>(x));
+  return add(a0, t);
+}
+
 }  // namespace math
 }  // namespace nt2cuda
 

@@ -15,7 +15,8 @@
 //   io         table files (nt2cuda::load / save): B = A*2 + 1 of a loaded table, saved
 //   trig       trigonometric functors inside one statement and a fold:
 //              y = sin(x) + cos(x)*tan(x*0.25f) + cospi(x)*sinpi(x), globalsum(sin(x))
-//   pow        z = pow(x, y) + pow(y, 2.0f): pow with a table and with a scalar exponent
+//   pow        z = pow(x, y) + pow(y, 2.0f): pow with a table and with a scalar exponent;
+//              w = cbrt(x) + logspace_add(x, y)
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -177,13 +178,15 @@ int main(int argc, char** argv)
     g(1) = nt2::globalsum(nt2::sin(x));
     write_table(argv[4], y);
     write_table(argv[5], g);
-  } else if (cmd == "pow") {                              // n; in: x y ; out: z
+  } else if (cmd == "pow") {                              // n; in: x y ; out: z w
     typedef float T;
-    nt2::table<T> x(nt2::of_size(n)), y(nt2::of_size(n)), z;
+    nt2::table<T> x(nt2::of_size(n)), y(nt2::of_size(n)), z, w;
     load(x, read_file<T>(argv[3], n));
     load(y, read_file<T>(argv[4], n));
     z = nt2::pow(x, y) + nt2::pow(y, T(2));
+    w = nt2::cbrt(x) + nt2::logspace_add(x, y);
     write_table(argv[5], z);
+    write_table(argv[6], w);
   } else if (cmd == "sigmadelta") {                       // n = pixels; argv[3] = frames; in: frames ; out: bkg var label
     typedef unsigned char T;
     const int nb_frames = std::atoi(argv[3]);

@@ -314,7 +314,7 @@ EXPORT double nt2o_log_d(double a0)
  * exp2/exp10 float: exponential/functions/scalar/impl/expo/f_expo_reduction.hpp:88-143,
  * double: d_expo_reduction.hpp:85-160, selections simd/common/impl/expo/expo_base.hpp:26-65;
  * log2/log10 float: simd/common/impl/logs/f_log.hpp:126-170, double:
- * simd/common/impl/logs/d_log.hpp:99-121.  Constants: exponential/constants/*.hpp. */
+ * simd/common/impl/logs/d_log.hpp:99-121.  Constants: the headers of exponential/constants. */
 #define MAXLOG2_F     fb(0x42fe0000u)
 #define MINLOG2_F     fb(0xc2fe0000u)
 #define MAXLOG10_F    fb(0x4218ec59u)
@@ -643,8 +643,6 @@ static const uint32_t TANH_F_P[5] = {0xbbbaf0eau, 0x3ca9134eu, 0xbd5c1e2du, 0x3e
 static const uint64_t TANH_D_P[3] = {0xbfeedc5baafd6f4bull, 0xc058d26a0e26682dull, 0xc0993ac030580563ull};
 static const uint64_t TANH_D_Q[4] = {0x3ff0000000000000ull, 0x405c33f28a581b86ull, 0x40a176fa0e5535faull,
                                      0x40b2ec102442040cull};
-#define LOG_2_F 0x3f317218u
-#define LOG_2_D 0x3fe62e42fefa39efull
 
 EXPORT float nt2o_sinh_f(float a0)
 {
@@ -654,7 +652,7 @@ EXPORT float nt2o_sinh_f(float a0)
   if (x < 1.0f) {
     r = horner_f(x * x, SINH_F_P, 4) * x;
   } else {
-    const int test1 = x > MAXLOG_F - fb(LOG_2_F);
+    const int test1 = x > MAXLOG_F - LOG_2_F;
     const float tmp = nt2o_exp_f(x * (test1 ? 0.5f : 1.0f));
     const float tmp1 = 0.5f * tmp;
     r = test1 ? tmp1 * tmp : tmp1 - 0.5f * (1.0f / tmp);
@@ -670,7 +668,7 @@ EXPORT double nt2o_sinh_d(double a0)
     const double x2 = x * x;
     r = x * (x2 * horner_d(x2, SINH_D_P, 4) / horner_d(x2, SINH_D_Q, 4)) + x;
   } else {
-    const int test1 = x > MAXLOG_D - db(LOG_2_D);
+    const int test1 = x > MAXLOG_D - LOG_2_D;
     const double tmp = nt2o_exp_d(x * (test1 ? 0.5 : 1.0));
     const double tmp1 = 0.5 * tmp;
     r = test1 ? tmp1 * tmp : tmp1 - 0.5 * (1.0 / tmp);
@@ -680,14 +678,14 @@ EXPORT double nt2o_sinh_d(double a0)
 EXPORT float nt2o_cosh_f(float a0)
 {
   const float x = fabsf(a0);
-  const int test1 = x > MAXLOG_F - fb(LOG_2_F);
+  const int test1 = x > MAXLOG_F - LOG_2_F;
   const float tmp = nt2o_exp_f(x * (test1 ? 0.5f : 1.0f));
   return test1 ? (0.5f * tmp) * tmp : tmp * 0.5f + (1.0f / tmp) * 0.5f;
 }
 EXPORT double nt2o_cosh_d(double a0)
 {
   const double x = fabs(a0);
-  const int test1 = x > MAXLOG_D - db(LOG_2_D);
+  const int test1 = x > MAXLOG_D - LOG_2_D;
   const double tmp = nt2o_exp_d(x * (test1 ? 0.5 : 1.0));
   return test1 ? (0.5 * tmp) * tmp : tmp * 0.5 + (1.0 / tmp) * 0.5;
 }
@@ -747,7 +745,6 @@ static const uint64_t POW1_DQ[5] = {0x3ff0000000000000ull, 0x4022aab49b20914eull
 static const uint64_t POW2_D[7] = {0x3eef6307d7f2937full, 0x3f242fbe60fc9259ull, 0x3f55d87ec84aef1dull,
                                    0x3f83b2ab6ef133b7ull, 0x3fac6b08d7041a92ull, 0x3fcebfbdff82c56dull,
                                    0x3fe62e42fefa39efull};
-#define LOG2_EM1_F 0x3ee2a8edu
 #define LOG2_EM1_D 0x3fdc551d94ae0bf8ull
 #define POWLARGE_F 0x44ffe000u
 #define POWLOW_F   0xc5160000u
@@ -861,8 +858,8 @@ static float pow_abs_f(float a0, float a1)
   float z = x * x;
   float w = (z * x) * horner_f(x, POW1_F, 4);
   w = -0.5f * z + w;
-  w = fb(LOG2_EM1_F) * w + w;
-  z = fb(LOG2_EM1_F) * x + w;
+  w = LOG2_EM1_F * w + w;
+  z = LOG2_EM1_F * x + w;
   z += x;
   w = (float)(-i) * 0.0625f + (float)e;
   const float ya = reduc_f(a1);
@@ -969,10 +966,192 @@ EXPORT void nt2o_pow2_d(const double* a0, const double* a1, double* y, size_t n)
   for (size_t i = 0; i < n; ++i) y[i] = nt2o_pow_d(a0[i], a1[i]);
 }
 
+/* --------------------------------------------------- rest of the exp family -- */
+/* cbrt, NT2's SIMD forms: exponential/functions/simd/common/cbrt.hpp:36-89 (double, two Newton
+ * steps) and :91-142 (float, one), with Boost.SIMD's fast_frexp/fast_ldexp
+ * (boost/simd/ieee/functions/simd/common/{fast_frexp,fast_ldexp}.hpp): no special cases inside,
+ * zeros and infinities returned as they are at the end. */
+static const uint32_t CBRT_PF[5] = {0xbe09e49au, 0x3f0bf0feu, 0xbf745265u, 0x3f91eb77u, 0x3ece0609u};
+static const uint64_t CBRT_PD[5] = {0xbfc13c93386fdff6ull, 0x3fe17e1fc7e59d58ull, 0xbfee8a4ca3ba37b8ull,
+                                    0x3ff23d6ee505873aull, 0x3fd9c0c12122a4feull};
+/* e -> (e / 3 with the sign of e, e mod 3 of |e|) as the integer steps of cbrt.hpp do */
+static inline int32_t cbrt_split(int32_t e, int32_t* rem)
+{
+  int32_t e1 = e < 0 ? -e : e;
+  *rem = e1 - (e1 / 3) * 3;
+  e1 /= 3;
+  return e > 0 ? e1 : (e < 0 ? -e1 : 0);   /* negate(e1, e) = e1 * sign(e) */
+}
+EXPORT float nt2o_cbrt_f(float a0)
+{
+  float z = fabsf(a0);
+  const int den = z < SMALLESTPOSVAL_F;
+  z = den ? z * TWOTONMB_F : z;
+  const float f = den ? fb(0x3ba14518u) : 1.0f;          /* Twotomnmbo_3 = 2^(-23/3) */
+  const uint32_t b = bf(z);
+  int32_t e = (int32_t)((b & 0x7f800000u) >> 23) - 126;
+  float x = fb((b & ~0x7f800000u) | 0x3f000000u);
+  x = horner_f(x, CBRT_PF, 5);
+  const int flag = e >= 0;
+  int32_t rem;
+  e = cbrt_split(e, &rem);
+  float fact = rem == 1 ? (flag ? fb(0x3fa14518u) : fb(0x3f4b2ff5u)) : 1.0f;
+  fact = rem == 2 ? (flag ? fb(0x3fcb2ff5u) : fb(0x3f214518u)) : fact;
+  x = (x * fact) * fb((uint32_t)(e + 127) << 23);
+  x -= (x - z / (x * x)) * fb(0x3eaaaaabu);
+  x = fb(bf(x) | (bf(a0) & 0x80000000u)) * f;
+  return (a0 == 0.0f || isinf(a0)) ? a0 : x;
+}
+EXPORT double nt2o_cbrt_d(double a0)
+{
+  double z = fabs(a0);
+  const int den = z < db(0x0010000000000000ull);
+  z = den ? z * 4503599627370496.0 : z;
+  const double f = den ? db(0x3ed428a2f98d7286ull) : 1.0;  /* 2^(-52/3) */
+  const uint64_t b = bd(z);
+  int32_t e = (int32_t)((b & 0x7ff0000000000000ull) >> 52) - 1022;
+  double x = db((b & ~0x7ff0000000000000ull) | 0x3fe0000000000000ull);
+  x = horner_d(x, CBRT_PD, 5);
+  const int flag = e >= 0;
+  int32_t rem;
+  e = cbrt_split(e, &rem);
+  double fact = rem == 1 ? (flag ? db(0x3ff428a2f98d728bull) : db(0x3fe965fea53d6e3dull)) : 1.0;
+  fact = rem == 2 ? (flag ? db(0x3ff965fea53d6e3dull) : db(0x3fe428a2f98d728bull)) : fact;
+  x = (x * fact) * db((uint64_t)(e + 1023) << 52);
+  x -= (x - z / (x * x)) * db(0x3fd5555555555555ull);
+  x -= (x - z / (x * x)) * db(0x3fd5555555555555ull);
+  x = db(bd(x) | (bd(a0) & 0x8000000000000000ull)) * f;
+  return (a0 == 0.0 || isinf(a0)) ? a0 : x;
+}
+/* sqrt1pm1 = sqrt(1+x)-1, generic/sqrt1pm1.hpp:27-33 */
+EXPORT float nt2o_sqrt1pm1_f(float a0)
+{
+  const float t = sqrtf(a0 + 1.0f);
+  return fabsf(a0) < 0.5f ? a0 / (t + 1.0f) : t - 1.0f;
+}
+EXPORT double nt2o_sqrt1pm1_d(double a0)
+{
+  const double t = sqrt(a0 + 1.0);
+  return fabs(a0) < 0.5 ? a0 / (t + 1.0) : t - 1.0;
+}
+/* exprecneg = exp(-1/x), exprecnegc = -expm1(-1/x): generic/exprecneg.hpp:27, exprecnegc.hpp:27 */
+EXPORT float nt2o_exprecneg_f(float a0) { return nt2o_exp_f(-(1.0f / a0)); }
+EXPORT double nt2o_exprecneg_d(double a0) { return nt2o_exp_d(-(1.0 / a0)); }
+EXPORT float nt2o_exprecnegc_f(float a0) { return -nt2o_expm1_f(-(1.0f / a0)); }
+EXPORT double nt2o_exprecnegc_d(double a0) { return -nt2o_expm1_d(-(1.0 / a0)); }
+/* expx2(x) = exp(x*x) and expx2(x, s) = exp(sign(s)*x*x) with x*x split at a multiple of
+ * 1/Expx2c1: simd/common/expx2.hpp:31-50 and :52-74 (signnz(s): -1 for -0). */
+EXPORT float nt2o_expx2s_f(float a0, float s)
+{
+  const float sgn = (bf(s) & 0x80000000u) ? -1.0f : 1.0f;
+  const float x = a0 * sgn;
+  const float m = 32.0f * floorf(0.03125f * x + 0.5f);
+  const float f = x - m;
+  const float u = sgn * (m * m);
+  const float u1 = sgn * ((m + m) * f + f * f);
+  float r = (u + u1 > MAXLOG_F) ? INFINITY : nt2o_exp_f(u) * nt2o_exp_f(u1);
+  return x == INFINITY ? x : r;
+}
+EXPORT double nt2o_expx2s_d(double a0, double s)
+{
+  const double sgn = (bd(s) & 0x8000000000000000ull) ? -1.0 : 1.0;
+  const double x = a0 * sgn;
+  const double m = 128.0 * floor(0.0078125 * x + 0.5);
+  const double f = x - m;
+  const double u = sgn * (m * m);
+  const double u1 = sgn * ((m + m) * f + f * f);
+  double r = (u + u1 > MAXLOG_D) ? INFINITY : nt2o_exp_d(u) * nt2o_exp_d(u1);
+  return x == INFINITY ? x : r;
+}
+EXPORT float nt2o_expx2_f(float a0)
+{
+  const float x = fabsf(a0);
+  const float m = 32.0f * floorf(0.03125f * x + 0.5f);
+  const float f = x - m;
+  const float u = m * m;
+  const float u1 = (m + m) * f + f * f;
+  float r = (u + u1 > MAXLOG_F) ? INFINITY : nt2o_exp_f(u) * nt2o_exp_f(u1);
+  return x == INFINITY ? x : r;
+}
+EXPORT double nt2o_expx2_d(double a0)
+{
+  const double x = fabs(a0);
+  const double m = 128.0 * floor(0.0078125 * x + 0.5);
+  const double f = x - m;
+  const double u = m * m;
+  const double u1 = (m + m) * f + f * f;
+  double r = (u + u1 > MAXLOG_D) ? INFINITY : nt2o_exp_d(u) * nt2o_exp_d(u1);
+  return x == INFINITY ? x : r;
+}
+/* logspace_add(a, b) = log(exp(a) + exp(b)), simd/common/logspace_add.hpp:27-36;
+ * logspace_sub(a, b) = log(exp(a) - exp(b)), simd/common/logspace_sub.hpp:27-35 */
+EXPORT float nt2o_logspace_add_f(float a0, float a1)
+{
+  const float t = -fabsf(a0 - a1);
+  const float r = (a0 > a1 ? a0 : a1) + nt2o_log1p_f(nt2o_exp_f(t));
+  return isnan(t) ? a0 + a1 : r;
+}
+EXPORT double nt2o_logspace_add_d(double a0, double a1)
+{
+  const double t = -fabs(a0 - a1);
+  const double r = (a0 > a1 ? a0 : a1) + nt2o_log1p_d(nt2o_exp_d(t));
+  return isnan(t) ? a0 + a1 : r;
+}
+EXPORT float nt2o_logspace_sub_f(float a0, float a1)
+{
+  const float x = a1 - a0;
+  const float t = x > -fb(0x3f317218u) ? nt2o_log_f(-nt2o_expm1_f(x)) : nt2o_log1p_f(-nt2o_exp_f(x));
+  return a0 + t;
+}
+EXPORT double nt2o_logspace_sub_d(double a0, double a1)
+{
+  const double x = a1 - a0;
+  const double t = x > -db(0x3fe62e42fefa39efull) ? nt2o_log_d(-nt2o_expm1_d(x)) : nt2o_log1p_d(-nt2o_exp_d(x));
+  return a0 + t;
+}
+EXPORT float nt2o_pow_abs_f(float a0, float a1) { return pow_abs_f(a0, a1); }
+EXPORT double nt2o_pow_abs_d(double a0, double a1) { return pow_abs_d(a0, a1); }
+
+/* Binary maps: op 0 atan2, 1 pow, 2 pow_abs, 3 realpow (= pow), 4 logspace_add, 5 logspace_sub,
+ * 6 expx2(a0, a1). */
+void nt2o_atan2_f(const float* a0, const float* a1, float* y, size_t n);
+void nt2o_atan2_d(const double* a0, const double* a1, double* y, size_t n);
+EXPORT int nt2o_map2_f(int op, const float* a0, const float* a1, float* y, size_t n)
+{
+  if (op == 0) { nt2o_atan2_f(a0, a1, y, n); return 0; }
+  for (size_t i = 0; i < n; ++i) {
+    switch (op) {
+      case 1: case 3: y[i] = nt2o_pow_f(a0[i], a1[i]); break;
+      case 2: y[i] = pow_abs_f(a0[i], a1[i]); break;
+      case 4: y[i] = nt2o_logspace_add_f(a0[i], a1[i]); break;
+      case 5: y[i] = nt2o_logspace_sub_f(a0[i], a1[i]); break;
+      case 6: y[i] = nt2o_expx2s_f(a0[i], a1[i]); break;
+      default: return 1;
+    }
+  }
+  return 0;
+}
+EXPORT int nt2o_map2_d(int op, const double* a0, const double* a1, double* y, size_t n)
+{
+  if (op == 0) { nt2o_atan2_d(a0, a1, y, n); return 0; }
+  for (size_t i = 0; i < n; ++i) {
+    switch (op) {
+      case 1: case 3: y[i] = nt2o_pow_d(a0[i], a1[i]); break;
+      case 2: y[i] = pow_abs_d(a0[i], a1[i]); break;
+      case 4: y[i] = nt2o_logspace_add_d(a0[i], a1[i]); break;
+      case 5: y[i] = nt2o_logspace_sub_d(a0[i], a1[i]); break;
+      case 6: y[i] = nt2o_expx2s_d(a0[i], a1[i]); break;
+      default: return 1;
+    }
+  }
+  return 0;
+}
+
 /* ------------------------------------------------------------- maps ------ */
 enum { OP_EXP = 0, OP_LOG = 1, OP_ERFC = 2, OP_NORMCDF = 3, OP_FASTNORMCDF = 4, OP_SQRT = 5,
        OP_ERFC_SCALAR = 6, OP_EXP2 = 7, OP_EXP10 = 8, OP_LOG2 = 9, OP_LOG10 = 10, OP_EXPM1 = 11,
-       OP_LOG1P = 12, OP_SINH = 13, OP_COSH = 14, OP_TANH = 15 };
+       OP_LOG1P = 12, OP_SINH = 13, OP_COSH = 14, OP_TANH = 15, OP_CBRT = 16, OP_SQRT1PM1 = 17,
+       OP_EXPRECNEG = 18, OP_EXPRECNEGC = 19, OP_EXPX2 = 20 };
 
 EXPORT int nt2o_map_f(int op, const float* x, float* y, size_t n)
 {
@@ -995,6 +1174,11 @@ EXPORT int nt2o_map_f(int op, const float* x, float* y, size_t n)
       case OP_SINH: y[i] = nt2o_sinh_f(a); break;
       case OP_COSH: y[i] = nt2o_cosh_f(a); break;
       case OP_TANH: y[i] = nt2o_tanh_f(a); break;
+      case OP_CBRT: y[i] = nt2o_cbrt_f(a); break;
+      case OP_SQRT1PM1: y[i] = nt2o_sqrt1pm1_f(a); break;
+      case OP_EXPRECNEG: y[i] = nt2o_exprecneg_f(a); break;
+      case OP_EXPRECNEGC: y[i] = nt2o_exprecnegc_f(a); break;
+      case OP_EXPX2: y[i] = nt2o_expx2_f(a); break;
       default: return 1;
     }
   }
@@ -1021,6 +1205,11 @@ EXPORT int nt2o_map_d(int op, const double* x, double* y, size_t n)
       case OP_SINH: y[i] = nt2o_sinh_d(a); break;
       case OP_COSH: y[i] = nt2o_cosh_d(a); break;
       case OP_TANH: y[i] = nt2o_tanh_d(a); break;
+      case OP_CBRT: y[i] = nt2o_cbrt_d(a); break;
+      case OP_SQRT1PM1: y[i] = nt2o_sqrt1pm1_d(a); break;
+      case OP_EXPRECNEG: y[i] = nt2o_exprecneg_d(a); break;
+      case OP_EXPRECNEGC: y[i] = nt2o_exprecnegc_d(a); break;
+      case OP_EXPX2: y[i] = nt2o_expx2_d(a); break;
       default: return 1;
     }
   }

@@ -48,7 +48,7 @@ static inline double tdb(uint64_t u) { double d; memcpy(&d, &u, 8); return d; }
 static inline uint64_t tbd(double d) { uint64_t u; memcpy(&u, &d, 8); return u; }
 
 /* ------------------------------------------------------------ constants -- */
-/* Bit patterns of the BOOST_SIMD_CONSTANT_REGISTER lines in constants/*.hpp. */
+/* Bit patterns of the BOOST_SIMD_CONSTANT_REGISTER lines in the constants headers. */
 #define F_PIO4    0x3f490fdbu
 #define F_PIO2    0x3fc90fdbu
 #define F_20PI    0x427b53d1u

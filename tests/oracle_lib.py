@@ -54,6 +54,8 @@ SIGS = {
     "nt2o_pow_d": (C.c_double, [C.c_double, C.c_double]),
     "nt2o_pow2_f": (None, [f32p, f32p, f32p, sz]),
     "nt2o_pow2_d": (None, [f64p, f64p, f64p, sz]),
+    "nt2o_map2_f": (C.c_int, [C.c_int, f32p, f32p, f32p, sz]),
+    "nt2o_map2_d": (C.c_int, [C.c_int, f64p, f64p, f64p, sz]),
     "nt2o_rem_pio2_exact_f": (C.c_int, [C.c_float, C.POINTER(C.c_float)]),
     "nt2o_rem_pio2_exact_d": (C.c_int, [C.c_double, C.POINTER(C.c_double)]),
     "nt2o_exp10_f": (C.c_float, [C.c_float]),
@@ -95,7 +97,10 @@ SIGS = {
 
 OP = {"exp": 0, "log": 1, "erfc": 2, "normcdf": 3, "fastnormcdf": 4, "sqrt": 5, "erfc_scalar": 6,
       "exp2": 7, "exp10": 8, "log2": 9, "log10": 10, "expm1": 11, "log1p": 12, "sinh": 13, "cosh": 14,
-      "tanh": 15}
+      "tanh": 15, "cbrt": 16, "sqrt1pm1": 17, "exprecneg": 18, "exprecnegc": 19, "expx2": 20,
+      "realsqrt": 5, "reallog": 1}
+# binary functors of nt2o_map2_f/d
+OP2 = {"atan2": 0, "pow": 1, "pow_abs": 2, "realpow": 3, "logspace_add": 4, "logspace_sub": 5, "expx2": 6}
 
 
 def load(variant: str = "libnt2oracle.so"):
@@ -152,6 +157,17 @@ def pow_(a0: np.ndarray, a1: np.ndarray) -> np.ndarray:
     a1 = np.ascontiguousarray(a1, dtype=a0.dtype)
     y = np.empty_like(a0)
     (L.nt2o_pow2_f if a0.dtype == np.float32 else L.nt2o_pow2_d)(a0, a1, y, a0.size)
+    return y
+
+
+def map2(op: str, a0: np.ndarray, a1: np.ndarray) -> np.ndarray:
+    """NT2's binary functor `op` (SIMD form) elementwise over a0, a1."""
+    L = load()
+    a0 = np.ascontiguousarray(a0)
+    a1 = np.ascontiguousarray(a1, dtype=a0.dtype)
+    y = np.empty_like(a0)
+    fn = L.nt2o_map2_f if a0.dtype == np.float32 else L.nt2o_map2_d
+    assert fn(OP2[op], a0, a1, y, a0.size) == 0
     return y
 
 

