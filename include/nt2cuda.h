@@ -129,7 +129,27 @@ enum {
   NT2CUDA_OP_EXPRECNEGC = 26, /* generic/exprecnegc.hpp: -expm1(-1/x) */
   NT2CUDA_OP_EXPX2 = 27,      /* simd/common/expx2.hpp: exp(x*x) */
   NT2CUDA_OP_REALSQRT = 28,   /* generic/realsqrt.hpp: sqrt (NT2 asserts x >= 0) */
-  NT2CUDA_OP_REALLOG = 29     /* generic/reallog.hpp: log (NT2 asserts x >= 0) */
+  NT2CUDA_OP_REALLOG = 29,    /* generic/reallog.hpp: log (NT2 asserts x >= 0) */
+  /* composed trigonometric functors (modules/core/trigonometric/.../functions/generic/<name>.hpp;
+   * asec: simd/common/asec.hpp).  CSC..CSCD follow NT2CUDA_MAP_SIMD128 as sin, cos, sinpi, cospi do. */
+  NT2CUDA_OP_CSC = 30,        /* rec(sin(x)) */
+  NT2CUDA_OP_SEC = 31,        /* rec(cos(x)) */
+  NT2CUDA_OP_CSCPI = 32,      /* rec(sinpi(x)), NaN at nonzero integers */
+  NT2CUDA_OP_SECPI = 33,      /* rec(cospi(x)), NaN where 2x is odd */
+  NT2CUDA_OP_CSCD = 34,       /* cscpi(x/180) */
+  NT2CUDA_OP_INDEG = 35,      /* radians to degrees */
+  NT2CUDA_OP_INRAD = 36,      /* degrees to radians */
+  NT2CUDA_OP_ACOT = 37,       /* atan(rec(x)) */
+  NT2CUDA_OP_ASIND = 38,      /* indeg(asin(x)) */
+  NT2CUDA_OP_ACOSD = 39,
+  NT2CUDA_OP_ATAND = 40,
+  NT2CUDA_OP_ASINPI = 41,     /* asin(x)/pi */
+  NT2CUDA_OP_ACOSPI = 42,
+  NT2CUDA_OP_ATANPI = 43,
+  NT2CUDA_OP_ACSC = 44,       /* asin(rec(x)) */
+  NT2CUDA_OP_ACSCD = 45,      /* indeg(acsc(x)) */
+  NT2CUDA_OP_ASEC = 46,       /* pi/2 - acsc(x) */
+  NT2CUDA_OP_ASECD = 47       /* indeg(asec(x)) */
 };
 
 /* out = atan2(a0, a1) elementwise (NT2's SIMD form,

@@ -353,6 +353,32 @@ NT2CUDA_FN2(selinc, selinc_)
 NT2CUDA_FN2(seldec, seldec_)
 #undef NT2CUDA_FN2
 
+// Trigonometric functors NT2 composes from the ones above, as one fused statement each
+// (modules/core/trigonometric/include/nt2/trigonometric/functions/generic/<name>.hpp; asec:
+// simd/common/asec.hpp).
+#define NT2CUDA_COMPOSED(NAME, EXPR)                                                    \
+  template <class A, std::enable_if_t<is_operand_v<A>, int> = 0>                        \
+  inline auto NAME(const A& a) { return EXPR; }
+NT2CUDA_COMPOSED(indeg, make_unary<tag::indeg_>(a))
+NT2CUDA_COMPOSED(inrad, make_unary<tag::inrad_>(a))
+NT2CUDA_COMPOSED(csc, rec(sin(a)))
+NT2CUDA_COMPOSED(sec, rec(cos(a)))
+NT2CUDA_COMPOSED(cscpi, make_binary<tag::cscpi_nan_>(a, rec(sinpi(a))))
+NT2CUDA_COMPOSED(secpi, make_binary<tag::secpi_nan_>(a, rec(cospi(a))))
+NT2CUDA_COMPOSED(cscd, cscpi(make_unary<tag::oneo_180_mul_>(a)))
+NT2CUDA_COMPOSED(acot, atan(rec(a)))
+NT2CUDA_COMPOSED(asind, indeg(asin(a)))
+NT2CUDA_COMPOSED(acosd, indeg(acos(a)))
+NT2CUDA_COMPOSED(atand, indeg(atan(a)))
+NT2CUDA_COMPOSED(asinpi, make_unary<tag::invpi_mul_>(asin(a)))
+NT2CUDA_COMPOSED(acospi, make_unary<tag::invpi_mul_>(acos(a)))
+NT2CUDA_COMPOSED(atanpi, make_unary<tag::invpi_mul_>(atan(a)))
+NT2CUDA_COMPOSED(acsc, asin(rec(a)))
+NT2CUDA_COMPOSED(acscd, indeg(acsc(a)))
+NT2CUDA_COMPOSED(asec, make_unary<tag::pio2_minus_>(acsc(a)))
+NT2CUDA_COMPOSED(asecd, indeg(asec(a)))
+#undef NT2CUDA_COMPOSED
+
 #define NT2CUDA_FN3(NAME, TAG)                                                          \
   template <class A, class B, class C,                                                  \
             std::enable_if_t<is_operand_v<A> || is_operand_v<B> || is_operand_v<C>, int> = 0> \

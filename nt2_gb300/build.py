@@ -32,6 +32,8 @@ SOURCES = [
     "capi_trig_f64.cu",
     "capi_expfam_f32.cu",
     "capi_expfam_f64.cu",
+    "capi_trigx_f32.cu",
+    "capi_trigx_f64.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -54,6 +54,9 @@ struct pow_ {};
 // the rest of NT2's exponential family (expx2s_ is the two-argument expx2)
 struct cbrt_ {}; struct sqrt1pm1_ {}; struct exprecneg_ {}; struct exprecnegc_ {}; struct expx2_ {};
 struct expx2s_ {}; struct pow_abs_ {}; struct logspace_add_ {}; struct logspace_sub_ {};
+// steps of the composed trigonometric functors (csc = rec(sin), asind = indeg(asin), ...)
+struct indeg_ {}; struct inrad_ {}; struct invpi_mul_ {}; struct oneo_180_mul_ {}; struct pio2_minus_ {};
+struct cscpi_nan_ {}; struct secpi_nan_ {};
 }  // namespace tag
 
 // ------------------------------------------------------------ tree nodes
@@ -140,6 +143,13 @@ NT2CUDA_BIN(logspace_add_, math::logspace_add<F>(a, (A)b))
 NT2CUDA_BIN(logspace_sub_, math::logspace_sub<F>(a, (A)b))
 NT2CUDA_BIN(expx2s_, math::expx2<F>(a, (A)b))
 NT2CUDA_UN(cbrt_, math::cbrt<F>(a))
+NT2CUDA_UN(indeg_, trig::indeg(a))
+NT2CUDA_UN(inrad_, trig::inrad(a))
+NT2CUDA_UN(invpi_mul_, trig::invpi_mul(a))
+NT2CUDA_UN(oneo_180_mul_, trig::oneo_180_mul(a))
+NT2CUDA_UN(pio2_minus_, trig::pio2_minus(a))
+NT2CUDA_BIN(cscpi_nan_, trig::cscpi_nan(a, (A)b))
+NT2CUDA_BIN(secpi_nan_, trig::secpi_nan(a, (A)b))
 NT2CUDA_UN(sqrt1pm1_, math::sqrt1pm1<F>(a))
 NT2CUDA_UN(exprecneg_, math::exprecneg<F>(a))
 NT2CUDA_UN(exprecnegc_, math::exprecnegc<F>(a))

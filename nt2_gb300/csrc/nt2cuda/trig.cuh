@@ -763,5 +763,32 @@ template <int K, bool F, int P, class T> __device__ __forceinline__ void scalar_
   }
 }
 
+// ----------------------------------------------------------- compositions
+// The steps NT2's composed trigonometric functors add around sin, cos, sinpi,
+// cospi, asin, acos, atan (modules/core/trigonometric/include/nt2/trigonometric/
+// functions/generic/{indeg,inrad,asinpi,cscd,asec,cscpi,secpi}.hpp), constants as
+// bit patterns of their BOOST_SIMD_CONSTANT_REGISTER lines.
+// indeg(x) = x*Radindeg - x*Radindegr (the second constant is the rounding residual of 180/pi)
+__device__ __forceinline__ float indeg(float a)
+{ return math::sub(math::mul(a, __uint_as_float(0x42652ee1u)), math::mul(a, __uint_as_float(0xb53387c1u))); }
+__device__ __forceinline__ double indeg(double a)
+{
+  return math::sub(math::mul(a, math::dbits(0x404ca5dc1a63c1f8ull)), math::mul(a, math::dbits(0xbce1e7ab456405f8ull)));
+}
+__device__ __forceinline__ float inrad(float a) { return math::mul(a, __uint_as_float(0x3c8efa35u)); }
+__device__ __forceinline__ double inrad(double a) { return math::mul(a, math::dbits(0x3f91df46a2529d39ull)); }
+__device__ __forceinline__ float invpi_mul(float a) { return math::mul(__uint_as_float(0x3ea2f983u), a); }
+__device__ __forceinline__ double invpi_mul(double a) { return math::mul(math::dbits(0x3fd45f306dc9c883ull), a); }
+__device__ __forceinline__ float oneo_180_mul(float a) { return math::mul(__uint_as_float(0x3bb60b61u), a); }
+__device__ __forceinline__ double oneo_180_mul(double a) { return math::mul(math::dbits(0x3f76c16c16c16c17ull), a); }
+__device__ __forceinline__ float pio2_minus(float a) { return math::sub(__uint_as_float(0x3fc90fdbu), a); }
+__device__ __forceinline__ double pio2_minus(double a) { return math::sub(math::dbits(0x3ff921fb54442d18ull), a); }
+// cscpi: NaN where x is a nonzero integer; secpi: NaN where 2x is odd (is_odd(y) =
+// is_flint((y - 1) / 2)); elsewhere the reciprocal v computed beside it
+template <class T> __device__ __forceinline__ T cscpi_nan(T x, T v)
+{ return (math::is_flint(x) && x != T(0)) ? T(NAN) : v; }
+template <class T> __device__ __forceinline__ T secpi_nan(T x, T v)
+{ return math::is_flint(math::mul(math::sub(math::mul(x, T(2)), T(1)), T(0.5))) ? T(NAN) : v; }
+
 }  // namespace trig
 }  // namespace nt2cuda

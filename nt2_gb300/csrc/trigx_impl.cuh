@@ -1,0 +1,84 @@
+// trigx_impl.cuh -- the trigonometric functors NT2 composes from sin, cos,
+// sinpi, cospi, asin, acos, atan (ops NT2CUDA_OP_CSC..NT2CUDA_OP_ASECD of
+// nt2cuda_map_f32/f64), lowered as expression trees onto the elementwise
+// transform: csc(x) is rec(sin(x)) evaluated in one pass, the sine part in
+// the scalar or the 128-bit pack form (nt2cuda/expr.cuh, nt2cuda/trig.cuh).
+// Included by capi_trigx_f32.cu and capi_trigx_f64.cu, one element type each.
+#pragma once
+#include <cuda_runtime.h>
+#include "internal.cuh"
+#include "nt2cuda/expr.cuh"
+#include "nt2cuda/launch.cuh"
+
+namespace nt2cuda {
+namespace detail_capi {
+
+namespace {
+
+template <class Tag, class... C> node<Tag, C...> nd(C... c) { return node<Tag, C...>{c...}; }
+
+template <bool F, class E, class T> nt2cuda_status run_e(const E& e, T* y, size_t n, nt2cuda_stream s)
+{
+  auto p = make_prog(assign<T, E>{y, e});
+  return launch_status(transform<F>(p, n, as_stream(s), "trig"));
+}
+
+template <class Tag, bool SIMD> struct pick { using type = Tag; };
+template <class Tag> struct pick<Tag, true> { using type = tag::simd128_<Tag>; };
+
+// csc, sec, cscpi, secpi, cscd: the sine/cosine node in the form SIMD selects
+template <bool F, bool SIMD, class T> nt2cuda_status recip_impl(int op, const T* x, T* y, size_t n, nt2cuda_stream s)
+{
+  const term<T> X{x};
+  using Sin = typename pick<tag::sin_, SIMD>::type;
+  using Cos = typename pick<tag::cos_, SIMD>::type;
+  using Sinpi = typename pick<tag::sinpi_, SIMD>::type;
+  using Cospi = typename pick<tag::cospi_, SIMD>::type;
+  switch (op) {
+    case NT2CUDA_OP_CSC: return run_e<F>(nd<tag::rec_>(nd<Sin>(X)), y, n, s);
+    case NT2CUDA_OP_SEC: return run_e<F>(nd<tag::rec_>(nd<Cos>(X)), y, n, s);
+    case NT2CUDA_OP_CSCPI: return run_e<F>(nd<tag::cscpi_nan_>(X, nd<tag::rec_>(nd<Sinpi>(X))), y, n, s);
+    case NT2CUDA_OP_SECPI: return run_e<F>(nd<tag::secpi_nan_>(X, nd<tag::rec_>(nd<Cospi>(X))), y, n, s);
+    case NT2CUDA_OP_CSCD: {
+      const auto Y = nd<tag::oneo_180_mul_>(X);
+      return run_e<F>(nd<tag::cscpi_nan_>(Y, nd<tag::rec_>(nd<Sinpi>(Y))), y, n, s);
+    }
+    default: return NT2CUDA_ERR_ARG;
+  }
+}
+
+// the inverse functors and the unit conversions: no pack dependence
+template <bool F, class T> nt2cuda_status inv_impl(int op, const T* x, T* y, size_t n, nt2cuda_stream s)
+{
+  const term<T> X{x};
+  const auto R = nd<tag::rec_>(X);
+  switch (op) {
+    case NT2CUDA_OP_INDEG: return run_e<F>(nd<tag::indeg_>(X), y, n, s);
+    case NT2CUDA_OP_INRAD: return run_e<F>(nd<tag::inrad_>(X), y, n, s);
+    case NT2CUDA_OP_ACOT: return run_e<F>(nd<tag::atan_>(R), y, n, s);
+    case NT2CUDA_OP_ASIND: return run_e<F>(nd<tag::indeg_>(nd<tag::asin_>(X)), y, n, s);
+    case NT2CUDA_OP_ACOSD: return run_e<F>(nd<tag::indeg_>(nd<tag::acos_>(X)), y, n, s);
+    case NT2CUDA_OP_ATAND: return run_e<F>(nd<tag::indeg_>(nd<tag::atan_>(X)), y, n, s);
+    case NT2CUDA_OP_ASINPI: return run_e<F>(nd<tag::invpi_mul_>(nd<tag::asin_>(X)), y, n, s);
+    case NT2CUDA_OP_ACOSPI: return run_e<F>(nd<tag::invpi_mul_>(nd<tag::acos_>(X)), y, n, s);
+    case NT2CUDA_OP_ATANPI: return run_e<F>(nd<tag::invpi_mul_>(nd<tag::atan_>(X)), y, n, s);
+    case NT2CUDA_OP_ACSC: return run_e<F>(nd<tag::asin_>(R), y, n, s);
+    case NT2CUDA_OP_ACSCD: return run_e<F>(nd<tag::indeg_>(nd<tag::asin_>(R)), y, n, s);
+    case NT2CUDA_OP_ASEC: return run_e<F>(nd<tag::pio2_minus_>(nd<tag::asin_>(R)), y, n, s);
+    case NT2CUDA_OP_ASECD: return run_e<F>(nd<tag::indeg_>(nd<tag::pio2_minus_>(nd<tag::asin_>(R))), y, n, s);
+    default: return NT2CUDA_ERR_ARG;
+  }
+}
+
+template <class T> nt2cuda_status trigx_dispatch(int op, const T* x, T* y, size_t n, bool fused, bool simd,
+                                                 nt2cuda_stream s)
+{
+  if (op >= NT2CUDA_OP_INDEG) return fused ? inv_impl<true>(op, x, y, n, s) : inv_impl<false>(op, x, y, n, s);
+  if (fused) return simd ? recip_impl<true, true>(op, x, y, n, s) : recip_impl<true, false>(op, x, y, n, s);
+  return simd ? recip_impl<false, true>(op, x, y, n, s) : recip_impl<false, false>(op, x, y, n, s);
+}
+
+}  // namespace
+
+}  // namespace detail_capi
+}  // namespace nt2cuda

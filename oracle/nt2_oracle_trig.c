@@ -38,6 +38,7 @@
 #include <math.h>
 #include <stddef.h>
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
 
 #define EXPORT __attribute__((visibility("default")))
@@ -742,3 +743,72 @@ EXPORT int nt2o_rem_pio2_exact_f(float x, float* xr)
   *xr = (float)r;
   return n;
 }
+
+/* ------------------------------------------------- compositions ------ */
+/* The trigonometric functors NT2 defines on top of the ones above
+ * (modules/core/trigonometric/include/nt2/trigonometric/functions/generic headers and
+ * simd/common/asec.hpp), op by op:
+ *   0 csc = rec(sin)          1 sec = rec(cos)
+ *   2 cscpi = NaN where x is a nonzero integer, else rec(sinpi)
+ *   3 secpi = NaN where 2x is odd, else rec(cospi)
+ *   4 cscd = cscpi(Oneo_180 * x)
+ *   5 indeg = x*Radindeg - x*Radindegr      6 inrad = x*Deginrad
+ *   7 acot = atan(rec)   8-10 asind, acosd, atand = indeg(asin, acos, atan)
+ *   11-13 asinpi, acospi, atanpi = Invpi * (asin, acos, atan)
+ *   14 acsc = asin(rec)  15 acscd = indeg(acsc)  16 asec = Pio_2 - acsc  17 asecd = indeg(asec)
+ * rec is the IEEE quotient 1/x; the sin/cos based ones use the pack form of the
+ * functors above (`pack` lanes). */
+static int flint_f(float x) { return isfinite(x) && (x - truncf(x)) == 0.0f; }
+static int flint_d(double x) { return isfinite(x) && (x - trunc(x)) == 0.0; }
+#define TRIGX_BODY(T, SFX, FLINT, RADINDEG, RADINDEGR, DEGINRAD, INVPI, ONEO_180, PIO_2)                 \
+  if (op < 0 || op > 17) return 1;                                                                      \
+  T* t = (T*)malloc((n ? n : 1) * sizeof(T));                                                          \
+  if (!t) return 1;                                                                                     \
+  int st = 0;                                                                                           \
+  switch (op) {                                                                                         \
+    case 0: case 1:                                                                                     \
+      st = nt2o_trig_##SFX(op == 0 ? TRIG_SIN : TRIG_COS, x, y, n, pack);                              \
+      for (size_t i = 0; i < n; ++i) y[i] = (T)1 / y[i];                                                \
+      break;                                                                                            \
+    case 2: case 4:                                                                                     \
+      for (size_t i = 0; i < n; ++i) t[i] = op == 4 ? ONEO_180 * x[i] : x[i];                           \
+      st = nt2o_trig_##SFX(TRIG_SINPI, t, y, n, pack);                                                  \
+      for (size_t i = 0; i < n; ++i) y[i] = (FLINT(t[i]) && t[i] != 0) ? (T)NAN : (T)1 / y[i];         \
+      break;                                                                                            \
+    case 3:                                                                                             \
+      st = nt2o_trig_##SFX(TRIG_COSPI, x, y, n, pack);                                                  \
+      for (size_t i = 0; i < n; ++i) y[i] = FLINT(((x[i] * 2) - 1) * (T)0.5) ? (T)NAN : (T)1 / y[i];   \
+      break;                                                                                            \
+    case 5: for (size_t i = 0; i < n; ++i) y[i] = x[i] * RADINDEG - x[i] * RADINDEGR; break;           \
+    case 6: for (size_t i = 0; i < n; ++i) y[i] = x[i] * DEGINRAD; break;                               \
+    case 7:                                                                                             \
+      for (size_t i = 0; i < n; ++i) t[i] = (T)1 / x[i];                                                \
+      st = nt2o_trig_##SFX(TRIG_ATAN, t, y, n, 1);                                                      \
+      break;                                                                                            \
+    default: {                                                                                          \
+      const int inner = (op == 9 || op == 12) ? TRIG_ACOS : ((op == 10 || op == 13) ? TRIG_ATAN : TRIG_ASIN); \
+      const int rec_first = op >= 14;                                                                   \
+      for (size_t i = 0; i < n; ++i) t[i] = rec_first ? (T)1 / x[i] : x[i];                             \
+      st = nt2o_trig_##SFX(inner, t, y, n, 1);                                                          \
+      for (size_t i = 0; i < n; ++i) {                                                                  \
+        T v = y[i];                                                                                     \
+        if (op >= 11 && op <= 13) v = INVPI * v;                                                        \
+        if (op == 16 || op == 17) v = PIO_2 - v;                                                        \
+        if ((op >= 8 && op <= 10) || op == 15 || op == 17) v = v * RADINDEG - v * RADINDEGR;          \
+        y[i] = v;                                                                                       \
+      }                                                                                                 \
+    }                                                                                                   \
+  }                                                                                                     \
+  free(t);                                                                                              \
+  return st;
+EXPORT int nt2o_trigx_f(int op, const float* x, float* y, size_t n, int pack)
+{
+  TRIGX_BODY(float, f, flint_f, tfb(0x42652ee1u), tfb(0xb53387c1u), tfb(0x3c8efa35u), tfb(0x3ea2f983u),
+             tfb(0x3bb60b61u), tfb(0x3fc90fdbu))
+}
+EXPORT int nt2o_trigx_d(int op, const double* x, double* y, size_t n, int pack)
+{
+  TRIGX_BODY(double, d, flint_d, tdb(0x404ca5dc1a63c1f8ull), tdb(0xbce1e7ab456405f8ull), tdb(0x3f91df46a2529d39ull),
+             tdb(0x3fd45f306dc9c883ull), tdb(0x3f76c16c16c16c17ull), tdb(0x3ff921fb54442d18ull))
+}
+#undef TRIGX_BODY

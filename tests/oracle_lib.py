@@ -54,6 +54,8 @@ SIGS = {
     "nt2o_pow_d": (C.c_double, [C.c_double, C.c_double]),
     "nt2o_pow2_f": (None, [f32p, f32p, f32p, sz]),
     "nt2o_pow2_d": (None, [f64p, f64p, f64p, sz]),
+    "nt2o_trigx_f": (C.c_int, [C.c_int, f32p, f32p, sz, C.c_int]),
+    "nt2o_trigx_d": (C.c_int, [C.c_int, f64p, f64p, sz, C.c_int]),
     "nt2o_map2_f": (C.c_int, [C.c_int, f32p, f32p, f32p, sz]),
     "nt2o_map2_d": (C.c_int, [C.c_int, f64p, f64p, f64p, sz]),
     "nt2o_rem_pio2_exact_f": (C.c_int, [C.c_float, C.POINTER(C.c_float)]),
@@ -140,6 +142,22 @@ def trig(op: str, x: np.ndarray, pack: int = 1) -> np.ndarray:
     return y
 
 
+# trigonometric functors NT2 composes from the ones above (nt2o_trigx_f/d op numbers)
+TRIGX = {"csc": 0, "sec": 1, "cscpi": 2, "secpi": 3, "cscd": 4, "indeg": 5, "inrad": 6, "acot": 7, "asind": 8,
+         "acosd": 9, "atand": 10, "asinpi": 11, "acospi": 12, "atanpi": 13, "acsc": 14, "acscd": 15, "asec": 16,
+         "asecd": 17}
+
+
+def trigx(op: str, x: np.ndarray, pack: int = 1) -> np.ndarray:
+    """NT2's composed trigonometric functor `op`; pack as in trig()."""
+    L = load()
+    x = np.ascontiguousarray(x)
+    y = np.empty_like(x)
+    fn = L.nt2o_trigx_f if x.dtype == np.float32 else L.nt2o_trigx_d
+    assert fn(TRIGX[op], x, y, x.size, pack) == 0
+    return y
+
+
 def atan2(a0: np.ndarray, a1: np.ndarray) -> np.ndarray:
     """NT2's atan2(a0, a1) (SIMD form), elementwise."""
     L = load()
@@ -174,6 +192,8 @@ def map2(op: str, a0: np.ndarray, a1: np.ndarray) -> np.ndarray:
 def map_(op: str, x: np.ndarray) -> np.ndarray:
     if op in TRIG:
         return trig(op, x)
+    if op in TRIGX:
+        return trigx(op, x)
     L = load()
     y = np.empty_like(x)
     fn = L.nt2o_map_f if x.dtype == np.float32 else L.nt2o_map_d

@@ -51,7 +51,7 @@ def test_argument_validation_without_device(cuda_lib):
     arr = (SdStream * 1)()
     assert L.nt2cuda_sigmadelta_batch_u8(arr, 1, 0, 1, None) == 1
     assert L.nt2cuda_sigmadelta_batch_u8(arr, 0, 4, 1, None) == 1
-    assert L.nt2cuda_map_f32(42, None, None, 0, 0, None) in (0, 1)
+    assert L.nt2cuda_map_f32(99, None, None, 0, 0, None) in (0, 1)   # unknown op
     assert L.nt2cuda_map_f32(12, None, None, 0, 4, None) == 1     # unknown flag bit
     assert L.nt2cuda_map_f64(14, None, None, 5, 2, None) == 1     # null tables
     assert L.nt2cuda_pow_f32(None, None, None, 5, 0, None) == 1   # null tables

@@ -167,6 +167,19 @@ def test_pow_demo(demos, oracle, tmp_path):
     assert not bad.any(), (np.flatnonzero(bad)[:5], x[bad][:5], y[bad][:5])
 
 
+def test_trigx_demo(demos, oracle, tmp_path):
+    """Composed trigonometric functors through the C++ front end: csc(x) + asind(x*1e-3f) + secpi(x)
+    in one statement, bit-exact against NT2's compositions."""
+    n = 30011
+    x = np.random.default_rng(14).uniform(-600, 600, n).astype(np.float32)
+    x[::7] = np.round(x[::7] * 2) / 2              # integers and halves: secpi's NaNs
+    _, (oy,) = run(demos, tmp_path, "trigx", n, [x], 1)
+    want = (oracle.trigx("csc", x) + oracle.trigx("asind", x * np.float32(1e-3))) + oracle.trigx("secpi", x)
+    got = np.fromfile(oy, np.float32)
+    bad = ~(np.isnan(got) & np.isnan(want)) & (got.view(np.uint32) != want.view(np.uint32))
+    assert not bad.any(), (np.flatnonzero(bad)[:5], x[bad][:5], got[bad][:5], want[bad][:5])
+
+
 def test_io_demo(demos, tmp_path):
     """nt2cuda::load reads a table file written from Python, the statement runs on the device, and
     nt2cuda::save writes the result back with its extent."""

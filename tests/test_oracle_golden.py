@@ -516,3 +516,58 @@ def test_logspace_and_expx2_accuracy(oracle):
         s = np.where(rng.integers(0, 2, x.size) == 1, -1.0, 1.0).astype(dt)
         m, w = oracle.max_ulp(oracle.map2("expx2", x, s), np.exp(s.astype(np.longdouble) * x.astype(np.longdouble) ** 2).astype(dt))
         assert m <= 8.0, ("expx2", dt, m, x[w], s[w])
+
+
+# Trigonometric functors composed from sin, cos, sinpi, cospi, asin, acos, atan:
+# modules/core/trigonometric/unit/scalar/{csc,sec,cscpi,secpi,cscd,indeg,inrad,acot,asind,acosd,atand,
+# asinpi,acospi,atanpi,acsc,acscd,asec,asecd}.cpp (0.5 ulp; acot 1.5).  Symbolic values are
+# rounded to the type first, as NT2's constants are.
+PI = math.pi
+TRIGX_SPECIALS = {
+    "csc": [(-0.0, -INF), (INF, NAN), (-INF, NAN), (NAN, NAN), (0.0, INF), (-PI / 2, -1.0),
+            (-PI / 4, -math.sqrt(2)), (PI / 2, 1.0), (PI / 4, math.sqrt(2))],
+    "sec": [(INF, NAN), (-INF, NAN), (NAN, NAN), (-PI, -1.0), (-PI / 4, math.sqrt(2)), (PI, -1.0),
+            (PI / 4, math.sqrt(2)), (0.0, 1.0)],
+    "cscpi": [(-0.0, -INF), (INF, NAN), (-INF, NAN), (-1.0, NAN), (NAN, NAN), (1.0, NAN), (0.0, INF),
+              (-0.25, -math.sqrt(2)), (0.5, 1.0), (-0.5, -1.0), (0.25, math.sqrt(2))],
+    "secpi": [(0.5, NAN), (INF, NAN), (-0.5, NAN), (-INF, NAN), (NAN, NAN), (-0.25, math.sqrt(2)), (1.0, -1.0),
+              (0.25, math.sqrt(2)), (0.0, 1.0)],
+    "cscd": [(-0.0, -INF), (-180.0, NAN), (INF, NAN), (-INF, NAN), (NAN, NAN), (0.0, INF), (180.0, NAN),
+             (-45.0, -math.sqrt(2)), (-90.0, -1.0), (45.0, math.sqrt(2)), (90.0, 1.0)],
+    "indeg": [(INF, INF), (-INF, -INF), (NAN, NAN), (-PI, -180.0), (-PI / 2, -90.0), (-PI / 4, -45.0), (PI, 180.0),
+              (PI / 2, 90.0), (PI / 4, 45.0), (0.0, 0.0)],
+    "inrad": [(INF, INF), (-INF, -INF), (NAN, NAN), (-180.0, -PI), (-45.0, -PI / 4), (-90.0, -PI / 2), (0.0, 0.0),
+              (180.0, PI), (45.0, PI / 4), (90.0, PI / 2)],
+    "acot": [(INF, 0.0), (-INF, 0.0), (NAN, NAN), (0.5, 1.107148717794090e+00), (-0.5, -1.107148717794090e+00),
+             (-1.0, -7.853981633974483e-01), (1.0, 7.853981633974483e-01), (0.0, 1.570796326794897e+00)],
+    "asind": [(INF, NAN), (-INF, NAN), (NAN, NAN), (0.5, 30.0), (-0.5, -30.0), (-1.0, -90.0), (1.0, 90.0), (0.0, 0.0)],
+    "acosd": [(INF, NAN), (-INF, NAN), (NAN, NAN), (0.5, 60.0), (-0.5, 120.0), (-1.0, 180.0), (1.0, 0.0), (0.0, 90.0)],
+    "atand": [(INF, 90.0), (-INF, -90.0), (NAN, NAN), (0.5, 2.656505117707799e+01), (-0.5, -2.656505117707799e+01),
+              (-1.0, -45.0), (1.0, 45.0), (0.0, 0.0)],
+    "asinpi": [(NAN, NAN), (0.5, "1/6"), (-0.5, "-1/6"), (-1.0, -0.5), (1.0, 0.5), (0.0, 0.0)],
+    "acospi": [(NAN, NAN), (0.5, "1/3"), (-0.5, "2/3"), (-1.0, 1.0), (1.0, 0.0), (0.0, 0.5)],
+    "atanpi": [(INF, 0.5), (-INF, -0.5), (NAN, NAN), (-1.0, -0.25), (1.0, 0.25), (0.0, 0.0)],
+    "acsc": [(INF, 0.0), (-INF, 0.0), (NAN, NAN), (0.0, NAN), (-2.0, -PI / 6), (-1.0, -PI / 2), (1.0, PI / 2),
+             (2.0, PI / 6)],
+    "acscd": [(INF, 0.0), (-INF, 0.0), (NAN, NAN), (0.0, NAN), (-2.0, -30.0), (-1.0, -90.0), (1.0, 90.0)],
+    "asec": [(INF, PI / 2), (-INF, PI / 2), (NAN, NAN), (0.0, NAN), (-2.0, 2 * PI / 3), (-1.0, PI), (1.0, 0.0),
+             (2.0, PI / 3)],
+    "asecd": [(INF, 90.0), (-INF, 90.0), (NAN, NAN), (0.0, NAN), (-2.0, 120.0), (-1.0, 180.0), (1.0, 0.0),
+              (2.0, 60.0)],
+}
+
+
+@pytest.mark.parametrize("fn", sorted(TRIGX_SPECIALS))
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_trig_compositions_special_values(oracle, fn, dt):
+    L = oracle.load()
+    u = ulp_f if dt == np.float32 else ulp_d
+    bound = 1.5 if fn == "acot" else 0.5
+    frac = {"1/6": dt(1) / dt(6), "-1/6": -(dt(1) / dt(6)), "1/3": dt(1) / dt(3), "2/3": dt(2) / dt(3)}
+    for x, r in TRIGX_SPECIALS[fn]:
+        got = oracle.trigx(fn, np.array([x], dt))[0]
+        want = frac[r] if isinstance(r, str) else dt(r)
+        assert u(L, float(got), float(want)) <= bound, (fn, dt, x, got, want)
+    if fn == "acot":   # unit/scalar/acot.cpp: acot(1/Eps) = Eps within 1.5
+        e = np.finfo(dt).eps
+        assert u(L, float(oracle.trigx(fn, np.array([dt(1) / e], dt))[0]), float(e)) <= 1.5
