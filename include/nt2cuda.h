@@ -149,7 +149,17 @@ enum {
   NT2CUDA_OP_ACSC = 44,       /* asin(rec(x)) */
   NT2CUDA_OP_ACSCD = 45,      /* indeg(acsc(x)) */
   NT2CUDA_OP_ASEC = 46,       /* pi/2 - acsc(x) */
-  NT2CUDA_OP_ASECD = 47       /* indeg(asec(x)) */
+  NT2CUDA_OP_ASECD = 47,      /* indeg(asec(x)) */
+  /* cot and the pi- and degree-unit functors (generic/<name>.hpp: trig_base cota/tana with the
+   * pi_tag and degree_tag reductions); they follow NT2CUDA_MAP_SIMD128 as sin and cos do. */
+  NT2CUDA_OP_COT = 48,
+  NT2CUDA_OP_TANPI = 49,      /* tan(pi x), NaN where x - 1/2 is an integer */
+  NT2CUDA_OP_COTPI = 50,      /* cot(pi x), NaN at nonzero integers */
+  NT2CUDA_OP_SIND = 51,       /* x in degrees */
+  NT2CUDA_OP_COSD = 52,
+  NT2CUDA_OP_TAND = 53,       /* NaN at odd multiples of 90 */
+  NT2CUDA_OP_COTD = 54,       /* NaN at nonzero multiples of 180 */
+  NT2CUDA_OP_SECD = 55        /* rec(cosd(x)), NaN where cosd(x) is 0 */
 };
 
 /* out = atan2(a0, a1) elementwise (NT2's SIMD form,

@@ -311,6 +311,13 @@ NT2CUDA_FN1(cos, cos_)
 NT2CUDA_FN1(tan, tan_)
 NT2CUDA_FN1(sinpi, sinpi_)
 NT2CUDA_FN1(cospi, cospi_)
+NT2CUDA_FN1(cot, cot_)
+NT2CUDA_FN1(tanpi, tanpi_)
+NT2CUDA_FN1(cotpi, cotpi_)
+NT2CUDA_FN1(sind, sind_)
+NT2CUDA_FN1(cosd, cosd_)
+NT2CUDA_FN1(tand, tand_)
+NT2CUDA_FN1(cotd, cotd_)
 NT2CUDA_FN1(asin, asin_)
 NT2CUDA_FN1(acos, acos_)
 NT2CUDA_FN1(atan, atan_)
@@ -377,6 +384,7 @@ NT2CUDA_COMPOSED(acsc, asin(rec(a)))
 NT2CUDA_COMPOSED(acscd, indeg(acsc(a)))
 NT2CUDA_COMPOSED(asec, make_unary<tag::pio2_minus_>(acsc(a)))
 NT2CUDA_COMPOSED(asecd, indeg(asec(a)))
+NT2CUDA_COMPOSED(secd, rec(make_unary<tag::nan_if_zero_>(cosd(a))))
 #undef NT2CUDA_COMPOSED
 
 #define NT2CUDA_FN3(NAME, TAG)                                                          \

@@ -19,7 +19,8 @@ OPS = {"exp": 0, "log": 1, "erfc": 2, "normcdf": 3, "fastnormcdf": 4, "sqrt": 5,
        "asin": 17, "acos": 18, "atan": 19, "sinh": 20, "cosh": 21, "tanh": 22, "cbrt": 23, "sqrt1pm1": 24,
        "exprecneg": 25, "exprecnegc": 26, "expx2": 27, "realsqrt": 28, "reallog": 29, "csc": 30, "sec": 31,
        "cscpi": 32, "secpi": 33, "cscd": 34, "indeg": 35, "inrad": 36, "acot": 37, "asind": 38, "acosd": 39,
-       "atand": 40, "asinpi": 41, "acospi": 42, "atanpi": 43, "acsc": 44, "acscd": 45, "asec": 46, "asecd": 47}
+       "atand": 40, "asinpi": 41, "acospi": 42, "atanpi": 43, "acsc": 44, "acscd": 45, "asec": 46, "asecd": 47,
+       "cot": 48, "tanpi": 49, "cotpi": 50, "sind": 51, "cosd": 52, "tand": 53, "cotd": 54, "secd": 55}
 # binary functors of nt2cuda_map2_f32/f64
 OPS2 = {"atan2": 0, "pow": 1, "pow_abs": 2, "realpow": 3, "logspace_add": 4, "logspace_sub": 5, "expx2": 6}
 CDF = {"normcdf": 0, "fastnormcdf": 1}
@@ -51,7 +52,8 @@ def map_(op: str, x: torch.Tensor, out: torch.Tensor | None = None, fused: bool 
     """out = nt2::op(x) for op in exp, log, erfc, normcdf, fastnormcdf, sqrt, exp2, exp10, log2, log10, expm1,
     log1p, sin, cos, tan, sinpi, cospi, asin, acos, atan, sinh, cosh, tanh, cbrt, sqrt1pm1, exprecneg, exprecnegc,
     expx2, realsqrt, reallog and the composed trigonometric ops (csc, sec, cscpi, secpi, cscd, indeg, inrad,
-    acot, asind, acosd, atand, asinpi, acospi, atanpi, acsc, acscd, asec, asecd).  The trigonometric ops reduce each
+    acot, asind, acosd, atand, asinpi, acospi, atanpi, acsc, acscd, asec, asecd), cot, tanpi, cotpi and the degree
+    forms sind, cosd, tand, cotd, secd.  The trigonometric ops reduce each
     element on its own (NT2's scalar
     code); with simd128 they reduce each 16-byte pack of x with the method NT2's 128-bit SIMD code picks for
     the pack's largest |x| (tables that are not 16-byte aligned: scalar code throughout)."""

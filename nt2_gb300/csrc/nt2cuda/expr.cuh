@@ -47,6 +47,7 @@ struct trunc_u8_ {};
 // simd128_<T> evaluates T over 16-byte packs as NT2's 128-bit SIMD code does
 // (see regs<node<simd128_<...>>> below)
 struct sin_ {}; struct cos_ {}; struct tan_ {}; struct sinpi_ {}; struct cospi_ {};
+struct cot_ {}; struct tanpi_ {}; struct cotpi_ {}; struct sind_ {}; struct cosd_ {}; struct tand_ {}; struct cotd_ {};
 template <class T> struct simd128_ {};
 struct asin_ {}; struct acos_ {}; struct atan_ {}; struct atan2_ {};
 struct sinh_ {}; struct cosh_ {}; struct tanh_ {};
@@ -56,7 +57,7 @@ struct cbrt_ {}; struct sqrt1pm1_ {}; struct exprecneg_ {}; struct exprecnegc_ {
 struct expx2s_ {}; struct pow_abs_ {}; struct logspace_add_ {}; struct logspace_sub_ {};
 // steps of the composed trigonometric functors (csc = rec(sin), asind = indeg(asin), ...)
 struct indeg_ {}; struct inrad_ {}; struct invpi_mul_ {}; struct oneo_180_mul_ {}; struct pio2_minus_ {};
-struct cscpi_nan_ {}; struct secpi_nan_ {};
+struct cscpi_nan_ {}; struct secpi_nan_ {}; struct nan_if_zero_ {};
 }  // namespace tag
 
 // ------------------------------------------------------------ tree nodes
@@ -150,6 +151,7 @@ NT2CUDA_UN(oneo_180_mul_, trig::oneo_180_mul(a))
 NT2CUDA_UN(pio2_minus_, trig::pio2_minus(a))
 NT2CUDA_BIN(cscpi_nan_, trig::cscpi_nan(a, (A)b))
 NT2CUDA_BIN(secpi_nan_, trig::secpi_nan(a, (A)b))
+NT2CUDA_UN(nan_if_zero_, (a == (A)0 ? (A)NAN : a))
 NT2CUDA_UN(sqrt1pm1_, math::sqrt1pm1<F>(a))
 NT2CUDA_UN(exprecneg_, math::exprecneg<F>(a))
 NT2CUDA_UN(exprecnegc_, math::exprecnegc<F>(a))
@@ -339,6 +341,13 @@ template <> struct trig_kind<tag::cos_> { static constexpr int value = trig::COS
 template <> struct trig_kind<tag::tan_> { static constexpr int value = trig::TAN; };
 template <> struct trig_kind<tag::sinpi_> { static constexpr int value = trig::SINPI; };
 template <> struct trig_kind<tag::cospi_> { static constexpr int value = trig::COSPI; };
+template <> struct trig_kind<tag::cot_> { static constexpr int value = trig::COT; };
+template <> struct trig_kind<tag::tanpi_> { static constexpr int value = trig::TANPI; };
+template <> struct trig_kind<tag::cotpi_> { static constexpr int value = trig::COTPI; };
+template <> struct trig_kind<tag::sind_> { static constexpr int value = trig::SIND; };
+template <> struct trig_kind<tag::cosd_> { static constexpr int value = trig::COSD; };
+template <> struct trig_kind<tag::tand_> { static constexpr int value = trig::TAND; };
+template <> struct trig_kind<tag::cotd_> { static constexpr int value = trig::COTD; };
 
 template <class NodeTag, class Tag, bool SIMD, class A, int V> struct trig_regs {
   using N = node<NodeTag, A>;
@@ -373,6 +382,13 @@ NT2CUDA_TRIG_REGS(cos_)
 NT2CUDA_TRIG_REGS(tan_)
 NT2CUDA_TRIG_REGS(sinpi_)
 NT2CUDA_TRIG_REGS(cospi_)
+NT2CUDA_TRIG_REGS(cot_)
+NT2CUDA_TRIG_REGS(tanpi_)
+NT2CUDA_TRIG_REGS(cotpi_)
+NT2CUDA_TRIG_REGS(sind_)
+NT2CUDA_TRIG_REGS(cosd_)
+NT2CUDA_TRIG_REGS(tand_)
+NT2CUDA_TRIG_REGS(cotd_)
 #undef NT2CUDA_TRIG_REGS
 
 // prefetch_terms(e, i): L2 prefetch of element i of every table read by e.

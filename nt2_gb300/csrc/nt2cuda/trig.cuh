@@ -32,7 +32,11 @@ namespace trig {
 using math::fbits;
 using math::dbits;
 
-enum kind { SIN = 0, COS = 1, TAN = 2, SINPI = 3, COSPI = 4 };
+enum kind { SIN = 0, COS = 1, TAN = 2, SINPI = 3, COSPI = 4, COT = 5, TANPI = 6, COTPI = 7, SIND = 8, COSD = 9,
+            TAND = 10, COTD = 11 };
+// the reduction a kind takes: pi_tag (x in half turns), degree_tag, or radians (pack-level method)
+__host__ __device__ constexpr bool pi_kind(int k) { return k == SINPI || k == COSPI || k == TANPI || k == COTPI; }
+__host__ __device__ constexpr bool deg_kind(int k) { return k >= SIND && k <= COTD; }
 
 // Bit patterns of the BOOST_SIMD_CONSTANT_REGISTER lines in constants/*.hpp.
 struct tf {
@@ -482,6 +486,27 @@ __device__ __forceinline__ int reduce_pi(double x, double& xr, bool simd)
   return simd ? (toint32(xi) & 3) : (int)(toint64(xi) & 3);
 }
 
+// degree_tag reduction (trig_reduction.hpp:262-278, the form without x87):
+// xi = round2even(x/90), xr = inrad(x - xi*90), n = fast_toint(xi), converted
+// as the pi_tag reduction converts it.
+__device__ __forceinline__ int reduce_deg(float x, float& xr, bool)
+{
+  const float xi = rintf(__fmul_rn(x, fbits(0x3c360b61u)));
+  xr = __fmul_rn(__fsub_rn(x, __fmul_rn(xi, 90.0f)), fbits(0x3c8efa35u));
+  return toint32(xi) & 3;
+}
+__device__ __forceinline__ int reduce_deg(double x, double& xr, bool simd)
+{
+  const double xi = rint(__dmul_rn(x, dbits(0x3f86c16c16c16c17ull)));
+  xr = __dmul_rn(__dsub_rn(x, __dmul_rn(xi, 90.0)), dbits(0x3f91df46a2529d39ull));
+  return simd ? (toint32(xi) & 3) : (int)(toint64(xi) & 3);
+}
+template <int K, class T> __device__ __forceinline__ int reduce_unit(T x, T& xr, bool simd)
+{
+  if constexpr (pi_kind(K)) return reduce_pi(x, xr, simd);
+  else return reduce_deg(x, xr, simd);
+}
+
 // ------------------------------------------------------------- evaluation
 // functions/simd/common/impl/trigo/f_trig_evaluation.hpp:25-56
 template <bool F> __device__ __forceinline__ float cos_eval(float z)
@@ -525,6 +550,9 @@ template <bool F> __device__ __forceinline__ double tan_eval(double x)
   return math::madd<F>(x, __dmul_rn(zz, q), x);
 }
 
+template <class T> __device__ __forceinline__ T oneo_180();
+template <> __device__ __forceinline__ float oneo_180<float>() { return fbits(0x3bb60b61u); }
+template <> __device__ __forceinline__ double oneo_180<double>() { return dbits(0x3f76c16c16c16c17ull); }
 __device__ __forceinline__ float flip(float v, uint32_t s) { return __uint_as_float(__float_as_uint(v) ^ s); }
 __device__ __forceinline__ double flip(double v, uint64_t s)
 {
@@ -536,18 +564,43 @@ template <class T> struct bits_of;
 template <> struct bits_of<float> { using type = uint32_t; static constexpr int top = 31; };
 template <> struct bits_of<double> { using type = uint64_t; static constexpr int top = 63; };
 
-// trig_base sina / cosa / tana (functions/simd/common/impl/trigo/trig_base.hpp:49-92)
+// NT2's invalid-argument tests of tana / cota per unit (scalar/impl/trigo/
+// trig_reduction.hpp:89-90, 268-269, 308-309): none in radians; pi_tag: tan
+// where x - 1/2 is an integer, cot at nonzero integers; degree_tag: tan where
+// (x - 90)/180 is an integer, cot at nonzero multiples of 180.
+template <int K, class T> __device__ __forceinline__ bool tan_invalid(T a0)
+{
+  if constexpr (K == TANPI) return math::is_flint(math::sub(a0, T(0.5)));
+  else if constexpr (K == TAND) return math::is_flint(math::mul(math::sub(a0, T(90)), oneo_180<T>()));
+  else return false;
+}
+template <int K, class T> __device__ __forceinline__ bool cot_invalid(T a0)
+{
+  if constexpr (K == COTPI) return a0 != T(0) && math::is_flint(a0);
+  else if constexpr (K == COTD) return a0 != T(0) && math::is_flint(math::mul(a0, oneo_180<T>()));
+  else return false;
+}
+
+// trig_base sina / cosa / tana / cota (functions/simd/common/impl/trigo/trig_base.hpp:72-141;
+// cota of a zero is rec(a0), an infinity with its sign)
 template <int K, bool F, class T> __device__ __forceinline__ T finish(T a0, T xr, int n)
 {
   using U = typename bits_of<T>::type;
   constexpr int top = bits_of<T>::top;
-  if constexpr (K == TAN) {
+  if constexpr (K == TAN || K == TANPI || K == TAND) {
     T y = tan_eval<F>(xr);
     if (n & 1) y = -math::div(T(1), y);
-    return flip(y, sign_of(a0));
+    y = flip(y, sign_of(a0));
+    return tan_invalid<K>(a0) ? T(NAN) : y;
+  } else if constexpr (K == COT || K == COTPI || K == COTD) {
+    T y = tan_eval<F>(xr);
+    y = (n & 1) ? -y : math::div(T(1), y);
+    y = flip(y, sign_of(a0));
+    y = cot_invalid<K>(a0) ? T(NAN) : y;
+    return a0 != T(0) ? y : math::div(T(1), a0);
   } else {
     const T z = math::mul(xr, xr);
-    if constexpr (K == SIN || K == SINPI) {
+    if constexpr (K == SIN || K == SINPI || K == SIND) {
       const T v = (n & 1) ? cos_eval<F>(z) : sin_eval<F>(z, xr);
       return flip(v, sign_of(a0) ^ ((U)(n & 2) << (top - 1)));
     } else {
@@ -567,9 +620,9 @@ __device__ __forceinline__ void pack_impl(const T (&a)[P], T (&y)[P])
   int n[P];
 #pragma unroll
   for (int l = 0; l < P; ++l) x[l] = fabs(a[l]);
-  if constexpr (K == SINPI || K == COSPI) {
+  if constexpr (pi_kind(K) || deg_kind(K)) {
 #pragma unroll
-    for (int l = 0; l < P; ++l) n[l] = reduce_pi(x[l], xr[l], SIMD);
+    for (int l = 0; l < P; ++l) n[l] = reduce_unit<K>(x[l], xr[l], SIMD);
   } else {
     reduce_pack<P>(x, xr, n);
   }
@@ -740,7 +793,7 @@ template <class T> __device__ __forceinline__ int reduce_low(int lv, T x, T& xr)
 }
 template <int K, bool F, int P, class T> __device__ __forceinline__ void scalar_group(const T (&a)[P], T (&y)[P])
 {
-  if constexpr (K == SINPI || K == COSPI) {
+  if constexpr (pi_kind(K) || deg_kind(K)) {
     pack_impl<K, F, P, false>(a, y);
   } else {
     T xr[P];

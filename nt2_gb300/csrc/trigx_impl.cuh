@@ -1,5 +1,6 @@
 // trigx_impl.cuh -- the trigonometric functors NT2 composes from sin, cos,
-// sinpi, cospi, asin, acos, atan (ops NT2CUDA_OP_CSC..NT2CUDA_OP_ASECD of
+// sinpi, cospi, asin, acos, atan, and cot with the pi- and degree-unit
+// functors (ops NT2CUDA_OP_CSC..NT2CUDA_OP_SECD of
 // nt2cuda_map_f32/f64), lowered as expression trees onto the elementwise
 // transform: csc(x) is rec(sin(x)) evaluated in one pass, the sine part in
 // the scalar or the 128-bit pack form (nt2cuda/expr.cuh, nt2cuda/trig.cuh).
@@ -26,7 +27,8 @@ template <bool F, class E, class T> nt2cuda_status run_e(const E& e, T* y, size_
 template <class Tag, bool SIMD> struct pick { using type = Tag; };
 template <class Tag> struct pick<Tag, true> { using type = tag::simd128_<Tag>; };
 
-// csc, sec, cscpi, secpi, cscd: the sine/cosine node in the form SIMD selects
+// csc, sec, cscpi, secpi, cscd, cot, tanpi, cotpi, sind, cosd, tand, cotd, secd: the
+// reduced node in the form SIMD selects
 template <bool F, bool SIMD, class T> nt2cuda_status recip_impl(int op, const T* x, T* y, size_t n, nt2cuda_stream s)
 {
   const term<T> X{x};
@@ -43,6 +45,15 @@ template <bool F, bool SIMD, class T> nt2cuda_status recip_impl(int op, const T*
       const auto Y = nd<tag::oneo_180_mul_>(X);
       return run_e<F>(nd<tag::cscpi_nan_>(Y, nd<tag::rec_>(nd<Sinpi>(Y))), y, n, s);
     }
+    case NT2CUDA_OP_COT: return run_e<F>(nd<typename pick<tag::cot_, SIMD>::type>(X), y, n, s);
+    case NT2CUDA_OP_TANPI: return run_e<F>(nd<typename pick<tag::tanpi_, SIMD>::type>(X), y, n, s);
+    case NT2CUDA_OP_COTPI: return run_e<F>(nd<typename pick<tag::cotpi_, SIMD>::type>(X), y, n, s);
+    case NT2CUDA_OP_SIND: return run_e<F>(nd<typename pick<tag::sind_, SIMD>::type>(X), y, n, s);
+    case NT2CUDA_OP_COSD: return run_e<F>(nd<typename pick<tag::cosd_, SIMD>::type>(X), y, n, s);
+    case NT2CUDA_OP_TAND: return run_e<F>(nd<typename pick<tag::tand_, SIMD>::type>(X), y, n, s);
+    case NT2CUDA_OP_COTD: return run_e<F>(nd<typename pick<tag::cotd_, SIMD>::type>(X), y, n, s);
+    case NT2CUDA_OP_SECD:
+      return run_e<F>(nd<tag::rec_>(nd<tag::nan_if_zero_>(nd<typename pick<tag::cosd_, SIMD>::type>(X))), y, n, s);
     default: return NT2CUDA_ERR_ARG;
   }
 }
@@ -73,7 +84,7 @@ template <bool F, class T> nt2cuda_status inv_impl(int op, const T* x, T* y, siz
 template <class T> nt2cuda_status trigx_dispatch(int op, const T* x, T* y, size_t n, bool fused, bool simd,
                                                  nt2cuda_stream s)
 {
-  if (op >= NT2CUDA_OP_INDEG) return fused ? inv_impl<true>(op, x, y, n, s) : inv_impl<false>(op, x, y, n, s);
+  if (op >= NT2CUDA_OP_INDEG && op <= NT2CUDA_OP_ASECD) return fused ? inv_impl<true>(op, x, y, n, s) : inv_impl<false>(op, x, y, n, s);
   if (fused) return simd ? recip_impl<true, true>(op, x, y, n, s) : recip_impl<true, false>(op, x, y, n, s);
   return simd ? recip_impl<false, true>(op, x, y, n, s) : recip_impl<false, false>(op, x, y, n, s);
 }

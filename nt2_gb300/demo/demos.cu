@@ -17,7 +17,8 @@
 //              y = sin(x) + cos(x)*tan(x*0.25f) + cospi(x)*sinpi(x), globalsum(sin(x))
 //   pow        z = pow(x, y) + pow(y, 2.0f): pow with a table and with a scalar exponent;
 //              w = cbrt(x) + logspace_add(x, y)
-//   trigx      y = csc(x) + asind(x*1e-3f) + secpi(x): composed trigonometric functors
+//   trigx      y = csc(x) + asind(x*1e-3f) + secpi(x): composed trigonometric functors;
+//              w = cot(x) + sind(x) + tanpi(x*0.01f)
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -188,12 +189,14 @@ int main(int argc, char** argv)
     w = nt2::cbrt(x) + nt2::logspace_add(x, y);
     write_table(argv[5], z);
     write_table(argv[6], w);
-  } else if (cmd == "trigx") {                            // n; in: x ; out: y
+  } else if (cmd == "trigx") {                            // n; in: x ; out: y w
     typedef float T;
-    nt2::table<T> x(nt2::of_size(n)), y;
+    nt2::table<T> x(nt2::of_size(n)), y, w;
     load(x, read_file<T>(argv[3], n));
     y = nt2::csc(x) + nt2::asind(x * T(1e-3)) + nt2::secpi(x);
+    w = nt2::cot(x) + nt2::sind(x) + nt2::tanpi(x * T(0.01));
     write_table(argv[4], y);
+    write_table(argv[5], w);
   } else if (cmd == "sigmadelta") {                       // n = pixels; argv[3] = frames; in: frames ; out: bkg var label
     typedef unsigned char T;
     const int nb_frames = std::atoi(argv[3]);

@@ -461,7 +461,12 @@ static inline double tan_eval_d(double x)
 }
 
 enum { TRIG_SIN = 0, TRIG_COS = 1, TRIG_TAN = 2, TRIG_SINPI = 3, TRIG_COSPI = 4,
-       TRIG_ASIN = 5, TRIG_ACOS = 6, TRIG_ATAN = 7 };
+       TRIG_ASIN = 5, TRIG_ACOS = 6, TRIG_ATAN = 7,
+       TRIG_COT = 8, TRIG_TANPI = 9, TRIG_COTPI = 10, TRIG_SIND = 11, TRIG_COSD = 12, TRIG_TAND = 13,
+       TRIG_COTD = 14 };
+/* which reduction a kind takes: radian (pack-level method), pi_tag or degree_tag */
+static inline int is_pi_kind(int k) { return k == TRIG_SINPI || k == TRIG_COSPI || k == TRIG_TANPI || k == TRIG_COTPI; }
+static inline int is_deg_kind(int k) { return k >= TRIG_SIND && k <= TRIG_COTD; }
 
 /* ------------------------------------------------ inverse functions ----- */
 /* NT2's SIMD forms (functions/simd/common/impl/invtrig/{f,d}_invtrig.hpp), element by element
@@ -625,37 +630,86 @@ static inline double inv_d(int kind, double a)
   return kind == TRIG_ASIN ? asin_d(a) : (kind == TRIG_ACOS ? acos_d(a) : atan_d(a));
 }
 
-/* trig_base sina / cosa / tana (simd/common/impl/trigo/trig_base.hpp:49-92) */
+/* NT2's invalid-argument tests of tana / cota per unit (scalar/impl/trigo/trig_reduction.hpp:89-90,
+ * 268-269, 308-309): none in radians; pi_tag: tan at x - 1/2 integral, cot at nonzero integers;
+ * degree_tag: tan at (x - 90)/180 integral, cot at nonzero x/180 integral. */
+static int flint_f(float x);
+static inline int tan_invalid_f(int kind, float a0)
+{
+  if (kind == TRIG_TANPI) return flint_f(a0 - 0.5f);
+  if (kind == TRIG_TAND) return flint_f((a0 - 90) * tfb(0x3bb60b61u));
+  return 0;
+}
+static inline int cot_invalid_f(int kind, float a0)
+{
+  if (kind == TRIG_COTPI) return a0 != 0 && flint_f(a0);
+  if (kind == TRIG_COTD) return a0 != 0 && flint_f(a0 * tfb(0x3bb60b61u));
+  return 0;
+}
+/* trig_base sina / cosa / tana / cota (simd/common/impl/trigo/trig_base.hpp:72-141) */
 static inline float finish_f(int kind, float a0, float xr, int n)
 {
-  const uint32_t sgn = tbf(a0) & 0x80000000u;
-  if (kind == TRIG_TAN) {
+  const uint32_t sgn = tbf(a0) & (uint32_t)1 << 31;
+  if (kind == TRIG_TAN || kind == TRIG_TANPI || kind == TRIG_TAND) {
     float y = tan_eval_f(xr);
     if (n & 1) y = -(1.0f / y);
-    return tfb(tbf(y) ^ sgn);
+    y = tfb(tbf(y) ^ sgn);
+    return tan_invalid_f(kind, a0) ? (float)NAN : y;
+  }
+  if (kind == TRIG_COT || kind == TRIG_COTPI || kind == TRIG_COTD) {
+    float y = tan_eval_f(xr);
+    y = (n & 1) ? -y : 1.0f / y;
+    y = tfb(tbf(y) ^ sgn);
+    y = cot_invalid_f(kind, a0) ? (float)NAN : y;
+    return a0 != 0 ? y : 1.0f / a0;
   }
   const float z = xr * xr;
   const int swap = n & 1;
-  if (kind == TRIG_SIN || kind == TRIG_SINPI) {
+  if (kind == TRIG_SIN || kind == TRIG_SINPI || kind == TRIG_SIND) {
     const float v = swap ? cos_eval_f(z) : sin_eval_f(z, xr);
-    return tfb(tbf(v) ^ sgn ^ ((uint32_t)(n & 2) << 30));
+    return tfb(tbf(v) ^ sgn ^ ((uint32_t)(n & 2) << (31 - 1)));
   }
   const float v = swap ? sin_eval_f(z, xr) : cos_eval_f(z);
   return tfb(tbf(v) ^ ((uint32_t)((n ^ (n >> 1)) & 1) << 31));
 }
+/* NT2's invalid-argument tests of tana / cota per unit (scalar/impl/trigo/trig_reduction.hpp:89-90,
+ * 268-269, 308-309): none in radians; pi_tag: tan at x - 1/2 integral, cot at nonzero integers;
+ * degree_tag: tan at (x - 90)/180 integral, cot at nonzero x/180 integral. */
+static int flint_d(double x);
+static inline int tan_invalid_d(int kind, double a0)
+{
+  if (kind == TRIG_TANPI) return flint_d(a0 - 0.5);
+  if (kind == TRIG_TAND) return flint_d((a0 - 90) * tdb(0x3f76c16c16c16c17ull));
+  return 0;
+}
+static inline int cot_invalid_d(int kind, double a0)
+{
+  if (kind == TRIG_COTPI) return a0 != 0 && flint_d(a0);
+  if (kind == TRIG_COTD) return a0 != 0 && flint_d(a0 * tdb(0x3f76c16c16c16c17ull));
+  return 0;
+}
+/* trig_base sina / cosa / tana / cota (simd/common/impl/trigo/trig_base.hpp:72-141) */
 static inline double finish_d(int kind, double a0, double xr, int n)
 {
-  const uint64_t sgn = tbd(a0) & 0x8000000000000000ull;
-  if (kind == TRIG_TAN) {
+  const uint64_t sgn = tbd(a0) & (uint64_t)1 << 63;
+  if (kind == TRIG_TAN || kind == TRIG_TANPI || kind == TRIG_TAND) {
     double y = tan_eval_d(xr);
     if (n & 1) y = -(1.0 / y);
-    return tdb(tbd(y) ^ sgn);
+    y = tdb(tbd(y) ^ sgn);
+    return tan_invalid_d(kind, a0) ? (double)NAN : y;
+  }
+  if (kind == TRIG_COT || kind == TRIG_COTPI || kind == TRIG_COTD) {
+    double y = tan_eval_d(xr);
+    y = (n & 1) ? -y : 1.0 / y;
+    y = tdb(tbd(y) ^ sgn);
+    y = cot_invalid_d(kind, a0) ? (double)NAN : y;
+    return a0 != 0 ? y : 1.0 / a0;
   }
   const double z = xr * xr;
   const int swap = n & 1;
-  if (kind == TRIG_SIN || kind == TRIG_SINPI) {
+  if (kind == TRIG_SIN || kind == TRIG_SINPI || kind == TRIG_SIND) {
     const double v = swap ? cos_eval_d(z) : sin_eval_d(z, xr);
-    return tdb(tbd(v) ^ sgn ^ ((uint64_t)(n & 2) << 62));
+    return tdb(tbd(v) ^ sgn ^ ((uint64_t)(n & 2) << (63 - 1)));
   }
   const double v = swap ? sin_eval_d(z, xr) : cos_eval_d(z);
   return tdb(tbd(v) ^ ((uint64_t)((n ^ (n >> 1)) & 1) << 63));
@@ -676,14 +730,30 @@ static inline int reduce_pi_d(double x, double* xr, int simd)
   /* SSE2 converts packed doubles through int32 (cvttpd2dq); scalar code casts to int64 */
   return simd ? (toint32(xi) & 3) : (int)(toint64(xi) & 3);
 }
+/* degree_tag reduction (trig_reduction.hpp:262-278, the form without x87): xi = round2even(x/90),
+ * xr = inrad(x - xi*90), n = fast_toint(xi) (through int32 for packed doubles, as for pi_tag). */
+static inline int reduce_deg_f(float x, float* xr)
+{
+  const float xi = r2e_tf(x * tfb(0x3c360b61u));
+  *xr = (x - xi * 90.0f) * tfb(0x3c8efa35u);
+  return toint32(xi) & 3;
+}
+static inline int reduce_deg_d(double x, double* xr, int simd)
+{
+  const double xi = r2e_td(x * tdb(0x3f86c16c16c16c17ull));
+  *xr = (x - xi * 90.0) * tdb(0x3f91df46a2529d39ull);
+  return simd ? (toint32(xi) & 3) : (int)(toint64(xi) & 3);
+}
 
 static void trig_pack_f(int kind, const float* a, float* y, int k)
 {
   float x[8], xr[8];
   int n[8];
   for (int l = 0; l < k; ++l) x[l] = fabsf(a[l]);
-  if (kind == TRIG_SINPI || kind == TRIG_COSPI) {
+  if (is_pi_kind(kind)) {
     for (int l = 0; l < k; ++l) n[l] = reduce_pi_f(x[l], &xr[l]);
+  } else if (is_deg_kind(kind)) {
+    for (int l = 0; l < k; ++l) n[l] = reduce_deg_f(x[l], &xr[l]);
   } else {
     reduce_pack_f(x, k, xr, n);
   }
@@ -694,8 +764,10 @@ static void trig_pack_d(int kind, const double* a, double* y, int k)
   double x[8], xr[8];
   int n[8];
   for (int l = 0; l < k; ++l) x[l] = fabs(a[l]);
-  if (kind == TRIG_SINPI || kind == TRIG_COSPI) {
+  if (is_pi_kind(kind)) {
     for (int l = 0; l < k; ++l) n[l] = reduce_pi_d(x[l], &xr[l], k > 1);
+  } else if (is_deg_kind(kind)) {
+    for (int l = 0; l < k; ++l) n[l] = reduce_deg_d(x[l], &xr[l], k > 1);
   } else {
     reduce_pack_d(x, k, xr, n);
   }
@@ -706,8 +778,8 @@ static void trig_pack_d(int kind, const double* a, double* y, int k)
  * n % pack tail one element at a time (NT2's scalar code). */
 EXPORT int nt2o_trig_f(int kind, const float* x, float* y, size_t n, int pack)
 {
-  if (kind < 0 || kind > TRIG_ATAN || pack < 1 || pack > 8) return 1;
-  if (kind >= TRIG_ASIN) {
+  if (kind < 0 || kind > TRIG_COTD || pack < 1 || pack > 8) return 1;
+  if (kind >= TRIG_ASIN && kind <= TRIG_ATAN) {
     for (size_t i = 0; i < n; ++i) y[i] = inv_f(kind, x[i]);
     return 0;
   }
@@ -718,8 +790,8 @@ EXPORT int nt2o_trig_f(int kind, const float* x, float* y, size_t n, int pack)
 }
 EXPORT int nt2o_trig_d(int kind, const double* x, double* y, size_t n, int pack)
 {
-  if (kind < 0 || kind > TRIG_ATAN || pack < 1 || pack > 8) return 1;
-  if (kind >= TRIG_ASIN) {
+  if (kind < 0 || kind > TRIG_COTD || pack < 1 || pack > 8) return 1;
+  if (kind >= TRIG_ASIN && kind <= TRIG_ATAN) {
     for (size_t i = 0; i < n; ++i) y[i] = inv_d(kind, x[i]);
     return 0;
   }
@@ -756,12 +828,13 @@ EXPORT int nt2o_rem_pio2_exact_f(float x, float* xr)
  *   7 acot = atan(rec)   8-10 asind, acosd, atand = indeg(asin, acos, atan)
  *   11-13 asinpi, acospi, atanpi = Invpi * (asin, acos, atan)
  *   14 acsc = asin(rec)  15 acscd = indeg(acsc)  16 asec = Pio_2 - acsc  17 asecd = indeg(asec)
+ *   18 secd = rec(cosd), NaN where cosd is 0
  * rec is the IEEE quotient 1/x; the sin/cos based ones use the pack form of the
  * functors above (`pack` lanes). */
 static int flint_f(float x) { return isfinite(x) && (x - truncf(x)) == 0.0f; }
 static int flint_d(double x) { return isfinite(x) && (x - trunc(x)) == 0.0; }
 #define TRIGX_BODY(T, SFX, FLINT, RADINDEG, RADINDEGR, DEGINRAD, INVPI, ONEO_180, PIO_2)                 \
-  if (op < 0 || op > 17) return 1;                                                                      \
+  if (op < 0 || op > 18) return 1;                                                                      \
   T* t = (T*)malloc((n ? n : 1) * sizeof(T));                                                          \
   if (!t) return 1;                                                                                     \
   int st = 0;                                                                                           \
@@ -778,6 +851,10 @@ static int flint_d(double x) { return isfinite(x) && (x - trunc(x)) == 0.0; }
     case 3:                                                                                             \
       st = nt2o_trig_##SFX(TRIG_COSPI, x, y, n, pack);                                                  \
       for (size_t i = 0; i < n; ++i) y[i] = FLINT(((x[i] * 2) - 1) * (T)0.5) ? (T)NAN : (T)1 / y[i];   \
+      break;                                                                                            \
+    case 18:                                                                                            \
+      st = nt2o_trig_##SFX(TRIG_COSD, x, y, n, pack);                                                   \
+      for (size_t i = 0; i < n; ++i) y[i] = y[i] == 0 ? (T)NAN : (T)1 / y[i];                           \
       break;                                                                                            \
     case 5: for (size_t i = 0; i < n; ++i) y[i] = x[i] * RADINDEG - x[i] * RADINDEGR; break;           \
     case 6: for (size_t i = 0; i < n; ++i) y[i] = x[i] * DEGINRAD; break;                               \

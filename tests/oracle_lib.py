@@ -128,7 +128,8 @@ def max_ulp(a: np.ndarray, b: np.ndarray):
     return m, w.value
 
 
-TRIG = {"sin": 0, "cos": 1, "tan": 2, "sinpi": 3, "cospi": 4, "asin": 5, "acos": 6, "atan": 7}
+TRIG = {"sin": 0, "cos": 1, "tan": 2, "sinpi": 3, "cospi": 4, "asin": 5, "acos": 6, "atan": 7, "cot": 8, "tanpi": 9,
+        "cotpi": 10, "sind": 11, "cosd": 12, "tand": 13, "cotd": 14}
 
 
 def trig(op: str, x: np.ndarray, pack: int = 1) -> np.ndarray:
@@ -145,7 +146,7 @@ def trig(op: str, x: np.ndarray, pack: int = 1) -> np.ndarray:
 # trigonometric functors NT2 composes from the ones above (nt2o_trigx_f/d op numbers)
 TRIGX = {"csc": 0, "sec": 1, "cscpi": 2, "secpi": 3, "cscd": 4, "indeg": 5, "inrad": 6, "acot": 7, "asind": 8,
          "acosd": 9, "atand": 10, "asinpi": 11, "acospi": 12, "atanpi": 13, "acsc": 14, "acscd": 15, "asec": 16,
-         "asecd": 17}
+         "asecd": 17, "secd": 18}
 
 
 def trigx(op: str, x: np.ndarray, pack: int = 1) -> np.ndarray:

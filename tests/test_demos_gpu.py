@@ -173,9 +173,13 @@ def test_trigx_demo(demos, oracle, tmp_path):
     n = 30011
     x = np.random.default_rng(14).uniform(-600, 600, n).astype(np.float32)
     x[::7] = np.round(x[::7] * 2) / 2              # integers and halves: secpi's NaNs
-    _, (oy,) = run(demos, tmp_path, "trigx", n, [x], 1)
+    _, (oy, ow) = run(demos, tmp_path, "trigx", n, [x], 2)
     want = (oracle.trigx("csc", x) + oracle.trigx("asind", x * np.float32(1e-3))) + oracle.trigx("secpi", x)
     got = np.fromfile(oy, np.float32)
+    bad = ~(np.isnan(got) & np.isnan(want)) & (got.view(np.uint32) != want.view(np.uint32))
+    assert not bad.any(), (np.flatnonzero(bad)[:5], x[bad][:5], got[bad][:5], want[bad][:5])
+    want = (oracle.trig("cot", x) + oracle.trig("sind", x)) + oracle.trig("tanpi", x * np.float32(0.01))
+    got = np.fromfile(ow, np.float32)
     bad = ~(np.isnan(got) & np.isnan(want)) & (got.view(np.uint32) != want.view(np.uint32))
     assert not bad.any(), (np.flatnonzero(bad)[:5], x[bad][:5], got[bad][:5], want[bad][:5])
 

@@ -571,3 +571,61 @@ def test_trig_compositions_special_values(oracle, fn, dt):
     if fn == "acot":   # unit/scalar/acot.cpp: acot(1/Eps) = Eps within 1.5
         e = np.finfo(dt).eps
         assert u(L, float(oracle.trigx(fn, np.array([dt(1) / e], dt))[0]), float(e)) <= 1.5
+
+
+# cot, tanpi, cotpi and the degree-unit functors: modules/core/trigonometric/unit/scalar/
+# {cot,tanpi,cotpi,sind,cosd,tand,cotd,secd}.cpp (bounds per value as there).
+S2O2 = math.sqrt(2) / 2
+TRIG_UNITS_SPECIALS = {
+    "cot": [(-0.0, -INF, .5), (INF, NAN, .5), (-INF, NAN, .5), (NAN, NAN, .5), (0.0, INF, .5), (-PI / 2, 0.0, .5),
+            (-PI / 4, -1.0, .5), (PI / 2, 0.0, .5), (PI / 4, 1.0, .5)],
+    "tanpi": [(0.5, NAN, .5), (INF, NAN, .5), (-0.5, NAN, .5), (-INF, NAN, .5), (NAN, NAN, .5), (-0.25, -1.0, 1.),
+              (-1.0, 0.0, .5), (1.0, 0.0, .5), (0.25, 1.0, 1.), (0.0, 0.0, .5)],
+    "cotpi": [(-0.0, -INF, .5), (INF, NAN, .5), (-INF, NAN, .5), (NAN, NAN, .5), (1.0, NAN, .5), (0.0, INF, .5),
+              (-0.25, -1.0, .5), (0.5, 0.0, .5), (-0.5, 0.0, .5), (0.25, 1.0, .5)],
+    "sind": [(INF, NAN, .5), (-INF, NAN, .5), (NAN, NAN, .5), (-180.0, 0.0, .5), (-45.0, -S2O2, .5), (-90.0, -1.0, .5),
+             (0.0, 0.0, .5), (180.0, 0.0, .5), (45.0, S2O2, .5), (90.0, 1.0, .5)],
+    "cosd": [(INF, NAN, .5), (-INF, NAN, .5), (NAN, NAN, .5), (-180.0, -1.0, .5), (-45.0, S2O2, .5), (-90.0, 0.0, .5),
+             (180.0, -1.0, .5), (45.0, S2O2, .5), (90.0, 0.0, .5), (0.0, 1.0, .5)],
+    "tand": [(-90.0, NAN, .5), (INF, NAN, .5), (-INF, NAN, .5), (NAN, NAN, .5), (90.0, NAN, .5), (-180.0, 0.0, .5),
+             (-45.0, -1.0, .5), (0.0, 0.0, .5), (180.0, 0.0, .5), (45.0, 1.0, .5)],
+    "cotd": [(-0.0, -INF, .5), (INF, NAN, .5), (-INF, NAN, .5), (NAN, NAN, .5), (0.0, INF, .5), (-45.0, -1.0, 4.),
+             (-90.0, 0.0, .5), (45.0, 1.0, 4.), (90.0, 0.0, .5)],
+    "secd": [(-90.0, NAN, .5), (INF, NAN, .5), (-INF, NAN, .5), (NAN, NAN, .5), (90.0, NAN, .5), (-180.0, -1.0, .5),
+             (-45.0, math.sqrt(2), .5), (0.0, 1.0, .5), (180.0, -1.0, .5), (45.0, math.sqrt(2), .5)],
+}
+
+
+@pytest.mark.parametrize("fn", sorted(TRIG_UNITS_SPECIALS))
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_trig_units_special_values(oracle, fn, dt):
+    L = oracle.load()
+    u = ulp_f if dt == np.float32 else ulp_d
+    for x, r, bound in TRIG_UNITS_SPECIALS[fn]:
+        xs = np.array([x], dt)
+        got = (oracle.trigx(fn, xs) if fn == "secd" else oracle.trig(fn, xs))[0]
+        assert u(L, float(got), float(dt(r))) <= bound, (fn, dt, x, got)
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_degree_and_pi_forms_accuracy(oracle, dt):
+    """sind/cosd/tand against sin/cos/tan of the exact angle (mpmath, 40 digits: x/180 and pi*x are
+    formed exactly there), and tanpi/cotpi against tan(pi x); NT2 states no cover bound for these,
+    the errors here stay within 2 ulps."""
+    mpmath = pytest.importorskip("mpmath")
+    mpmath.mp.dps = 40
+    rng = np.random.default_rng(31)
+    x = rng.uniform(-720, 720, 3000).astype(dt)
+    x = x[np.abs(np.remainder(x, 90)) > 1e-2]          # away from the poles and zeros
+    for fn, ref in (("sind", mpmath.sinpi), ("cosd", mpmath.cospi),
+                    ("tand", lambda t: mpmath.sinpi(t) / mpmath.cospi(t))):
+        want = np.array([float(ref(mpmath.mpf(float(v)) / 180)) for v in x]).astype(dt)
+        m, w = oracle.max_ulp(oracle.trig(fn, x), want)
+        assert m <= 4.0, (fn, dt, m, x[w])
+    p = rng.uniform(-4, 4, 3000).astype(dt)
+    p = p[np.abs(np.remainder(p, 0.5)) > 1e-3]
+    tp = [mpmath.sinpi(mpmath.mpf(float(v))) / mpmath.cospi(mpmath.mpf(float(v))) for v in p]
+    m, w = oracle.max_ulp(oracle.trig("tanpi", p), np.array([float(t) for t in tp]).astype(dt))
+    assert m <= 4.0, ("tanpi", dt, m, p[w])
+    m, w = oracle.max_ulp(oracle.trig("cotpi", p), np.array([float(1 / t) for t in tp]).astype(dt))
+    assert m <= 4.0, ("cotpi", dt, m, p[w])

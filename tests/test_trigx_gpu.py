@@ -1,6 +1,7 @@
 """Composed trigonometric functors on the GPU against the CPU oracle.
 
-csc, sec, cscpi, secpi, cscd (in NT2's scalar form and its 128-bit pack form),
+csc, sec, cscpi, secpi, cscd, cot, tanpi, cotpi and the degree forms sind,
+cosd, tand, cotd, secd (in NT2's scalar form and its 128-bit pack form),
 indeg, inrad, acot, asind, acosd, atand, asinpi, acospi, atanpi, acsc, acscd,
 asec, asecd.  Exact mode (fused = 0) must be bit-identical to the oracle;
 fused mode (hardware FMA in the polynomials) is held to the bounds below.
@@ -11,7 +12,7 @@ import torch
 
 pytestmark = pytest.mark.gpu
 
-FORWARD = ["csc", "sec", "cscpi", "secpi", "cscd"]
+FORWARD = ["csc", "sec", "cscpi", "secpi", "cscd", "cot", "tanpi", "cotpi", "sind", "cosd", "tand", "cotd", "secd"]
 INVERSE = ["indeg", "inrad", "acot", "asind", "acosd", "atand", "asinpi", "acospi", "atanpi", "acsc", "acscd",
            "asec", "asecd"]
 SPECIALS = [0.0, -0.0, 1.0, -1.0, 0.5, -0.5, 2.0, 0.25, np.inf, -np.inf, np.nan, 180.0, -90.0, 45.0, 1e-30]
@@ -30,6 +31,10 @@ def host(t):
     return t.cpu().numpy()
 
 
+def ref(oracle, op, x, pack=1):
+    return oracle.trig(op, x, pack) if op in oracle.TRIG else oracle.trigx(op, x, pack)
+
+
 def same_bits(y, ref):
     it = np.uint64 if y.dtype == np.float64 else np.uint32
     nan = np.isnan(y) & np.isnan(ref)
@@ -43,7 +48,7 @@ def inputs(op, n, dtype, seed):
         hi = np.array([0.78, 1.57, 62.8, 201.0, 8.2e5, 1e30 if dtype == np.float32 else 1e200])
         x = rng.uniform(0, 1, n) * hi[rng.integers(0, hi.size, n)]
         x[::4] = np.round(x[::4] * 4) / 4
-        if op == "cscd":
+        if op in ("cscd", "sind", "cosd", "tand", "cotd", "secd"):
             x[1::4] = np.round(x[1::4] / 45) * 45
     elif op in ("acsc", "acscd", "asec", "asecd", "acot"):
         x = np.exp(rng.uniform(-5, 8, n))
@@ -67,7 +72,7 @@ def test_forward_bit_exact(gpu, oracle, op, dtype, simd, n):
     x = inputs(op, n, dtype, n)
     y = host(gpu.map_(op, to_dev(x), simd128=simd))
     pack = 16 // np.dtype(dtype).itemsize if simd else 1
-    bad = same_bits(y, oracle.trigx(op, x, pack))
+    bad = same_bits(y, ref(oracle, op, x, pack))
     assert bad.size == 0, (op, dtype, simd, bad[:5], x[bad[:5]], y[bad[:5]])
 
 
@@ -77,7 +82,7 @@ def test_forward_bit_exact(gpu, oracle, op, dtype, simd, n):
 def test_inverse_bit_exact(gpu, oracle, op, dtype, n):
     x = inputs(op, n, dtype, n + 1)
     y = host(gpu.map_(op, to_dev(x)))
-    bad = same_bits(y, oracle.trigx(op, x))
+    bad = same_bits(y, ref(oracle, op, x))
     assert bad.size == 0, (op, dtype, bad[:5], x[bad[:5]], y[bad[:5]])
 
 
@@ -88,14 +93,14 @@ def test_fused_bound(gpu, oracle, op, dtype):
     n = 1 << 16
     if op in FORWARD:
         x = rng.uniform(-60, 60, n).astype(dtype)
-        if op == "cscd":
+        if op in ("cscd", "sind", "cosd", "tand", "cotd", "secd"):
             x = (x * 6).astype(dtype)
     else:
         x = inputs(op, n, dtype, 6)
     for simd in ((False, True) if op in FORWARD else (False,)):
         y = host(gpu.map_(op, to_dev(x), fused=True, simd128=simd))
         pack = 16 // np.dtype(dtype).itemsize if simd else 1
-        m, w = oracle.max_ulp(y, oracle.trigx(op, x, pack))
+        m, w = oracle.max_ulp(y, ref(oracle, op, x, pack))
         bound = FUSED_FORWARD[simd] if op in FORWARD else FUSED_INVERSE
         assert m <= bound, (op, dtype, simd, m, x[w])
 
