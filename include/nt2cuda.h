@@ -159,7 +159,23 @@ enum {
   NT2CUDA_OP_COSD = 52,
   NT2CUDA_OP_TAND = 53,       /* NaN at odd multiples of 90 */
   NT2CUDA_OP_COTD = 54,       /* NaN at nonzero multiples of 180 */
-  NT2CUDA_OP_SECD = 55        /* rec(cosd(x)), NaN where cosd(x) is 0 */
+  NT2CUDA_OP_SECD = 55,       /* rec(cosd(x)), NaN where cosd(x) is 0 */
+  /* fast forms (generic/fast_<name>.hpp): no reduction, NaN outside |x| <= pi/4 (radians),
+   * 1/4 (half turns) or 45 (degrees) */
+  NT2CUDA_OP_FAST_SIN = 56,
+  NT2CUDA_OP_FAST_COS = 57,
+  NT2CUDA_OP_FAST_TAN = 58,
+  NT2CUDA_OP_FAST_COT = 59,
+  NT2CUDA_OP_FAST_SINPI = 60,
+  NT2CUDA_OP_FAST_COSPI = 61,
+  NT2CUDA_OP_FAST_TANPI = 62,
+  NT2CUDA_OP_FAST_COTPI = 63,
+  NT2CUDA_OP_FAST_SIND = 64,
+  NT2CUDA_OP_FAST_COSD = 65,
+  NT2CUDA_OP_FAST_TAND = 66,
+  NT2CUDA_OP_FAST_COTD = 67,
+  NT2CUDA_OP_SINC = 68,       /* sin(x)/x (simd/common/sinc.hpp); follows NT2CUDA_MAP_SIMD128 */
+  NT2CUDA_OP_SINCPI = 69      /* sinpi(x)/(pi x) (simd/common/sincpi.hpp); follows NT2CUDA_MAP_SIMD128 */
 };
 
 /* out = atan2(a0, a1) elementwise (NT2's SIMD form,
@@ -188,7 +204,9 @@ enum {
   NT2CUDA_OP2_REALPOW = 3,      /* simd/common/realpow.hpp: pow (NT2 asserts a0 >= 0 or a1 integral) */
   NT2CUDA_OP2_LOGSPACE_ADD = 4, /* simd/common/logspace_add.hpp: log(exp(a0) + exp(a1)) */
   NT2CUDA_OP2_LOGSPACE_SUB = 5, /* simd/common/logspace_sub.hpp: log(exp(a0) - exp(a1)) */
-  NT2CUDA_OP2_EXPX2 = 6         /* simd/common/expx2.hpp:52-74: exp(sign(a1) * a0^2) */
+  NT2CUDA_OP2_EXPX2 = 6,        /* simd/common/expx2.hpp:52-74: exp(sign(a1) * a0^2) */
+  NT2CUDA_OP2_ATAN2D = 7,       /* modules/core/trigonometric/.../generic/atan2d.hpp: indeg(atan2) */
+  NT2CUDA_OP2_NBD_ATAN2 = 8     /* .../simd/common/nbd_atan2.hpp: atan2 without its Inf/NaN cases */
 };
 /* out = op(a0, a1) elementwise.  Replaces `z = nt2::op(x, y)` over two tables of one
  * floating type, evaluated by transform_.  flags: NT2CUDA_MAP_FUSED or 0. */

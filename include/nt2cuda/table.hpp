@@ -353,6 +353,8 @@ NT2CUDA_FN2(pow_abs, pow_abs_)
 NT2CUDA_FN2(logspace_add, logspace_add_)
 NT2CUDA_FN2(logspace_sub, logspace_sub_)
 NT2CUDA_FN2(expx2, expx2s_)
+NT2CUDA_FN2(atan2d, atan2d_)
+NT2CUDA_FN2(nbd_atan2, nbd_atan2_)
 NT2CUDA_FN2(min, min_)
 NT2CUDA_FN2(adds, adds_)
 NT2CUDA_FN2(subs, subs_)
@@ -385,6 +387,20 @@ NT2CUDA_COMPOSED(acscd, indeg(acsc(a)))
 NT2CUDA_COMPOSED(asec, make_unary<tag::pio2_minus_>(acsc(a)))
 NT2CUDA_COMPOSED(asecd, indeg(asec(a)))
 NT2CUDA_COMPOSED(secd, rec(make_unary<tag::nan_if_zero_>(cosd(a))))
+NT2CUDA_COMPOSED(sinc, make_binary<tag::sinc_fix_>(a, sin(a) / a))
+NT2CUDA_COMPOSED(sincpi, make_binary<tag::sinc_fix_>(a, make_unary<tag::invpi_mul_>(sinpi(a) / a)))
+NT2CUDA_COMPOSED(fast_sin, (make_unary<tag::fast_<0, 0>>(a)))
+NT2CUDA_COMPOSED(fast_cos, (make_unary<tag::fast_<1, 0>>(a)))
+NT2CUDA_COMPOSED(fast_tan, (make_unary<tag::fast_<2, 0>>(a)))
+NT2CUDA_COMPOSED(fast_cot, (make_unary<tag::fast_<3, 0>>(a)))
+NT2CUDA_COMPOSED(fast_sinpi, (make_unary<tag::fast_<0, 1>>(a)))
+NT2CUDA_COMPOSED(fast_cospi, (make_unary<tag::fast_<1, 1>>(a)))
+NT2CUDA_COMPOSED(fast_tanpi, (make_unary<tag::fast_<2, 1>>(a)))
+NT2CUDA_COMPOSED(fast_cotpi, (make_unary<tag::fast_<3, 1>>(a)))
+NT2CUDA_COMPOSED(fast_sind, (make_unary<tag::fast_<0, 2>>(a)))
+NT2CUDA_COMPOSED(fast_cosd, (make_unary<tag::fast_<1, 2>>(a)))
+NT2CUDA_COMPOSED(fast_tand, (make_unary<tag::fast_<2, 2>>(a)))
+NT2CUDA_COMPOSED(fast_cotd, (make_unary<tag::fast_<3, 2>>(a)))
 #undef NT2CUDA_COMPOSED
 
 #define NT2CUDA_FN3(NAME, TAG)                                                          \

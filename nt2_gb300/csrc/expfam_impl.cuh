@@ -50,6 +50,8 @@ template <bool F, class T> nt2cuda_status map2_impl(int op, const T* a0, const T
     case NT2CUDA_OP2_LOGSPACE_ADD: return run_binary<F, tag::logspace_add_>(a0, a1, y, n, s);
     case NT2CUDA_OP2_LOGSPACE_SUB: return run_binary<F, tag::logspace_sub_>(a0, a1, y, n, s);
     case NT2CUDA_OP2_EXPX2: return run_binary<F, tag::expx2s_>(a0, a1, y, n, s);
+    case NT2CUDA_OP2_ATAN2D: return run_binary<F, tag::atan2d_>(a0, a1, y, n, s);
+    case NT2CUDA_OP2_NBD_ATAN2: return run_binary<F, tag::nbd_atan2_>(a0, a1, y, n, s);
     default: return NT2CUDA_ERR_ARG;
   }
 }

@@ -56,7 +56,7 @@ void warm_blackscholes_f32(int cdf_kind, int precision);
 // its own so that the build compiles it in parallel).
 nt2cuda_status map_trig(int op, const float* x, float* y, size_t n, bool fused, bool simd128, nt2cuda_stream s);
 nt2cuda_status map_trig(int op, const double* x, double* y, size_t n, bool fused, bool simd128, nt2cuda_stream s);
-// capi_trigx_f32.cu / capi_trigx_f64.cu: ops NT2CUDA_OP_CSC..NT2CUDA_OP_SECD
+// capi_trigx_f32.cu / capi_trigx_f64.cu: ops NT2CUDA_OP_CSC..NT2CUDA_OP_SINCPI
 nt2cuda_status map_trigx(int op, const float* x, float* y, size_t n, bool fused, bool simd128, nt2cuda_stream s);
 nt2cuda_status map_trigx(int op, const double* x, double* y, size_t n, bool fused, bool simd128, nt2cuda_stream s);
 // capi_expfam_f32.cu / capi_expfam_f64.cu: ops NT2CUDA_OP_CBRT..NT2CUDA_OP_REALLOG

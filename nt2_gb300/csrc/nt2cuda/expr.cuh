@@ -57,7 +57,10 @@ struct cbrt_ {}; struct sqrt1pm1_ {}; struct exprecneg_ {}; struct exprecnegc_ {
 struct expx2s_ {}; struct pow_abs_ {}; struct logspace_add_ {}; struct logspace_sub_ {};
 // steps of the composed trigonometric functors (csc = rec(sin), asind = indeg(asin), ...)
 struct indeg_ {}; struct inrad_ {}; struct invpi_mul_ {}; struct oneo_180_mul_ {}; struct pio2_minus_ {};
-struct cscpi_nan_ {}; struct secpi_nan_ {}; struct nan_if_zero_ {};
+struct cscpi_nan_ {}; struct secpi_nan_ {}; struct nan_if_zero_ {}; struct sinc_fix_ {};
+struct atan2d_ {}; struct nbd_atan2_ {};
+// fast_sin ... fast_cotd: K 0 sin, 1 cos, 2 tan, 3 cot; U 0 radian, 1 pi, 2 degree
+template <int K, int U> struct fast_ {};
 }  // namespace tag
 
 // ------------------------------------------------------------ tree nodes
@@ -152,6 +155,12 @@ NT2CUDA_UN(pio2_minus_, trig::pio2_minus(a))
 NT2CUDA_BIN(cscpi_nan_, trig::cscpi_nan(a, (A)b))
 NT2CUDA_BIN(secpi_nan_, trig::secpi_nan(a, (A)b))
 NT2CUDA_UN(nan_if_zero_, (a == (A)0 ? (A)NAN : a))
+NT2CUDA_BIN(sinc_fix_, trig::sinc_fix(a, (A)b))
+NT2CUDA_BIN(atan2d_, trig::indeg(trig::atan2<F>(a, (A)b)))
+NT2CUDA_BIN(nbd_atan2_, trig::nbd_atan2<F>(a, (A)b))
+template <int K, int U, bool F> struct fn<tag::fast_<K, U>, F> {
+  template <class A> __device__ __forceinline__ static auto apply(A a) { return trig::fast<K, U, F>(a); }
+};
 NT2CUDA_UN(sqrt1pm1_, math::sqrt1pm1<F>(a))
 NT2CUDA_UN(exprecneg_, math::exprecneg<F>(a))
 NT2CUDA_UN(exprecnegc_, math::exprecnegc<F>(a))

@@ -843,5 +843,41 @@ template <class T> __device__ __forceinline__ T cscpi_nan(T x, T v)
 template <class T> __device__ __forceinline__ T secpi_nan(T x, T v)
 { return math::is_flint(math::mul(math::sub(math::mul(x, T(2)), T(1)), T(0.5))) ? T(NAN) : v; }
 
+// ------------------------------------------------------------ fast forms
+// fast_sin ... fast_cotd (generic/fast_<name>.hpp: trig_base with the clipped_pio4_
+// mode, NT2's "fast" style, functions/simd/common/impl/trigo/trig_base.hpp:67-135,
+// 143-149): no reduction; x = (|x| > max_range ? NaN : x) * scale, (max_range,
+// scale) = (pi/4, 1) radians, (1/4, pi) half turns, (45, Pio_180) degrees; then the
+// kind's polynomial.  K: 0 sin, 1 cos, 2 tan, 3 cot; U: 0 radian, 1 pi, 2 degree.
+template <int K, int U, bool F, class T> __device__ __forceinline__ T fast(T a0)
+{
+  constexpr bool S = sizeof(T) == 4;
+  const T range = U == 0 ? (S ? (T)fbits(0x3f490fdbu) : (T)dbits(0x3fe921fb54442d18ull)) : (U == 1 ? T(0.25) : T(45));
+  T x = fabs(a0) > range ? T(NAN) : a0;
+  if constexpr (U == 1) x = math::mul(x, S ? (T)fbits(tf::pi) : (T)dbits(td::pi));
+  if constexpr (U == 2) x = math::mul(x, S ? (T)fbits(0x3c8efa35u) : (T)dbits(0x3f91df46a2529d3aull));
+  if constexpr (K == 0) return sin_eval<F>(math::mul(x, x), x);
+  else if constexpr (K == 1) return cos_eval<F>(math::mul(x, x));
+  else if constexpr (K == 2) return tan_eval<F>(x);
+  else return math::div(T(1), tan_eval<F>(x));
+}
+// sinc / sincpi final steps (simd/common/sinc.hpp:33-45, sincpi.hpp:33-45): 1 where
+// |x| < Eps, 0 where x is infinite, else the quotient r computed beside it
+template <class T> __device__ __forceinline__ T sinc_fix(T x, T r)
+{
+  const T eps = sizeof(T) == 4 ? (T)fbits(0x34000000u) : (T)dbits(0x3cb0000000000000ull);
+  r = fabs(x) < eps ? T(1) : r;
+  return isinf(x) ? T(0) : r;
+}
+// nbd_atan2 (simd/common/nbd_atan2.hpp:35-42): atan2 without its infinity and NaN cases
+template <bool F, class T> __device__ __forceinline__ T nbd_atan2(T a0, T a1)
+{
+  const T pi = sizeof(T) == 4 ? (T)fbits(tf::pi) : (T)dbits(td::pi);
+  T z = kernel_atan<F>(math::div(a0, a1));
+  z = (a1 > T(0)) ? z : math::sub(pi, z);
+  z = flip(z, sign_of(a0));
+  return (a0 == T(0)) ? ((a1 < T(0)) ? pi : T(0)) : z;
+}
+
 }  // namespace trig
 }  // namespace nt2cuda

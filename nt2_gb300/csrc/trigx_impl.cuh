@@ -52,6 +52,10 @@ template <bool F, bool SIMD, class T> nt2cuda_status recip_impl(int op, const T*
     case NT2CUDA_OP_COSD: return run_e<F>(nd<typename pick<tag::cosd_, SIMD>::type>(X), y, n, s);
     case NT2CUDA_OP_TAND: return run_e<F>(nd<typename pick<tag::tand_, SIMD>::type>(X), y, n, s);
     case NT2CUDA_OP_COTD: return run_e<F>(nd<typename pick<tag::cotd_, SIMD>::type>(X), y, n, s);
+    case NT2CUDA_OP_SINC:
+      return run_e<F>(nd<tag::sinc_fix_>(X, nd<tag::divides_>(nd<Sin>(X), X)), y, n, s);
+    case NT2CUDA_OP_SINCPI:
+      return run_e<F>(nd<tag::sinc_fix_>(X, nd<tag::invpi_mul_>(nd<tag::divides_>(nd<Sinpi>(X), X))), y, n, s);
     case NT2CUDA_OP_SECD:
       return run_e<F>(nd<tag::rec_>(nd<tag::nan_if_zero_>(nd<typename pick<tag::cosd_, SIMD>::type>(X))), y, n, s);
     default: return NT2CUDA_ERR_ARG;
@@ -77,6 +81,18 @@ template <bool F, class T> nt2cuda_status inv_impl(int op, const T* x, T* y, siz
     case NT2CUDA_OP_ACSCD: return run_e<F>(nd<tag::indeg_>(nd<tag::asin_>(R)), y, n, s);
     case NT2CUDA_OP_ASEC: return run_e<F>(nd<tag::pio2_minus_>(nd<tag::asin_>(R)), y, n, s);
     case NT2CUDA_OP_ASECD: return run_e<F>(nd<tag::indeg_>(nd<tag::pio2_minus_>(nd<tag::asin_>(R))), y, n, s);
+    case NT2CUDA_OP_FAST_SIN: return run_e<F>(nd<tag::fast_<0, 0>>(X), y, n, s);
+    case NT2CUDA_OP_FAST_COS: return run_e<F>(nd<tag::fast_<1, 0>>(X), y, n, s);
+    case NT2CUDA_OP_FAST_TAN: return run_e<F>(nd<tag::fast_<2, 0>>(X), y, n, s);
+    case NT2CUDA_OP_FAST_COT: return run_e<F>(nd<tag::fast_<3, 0>>(X), y, n, s);
+    case NT2CUDA_OP_FAST_SINPI: return run_e<F>(nd<tag::fast_<0, 1>>(X), y, n, s);
+    case NT2CUDA_OP_FAST_COSPI: return run_e<F>(nd<tag::fast_<1, 1>>(X), y, n, s);
+    case NT2CUDA_OP_FAST_TANPI: return run_e<F>(nd<tag::fast_<2, 1>>(X), y, n, s);
+    case NT2CUDA_OP_FAST_COTPI: return run_e<F>(nd<tag::fast_<3, 1>>(X), y, n, s);
+    case NT2CUDA_OP_FAST_SIND: return run_e<F>(nd<tag::fast_<0, 2>>(X), y, n, s);
+    case NT2CUDA_OP_FAST_COSD: return run_e<F>(nd<tag::fast_<1, 2>>(X), y, n, s);
+    case NT2CUDA_OP_FAST_TAND: return run_e<F>(nd<tag::fast_<2, 2>>(X), y, n, s);
+    case NT2CUDA_OP_FAST_COTD: return run_e<F>(nd<tag::fast_<3, 2>>(X), y, n, s);
     default: return NT2CUDA_ERR_ARG;
   }
 }
@@ -84,7 +100,9 @@ template <bool F, class T> nt2cuda_status inv_impl(int op, const T* x, T* y, siz
 template <class T> nt2cuda_status trigx_dispatch(int op, const T* x, T* y, size_t n, bool fused, bool simd,
                                                  nt2cuda_stream s)
 {
-  if (op >= NT2CUDA_OP_INDEG && op <= NT2CUDA_OP_ASECD) return fused ? inv_impl<true>(op, x, y, n, s) : inv_impl<false>(op, x, y, n, s);
+  const bool packless = (op >= NT2CUDA_OP_INDEG && op <= NT2CUDA_OP_ASECD) ||
+                        (op >= NT2CUDA_OP_FAST_SIN && op <= NT2CUDA_OP_FAST_COTD);
+  if (packless) return fused ? inv_impl<true>(op, x, y, n, s) : inv_impl<false>(op, x, y, n, s);
   if (fused) return simd ? recip_impl<true, true>(op, x, y, n, s) : recip_impl<true, false>(op, x, y, n, s);
   return simd ? recip_impl<false, true>(op, x, y, n, s) : recip_impl<false, false>(op, x, y, n, s);
 }

@@ -1113,12 +1113,15 @@ EXPORT float nt2o_pow_abs_f(float a0, float a1) { return pow_abs_f(a0, a1); }
 EXPORT double nt2o_pow_abs_d(double a0, double a1) { return pow_abs_d(a0, a1); }
 
 /* Binary maps: op 0 atan2, 1 pow, 2 pow_abs, 3 realpow (= pow), 4 logspace_add, 5 logspace_sub,
- * 6 expx2(a0, a1). */
+ * 6 expx2(a0, a1), 7 atan2d, 8 nbd_atan2. */
 void nt2o_atan2_f(const float* a0, const float* a1, float* y, size_t n);
 void nt2o_atan2_d(const double* a0, const double* a1, double* y, size_t n);
+void nt2o_atan2x_f(int op, const float* a0, const float* a1, float* y, size_t n);
+void nt2o_atan2x_d(int op, const double* a0, const double* a1, double* y, size_t n);
 EXPORT int nt2o_map2_f(int op, const float* a0, const float* a1, float* y, size_t n)
 {
   if (op == 0) { nt2o_atan2_f(a0, a1, y, n); return 0; }
+  if (op == 7 || op == 8) { nt2o_atan2x_f(op - 7, a0, a1, y, n); return 0; }
   for (size_t i = 0; i < n; ++i) {
     switch (op) {
       case 1: case 3: y[i] = nt2o_pow_f(a0[i], a1[i]); break;
@@ -1134,6 +1137,7 @@ EXPORT int nt2o_map2_f(int op, const float* a0, const float* a1, float* y, size_
 EXPORT int nt2o_map2_d(int op, const double* a0, const double* a1, double* y, size_t n)
 {
   if (op == 0) { nt2o_atan2_d(a0, a1, y, n); return 0; }
+  if (op == 7 || op == 8) { nt2o_atan2x_d(op - 7, a0, a1, y, n); return 0; }
   for (size_t i = 0; i < n; ++i) {
     switch (op) {
       case 1: case 3: y[i] = nt2o_pow_d(a0[i], a1[i]); break;

@@ -816,6 +816,63 @@ EXPORT int nt2o_rem_pio2_exact_f(float x, float* xr)
   return n;
 }
 
+/* -------------------------------------------------- fast forms ------ */
+/* fast_sin ... fast_cotd (generic/fast_<name>.hpp): trig_base with the clipped_pio4_ mode, whose
+ * style is "fast" (simd/common/impl/trigo/trig_base.hpp:67-135, scale at 143-149): no reduction;
+ * x = (|x| > max_range ? NaN : x) * scale with (max_range, scale) = (pi/4, 1), (1/4, pi),
+ * (45, pi/180) per unit; then sin_eval, cos_eval, base_tancot_eval or its reciprocal.
+ * kind 0 sin 1 cos 2 tan 3 cot; unit 0 radian 1 pi 2 degree. */
+static float fast_f(int kind, int unit, float a0)
+{
+  const float r = unit == 0 ? tfb(0x3f490fdbu) : (unit == 1 ? 0.25f : 45.0f);
+  float x = fabsf(a0) > r ? NAN : a0;
+  if (unit) x = x * (unit == 1 ? tfb(F_PI) : tfb(0x3c8efa35u));
+  if (kind == 0) return sin_eval_f(x * x, x);
+  if (kind == 1) return cos_eval_f(x * x);
+  return kind == 2 ? tan_eval_f(x) : 1.0f / tan_eval_f(x);
+}
+static double fast_d(int kind, int unit, double a0)
+{
+  const double r = unit == 0 ? tdb(0x3fe921fb54442d18ull) : (unit == 1 ? 0.25 : 45.0);
+  double x = fabs(a0) > r ? NAN : a0;
+  if (unit) x = x * (unit == 1 ? tdb(D_PI) : tdb(0x3f91df46a2529d3aull));
+  if (kind == 0) return sin_eval_d(x * x, x);
+  if (kind == 1) return cos_eval_d(x * x);
+  return kind == 2 ? tan_eval_d(x) : 1.0 / tan_eval_d(x);
+}
+/* nbd_atan2 (simd/common/nbd_atan2.hpp:35-42): atan2 without the infinity and NaN cases;
+ * atan2d = indeg(atan2) (generic/atan2d.hpp). op 0 atan2d, 1 nbd_atan2. */
+static float nbd_atan2_f(float a0, float a1)
+{
+  float z = kernel_atan_f(a0 / a1);
+  z = (a1 > 0.0f) ? z : tfb(F_PI) - z;
+  z = (tbf(a0) & 0x80000000u) ? -z : z;
+  return (a0 == 0.0f) ? ((a1 < 0.0f) ? tfb(F_PI) : 0.0f) : z;
+}
+static double nbd_atan2_d(double a0, double a1)
+{
+  double z = kernel_atan_d(a0 / a1);
+  z = (a1 > 0.0) ? z : tdb(D_PI) - z;
+  z = (tbd(a0) & 0x8000000000000000ull) ? -z : z;
+  return (a0 == 0.0) ? ((a1 < 0.0) ? tdb(D_PI) : 0.0) : z;
+}
+EXPORT void nt2o_atan2x_f(int op, const float* a0, const float* a1, float* y, size_t n)
+{
+  for (size_t i = 0; i < n; ++i) {
+    if (op == 1) { y[i] = nbd_atan2_f(a0[i], a1[i]); continue; }
+    const float t = atan2_f(a0[i], a1[i]);
+    y[i] = t * tfb(0x42652ee1u) - t * tfb(0xb53387c1u);
+  }
+}
+EXPORT void nt2o_atan2x_d(int op, const double* a0, const double* a1, double* y, size_t n)
+{
+  for (size_t i = 0; i < n; ++i) {
+    if (op == 1) { y[i] = nbd_atan2_d(a0[i], a1[i]); continue; }
+    const double t = atan2_d(a0[i], a1[i]);
+    y[i] = t * tdb(0x404ca5dc1a63c1f8ull) - t * tdb(0xbce1e7ab456405f8ull);
+  }
+}
+
 /* ------------------------------------------------- compositions ------ */
 /* The trigonometric functors NT2 defines on top of the ones above
  * (modules/core/trigonometric/include/nt2/trigonometric/functions/generic headers and
@@ -829,12 +886,15 @@ EXPORT int nt2o_rem_pio2_exact_f(float x, float* xr)
  *   11-13 asinpi, acospi, atanpi = Invpi * (asin, acos, atan)
  *   14 acsc = asin(rec)  15 acscd = indeg(acsc)  16 asec = Pio_2 - acsc  17 asecd = indeg(asec)
  *   18 secd = rec(cosd), NaN where cosd is 0
+ *   19-30 fast_sin, fast_cos, fast_tan, fast_cot, then the pi and the degree forms (fast_f)
+ *   31 sinc = sin(x)/x, 32 sincpi = Invpi * (sinpi(x)/x): 1 for |x| < Eps, 0 for infinite x
+ *      (simd/common/sinc.hpp:33-45, sincpi.hpp:33-45)
  * rec is the IEEE quotient 1/x; the sin/cos based ones use the pack form of the
  * functors above (`pack` lanes). */
 static int flint_f(float x) { return isfinite(x) && (x - truncf(x)) == 0.0f; }
 static int flint_d(double x) { return isfinite(x) && (x - trunc(x)) == 0.0; }
-#define TRIGX_BODY(T, SFX, FLINT, RADINDEG, RADINDEGR, DEGINRAD, INVPI, ONEO_180, PIO_2)                 \
-  if (op < 0 || op > 18) return 1;                                                                      \
+#define TRIGX_BODY(T, SFX, FLINT, RADINDEG, RADINDEGR, DEGINRAD, INVPI, ONEO_180, PIO_2, FABS, EPS)     \
+  if (op < 0 || op > 32) return 1;                                                                      \
   T* t = (T*)malloc((n ? n : 1) * sizeof(T));                                                          \
   if (!t) return 1;                                                                                     \
   int st = 0;                                                                                           \
@@ -852,9 +912,21 @@ static int flint_d(double x) { return isfinite(x) && (x - trunc(x)) == 0.0; }
       st = nt2o_trig_##SFX(TRIG_COSPI, x, y, n, pack);                                                  \
       for (size_t i = 0; i < n; ++i) y[i] = FLINT(((x[i] * 2) - 1) * (T)0.5) ? (T)NAN : (T)1 / y[i];   \
       break;                                                                                            \
+    case 31: case 32:                                                                                   \
+      st = nt2o_trig_##SFX(op == 31 ? TRIG_SIN : TRIG_SINPI, x, y, n, pack);                            \
+      for (size_t i = 0; i < n; ++i) {                                                                  \
+        T r = y[i] / x[i];                                                                              \
+        if (op == 32) r = INVPI * r;                                                                    \
+        r = FABS(x[i]) < EPS ? (T)1 : r;                                                                \
+        y[i] = isinf(x[i]) ? (T)0 : r;                                                                  \
+      }                                                                                                 \
+      break;                                                                                            \
     case 18:                                                                                            \
       st = nt2o_trig_##SFX(TRIG_COSD, x, y, n, pack);                                                   \
       for (size_t i = 0; i < n; ++i) y[i] = y[i] == 0 ? (T)NAN : (T)1 / y[i];                           \
+      break;                                                                                            \
+    case 19: case 20: case 21: case 22: case 23: case 24: case 25: case 26: case 27: case 28: case 29: case 30: \
+      for (size_t i = 0; i < n; ++i) y[i] = fast_##SFX((op - 19) % 4, (op - 19) / 4, x[i]);              \
       break;                                                                                            \
     case 5: for (size_t i = 0; i < n; ++i) y[i] = x[i] * RADINDEG - x[i] * RADINDEGR; break;           \
     case 6: for (size_t i = 0; i < n; ++i) y[i] = x[i] * DEGINRAD; break;                               \
@@ -881,11 +953,12 @@ static int flint_d(double x) { return isfinite(x) && (x - trunc(x)) == 0.0; }
 EXPORT int nt2o_trigx_f(int op, const float* x, float* y, size_t n, int pack)
 {
   TRIGX_BODY(float, f, flint_f, tfb(0x42652ee1u), tfb(0xb53387c1u), tfb(0x3c8efa35u), tfb(0x3ea2f983u),
-             tfb(0x3bb60b61u), tfb(0x3fc90fdbu))
+             tfb(0x3bb60b61u), tfb(0x3fc90fdbu), fabsf, tfb(0x34000000u))
 }
 EXPORT int nt2o_trigx_d(int op, const double* x, double* y, size_t n, int pack)
 {
   TRIGX_BODY(double, d, flint_d, tdb(0x404ca5dc1a63c1f8ull), tdb(0xbce1e7ab456405f8ull), tdb(0x3f91df46a2529d39ull),
-             tdb(0x3fd45f306dc9c883ull), tdb(0x3f76c16c16c16c17ull), tdb(0x3ff921fb54442d18ull))
+             tdb(0x3fd45f306dc9c883ull), tdb(0x3f76c16c16c16c17ull), tdb(0x3ff921fb54442d18ull), fabs,
+             tdb(0x3cb0000000000000ull))
 }
 #undef TRIGX_BODY

@@ -102,7 +102,8 @@ OP = {"exp": 0, "log": 1, "erfc": 2, "normcdf": 3, "fastnormcdf": 4, "sqrt": 5, 
       "tanh": 15, "cbrt": 16, "sqrt1pm1": 17, "exprecneg": 18, "exprecnegc": 19, "expx2": 20,
       "realsqrt": 5, "reallog": 1}
 # binary functors of nt2o_map2_f/d
-OP2 = {"atan2": 0, "pow": 1, "pow_abs": 2, "realpow": 3, "logspace_add": 4, "logspace_sub": 5, "expx2": 6}
+OP2 = {"atan2": 0, "pow": 1, "pow_abs": 2, "realpow": 3, "logspace_add": 4, "logspace_sub": 5, "expx2": 6, "atan2d": 7,
+       "nbd_atan2": 8}
 
 
 def load(variant: str = "libnt2oracle.so"):
@@ -146,7 +147,9 @@ def trig(op: str, x: np.ndarray, pack: int = 1) -> np.ndarray:
 # trigonometric functors NT2 composes from the ones above (nt2o_trigx_f/d op numbers)
 TRIGX = {"csc": 0, "sec": 1, "cscpi": 2, "secpi": 3, "cscd": 4, "indeg": 5, "inrad": 6, "acot": 7, "asind": 8,
          "acosd": 9, "atand": 10, "asinpi": 11, "acospi": 12, "atanpi": 13, "acsc": 14, "acscd": 15, "asec": 16,
-         "asecd": 17, "secd": 18}
+         "asecd": 17, "secd": 18, "fast_sin": 19, "fast_cos": 20, "fast_tan": 21, "fast_cot": 22, "fast_sinpi": 23,
+         "fast_cospi": 24, "fast_tanpi": 25, "fast_cotpi": 26, "fast_sind": 27, "fast_cosd": 28, "fast_tand": 29,
+         "fast_cotd": 30, "sinc": 31, "sincpi": 32}
 
 
 def trigx(op: str, x: np.ndarray, pack: int = 1) -> np.ndarray:

@@ -629,3 +629,51 @@ def test_degree_and_pi_forms_accuracy(oracle, dt):
     assert m <= 4.0, ("tanpi", dt, m, p[w])
     m, w = oracle.max_ulp(oracle.trig("cotpi", p), np.array([float(1 / t) for t in tp]).astype(dt))
     assert m <= 4.0, ("cotpi", dt, m, p[w])
+
+
+# fast_* forms, sinc, sincpi, atan2d, nbd_atan2: modules/core/trigonometric/unit/scalar/*.cpp
+# (NaN outside the fast forms' range; 0.5 ulp, 1 for the values NT2 gives 1).
+FAST_SPECIALS = {
+    "fast_sin": [(-PI, NAN), (-PI / 2, NAN), (INF, NAN), (NAN, NAN), (PI / 2, NAN), (-PI / 4, -S2O2), (PI / 4, S2O2)],
+    "fast_cos": [(-PI, NAN), (-PI / 2, NAN), (-INF, NAN), (NAN, NAN), (PI, NAN), (-PI / 4, S2O2), (PI / 4, S2O2)],
+    "fast_tan": [(-PI, NAN), (PI / 2, NAN), (INF, NAN), (NAN, NAN), (-PI / 4, -1.0), (PI / 4, 1.0)],
+    "fast_cot": [(-PI / 2, NAN), (-0.0, -INF), (INF, NAN), (NAN, NAN), (0.0, INF), (-PI / 4, -1.0), (PI / 4, 1.0)],
+    "fast_sinpi": [(0.5, NAN), (INF, NAN), (-0.5, NAN), (1.0, NAN), (-0.25, -S2O2), (0.25, S2O2), (0.0, 0.0)],
+    "fast_cospi": [(0.5, NAN), (-INF, NAN), (NAN, NAN), (1.0, NAN), (-0.25, S2O2), (0.25, S2O2), (0.0, 1.0)],
+    "fast_tanpi": [(0.5, NAN), (-0.5, NAN), (NAN, NAN), (1.0, NAN), (-0.25, -1.0), (0.25, 1.0), (0.0, 0.0)],
+    "fast_cotpi": [(-0.0, -INF), (0.5, NAN), (INF, NAN), (-0.5, NAN), (1.0, NAN), (0.0, INF), (-0.25, -1.0)],
+    "fast_sind": [(-180.0, NAN), (-90.0, NAN), (INF, NAN), (NAN, NAN), (90.0, NAN), (-45.0, -S2O2), (0.0, 0.0)],
+    "fast_cosd": [(-180.0, NAN), (-90.0, NAN), (-INF, NAN), (NAN, NAN), (180.0, NAN), (-45.0, S2O2), (0.0, 1.0)],
+    "fast_tand": [(-180.0, NAN), (-90.0, NAN), (INF, NAN), (NAN, NAN), (90.0, NAN), (-45.0, -1.0), (0.0, 0.0)],
+    "fast_cotd": [(-0.0, -INF), (-180.0, NAN), (-90.0, NAN), (INF, NAN), (NAN, NAN), (0.0, INF), (90.0, NAN)],
+    "sinc": [(INF, 0.0), (-INF, 0.0), (NAN, NAN), (-PI / 2, "2/pi"), (PI / 2, "2/pi"), ("eps", 1.0), ("denorm", 1.0)],
+    "sincpi": [(INF, 0.0), (-INF, 0.0), (NAN, NAN), (-0.5, "2/pi"), (0.5, "2/pi"), ("eps", 1.0), ("denorm", 1.0)],
+}
+
+
+@pytest.mark.parametrize("fn", sorted(FAST_SPECIALS))
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_fast_and_sinc_special_values(oracle, fn, dt):
+    L = oracle.load()
+    u = ulp_f if dt == np.float32 else ulp_d
+    sym = {"2/pi": dt(2) / dt(math.pi), "eps": np.finfo(dt).eps, "denorm": np.finfo(dt).smallest_subnormal}
+    for x, r in FAST_SPECIALS[fn]:
+        xs = np.array([sym.get(x, x) if isinstance(x, str) else x], dt)
+        want = sym[r] if isinstance(r, str) else dt(r)
+        got = oracle.trigx(fn, xs)[0]
+        assert u(L, float(got), float(want)) <= 1.0, (fn, dt, x, got, want)
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_atan2d_and_nbd_atan2(oracle, dt):
+    """atan2d = indeg(atan2) (unit/scalar/atan2d.cpp: (1,1) -> 45, (-1,-1) -> -135, (0,0) -> 0,
+    (Inf,Inf) -> 45); nbd_atan2 equals atan2 away from infinities and NaNs
+    (unit/scalar/nbd_atan2.cpp)."""
+    L = oracle.load()
+    u = ulp_f if dt == np.float32 else ulp_d
+    for a, b, r in ((1.0, 1.0, 45.0), (-1.0, -1.0, -135.0), (0.0, 0.0, 0.0), (INF, INF, 45.0), (1.0, 0.0, 90.0)):
+        got = oracle.map2("atan2d", np.array([a], dt), np.array([b], dt))[0]
+        assert u(L, float(got), float(dt(r))) <= 0.5, (dt, a, b, got)
+    rng = np.random.default_rng(37)
+    a, b = rng.uniform(-5, 5, 4000).astype(dt), rng.uniform(-5, 5, 4000).astype(dt)
+    assert np.array_equal(oracle.map2("nbd_atan2", a, b), oracle.map2("atan2", a, b))

@@ -12,7 +12,10 @@ import torch
 
 pytestmark = pytest.mark.gpu
 
-FORWARD = ["csc", "sec", "cscpi", "secpi", "cscd", "cot", "tanpi", "cotpi", "sind", "cosd", "tand", "cotd", "secd"]
+FORWARD = ["csc", "sec", "cscpi", "secpi", "cscd", "cot", "tanpi", "cotpi", "sind", "cosd", "tand", "cotd", "secd",
+           "sinc", "sincpi"]
+FAST = ["fast_sin", "fast_cos", "fast_tan", "fast_cot", "fast_sinpi", "fast_cospi", "fast_tanpi", "fast_cotpi",
+        "fast_sind", "fast_cosd", "fast_tand", "fast_cotd"]
 INVERSE = ["indeg", "inrad", "acot", "asind", "acosd", "atand", "asinpi", "acospi", "atanpi", "acsc", "acscd",
            "asec", "asecd"]
 SPECIALS = [0.0, -0.0, 1.0, -1.0, 0.5, -0.5, 2.0, 0.25, np.inf, -np.inf, np.nan, 180.0, -90.0, 45.0, 1e-30]
@@ -50,6 +53,10 @@ def inputs(op, n, dtype, seed):
         x[::4] = np.round(x[::4] * 4) / 4
         if op in ("cscd", "sind", "cosd", "tand", "cotd", "secd"):
             x[1::4] = np.round(x[1::4] / 45) * 45
+    elif op in FAST:
+        # the fast forms' range and a margin beyond it (NaN there)
+        r = 45.0 if op.endswith("d") else (0.25 if "pi" in op else 0.7854)
+        x = rng.uniform(0, 1.2 * r, n)
     elif op in ("acsc", "acscd", "asec", "asecd", "acot"):
         x = np.exp(rng.uniform(-5, 8, n))
     elif op in ("indeg", "inrad"):
@@ -76,7 +83,7 @@ def test_forward_bit_exact(gpu, oracle, op, dtype, simd, n):
     assert bad.size == 0, (op, dtype, simd, bad[:5], x[bad[:5]], y[bad[:5]])
 
 
-@pytest.mark.parametrize("op", INVERSE)
+@pytest.mark.parametrize("op", INVERSE + FAST)
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
 @pytest.mark.parametrize("n", [1, 7, 4097, (1 << 18) + 3])
 def test_inverse_bit_exact(gpu, oracle, op, dtype, n):
@@ -86,7 +93,7 @@ def test_inverse_bit_exact(gpu, oracle, op, dtype, n):
     assert bad.size == 0, (op, dtype, bad[:5], x[bad[:5]], y[bad[:5]])
 
 
-@pytest.mark.parametrize("op", FORWARD + INVERSE)
+@pytest.mark.parametrize("op", FORWARD + INVERSE + FAST)
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
 def test_fused_bound(gpu, oracle, op, dtype):
     rng = np.random.default_rng(6)
