@@ -195,6 +195,24 @@ nt2cuda_status nt2cuda_pow_f32(const float* a0, const float* a1, float* out, siz
 nt2cuda_status nt2cuda_pow_f64(const double* a0, const double* a1, double* out, size_t n, int flags,
                                nt2cuda_stream stream);
 
+/* Forms of nt2cuda_sincos_*: sincos, sincospi, sincosd and their fast forms
+ * (modules/core/trigonometric/.../functions/generic/<name>.hpp: trig_base sincosa, which
+ * takes one reduction and gives the values sina and cosa give). */
+enum {
+  NT2CUDA_SINCOS = 0,
+  NT2CUDA_SINCOSPI = 1,
+  NT2CUDA_SINCOSD = 2,
+  NT2CUDA_FAST_SINCOS = 3,
+  NT2CUDA_FAST_SINCOSPI = 4,
+  NT2CUDA_FAST_SINCOSD = 5
+};
+/* tie(s, c) = sincos(x) (or the form's variant) in one pass over x.  flags: NT2CUDA_MAP_FUSED,
+ * NT2CUDA_MAP_SIMD128 (the reduction of the three full forms, as for sin and cos). */
+nt2cuda_status nt2cuda_sincos_f32(int form, const float* x, float* s, float* c, size_t n, int flags,
+                                  nt2cuda_stream stream);
+nt2cuda_status nt2cuda_sincos_f64(int form, const double* x, double* s, double* c, size_t n, int flags,
+                                  nt2cuda_stream stream);
+
 /* Binary functors of nt2cuda_map2_*, NT2's SIMD forms (paths under
  * modules/core/exponential/include/nt2/exponential/functions/ unless noted). */
 enum {

@@ -88,6 +88,8 @@ _SIGS = {
     "nt2cuda_atan2_f64": (c_int, [c_vp, c_vp, c_vp, c_size, c_int, c_vp]),
     "nt2cuda_pow_f32": (c_int, [c_vp, c_vp, c_vp, c_size, c_int, c_vp]),
     "nt2cuda_pow_f64": (c_int, [c_vp, c_vp, c_vp, c_size, c_int, c_vp]),
+    "nt2cuda_sincos_f32": (c_int, [c_int, c_vp, c_vp, c_vp, c_size, c_int, c_vp]),
+    "nt2cuda_sincos_f64": (c_int, [c_int, c_vp, c_vp, c_vp, c_size, c_int, c_vp]),
     "nt2cuda_map2_f32": (c_int, [c_int, c_vp, c_vp, c_vp, c_size, c_int, c_vp]),
     "nt2cuda_map2_f64": (c_int, [c_int, c_vp, c_vp, c_vp, c_size, c_int, c_vp]),
     "nt2cuda_selftest_wait_timeout": (c_int, [c_vp]),

@@ -111,6 +111,28 @@ def map2(op: str, a0: torch.Tensor, a1: torch.Tensor, out: torch.Tensor | None =
     return out
 
 
+SINCOS = {"sincos": 0, "sincospi": 1, "sincosd": 2, "fast_sincos": 3, "fast_sincospi": 4, "fast_sincosd": 5}
+
+
+def sincos(x: torch.Tensor, form: str = "sincos", s: torch.Tensor | None = None, c: torch.Tensor | None = None,
+           fused: bool = False, simd128: bool = False) -> tuple[torch.Tensor, torch.Tensor]:
+    """tie(s, c) = nt2::sincos(x) (or sincospi, sincosd, fast_sincos, fast_sincospi, fast_sincosd) in one pass."""
+    s = torch.empty_like(x) if s is None else s
+    c = torch.empty_like(x) if c is None else c
+    flags = (MAP_FUSED if fused else 0) | (MAP_SIMD128 if simd128 else 0)
+    L = lib()
+    if x.dtype == torch.float32:
+        st = L.nt2cuda_sincos_f32(SINCOS[form], _dev(x), _dev(s, torch.float32), _dev(c, torch.float32), x.numel(),
+                                  flags, _stream())
+    elif x.dtype == torch.float64:
+        st = L.nt2cuda_sincos_f64(SINCOS[form], _dev(x), _dev(s, torch.float64), _dev(c, torch.float64), x.numel(),
+                                  flags, _stream())
+    else:
+        raise TypeError("sincos takes float32 or float64 tables")
+    check(st, form)
+    return s, c
+
+
 def atan2(a0: torch.Tensor, a1: torch.Tensor, out: torch.Tensor | None = None, fused: bool = False) -> torch.Tensor:
     """out = nt2::atan2(a0, a1) elementwise (NT2's SIMD form)."""
     return _binary("atan2", a0, a1, out, fused)

@@ -34,6 +34,10 @@ SOURCES = [
     "capi_expfam_f64.cu",
     "capi_trigx_f32.cu",
     "capi_trigx_f64.cu",
+    "capi_trigx_fwd_f32.cu",
+    "capi_trigx_fwd_f64.cu",
+    "capi_trigx_fwd128_f32.cu",
+    "capi_trigx_fwd128_f64.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -1,4 +1,4 @@
-// capi_trigx_f64.cu -- nt2cuda_map_f64's composed trigonometric ops (double tables).
+// capi_trigx_f64.cu -- nt2cuda_map_f64's composed trigonometric ops and nt2cuda_sincos_f64 (double tables).
 #include "trigx_impl.cuh"
 
 namespace nt2cuda {
@@ -11,3 +11,15 @@ nt2cuda_status map_trigx(int op, const double* x, double* y, size_t n, bool fuse
 
 }  // namespace detail_capi
 }  // namespace nt2cuda
+
+extern "C" nt2cuda_status nt2cuda_sincos_f64(int form, const double* x, double* s, double* c, size_t n, int flags,
+                                             nt2cuda_stream stream)
+{
+  NT2CUDA_NVTX_RANGE;
+  if (n && (!x || !s || !c)) return NT2CUDA_ERR_ARG;
+  if (flags & ~(NT2CUDA_MAP_FUSED | NT2CUDA_MAP_SIMD128)) return NT2CUDA_ERR_ARG;
+  if (form < NT2CUDA_SINCOS || form > NT2CUDA_FAST_SINCOSD) return NT2CUDA_ERR_ARG;
+  if (n == 0) return NT2CUDA_OK;
+  return nt2cuda::detail_capi::sincos_dispatch(form, x, s, c, n, (flags & NT2CUDA_MAP_FUSED) != 0,
+                                               (flags & NT2CUDA_MAP_SIMD128) != 0, stream);
+}

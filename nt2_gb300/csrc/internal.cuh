@@ -59,6 +59,11 @@ nt2cuda_status map_trig(int op, const double* x, double* y, size_t n, bool fused
 // capi_trigx_f32.cu / capi_trigx_f64.cu: ops NT2CUDA_OP_CSC..NT2CUDA_OP_SINCPI
 nt2cuda_status map_trigx(int op, const float* x, float* y, size_t n, bool fused, bool simd128, nt2cuda_stream s);
 nt2cuda_status map_trigx(int op, const double* x, double* y, size_t n, bool fused, bool simd128, nt2cuda_stream s);
+// capi_trigx_fwd{,128}_f32.cu / _f64.cu: the reduced ops of map_trigx in NT2's scalar / 128-bit form
+nt2cuda_status trigx_fwd_scalar(int op, const float* x, float* y, size_t n, bool fused, nt2cuda_stream s);
+nt2cuda_status trigx_fwd_scalar(int op, const double* x, double* y, size_t n, bool fused, nt2cuda_stream s);
+nt2cuda_status trigx_fwd_simd128(int op, const float* x, float* y, size_t n, bool fused, nt2cuda_stream s);
+nt2cuda_status trigx_fwd_simd128(int op, const double* x, double* y, size_t n, bool fused, nt2cuda_stream s);
 // capi_expfam_f32.cu / capi_expfam_f64.cu: ops NT2CUDA_OP_CBRT..NT2CUDA_OP_REALLOG
 nt2cuda_status map_expfam(int op, const float* x, float* y, size_t n, bool fused, nt2cuda_stream s);
 nt2cuda_status map_expfam(int op, const double* x, double* y, size_t n, bool fused, nt2cuda_stream s);

@@ -97,14 +97,57 @@ template <bool F, class T> nt2cuda_status inv_impl(int op, const T* x, T* y, siz
   }
 }
 
+// tie(s, c) = sincos(x) and its pi, degree and fast forms: two assigns of one statement
+template <bool F, class ES, class EC, class T>
+nt2cuda_status run_pair(const ES& es, const EC& ec, T* s_out, T* c_out, size_t n, nt2cuda_stream s)
+{
+  auto p = make_prog(assign<T, ES>{s_out, es}, assign<T, EC>{c_out, ec});
+  return launch_status(transform<F>(p, n, as_stream(s), "trig"));
+}
+template <bool F, bool SIMD, class T>
+nt2cuda_status sincos_impl(int form, const T* x, T* so, T* co, size_t n, nt2cuda_stream s)
+{
+  const term<T> X{x};
+  switch (form) {
+    case NT2CUDA_SINCOS:
+      return run_pair<F>(nd<typename pick<tag::sin_, SIMD>::type>(X), nd<typename pick<tag::cos_, SIMD>::type>(X), so, co, n, s);
+    case NT2CUDA_SINCOSPI:
+      return run_pair<F>(nd<typename pick<tag::sinpi_, SIMD>::type>(X), nd<typename pick<tag::cospi_, SIMD>::type>(X), so, co,
+                         n, s);
+    case NT2CUDA_SINCOSD:
+      return run_pair<F>(nd<typename pick<tag::sind_, SIMD>::type>(X), nd<typename pick<tag::cosd_, SIMD>::type>(X), so, co,
+                         n, s);
+    default: return NT2CUDA_ERR_ARG;
+  }
+}
+template <bool F, class T> nt2cuda_status fast_sincos_impl(int form, const T* x, T* so, T* co, size_t n, nt2cuda_stream s)
+{
+  const term<T> X{x};
+  switch (form) {
+    case NT2CUDA_FAST_SINCOS: return run_pair<F>(nd<tag::fast_<0, 0>>(X), nd<tag::fast_<1, 0>>(X), so, co, n, s);
+    case NT2CUDA_FAST_SINCOSPI: return run_pair<F>(nd<tag::fast_<0, 1>>(X), nd<tag::fast_<1, 1>>(X), so, co, n, s);
+    case NT2CUDA_FAST_SINCOSD: return run_pair<F>(nd<tag::fast_<0, 2>>(X), nd<tag::fast_<1, 2>>(X), so, co, n, s);
+    default: return NT2CUDA_ERR_ARG;
+  }
+}
+template <class T> nt2cuda_status sincos_dispatch(int form, const T* x, T* so, T* co, size_t n, bool fused, bool simd,
+                                                  nt2cuda_stream s)
+{
+  if (form >= NT2CUDA_FAST_SINCOS)
+    return fused ? fast_sincos_impl<true>(form, x, so, co, n, s) : fast_sincos_impl<false>(form, x, so, co, n, s);
+  if (fused) return simd ? sincos_impl<true, true>(form, x, so, co, n, s) : sincos_impl<true, false>(form, x, so, co, n, s);
+  return simd ? sincos_impl<false, true>(form, x, so, co, n, s) : sincos_impl<false, false>(form, x, so, co, n, s);
+}
+
+// The functors with a reduction are compiled in their own translation units, one
+// per form (capi_trigx_fwd_*.cu: scalar form, capi_trigx_fwd128_*.cu: 128-bit form).
 template <class T> nt2cuda_status trigx_dispatch(int op, const T* x, T* y, size_t n, bool fused, bool simd,
                                                  nt2cuda_stream s)
 {
   const bool packless = (op >= NT2CUDA_OP_INDEG && op <= NT2CUDA_OP_ASECD) ||
                         (op >= NT2CUDA_OP_FAST_SIN && op <= NT2CUDA_OP_FAST_COTD);
   if (packless) return fused ? inv_impl<true>(op, x, y, n, s) : inv_impl<false>(op, x, y, n, s);
-  if (fused) return simd ? recip_impl<true, true>(op, x, y, n, s) : recip_impl<true, false>(op, x, y, n, s);
-  return simd ? recip_impl<false, true>(op, x, y, n, s) : recip_impl<false, false>(op, x, y, n, s);
+  return simd ? trigx_fwd_simd128(op, x, y, n, fused, s) : trigx_fwd_scalar(op, x, y, n, fused, s);
 }
 
 }  // namespace

@@ -57,6 +57,8 @@ def test_argument_validation_without_device(cuda_lib):
     assert L.nt2cuda_pow_f32(None, None, None, 5, 0, None) == 1   # null tables
     assert L.nt2cuda_pow_f64(None, None, None, 0, 2, None) == 1   # SIMD128 is not a pow flag
     assert L.nt2cuda_map2_f32(4, None, None, None, 3, 0, None) == 1  # null tables
+    assert L.nt2cuda_sincos_f32(0, None, None, None, 3, 0, None) == 1  # null tables
+    assert L.nt2cuda_sincos_f64(9, None, None, None, 0, 0, None) == 1  # unknown form
     assert L.nt2cuda_map2_f64(4, None, None, None, 0, 2, None) == 1  # SIMD128 is not a map2 flag
 
 

@@ -121,3 +121,22 @@ def test_misaligned_views(gpu, oracle):
             gpu.map_(op, d[1:], out=out[1:], simd128=simd and op == "csc")
             # an unaligned table takes NT2's scalar code throughout, in both forms
             assert same_bits(host(out)[1:], oracle.trigx(op, x[1:])).size == 0, (op, simd)
+
+
+SINCOS = {"sincos": ("sin", "cos"), "sincospi": ("sinpi", "cospi"), "sincosd": ("sind", "cosd"),
+          "fast_sincos": ("fast_sin", "fast_cos"), "fast_sincospi": ("fast_sinpi", "fast_cospi"),
+          "fast_sincosd": ("fast_sind", "fast_cosd")}
+
+
+@pytest.mark.parametrize("form", sorted(SINCOS))
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("simd", [False, True])
+def test_sincos_pairs(gpu, oracle, form, dtype, simd):
+    """tie(s, c) = sincos(x) in one pass equals (sin(x), cos(x)) of the same form, bit for bit
+    (NT2's sincosa takes the reduction and the signs sina and cosa take)."""
+    sname, cname = SINCOS[form]
+    x = inputs(sname, 65537, dtype, 8)
+    s, c = gpu.sincos(to_dev(x), form=form, simd128=simd)
+    pack = 16 // np.dtype(dtype).itemsize if simd and not form.startswith("fast") else 1
+    assert same_bits(host(s), ref(oracle, sname, x, pack)).size == 0, (form, "sin")
+    assert same_bits(host(c), ref(oracle, cname, x, pack)).size == 0, (form, "cos")
