@@ -175,7 +175,14 @@ enum {
   NT2CUDA_OP_FAST_TAND = 66,
   NT2CUDA_OP_FAST_COTD = 67,
   NT2CUDA_OP_SINC = 68,       /* sin(x)/x (simd/common/sinc.hpp); follows NT2CUDA_MAP_SIMD128 */
-  NT2CUDA_OP_SINCPI = 69      /* sinpi(x)/(pi x) (simd/common/sincpi.hpp); follows NT2CUDA_MAP_SIMD128 */
+  NT2CUDA_OP_SINCPI = 69,     /* sinpi(x)/(pi x) (simd/common/sincpi.hpp); follows NT2CUDA_MAP_SIMD128 */
+  /* modules/core/hyperbolic: simd/common/{atanh,acosh}.hpp, generic/{sech,csch,acoth,asech}.hpp */
+  NT2CUDA_OP_ATANH = 70,
+  NT2CUDA_OP_ACOSH = 71,
+  NT2CUDA_OP_SECH = 72,       /* rec(cosh(x)) */
+  NT2CUDA_OP_CSCH = 73,       /* rec(sinh(x)) */
+  NT2CUDA_OP_ACOTH = 74,      /* atanh(rec(x)) */
+  NT2CUDA_OP_ASECH = 75       /* acosh(rec(x)) */
 };
 
 /* out = atan2(a0, a1) elementwise (NT2's SIMD form,

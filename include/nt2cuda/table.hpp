@@ -324,6 +324,8 @@ NT2CUDA_FN1(atan, atan_)
 NT2CUDA_FN1(sinh, sinh_)
 NT2CUDA_FN1(cosh, cosh_)
 NT2CUDA_FN1(tanh, tanh_)
+NT2CUDA_FN1(atanh, atanh_)
+NT2CUDA_FN1(acosh, acosh_)
 NT2CUDA_FN1(cbrt, cbrt_)
 NT2CUDA_FN1(sqrt1pm1, sqrt1pm1_)
 NT2CUDA_FN1(exprecneg, exprecneg_)
@@ -389,6 +391,10 @@ NT2CUDA_COMPOSED(asecd, indeg(asec(a)))
 NT2CUDA_COMPOSED(secd, rec(make_unary<tag::nan_if_zero_>(cosd(a))))
 NT2CUDA_COMPOSED(sinc, make_binary<tag::sinc_fix_>(a, sin(a) / a))
 NT2CUDA_COMPOSED(sincpi, make_binary<tag::sinc_fix_>(a, make_unary<tag::invpi_mul_>(sinpi(a) / a)))
+NT2CUDA_COMPOSED(sech, rec(cosh(a)))
+NT2CUDA_COMPOSED(csch, rec(sinh(a)))
+NT2CUDA_COMPOSED(acoth, atanh(rec(a)))
+NT2CUDA_COMPOSED(asech, acosh(rec(a)))
 NT2CUDA_COMPOSED(fast_sin, (make_unary<tag::fast_<0, 0>>(a)))
 NT2CUDA_COMPOSED(fast_cos, (make_unary<tag::fast_<1, 0>>(a)))
 NT2CUDA_COMPOSED(fast_tan, (make_unary<tag::fast_<2, 0>>(a)))

@@ -20,6 +20,12 @@ template <bool F, class Tag, class T> nt2cuda_status run_unary(const T* x, T* y,
   return launch_status(transform<F>(p, n, as_stream(s), "map"));
 }
 
+template <bool F, class E, class T> nt2cuda_status run_tree(const E& e, T* y, size_t n, nt2cuda_stream s)
+{
+  auto p = make_prog(assign<T, E>{y, e});
+  return launch_status(transform<F>(p, n, as_stream(s), "map"));
+}
+
 template <bool F, class T> nt2cuda_status expfam_impl(int op, const T* x, T* y, size_t n, nt2cuda_stream s)
 {
   switch (op) {
@@ -31,6 +37,12 @@ template <bool F, class T> nt2cuda_status expfam_impl(int op, const T* x, T* y, 
     // NT2's assertion (x >= 0) is a debug check; the value is sqrt's / log's
     case NT2CUDA_OP_REALSQRT: return run_unary<F, tag::sqrt_>(x, y, n, s);
     case NT2CUDA_OP_REALLOG: return run_unary<F, tag::log_>(x, y, n, s);
+    case NT2CUDA_OP_ATANH: return run_unary<F, tag::atanh_>(x, y, n, s);
+    case NT2CUDA_OP_ACOSH: return run_unary<F, tag::acosh_>(x, y, n, s);
+    case NT2CUDA_OP_SECH: return run_tree<F>(node<tag::rec_, node<tag::cosh_, term<T>>>{{term<T>{x}}}, y, n, s);
+    case NT2CUDA_OP_CSCH: return run_tree<F>(node<tag::rec_, node<tag::sinh_, term<T>>>{{term<T>{x}}}, y, n, s);
+    case NT2CUDA_OP_ACOTH: return run_tree<F>(node<tag::atanh_, node<tag::rec_, term<T>>>{{term<T>{x}}}, y, n, s);
+    case NT2CUDA_OP_ASECH: return run_tree<F>(node<tag::acosh_, node<tag::rec_, term<T>>>{{term<T>{x}}}, y, n, s);
     default: return NT2CUDA_ERR_ARG;
   }
 }

@@ -675,6 +675,28 @@ template <bool F = false> __device__ __forceinline__ double tanh(double a0)
   return bits_xor(r, a0);
 }
 
+// ------------------------------------------------------ inverse hyperbolic
+// atanh and acosh, NT2's SIMD forms (modules/core/hyperbolic/include/nt2/hyperbolic/functions/
+// simd/common/atanh.hpp:38-47, acosh.hpp:36-43); NT2's fma(t, tmp, t) is rounded twice in
+// the exact form; seladd(c, a, b) = a + (c ? b : 0) is an add on every lane.
+template <bool F = false, class T> __device__ __forceinline__ T atanh(T a0)
+{
+  const T ax = fabs(a0), t = add(ax, ax), z1 = sub(T(1), ax);
+  const bool test = ax < T(0.5);
+  const T tmp = div(test ? ax : t, z1);
+  const T r = mul(T(0.5), log1p<F>(test ? madd<F>(t, tmp, t) : tmp));
+  return bits_xor(r, a0);
+}
+template <bool F = false, class T> __device__ __forceinline__ T acosh(T a0)
+{
+  const T t = sub(a0, T(1));
+  const T oneotwoeps = sizeof(T) == 4 ? (T)fbits(0x4a800000u) : (T)dbits(0x4320000000000000ull);
+  const T log_2 = sizeof(T) == 4 ? (T)fbits(0x3f317218u) : (T)dbits(0x3fe62e42fefa39efull);
+  const bool test = t > oneotwoeps;
+  const T z = test ? a0 : add(t, sqrt_(add(add(t, t), mul(t, t))));
+  return add(log1p<F>(z), test ? log_2 : T(0));
+}
+
 // -------------------------------------------------------------------- pow
 // pow(a0, a1) for floating a0 and a1, NT2's SIMD form:
 // modules/core/exponential/include/nt2/exponential/functions/simd/common/pow.hpp:29-37 over

@@ -716,6 +716,41 @@ EXPORT double nt2o_tanh_d(double a0)
   return db(bd(r) ^ bts);
 }
 
+/* ------------------------------------------------ inverse hyperbolic -- */
+/* atanh and acosh, NT2's SIMD forms (modules/core/hyperbolic/include/nt2/hyperbolic/functions/
+ * simd/common/atanh.hpp:38-47, acosh.hpp:36-43); seladd(c, a, b) = a + (c ? b : 0).
+ * sech = rec(cosh), csch = rec(sinh), acoth = atanh(rec), asech = acosh(rec) (generic headers). */
+EXPORT float nt2o_atanh_f(float a0)
+{
+  const float ax = fabsf(a0), t = ax + ax, z1 = 1.0f - ax;
+  const int test = ax < 0.5f;
+  const float tmp = (test ? ax : t) / z1;
+  const float r = 0.5f * nt2o_log1p_f(test ? t * tmp + t : tmp);
+  return fb(bf(r) ^ (bf(a0) & 0x80000000u));
+}
+EXPORT double nt2o_atanh_d(double a0)
+{
+  const double ax = fabs(a0), t = ax + ax, z1 = 1.0 - ax;
+  const int test = ax < 0.5;
+  const double tmp = (test ? ax : t) / z1;
+  const double r = 0.5 * nt2o_log1p_d(test ? t * tmp + t : tmp);
+  return db(bd(r) ^ (bd(a0) & 0x8000000000000000ull));
+}
+EXPORT float nt2o_acosh_f(float a0)
+{
+  const float t = a0 - 1.0f;
+  const int test = t > fb(0x4a800000u);                 /* Oneotwoeps */
+  const float z = test ? a0 : t + sqrtf((t + t) + t * t);
+  return nt2o_log1p_f(z) + (test ? LOG_2_F : 0.0f);
+}
+EXPORT double nt2o_acosh_d(double a0)
+{
+  const double t = a0 - 1.0;
+  const int test = t > db(0x4320000000000000ull);
+  const double z = test ? a0 : t + sqrt((t + t) + t * t);
+  return nt2o_log1p_d(z) + (test ? LOG_2_D : 0.0);
+}
+
 /* ------------------------------------------------------------------ pow -- */
 /* pow(a0, a1) for floating a1, NT2's SIMD form: exponential/functions/simd/common/pow.hpp:20-29
  * over pow_abs (simd/common/pow_abs.hpp:23-79, the cephes algorithm with 2^(-i/16) tables in
@@ -1155,7 +1190,8 @@ EXPORT int nt2o_map2_d(int op, const double* a0, const double* a1, double* y, si
 enum { OP_EXP = 0, OP_LOG = 1, OP_ERFC = 2, OP_NORMCDF = 3, OP_FASTNORMCDF = 4, OP_SQRT = 5,
        OP_ERFC_SCALAR = 6, OP_EXP2 = 7, OP_EXP10 = 8, OP_LOG2 = 9, OP_LOG10 = 10, OP_EXPM1 = 11,
        OP_LOG1P = 12, OP_SINH = 13, OP_COSH = 14, OP_TANH = 15, OP_CBRT = 16, OP_SQRT1PM1 = 17,
-       OP_EXPRECNEG = 18, OP_EXPRECNEGC = 19, OP_EXPX2 = 20 };
+       OP_EXPRECNEG = 18, OP_EXPRECNEGC = 19, OP_EXPX2 = 20, OP_ATANH = 21, OP_ACOSH = 22, OP_SECH = 23,
+       OP_CSCH = 24, OP_ACOTH = 25, OP_ASECH = 26 };
 
 EXPORT int nt2o_map_f(int op, const float* x, float* y, size_t n)
 {
@@ -1183,6 +1219,12 @@ EXPORT int nt2o_map_f(int op, const float* x, float* y, size_t n)
       case OP_EXPRECNEG: y[i] = nt2o_exprecneg_f(a); break;
       case OP_EXPRECNEGC: y[i] = nt2o_exprecnegc_f(a); break;
       case OP_EXPX2: y[i] = nt2o_expx2_f(a); break;
+      case OP_ATANH: y[i] = nt2o_atanh_f(a); break;
+      case OP_ACOSH: y[i] = nt2o_acosh_f(a); break;
+      case OP_SECH: y[i] = (float)1 / nt2o_cosh_f(a); break;
+      case OP_CSCH: y[i] = (float)1 / nt2o_sinh_f(a); break;
+      case OP_ACOTH: y[i] = nt2o_atanh_f((float)1 / a); break;
+      case OP_ASECH: y[i] = nt2o_acosh_f((float)1 / a); break;
       default: return 1;
     }
   }
@@ -1214,6 +1256,12 @@ EXPORT int nt2o_map_d(int op, const double* x, double* y, size_t n)
       case OP_EXPRECNEG: y[i] = nt2o_exprecneg_d(a); break;
       case OP_EXPRECNEGC: y[i] = nt2o_exprecnegc_d(a); break;
       case OP_EXPX2: y[i] = nt2o_expx2_d(a); break;
+      case OP_ATANH: y[i] = nt2o_atanh_d(a); break;
+      case OP_ACOSH: y[i] = nt2o_acosh_d(a); break;
+      case OP_SECH: y[i] = (double)1 / nt2o_cosh_d(a); break;
+      case OP_CSCH: y[i] = (double)1 / nt2o_sinh_d(a); break;
+      case OP_ACOTH: y[i] = nt2o_atanh_d((double)1 / a); break;
+      case OP_ASECH: y[i] = nt2o_acosh_d((double)1 / a); break;
       default: return 1;
     }
   }
