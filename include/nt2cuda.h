@@ -182,7 +182,9 @@ enum {
   NT2CUDA_OP_SECH = 72,       /* rec(cosh(x)) */
   NT2CUDA_OP_CSCH = 73,       /* rec(sinh(x)) */
   NT2CUDA_OP_ACOTH = 74,      /* atanh(rec(x)) */
-  NT2CUDA_OP_ASECH = 75       /* acosh(rec(x)) */
+  NT2CUDA_OP_ASECH = 75,      /* acosh(rec(x)) */
+  NT2CUDA_OP_ASINH = 76,      /* simd/common/asinh.hpp (double and float forms differ) */
+  NT2CUDA_OP_ACSCH = 77       /* asinh(rec(x)) */
 };
 
 /* out = atan2(a0, a1) elementwise (NT2's SIMD form,
@@ -231,7 +233,8 @@ enum {
   NT2CUDA_OP2_LOGSPACE_SUB = 5, /* simd/common/logspace_sub.hpp: log(exp(a0) - exp(a1)) */
   NT2CUDA_OP2_EXPX2 = 6,        /* simd/common/expx2.hpp:52-74: exp(sign(a1) * a0^2) */
   NT2CUDA_OP2_ATAN2D = 7,       /* modules/core/trigonometric/.../generic/atan2d.hpp: indeg(atan2) */
-  NT2CUDA_OP2_NBD_ATAN2 = 8     /* .../simd/common/nbd_atan2.hpp: atan2 without its Inf/NaN cases */
+  NT2CUDA_OP2_NBD_ATAN2 = 8,    /* .../simd/common/nbd_atan2.hpp: atan2 without its Inf/NaN cases */
+  NT2CUDA_OP2_HYPOT = 9         /* boost/simd/arithmetic/functions/simd/common/hypot.hpp */
 };
 /* out = op(a0, a1) elementwise.  Replaces `z = nt2::op(x, y)` over two tables of one
  * floating type, evaluated by transform_.  flags: NT2CUDA_MAP_FUSED or 0. */

@@ -326,6 +326,7 @@ NT2CUDA_FN1(cosh, cosh_)
 NT2CUDA_FN1(tanh, tanh_)
 NT2CUDA_FN1(atanh, atanh_)
 NT2CUDA_FN1(acosh, acosh_)
+NT2CUDA_FN1(asinh, asinh_)
 NT2CUDA_FN1(cbrt, cbrt_)
 NT2CUDA_FN1(sqrt1pm1, sqrt1pm1_)
 NT2CUDA_FN1(exprecneg, exprecneg_)
@@ -357,6 +358,7 @@ NT2CUDA_FN2(logspace_sub, logspace_sub_)
 NT2CUDA_FN2(expx2, expx2s_)
 NT2CUDA_FN2(atan2d, atan2d_)
 NT2CUDA_FN2(nbd_atan2, nbd_atan2_)
+NT2CUDA_FN2(hypot, hypot_)
 NT2CUDA_FN2(min, min_)
 NT2CUDA_FN2(adds, adds_)
 NT2CUDA_FN2(subs, subs_)
@@ -395,6 +397,7 @@ NT2CUDA_COMPOSED(sech, rec(cosh(a)))
 NT2CUDA_COMPOSED(csch, rec(sinh(a)))
 NT2CUDA_COMPOSED(acoth, atanh(rec(a)))
 NT2CUDA_COMPOSED(asech, acosh(rec(a)))
+NT2CUDA_COMPOSED(acsch, asinh(rec(a)))
 NT2CUDA_COMPOSED(fast_sin, (make_unary<tag::fast_<0, 0>>(a)))
 NT2CUDA_COMPOSED(fast_cos, (make_unary<tag::fast_<1, 0>>(a)))
 NT2CUDA_COMPOSED(fast_tan, (make_unary<tag::fast_<2, 0>>(a)))

@@ -43,6 +43,8 @@ template <bool F, class T> nt2cuda_status expfam_impl(int op, const T* x, T* y, 
     case NT2CUDA_OP_CSCH: return run_tree<F>(node<tag::rec_, node<tag::sinh_, term<T>>>{{term<T>{x}}}, y, n, s);
     case NT2CUDA_OP_ACOTH: return run_tree<F>(node<tag::atanh_, node<tag::rec_, term<T>>>{{term<T>{x}}}, y, n, s);
     case NT2CUDA_OP_ASECH: return run_tree<F>(node<tag::acosh_, node<tag::rec_, term<T>>>{{term<T>{x}}}, y, n, s);
+    case NT2CUDA_OP_ASINH: return run_unary<F, tag::asinh_>(x, y, n, s);
+    case NT2CUDA_OP_ACSCH: return run_tree<F>(node<tag::asinh_, node<tag::rec_, term<T>>>{{term<T>{x}}}, y, n, s);
     default: return NT2CUDA_ERR_ARG;
   }
 }
@@ -64,6 +66,7 @@ template <bool F, class T> nt2cuda_status map2_impl(int op, const T* a0, const T
     case NT2CUDA_OP2_EXPX2: return run_binary<F, tag::expx2s_>(a0, a1, y, n, s);
     case NT2CUDA_OP2_ATAN2D: return run_binary<F, tag::atan2d_>(a0, a1, y, n, s);
     case NT2CUDA_OP2_NBD_ATAN2: return run_binary<F, tag::nbd_atan2_>(a0, a1, y, n, s);
+    case NT2CUDA_OP2_HYPOT: return run_binary<F, tag::hypot_>(a0, a1, y, n, s);
     default: return NT2CUDA_ERR_ARG;
   }
 }

@@ -1001,6 +1001,42 @@ template <bool F = false, class T> __device__ __forceinline__ T logspace_sub(T a
   return add(a0, t);
 }
 
+// hypot, Boost.SIMD's SIMD form (boost/simd/arithmetic/functions/simd/common/hypot.hpp:33-49):
+// e = exponent(max(|a0|, |a1|)) -- 0 for Inf and NaN, the biased exponent minus Maxexponent
+// otherwise (so -Maxexponent for zeros and denormals) -- clamped to [Minexponent,
+// Maxexponentm1]; both scaled by 2^-e with Boost.SIMD's ldexp, squared, added, square-rooted,
+// scaled back; Inf where one argument is NaN and the other infinite.
+template <class T> __device__ __forceinline__ T hypot(T a0, T a1)
+{
+  using C = powc<T>;
+  const T r = fabs(a0), i = fabs(a1), m = i > r ? i : r;
+  int e = isfinite(m) ? (int)((C::ubits(m) & C::expmask) >> C::nbm) - (m != T(0) ? C::maxe : 0) : 0;
+  e = min(max(e, C::mine), C::maxe - 1);
+  const T a = pow_ldexp(r, -e), b = pow_ldexp(i, -e);
+  const T res = pow_ldexp(sqrt_(add(mul(a, a), mul(b, b))), e);
+  return ((isnan(a0) && isinf(a1)) || (isnan(a1) && isinf(a0))) ? T(INFINITY) : res;
+}
+// asinh, NT2's SIMD forms (modules/core/hyperbolic/include/nt2/hyperbolic/functions/simd/common/
+// asinh.hpp:46-64 double: log1p of x + x^2/(1 + hypot(1, x)); :66-94 float: a polynomial below
+// 1/2, else log of average(x, hypot(1, x)) plus log 2; average(a, b) = fma(a, 1/2, b/2))
+template <bool F = false> __device__ __forceinline__ float asinh(float a0)
+{
+  constexpr uint32_t P[5] = {0x3ca4d6e6u, 0xbd2ee581u, 0x3d9949b1u, 0xbe2aa9adu, 0x3f800000u};
+  const float x = fabsf(a0), x2 = mul(x, x);
+  const float z = mul(horner<F>(x2, P), x);
+  const float tmp = x > fbits(0x453504f3u) ? x : madd<F>(x, 0.5f, mul(hypot(1.0f, x), 0.5f));
+  const float r = x < 0.5f ? z : add(log<F>(tmp), fbits(0x3f317218u));
+  return bits_xor(r, a0);
+}
+template <bool F = false> __device__ __forceinline__ double asinh(double a0)
+{
+  const double x = fabs(a0);
+  const bool test = x > dbits(0x4190000000000000ull);
+  double z = test ? sub(x, 1.0) : add(x, div(mul(x, x), add(1.0, hypot(1.0, x))));
+  z = x == INFINITY ? x : z;
+  return bits_xor(add(log1p<F>(z), test ? dbits(0x3fe62e42fefa39efull) : 0.0), a0);
+}
+
 }  // namespace math
 }  // namespace nt2cuda
 

@@ -1144,11 +1144,53 @@ EXPORT double nt2o_logspace_sub_d(double a0, double a1)
   const double t = x > -db(0x3fe62e42fefa39efull) ? nt2o_log_d(-nt2o_expm1_d(x)) : nt2o_log1p_d(-nt2o_exp_d(x));
   return a0 + t;
 }
+/* hypot, Boost.SIMD's SIMD form (boost/simd/arithmetic/functions/simd/common/hypot.hpp:33-49):
+ * e = exponent(max(|a0|, |a1|)) (0 for Inf/NaN, -Maxexponent for 0 and denormals, ieee/functions/
+ * simd/common/exponent.hpp), clamped to [Minexponent, Maxexponentm1]; ldexp as in pow; Inf where
+ * one argument is NaN and the other infinite. */
+static float hypot_f(float a0, float a1)
+{
+  const float r = fabsf(a0), i = fabsf(a1), m = i > r ? i : r;
+  int32_t e = isfinite(m) ? (int32_t)((bf(m) & 0x7f800000u) >> 23) - (m != 0.0f ? 127 : 0) : 0;
+  e = e < -126 ? -126 : (e > 126 ? 126 : e);
+  const float a = pow_ldexp_f(r, -e), b = pow_ldexp_f(i, -e);
+  const float res = pow_ldexp_f(sqrtf(a * a + b * b), e);
+  return ((isnan(a0) && isinf(a1)) || (isnan(a1) && isinf(a0))) ? INFINITY : res;
+}
+static double hypot_d(double a0, double a1)
+{
+  const double r = fabs(a0), i = fabs(a1), m = i > r ? i : r;
+  int64_t e = isfinite(m) ? (int64_t)((bd(m) & 0x7ff0000000000000ull) >> 52) - (m != 0.0 ? 1023 : 0) : 0;
+  e = e < -1022 ? -1022 : (e > 1022 ? 1022 : e);
+  const double a = pow_ldexp_d(r, -e), b = pow_ldexp_d(i, -e);
+  const double res = pow_ldexp_d(sqrt(a * a + b * b), e);
+  return ((isnan(a0) && isinf(a1)) || (isnan(a1) && isinf(a0))) ? INFINITY : res;
+}
+/* asinh, NT2's SIMD forms (hyperbolic/functions/simd/common/asinh.hpp:46-64 double, 66-94 float);
+ * average(a, b) = a*0.5 + b*0.5; acsch = asinh(rec) (generic/acsch.hpp). */
+static const uint32_t ASINH_F[5] = {0x3ca4d6e6u, 0xbd2ee581u, 0x3d9949b1u, 0xbe2aa9adu, 0x3f800000u};
+EXPORT float nt2o_asinh_f(float a0)
+{
+  const float x = fabsf(a0), x2 = x * x;
+  const float z = horner_f(x2, ASINH_F, 5) * x;
+  const float tmp = x > fb(0x453504f3u) ? x : x * 0.5f + hypot_f(1.0f, x) * 0.5f;
+  const float r = x < 0.5f ? z : nt2o_log_f(tmp) + LOG_2_F;
+  return fb(bf(r) ^ (bf(a0) & 0x80000000u));
+}
+EXPORT double nt2o_asinh_d(double a0)
+{
+  const double x = fabs(a0);
+  const int test = x > db(0x4190000000000000ull);
+  double z = test ? x - 1.0 : x + (x * x) / (1.0 + hypot_d(1.0, x));
+  z = x == INFINITY ? x : z;
+  z = nt2o_log1p_d(z) + (test ? LOG_2_D : 0.0);
+  return db(bd(z) ^ (bd(a0) & 0x8000000000000000ull));
+}
 EXPORT float nt2o_pow_abs_f(float a0, float a1) { return pow_abs_f(a0, a1); }
 EXPORT double nt2o_pow_abs_d(double a0, double a1) { return pow_abs_d(a0, a1); }
 
 /* Binary maps: op 0 atan2, 1 pow, 2 pow_abs, 3 realpow (= pow), 4 logspace_add, 5 logspace_sub,
- * 6 expx2(a0, a1), 7 atan2d, 8 nbd_atan2. */
+ * 6 expx2(a0, a1), 7 atan2d, 8 nbd_atan2, 9 hypot. */
 void nt2o_atan2_f(const float* a0, const float* a1, float* y, size_t n);
 void nt2o_atan2_d(const double* a0, const double* a1, double* y, size_t n);
 void nt2o_atan2x_f(int op, const float* a0, const float* a1, float* y, size_t n);
@@ -1164,6 +1206,7 @@ EXPORT int nt2o_map2_f(int op, const float* a0, const float* a1, float* y, size_
       case 4: y[i] = nt2o_logspace_add_f(a0[i], a1[i]); break;
       case 5: y[i] = nt2o_logspace_sub_f(a0[i], a1[i]); break;
       case 6: y[i] = nt2o_expx2s_f(a0[i], a1[i]); break;
+      case 9: y[i] = hypot_f(a0[i], a1[i]); break;
       default: return 1;
     }
   }
@@ -1180,6 +1223,7 @@ EXPORT int nt2o_map2_d(int op, const double* a0, const double* a1, double* y, si
       case 4: y[i] = nt2o_logspace_add_d(a0[i], a1[i]); break;
       case 5: y[i] = nt2o_logspace_sub_d(a0[i], a1[i]); break;
       case 6: y[i] = nt2o_expx2s_d(a0[i], a1[i]); break;
+      case 9: y[i] = hypot_d(a0[i], a1[i]); break;
       default: return 1;
     }
   }
@@ -1191,7 +1235,7 @@ enum { OP_EXP = 0, OP_LOG = 1, OP_ERFC = 2, OP_NORMCDF = 3, OP_FASTNORMCDF = 4, 
        OP_ERFC_SCALAR = 6, OP_EXP2 = 7, OP_EXP10 = 8, OP_LOG2 = 9, OP_LOG10 = 10, OP_EXPM1 = 11,
        OP_LOG1P = 12, OP_SINH = 13, OP_COSH = 14, OP_TANH = 15, OP_CBRT = 16, OP_SQRT1PM1 = 17,
        OP_EXPRECNEG = 18, OP_EXPRECNEGC = 19, OP_EXPX2 = 20, OP_ATANH = 21, OP_ACOSH = 22, OP_SECH = 23,
-       OP_CSCH = 24, OP_ACOTH = 25, OP_ASECH = 26 };
+       OP_CSCH = 24, OP_ACOTH = 25, OP_ASECH = 26, OP_ASINH = 27, OP_ACSCH = 28 };
 
 EXPORT int nt2o_map_f(int op, const float* x, float* y, size_t n)
 {
@@ -1225,6 +1269,8 @@ EXPORT int nt2o_map_f(int op, const float* x, float* y, size_t n)
       case OP_CSCH: y[i] = (float)1 / nt2o_sinh_f(a); break;
       case OP_ACOTH: y[i] = nt2o_atanh_f((float)1 / a); break;
       case OP_ASECH: y[i] = nt2o_acosh_f((float)1 / a); break;
+      case OP_ASINH: y[i] = nt2o_asinh_f(a); break;
+      case OP_ACSCH: y[i] = nt2o_asinh_f((float)1 / a); break;
       default: return 1;
     }
   }
@@ -1262,6 +1308,8 @@ EXPORT int nt2o_map_d(int op, const double* x, double* y, size_t n)
       case OP_CSCH: y[i] = (double)1 / nt2o_sinh_d(a); break;
       case OP_ACOTH: y[i] = nt2o_atanh_d((double)1 / a); break;
       case OP_ASECH: y[i] = nt2o_acosh_d((double)1 / a); break;
+      case OP_ASINH: y[i] = nt2o_asinh_d(a); break;
+      case OP_ACSCH: y[i] = nt2o_asinh_d((double)1 / a); break;
       default: return 1;
     }
   }

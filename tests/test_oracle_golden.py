@@ -723,3 +723,38 @@ def test_hyperbolic_inverse_cover(oracle, fn, dt):
     u = L.nt2o_ulpdist_f if dt == np.float32 else L.nt2o_ulpdist_d
     over = sum(u(float(a), float(b)) > bound for a, b in zip(y, want))
     assert over <= 0.02 * x.size, (fn, dt, over)
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_asinh_acsch_hypot(oracle, dt):
+    """asinh: modules/core/hyperbolic/unit/scalar/asinh.cpp (Inf, -Inf, NaN, 0 exact; Valmax,
+    2/Sqrteps, Eps and sample values within 0.5 of the true value) and cover/scalar/asinh.cpp (2 ulp);
+    acsch: unit/scalar/acsch.cpp; hypot: Boost.SIMD's hypot (Inf with a NaN partner, 3-4-5, within
+    one ulp of the true value over the exponent range)."""
+    mpmath = pytest.importorskip("mpmath")
+    mpmath.mp.dps = 40
+    L = oracle.load()
+    u = ulp_f if dt == np.float32 else ulp_d
+    fi = np.finfo(dt)
+    for x, r in ((INF, INF), (-INF, -INF), (NAN, NAN), (0.0, 0.0), (float(fi.eps), float(fi.eps))):
+        assert u(L, float(oracle.map_("asinh", np.array([x], dt))[0]), float(dt(r))) <= 0.5, (dt, x)
+    for x in (float(fi.max), 2 / math.sqrt(float(fi.eps)), 0.3, -2.5, 1e5):
+        want = float(dt(float(mpmath.asinh(mpmath.mpf(float(dt(x)))))))
+        assert u(L, float(oracle.map_("asinh", np.array([x], dt))[0]), want) <= 0.5, (dt, x)
+    for x, r in ((INF, 0.0), (-INF, 0.0), (NAN, NAN)):
+        assert u(L, float(oracle.map_("acsch", np.array([x], dt))[0]), float(dt(r))) <= 0.5, (dt, x)
+    x = np.random.default_rng(43).uniform(-10, 10, 3000).astype(dt)
+    want = np.array([float(mpmath.asinh(mpmath.mpf(float(v)))) for v in x]).astype(dt)
+    m, w = oracle.max_ulp(oracle.map_("asinh", x), want)
+    assert m <= 2.0, ("asinh", dt, m, x[w])
+    h = lambda a, b: oracle.map2("hypot", np.array([a], dt), np.array([b], dt))[0]
+    assert h(INF, NAN) == INF and h(NAN, -INF) == INF and np.isnan(h(NAN, 1.0))
+    assert h(3.0, 4.0) == 5.0 and h(0.0, 0.0) == 0.0 and h(-0.0, 0.0) == 0.0
+    rng = np.random.default_rng(47)
+    lim = 120 if dt == np.float32 else 1000
+    a = (rng.uniform(-1, 1, 3000) * 2.0 ** rng.uniform(-lim, lim, 3000)).astype(dt)
+    b = (rng.uniform(-1, 1, 3000) * 2.0 ** rng.uniform(-lim, lim, 3000)).astype(dt)
+    want = np.array([float(mpmath.sqrt(mpmath.mpf(float(p)) ** 2 + mpmath.mpf(float(q)) ** 2))
+                     for p, q in zip(a, b)]).astype(dt)
+    m, w = oracle.max_ulp(oracle.map2("hypot", a, b), want)
+    assert m <= 2.0, ("hypot", dt, m, a[w], b[w])
