@@ -327,6 +327,8 @@ NT2CUDA_FN1(tanh, tanh_)
 NT2CUDA_FN1(atanh, atanh_)
 NT2CUDA_FN1(acosh, acosh_)
 NT2CUDA_FN1(asinh, asinh_)
+NT2CUDA_FN1(coth, coth_)
+NT2CUDA_FN1(sinhc, sinhc_)
 NT2CUDA_FN1(cbrt, cbrt_)
 NT2CUDA_FN1(sqrt1pm1, sqrt1pm1_)
 NT2CUDA_FN1(exprecneg, exprecneg_)

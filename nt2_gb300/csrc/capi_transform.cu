@@ -264,7 +264,7 @@ nt2cuda_status nt2cuda_map_f32(int op, const float* x, float* y, size_t n, int f
   const bool fused = (flags & NT2CUDA_MAP_FUSED) != 0;
   if (op >= NT2CUDA_OP_SIN && op <= NT2CUDA_OP_TANH)
     return map_trig(op, x, y, n, fused, (flags & NT2CUDA_MAP_SIMD128) != 0, s);
-  if ((op >= NT2CUDA_OP_CBRT && op <= NT2CUDA_OP_REALLOG) || (op >= NT2CUDA_OP_ATANH && op <= NT2CUDA_OP_ACSCH))
+  if ((op >= NT2CUDA_OP_CBRT && op <= NT2CUDA_OP_REALLOG) || (op >= NT2CUDA_OP_ATANH && op <= NT2CUDA_OP_SINHC))
     return map_expfam(op, x, y, n, fused, s);
   if (op >= NT2CUDA_OP_CSC && op <= NT2CUDA_OP_SINCPI)
     return map_trigx(op, x, y, n, fused, (flags & NT2CUDA_MAP_SIMD128) != 0, s);
@@ -279,7 +279,7 @@ nt2cuda_status nt2cuda_map_f64(int op, const double* x, double* y, size_t n, int
   const bool fused = (flags & NT2CUDA_MAP_FUSED) != 0;
   if (op >= NT2CUDA_OP_SIN && op <= NT2CUDA_OP_TANH)
     return map_trig(op, x, y, n, fused, (flags & NT2CUDA_MAP_SIMD128) != 0, s);
-  if ((op >= NT2CUDA_OP_CBRT && op <= NT2CUDA_OP_REALLOG) || (op >= NT2CUDA_OP_ATANH && op <= NT2CUDA_OP_ACSCH))
+  if ((op >= NT2CUDA_OP_CBRT && op <= NT2CUDA_OP_REALLOG) || (op >= NT2CUDA_OP_ATANH && op <= NT2CUDA_OP_SINHC))
     return map_expfam(op, x, y, n, fused, s);
   if (op >= NT2CUDA_OP_CSC && op <= NT2CUDA_OP_SINCPI)
     return map_trigx(op, x, y, n, fused, (flags & NT2CUDA_MAP_SIMD128) != 0, s);

@@ -44,6 +44,8 @@ template <bool F, class T> nt2cuda_status expfam_impl(int op, const T* x, T* y, 
     case NT2CUDA_OP_ACOTH: return run_tree<F>(node<tag::atanh_, node<tag::rec_, term<T>>>{{term<T>{x}}}, y, n, s);
     case NT2CUDA_OP_ASECH: return run_tree<F>(node<tag::acosh_, node<tag::rec_, term<T>>>{{term<T>{x}}}, y, n, s);
     case NT2CUDA_OP_ASINH: return run_unary<F, tag::asinh_>(x, y, n, s);
+    case NT2CUDA_OP_COTH: return run_unary<F, tag::coth_>(x, y, n, s);
+    case NT2CUDA_OP_SINHC: return run_unary<F, tag::sinhc_>(x, y, n, s);
     case NT2CUDA_OP_ACSCH: return run_tree<F>(node<tag::asinh_, node<tag::rec_, term<T>>>{{term<T>{x}}}, y, n, s);
     default: return NT2CUDA_ERR_ARG;
   }

@@ -64,7 +64,7 @@ nt2cuda_status trigx_fwd_scalar(int op, const float* x, float* y, size_t n, bool
 nt2cuda_status trigx_fwd_scalar(int op, const double* x, double* y, size_t n, bool fused, nt2cuda_stream s);
 nt2cuda_status trigx_fwd_simd128(int op, const float* x, float* y, size_t n, bool fused, nt2cuda_stream s);
 nt2cuda_status trigx_fwd_simd128(int op, const double* x, double* y, size_t n, bool fused, nt2cuda_stream s);
-// capi_expfam_f32.cu / capi_expfam_f64.cu: ops NT2CUDA_OP_CBRT..NT2CUDA_OP_REALLOG, NT2CUDA_OP_ATANH..ACSCH
+// capi_expfam_f32.cu / capi_expfam_f64.cu: ops NT2CUDA_OP_CBRT..NT2CUDA_OP_REALLOG, NT2CUDA_OP_ATANH..SINHC
 nt2cuda_status map_expfam(int op, const float* x, float* y, size_t n, bool fused, nt2cuda_stream s);
 nt2cuda_status map_expfam(int op, const double* x, double* y, size_t n, bool fused, nt2cuda_stream s);
 

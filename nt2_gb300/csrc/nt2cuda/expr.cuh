@@ -54,7 +54,7 @@ struct sinh_ {}; struct cosh_ {}; struct tanh_ {};
 struct pow_ {};
 // the rest of NT2's exponential family (expx2s_ is the two-argument expx2)
 struct cbrt_ {}; struct sqrt1pm1_ {}; struct exprecneg_ {}; struct exprecnegc_ {}; struct expx2_ {};
-struct atanh_ {}; struct acosh_ {}; struct asinh_ {}; struct hypot_ {};
+struct atanh_ {}; struct acosh_ {}; struct asinh_ {}; struct hypot_ {}; struct coth_ {}; struct sinhc_ {};
 struct expx2s_ {}; struct pow_abs_ {}; struct logspace_add_ {}; struct logspace_sub_ {};
 // steps of the composed trigonometric functors (csc = rec(sin), asind = indeg(asin), ...)
 struct indeg_ {}; struct inrad_ {}; struct invpi_mul_ {}; struct oneo_180_mul_ {}; struct pio2_minus_ {};
@@ -169,6 +169,8 @@ NT2CUDA_UN(expx2_, math::expx2<F>(a))
 NT2CUDA_UN(atanh_, math::atanh<F>(a))
 NT2CUDA_UN(acosh_, math::acosh<F>(a))
 NT2CUDA_UN(asinh_, math::asinh<F>(a))
+NT2CUDA_UN(coth_, math::coth<F>(a))
+NT2CUDA_UN(sinhc_, math::sinhc<F>(a))
 NT2CUDA_BIN(hypot_, math::hypot(a, (A)b))
 NT2CUDA_UN(unary_minus_, (A)(-a))
 NT2CUDA_UN(sqr_, detail::mul(a, a))

@@ -675,6 +675,56 @@ template <bool F = false> __device__ __forceinline__ double tanh(double a0)
   return bits_xor(r, a0);
 }
 
+// coth and sinhc, NT2's SIMD forms (modules/core/hyperbolic/include/nt2/hyperbolic/functions/
+// simd/common/coth.hpp:32-48, sinhc.hpp:32-56; kernels details/tanh_kernel.hpp:40-58,
+// sinhc_kernel.hpp:25-57); average(a, b) = fma(a, 1/2, b/2); fma(2, r, 1) = 2r + 1.
+template <bool F = false> __device__ __forceinline__ float coth(float a0)
+{
+  constexpr uint32_t P[5] = {0xbbbaf0eau, 0x3ca9134eu, 0xbd5c1e2du, 0x3e088393u, 0xbeaaaa99u};
+  const float x = fabsf(a0), x2 = mul(x, x);
+  const float r = x < 0.625f ? div(1.0f, madd<F>(mul(horner<F>(x2, P), x2), x, x))
+                             : madd<F>(2.0f, div(1.0f, sub(exp<F>(add(x, x)), 1.0f)), 1.0f);
+  return bits_xor(r, a0);
+}
+template <bool F = false> __device__ __forceinline__ double coth(double a0)
+{
+  constexpr uint64_t P[3] = {0xbfeedc5baafd6f4bull, 0xc058d26a0e26682dull, 0xc0993ac030580563ull};
+  constexpr uint64_t Q[4] = {0x3ff0000000000000ull, 0x405c33f28a581b86ull, 0x40a176fa0e5535faull,
+                             0x40b2ec102442040cull};
+  const double x = fabs(a0), x2 = mul(x, x);
+  double r;
+  if (x < 0.625) {
+    const double q = horner<F>(x2, Q);
+    r = div(q, mul(x, madd<F>(horner<F>(x2, P), x2, q)));
+  } else {
+    r = madd<F>(2.0, div(1.0, sub(exp<F>(add(x, x)), 1.0)), 1.0);
+  }
+  return bits_xor(r, a0);
+}
+template <bool F = false, class T> __device__ __forceinline__ T sinhc(T a0)
+{
+  const T x = fabs(a0);
+  T z;
+  if constexpr (sizeof(T) == 4) {
+    constexpr uint32_t P[4] = {0x39559e2fu, 0x3c087bbeu, 0x3e2aaaccu, 0x3f800000u};
+    z = horner<F>(mul(x, x), P);
+  } else {
+    constexpr uint64_t P[4] = {0xbfe9435fe8bb3cd6ull, 0xc064773a398ff4feull, 0xc0c694b8c71d6182ull,
+                               0xc115782bdbf6ab05ull};
+    constexpr uint64_t Q[4] = {0x3ff0000000000000ull, 0xc0715b6096e96484ull, 0x40e1a7ba7ed72245ull,
+                               0xc1401a20e4f90044ull};
+    const T x2 = mul(x, x);
+    z = add(T(1), div(mul(x2, horner<F>(x2, P)), horner<F>(x2, Q)));
+  }
+  if (x < T(1)) return z;
+  const T log_2 = sizeof(T) == 4 ? (T)fbits(0x3f317218u) : (T)dbits(0x3fe62e42fefa39efull);
+  const bool test1 = x > sub(hyp<T>::maxlog(), log_2);
+  const T tmp = exp<F>(mul(x, test1 ? T(0.5) : T(1)));
+  const T tmp1 = div(mul(T(0.5), tmp), x);
+  const T r = test1 ? mul(tmp1, tmp) : div(madd<F>(tmp, T(0.5), mul(-div(T(1), tmp), T(0.5))), x);
+  return x == T(INFINITY) ? x : r;
+}
+
 // ------------------------------------------------------ inverse hyperbolic
 // atanh and acosh, NT2's SIMD forms (modules/core/hyperbolic/include/nt2/hyperbolic/functions/
 // simd/common/atanh.hpp:38-47, acosh.hpp:36-43); NT2's fma(t, tmp, t) is rounded twice in

@@ -716,6 +716,49 @@ EXPORT double nt2o_tanh_d(double a0)
   return db(bd(r) ^ bts);
 }
 
+/* coth and sinhc, NT2's SIMD forms (hyperbolic/functions/simd/common/coth.hpp:32-48,
+ * sinhc.hpp:32-56; kernels details/tanh_kernel.hpp:40-58, sinhc_kernel.hpp:25-57):
+ * coth: |x| < 5/8 -> rec of the tanh kernel (float) or q/(x*(p*x2 + q)) (double), else
+ * 2*rec(exp(2|x|) - 1) + 1; sign of x.  sinhc: |x| < 1 -> the sinh kernel's polynomial
+ * (float) or 1 + x2*p/q (double), else exp-based as sinh, divided by |x|. */
+EXPORT float nt2o_coth_f(float a0)
+{
+  const float x = fabsf(a0), x2 = x * x;
+  const float z = 1.0f / ((horner_f(x2, TANH_F_P, 5) * x2) * x + x);
+  const float r = 2.0f * (1.0f / (nt2o_exp_f(x + x) - 1.0f)) + 1.0f;
+  return fb(bf(x < 0.625f ? z : r) ^ (bf(a0) & 0x80000000u));
+}
+EXPORT double nt2o_coth_d(double a0)
+{
+  const double x = fabs(a0), x2 = x * x;
+  const double q = horner_d(x2, TANH_D_Q, 4);
+  const double z = q / (x * (horner_d(x2, TANH_D_P, 3) * x2 + q));
+  const double r = 2.0 * (1.0 / (nt2o_exp_d(x + x) - 1.0)) + 1.0;
+  return db(bd(x < 0.625 ? z : r) ^ (bd(a0) & 0x8000000000000000ull));
+}
+EXPORT float nt2o_sinhc_f(float a0)
+{
+  const float x = fabsf(a0);
+  const float z = horner_f(x * x, SINH_F_P, 4);
+  const int test1 = x > MAXLOG_F - LOG_2_F;
+  const float tmp = nt2o_exp_f(x * (test1 ? 0.5f : 1.0f));
+  const float tmp1 = (0.5f * tmp) / x;
+  float r = test1 ? tmp1 * tmp : (tmp * 0.5f + (-(1.0f / tmp)) * 0.5f) / x;
+  r = x == INFINITY ? x : r;
+  return x < 1.0f ? z : r;
+}
+EXPORT double nt2o_sinhc_d(double a0)
+{
+  const double x = fabs(a0), x2 = x * x;
+  const double z = 1.0 + x2 * horner_d(x2, SINH_D_P, 4) / horner_d(x2, SINH_D_Q, 4);
+  const int test1 = x > MAXLOG_D - LOG_2_D;
+  const double tmp = nt2o_exp_d(x * (test1 ? 0.5 : 1.0));
+  const double tmp1 = (0.5 * tmp) / x;
+  double r = test1 ? tmp1 * tmp : (tmp * 0.5 + (-(1.0 / tmp)) * 0.5) / x;
+  r = x == INFINITY ? x : r;
+  return x < 1.0 ? z : r;
+}
+
 /* ------------------------------------------------ inverse hyperbolic -- */
 /* atanh and acosh, NT2's SIMD forms (modules/core/hyperbolic/include/nt2/hyperbolic/functions/
  * simd/common/atanh.hpp:38-47, acosh.hpp:36-43); seladd(c, a, b) = a + (c ? b : 0).
@@ -1235,7 +1278,7 @@ enum { OP_EXP = 0, OP_LOG = 1, OP_ERFC = 2, OP_NORMCDF = 3, OP_FASTNORMCDF = 4, 
        OP_ERFC_SCALAR = 6, OP_EXP2 = 7, OP_EXP10 = 8, OP_LOG2 = 9, OP_LOG10 = 10, OP_EXPM1 = 11,
        OP_LOG1P = 12, OP_SINH = 13, OP_COSH = 14, OP_TANH = 15, OP_CBRT = 16, OP_SQRT1PM1 = 17,
        OP_EXPRECNEG = 18, OP_EXPRECNEGC = 19, OP_EXPX2 = 20, OP_ATANH = 21, OP_ACOSH = 22, OP_SECH = 23,
-       OP_CSCH = 24, OP_ACOTH = 25, OP_ASECH = 26, OP_ASINH = 27, OP_ACSCH = 28 };
+       OP_CSCH = 24, OP_ACOTH = 25, OP_ASECH = 26, OP_ASINH = 27, OP_ACSCH = 28, OP_COTH = 29, OP_SINHC = 30 };
 
 EXPORT int nt2o_map_f(int op, const float* x, float* y, size_t n)
 {
@@ -1270,6 +1313,8 @@ EXPORT int nt2o_map_f(int op, const float* x, float* y, size_t n)
       case OP_ACOTH: y[i] = nt2o_atanh_f((float)1 / a); break;
       case OP_ASECH: y[i] = nt2o_acosh_f((float)1 / a); break;
       case OP_ASINH: y[i] = nt2o_asinh_f(a); break;
+      case OP_COTH: y[i] = nt2o_coth_f(a); break;
+      case OP_SINHC: y[i] = nt2o_sinhc_f(a); break;
       case OP_ACSCH: y[i] = nt2o_asinh_f((float)1 / a); break;
       default: return 1;
     }
@@ -1309,6 +1354,8 @@ EXPORT int nt2o_map_d(int op, const double* x, double* y, size_t n)
       case OP_ACOTH: y[i] = nt2o_atanh_d((double)1 / a); break;
       case OP_ASECH: y[i] = nt2o_acosh_d((double)1 / a); break;
       case OP_ASINH: y[i] = nt2o_asinh_d(a); break;
+      case OP_COTH: y[i] = nt2o_coth_d(a); break;
+      case OP_SINHC: y[i] = nt2o_sinhc_d(a); break;
       case OP_ACSCH: y[i] = nt2o_asinh_d((double)1 / a); break;
       default: return 1;
     }

@@ -101,7 +101,7 @@ OP = {"exp": 0, "log": 1, "erfc": 2, "normcdf": 3, "fastnormcdf": 4, "sqrt": 5, 
       "exp2": 7, "exp10": 8, "log2": 9, "log10": 10, "expm1": 11, "log1p": 12, "sinh": 13, "cosh": 14,
       "tanh": 15, "cbrt": 16, "sqrt1pm1": 17, "exprecneg": 18, "exprecnegc": 19, "expx2": 20,
       "realsqrt": 5, "reallog": 1, "atanh": 21, "acosh": 22, "sech": 23, "csch": 24, "acoth": 25, "asech": 26,
-      "asinh": 27, "acsch": 28}
+      "asinh": 27, "acsch": 28, "coth": 29, "sinhc": 30}
 # binary functors of nt2o_map2_f/d
 OP2 = {"atan2": 0, "pow": 1, "pow_abs": 2, "realpow": 3, "logspace_add": 4, "logspace_sub": 5, "expx2": 6, "atan2d": 7,
        "nbd_atan2": 8, "hypot": 9}

@@ -13,7 +13,7 @@ import torch
 pytestmark = pytest.mark.gpu
 
 UNARY = ["cbrt", "sqrt1pm1", "exprecneg", "exprecnegc", "expx2", "realsqrt", "reallog", "atanh", "acosh", "sech",
-         "csch", "acoth", "asech", "asinh", "acsch"]
+         "csch", "acoth", "asech", "asinh", "acsch", "coth", "sinhc"]
 BINARY = ["atan2", "pow", "pow_abs", "realpow", "logspace_add", "logspace_sub", "expx2", "atan2d", "nbd_atan2", "hypot"]
 SPECIALS = [0.0, -0.0, 1.0, -1.0, 0.5, -0.5, 8.0, -27.0, np.inf, -np.inf, np.nan, 1e-40, -1e-40, 88.7, 9.5]
 # fused mode against the exact oracle, ulpdist units, on [-10, 10] (measured maxima: 2, 0, 2, 4, 2 and
@@ -21,7 +21,7 @@ SPECIALS = [0.0, -0.0, 1.0, -1.0, 0.5, -0.5, 8.0, -27.0, np.inf, -np.inf, np.nan
 # eps of max(|a0|, |a1|, 1)) because they cancel where their result is near zero
 FUSED_BOUND = {"cbrt": 2.0, "sqrt1pm1": 0.0, "exprecneg": 2.0, "exprecnegc": 4.0, "expx2": 2.0,
                "realsqrt": 0.0, "reallog": 1.0, "atanh": 4.0, "acosh": 4.0, "sech": 4.0, "csch": 4.0, "acoth": 4.0,
-               "asech": 4.0, "asinh": 4.0, "acsch": 4.0}
+               "asech": 4.0, "asinh": 4.0, "acsch": 4.0, "coth": 4.0, "sinhc": 4.0}
 FUSED_BOUND2 = {"pow_abs": 2.0, "realpow": 2.0, "pow": 2.0, "expx2": 4.0, "atan2": 2.0, "atan2d": 4.0, "nbd_atan2": 2.0, "hypot": 0.0}
 
 

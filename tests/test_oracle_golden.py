@@ -758,3 +758,23 @@ def test_asinh_acsch_hypot(oracle, dt):
                      for p, q in zip(a, b)]).astype(dt)
     m, w = oracle.max_ulp(oracle.map2("hypot", a, b), want)
     assert m <= 2.0, ("hypot", dt, m, a[w], b[w])
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_coth_sinhc(oracle, dt):
+    """coth, sinhc: modules/core/hyperbolic/unit/scalar/{coth,sinhc}.cpp (specials, 0.5 ulp) and
+    cover/scalar/{coth,sinhc}.cpp-style accuracy (mpmath at 40 digits, within 2 ulps)."""
+    mpmath = pytest.importorskip("mpmath")
+    mpmath.mp.dps = 40
+    L = oracle.load()
+    u = ulp_f if dt == np.float32 else ulp_d
+    for fn, x, r in (("coth", INF, 1.0), ("coth", -INF, -1.0), ("coth", NAN, NAN), ("coth", -0.0, -INF),
+                     ("coth", 0.0, INF), ("sinhc", INF, INF), ("sinhc", -INF, INF), ("sinhc", NAN, NAN),
+                     ("sinhc", 0.0, 1.0)):
+        assert u(L, float(oracle.map_(fn, np.array([x], dt))[0]), float(dt(r))) <= 0.5, (fn, dt, x)
+    x = np.random.default_rng(53).uniform(-10, 10, 3000).astype(dt)
+    x = x[x != 0]
+    for fn, mf in (("coth", mpmath.coth), ("sinhc", lambda v: mpmath.sinh(v) / v)):
+        want = np.array([float(mf(mpmath.mpf(float(v)))) for v in x]).astype(dt)
+        m, w = oracle.max_ulp(oracle.map_(fn, x), want)
+        assert m <= 2.0, (fn, dt, m, x[w])
