@@ -215,9 +215,11 @@ enum {
   NT2CUDA_SINCOSD = 2,
   NT2CUDA_FAST_SINCOS = 3,
   NT2CUDA_FAST_SINCOSPI = 4,
-  NT2CUDA_FAST_SINCOSD = 5
+  NT2CUDA_FAST_SINCOSD = 5,
+  NT2CUDA_SINHCOSH = 6        /* tie(s, c) = sinhcosh(x): modules/core/hyperbolic/.../simd/common/sinhcosh.hpp,
+                               * the steps of sinh and cosh, so equal to them bit for bit */
 };
-/* tie(s, c) = sincos(x) (or the form's variant) in one pass over x.  flags: NT2CUDA_MAP_FUSED,
+/* tie(s, c) = sincos(x) (or the form's variant; sinhcosh for NT2CUDA_SINHCOSH) in one pass over x.  flags: NT2CUDA_MAP_FUSED,
  * NT2CUDA_MAP_SIMD128 (the reduction of the three full forms, as for sin and cos). */
 nt2cuda_status nt2cuda_sincos_f32(int form, const float* x, float* s, float* c, size_t n, int flags,
                                   nt2cuda_stream stream);

@@ -112,12 +112,14 @@ def map2(op: str, a0: torch.Tensor, a1: torch.Tensor, out: torch.Tensor | None =
     return out
 
 
-SINCOS = {"sincos": 0, "sincospi": 1, "sincosd": 2, "fast_sincos": 3, "fast_sincospi": 4, "fast_sincosd": 5}
+SINCOS = {"sincos": 0, "sincospi": 1, "sincosd": 2, "fast_sincos": 3, "fast_sincospi": 4, "fast_sincosd": 5,
+          "sinhcosh": 6}
 
 
 def sincos(x: torch.Tensor, form: str = "sincos", s: torch.Tensor | None = None, c: torch.Tensor | None = None,
            fused: bool = False, simd128: bool = False) -> tuple[torch.Tensor, torch.Tensor]:
-    """tie(s, c) = nt2::sincos(x) (or sincospi, sincosd, fast_sincos, fast_sincospi, fast_sincosd) in one pass."""
+    """tie(s, c) = nt2::sincos(x) (or sincospi, sincosd, fast_sincos, fast_sincospi, fast_sincosd, sinhcosh) in one
+    pass."""
     s = torch.empty_like(x) if s is None else s
     c = torch.empty_like(x) if c is None else c
     flags = (MAP_FUSED if fused else 0) | (MAP_SIMD128 if simd128 else 0)

@@ -18,7 +18,7 @@ extern "C" nt2cuda_status nt2cuda_sincos_f64(int form, const double* x, double* 
   NT2CUDA_NVTX_RANGE;
   if (n && (!x || !s || !c)) return NT2CUDA_ERR_ARG;
   if (flags & ~(NT2CUDA_MAP_FUSED | NT2CUDA_MAP_SIMD128)) return NT2CUDA_ERR_ARG;
-  if (form < NT2CUDA_SINCOS || form > NT2CUDA_FAST_SINCOSD) return NT2CUDA_ERR_ARG;
+  if (form < NT2CUDA_SINCOS || form > NT2CUDA_SINHCOSH) return NT2CUDA_ERR_ARG;
   if (n == 0) return NT2CUDA_OK;
   return nt2cuda::detail_capi::sincos_dispatch(form, x, s, c, n, (flags & NT2CUDA_MAP_FUSED) != 0,
                                                (flags & NT2CUDA_MAP_SIMD128) != 0, stream);

@@ -127,6 +127,7 @@ template <bool F, class T> nt2cuda_status fast_sincos_impl(int form, const T* x,
     case NT2CUDA_FAST_SINCOS: return run_pair<F>(nd<tag::fast_<0, 0>>(X), nd<tag::fast_<1, 0>>(X), so, co, n, s);
     case NT2CUDA_FAST_SINCOSPI: return run_pair<F>(nd<tag::fast_<0, 1>>(X), nd<tag::fast_<1, 1>>(X), so, co, n, s);
     case NT2CUDA_FAST_SINCOSD: return run_pair<F>(nd<tag::fast_<0, 2>>(X), nd<tag::fast_<1, 2>>(X), so, co, n, s);
+    case NT2CUDA_SINHCOSH: return run_pair<F>(nd<tag::sinh_>(X), nd<tag::cosh_>(X), so, co, n, s);
     default: return NT2CUDA_ERR_ARG;
   }
 }
