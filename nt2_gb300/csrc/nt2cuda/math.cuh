@@ -759,16 +759,18 @@ template <bool F = false, class T> __device__ __forceinline__ T acosh(T a0)
 // The tables are 2^(-i/16) rounded to the type (A) and, for even i, the rounding residual
 // 2^(-i/16) - A[i] (B, indexed by i/2); they are read through the L1 (a warp's indices fall
 // in one or two 128-byte lines).
-static __device__ const uint32_t kPowAf[17] = {
-    0x3f800000u, 0x3f75257du, 0x3f6ac0c7u, 0x3f60ccdfu, 0x3f5744fdu, 0x3f4e248cu, 0x3f45672au, 0x3f3d08a4u, 0x3f3504f3u,
-    0x3f2d583fu, 0x3f25fed7u, 0x3f1ef532u, 0x3f1837f0u, 0x3f11c3d3u, 0x3f0b95c2u, 0x3f05aac3u, 0x3f000000u};
+#define NT2CUDA_POW_AF                                                                                          \
+  0x3f800000u, 0x3f75257du, 0x3f6ac0c7u, 0x3f60ccdfu, 0x3f5744fdu, 0x3f4e248cu, 0x3f45672au, 0x3f3d08a4u, 0x3f3504f3u, \
+      0x3f2d583fu, 0x3f25fed7u, 0x3f1ef532u, 0x3f1837f0u, 0x3f11c3d3u, 0x3f0b95c2u, 0x3f05aac3u, 0x3f000000u
+#define NT2CUDA_POW_AD                                                                                          \
+  0x3ff0000000000000ull, 0x3feea4afa2a490daull, 0x3fed5818dcfba487ull, 0x3fec199bdd85529cull, 0x3feae89f995ad3adull, \
+      0x3fe9c49182a3f090ull, 0x3fe8ace5422aa0dbull, 0x3fe7a11473eb0187ull, 0x3fe6a09e667f3bcdull,                 \
+      0x3fe5ab07dd485429ull, 0x3fe4bfdad5362a27ull, 0x3fe3dea64c123422ull, 0x3fe306fe0a31b715ull,                 \
+      0x3fe2387a6e756238ull, 0x3fe172b83c7d517bull, 0x3fe0b5586cf9890full, 0x3fe0000000000000ull
+static __device__ const uint32_t kPowAf[17] = {NT2CUDA_POW_AF};
 static __device__ const uint32_t kPowBf[9] = {0x00000000u, 0xb1c116deu, 0xb254a58au, 0x318aa837u, 0x324fe77au,
                                               0xb2ac9d5eu, 0x32a31b71u, 0xb1e0aba1u, 0x00000000u};
-static __device__ const uint64_t kPowAd[17] = {
-    0x3ff0000000000000ull, 0x3feea4afa2a490daull, 0x3fed5818dcfba487ull, 0x3fec199bdd85529cull, 0x3feae89f995ad3adull,
-    0x3fe9c49182a3f090ull, 0x3fe8ace5422aa0dbull, 0x3fe7a11473eb0187ull, 0x3fe6a09e667f3bcdull, 0x3fe5ab07dd485429ull,
-    0x3fe4bfdad5362a27ull, 0x3fe3dea64c123422ull, 0x3fe306fe0a31b715ull, 0x3fe2387a6e756238ull, 0x3fe172b83c7d517bull,
-    0x3fe0b5586cf9890full, 0x3fe0000000000000ull};
+static __device__ const uint64_t kPowAd[17] = {NT2CUDA_POW_AD};
 static __device__ const uint64_t kPowBd[9] = {0x0000000000000000ull, 0x3c72ed02d75b3707ull, 0x3c87a1cd345dcc81ull,
                                               0x3c86e9f156864b27ull, 0xbc8bdd3413b26456ull, 0x3c6d4397afec42e2ull,
                                               0x3c76f46ad23182e4ull, 0xbc719041b9d78a76ull, 0x0000000000000000ull};
@@ -835,13 +837,27 @@ template <class T> __device__ __forceinline__ T pow_reduc(T x) { return mul(T(0.
 
 // pow_kernel::select: i in 0..16 from x in [0.5, 1); x <- (x - A[i] - B[i/2]) / A[i].  The
 // indices it reads are 9, 13, 3..15 (odd), 1 and i itself, all inside the table.
+template <class T> __device__ __forceinline__ T pow_ac(int i);  // A[i] for a constant i
+template <> __device__ __forceinline__ float pow_ac<float>(int i)
+{
+  constexpr uint32_t A[17] = {NT2CUDA_POW_AF};
+  return __uint_as_float(A[i]);
+}
+template <> __device__ __forceinline__ double pow_ac<double>(int i)
+{
+  constexpr uint64_t A[17] = {NT2CUDA_POW_AD};
+  return __longlong_as_double((long long)A[i]);
+}
 template <class T> __device__ __forceinline__ int pow_select(T& x)
 {
+  // The search compares x with A[9], then A[5] or A[13], then one of A[3], A[7],
+  // A[11], A[15], then A[1]: values picked from constants instead of table reads.
   int i = 1;
-  i = (x <= pow_a(x, 9)) ? 9 : i;
-  i = (x <= pow_a(x, i + 4)) ? i + 4 : i;
-  i = (x <= pow_a(x, i + 2)) ? i + 2 : i;
-  i = (x >= pow_a(x, 1)) ? -1 : i;
+  i = (x <= pow_ac<T>(9)) ? 9 : i;
+  i = (x <= (i == 9 ? pow_ac<T>(13) : pow_ac<T>(5))) ? i + 4 : i;
+  const T a2 = i == 1 ? pow_ac<T>(3) : (i == 5 ? pow_ac<T>(7) : (i == 9 ? pow_ac<T>(11) : pow_ac<T>(15)));
+  i = (x <= a2) ? i + 2 : i;
+  i = (x >= pow_ac<T>(1)) ? -1 : i;
   i = i + 1;
   const T tmp = pow_a(x, i);
   x = sub(x, tmp);
