@@ -186,7 +186,8 @@ enum {
   NT2CUDA_OP_ASINH = 76,      /* simd/common/asinh.hpp (double and float forms differ) */
   NT2CUDA_OP_ACSCH = 77,      /* asinh(rec(x)) */
   NT2CUDA_OP_COTH = 78,       /* simd/common/coth.hpp */
-  NT2CUDA_OP_SINHC = 79       /* simd/common/sinhc.hpp: sinh(x)/x */
+  NT2CUDA_OP_SINHC = 79,      /* simd/common/sinhc.hpp: sinh(x)/x */
+  NT2CUDA_OP_PROPER_TANPI = 80  /* modules/core/trigonometric/.../simd/common/proper_tanpi.hpp */
 };
 
 /* out = atan2(a0, a1) elementwise (NT2's SIMD form,

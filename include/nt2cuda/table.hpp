@@ -412,6 +412,7 @@ NT2CUDA_COMPOSED(fast_sind, (make_unary<tag::fast_<0, 2>>(a)))
 NT2CUDA_COMPOSED(fast_cosd, (make_unary<tag::fast_<1, 2>>(a)))
 NT2CUDA_COMPOSED(fast_tand, (make_unary<tag::fast_<2, 2>>(a)))
 NT2CUDA_COMPOSED(fast_cotd, (make_unary<tag::fast_<3, 2>>(a)))
+NT2CUDA_COMPOSED(proper_tanpi, make_unary<tag::proper_tanpi_>(a))
 #undef NT2CUDA_COMPOSED
 
 #define NT2CUDA_FN3(NAME, TAG)                                                          \

@@ -23,7 +23,7 @@ OPS = {"exp": 0, "log": 1, "erfc": 2, "normcdf": 3, "fastnormcdf": 4, "sqrt": 5,
        "cot": 48, "tanpi": 49, "cotpi": 50, "sind": 51, "cosd": 52, "tand": 53, "cotd": 54, "secd": 55,
        "fast_sin": 56, "fast_cos": 57, "fast_tan": 58, "fast_cot": 59, "fast_sinpi": 60, "fast_cospi": 61,
        "fast_tanpi": 62, "fast_cotpi": 63, "fast_sind": 64, "fast_cosd": 65, "fast_tand": 66, "fast_cotd": 67,
-       "sinc": 68, "sincpi": 69, "atanh": 70, "acosh": 71, "sech": 72, "csch": 73, "acoth": 74, "asech": 75, "asinh": 76, "acsch": 77, "coth": 78, "sinhc": 79}
+       "sinc": 68, "sincpi": 69, "atanh": 70, "acosh": 71, "sech": 72, "csch": 73, "acoth": 74, "asech": 75, "asinh": 76, "acsch": 77, "coth": 78, "sinhc": 79, "proper_tanpi": 80}
 # binary functors of nt2cuda_map2_f32/f64
 OPS2 = {"atan2": 0, "pow": 1, "pow_abs": 2, "realpow": 3, "logspace_add": 4, "logspace_sub": 5, "expx2": 6,
         "atan2d": 7, "nbd_atan2": 8, "hypot": 9}
@@ -58,7 +58,7 @@ def map_(op: str, x: torch.Tensor, out: torch.Tensor | None = None, fused: bool 
     expx2, realsqrt, reallog and the composed trigonometric ops (csc, sec, cscpi, secpi, cscd, indeg, inrad,
     acot, asind, acosd, atand, asinpi, acospi, atanpi, acsc, acscd, asec, asecd), cot, tanpi, cotpi and the degree
     forms sind, cosd, tand, cotd, secd, the fast_ forms (fast_sin ... fast_cotd), sinc, sincpi, and atanh, acosh,
-    sech, csch, acoth, asech, asinh, acsch, coth, sinhc.  The
+    sech, csch, acoth, asech, asinh, acsch, coth, sinhc, proper_tanpi.  The
     trigonometric ops reduce each
     element on its own (NT2's scalar
     code); with simd128 they reduce each 16-byte pack of x with the method NT2's 128-bit SIMD code picks for

@@ -266,7 +266,7 @@ nt2cuda_status nt2cuda_map_f32(int op, const float* x, float* y, size_t n, int f
     return map_trig(op, x, y, n, fused, (flags & NT2CUDA_MAP_SIMD128) != 0, s);
   if ((op >= NT2CUDA_OP_CBRT && op <= NT2CUDA_OP_REALLOG) || (op >= NT2CUDA_OP_ATANH && op <= NT2CUDA_OP_SINHC))
     return map_expfam(op, x, y, n, fused, s);
-  if (op >= NT2CUDA_OP_CSC && op <= NT2CUDA_OP_SINCPI)
+  if ((op >= NT2CUDA_OP_CSC && op <= NT2CUDA_OP_SINCPI) || op == NT2CUDA_OP_PROPER_TANPI)
     return map_trigx(op, x, y, n, fused, (flags & NT2CUDA_MAP_SIMD128) != 0, s);
   return fused ? map_impl<true>(op, x, y, n, s) : map_impl<false>(op, x, y, n, s);
 }
@@ -281,7 +281,7 @@ nt2cuda_status nt2cuda_map_f64(int op, const double* x, double* y, size_t n, int
     return map_trig(op, x, y, n, fused, (flags & NT2CUDA_MAP_SIMD128) != 0, s);
   if ((op >= NT2CUDA_OP_CBRT && op <= NT2CUDA_OP_REALLOG) || (op >= NT2CUDA_OP_ATANH && op <= NT2CUDA_OP_SINHC))
     return map_expfam(op, x, y, n, fused, s);
-  if (op >= NT2CUDA_OP_CSC && op <= NT2CUDA_OP_SINCPI)
+  if ((op >= NT2CUDA_OP_CSC && op <= NT2CUDA_OP_SINCPI) || op == NT2CUDA_OP_PROPER_TANPI)
     return map_trigx(op, x, y, n, fused, (flags & NT2CUDA_MAP_SIMD128) != 0, s);
   return fused ? map_impl<true>(op, x, y, n, s) : map_impl<false>(op, x, y, n, s);
 }

@@ -59,7 +59,7 @@ struct expx2s_ {}; struct pow_abs_ {}; struct logspace_add_ {}; struct logspace_
 // steps of the composed trigonometric functors (csc = rec(sin), asind = indeg(asin), ...)
 struct indeg_ {}; struct inrad_ {}; struct invpi_mul_ {}; struct oneo_180_mul_ {}; struct pio2_minus_ {};
 struct cscpi_nan_ {}; struct secpi_nan_ {}; struct nan_if_zero_ {}; struct sinc_fix_ {};
-struct atan2d_ {}; struct nbd_atan2_ {};
+struct atan2d_ {}; struct nbd_atan2_ {}; struct proper_tanpi_ {};
 // fast_sin ... fast_cotd: K 0 sin, 1 cos, 2 tan, 3 cot; U 0 radian, 1 pi, 2 degree
 template <int K, int U> struct fast_ {};
 }  // namespace tag
@@ -159,6 +159,7 @@ NT2CUDA_UN(nan_if_zero_, (a == (A)0 ? (A)NAN : a))
 NT2CUDA_BIN(sinc_fix_, trig::sinc_fix(a, (A)b))
 NT2CUDA_BIN(atan2d_, trig::indeg(trig::atan2<F>(a, (A)b)))
 NT2CUDA_BIN(nbd_atan2_, trig::nbd_atan2<F>(a, (A)b))
+NT2CUDA_UN(proper_tanpi_, trig::proper_tanpi<F>(a))
 template <int K, int U, bool F> struct fn<tag::fast_<K, U>, F> {
   template <class A> __device__ __forceinline__ static auto apply(A a) { return trig::fast<K, U, F>(a); }
 };

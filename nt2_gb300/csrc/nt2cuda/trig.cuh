@@ -861,6 +861,16 @@ template <int K, int U, bool F, class T> __device__ __forceinline__ T fast(T a0)
   else if constexpr (K == 2) return tan_eval<F>(x);
   else return math::div(T(1), tan_eval<F>(x));
 }
+// proper_tanpi (simd/common/proper_tanpi.hpp:33-43): fast_tanpi of |x| (|x| <= 1/4) or of
+// 1/2 - |x| and its reciprocal, the sign of x, NaN unless |x| <= 1/2
+template <bool F, class T> __device__ __forceinline__ T proper_tanpi(T a0)
+{
+  const T ax = fabs(a0);
+  const bool test = ax <= T(0.25);
+  T t = fast<2, 1, F>(test ? ax : math::sub(T(0.5), ax));
+  t = a0 < T(0) ? -t : t;
+  return !(ax <= T(0.5)) ? T(NAN) : (test ? t : math::div(T(1), t));
+}
 // sinc / sincpi final steps (simd/common/sinc.hpp:33-45, sincpi.hpp:33-45): 1 where
 // |x| < Eps, 0 where x is infinite, else the quotient r computed beside it
 template <class T> __device__ __forceinline__ T sinc_fix(T x, T r)

@@ -93,6 +93,7 @@ template <bool F, class T> nt2cuda_status inv_impl(int op, const T* x, T* y, siz
     case NT2CUDA_OP_FAST_COSD: return run_e<F>(nd<tag::fast_<1, 2>>(X), y, n, s);
     case NT2CUDA_OP_FAST_TAND: return run_e<F>(nd<tag::fast_<2, 2>>(X), y, n, s);
     case NT2CUDA_OP_FAST_COTD: return run_e<F>(nd<tag::fast_<3, 2>>(X), y, n, s);
+    case NT2CUDA_OP_PROPER_TANPI: return run_e<F>(nd<tag::proper_tanpi_>(X), y, n, s);
     default: return NT2CUDA_ERR_ARG;
   }
 }
@@ -146,7 +147,7 @@ template <class T> nt2cuda_status trigx_dispatch(int op, const T* x, T* y, size_
                                                  nt2cuda_stream s)
 {
   const bool packless = (op >= NT2CUDA_OP_INDEG && op <= NT2CUDA_OP_ASECD) ||
-                        (op >= NT2CUDA_OP_FAST_SIN && op <= NT2CUDA_OP_FAST_COTD);
+                        (op >= NT2CUDA_OP_FAST_SIN && op <= NT2CUDA_OP_FAST_COTD) || op == NT2CUDA_OP_PROPER_TANPI;
   if (packless) return fused ? inv_impl<true>(op, x, y, n, s) : inv_impl<false>(op, x, y, n, s);
   return simd ? trigx_fwd_simd128(op, x, y, n, fused, s) : trigx_fwd_scalar(op, x, y, n, fused, s);
 }

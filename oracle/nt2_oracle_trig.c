@@ -840,6 +840,24 @@ static double fast_d(int kind, int unit, double a0)
   if (kind == 1) return cos_eval_d(x * x);
   return kind == 2 ? tan_eval_d(x) : 1.0 / tan_eval_d(x);
 }
+/* proper_tanpi (simd/common/proper_tanpi.hpp:33-43): fast_tanpi of |x| or of 1/2 - |x|, the
+ * sign of x, the reciprocal in the second case, NaN unless |x| <= 1/2. */
+static float proper_tanpi_f(float a0)
+{
+  const float ax = fabsf(a0);
+  const int test = ax <= 0.25f;
+  float t = fast_f(2, 1, test ? ax : 0.5f - ax);
+  t = a0 < 0.0f ? -t : t;
+  return !(ax <= 0.5f) ? NAN : (test ? t : 1.0f / t);
+}
+static double proper_tanpi_d(double a0)
+{
+  const double ax = fabs(a0);
+  const int test = ax <= 0.25;
+  double t = fast_d(2, 1, test ? ax : 0.5 - ax);
+  t = a0 < 0.0 ? -t : t;
+  return !(ax <= 0.5) ? NAN : (test ? t : 1.0 / t);
+}
 /* nbd_atan2 (simd/common/nbd_atan2.hpp:35-42): atan2 without the infinity and NaN cases;
  * atan2d = indeg(atan2) (generic/atan2d.hpp). op 0 atan2d, 1 nbd_atan2. */
 static float nbd_atan2_f(float a0, float a1)
@@ -889,12 +907,13 @@ EXPORT void nt2o_atan2x_d(int op, const double* a0, const double* a1, double* y,
  *   19-30 fast_sin, fast_cos, fast_tan, fast_cot, then the pi and the degree forms (fast_f)
  *   31 sinc = sin(x)/x, 32 sincpi = Invpi * (sinpi(x)/x): 1 for |x| < Eps, 0 for infinite x
  *      (simd/common/sinc.hpp:33-45, sincpi.hpp:33-45)
+ *   33 proper_tanpi
  * rec is the IEEE quotient 1/x; the sin/cos based ones use the pack form of the
  * functors above (`pack` lanes). */
 static int flint_f(float x) { return isfinite(x) && (x - truncf(x)) == 0.0f; }
 static int flint_d(double x) { return isfinite(x) && (x - trunc(x)) == 0.0; }
 #define TRIGX_BODY(T, SFX, FLINT, RADINDEG, RADINDEGR, DEGINRAD, INVPI, ONEO_180, PIO_2, FABS, EPS)     \
-  if (op < 0 || op > 32) return 1;                                                                      \
+  if (op < 0 || op > 33) return 1;                                                                      \
   T* t = (T*)malloc((n ? n : 1) * sizeof(T));                                                          \
   if (!t) return 1;                                                                                     \
   int st = 0;                                                                                           \
@@ -912,6 +931,7 @@ static int flint_d(double x) { return isfinite(x) && (x - trunc(x)) == 0.0; }
       st = nt2o_trig_##SFX(TRIG_COSPI, x, y, n, pack);                                                  \
       for (size_t i = 0; i < n; ++i) y[i] = FLINT(((x[i] * 2) - 1) * (T)0.5) ? (T)NAN : (T)1 / y[i];   \
       break;                                                                                            \
+    case 33: for (size_t i = 0; i < n; ++i) y[i] = proper_tanpi_##SFX(x[i]); break;                   \
     case 31: case 32:                                                                                   \
       st = nt2o_trig_##SFX(op == 31 ? TRIG_SIN : TRIG_SINPI, x, y, n, pack);                            \
       for (size_t i = 0; i < n; ++i) {                                                                  \

@@ -150,7 +150,7 @@ TRIGX = {"csc": 0, "sec": 1, "cscpi": 2, "secpi": 3, "cscd": 4, "indeg": 5, "inr
          "acosd": 9, "atand": 10, "asinpi": 11, "acospi": 12, "atanpi": 13, "acsc": 14, "acscd": 15, "asec": 16,
          "asecd": 17, "secd": 18, "fast_sin": 19, "fast_cos": 20, "fast_tan": 21, "fast_cot": 22, "fast_sinpi": 23,
          "fast_cospi": 24, "fast_tanpi": 25, "fast_cotpi": 26, "fast_sind": 27, "fast_cosd": 28, "fast_tand": 29,
-         "fast_cotd": 30, "sinc": 31, "sincpi": 32}
+         "fast_cotd": 30, "sinc": 31, "sincpi": 32, "proper_tanpi": 33}
 
 
 def trigx(op: str, x: np.ndarray, pack: int = 1) -> np.ndarray:

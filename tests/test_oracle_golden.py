@@ -778,3 +778,14 @@ def test_coth_sinhc(oracle, dt):
         want = np.array([float(mf(mpmath.mpf(float(v)))) for v in x]).astype(dt)
         m, w = oracle.max_ulp(oracle.map_(fn, x), want)
         assert m <= 2.0, (fn, dt, m, x[w])
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_proper_tanpi_special_values(oracle, dt):
+    """modules/core/trigonometric/unit/scalar/proper_tanpi.cpp (0.5 ulp; +-1/4 within 1)."""
+    L = oracle.load()
+    u = ulp_f if dt == np.float32 else ulp_d
+    for x, r, b in ((0.5, INF, .5), (INF, NAN, .5), (-0.5, -INF, .5), (-INF, NAN, .5), (-1.0, NAN, .5),
+                    (NAN, NAN, .5), (1.0, NAN, .5), (-0.25, -1.0, 1.), (0.25, 1.0, 1.)):
+        got = oracle.trigx("proper_tanpi", np.array([x], dt))[0]
+        assert u(L, float(got), float(dt(r))) <= b, (dt, x, got)

@@ -15,7 +15,7 @@ pytestmark = pytest.mark.gpu
 FORWARD = ["csc", "sec", "cscpi", "secpi", "cscd", "cot", "tanpi", "cotpi", "sind", "cosd", "tand", "cotd", "secd",
            "sinc", "sincpi"]
 FAST = ["fast_sin", "fast_cos", "fast_tan", "fast_cot", "fast_sinpi", "fast_cospi", "fast_tanpi", "fast_cotpi",
-        "fast_sind", "fast_cosd", "fast_tand", "fast_cotd"]
+        "fast_sind", "fast_cosd", "fast_tand", "fast_cotd", "proper_tanpi"]
 INVERSE = ["indeg", "inrad", "acot", "asind", "acosd", "atand", "asinpi", "acospi", "atanpi", "acsc", "acscd",
            "asec", "asecd"]
 SPECIALS = [0.0, -0.0, 1.0, -1.0, 0.5, -0.5, 2.0, 0.25, np.inf, -np.inf, np.nan, 180.0, -90.0, 45.0, 1e-30]
@@ -55,7 +55,7 @@ def inputs(op, n, dtype, seed):
             x[1::4] = np.round(x[1::4] / 45) * 45
     elif op in FAST:
         # the fast forms' range and a margin beyond it (NaN there)
-        r = 45.0 if op.endswith("d") else (0.25 if "pi" in op else 0.7854)
+        r = 45.0 if op.endswith("d") else (0.5 if op == "proper_tanpi" else (0.25 if "pi" in op else 0.7854))
         x = rng.uniform(0, 1.2 * r, n)
     elif op in ("acsc", "acscd", "asec", "asecd", "acot"):
         x = np.exp(rng.uniform(-5, 8, n))
