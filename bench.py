@@ -519,6 +519,19 @@ def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: in
                         api.map_(op, x, out=y, simd128=simd)
                     ms, _, _ = time_device(trig_step, K(100), warmup, ws)
                     out.append(line(label, ms, 2 * n * xs[0].element_size(), n, "elements/s"))
+            # more functors of the trigonometric, exponential and hyperbolic modules, NT2's scalar form
+            for op in ("cot", "sind", "csc", "cbrt", "asinh"):
+                label = f"{op} {tname} 2^24 [-60,60]"
+                if part and part not in label:
+                    continue
+                it = [0]
+
+                def op_step(op=op):
+                    x = xs[it[0] & 1]
+                    it[0] += 1
+                    api.map_(op, x, out=y)
+                ms, _, _ = time_device(op_step, K(100), warmup, ws)
+                out.append(line(label, ms, 2 * n * xs[0].element_size(), n, "elements/s"))
             # z = pow(a0, a1) over NT2's cover range: a0 in [0, 100], a1 in [-10, 10];
             # 12 (float) or 24 (double) bytes per element
             label = f"pow {tname} 2^24 a0 in [0,100], a1 in [-10,10]"
