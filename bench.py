@@ -32,6 +32,7 @@ N_OPTIONS = 1 << 24
 R, SIGMA = 0.02, 0.30
 BYTES_PER_OPTION = 20            # S, K, T read; call, put written (float32)
 NOMINAL_HBM_GBS = 8000.0
+INFLIGHT = 3                     # launches in flight, for both serving modes
 
 
 def peaks():
@@ -166,47 +167,141 @@ def time_device(fn, steps: int, warmup: int, ws: int):
 
 
 # ---------------------------------------------------------- CPU baseline
-def cpu_baseline(sample: int = 1 << 22, seconds: float = 3.0):
-    """The oracle's NT2-restated Black-Scholes on the host cores (options/s, median of reps): the
-    scalar+OpenMP build NT2 runs on aarch64 is the baseline; the compiler-vectorised build of the
-    same loops is reported beside it as an upper bound for a vectorised CPU path."""
-    import numpy as np
+def _oracle():
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib
-    rng = np.random.default_rng(1)
-    S = rng.uniform(5, 30, sample).astype(np.float32)
-    K = rng.uniform(1, 100, sample).astype(np.float32)
-    T = rng.uniform(0.25, 10, sample).astype(np.float32)
+    return oracle_lib
+
+
+def cpu_rate(fn, units: float, seconds: float = 2.0, min_reps: int = 5):
+    """Median units/s of fn() after one warm-up call, over >= min_reps calls and about `seconds`."""
+    fn()
+    rates = []
+    t_end = time.perf_counter() + seconds
+    while time.perf_counter() < t_end or len(rates) < min_reps:
+        t = time.perf_counter()
+        fn()
+        rates.append(units / (time.perf_counter() - t))
+    return statistics.median(rates), len(rates)
+
+
+def nt2_threading(L, n: int, elem_size: int) -> dict:
+    """How NT2's transform spawner treats a table of n elements on this host: grain = L2 bytes /
+    sizeof(T), OpenMP only when n > 8 * grain (shared_memory/transform.hpp:38-48)."""
+    l2 = int(L.nt2o_l2_bytes())
+    grain = max(1, l2 // elem_size)
+    par = n > 8 * grain
+    return {"l2_bytes": l2, "grain": grain, "parallel": par, "threads": int(L.nt2o_max_threads()) if par else 1}
+
+
+def cpu_baseline(S, K, T, seconds: float = 3.0):
+    """The oracle's NT2-restated Black-Scholes on the host cores over the same 2^24-option batch
+    (options/s, median of reps): the scalar+OpenMP build NT2 runs on aarch64 is the baseline; the
+    compiler-vectorised build of the same loops is reported beside it as an upper bound."""
+    import numpy as np
+    oracle_lib = _oracle()
+    n = S.size
     call = np.empty_like(S)
     put = np.empty_like(S)
 
     def rate(variant):
         L = oracle_lib.load(variant)
-        threads = L.nt2o_max_threads()
-        L.nt2o_bs_f(S, K, T, R, SIGMA, call, put, sample, 0, threads)
-        rates = []
-        t_end = time.perf_counter() + seconds
-        while time.perf_counter() < t_end or len(rates) < 10:
-            t = time.perf_counter()
-            L.nt2o_bs_f(S, K, T, R, SIGMA, call, put, sample, 0, threads)
-            rates.append(sample / (time.perf_counter() - t))
-        return statistics.median(rates), len(rates), threads
+        v, reps = cpu_rate(lambda: L.nt2o_bs_f(S, K, T, R, SIGMA, call, put, n, 0, 0), n, seconds)
+        return v, reps, L
 
-    value, reps, threads = rate("libnt2oracle.so")
+    value, reps, L = rate("libnt2oracle.so")
     vec, vreps, _ = rate("libnt2oracle_vec.so")
-    return {"value": value, "unit": "options/s", "cores": threads, "kind": "port",
-            "sample": f"{sample} options per rep (1/{N_OPTIONS // sample} of the 2^24-option batch), "
-                      f"{reps} reps, median; NT2 scalar+OpenMP restatement (oracle/nt2_oracle.c, -O2)",
+    th = nt2_threading(L, n, 4)
+    return {"value": value, "unit": "options/s", "cores": th["threads"], "kind": "port",
+            "sample": f"the full {n}-option batch (the GPU's inputs), {reps} reps, median; NT2 scalar+OpenMP "
+                      f"restatement (oracle/nt2_oracle.c, -O2), NT2's spawner rule: grain {th['grain']} "
+                      f"elements (L2 {th['l2_bytes']} B), parallel={th['parallel']}",
             "vectorised_upper_bound": {"value": vec, "unit": "options/s", "reps": vreps,
                                        "build": "same loops, -O3 auto-vectorised"}}
 
 
+# ------------------------------------------------------------- accuracy
+def _ulp_dist_f32(a, b):
+    """|a - b| in units in the last place of float32 (ordered-integer distance; NaN-aware)."""
+    import numpy as np
+    ia = a.view(np.int32).astype(np.int64)
+    ib = b.view(np.int32).astype(np.int64)
+    ia = np.where(ia < 0, -(ia & 0x7FFFFFFF), ia)
+    ib = np.where(ib < 0, -(ib & 0x7FFFFFFF), ib)
+    d = np.abs(ia - ib)
+    both_nan = np.isnan(a) & np.isnan(b)
+    one_nan = np.isnan(a) ^ np.isnan(b)
+    d = np.where(both_nan, 0, d)
+    return np.where(one_nan, np.int64(1) << 40, d)
+
+
+def normcdf64(x):
+    try:
+        from scipy.special import ndtr
+        return ndtr(x)
+    except Exception:                                   # the NT2 FP64 normcdf of the oracle
+        import numpy as np
+        o = _oracle()
+        out = np.empty_like(x)
+        o.load().nt2o_map_d(o.OP["normcdf"], np.ascontiguousarray(x), out, x.size)
+        return out
+
+
+class BSReference:
+    """FP32 oracle and FP64 reference prices of one batch, for the error of each result."""
+
+    def __init__(self, S, K, T):
+        import numpy as np
+        o = _oracle()
+        L = o.load()
+        n = S.size
+        self.rc = np.empty(n, np.float32)
+        self.rp = np.empty(n, np.float32)
+        L.nt2o_bs_f(S, K, T, R, SIGMA, self.rc, self.rp, n, 0, 0)
+        S64, K64, T64 = (a.astype(np.float64) for a in (S, K, T))
+        self.dc = np.empty(n)
+        self.dp = np.empty(n)
+        L.nt2o_bs_d(S64, K64, T64, R, SIGMA, self.dc, self.dp, n, 0)
+        # the sizes of the two terms each price is the difference of: an error relative to them
+        # is what FP32 can promise where the price cancels
+        vda = SIGMA * np.sqrt(T64)
+        d1 = (np.log(S64 / K64) + (R + 0.5 * SIGMA * SIGMA) * T64) / vda
+        d2 = d1 - vda
+        e = K64 * np.exp(-R * T64)
+        self.scale_c = S64 * normcdf64(d1) + e * normcdf64(d2)
+        self.scale_p = e * normcdf64(-d2) + S64 * normcdf64(-d1)
+
+    def errors(self, call, put, floor: float = 0.01) -> dict:
+        import numpy as np
+        eps = 2.0 ** -24
+        out = {}
+        u_or = max(int(_ulp_dist_f32(call, self.rc).max()), int(_ulp_dist_f32(put, self.rp).max()))
+        out["max_ulp_vs_oracle"] = u_or
+        ec = np.abs(call.astype(np.float64) - self.dc)
+        ep = np.abs(put.astype(np.float64) - self.dp)
+        out["max_abs_err_vs_fp64"] = float(max(ec.max(), ep.max()))
+        out["max_err_vs_fp64_in_eps_of_terms"] = float(max((ec / (eps * self.scale_c)).max(),
+                                                           (ep / (eps * self.scale_p)).max()))
+        c64 = self.dc.astype(np.float32)
+        p64 = self.dp.astype(np.float32)
+        mc = self.dc >= floor
+        mp = self.dp >= floor
+        out[f"max_ulp_vs_fp64_prices_ge_{floor}"] = int(max(_ulp_dist_f32(call[mc], c64[mc]).max(initial=0),
+                                                           _ulp_dist_f32(put[mp], p64[mp]).max(initial=0)))
+        mo_c = self.rc >= floor
+        mo_p = self.rp >= floor
+        out[f"max_ulp_vs_oracle_prices_ge_{floor}"] = int(max(_ulp_dist_f32(call[mo_c], self.rc[mo_c]).max(initial=0),
+                                                             _ulp_dist_f32(put[mo_p], self.rp[mo_p]).max(initial=0)))
+        return out
+
+
 # -------------------------------------------------------------- serving
-def serving_bench(seconds: float = 1.0, rates=(1000, 10000, 50000), seed: int = 7):
+def serving_bench(seconds: float = 1.0, rates=(1000, 5000, 10000, 20000, 50000), seed: int = 7):
     """Poisson arrivals of Black-Scholes requests (sizes log-uniform 256..2^22 options) into the
-    continuous-batching server and into a one-launch-per-request server on the same GPU.  The
-    trace is replayed natively (nt2cuda_server_replay): arrivals, completion waits and releases
-    run in C++ threads, so the numbers are the server's, not a Python client's."""
+    continuous-batching server and into a one-launch-per-request server on the same GPU, both
+    allowed the same number of launches in flight.  The trace is replayed natively
+    (nt2cuda_server_replay): arrivals, completion waits and releases run in C++ threads, so the
+    numbers are the server's, not a Python client's."""
     import numpy as np
     import torch
     from nt2_gb300.server import Server
@@ -219,7 +314,7 @@ def serving_bench(seconds: float = 1.0, rates=(1000, 10000, 50000), seed: int = 
 
     def replay(mode, sizes, offs, arrivals):
         coalesce = mode == "batched"
-        srv = Server(budget_bytes=40 << 30, max_batch_requests=4096, max_inflight_batches=3 if coalesce else 1,
+        srv = Server(budget_bytes=40 << 30, max_batch_requests=4096, max_inflight_batches=INFLIGHT,
                      coalesce=coalesce)
         lat, elapsed = srv.replay(sp, kp, tp, R, SIGMA, offs, sizes, arrivals)
         st = srv.stats()
@@ -246,6 +341,7 @@ def serving_bench(seconds: float = 1.0, rates=(1000, 10000, 50000), seed: int = 
     sat = {m: replay(m, sizes, offs, zero) for m in ("batched", "launch_per_request")}
     sat["throughput_ratio"] = sat["batched"]["options_per_s"] / sat["launch_per_request"]["options_per_s"]
     out["saturation_small_requests"] = sat
+    out["inflight_launches_both_modes"] = INFLIGHT
     return out
 
 

@@ -63,6 +63,11 @@ int nt2cuda_version(void);
 nt2cuda_status nt2cuda_init(int device);
 nt2cuda_status nt2cuda_device_info(int* sm_count, size_t* free_bytes, size_t* total_bytes);
 nt2cuda_status nt2cuda_last_cuda_error(int* code);
+/* No counterpart in the reference.  *count = device allocations the library
+ * has made for its per-stream scratch (fold partials and counters, scan
+ * flags, batch descriptors) since it was loaded; a call that needs no new
+ * scratch leaves it unchanged. */
+nt2cuda_status nt2cuda_scratch_allocations(unsigned long long* count);
 
 /* Device-resident table storage.  Replaces cuda_buffer's cudaMalloc /
  * cudaMemcpyAsync members (modules/arch/cuda/include/nt2/sdk/cuda/memory/buffer.hpp:36-242),
@@ -339,17 +344,20 @@ nt2cuda_status nt2cuda_blackscholes_f32_host(const float* S, const float* K, con
 nt2cuda_status nt2cuda_globalsum_f32(const float* x, size_t n, float* out, int compensated, nt2cuda_stream stream);
 nt2cuda_status nt2cuda_dot_f32(const float* x, const float* y, size_t n, float* out, int compensated,
                                nt2cuda_stream stream);
-/* No counterpart in the reference: NT2 has no device code.  The same result
- * as nt2cuda_dot_f32, for callers that cannot allocate device memory (their
- * device memory belongs to another allocator, or cudaMalloc's device-wide
- * synchronisation is not acceptable in their loop).  It allocates nothing:
- * its scratch is a fixed 512.25 KiB array in device memory, held by every GPU
- * that loads the library until the process exits.  n may not exceed
- * NT2CUDA_DOT_NOALLOC_MAX_N (larger n returns NT2CUDA_ERR_ARG).  The first
- * call on a device looks up the array's address on that device; make that
- * first call before any stream capture.  All calls share the array, so calls
- * whose kernels overlap on the GPU (other streams, other threads) race;
- * calls on one stream are safe.  *out is a DEVICE scalar. */
+/* No counterpart in the reference: NT2 has no device code.  globalsum(X*Y)
+ * for callers that cannot allocate device memory (their device memory
+ * belongs to another allocator, or cudaMalloc's device-wide synchronisation
+ * is not acceptable in their loop).  It allocates nothing: its scratch is a
+ * fixed 512.25 KiB array in device memory, held by every GPU that loads the
+ * library until the process exits.  The result is within nt2cuda_dot_f32's
+ * error bound and bitwise reproducible from call to call of this entry point,
+ * but it is not bit for bit nt2cuda_dot_f32's (that one takes the TMA fold
+ * for long aligned vectors).  n may not exceed NT2CUDA_DOT_NOALLOC_MAX_N
+ * (larger n returns NT2CUDA_ERR_ARG).  The first call on a device, and the
+ * first after its context was reset, looks up the array's address in that
+ * context; make that first call before any stream capture.  All calls share
+ * the array, so calls whose kernels overlap on the GPU (other streams, other
+ * threads) race; calls on one stream are safe.  *out is a DEVICE scalar. */
 #define NT2CUDA_DOT_NOALLOC_MAX_N ((size_t)1 << 30)
 nt2cuda_status nt2cuda_dot_f32_noalloc(const float* x, const float* y, size_t n, float* out, int compensated,
                                        nt2cuda_stream stream);
@@ -422,15 +430,25 @@ nt2cuda_status nt2cuda_scan_f64(int op, const double* A, size_t rows, size_t col
                                 nt2cuda_stream stream);
 
 /* Scans of columns longer than one tile chain their tiles through bounded
- * waits on each other's published prefixes.  A wait that runs out (well
- * under a second; it means a fault) makes its tile write NaN and is counted:
- * *count = waits that ran out since the library was loaded (synchronous). */
+ * waits on each other's published prefixes, and the TMA folds wait (bounded)
+ * for their own bulk copies.  A wait that runs out (it means a fault) makes
+ * its tile or its fold's column write NaN and is counted: *count = waits that
+ * ran out since the library was loaded, over both kinds (synchronous). */
 nt2cuda_status nt2cuda_wait_timeouts(unsigned long long* count);
 /* Check that a wait which cannot be satisfied runs out and is reported: scans
  * a two-tile column whose first tile no block takes.  Returns
  * NT2CUDA_ERR_TIMEOUT when the kernel reported the timeout (the expected
  * result, after about a second), NT2CUDA_OK if it did not. */
 nt2cuda_status nt2cuda_selftest_wait_timeout(nt2cuda_stream stream);
+/* The same for the TMA column fold: out = sum(A,1) of a 16-byte aligned
+ * rows x cols table (rows a multiple of 4 and above 65536, so every column is
+ * split into several units) with the first tile of unit 0 armed but never
+ * copied.  That block's wait runs out after a short bound; column 0 becomes
+ * NaN, the other columns are the normal result, and the column's arrival
+ * counter is left at zero for the next fold on the stream.  Synchronous;
+ * returns NT2CUDA_ERR_TIMEOUT when the timeout was reported. */
+nt2cuda_status nt2cuda_selftest_fold_timeout(const float* A, size_t rows, size_t cols, float* out,
+                                             nt2cuda_stream stream);
 
 /* --------------------------------------------------------- sigmadelta ---- */
 /* One grey video stream for the batched sigma-delta background subtraction

@@ -63,6 +63,7 @@ _SIGS = {
     "nt2cuda_init": (c_int, [c_int]),
     "nt2cuda_device_info": (c_int, [C.POINTER(c_int), C.POINTER(c_size), C.POINTER(c_size)]),
     "nt2cuda_last_cuda_error": (c_int, [C.POINTER(c_int)]),
+    "nt2cuda_scratch_allocations": (c_int, [C.POINTER(C.c_ulonglong)]),
     "nt2cuda_alloc": (c_int, [c_size, C.POINTER(c_vp)]),
     "nt2cuda_free": (c_int, [c_vp]),
     "nt2cuda_alloc_host": (c_int, [c_size, C.POINTER(c_vp)]),
@@ -93,6 +94,7 @@ _SIGS = {
     "nt2cuda_map2_f32": (c_int, [c_int, c_vp, c_vp, c_vp, c_size, c_int, c_vp]),
     "nt2cuda_map2_f64": (c_int, [c_int, c_vp, c_vp, c_vp, c_size, c_int, c_vp]),
     "nt2cuda_selftest_wait_timeout": (c_int, [c_vp]),
+    "nt2cuda_selftest_fold_timeout": (c_int, [c_vp, c_size, c_size, c_vp, c_vp]),
     "nt2cuda_scan_f64": (c_int, [c_int, c_vp, c_size, c_size, c_int, c_vp, c_int, c_vp]),
     "nt2cuda_rgb2grey_u8": (c_int, [c_vp, c_vp, c_vp, c_vp, c_size, c_int, c_vp]),
     "nt2cuda_rgb2yuv_f32": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_size, c_int, c_vp]),

@@ -6,6 +6,7 @@
 #include <string>
 #include "internal.cuh"
 #include "nt2cuda/launch.cuh"
+#include "nt2cuda/scratch.cuh"
 #include "nt2cuda/tuning.cuh"
 
 using namespace nt2cuda;
@@ -60,6 +61,15 @@ nt2cuda_status nt2cuda_device_info(int* sms, size_t* free_bytes, size_t* total_b
     if (free_bytes) *free_bytes = f;
     if (total_bytes) *total_bytes = t;
   }
+  return NT2CUDA_OK;
+}
+
+nt2cuda_status nt2cuda_scratch_allocations(unsigned long long* count)
+{
+  if (!count) return NT2CUDA_ERR_ARG;
+  nt2cuda::scratch_pool& P = nt2cuda::global_scratch_pool();
+  std::lock_guard<std::mutex> g(P.m);
+  *count = P.allocations;
   return NT2CUDA_OK;
 }
 

@@ -6,6 +6,7 @@
 #include "nt2cuda/expr.cuh"
 #include "nt2cuda/fold.cuh"
 #include "nt2cuda/fold_launch.cuh"
+#include "nt2cuda/fold_tma.cuh"
 #include "nt2cuda/launch.cuh"
 
 using namespace nt2cuda;
@@ -80,6 +81,21 @@ nt2cuda_status nt2cuda_sum_outer_f64(const double* A, size_t rows, size_t cols, 
   NT2CUDA_NVTX_RANGE;
   if ((rows && cols && !A) || !out) return NT2CUDA_ERR_ARG;
   return launch_status(nt2cuda::fold::outer_fold<fold::op_sum<false>, double>(term<double>{A}, rows, cols, out, as_stream(s)));
+}
+
+nt2cuda_status nt2cuda_selftest_fold_timeout(const float* A, size_t rows, size_t cols, float* out, nt2cuda_stream s)
+{
+  NT2CUDA_NVTX_RANGE;
+  if (!A || !out || !cols || ((uintptr_t)A & 15u) || rows % 4 || rows <= (size_t)fold::inner_tile<float>() * 16)
+    return NT2CUDA_ERR_ARG;
+  unsigned long long before = 0, after = 0;
+  cudaError_t e = fold::read_fold_wait_timeouts(&before);
+  if (e == cudaSuccess)
+    e = fold::inner_fold_tma<fold::op_sum<true>, float>(A, nullptr, rows, cols, out, as_stream(s), 0, 1u << 12);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(as_stream(s));
+  if (e == cudaSuccess) e = fold::read_fold_wait_timeouts(&after);
+  if (e != cudaSuccess) return from_cuda(e);
+  return after > before ? NT2CUDA_ERR_TIMEOUT : NT2CUDA_OK;
 }
 
 nt2cuda_status nt2cuda_set_fold_path(int path)

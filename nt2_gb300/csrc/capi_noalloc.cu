@@ -16,6 +16,11 @@
 // different host threads) race on it; calls on one stream are ordered and
 // safe.  The counter is cleared by a memset before every launch, so a call
 // does not depend on what an earlier call left behind.
+//
+// The result is within the error bound of nt2cuda_dot_f32 and bitwise
+// reproducible from one call of this entry point to the next, but not bit
+// for bit nt2cuda_dot_f32's: that entry point takes the TMA fold for long
+// aligned vectors, this one always takes the register-staged fold kernel.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <mutex>
@@ -41,24 +46,65 @@ __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
-void* g_scratch_addr[kMaxDevices] = {};
+struct scratch_slot {
+  unsigned long long ctx_id = 0;     // the context the address belongs to (0: none yet)
+  void* addr = nullptr;
+};
+scratch_slot g_scratch[kMaxDevices];
 
-// Once per device, with that device current: look up the device address of
-// the scratch array.  Done by the first call on each device.
+// The driver's identifier of the current context: unique over the process,
+// so a context torn down (cudaDeviceReset) and created again gets a new one.
+using ctx_get_current_fn = int (*)(void**);
+using ctx_get_id_fn = int (*)(void*, unsigned long long*);
+cudaError_t current_context_id(unsigned long long* id)
+{
+  static ctx_get_current_fn get_current = nullptr;
+  static ctx_get_id_fn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<ctx_get_current_fn>(p);
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<ctx_get_id_fn>(p);
+    cudaGetLastError();
+  });
+  if (!get_current || !get_id) return cudaErrorNotSupported;
+  void* ctx = nullptr;
+  if (get_current(&ctx) != 0) return cudaErrorDeviceUninitialized;
+  if (!ctx) {                                  // no context yet: 0, which no context has
+    *id = 0;
+    return cudaSuccess;
+  }
+  return get_id(ctx, id) == 0 ? cudaSuccess : cudaErrorDeviceUninitialized;
+}
+
+// Once per device and context, with that device current: look up the device
+// address of the scratch array.  Done by the first call on each device, and
+// again by the first call after the device's context was reset.
 nt2cuda_status scratch_address(void** out)
 {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return from_cuda(e);
   if (dev < 0 || dev >= kMaxDevices) return NT2CUDA_ERR_ARG;
+  unsigned long long ctx = 0;
+  if ((e = current_context_id(&ctx)) != cudaSuccess) return from_cuda(e);
   std::lock_guard<std::mutex> g(g_setup_mutex);
-  if (!g_scratch_addr[dev]) {
+  scratch_slot& slot = g_scratch[dev];
+  if (ctx == 0 || slot.ctx_id != ctx || !slot.addr) {
     void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);    // also creates the context when there is none
     if (e != cudaSuccess) return from_cuda(e);
-    g_scratch_addr[dev] = p;
+    if ((e = current_context_id(&ctx)) != cudaSuccess) return from_cuda(e);
+    slot.addr = p;
+    slot.ctx_id = ctx;
   }
-  *out = g_scratch_addr[dev];
+  *out = slot.addr;
   return NT2CUDA_OK;
 }
 

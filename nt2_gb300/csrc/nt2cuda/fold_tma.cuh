@@ -13,9 +13,13 @@
 // NT2's counterparts: modules/arch/shared_memory/include/nt2/sdk/shared_memory/worker/inner_fold.hpp:53-108
 // and .../worker/outer_fold.hpp:31-155.
 //
-// A block whose barrier wait runs out (tma::mbar_wait) writes NaN for the
-// unit it was working on, waits (bounded) for the copies it still has in
-// flight and leaves.
+// A block whose barrier wait runs out (tma::mbar_wait) waits (bounded) for
+// the copies it still has in flight, counts itself in g_fold_wait_timeouts
+// (read by nt2cuda_wait_timeouts) and gives up the units it still owns: a unit
+// of a column or strip that is folded in one piece gets NaN at once; a split
+// one still arrives on its column's counter with the poison bit set, so the
+// counter returns to zero as in a complete fold and the last arriver writes
+// NaN instead of merging partials that were never written.
 #pragma once
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -26,11 +30,30 @@
 #include "launch.cuh"
 #include "scratch.cuh"
 #include "tma.cuh"
+#include "wait_status.cuh"
 
 namespace nt2cuda {
 namespace fold {
 
 constexpr int kTmaTileBytes = 16384;
+
+// Barrier waits of these kernels that ran out since this translation unit was
+// loaded; every unit including this header registers a reader (fold_status.hpp).
+static __device__ unsigned long long g_fold_wait_timeouts = 0;
+static cudaError_t read_fold_wait_timeouts(unsigned long long* count)
+{
+  return cudaMemcpyFromSymbol(count, g_fold_wait_timeouts, sizeof(unsigned long long));
+}
+static const timeout_reader_registration fold_wait_timeouts_reader(read_fold_wait_timeouts);
+
+// Arrival counters: the low 31 bits count the units merged so far, the top bit
+// records that a unit of the column gave up.
+constexpr unsigned kPoison = 0x80000000u;
+__device__ __forceinline__ unsigned arrive(unsigned* counter, bool poisoned)
+{
+  if (poisoned) atomicOr(counter, kPoison);
+  return atomicAdd(counter, 1u);
+}
 
 // value written for a unit whose copies did not arrive: NaN, or 0xFF for a logical output
 template <class T> __device__ __forceinline__ T quiet_nan()
@@ -74,9 +97,37 @@ __device__ __forceinline__ state_of<Op, T> block_merge(state_of<Op, T> v, state_
 }
 
 // ------------------------------------------------------------ inner fold
+// fail_unit: the unit whose first tile the producer arms but never copies, so
+// that its barrier wait runs out (~0 in every fold; set only by the timeout
+// self-test); wait_rounds bounds every barrier wait.
 struct inner_tma_shape {
   size_t rows, cols, seg, splits, units;
+  size_t fail_unit;
+  uint32_t wait_rounds;
 };
+
+// A block that gave up: count it, then let every unit it still owns arrive
+// poisoned (a column folded in one piece gets NaN at once; a split column's
+// last arriver writes NaN and clears the counter).  Every thread of the block
+// calls this with the same first unit.
+template <class O>
+__device__ void inner_give_up(const inner_tma_shape& sh, size_t cu, O* out, unsigned* counters)
+{
+  if (threadIdx.x != 0) return;
+  atomicAdd(&g_fold_wait_timeouts, 1ull);
+  for (size_t u = cu; u < sh.units; u += gridDim.x) {
+    const size_t j = u / sh.splits;
+    if (sh.splits == 1) {
+      out[j] = quiet_nan<O>();
+    } else {
+      const unsigned prev = arrive(&counters[j], true);
+      if ((prev & ~kPoison) == (unsigned)sh.splits - 1u) {
+        counters[j] = 0u;
+        out[j] = quiet_nan<O>();
+      }
+    }
+  }
+}
 
 template <class T> __host__ __device__ constexpr int inner_tile() { return kTmaTileBytes / (int)sizeof(T); }
 
@@ -132,8 +183,10 @@ __global__ void __launch_bounds__(256) k_inner_tma(const T* __restrict__ x, cons
     const uint32_t cnt = (uint32_t)((rend - r0) < (size_t)TILE ? (rend - r0) : (size_t)TILE);
     const uint32_t bytes = cnt * (uint32_t)sizeof(T);
     tma::mbar_arrive_expect_tx(&bar[s], bytes * NT);
-    tma::bulk_g2s(buf + (size_t)(s * NT) * TILE, x + j * sh.rows + r0, bytes, &bar[s]);
-    if constexpr (NT == 2) tma::bulk_g2s(buf + (size_t)(s * NT + 1) * TILE, y + j * sh.rows + r0, bytes, &bar[s]);
+    if (!(pu == sh.fail_unit && pt == 0)) {
+      tma::bulk_g2s(buf + (size_t)(s * NT) * TILE, x + j * sh.rows + r0, bytes, &bar[s]);
+      if constexpr (NT == 2) tma::bulk_g2s(buf + (size_t)(s * NT + 1) * TILE, y + j * sh.rows + r0, bytes, &bar[s]);
+    }
     ++issued;
     if (++pt == inner_unit_tiles<T>(sh, pu)) { pt = 0; pu += gridDim.x; }
   };
@@ -147,12 +200,13 @@ __global__ void __launch_bounds__(256) k_inner_tma(const T* __restrict__ x, cons
   for (int l = 0; l < V; ++l) a[l] = Op::template init<T>();
   while (cu < sh.units) {
     const int s = (int)(iter % STAGES);
-    const bool ok = tma::mbar_wait(&bar[s], (iter / STAGES) & 1u);
+    const bool ok = tma::mbar_wait(&bar[s], (iter / STAGES) & 1u, sh.wait_rounds);
     if (__syncthreads_or(!ok)) {
-      if (threadIdx.x == 0) {
-        out[cu / sh.splits] = quiet_nan<out_of<Op, T>>();
-        for (uint32_t k = iter; k < issued; ++k) tma::mbar_wait(&bar[k % STAGES], (k / STAGES) & 1u);
-      }
+      // copies still in flight land in this block's shared memory: wait for
+      // them (bounded) before leaving, the one that ran out included
+      if (threadIdx.x == 0)
+        for (uint32_t k = iter; k < issued; ++k) tma::mbar_wait(&bar[k % STAGES], (k / STAGES) & 1u, sh.wait_rounds);
+      inner_give_up(sh, cu, out, counters);
       __syncthreads();
       return;
     }
@@ -194,12 +248,14 @@ __global__ void __launch_bounds__(256) k_inner_tma(const T* __restrict__ x, cons
         if (threadIdx.x == 0) {
           partials[cu] = t;
           __threadfence();
-          const unsigned prev = atomicAdd(&counters[j], 1u);
-          s_last = (prev == (unsigned)sh.splits - 1u);
+          const unsigned prev = arrive(&counters[j], false);
+          s_last = ((prev & ~kPoison) == (unsigned)sh.splits - 1u) ? 1u + (prev >> 31) : 0u;
           if (s_last) counters[j] = 0u;
         }
         __syncthreads();
-        if (s_last) {
+        if (s_last == 2u) {                            // a unit of this column gave up
+          if (threadIdx.x == 0) out[j] = quiet_nan<out_of<Op, T>>();
+        } else if (s_last) {
           __threadfence();
           S m = Op::template init<T>();
           for (size_t q = threadIdx.x; q < sh.splits; q += blockDim.x)
@@ -220,6 +276,7 @@ __global__ void __launch_bounds__(256) k_inner_tma(const T* __restrict__ x, cons
 // ------------------------------------------------------------ outer fold
 struct outer_tma_shape {
   size_t rows, cols, cchunk, splits, strips, units;
+  uint32_t wait_rounds;
 };
 
 constexpr int kOuterRows = 256;   // box rows (and threads per block)
@@ -268,13 +325,28 @@ __global__ void __launch_bounds__(256) k_outer_tma(const __grid_constant__ CUten
   S a0 = Op::template init<T>(), a1 = Op::template init<T>();
   while (cu < sh.units) {
     const int s = (int)(iter % STAGES);
-    const bool ok = tma::mbar_wait(&bar[s], (iter / STAGES) & 1u);
+    const bool ok = tma::mbar_wait(&bar[s], (iter / STAGES) & 1u, sh.wait_rounds);
     if (__syncthreads_or(!ok)) {
-      const size_t row = (cu / sh.splits) * BR + threadIdx.x;
-      if (row < sh.rows) out[row] = quiet_nan<out_of<Op, T>>();
-      if (threadIdx.x == 0)
-        for (uint32_t k = iter; k < issued; ++k) tma::mbar_wait(&bar[k % STAGES], (k / STAGES) & 1u);
-      __syncthreads();
+      if (threadIdx.x == 0) {
+        for (uint32_t k = iter; k < issued; ++k) tma::mbar_wait(&bar[k % STAGES], (k / STAGES) & 1u, sh.wait_rounds);
+        atomicAdd(&g_fold_wait_timeouts, 1ull);
+      }
+      // every unit this block still owns arrives poisoned (see inner_give_up)
+      for (size_t u = cu; u < sh.units; u += gridDim.x) {
+        const size_t strip = u / sh.splits;
+        if (sh.splits > 1) {
+          if (threadIdx.x == 0) {
+            const unsigned prev = arrive(&counters[strip], true);
+            s_last = ((prev & ~kPoison) == (unsigned)sh.splits - 1u) ? 1u : 0u;
+            if (s_last) counters[strip] = 0u;
+          }
+          __syncthreads();
+        }
+        const bool last = sh.splits == 1 || s_last;
+        const size_t row = strip * BR + threadIdx.x;
+        if (last && row < sh.rows) out[row] = quiet_nan<out_of<Op, T>>();
+        __syncthreads();
+      }
       return;
     }
     const T* tile = buf + (size_t)s * BC * BR;
@@ -307,12 +379,14 @@ __global__ void __launch_bounds__(256) k_outer_tma(const __grid_constant__ CUten
         __syncthreads();                    // the block's partials, then one device-scope fence
         if (threadIdx.x == 0) {
           __threadfence();
-          const unsigned prev = atomicAdd(&counters[strip], 1u);
-          s_last = (prev == (unsigned)sh.splits - 1u);
+          const unsigned prev = arrive(&counters[strip], false);
+          s_last = ((prev & ~kPoison) == (unsigned)sh.splits - 1u) ? 1u + (prev >> 31) : 0u;
           if (s_last) counters[strip] = 0u;
         }
         __syncthreads();
-        if (s_last) {
+        if (s_last == 2u) {                  // a unit of this strip gave up
+          if (row < sh.rows) out[row] = quiet_nan<out_of<Op, T>>();
+        } else if (s_last) {
           __threadfence();
           S m = merge_partials<Op, T>(partials + strip * sh.splits * BR + threadIdx.x, sh.splits, BR);
           if (row < sh.rows) out[row] = Op::finish(m, sh.cols);
@@ -351,8 +425,10 @@ template <class K> inline cudaError_t set_smem(K kernel, int bytes)
 }
 
 // x (and y when not null) are 16-byte aligned and rows % (16/sizeof(T)) == 0.
+// fail_unit and wait_rounds are for the timeout self-test (see inner_tma_shape).
 template <class Op, class T>
-cudaError_t inner_fold_tma(const T* x, const T* y, size_t rows, size_t cols, out_of<Op, T>* out, cudaStream_t s)
+cudaError_t inner_fold_tma(const T* x, const T* y, size_t rows, size_t cols, out_of<Op, T>* out, cudaStream_t s,
+                           size_t fail_unit = ~(size_t)0, uint32_t wait_rounds = tma::kMaxRounds)
 {
   using S = state_of<Op, T>;
   constexpr int TILE = inner_tile<T>();
@@ -362,6 +438,8 @@ cudaError_t inner_fold_tma(const T* x, const T* y, size_t rows, size_t cols, out
   sh.seg = (size_t)TILE * 16;
   sh.splits = (rows + sh.seg - 1) / sh.seg;
   sh.units = cols * sh.splits;
+  sh.fail_unit = fail_unit;
+  sh.wait_rounds = wait_rounds;
   if (sh.units == 0) return cudaSuccess;
   S* partials = nullptr;
   unsigned* counters = nullptr;
@@ -430,6 +508,7 @@ cudaError_t outer_fold_tma(const T* A, size_t rows, size_t cols, out_of<Op, T>* 
   if (sh.cchunk < (size_t)BC) sh.cchunk = BC;
   sh.splits = (cols + sh.cchunk - 1) / sh.cchunk;
   sh.units = sh.strips * sh.splits;
+  sh.wait_rounds = tma::kMaxRounds;
   S* partials = nullptr;
   unsigned* counters = nullptr;
   if (sh.splits > 1) {

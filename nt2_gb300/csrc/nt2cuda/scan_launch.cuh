@@ -8,6 +8,7 @@
 #include "launch.cuh"
 #include "scan.cuh"
 #include "scratch.cuh"
+#include "wait_status.cuh"
 
 namespace nt2cuda {
 namespace scan {
@@ -54,11 +55,15 @@ cudaError_t inner_scan(const T* x, T* y, size_t rows, size_t cols, cudaStream_t 
   return launch_dependent(k, grid, 256, s, args);
 }
 
-// Look-back waits that ran out since the library was loaded (synchronous).
-inline cudaError_t wait_timeouts(unsigned long long* count)
+static cudaError_t read_scan_wait_timeouts(unsigned long long* count)
 {
   return cudaMemcpyFromSymbol(count, g_wait_timeouts, sizeof(unsigned long long));
 }
+static const timeout_reader_registration scan_wait_timeouts_reader(read_scan_wait_timeouts);
+
+// Bounded waits that ran out since the library was loaded, over every kernel
+// that counts them (scan look-backs, TMA fold barriers); synchronous.
+inline cudaError_t wait_timeouts(unsigned long long* count) { return total_wait_timeouts(count); }
 
 // A look-back wait that must run out: a two-tile column scanned with the
 // ticket counter started at 1, so the block that takes tile 1 waits for a tile

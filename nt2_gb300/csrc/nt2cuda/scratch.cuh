@@ -21,6 +21,7 @@ struct scratch_pool {
   struct entry { void* p = nullptr; size_t bytes = 0; };
   std::mutex m;
   std::unordered_map<uintptr_t, entry> by_key;
+  unsigned long long allocations = 0;     // cudaMalloc calls made for scratch so far
 };
 inline scratch_pool& global_scratch_pool() { static scratch_pool p; return p; }
 
@@ -59,6 +60,7 @@ inline cudaError_t stream_scratch(cudaStream_t s, size_t bytes, void** out, int 
     size_t want = bytes < 4096 ? 4096 : bytes;
     cudaError_t err = cudaMalloc(&e.p, want);
     if (err != cudaSuccess) { e.p = nullptr; return err; }
+    ++P.allocations;
     err = cudaMemsetAsync(e.p, 0, want, s);
     if (err != cudaSuccess) return err;
     e.bytes = want;

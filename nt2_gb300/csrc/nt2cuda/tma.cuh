@@ -65,9 +65,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase)
 // round suspends for a hardware-defined time slice; kMaxRounds rounds bound
 // the wait to well under a few seconds.
 constexpr uint32_t kMaxRounds = 1u << 22;
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, uint32_t rounds = kMaxRounds)
 {
-  for (uint32_t i = 0; i < kMaxRounds; ++i)
+  for (uint32_t i = 0; i < rounds; ++i)
     if (mbar_try_wait(bar, phase)) return true;
   return false;
 }

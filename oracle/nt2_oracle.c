@@ -1748,6 +1748,62 @@ EXPORT void nt2o_outer_fold_f(const float* A, size_t rows, size_t cols,
  * and combines the per-block partials in arrival order.  Arrival order is
  * what makes NT2's FP32 sums vary run to run; here the combine is an OpenMP
  * reduction, the same class of order. */
+/* Row sums (sum(A,2)) with the loop structure of NT2's shared-memory
+ * outer_fold in its in-cache branch (arch/shared_memory/.../worker/outer_fold.hpp:119-147,
+ * reduction/.../details/outer_fold_step.hpp:33-66): the rows are cut into
+ * chunks of one 64-byte line of floats (16), chunks are spread over the
+ * threads by the transform spawner's static schedule (openmp/spawner/transform.hpp:47-58,
+ * the last chunk taking the leftover), and each chunk adds the columns one
+ * after another into its 16 outputs.  Every output is the sequential FP32 sum
+ * over the columns, as out32 of nt2o_outer_fold_f; this form is the one to
+ * time. */
+EXPORT void nt2o_outer_fold_nt2_f(const float* A, size_t rows, size_t cols, float* out, int threads)
+{
+  const size_t grain = 16;
+  const size_t iib = rows / 4 * 4;
+  (void)threads;
+  if (iib >= grain) {
+    const ptrdiff_t nb = (ptrdiff_t)(iib / grain);
+    const size_t left = iib % grain;
+#ifdef _OPENMP
+    int th = threads > 0 ? threads : omp_get_max_threads();
+    #pragma omp parallel for schedule(static) num_threads(th)
+#endif
+    for (ptrdiff_t c = 0; c < nb; ++c) {
+      const size_t lo = (size_t)c * grain, hi = lo + ((c < nb - 1) ? grain : grain + left);
+      for (size_t i = lo; i < hi; ++i) out[i] = 0.0f;
+      for (size_t m = 0; m < cols; ++m) {
+        const float* a = A + m * rows;
+        for (size_t i = lo; i < hi; ++i) out[i] = out[i] + a[i];
+      }
+    }
+  }
+  for (size_t i = (iib >= grain ? iib : 0); i < rows; ++i) {
+    float s = 0.0f;
+    for (size_t m = 0; m < cols; ++m) s = s + A[m * rows + i];
+    out[i] = s;
+  }
+}
+
+/* Many sigma-delta streams, each the NT2 statement of nt2o_sigmadelta_u8.
+ * NT2 evaluates one stream's statement at a time and runs it on one thread
+ * while its table is below the spawner's threshold (8 * L2 bytes of
+ * pixels), which every stream of a 1920x1080 or smaller video is; the
+ * streams themselves are independent, so this spreads whole streams over
+ * the threads (the most a caller of NT2 gets from the host cores). */
+EXPORT void nt2o_sigmadelta_batch_u8(int nstreams, const uint8_t* const* frames, const size_t* frame_stride,
+                                     const size_t* npix, int nframes, uint8_t* const* bkg, uint8_t* const* var,
+                                     uint8_t* const* labels, int init, int threads)
+{
+  (void)threads;
+#ifdef _OPENMP
+  int th = threads > 0 ? threads : omp_get_max_threads();
+  #pragma omp parallel for schedule(dynamic, 1) num_threads(th)
+#endif
+  for (int k = 0; k < nstreams; ++k)
+    nt2o_sigmadelta_u8(frames[k], frame_stride[k], npix[k], nframes, bkg[k], var[k], labels[k], init, 1);
+}
+
 EXPORT float nt2o_dot_omp_f(const float* x, const float* y, size_t n, int lanes, int threads)
 {
   (void)lanes;

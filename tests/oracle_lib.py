@@ -93,6 +93,9 @@ SIGS = {
     "nt2o_inner_fold_f": (None, [f32p, sz, sz, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     "nt2o_outer_fold_f": (None, [f32p, sz, sz, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     "nt2o_dot_omp_f": (C.c_float, [f32p, C.c_void_p, sz, C.c_int, C.c_int]),
+    "nt2o_outer_fold_nt2_f": (None, [f32p, sz, sz, f32p, C.c_int]),
+    "nt2o_sigmadelta_batch_u8": (None, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                        C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
     "nt2o_l2_bytes": (sz, []),
     "nt2o_max_threads": (C.c_int, []),
 }

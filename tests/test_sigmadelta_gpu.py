@@ -64,6 +64,33 @@ def test_graph_plan_matches_direct_launch(gpu, oracle):
         check_stream(oracle, e, 8, True)
 
 
+def test_benchmark_batch_bit_exact(gpu, oracle):
+    """The batch the benchmark times: 256 streams of 8 frames, sizes log-uniform between
+    320x240 and 1920x1080 (seed 11), through the direct batched launch and through the
+    CUDA-graph plan; every stream's bkg, var and label planes equal the oracle's."""
+    batch = video.make_batch(256, 8, seed=11)
+    gpu.sigmadelta_batch(batch, 8, init=True)
+    torch.cuda.synchronize()
+    direct = [{k: e[k].cpu() for k in ("bkg", "var", "labels")} for e in batch]
+    for e in batch:
+        check_stream(oracle, e, 8, True)
+    for e in batch:                                  # the plan must recompute everything
+        for k in ("bkg", "var", "labels"):
+            e[k].fill_(0x5a)
+    plan = gpu.SigmaDeltaPlan(batch, 8, init=True)
+    plan.launch()
+    torch.cuda.synchronize()
+    plan.close()
+    for e, d in zip(batch, direct):
+        for k in ("bkg", "var"):
+            assert torch.equal(e[k].cpu(), d[k])
+        npix = e["width"] * e["height"]
+        gl, dl = e["labels"].cpu(), d["labels"]
+        for f in range(7):
+            lo = f * e["label_stride"]
+            assert torch.equal(gl[lo:lo + npix], dl[lo:lo + npix]), f
+
+
 def test_bad_arguments_rejected(gpu):
     import nt2_gb300
     e = video.make_stream(8, 8, 2, seed=1)

@@ -1,8 +1,10 @@
 """nt2cuda_dot_f32_noalloc: the sdot fold for callers that cannot allocate
 device memory (their memory belongs to another allocator, or cudaMalloc's
 device-wide synchronisation is not acceptable where they run).  Its scratch
-is a fixed array in device memory, so it must give the allocating entry
-point's result, call after call, and refuse sizes beyond its fixed limit.
+is a fixed array in device memory, so it must agree with the allocating
+entry point within the sdot tolerance, call after call, reproduce its own
+result bit for bit, allocate nothing on a stream it has never seen, and
+refuse sizes beyond its fixed limit.
 
 This file is collected last, so a failure here comes after every other test
 has run; it also passes on its own in a fresh process."""
@@ -43,6 +45,41 @@ def test_noalloc_matches_allocating_entry_twice(gpu, oracle, comp):
         tol = (4 * EPS * abs(ref) + 64 * EPS * EPS * n * ab) if comp else (np.log2(n) + 256) * EPS * ab
         assert abs(a - b) <= tol + EPS * ab, (call, a, b)
         assert abs(a - ref) <= tol + EPS * ab, (call, a, ref)
+
+
+def _scratch_allocations(L):
+    c = C.c_ulonglong()
+    assert L.nt2cuda_scratch_allocations(C.byref(c)) == 0
+    return c.value
+
+
+def test_noalloc_allocates_nothing_on_a_fresh_stream(gpu):
+    """On a stream the library has never seen, nt2cuda_dot_f32 must allocate that
+    stream's scratch (the control) while the no-allocation entry point must not;
+    its repeated calls also give the same bits."""
+    import nt2_gb300
+    L = nt2_gb300.lib()
+    n = (1 << 22) + 12
+    x = torch.empty(n, dtype=torch.float32, device="cuda")
+    y = torch.empty(n, dtype=torch.float32, device="cuda")
+    gpu.fill_normal(x, 31)
+    gpu.fill_normal(y, 32)
+    outs = []
+    for _ in range(2):
+        s = torch.cuda.Stream()
+        before = _scratch_allocations(L)
+        out = torch.empty(1, dtype=torch.float32, device="cuda")
+        assert L.nt2cuda_dot_f32_noalloc(x.data_ptr(), y.data_ptr(), n, out.data_ptr(), 1, s.cuda_stream) == 0
+        s.synchronize()
+        assert _scratch_allocations(L) == before
+        outs.append(out.cpu().numpy().view(np.uint32)[0])
+    assert outs[0] == outs[1]
+    s = torch.cuda.Stream()
+    before = _scratch_allocations(L)
+    out = torch.empty(1, dtype=torch.float32, device="cuda")
+    assert L.nt2cuda_dot_f32(x.data_ptr(), y.data_ptr(), n, out.data_ptr(), 1, s.cuda_stream) == 0
+    s.synchronize()
+    assert _scratch_allocations(L) > before
 
 
 def test_noalloc_small_and_empty(gpu):
