@@ -57,6 +57,16 @@ def profiled_traffic(name: str):
     return None
 
 
+DATA = ("synthetic (seeded counter-based uniforms: S~U[5,30], K~U[1,100], T~U[0.25,10]; r=0.02, sigma=0.30)")
+
+
+def headline_config(n: int, ws: int) -> dict:
+    return {"workload": "Black-Scholes call+put, FP32, 2^24 options per GPU, normcdf via erfc, "
+                        "NT2 unfused arithmetic (bit-exact with the oracle)",
+            "options_per_gpu": n, "parallelism": f"replicas x{ws}",
+            "l2": "inputs+outputs 335 MB > 129 MB L2, no flush needed"}
+
+
 # ------------------------------------------------------------------ clocks
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled while the bench runs."""
@@ -280,8 +290,10 @@ class BSReference:
         ec = np.abs(call.astype(np.float64) - self.dc)
         ep = np.abs(put.astype(np.float64) - self.dp)
         out["max_abs_err_vs_fp64"] = float(max(ec.max(), ep.max()))
-        out["max_err_vs_fp64_in_eps_of_terms"] = float(max((ec / (eps * self.scale_c)).max(),
-                                                           (ep / (eps * self.scale_p)).max()))
+        # eps = 2^-24 of the larger term, or of FLT_MIN where the terms are below the normal range
+        tiny = 2.0 ** -126
+        out["max_err_vs_fp64_in_eps_of_terms"] = float(max((ec / (eps * self.scale_c + tiny)).max(),
+                                                           (ep / (eps * self.scale_p + tiny)).max()))
         c64 = self.dc.astype(np.float32)
         p64 = self.dp.astype(np.float32)
         mc = self.dc >= floor
@@ -293,6 +305,208 @@ class BSReference:
         out[f"max_ulp_vs_oracle_prices_ge_{floor}"] = int(max(_ulp_dist_f32(call[mo_c], self.rc[mo_c]).max(initial=0),
                                                              _ulp_dist_f32(put[mo_p], self.rp[mo_p]).max(initial=0)))
         return out
+
+
+# ------------------------------------------- the other configurations
+def _roof(bytes_, ms, peak):
+    gbs = bytes_ / (ms * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+            "algorithmic_bytes_per_launch": int(bytes_)}
+
+
+def _cpu(value, unit, cores, sample, reps):
+    return {"value": value, "unit": unit, "cores": cores, "kind": "port", "reps": reps, "sample": sample}
+
+
+def config_lines(ws: int, steps: int, warmup: int) -> dict:
+    """Every other configuration of the benchmark list, measured the same way as the headline:
+    device time with inputs resident (rotating copies larger than L2 where one table fits in it),
+    the fraction of the measured copy bandwidth, the NT2-restated CPU path timed on the same
+    inputs on the host cores, and each result's error against the oracle and an FP64 oracle."""
+    import numpy as np
+    import torch
+    import nt2_gb300.api as api
+    from nt2_gb300 import video
+    o = _oracle()
+    L = o.load()
+    peak, _ = peaks()
+    eps = 2.0 ** -24
+    out = {}
+    K = lambda d: max(3, min(steps, d))
+
+    def guarded(name, fn):
+        try:
+            out[name] = fn()
+        except Exception as e:                     # one configuration's failure is reported, not fatal
+            out[name] = {"error": repr(e)[:300]}
+        torch.cuda.empty_cache()
+
+    def saxpy():
+        n = 1 << 24
+        xs = [torch.empty(n, device="cuda") for _ in range(4)]
+        ys = [torch.empty(n, device="cuda") for _ in range(4)]
+        for i in range(4):
+            api.fill_uniform(xs[i], -1, 1, 1 + i)
+            api.fill_uniform(ys[i], -1, 1, 11 + i)
+        x0, y0 = xs[0].cpu().numpy(), ys[0].cpu().numpy()
+        api.autotune("saxpy_f32", n)
+        it = [0]
+
+        def step():
+            i = it[0] & 3
+            it[0] += 1
+            api.saxpy(2.5, xs[i], ys[i])
+        ms, _, _ = time_device(step, K(200), warmup, ws)
+        # accuracy on fresh copies of pair 0
+        xg = torch.from_numpy(x0).cuda()
+        yg = torch.from_numpy(y0.copy()).cuda()
+        api.saxpy(2.5, xg, yg)
+        got = yg.cpu().numpy()
+        ref = y0.copy()
+        L.nt2o_saxpy_f(2.5, x0, ref, n, 0)
+        r64 = 2.5 * x0.astype(np.float64) + y0.astype(np.float64)
+        yc = y0.copy()
+        rate, reps = cpu_rate(lambda: L.nt2o_saxpy_f(2.5, x0, yc, n, 0), n)
+        th = nt2_threading(L, n, 4)
+        return {"ms": ms, "value": ws * n / (ms * 1e-3), "unit": "elements/s", "roofline": _roof(12 * n, ms, peak),
+                "l2": "4 rotating (x, y) pairs, 536 MB > L2",
+                "cpu_baseline": _cpu(rate, "elements/s", th["threads"], f"same 2^24-element x, y; NT2 spawner "
+                                     f"parallel={th['parallel']}", reps),
+                "error": {"mismatches_vs_oracle": int(np.count_nonzero(got.view(np.uint32) != ref.view(np.uint32))),
+                          "max_ulp_vs_fp64": int(_ulp_dist_f32(got, r64.astype(np.float32)).max())}}
+
+    def sdot():
+        n = 1 << 26
+        x = torch.empty(n, device="cuda")
+        y = torch.empty(n, device="cuda")
+        api.fill_normal(x, 1)
+        api.fill_normal(y, 2)
+        xh, yh = x.cpu().numpy(), y.cpu().numpy()
+        ref, ab = o.dot_fp64(xh, yh)
+        res = {}
+        oc = torch.empty(1, device="cuda")
+        cpu_v, reps = cpu_rate(lambda: L.nt2o_dot_omp_f(xh, yh.ctypes.data, n, 8, 0), n)
+        cpu_err = abs(float(L.nt2o_dot_omp_f(xh, yh.ctypes.data, n, 8, 0)) - ref) / (eps * ab)
+        for comp in (True, False):
+            ms, _, _ = time_device(lambda: api.dot(x, y, compensated=comp, out=oc), K(100), warmup, ws)
+            g = float(api.dot(x, y, compensated=comp).cpu()[0])
+            res["compensated" if comp else "plain"] = {
+                "ms": ms, "value": ws * n / (ms * 1e-3), "unit": "elements/s", "roofline": _roof(8 * n, ms, peak),
+                "error": {"abs_err_vs_fp64": abs(g - ref), "err_in_eps_sum_abs": abs(g - ref) / (eps * ab)}}
+        res["cpu_baseline"] = _cpu(cpu_v, "elements/s", int(L.nt2o_max_threads()),
+                                   "same 2^26 x, y; NT2's OpenMP fold (static chunks, partials summed)", reps)
+        res["cpu_baseline"]["err_in_eps_sum_abs"] = cpu_err
+        res["l2"] = "inputs 536 MB > L2"
+        return res
+
+    def folds():
+        rows, cols = 8192, 4096
+        As = [torch.empty(rows * cols, device="cuda") for _ in range(4)]
+        for i in range(4):
+            api.fill_normal(As[i], 3 + i)
+        Ah = As[0].cpu().numpy()
+        o32c, o64c, abc = o.inner_fold(Ah, rows, cols, lanes=4)
+        o32r, o64r, abr = o.outer_fold(Ah, rows, cols)
+        res = {}
+        for dim, name, m, ref64, ab, cpu32 in ((1, "column_sums_inner_fold", cols, o64c, abc, o32c),
+                                               (2, "row_sums_outer_fold", rows, o64r, abr, o32r)):
+            oo = torch.empty(m, device="cuda")
+            it = [0]
+
+            def step(dim=dim, oo=oo):
+                i = it[0] & 3
+                it[0] += 1
+                api.sum_colmajor(As[i], rows, cols, dim, out=oo)
+            ms, _, _ = time_device(step, K(100), warmup, ws)
+            g = api.sum_colmajor(As[0], rows, cols, dim).cpu().numpy().astype(np.float64)
+            if dim == 1:
+                tmp = np.empty(cols, np.float32)
+                fn = lambda: L.nt2o_inner_fold_f(Ah, rows, cols, 4, tmp.ctypes.data, None, None, 0)
+                how = "NT2's inner_fold: columns over the threads, 4-lane fold per column"
+            else:
+                tmp = np.empty(rows, np.float32)
+                fn = lambda: L.nt2o_outer_fold_nt2_f(Ah, rows, cols, tmp, 0)
+                how = "NT2's in-cache outer_fold: 16-row chunks over the threads, columns added in turn"
+            rate, reps = cpu_rate(fn, rows * cols)
+            res[name] = {
+                "ms": ms, "value": ws * rows * cols / (ms * 1e-3), "unit": "elements/s",
+                "roofline": _roof(4 * rows * cols + 4 * m, ms, peak),
+                "cpu_baseline": _cpu(rate, "elements/s", int(L.nt2o_max_threads()), f"same 8192x4096 table; {how}",
+                                     reps),
+                "error": {"max_err_in_eps_sum_abs": float((np.abs(g - ref64) / (eps * ab)).max()),
+                          "cpu_nt2_fp32_max_err_in_eps_sum_abs":
+                              float((np.abs(cpu32.astype(np.float64) - ref64) / (eps * ab)).max())}}
+        res["l2"] = "4 rotating 134 MB tables, 536 MB > L2"
+        return res
+
+    def bs_f64():
+        n = 1 << 24
+        Sd = torch.empty(n, dtype=torch.float64, device="cuda")
+        Kd = torch.empty(n, dtype=torch.float64, device="cuda")
+        Td = torch.empty(n, dtype=torch.float64, device="cuda")
+        api.fill_uniform(Sd, 5, 30, 1)
+        api.fill_uniform(Kd, 1, 100, 2)
+        api.fill_uniform(Td, 0.25, 10, 3)
+        c = torch.empty_like(Sd)
+        p = torch.empty_like(Sd)
+        ms, _, _ = time_device(lambda: api.blackscholes(Sd, Kd, Td, R, SIGMA, call=c, put=p), K(20), warmup, ws)
+        api.blackscholes(Sd, Kd, Td, R, SIGMA, call=c, put=p)
+        Sh, Kh, Th = (a.cpu().numpy() for a in (Sd, Kd, Td))
+        rc, rp = np.empty(n), np.empty(n)
+        L.nt2o_bs_d(Sh, Kh, Th, R, SIGMA, rc, rp, n, 0)
+        gc, gp = c.cpu().numpy(), p.cpu().numpy()
+        mism = int(np.count_nonzero(gc.view(np.uint64) != rc.view(np.uint64)) +
+                   np.count_nonzero(gp.view(np.uint64) != rp.view(np.uint64)))
+        rate, reps = cpu_rate(lambda: L.nt2o_bs_d(Sh, Kh, Th, R, SIGMA, rc, rp, n, 0), n)
+        th = nt2_threading(L, n, 8)
+        return {"ms": ms, "value": ws * n / (ms * 1e-3), "unit": "options/s",
+                "roofline": _roof(40 * n, ms, peak), "bound_note": "FP64 issue (GB300's FP64 rate), not HBM",
+                "cpu_baseline": _cpu(rate, "options/s", th["threads"], "same 2^24 FP64 options; NT2 double path",
+                                     reps),
+                "error": {"mismatches_vs_fp64_oracle": mism,
+                          "note": "the FP64 oracle is NT2's double arithmetic restated; 0 = bit-exact"}}
+
+    def sigmadelta():
+        batch = video.make_batch(256, 8, seed=11)
+        torch.cuda.synchronize()
+        plan = api.SigmaDeltaPlan(batch, 8, init=True)
+        ms, _, _ = time_device(plan.launch, K(20), warmup, ws)
+        plan.close()
+        torch.cuda.synchronize()
+        frames = [e["frames"].cpu().numpy() for e in batch]
+        npix = np.array([e["width"] * e["height"] for e in batch], np.uint64)
+        fstride = np.array([e["frame_stride"] for e in batch], np.uint64)
+        bk = [np.zeros(int(m), np.uint8) for m in npix]
+        vr = [np.zeros(int(m), np.uint8) for m in npix]
+        lb = [np.zeros(7 * int(m), np.uint8) for m in npix]
+        keep = [(C.c_void_p * len(a))(*[x.ctypes.data for x in a]) for a in (frames, bk, vr, lb)]
+        pf, pb, pv, pl = (C.cast(a, C.c_void_p) for a in keep)
+        run = lambda: L.nt2o_sigmadelta_batch_u8(len(batch), pf, fstride.ctypes.data, npix.ctypes.data, 8, pb,
+                                                 pv, pl, 1, 0)
+        pfr = video.pixel_frames(batch, 8, True)
+        rate, reps = cpu_rate(run, pfr, seconds=3.0, min_reps=3)
+        mism = 0
+        for e, b, v, l in zip(batch, bk, vr, lb):
+            m = e["width"] * e["height"]
+            mism += int(np.count_nonzero(e["bkg"].cpu().numpy() != b) + np.count_nonzero(e["var"].cpu().numpy() != v))
+            gl = e["labels"].cpu().numpy()
+            for f in range(7):
+                lo = f * e["label_stride"]
+                mism += int(np.count_nonzero(gl[lo:lo + m] != l[f * m:(f + 1) * m]))
+        return {"ms": ms, "value": ws * pfr / (ms * 1e-3), "unit": "pixel-frames/s",
+                "roofline": _roof(video.bytes_moved(batch, 8, True), ms, peak),
+                "streams": len(batch), "pixels": int(npix.sum()), "launch": "one persistent kernel in a CUDA graph",
+                "cpu_baseline": _cpu(rate, "pixel-frames/s", int(L.nt2o_max_threads()),
+                                     "same 256 streams x 8 frames; each stream's NT2 statement on one thread "
+                                     "(below NT2's spawner threshold), streams spread over the threads", reps),
+                "error": {"mismatched_bytes_vs_oracle": mism}}
+
+    guarded("saxpy_f32_2^24", saxpy)
+    guarded("sdot_f32_2^26", sdot)
+    guarded("folds_f32_8192x4096", folds)
+    guarded("blackscholes_f64_2^24", bs_f64)
+    guarded("sigmadelta_u8_256x8", sigmadelta)
+    return out
 
 
 # -------------------------------------------------------------- serving
@@ -388,6 +602,21 @@ def run_ours(args):
         mms, _, _ = time_device(make_step(prec), min(args.steps, 500), max(args.warmup, 3), ws)
         gbs = BYTES_PER_OPTION * n / (mms * 1e-3) / 1e9
         modes[name] = {"ms_per_step": mms, "options_per_s": ws * n / (mms * 1e-3), "gb_per_s": gbs}
+    # each mode's results against the FP32 oracle and an FP64 oracle, over the whole batch
+    accuracy = {}
+    S_h = K_h = T_h = None
+    if rank == 0 and not args.no_cpu:
+        from nt2_gb300 import synthetic
+        S_h, K_h, T_h = synthetic.blackscholes_inputs(n, seed=rank)
+        try:
+            ref = BSReference(S_h, K_h, T_h)
+            for name, prec in (("exact", 0), ("fused", 1), ("fast", 2)):
+                make_step(prec)()
+                torch.cuda.synchronize()
+                accuracy[name] = ref.errors(call.cpu().numpy(), put.cpu().numpy())
+            del ref
+        except Exception as e:
+            accuracy = {"error": repr(e)[:300]}
     from nt2_gb300 import replicas
     value = replicas.job_throughput(n, ws, ms * 1e-3)
     peak, peak_kind = peaks()
@@ -437,12 +666,8 @@ def run_ours(args):
     line = {
         "metric": METRIC, "value": value, "unit": "options/s", "n_gpus": ws, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded counter-based uniforms: S~U[5,30], "
-        "K~U[1,100], T~U[0.25,10]; r=0.02, sigma=0.30)",
-        "config": {"workload": "Black-Scholes call+put, FP32, 2^24 options per GPU, normcdf via erfc, "
-                   "NT2 unfused arithmetic (bit-exact with the oracle)",
-                   "options_per_gpu": n, "parallelism": f"replicas x{ws}",
-                   "l2": "inputs+outputs 335 MB > 129 MB L2, no flush needed"},
+        "vs_baseline": None, "dtype": "f32", "data": DATA,
+        "config": headline_config(n, ws),
         "hbm_frac_measured": achieved / peak, "hbm_frac_nominal": achieved / NOMINAL_HBM_GBS,
         "gb_per_s": achieved,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -456,6 +681,7 @@ def run_ours(args):
         "gpu_launches": args.steps,
         "clocks": clocks,
         "precision_modes": modes,
+        "accuracy": accuracy,
         "autotune": tuned,
     }
     peak_v = peak
@@ -463,12 +689,17 @@ def run_ours(args):
         m["hbm_frac_measured"] = m["gb_per_s"] / peak_v
         m["hbm_frac_nominal"] = m["gb_per_s"] / NOMINAL_HBM_GBS
     if rank == 0 and ws == 1 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline()
+        line["cpu_baseline"] = cpu_baseline(S_h, K_h, T_h)
+    del S_h, K_h, T_h
     if rank == 0 and ws == 1 and not args.no_serving:
         try:
             line["serving"] = serving_bench()
         except Exception as e:          # the headline number stands without it
             line["serving"] = {"error": repr(e)}
+    del S, K, T, call, put, Sh, Kh, Th, ch, ph
+    torch.cuda.empty_cache()
+    if rank == 0 and ws == 1 and not args.no_configs:
+        line["configs"] = config_lines(ws, args.steps, max(args.warmup, 3))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if args.suite and rank == 0:
@@ -766,40 +997,41 @@ def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: in
 
 # ---------------------------------------------------------- reference arm
 def run_reference(args):
+    """NT2's Black-Scholes statement on the host cores: the oracle's restatement of NT2's
+    SIMD+OpenMP path (NT2 itself needs Boost, absent on both machines) over the same 2^24-option
+    batch the GPU arm prices, so NT2's spawner takes its OpenMP branch (n > 8 * grain)."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
     import numpy as np
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import oracle_lib
+    from nt2_gb300 import synthetic
+    oracle_lib = _oracle()
     L = oracle_lib.load()
-    sample = 1 << 20
-    rng = np.random.default_rng(1)
-    S = rng.uniform(5, 30, sample).astype(np.float32)
-    K = rng.uniform(1, 100, sample).astype(np.float32)
-    T = rng.uniform(0.25, 10, sample).astype(np.float32)
+    n = N_OPTIONS
+    S, K, T = synthetic.blackscholes_inputs(n, seed=0)
     call = np.empty_like(S)
     put = np.empty_like(S)
-    threads = L.nt2o_max_threads()
+    th = nt2_threading(L, n, 4)
     steps = args.steps
     for _ in range(max(args.warmup, 3)):
-        L.nt2o_bs_f(S, K, T, R, SIGMA, call, put, sample, 0, threads)
+        L.nt2o_bs_f(S, K, T, R, SIGMA, call, put, n, 0, 0)
     t0 = time.perf_counter()
     for _ in range(steps):
-        L.nt2o_bs_f(S, K, T, R, SIGMA, call, put, sample, 0, threads)
+        L.nt2o_bs_f(S, K, T, R, SIGMA, call, put, n, 0, 0)
     t1 = time.perf_counter()
     ms = (t1 - t0) * 1e3 / steps
-    value = sample / (ms * 1e-3)
-    desc = (f"{sample} options per step (1/{N_OPTIONS // sample} of the 2^24-option batch); NT2's SIMD+OpenMP "
-            "Black-Scholes path restated in C (oracle/nt2_oracle.c) because NT2 itself needs Boost, which is "
-            "absent; scalar+OpenMP, as NT2 runs on aarch64 (no Boost.SIMD NEON backend)")
+    value = n / (ms * 1e-3)
+    desc = (f"the full {n}-option batch each step; NT2's SIMD+OpenMP Black-Scholes path restated in C "
+            "(oracle/nt2_oracle.c) because NT2 itself needs Boost, which is absent; scalar+OpenMP, as NT2 "
+            f"runs on aarch64 (no Boost.SIMD NEON backend); NT2's spawner rule: grain {th['grain']} elements "
+            f"(L2 {th['l2_bytes']} B), parallel={th['parallel']}, {th['threads']} threads")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": "options/s", "n_gpus": ws, "steps": steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "Black-Scholes call+put, FP32, normcdf via erfc (bounded CPU sample)",
-                   "options_per_step": sample},
-        "cpu_baseline": {"value": value, "unit": "options/s", "cores": threads, "kind": "port", "sample": desc},
+        "vs_baseline": None, "dtype": "f32", "data": DATA,
+        "config": headline_config(n, 1),
+        "cpu_baseline": {"value": value, "unit": "options/s", "cores": th["threads"], "kind": "port",
+                         "sample": desc, "nt2_threading": th},
         "e2e": {"value": value, "unit": "options/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
 
@@ -813,6 +1045,7 @@ def main():
     ap.add_argument("--suite", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-configs", action="store_true", help="skip the other configurations' measurements")
     ap.add_argument("--case", choices=CASES, help="run one configuration alone (for profiling)")
     ap.add_argument("--no-autotune", action="store_true", help="with --case: default launch shapes")
     ap.add_argument("--tuning", default=None, help="tuning-table text to import first (\"key@bucket unroll waves\" lines)")

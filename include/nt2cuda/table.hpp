@@ -444,10 +444,15 @@ template <class E> inline auto if_zero_else_one(const xpr<E>& c)
 // ------------------------------------------------------- evaluation
 template <class T> template <class E> table<T>& table<T>::operator=(const xpr<E>& x)
 {
-  // resize: inputs were captured as device pointers when the tree was built
-  if (x.size.numel() != numel()) {
-    if (numel()) throw std::invalid_argument("nt2cuda: assignment to a table of another size");
-    resize(x.size);
+  // NT2 resizes the left-hand side to the right-hand side's extent before
+  // evaluating (modules/core/base/include/nt2/dsl/functions/elementwise/run.hpp:32).
+  // The same number of elements in another shape keeps the buffer (the tree
+  // may read this table: its device pointer was captured when the tree was
+  // built); another number of elements gets a new buffer (an elementwise
+  // tree of that size cannot read this table).
+  if (x.size.d[0] != sz_.d[0] || x.size.d[1] != sz_.d[1]) {
+    if (x.size.numel() == numel()) sz_ = x.size;
+    else resize(x.size);
   }
   T* out = device();
   auto p = make_prog(assign<T, E>{out, x.e});
@@ -516,16 +521,18 @@ template <class X, std::enable_if_t<is_operand_v<X>, int> = 0> inline auto globa
   using V = typename decltype(e)::value_type;
   using A = std::conditional_t<std::is_floating_point<V>::value, V, double>;
   static_assert(std::is_same<A, float>::value || std::is_same<A, double>::value, "globalsum: float or double");
-  A* d = nullptr;
-  check(cudaMalloc(&d, sizeof(A)), "globalsum alloc");
+  // the device scalar lives in the stream's own scratch (allocated by the
+  // first reduction on the stream, reused after): no allocation per call
   cudaStream_t s = settings().stream;
+  void* scratch = nullptr;
+  check(stream_scratch(s, sizeof(A), &scratch, kResultSlot), "globalsum scratch");
+  A* d = static_cast<A*>(scratch);
   cudaError_t err = (std::is_same<A, float>::value && settings().compensated)
                         ? fold::inner_fold<fold::op_sum<true>, A>(e.e, e.size.numel(), 1, d, s)
                         : fold::inner_fold<fold::op_sum<false>, A>(e.e, e.size.numel(), 1, d, s);
   A r = 0;
   if (err == cudaSuccess) err = cudaMemcpyAsync(&r, d, sizeof(A), cudaMemcpyDeviceToHost, s);
   if (err == cudaSuccess) err = cudaStreamSynchronize(s);
-  cudaFree(d);
   check(err, "globalsum");
   return (V)r;
 }
@@ -592,14 +599,14 @@ template <class Op, class X> inline auto reduce_all(const X& x, const char* what
   auto e = as_xpr(x);
   using V = typename decltype(e)::value_type;
   using O = fold::out_of<Op, V>;
-  O* d = nullptr;
-  check(cudaMalloc(&d, sizeof(O)), what);
   cudaStream_t s = settings().stream;
+  void* scratch = nullptr;                       // the stream's result slot, as globalsum
+  check(stream_scratch(s, sizeof(O), &scratch, kResultSlot), what);
+  O* d = static_cast<O*>(scratch);
   cudaError_t err = fold::inner_fold<Op, V>(e.e, e.size.numel(), 1, d, s);
   O r{};
   if (err == cudaSuccess) err = cudaMemcpyAsync(&r, d, sizeof(O), cudaMemcpyDeviceToHost, s);
   if (err == cudaSuccess) err = cudaStreamSynchronize(s);
-  cudaFree(d);
   check(err, what);
   return r;
 }

@@ -26,7 +26,9 @@ struct scratch_pool {
 inline scratch_pool& global_scratch_pool() { static scratch_pool p; return p; }
 
 // slot 0: fold arrival counters only; slot 1: per-call data (batched-launch
-// descriptors, scan flags and carries); slot 2: fold partials.
+// descriptors, scan flags and carries); slot 2: fold partials; slot 3
+// (kResultSlot): device results the C++ front end reads back (globalsum).
+constexpr int kResultSlot = 3;
 inline cudaError_t stream_scratch(cudaStream_t s, size_t bytes, void** out, int slot = 0);
 
 // The two buffers of a fold: ncounters zero-valued arrival counters and room

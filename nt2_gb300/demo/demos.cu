@@ -19,6 +19,8 @@
 //              w = cbrt(x) + logspace_add(x, y)
 //   trigx      y = csc(x) + asind(x*1e-3f) + secpi(x): composed trigonometric functors;
 //              w = cot(x) + sind(x) + tanpi(x*0.01f)
+//   reshape    assignments that change the left-hand table's extent, and
+//              repeated globalsum on one stream
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -214,6 +216,28 @@ int main(int argc, char** argv)
     write_table(argv[5], background_img);
     write_table(argv[6], image_variance);
     write_table(argv[7], binary_label);
+  } else if (cmd == "reshape") {                          // n = rows; argv[3] = cols; in: A ; out: B1 B2 B3
+    // NT2's assignment takes the right-hand side's extent (elementwise/run.hpp:32):
+    // B = A*2+1 sizes B as A; B = At+1 (same elements, cols x rows) reshapes B in
+    // place; B = C*3 (another size) reallocates it; globalsum twice on one stream.
+    typedef float T;
+    const std::size_t rows = n, cols = std::strtoull(argv[3], nullptr, 10);
+    std::vector<T> a = read_file<T>(argv[4], rows * cols);
+    nt2::table<T> A(nt2::of_size(rows, cols)), At(nt2::of_size(cols, rows)), C(nt2::of_size(5, 7)), B;
+    load(A, a);
+    load(At, a);
+    for (std::size_t i = 1; i <= 35; ++i) C(i) = T(i);
+    B = A * T(2) + T(1);
+    std::printf("B1 %zu %zu\n", B.height(), B.width());
+    write_table(argv[5], B);
+    B = At + T(1);
+    std::printf("B2 %zu %zu\n", B.height(), B.width());
+    write_table(argv[6], B);
+    B = C * T(3);
+    std::printf("B3 %zu %zu\n", B.height(), B.width());
+    write_table(argv[7], B);
+    const T g1 = nt2::globalsum(C), g2 = nt2::globalsum(C * C);
+    std::printf("G %.9g %.9g\n", (double)g1, (double)g2);
   } else {
     std::fprintf(stderr, "unknown demo %s\n", cmd.c_str());
     return 2;

@@ -198,3 +198,26 @@ def test_io_demo(demos, tmp_path):
     B, ext = tableio.load(dst)
     assert ext == (rows, cols)
     assert np.array_equal(B, A * 2.0 + 1.0)
+
+
+def test_reshape_demo(demos, tmp_path):
+    """B = expr takes the right-hand side's extent (NT2's run_assign resizes the lhs):
+    same element count in another shape, then another element count."""
+    rows, cols = 37, 11
+    A = np.arange(rows * cols, dtype=np.float32) * 0.5 - 3
+    f = tmp_path / "A"
+    A.tofile(f)
+    outs = [tmp_path / f"B{k}" for k in (1, 2, 3)]
+    r = subprocess.run([demos, "reshape", str(rows), str(cols), str(f), *map(str, outs)], capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    lines = dict((l.split()[0], l.split()[1:]) for l in r.stdout.splitlines())
+    assert lines["B1"] == [str(rows), str(cols)]
+    assert lines["B2"] == [str(cols), str(rows)]
+    assert lines["B3"] == ["5", "7"]
+    assert np.array_equal(np.fromfile(outs[0], np.float32), A * np.float32(2) + np.float32(1))
+    assert np.array_equal(np.fromfile(outs[1], np.float32), A + np.float32(1))
+    C = np.arange(1, 36, dtype=np.float32)
+    assert np.array_equal(np.fromfile(outs[2], np.float32), C * np.float32(3))
+    assert float(lines["G"][0]) == float(C.sum())
+    assert float(lines["G"][1]) == float((C.astype(np.float64) ** 2).sum())
