@@ -32,7 +32,8 @@ N_OPTIONS = 1 << 24
 R, SIGMA = 0.02, 0.30
 BYTES_PER_OPTION = 20            # S, K, T read; call, put written (float32)
 NOMINAL_HBM_GBS = 8000.0
-INFLIGHT = 3                     # launches in flight, for both serving modes
+INFLIGHT = 3                     # launches in flight, for both launching serving modes
+MODES = ("resident", "batched", "launch_per_request")
 
 
 def peaks():
@@ -512,8 +513,9 @@ def config_lines(ws: int, steps: int, warmup: int) -> dict:
 # -------------------------------------------------------------- serving
 def serving_bench(seconds: float = 1.0, rates=(1000, 5000, 10000, 20000, 50000), seed: int = 7):
     """Poisson arrivals of Black-Scholes requests (sizes log-uniform 256..2^22 options) into the
-    continuous-batching server and into a one-launch-per-request server on the same GPU, both
-    allowed the same number of launches in flight.  The trace is replayed natively
+    server's three modes on the same GPU: a resident kernel draining a request ring, one launch
+    per step over the admitted requests, and one launch per request (the last two allowed the
+    same number of launches in flight).  The trace is replayed natively
     (nt2cuda_server_replay): arrivals, completion waits and releases run in C++ threads, so the
     numbers are the server's, not a Python client's."""
     import numpy as np
@@ -527,9 +529,9 @@ def serving_bench(seconds: float = 1.0, rates=(1000, 5000, 10000, 20000, 50000),
     out = {}
 
     def replay(mode, sizes, offs, arrivals):
-        coalesce = mode == "batched"
         srv = Server(budget_bytes=40 << 30, max_batch_requests=4096, max_inflight_batches=INFLIGHT,
-                     coalesce=coalesce)
+                     mode={"resident": "resident", "batched": "batched", "launch_per_request": "launch"}[mode],
+                     wait_timeout_ms=20000)
         lat, elapsed = srv.replay(sp, kp, tp, R, SIGMA, offs, sizes, arrivals)
         st = srv.stats()
         srv.close()
@@ -545,15 +547,16 @@ def serving_bench(seconds: float = 1.0, rates=(1000, 5000, 10000, 20000, 50000),
         sizes = np.exp(rng.uniform(math.log(256), math.log(1 << 22), nreq)).astype(np.uint64)
         offs = ((rng.integers(0, pool_n - (1 << 22), nreq) // 4) * 4).astype(np.uint64)
         arrivals = (np.cumsum(rng.exponential(1.0 / rate, nreq)) * 1e9).astype(np.uint64)
-        out[f"{rate}_req_s"] = {m: replay(m, sizes, offs, arrivals) for m in ("batched", "launch_per_request")}
+        out[f"{rate}_req_s"] = {m: replay(m, sizes, offs, arrivals) for m in MODES}
     # saturation: every request offered at once (small requests, where launch cost dominates)
     sat_rng = np.random.default_rng(seed + 1)
     nreq, lo, hi = 20000, 256, 1 << 14
     sizes = np.exp(sat_rng.uniform(math.log(lo), math.log(hi), nreq)).astype(np.uint64)
     offs = ((sat_rng.integers(0, pool_n - hi, nreq) // 4) * 4).astype(np.uint64)
     zero = np.zeros(nreq, np.uint64)
-    sat = {m: replay(m, sizes, offs, zero) for m in ("batched", "launch_per_request")}
-    sat["throughput_ratio"] = sat["batched"]["options_per_s"] / sat["launch_per_request"]["options_per_s"]
+    sat = {m: replay(m, sizes, offs, zero) for m in MODES}
+    for m in ("resident", "batched"):
+        sat[f"throughput_ratio_{m}"] = sat[m]["options_per_s"] / sat["launch_per_request"]["options_per_s"]
     out["saturation_small_requests"] = sat
     out["inflight_launches_both_modes"] = INFLIGHT
     return out

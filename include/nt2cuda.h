@@ -450,6 +450,16 @@ nt2cuda_status nt2cuda_selftest_wait_timeout(nt2cuda_stream stream);
 nt2cuda_status nt2cuda_selftest_fold_timeout(const float* A, size_t rows, size_t cols, float* out,
                                              nt2cuda_stream stream);
 
+/* No counterpart in the reference.  The exact FP32 Black-Scholes kernel prices
+ * two options at a time on the packed FP32 instructions; this checks its
+ * two-lane functors against the one-lane ones over every float argument
+ * (2^32 values): which = 0 exp, 1 log, 2 erfc of |a|, 3 normcdf(a) with
+ * normcdf(-a).  *mismatches = arguments whose results differ in any bit (two
+ * NaNs are equal); first_bad (8 entries, may be NULL) gets the first ones'
+ * bit patterns.  Synchronous. */
+nt2cuda_status nt2cuda_selftest_x2(int which, unsigned long long* mismatches, uint32_t* first_bad,
+                                   nt2cuda_stream stream);
+
 /* --------------------------------------------------------- sigmadelta ---- */
 /* One grey video stream for the batched sigma-delta background subtraction
  * (demo/sigmadelta/nt2/sigmadelta_nt2.cpp:37-58, 85-106).  frames holds
@@ -490,12 +500,17 @@ nt2cuda_status nt2cuda_sigmadelta_plan_destroy(nt2cuda_sd_plan* plan);
  * against budget_bytes and stay resident until nt2cuda_server_release.
  * coalesce = 1 launches every admitted request of a step in one kernel over a
  * (request, tile) work-list; 0 launches one kernel per request.  At most
- * max_inflight_batches launches are on the device at once. */
+ * max_inflight_batches launches are on the device at once.  coalesce = 2
+ * keeps one kernel on the device that drains a ring of requests published in
+ * pinned host memory: requests that arrive while it runs join it without a
+ * launch; it leaves after 20 ms without requests (every wait it makes is
+ * bounded in time) and is launched again by the next request. */
 typedef struct {
   size_t budget_bytes;        /* device memory for request outputs          */
   int max_batch_requests;     /* requests coalesced into one launch         */
   int max_inflight_batches;   /* launches on the device at once (streams)   */
-  int coalesce;               /* 1 = batched work-list, 0 = launch per request */
+  int coalesce;               /* 2 = resident kernel, 1 = batched work-list,
+                                 0 = launch per request                     */
   int fused;                  /* precision mode: 0 exact, 1 fused, 2 fast   */
   int cdf_kind;               /* 0 = normcdf, 1 = fastnormcdf               */
   int wait_timeout_ms;        /* default bound of waits (<= 0: 60000)       */

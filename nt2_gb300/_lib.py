@@ -95,6 +95,7 @@ _SIGS = {
     "nt2cuda_map2_f64": (c_int, [c_int, c_vp, c_vp, c_vp, c_size, c_int, c_vp]),
     "nt2cuda_selftest_wait_timeout": (c_int, [c_vp]),
     "nt2cuda_selftest_fold_timeout": (c_int, [c_vp, c_size, c_size, c_vp, c_vp]),
+    "nt2cuda_selftest_x2": (c_int, [c_int, C.POINTER(C.c_ulonglong), C.POINTER(C.c_uint32), c_vp]),
     "nt2cuda_scan_f64": (c_int, [c_int, c_vp, c_size, c_size, c_int, c_vp, c_int, c_vp]),
     "nt2cuda_rgb2grey_u8": (c_int, [c_vp, c_vp, c_vp, c_vp, c_size, c_int, c_vp]),
     "nt2cuda_rgb2yuv_f32": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_size, c_int, c_vp]),

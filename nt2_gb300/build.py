@@ -28,6 +28,7 @@ SOURCES = [
     "capi_scan.cu",
     "server.cu",
     "capi_noalloc.cu",
+    "capi_selftest.cu",
     "capi_trig_f32.cu",
     "capi_trig_f64.cu",
     "capi_expfam_f32.cu",

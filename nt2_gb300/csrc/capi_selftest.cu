@@ -1,0 +1,94 @@
+// capi_selftest.cu -- exhaustive checks that the two-lane forms of NT2's
+// float functors (nt2cuda/bs_x2.cuh) give the one-lane forms' bits
+// (nt2cuda/math.cuh) for every float argument.
+//
+// Each check runs one kernel over all 2^32 float bit patterns (2^31 pairs),
+// compares the packed result of both lanes with the scalar functor bit for
+// bit (two NaNs count as equal: the results' contract covers NaN-ness, not
+// payloads) and counts the differences.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "internal.cuh"
+#include "nt2cuda/bs_x2.cuh"
+#include "nt2cuda/launch.cuh"
+#include "nt2cuda/math.cuh"
+
+using namespace nt2cuda;
+using namespace nt2cuda::detail_capi;
+
+namespace {
+
+__device__ __forceinline__ bool same(float a, float b)
+{
+  return __float_as_uint(a) == __float_as_uint(b) || (a != a && b != b);
+}
+
+struct x2_report {
+  unsigned long long mismatches;
+  uint32_t first[8];
+};
+
+__device__ __forceinline__ void record(x2_report* rep, uint32_t u)
+{
+  const unsigned long long k = atomicAdd(&rep->mismatches, 1ull);
+  if (k < 8) rep->first[k] = u;
+}
+
+// which: 0 exp, 1 log, 2 erfc of |a|, 3 normcdf(a) and normcdf(-a)
+__global__ void __launch_bounds__(256) k_x2_check(int which, uint64_t pairs, x2_report* rep)
+{
+  for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < pairs; p += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t u0 = (uint32_t)(2 * p), u1 = u0 + 1;
+    const float2 a = make_float2(__uint_as_float(u0), __uint_as_float(u1));
+    if (which == 0) {
+      const float2 r = x2::exp(a);
+      if (!same(r.x, math::exp<false>(a.x))) record(rep, u0);
+      if (!same(r.y, math::exp<false>(a.y))) record(rep, u1);
+    } else if (which == 1) {
+      const float2 r = x2::log(a);
+      if (!same(r.x, math::log<false>(a.x))) record(rep, u0);
+      if (!same(r.y, math::log<false>(a.y))) record(rep, u1);
+    } else if (which == 2) {
+      const float2 x = make_float2(fabsf(a.x), fabsf(a.y));
+      const float2 r = x2::erfc_abs(x);
+      if (!same(r.x, math::erfc_abs<false>(x.x))) record(rep, u0);
+      if (!same(r.y, math::erfc_abs<false>(x.y))) record(rep, u1);
+    } else {
+      float2 pos, neg;
+      x2::normcdf_pair(a, pos, neg);
+      float p0, n0, p1, n1;
+      math::normcdf_pair<false>(a.x, p0, n0);
+      math::normcdf_pair<false>(a.y, p1, n1);
+      if (!same(pos.x, p0) || !same(neg.x, n0)) record(rep, u0);
+      if (!same(pos.y, p1) || !same(neg.y, n1)) record(rep, u1);
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" nt2cuda_status nt2cuda_selftest_x2(int which, unsigned long long* mismatches, uint32_t* first_bad,
+                                              nt2cuda_stream stream)
+{
+  NT2CUDA_NVTX_RANGE;
+  if (which < 0 || which > 3 || !mismatches) return NT2CUDA_ERR_ARG;
+  cudaStream_t s = as_stream(stream);
+  x2_report* rep = nullptr;
+  cudaError_t e = cudaMalloc(&rep, sizeof(x2_report));
+  if (e != cudaSuccess) return from_cuda(e);
+  e = cudaMemsetAsync(rep, 0, sizeof(x2_report), s);
+  if (e == cudaSuccess) {
+    const uint64_t pairs = (uint64_t)1 << 31;
+    k_x2_check<<<(unsigned)(sm_count() * 8), 256, 0, s>>>(which, pairs, rep);
+    e = cudaGetLastError();
+  }
+  x2_report h{};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, rep, sizeof(h), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(rep);
+  if (e != cudaSuccess) return from_cuda(e);
+  *mismatches = h.mismatches;
+  if (first_bad)
+    for (int i = 0; i < 8; ++i) first_bad[i] = h.first[i];
+  return NT2CUDA_OK;
+}

@@ -17,8 +17,12 @@
 // The proto optimizer's a + b*c -> fma(b,c,a) rewrite
 // (modules/boost/simd/base/include/boost/simd/operator/functions/optimize/plus.hpp:20-45)
 // applies to log(S/K) + c*T, which is why that sum is a madd.
+//
+// Exact FP32 normcdf options are priced two at a time on the packed FP32
+// instructions (nt2cuda/bs_x2.cuh), bit-identical to bs_lane.
 #pragma once
 #include <cuda_runtime.h>
+#include "bs_x2.cuh"
 #include "math.cuh"
 #include "memory.cuh"
 
@@ -72,6 +76,10 @@ __device__ __forceinline__ void bs_lane(T S, T K, T Tm, T r, T v, T c, T& call, 
   put = nmsub<F>(S, m1, mul(e, m2));
 }
 
+// Statements priced two options at a time (bs_x2.cuh): exact FP32 with normcdf.
+template <class T, int CDF, int P>
+constexpr bool kPacked = sizeof(T) == 4 && CDF == CDF_NORMCDF && P == PREC_EXACT;
+
 // V options per thread per group (16 bytes of each input), U groups in
 // flight per grid-stride trip.
 template <class T, int CDF, int P, int U>
@@ -99,8 +107,19 @@ __global__ void __launch_bounds__(256) k_blackscholes(const T* __restrict__ S, c
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       T oc[V], op[V];
+      if constexpr (kPacked<T, CDF, P>) {
 #pragma unroll
-      for (int l = 0; l < V; ++l) bs_lane<T, CDF, P>(s[u][l], k[u][l], t[u][l], r, v, c, oc[l], op[l]);
+        for (int l = 0; l < V; l += 2) {
+          float2 pc, pp;
+          x2::blackscholes(make_float2(s[u][l], s[u][l + 1]), make_float2(k[u][l], k[u][l + 1]),
+                           make_float2(t[u][l], t[u][l + 1]), r, v, c, pc, pp);
+          oc[l] = pc.x; oc[l + 1] = pc.y;
+          op[l] = pp.x; op[l + 1] = pp.y;
+        }
+      } else {
+#pragma unroll
+        for (int l = 0; l < V; ++l) bs_lane<T, CDF, P>(s[u][l], k[u][l], t[u][l], r, v, c, oc[l], op[l]);
+      }
       size_t i = (g + (size_t)u * stride) * V;
       mem::store_vec<T, V>(call, i, oc);
       mem::store_vec<T, V>(put, i, op);
@@ -113,8 +132,19 @@ __global__ void __launch_bounds__(256) k_blackscholes(const T* __restrict__ S, c
     mem::load_vec<T, V, true>(S, i, s);
     mem::load_vec<T, V, true>(K, i, k);
     mem::load_vec<T, V, true>(Tm, i, t);
+    if constexpr (kPacked<T, CDF, P>) {
 #pragma unroll
-    for (int l = 0; l < V; ++l) bs_lane<T, CDF, P>(s[l], k[l], t[l], r, v, c, oc[l], op[l]);
+      for (int l = 0; l < V; l += 2) {
+        float2 pc, pp;
+        x2::blackscholes(make_float2(s[l], s[l + 1]), make_float2(k[l], k[l + 1]), make_float2(t[l], t[l + 1]), r,
+                         v, c, pc, pp);
+        oc[l] = pc.x; oc[l + 1] = pc.y;
+        op[l] = pp.x; op[l + 1] = pp.y;
+      }
+    } else {
+#pragma unroll
+      for (int l = 0; l < V; ++l) bs_lane<T, CDF, P>(s[l], k[l], t[l], r, v, c, oc[l], op[l]);
+    }
     mem::store_vec<T, V>(call, i, oc);
     mem::store_vec<T, V>(put, i, op);
   }

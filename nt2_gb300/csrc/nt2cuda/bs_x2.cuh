@@ -1,0 +1,243 @@
+// nt2cuda/bs_x2.cuh -- NT2's float exp, log, erfc and normcdf, two lanes at
+// a time on Blackwell's packed FP32 instructions, bit-identical to the
+// one-lane forms of math.cuh.
+//
+// sm_100-family SMs execute add.rn.f32x2 / mul.rn.f32x2 on a 64-bit
+// register pair at the issue cost of one scalar FP32 instruction, each half
+// rounded exactly as the scalar add or multiply.  NT2's exact arithmetic is
+// nothing but correctly rounded adds, multiplies, divisions and square roots
+// (its fma/fnms are a*b+c rounded twice), so the same sequence run on
+// register pairs gives, lane by lane, the same bits for half the issue
+// slots.  What does not pack stays per lane: comparisons, selects,
+// exponent-bit arithmetic and the special-function unit.
+//
+// Beyond packing, the steps below are rearranged only where the result is
+// provably the same:
+//  * rint(v) for |v| <= 2^22 is (v + 1.5*2^23) - 1.5*2^23, and the sum's low
+//    bits are the integer itself, so exp needs neither the FP32-to-integer
+//    conversion nor the round instruction (both on the slow XU pipe); lanes
+//    outside that range are the ones exp's selections replace.
+//  * exp's `a0 != a0 ? a0 : r` is dropped: a NaN argument already makes the
+//    computed r NaN (NaN payloads are not part of the results' contract; the
+//    CPU and the GPU make different ones).
+//  * z = x/(1+x) inside erfc uses one reciprocal approximation, a Newton step
+//    and Markstein's correction of the quotient (P. Markstein, "IA-64 and
+//    Elementary Functions", 2000: with y within half an ulp of 1/b and q
+//    within an ulp of a/b, q + (a - b q) y rounds to a/b); x is first clamped
+//    to 2^64, where x/(1+x) is already exactly 1, which keeps every step
+//    normal.  The quotient, and erfc as a whole, are checked bit for bit
+//    against the one-lane form over every non-negative float.
+//  * log takes a branch-free path when every lane of the warp has a positive,
+//    normal, finite argument (no denormal rescale, no special values) and the
+//    one-lane form otherwise.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "math.cuh"
+
+namespace nt2cuda {
+namespace x2 {
+
+using math::fbits;
+using math::cf;
+
+// add, sub, mul and fma are spelled in PTX with an explicit rounding
+// modifier.  Unlike the scalar forms, that does not keep ptxas from merging
+// a packed multiply whose only use is a packed add or subtract into one
+// fused operation, which rounds once and changes NT2's twice-rounded result
+// (seen on sm_103a with CUDA 13.0; -fmad=false does not stop it).  So every
+// product that is an operand of an add or a subtract is formed by mul_r:
+// fma(a, b, z) with z = -0 read from constant memory, which is a*b rounded
+// once (a*b + (-0) is a*b, the sign of a zero product included) and which
+// the code generator cannot merge with the add, since it does not know z.
+// Plain mul is kept for products that feed only multiplies, divisions,
+// comparisons and selections.
+__constant__ float c_x2_negzero = -0.0f;
+
+__device__ __forceinline__ float2 splat(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add(float2 a, float2 b)
+{
+  float2 r;
+  asm("{.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
+      "add.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;}"
+      : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+__device__ __forceinline__ float2 sub(float2 a, float2 b)
+{
+  float2 r;
+  asm("{.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
+      "sub.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;}"
+      : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+__device__ __forceinline__ float2 mul(float2 a, float2 b)
+{
+  float2 r;
+  asm("{.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
+      "mul.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;}"
+      : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+__device__ __forceinline__ float2 fma(float2 a, float2 b, float2 c)
+{
+  float2 r;
+  asm("{.reg .b64 a, b, c, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\tmov.b64 c, {%6, %7};\n\t"
+      "fma.rn.f32x2 d, a, b, c;\n\tmov.b64 {%0, %1}, d;}"
+      : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return r;
+}
+// a*b rounded once, as an operand of a later add or subtract (see above)
+__device__ __forceinline__ float2 mul_r(float2 a, float2 b) { return fma(a, b, splat(c_x2_negzero)); }
+// NT2's fma / fnms: a*b+c and c-a*b, each rounded twice
+__device__ __forceinline__ float2 madd(float2 a, float2 b, float2 c) { return add(mul_r(a, b), c); }
+__device__ __forceinline__ float2 nmsub(float2 a, float2 b, float2 c) { return sub(c, mul_r(a, b)); }
+
+template <int N>
+__device__ __forceinline__ float2 horner(float2 x, const uint32_t (&c)[N])
+{
+  float2 acc = splat(fbits(c[0]));
+#pragma unroll
+  for (int i = 1; i < N; ++i) acc = madd(x, acc, splat(fbits(c[i])));
+  return acc;
+}
+
+constexpr float kRound = 12582912.0f;   // 1.5 * 2^23
+
+// 2^k as a float from t = k + 1.5*2^23 (|k| <= 127): the low bits of t's
+// pattern are k, and (k + 127) << 23 is the pattern of 2^k.
+__device__ __forceinline__ float scale_from_rounded(float t)
+{
+  return __uint_as_float((__float_as_uint(t) << 23) + 0x3f800000u);
+}
+
+// exp's reduction and polynomial (math::exp) before its selections:
+// returns c * 2^k with k = rint(a0 / ln 2); exact for minlog < a0 < maxlog.
+__device__ __forceinline__ float2 exp_core(float2 a0)
+{
+  constexpr uint32_t P[5] = {0x3ab778cfu, 0x3c098d8bu, 0x3d2aa957u, 0x3e2aa9a5u, 0x3f000000u};
+  const float2 t = add(mul_r(splat(fbits(cf::invlog_2)), a0), splat(kRound));
+  const float2 k = sub(t, splat(kRound));
+  float2 x = nmsub(k, splat(fbits(cf::log_2hi)), a0);
+  x = nmsub(k, splat(fbits(cf::log_2lo)), x);
+  const float2 y = horner(x, P);
+  const float2 c = add(madd(y, mul(x, x), x), splat(1.0f));
+  return mul(c, make_float2(scale_from_rounded(t.x), scale_from_rounded(t.y)));
+}
+
+// NT2's float exp (math::exp), two lanes.
+__device__ __forceinline__ float2 exp(float2 a0)
+{
+  float2 r = exp_core(a0);
+  const float lo = fbits(cf::minlog), hi = fbits(cf::maxlog), inf = __int_as_float(0x7f800000);
+  r.x = (a0.x <= lo) ? 0.0f : r.x;
+  r.y = (a0.y <= lo) ? 0.0f : r.y;
+  r.x = (a0.x >= hi) ? inf : r.x;
+  r.y = (a0.y >= hi) ? inf : r.y;
+  return r;
+}
+
+// NT2's float log (math::log), two lanes.
+__device__ __forceinline__ bool log_fast_ok(float a)
+{
+  return __float_as_uint(a) - 0x00800000u < 0x7f000000u;   // positive, normal, finite
+}
+__device__ __forceinline__ float2 log(float2 a0)
+{
+  if (!__all_sync(__activemask(), log_fast_ok(a0.x) && log_fast_ok(a0.y)))
+    return make_float2(math::log<false>(a0.x), math::log<false>(a0.y));
+  constexpr uint32_t P[8] = {0xbda5dff0u, 0x3e0229f9u, 0xbe04d6b7u, 0x3e116e80u,
+                             0xbe2a6aa0u, 0x3e4cd0a3u, 0xbe800064u, 0x3eaaaaa9u};
+  const uint32_t u0 = __float_as_uint(a0.x), u1 = __float_as_uint(a0.y);
+  float2 x = make_float2(__uint_as_float((u0 & 0x007fffffu) | 0x3f000000u),
+                         __uint_as_float((u1 & 0x007fffffu) | 0x3f000000u));   // fast_frexp mantissa
+  const bool lt0 = x.x < fbits(cf::sqrt_2o_2), lt1 = x.y < fbits(cf::sqrt_2o_2);
+  // fe = e, or e - 1 below sqrt(2)/2, e = biased exponent - 126, as a float:
+  // (e + 1.5*2^23) - 1.5*2^23, the integer placed in the sum's low bits
+  const float2 fe = sub(make_float2(__uint_as_float((u0 >> 23) + (0x4b400000u - 126u) - (lt0 ? 1u : 0u)),
+                                    __uint_as_float((u1 >> 23) + (0x4b400000u - 126u) - (lt1 ? 1u : 0u))),
+                        splat(kRound));
+  x = sub(mul_r(x, make_float2(lt0 ? 2.0f : 1.0f, lt1 ? 2.0f : 1.0f)), splat(1.0f));
+  const float2 x2 = mul(x, x);
+  float2 y = mul_r(mul(horner(x, P), x), x2);
+  y = madd(fe, splat(fbits(cf::log_2lo)), y);
+  y = madd(splat(-0.5f), x2, y);
+  return madd(splat(fbits(cf::log_2hi)), fe, add(add(x, y), splat(0.0f)));
+}
+
+// x/(1+x) for x >= 0 (and NaN), as __fdiv_rn(x, 1+x) with x clamped to 2^64
+// (see the header comment); the reciprocals are per lane.
+__device__ __forceinline__ float2 x_over_1px(float2 x)
+{
+  const float2 a = make_float2(fminf(x.x, 18446744073709551616.0f), fminf(x.y, 18446744073709551616.0f));
+  const float2 b = add(splat(1.0f), a);
+  float2 y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y.x) : "f"(b.x));
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y.y) : "f"(b.y));
+  const float2 nb = make_float2(-b.x, -b.y);
+  const float2 e = fma(nb, y, splat(1.0f));
+  y = fma(y, e, y);
+  const float2 q = mul(a, y);
+  const float2 r = fma(nb, q, a);
+  return fma(r, y, q);
+}
+
+// NT2's float erfc of x = |a| (math::erfc_abs), two lanes, both regions
+// computed and the right one selected per lane.
+__device__ __forceinline__ float2 erfc_abs(float2 x)
+{
+  constexpr uint32_t P3[9] = {0x41aa8e55u, 0x401b5680u, 0xc010d956u, 0x3f2cff3bu,
+                              0xc016c985u, 0xbffc9284u, 0xbfa11698u, 0xbe036d7eu, 0x3f7ffffeu};
+  constexpr uint32_t P2[11] = {0xc0283611u, 0x40d67e3bu, 0xc0cd1a85u, 0x4050b063u,
+                               0xbfaea865u, 0x3e2006f0u, 0x3e1175c7u, 0x3ec4ca6eu,
+                               0x3e243828u, 0xbf918a62u, 0x3f0a0e8bu};
+  const float2 z = x_over_1px(x);
+  const float2 small = mul(sub(splat(1.0f), z), horner(z, P3));
+  // exp(-x*x): the argument is <= 0, so only the underflow selection applies
+  const float2 m = mul_r(x, x);
+  const float2 na = make_float2(-m.x, -m.y);
+  float2 ex = exp_core(na);
+  const float lo = fbits(cf::minlog);
+  ex.x = (na.x <= lo) ? 0.0f : ex.x;
+  ex.y = (na.y <= lo) ? 0.0f : ex.y;
+  const float2 large = mul(ex, horner(sub(z, splat(0.4f)), P2));
+  const float inf = __int_as_float(0x7f800000), two3 = fbits(cf::twothird);
+  float2 r;
+  r.x = (x.x < two3) ? small.x : large.x;
+  r.y = (x.y < two3) ? small.y : large.y;
+  r.x = (x.x == inf) ? 0.0f : r.x;
+  r.y = (x.y == inf) ? 0.0f : r.y;
+  return r;
+}
+
+// normcdf(a) and normcdf(-a) from one erfc core (math::normcdf_pair), two lanes.
+__device__ __forceinline__ void normcdf_pair(float2 a0, float2& pos, float2& neg)
+{
+  const float2 y = mul(splat(-fbits(cf::sqrt_2o_2)), a0);
+  const float2 r1 = erfc_abs(make_float2(fabsf(y.x), fabsf(y.y)));
+  const float2 two_m = sub(splat(2.0f), r1);
+  pos = mul(splat(0.5f), make_float2((y.x < 0.0f) ? two_m.x : r1.x, (y.y < 0.0f) ? two_m.y : r1.y));
+  neg = mul(splat(0.5f), make_float2((y.x > 0.0f) ? two_m.x : r1.x, (y.y > 0.0f) ? two_m.y : r1.y));
+}
+
+// The Black-Scholes statement of nt2cuda/blackscholes.cuh (exact mode,
+// normcdf via erfc) for two options; c = fma(sqr(v), 0.5, r).
+__device__ __forceinline__ void blackscholes(float2 S, float2 K, float2 T, float r, float v, float c, float2& call,
+                                             float2& put)
+{
+  const float2 da = make_float2(__fsqrt_rn(T.x), __fsqrt_rn(T.y));
+  const float2 vda = mul_r(splat(v), da);
+  const float2 q = make_float2(__fdiv_rn(S.x, K.x), __fdiv_rn(S.y, K.y));
+  const float2 num = madd(splat(c), T, log(q));
+  const float2 d1 = make_float2(__fdiv_rn(num.x, vda.x), __fdiv_rn(num.y, vda.y));
+  const float2 d2 = sub(d1, vda);
+  const float2 e = mul(K, exp(mul_r(splat(-r), T)));
+  float2 n1, m1, n2, m2;
+  normcdf_pair(d1, n1, m1);
+  normcdf_pair(d2, n2, m2);
+  call = nmsub(e, n2, mul_r(S, n1));
+  put = nmsub(S, m1, mul_r(e, m2));
+}
+
+}  // namespace x2
+}  // namespace nt2cuda

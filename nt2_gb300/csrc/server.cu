@@ -8,11 +8,13 @@
 // each step into one launch over a (request, tile) work-list.  Up to
 // max_inflight_batches launches are on the device at once (one stream each),
 // so requests that arrive while a batch runs are admitted and launched
-// without waiting for it.  All waiting happens on the host with bounded
-// waits; no kernel spins.
+// without waiting for it.  All waiting of these two modes happens on the
+// host with bounded waits.  The resident mode (below) keeps one kernel on
+// the device instead; its waits are bounded in time.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <algorithm>
+#include <cstring>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
@@ -63,6 +65,43 @@ struct inline_list {
 // work-list; tile_start[i] is the first tile of request i.  The per-option
 // arithmetic is bs_lane, the same function the single-request kernel uses,
 // so a request's results do not depend on what it was batched with.
+// Options [base, base + BS_TILE) of one request, by the whole block.
+template <int CDF, int P>
+__device__ __forceinline__ void bs_tile(const req_desc& d, uint64_t base)
+{
+  const float c = math::madd<(P != PREC_EXACT)>(math::mul(d.sigma, d.sigma), 0.5f, d.r);
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const uint64_t i = base + (uint64_t)h * 1024 + (uint64_t)threadIdx.x * 4;
+    if (i >= d.n) continue;
+    if (d.vec_ok && i + 4 <= d.n) {
+      float s[4], k[4], tt[4], oc[4], op[4];
+      mem::load_vec<float, 4, true>(d.S, i, s);
+      mem::load_vec<float, 4, true>(d.K, i, k);
+      mem::load_vec<float, 4, true>(d.T, i, tt);
+      if constexpr (kPacked<float, CDF, P>) {
+#pragma unroll
+        for (int l = 0; l < 4; l += 2) {
+          float2 pc, pp;
+          x2::blackscholes(make_float2(s[l], s[l + 1]), make_float2(k[l], k[l + 1]), make_float2(tt[l], tt[l + 1]),
+                           d.r, d.sigma, c, pc, pp);
+          oc[l] = pc.x; oc[l + 1] = pc.y;
+          op[l] = pp.x; op[l + 1] = pp.y;
+        }
+      } else {
+#pragma unroll
+        for (int l = 0; l < 4; ++l) bs_lane<float, CDF, P>(s[l], k[l], tt[l], d.r, d.sigma, c, oc[l], op[l]);
+      }
+      mem::store_vec<float, 4>(d.call, i, oc);
+      mem::store_vec<float, 4>(d.put, i, op);
+    } else {
+      const uint64_t e = (i + 4 < d.n) ? i + 4 : d.n;
+      for (uint64_t q = i; q < e; ++q)
+        bs_lane<float, CDF, P>(d.S[q], d.K[q], d.T[q], d.r, d.sigma, c, d.call[q], d.put[q]);
+    }
+  }
+}
+
 template <int CDF, int P>
 __device__ __forceinline__ void bs_batch_body(const req_desc* desc, const uint64_t* tile_start, int nreq)
 {
@@ -82,27 +121,7 @@ __device__ __forceinline__ void bs_batch_body(const req_desc* desc, const uint64
     const req_desc d = desc[ri];
     const uint64_t t0 = tile_start[ri];
     __syncthreads();
-    const float c = math::madd<(P != PREC_EXACT)>(math::mul(d.sigma, d.sigma), 0.5f, d.r);
-    const uint64_t base = (t - t0) * BS_TILE;
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const uint64_t i = base + (uint64_t)h * 1024 + (uint64_t)threadIdx.x * 4;
-      if (i >= d.n) continue;
-      if (d.vec_ok && i + 4 <= d.n) {
-        float s[4], k[4], tt[4], oc[4], op[4];
-        mem::load_vec<float, 4, true>(d.S, i, s);
-        mem::load_vec<float, 4, true>(d.K, i, k);
-        mem::load_vec<float, 4, true>(d.T, i, tt);
-#pragma unroll
-        for (int l = 0; l < 4; ++l) bs_lane<float, CDF, P>(s[l], k[l], tt[l], d.r, d.sigma, c, oc[l], op[l]);
-        mem::store_vec<float, 4>(d.call, i, oc);
-        mem::store_vec<float, 4>(d.put, i, op);
-      } else {
-        const uint64_t e = (i + 4 < d.n) ? i + 4 : d.n;
-        for (uint64_t q = i; q < e; ++q)
-          bs_lane<float, CDF, P>(d.S[q], d.K[q], d.T[q], d.r, d.sigma, c, d.call[q], d.put[q]);
-      }
-    }
+    bs_tile<CDF, P>(d, (t - t0) * BS_TILE);
   }
 }
 
@@ -117,6 +136,236 @@ template <int CDF, int P>
 __global__ void __launch_bounds__(256) k_bs_batch_inline(const __grid_constant__ inline_list list, int nreq)
 {
   bs_batch_body<CDF, P>(list.d, list.tile_start, nreq);
+}
+
+// ------------------------------------------------------- resident mode
+// coalesce = 2: one kernel stays on the device and drains a ring of requests
+// that the host publishes in pinned, device-mapped memory, so a request that
+// arrives while others run joins the running kernel instead of waiting for a
+// launch.  Block 0 is the manager: it copies newly published ring entries
+// into device memory and publishes their tiles.  Every other block claims
+// tiles one at a time (a compare-and-swap on the next-tile counter), prices
+// them with the batch kernel's arithmetic, and the block that finishes a
+// request's last tile writes the request's completion word in host memory.
+// Every wait is bounded in time (%globaltimer): the manager leaves after
+// idle_ns without new requests once every published tile is claimed, or
+// after stall_ns without a claim while tiles wait (the workers are gone); a
+// block whose wait for work exceeds its own bound records an error and
+// leaves.  The host launches the kernel again when a request is published
+// after it left.
+constexpr uint32_t kRing = 4096;            // requests published and not yet complete, at most
+
+struct ring_entry {
+  req_desc d;
+  uint64_t tile_begin, ntiles, seq, pad;
+};
+
+enum : uint32_t { RES_RUNNING = 0, RES_IDLE_EXIT = 1, RES_STOPPED = 2, RES_WAIT_TIMEOUT = 3 };
+
+// pinned host memory mapped into the device's address space
+struct resident_host {
+  ring_entry ring[kRing];                   // written by the host
+  uint64_t tail;                            // requests published (host, store-release)
+  uint32_t stop;                            // host: leave once drained
+  uint32_t status;                          // kernel: why it left
+  uint64_t consumed;                        // kernel: requests copied when it left
+  uint64_t done[kRing];                     // kernel: seq + 1 once request seq is complete
+};
+
+// device memory, kept across launches
+struct resident_dev {
+  ring_entry ring[kRing];
+  uint64_t nreq;                            // requests copied
+  uint64_t pub;                             // end of the published tiles
+  uint64_t next;                            // next tile to claim
+  uint32_t closing;
+  uint32_t error;
+  unsigned tiles_done[kRing];
+};
+
+__device__ __forceinline__ uint64_t gtimer()
+{
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ uint64_t ld_acq_sys(const uint64_t* p)
+{
+  uint64_t v;
+  asm volatile("ld.acquire.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ uint32_t ld_acq_sys32(const uint32_t* p)
+{
+  uint32_t v;
+  asm volatile("ld.acquire.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ uint64_t ld_acq_gpu(const uint64_t* p)
+{
+  uint64_t v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ uint32_t ld_acq_gpu32(const uint32_t* p)
+{
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_rel_gpu(uint64_t* p, uint64_t v)
+{
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void st_rel_gpu32(uint32_t* p, uint32_t v)
+{
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void st_rel_sys(uint64_t* p, uint64_t v)
+{
+  asm volatile("st.release.sys.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void st_rel_sys32(uint32_t* p, uint32_t v)
+{
+  asm volatile("st.release.sys.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// A ring entry read past the L1 cache (ld.cv: fetched again on every read):
+// its slot was written by another agent (the host, or the manager) after
+// this SM may have cached the slot's previous occupant.
+__device__ __forceinline__ ring_entry load_entry_cv(const ring_entry* p)
+{
+  ring_entry e;
+  const unsigned long long* src = reinterpret_cast<const unsigned long long*>(p);
+  unsigned long long* dst = reinterpret_cast<unsigned long long*>(&e);
+#pragma unroll
+  for (int i = 0; i < (int)(sizeof(ring_entry) / 8); ++i) dst[i] = __ldcv(src + i);
+  return e;
+}
+__device__ __forceinline__ ring_entry load_entry_cg(const ring_entry* p)
+{
+  ring_entry e;
+  const unsigned long long* src = reinterpret_cast<const unsigned long long*>(p);
+  unsigned long long* dst = reinterpret_cast<unsigned long long*>(&e);
+#pragma unroll
+  for (int i = 0; i < (int)(sizeof(ring_entry) / 8); ++i) dst[i] = __ldcg(src + i);
+  return e;
+}
+
+__device__ void resident_manager(resident_host* h, resident_dev* d, uint64_t idle_ns)
+{
+  uint64_t copied = d->nreq;
+  uint64_t last = gtimer();                                  // last new request
+  uint64_t seen_next = ld_acq_gpu(&d->next), moved = last;   // last tile claimed
+  uint32_t reason = RES_IDLE_EXIT;
+  // published tiles that no block claims for this long mean the workers are gone
+  const uint64_t stall_ns = 4 * idle_ns + 1000000000ull;
+  for (;;) {
+    const uint64_t tail = ld_acq_sys(&h->tail);
+    if (tail > copied) {
+      const uint64_t end = (tail - copied > 64) ? copied + 64 : tail;
+      uint64_t pub_end = 0;
+      for (uint64_t i = copied; i < end; ++i) {
+        const ring_entry e = load_entry_cv(&h->ring[i % kRing]);
+        d->ring[i % kRing] = e;
+        d->tiles_done[i % kRing] = 0u;
+        pub_end = e.tile_begin + e.ntiles;
+      }
+      d->nreq = end;
+      __threadfence();                                       // the entries and counters before the tiles
+      st_rel_gpu(&d->pub, pub_end);
+      copied = end;
+      last = gtimer();
+      continue;
+    }
+    const uint64_t now = gtimer();
+    const uint64_t nxt = ld_acq_gpu(&d->next);
+    const bool drained = nxt >= ld_acq_gpu(&d->pub);
+    if (nxt != seen_next) { seen_next = nxt; moved = now; }
+    if (drained && ld_acq_sys32(&h->stop)) { reason = RES_STOPPED; break; }
+    if (drained && now - last > idle_ns) break;
+    if (!drained && now - moved > stall_ns) { reason = RES_WAIT_TIMEOUT; break; }
+    __nanosleep(256);
+  }
+  st_rel_gpu32(&d->closing, 1u);
+  h->consumed = copied;
+  __threadfence_system();
+  st_rel_sys32(&h->status, reason);
+}
+
+template <int CDF, int P>
+__global__ void __launch_bounds__(256) k_bs_resident(resident_host* h, resident_dev* d, uint64_t idle_ns,
+                                                     uint64_t first_req)
+{
+  if (blockIdx.x == 0) {
+    if (threadIdx.x == 0) resident_manager(h, d, idle_ns);
+    return;
+  }
+  __shared__ uint64_t s_tile, s_cursor;
+  __shared__ ring_entry s_e;
+  uint64_t cursor = first_req;
+  // a wait for work outlives the manager's idle bound only if the manager is gone
+  const uint64_t wait_ns = 2 * idle_ns + 100000000ull;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      uint64_t tile = ~0ull;
+      const uint64_t t0 = gtimer();
+      for (;;) {
+        const uint64_t pub = ld_acq_gpu(&d->pub);
+        const uint64_t nxt = ld_acq_gpu(&d->next);
+        if (nxt < pub) {
+          if (atomicCAS((unsigned long long*)&d->next, (unsigned long long)nxt, (unsigned long long)(nxt + 1)) == nxt) {
+            tile = nxt;
+            break;
+          }
+          continue;
+        }
+        if (ld_acq_gpu32(&d->closing)) break;
+        if (gtimer() - t0 > wait_ns) {
+          atomicExch(&d->error, 1u);
+          st_rel_sys32(&h->status, RES_WAIT_TIMEOUT);
+          break;
+        }
+        __nanosleep(128);
+      }
+      if (tile != ~0ull) {
+        // the request holding this tile: scan forward from the last one (a ring
+        // slot whose seq moved on belongs to a later request: this one is done);
+        // every request up to the one holding the tile is already copied, so the
+        // scan ends before d->nreq, or the ring is corrupt and the block leaves
+        const uint64_t nreq = ld_acq_gpu(&d->nreq);
+        ring_entry e = load_entry_cg(&d->ring[cursor % kRing]);
+        while (!(e.seq == cursor && tile < e.tile_begin + e.ntiles) && cursor < nreq) {
+          ++cursor;
+          e = load_entry_cg(&d->ring[cursor % kRing]);
+        }
+        if (cursor >= nreq) {
+          atomicExch(&d->error, 2u);
+          st_rel_sys32(&h->status, RES_WAIT_TIMEOUT);
+          tile = ~0ull;
+        } else {
+          s_e = e;
+          s_cursor = cursor;
+        }
+      }
+      s_tile = tile;
+    }
+    __syncthreads();
+    const uint64_t tile = s_tile;
+    if (tile == ~0ull) return;
+    const ring_entry e = s_e;
+    bs_tile<CDF, P>(e.d, (tile - e.tile_begin) * BS_TILE);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      const unsigned prev = atomicAdd(&d->tiles_done[s_cursor % kRing], 1u);
+      if (prev + 1u == (unsigned)e.ntiles) {
+        __threadfence_system();                              // the request's prices before its completion word
+        st_rel_sys(&h->done[s_cursor % kRing], e.seq + 1);
+      }
+    }
+    __syncthreads();
+  }
 }
 
 // Persistent grid of a batch kernel: resident blocks per SM x SMs, computed
@@ -226,6 +475,17 @@ struct nt2cuda_server {
   nt2cuda_status worker_error = NT2CUDA_OK;
   std::atomic<int> n_admitted{0};    // admitted.size(), readable without the lock
   uint64_t spin_ns = 0;
+  // resident mode (coalesce = 2)
+  resident_host* rh = nullptr;       // pinned, mapped
+  resident_host* rh_dev = nullptr;   // its device address
+  resident_dev* rd = nullptr;
+  cudaStream_t rstream = nullptr;
+  bool rrunning = false;             // a resident kernel was launched and has not been seen to finish
+  uint64_t rseq = 0;                 // requests published
+  uint64_t rtiles = 0;               // tiles published
+  uint64_t rfirst = 0;               // first request of the running kernel
+  int rgrid = 0;
+  std::deque<std::pair<uint64_t, uint64_t>> rpending;   // (seq, request id) published, not seen complete
 };
 
 namespace {
@@ -429,6 +689,147 @@ void worker_loop(nt2cuda_server* s)
   }
 }
 
+// ---------------------------------------------------- resident mode, host
+constexpr uint64_t kResidentIdleNs = 20000000ull;   // the kernel leaves after 20 ms without requests
+
+template <int CDF, int P> cudaError_t launch_resident_t(nt2cuda_server* s)
+{
+  k_bs_resident<CDF, P><<<(unsigned)s->rgrid, 256, 0, s->rstream>>>(s->rh_dev, s->rd, kResidentIdleNs, s->rfirst);
+  return cudaGetLastError();
+}
+cudaError_t launch_resident(nt2cuda_server* s)
+{
+  const int P = s->cfg.fused;
+  if (s->cfg.cdf_kind == CDF_FASTNORMCDF)
+    return P == PREC_FAST ? launch_resident_t<CDF_FASTNORMCDF, PREC_FAST>(s)
+         : P == PREC_FUSED ? launch_resident_t<CDF_FASTNORMCDF, PREC_FUSED>(s)
+                           : launch_resident_t<CDF_FASTNORMCDF, PREC_EXACT>(s);
+  return P == PREC_FAST ? launch_resident_t<CDF_NORMCDF, PREC_FAST>(s)
+       : P == PREC_FUSED ? launch_resident_t<CDF_NORMCDF, PREC_FUSED>(s)
+                         : launch_resident_t<CDF_NORMCDF, PREC_EXACT>(s);
+}
+template <int CDF, int P> int resident_grid_t()
+{
+  // the manager and the workers all resident at once, one block per SM
+  // below full occupancy so that other streams' kernels still find room
+  const int per = resident_blocks(k_bs_resident<CDF, P>, 256);
+  return sm_count() * (per > 1 ? per - 1 : 1) + 1;
+}
+int resident_grid(const nt2cuda_server_config& c)
+{
+  const int P = c.fused;
+  if (c.cdf_kind == CDF_FASTNORMCDF)
+    return P == PREC_FAST ? resident_grid_t<CDF_FASTNORMCDF, PREC_FAST>()
+         : P == PREC_FUSED ? resident_grid_t<CDF_FASTNORMCDF, PREC_FUSED>() : resident_grid_t<CDF_FASTNORMCDF, PREC_EXACT>();
+  return P == PREC_FAST ? resident_grid_t<CDF_NORMCDF, PREC_FAST>()
+       : P == PREC_FUSED ? resident_grid_t<CDF_NORMCDF, PREC_FUSED>() : resident_grid_t<CDF_NORMCDF, PREC_EXACT>();
+}
+
+// The resident-mode thread: publishes admitted requests to the ring, keeps a
+// kernel running while requests are outstanding, and marks requests done as
+// their completion words appear.
+void resident_loop(nt2cuda_server* s)
+{
+  cudaSetDevice(s->device);
+  uint64_t idle_since = now_ns();
+  for (;;) {
+    bool active = false;
+    uint64_t published = 0;
+    {
+      std::unique_lock<std::mutex> lk(s->m);
+      if (s->stop && s->rpending.empty()) break;      // published requests finish; the rest are dropped
+      bool any = false;
+      while (!s->stop && !s->admitted.empty()) {
+        const uint64_t seq = s->rseq;
+        const uint32_t slot = (uint32_t)(seq % kRing);
+        if (seq >= kRing && __atomic_load_n(&s->rh->done[slot], __ATOMIC_ACQUIRE) != seq - kRing + 1) break;
+        request& r = s->reqs[s->admitted.front()];
+        s->admitted.pop_front();
+        const uint64_t ntiles = (r.d.n + BS_TILE - 1) / BS_TILE;
+        ring_entry& e = s->rh->ring[slot];
+        e.d = r.d;
+        e.tile_begin = s->rtiles;
+        e.ntiles = ntiles;
+        e.seq = seq;
+        s->rtiles += ntiles;
+        s->rseq = seq + 1;
+        r.state = LAUNCHED;
+        s->rpending.emplace_back(seq, r.id);
+        any = true;
+      }
+      s->n_admitted.store((int)s->admitted.size(), std::memory_order_release);
+      if (any) {
+        __atomic_store_n(&s->rh->tail, s->rseq, __ATOMIC_RELEASE);
+        s->st.batches++;
+      }
+      published = s->rseq;
+      active = !s->rpending.empty() || !s->admitted.empty();
+    }
+    // the kernel: notice that it left; launch one while requests are not yet taken
+    if (s->rrunning && cudaStreamQuery(s->rstream) != cudaErrorNotReady) {
+      s->rrunning = false;
+      const cudaError_t e = cudaStreamSynchronize(s->rstream);
+      const uint32_t why = __atomic_load_n(&s->rh->status, __ATOMIC_ACQUIRE);
+      if (e != cudaSuccess || why == RES_WAIT_TIMEOUT) {
+        std::lock_guard<std::mutex> g(s->m);
+        if (s->worker_error == NT2CUDA_OK)
+          s->worker_error = e != cudaSuccess ? from_cuda(e, NT2CUDA_ERR_LAUNCH) : NT2CUDA_ERR_TIMEOUT;
+      }
+    }
+    if (!s->rrunning && __atomic_load_n(&s->rh->consumed, __ATOMIC_ACQUIRE) < published) {
+      s->rfirst = __atomic_load_n(&s->rh->consumed, __ATOMIC_ACQUIRE);
+      __atomic_store_n(&s->rh->status, (uint32_t)RES_RUNNING, __ATOMIC_RELEASE);
+      // the previous kernel left d->closing set: clear it before the next one starts
+      cudaError_t e = cudaMemsetAsync(&s->rd->closing, 0, sizeof(uint32_t), s->rstream);
+      if (e == cudaSuccess) e = launch_resident(s);
+      std::lock_guard<std::mutex> g(s->m);
+      if (e != cudaSuccess) {
+        if (s->worker_error == NT2CUDA_OK) s->worker_error = from_cuda(e, NT2CUDA_ERR_LAUNCH);
+      } else {
+        s->rrunning = true;
+        s->st.launches++;
+      }
+    }
+    // completions, in any order
+    bool completed = false;
+    {
+      std::lock_guard<std::mutex> g(s->m);
+      const uint64_t t = now_ns();
+      for (auto it = s->rpending.begin(); it != s->rpending.end();) {
+        const uint64_t seq = it->first;
+        if (__atomic_load_n(&s->rh->done[seq % kRing], __ATOMIC_ACQUIRE) == seq + 1 || s->worker_error != NT2CUDA_OK) {
+          auto q = s->reqs.find(it->second);
+          if (q != s->reqs.end()) {
+            q->second.state = DONE;
+            q->second.t_done = t;
+            s->st.completed++;
+          }
+          it = s->rpending.erase(it);
+          completed = true;
+        } else {
+          ++it;
+        }
+      }
+    }
+    if (completed) s->cv_done.notify_all();
+    if (active) {
+      idle_since = now_ns();
+      continue;                                     // poll while requests are outstanding
+    }
+    // idle: poll briefly for new requests, then sleep until one arrives
+    if (now_ns() - idle_since < s->spin_ns) continue;
+    std::unique_lock<std::mutex> lk(s->m);
+    s->cv_work.wait_for(lk, std::chrono::milliseconds(2),
+                        [&] { return s->stop || !s->admitted.empty() || !s->waiting.empty(); });
+  }
+  // stopping: let the kernel leave and wait for it
+  __atomic_store_n(&s->rh->stop, 1u, __ATOMIC_RELEASE);
+  if (s->rrunning) {
+    cudaStreamSynchronize(s->rstream);
+    s->rrunning = false;
+  }
+}
+
 nt2cuda_status wait_done_locked(nt2cuda_server* s, std::unique_lock<std::mutex>& lk, uint64_t id, int timeout_ms)
 {
   auto it = s->reqs.find(id);
@@ -453,7 +854,7 @@ nt2cuda_status nt2cuda_server_create(const nt2cuda_server_config* cfg, nt2cuda_s
   if (!cfg || !out) return NT2CUDA_ERR_ARG;
   *out = nullptr;
   if (cfg->budget_bytes < 4096 || cfg->max_inflight_batches < 1 || cfg->max_inflight_batches > 16 ||
-      cfg->max_batch_requests < 1 || cfg->max_batch_requests > (1 << 20) ||
+      cfg->max_batch_requests < 1 || cfg->max_batch_requests > (1 << 20) || cfg->coalesce < 0 || cfg->coalesce > 2 ||
       (cfg->cdf_kind != CDF_NORMCDF && cfg->cdf_kind != CDF_FASTNORMCDF) || cfg->fused < 0 || cfg->fused > 2 ||
       cfg->spin_us > 100000)
     return NT2CUDA_ERR_ARG;
@@ -479,6 +880,26 @@ nt2cuda_status nt2cuda_server_create(const nt2cuda_server_config* cfg, nt2cuda_s
     sl.d_desc = (req_desc*)sl.d_buf;
     sl.d_tiles = (uint64_t*)(sl.d_buf + desc_bytes);
   }
+  if (s->cfg.coalesce == 2) {
+    void* hp = nullptr;
+    void* dp = nullptr;
+    bool ok = cudaHostAlloc(&hp, sizeof(resident_host), cudaHostAllocMapped | cudaHostAllocPortable) == cudaSuccess;
+    if (ok) {
+      s->rh = (resident_host*)hp;
+      std::memset(hp, 0, sizeof(resident_host));
+      ok = cudaHostGetDevicePointer(&dp, hp, 0) == cudaSuccess;
+      s->rh_dev = (resident_host*)dp;
+    }
+    ok = ok && cudaMalloc(&s->rd, sizeof(resident_dev)) == cudaSuccess &&
+         cudaMemset(s->rd, 0, sizeof(resident_dev)) == cudaSuccess &&
+         cudaStreamCreateWithFlags(&s->rstream, cudaStreamNonBlocking) == cudaSuccess &&
+         cudaDeviceSynchronize() == cudaSuccess;
+    if (!ok) { nt2cuda_server_destroy(s); return NT2CUDA_ERR_OOM; }
+    s->rgrid = resident_grid(s->cfg);                  // also loads the kernel
+    s->worker = std::thread(resident_loop, s);
+    *out = s;
+    return NT2CUDA_OK;
+  }
   warm(s->cfg);
   s->worker = std::thread(worker_loop, s);
   s->reaper = std::thread(reaper_loop, s);
@@ -498,6 +919,12 @@ nt2cuda_status nt2cuda_server_destroy(nt2cuda_server* s)
   s->cv_inflight.notify_all();
   if (s->reaper.joinable()) s->reaper.join();   // drains every launched batch first
   for (slot& sl : s->slots) if (sl.stream) cudaStreamSynchronize(sl.stream);
+  if (s->rstream) {
+    cudaStreamSynchronize(s->rstream);
+    cudaStreamDestroy(s->rstream);
+  }
+  if (s->rd) cudaFree(s->rd);
+  if (s->rh) cudaFreeHost(s->rh);
   for (slot& sl : s->slots) {
     if (sl.done) cudaEventDestroy(sl.done);
     if (sl.stream) cudaStreamDestroy(sl.stream);

@@ -14,12 +14,18 @@ TIMEOUT = 5
 class Server:
     """Black-Scholes request server (float32; inputs are device tables)."""
 
+    MODES = {"launch": 0, "batched": 1, "resident": 2}
+
     def __init__(self, budget_bytes: int = 40 << 30, max_batch_requests: int = 4096,
                  max_inflight_batches: int = 3, coalesce: bool = True, fused: bool = False,
                  cdf: str = "normcdf", wait_timeout_ms: int = 60000, precision: str | None = None,
-                 spin_us: int = 0):
+                 spin_us: int = 0, mode: str | None = None):
+        """mode: "resident" (one kernel stays on the device and drains a request ring),
+        "batched" (one launch per step over the admitted requests) or "launch" (one launch
+        per request); without it, coalesce picks "batched" or "launch"."""
         prec = {"exact": 0, "fused": 1, "fast": 2}[precision] if precision else int(fused)
-        cfg = ServerConfig(budget_bytes, max_batch_requests, max_inflight_batches, int(coalesce), prec,
+        co = self.MODES[mode] if mode else int(coalesce)
+        cfg = ServerConfig(budget_bytes, max_batch_requests, max_inflight_batches, co, prec,
                            {"normcdf": 0, "fastnormcdf": 1}[cdf], wait_timeout_ms, spin_us)
         self._h = C.c_void_p()
         check(lib().nt2cuda_server_create(C.byref(cfg), C.byref(self._h)), "server_create")

@@ -32,11 +32,12 @@ def requests(total, sizes_seed, lo=256, hi=1 << 16, count=200):
     return list(zip(offs.tolist(), sizes.tolist()))
 
 
-@pytest.mark.parametrize("coalesce", [True, False])
-def test_mix_equals_alone(gpu, oracle, coalesce):
+@pytest.mark.parametrize("mode", ["resident", "batched", "launch"])
+def test_mix_equals_alone(gpu, oracle, mode):
+    coalesce = mode != "launch"
     S, K, T = pool(1 << 20)
     reqs = requests(1 << 20, 1)
-    with Server(budget_bytes=256 << 20, max_batch_requests=64, max_inflight_batches=3, coalesce=coalesce) as srv:
+    with Server(budget_bytes=256 << 20, max_batch_requests=64, max_inflight_batches=3, mode=mode) as srv:
         tickets = [srv.submit_ptr(S.data_ptr() + 4 * o, K.data_ptr() + 4 * o, T.data_ptr() + 4 * o, 0.02, 0.30, n)
                    for o, n in reqs]
         outs = []
@@ -162,3 +163,65 @@ def test_replay_rejects_oversized_request(gpu):
         with pytest.raises(NT2CudaError):
             srv.replay(S.data_ptr(), S.data_ptr(), S.data_ptr(), 0.02, 0.3, np.zeros(2, np.uint64),
                        np.array([16, 1 << 16], np.uint64), np.zeros(2, np.uint64))
+
+
+def test_resident_kernel_leaves_when_idle_and_comes_back(gpu, oracle):
+    """The resident kernel's waits are bounded: with no request for its idle bound (20 ms) it
+    leaves; the next request launches it again, and results stay bit-exact."""
+    S, K, T = pool(1 << 16, seed=4)
+    with Server(budget_bytes=64 << 20, mode="resident") as srv:
+        outs = []
+        for k in range(3):
+            o, n = 1000 * k, 4099 + k
+            t = srv.submit_ptr(S.data_ptr() + 4 * o, K.data_ptr() + 4 * o, T.data_ptr() + 4 * o, 0.02, 0.30, n)
+            c, p = srv.wait(t, 30000)
+            outs.append((o, n, copy_out(c, n), copy_out(p, n)))
+            srv.release(t)
+            time.sleep(0.08)                     # longer than the kernel's idle bound
+        st = srv.stats()
+    assert st["completed"] == 3
+    assert st["launches"] == 3                   # it left after each request and came back
+    for o, n, c, p in outs:
+        ca, pa = gpu.blackscholes(S[o:o + n], K[o:o + n], T[o:o + n], 0.02, 0.30)
+        assert torch.equal(c, ca) and torch.equal(p, pa)
+
+
+def test_resident_requests_join_the_running_kernel(gpu):
+    """Requests submitted while the kernel runs are taken by the same launch."""
+    S, K, T = pool(1 << 22, seed=5)
+    reqs = requests(1 << 22, 3, lo=1 << 12, hi=1 << 18, count=400)
+    with Server(budget_bytes=1 << 30, mode="resident") as srv:
+        tickets = []
+        for o, n in reqs:
+            tickets.append(srv.submit_ptr(S.data_ptr() + 4 * o, K.data_ptr() + 4 * o, T.data_ptr() + 4 * o,
+                                          0.02, 0.30, n))
+        for t in tickets:
+            srv.wait(t, 30000)
+            srv.release(t)
+        st = srv.stats()
+    assert st["completed"] == len(reqs)
+    assert st["launches"] <= 2
+
+
+def test_resident_ring_wraps(gpu):
+    """More requests than the ring holds (4096), submitted as fast as possible: ring slots are
+    reused only after their request completes, and every request completes, bit-exact."""
+    S, K, T = pool(1 << 20, seed=6)
+    rng = np.random.default_rng(8)
+    count = 10000
+    sizes = rng.integers(1, 3000, count)
+    offs = rng.integers(0, (1 << 20) - 3000, count)
+    with Server(budget_bytes=1 << 30, mode="resident", wait_timeout_ms=20000) as srv:
+        tickets = [srv.submit_ptr(S.data_ptr() + 4 * int(o), K.data_ptr() + 4 * int(o), T.data_ptr() + 4 * int(o),
+                                  0.02, 0.30, int(n)) for o, n in zip(offs, sizes)]
+        check = []
+        for k, (t, o, n) in enumerate(zip(tickets, offs, sizes)):
+            c, p = srv.wait(t, 20000)
+            if k % 997 == 0:
+                check.append((int(o), int(n), copy_out(c, int(n)), copy_out(p, int(n))))
+            srv.release(t)
+        st = srv.stats()
+    assert st["completed"] == count
+    for o, n, c, p in check:
+        ca, pa = gpu.blackscholes(S[o:o + n], K[o:o + n], T[o:o + n], 0.02, 0.30)
+        assert torch.equal(c, ca) and torch.equal(p, pa)
