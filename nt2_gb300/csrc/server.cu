@@ -143,15 +143,15 @@ __global__ void __launch_bounds__(256) k_bs_batch_inline(const __grid_constant__
 // that the host publishes in pinned, device-mapped memory, so a request that
 // arrives while others run joins the running kernel instead of waiting for a
 // launch.  Block 0 is the manager: it copies newly published ring entries
-// into device memory and publishes their tiles.  Every other block claims
-// tiles one at a time (a compare-and-swap on the next-tile counter), prices
-// them with the batch kernel's arithmetic, and the block that finishes a
-// request's last tile writes the request's completion word in host memory.
-// Every wait is bounded in time (%globaltimer): the manager leaves after
-// idle_ns without new requests once every published tile is claimed, or
-// after stall_ns without a claim while tiles wait (the workers are gone); a
-// block whose wait for work exceeds its own bound records an error and
-// leaves.  The host launches the kernel again when a request is published
+// into device memory and publishes their tiles.  Every other block takes a
+// tile ticket (one atomic add on the next-tile counter) and, once that tile
+// is published, prices it with the batch kernel's arithmetic; the block that
+// finishes a request's last tile writes the request's completion word in host
+// memory.  Every wait is bounded in time (%globaltimer): the manager leaves
+// after idle_ns without new requests once every published tile is finished,
+// or after stall_ns without a finished tile while tiles wait (the workers are
+// gone); a block whose wait for its tile exceeds its own bound records an
+// error and leaves.  The host launches the kernel again when a request is published
 // after it left.
 constexpr uint32_t kRing = 4096;            // requests published and not yet complete, at most
 
@@ -172,13 +172,16 @@ struct resident_host {
   uint64_t done[kRing];                     // kernel: seq + 1 once request seq is complete
 };
 
-// device memory, kept across launches
+// device memory, kept across launches; the counters every block touches sit
+// on 128-byte lines of their own
+struct __align__(128) resident_line { uint64_t v; uint64_t pad[15]; };
 struct resident_dev {
   ring_entry ring[kRing];
-  uint64_t nreq;                            // requests copied
-  uint64_t pub;                             // end of the published tiles
-  uint64_t next;                            // next tile to claim
-  uint32_t closing;
+  resident_line nreq;                       // requests copied
+  resident_line pub;                        // end of the published tiles
+  resident_line next;                       // next tile ticket (may run ahead of pub)
+  resident_line processed;                  // tiles finished
+  resident_line closing;                    // 1: no tile will be published any more
   uint32_t error;
   unsigned tiles_done[kRing];
 };
@@ -254,11 +257,11 @@ __device__ __forceinline__ ring_entry load_entry_cg(const ring_entry* p)
 
 __device__ void resident_manager(resident_host* h, resident_dev* d, uint64_t idle_ns)
 {
-  uint64_t copied = d->nreq;
-  uint64_t last = gtimer();                                  // last new request
-  uint64_t seen_next = ld_acq_gpu(&d->next), moved = last;   // last tile claimed
+  uint64_t copied = d->nreq.v;
+  uint64_t last = gtimer();                                       // last new request
+  uint64_t seen = ld_acq_gpu(&d->processed.v), moved = last;      // last tile finished
   uint32_t reason = RES_IDLE_EXIT;
-  // published tiles that no block claims for this long mean the workers are gone
+  // published tiles that none finishes for this long mean the workers are gone
   const uint64_t stall_ns = 4 * idle_ns + 1000000000ull;
   for (;;) {
     const uint64_t tail = ld_acq_sys(&h->tail);
@@ -271,23 +274,23 @@ __device__ void resident_manager(resident_host* h, resident_dev* d, uint64_t idl
         d->tiles_done[i % kRing] = 0u;
         pub_end = e.tile_begin + e.ntiles;
       }
-      d->nreq = end;
-      __threadfence();                                       // the entries and counters before the tiles
-      st_rel_gpu(&d->pub, pub_end);
+      d->nreq.v = end;
+      __threadfence();                                            // the entries and counters before the tiles
+      st_rel_gpu(&d->pub.v, pub_end);
       copied = end;
       last = gtimer();
       continue;
     }
     const uint64_t now = gtimer();
-    const uint64_t nxt = ld_acq_gpu(&d->next);
-    const bool drained = nxt >= ld_acq_gpu(&d->pub);
-    if (nxt != seen_next) { seen_next = nxt; moved = now; }
+    const uint64_t done = ld_acq_gpu(&d->processed.v);
+    const bool drained = done >= ld_acq_gpu(&d->pub.v);
+    if (done != seen) { seen = done; moved = now; }
     if (drained && ld_acq_sys32(&h->stop)) { reason = RES_STOPPED; break; }
     if (drained && now - last > idle_ns) break;
     if (!drained && now - moved > stall_ns) { reason = RES_WAIT_TIMEOUT; break; }
     __nanosleep(256);
   }
-  st_rel_gpu32(&d->closing, 1u);
+  st_rel_gpu(&d->closing.v, 1u);
   h->consumed = copied;
   __threadfence_system();
   st_rel_sys32(&h->status, reason);
@@ -308,32 +311,30 @@ __global__ void __launch_bounds__(256) k_bs_resident(resident_host* h, resident_
   const uint64_t wait_ns = 2 * idle_ns + 100000000ull;
   for (;;) {
     if (threadIdx.x == 0) {
-      uint64_t tile = ~0ull;
+      // a ticket always succeeds; it may name a tile not published yet, which
+      // the block waits for (the next request's first tiles go to the blocks
+      // already waiting, in ticket order)
+      uint64_t tile = atomicAdd((unsigned long long*)&d->next.v, 1ull);
       const uint64_t t0 = gtimer();
+      unsigned nap = 64;
       for (;;) {
-        const uint64_t pub = ld_acq_gpu(&d->pub);
-        const uint64_t nxt = ld_acq_gpu(&d->next);
-        if (nxt < pub) {
-          if (atomicCAS((unsigned long long*)&d->next, (unsigned long long)nxt, (unsigned long long)(nxt + 1)) == nxt) {
-            tile = nxt;
-            break;
-          }
-          continue;
-        }
-        if (ld_acq_gpu32(&d->closing)) break;
+        if (tile < ld_acq_gpu(&d->pub.v)) break;
+        if (ld_acq_gpu(&d->closing.v)) { tile = ~0ull; break; }   // nothing more will be published
         if (gtimer() - t0 > wait_ns) {
           atomicExch(&d->error, 1u);
           st_rel_sys32(&h->status, RES_WAIT_TIMEOUT);
+          tile = ~0ull;
           break;
         }
-        __nanosleep(128);
+        __nanosleep(nap);
+        if (nap < 1024) nap <<= 1;
       }
       if (tile != ~0ull) {
         // the request holding this tile: scan forward from the last one (a ring
         // slot whose seq moved on belongs to a later request: this one is done);
         // every request up to the one holding the tile is already copied, so the
         // scan ends before d->nreq, or the ring is corrupt and the block leaves
-        const uint64_t nreq = ld_acq_gpu(&d->nreq);
+        const uint64_t nreq = ld_acq_gpu(&d->nreq.v);
         ring_entry e = load_entry_cg(&d->ring[cursor % kRing]);
         while (!(e.seq == cursor && tile < e.tile_begin + e.ntiles) && cursor < nreq) {
           ++cursor;
@@ -360,9 +361,10 @@ __global__ void __launch_bounds__(256) k_bs_resident(resident_host* h, resident_
       __threadfence();
       const unsigned prev = atomicAdd(&d->tiles_done[s_cursor % kRing], 1u);
       if (prev + 1u == (unsigned)e.ntiles) {
-        __threadfence_system();                              // the request's prices before its completion word
+        __threadfence_system();                                  // the request's prices before its completion word
         st_rel_sys(&h->done[s_cursor % kRing], e.seq + 1);
       }
+      atomicAdd((unsigned long long*)&d->processed.v, 1ull);
     }
     __syncthreads();
   }
@@ -779,8 +781,12 @@ void resident_loop(nt2cuda_server* s)
     if (!s->rrunning && __atomic_load_n(&s->rh->consumed, __ATOMIC_ACQUIRE) < published) {
       s->rfirst = __atomic_load_n(&s->rh->consumed, __ATOMIC_ACQUIRE);
       __atomic_store_n(&s->rh->status, (uint32_t)RES_RUNNING, __ATOMIC_RELEASE);
-      // the previous kernel left d->closing set: clear it before the next one starts
-      cudaError_t e = cudaMemsetAsync(&s->rd->closing, 0, sizeof(uint32_t), s->rstream);
+      // the previous kernel left closing set and its tickets run ahead of the
+      // published tiles (blocks that waited took tickets no tile got): clear
+      // the one and bring the other back to the first tile not yet published
+      cudaError_t e = cudaMemsetAsync(&s->rd->closing.v, 0, sizeof(uint64_t), s->rstream);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&s->rd->next.v, &s->rd->pub.v, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s->rstream);
       if (e == cudaSuccess) e = launch_resident(s);
       std::lock_guard<std::mutex> g(s->m);
       if (e != cudaSuccess) {
