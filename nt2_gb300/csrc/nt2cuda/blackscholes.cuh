@@ -82,8 +82,15 @@ constexpr bool kPacked = sizeof(T) == 4 && CDF == CDF_NORMCDF && P == PREC_EXACT
 
 // V options per thread per group (16 bytes of each input), U groups in
 // flight per grid-stride trip.
+// The packed form is held to the registers of 5, 4 and 2 resident blocks per
+// SM at U = 1, 2, 4, so that its independent option pairs come with enough
+// warps to hide the FP32 pipes' latency (0: the compiler's own choice).
 template <class T, int CDF, int P, int U>
-__global__ void __launch_bounds__(256) k_blackscholes(const T* __restrict__ S, const T* __restrict__ K,
+constexpr int kMinBlocks = !kPacked<T, CDF, P> ? 0 : (U == 1 ? 5 : (U == 2 ? 4 : 2));
+
+template <class T, int CDF, int P, int U>
+__global__ void __launch_bounds__(256, (kMinBlocks<T, CDF, P, U>))
+    k_blackscholes(const T* __restrict__ S, const T* __restrict__ K,
                                                       const T* __restrict__ Tm, T r, T v,
                                                       T* __restrict__ call, T* __restrict__ put, size_t n)
 {
