@@ -182,17 +182,19 @@ __device__ __forceinline__ float2 x_over_1px(float2 x)
   return fma(r, y, q);
 }
 
-// NT2's float erfc of x = |a| (math::erfc_abs), two lanes, both regions
-// computed and the right one selected per lane.
-__device__ __forceinline__ float2 erfc_abs(float2 x)
+// The two regions of NT2's float erfc (math::erfc_small / erfc_large) on
+// z = x/(1+x), and the final selection for x = inf.
+__device__ __forceinline__ float2 erfc_small(float2 z)
 {
   constexpr uint32_t P3[9] = {0x41aa8e55u, 0x401b5680u, 0xc010d956u, 0x3f2cff3bu,
                               0xc016c985u, 0xbffc9284u, 0xbfa11698u, 0xbe036d7eu, 0x3f7ffffeu};
+  return mul(sub(splat(1.0f), z), horner(z, P3));
+}
+__device__ __forceinline__ float2 erfc_large(float2 x, float2 z)
+{
   constexpr uint32_t P2[11] = {0xc0283611u, 0x40d67e3bu, 0xc0cd1a85u, 0x4050b063u,
                                0xbfaea865u, 0x3e2006f0u, 0x3e1175c7u, 0x3ec4ca6eu,
                                0x3e243828u, 0xbf918a62u, 0x3f0a0e8bu};
-  const float2 z = x_over_1px(x);
-  const float2 small = mul(sub(splat(1.0f), z), horner(z, P3));
   // exp(-x*x): the argument is <= 0, so only the underflow selection applies
   const float2 m = mul_r(x, x);
   const float2 na = make_float2(-m.x, -m.y);
@@ -200,30 +202,58 @@ __device__ __forceinline__ float2 erfc_abs(float2 x)
   const float lo = fbits(cf::minlog);
   ex.x = (na.x <= lo) ? 0.0f : ex.x;
   ex.y = (na.y <= lo) ? 0.0f : ex.y;
-  const float2 large = mul(ex, horner(sub(z, splat(0.4f)), P2));
-  const float inf = __int_as_float(0x7f800000), two3 = fbits(cf::twothird);
-  float2 r;
-  r.x = (x.x < two3) ? small.x : large.x;
-  r.y = (x.y < two3) ? small.y : large.y;
+  return mul(ex, horner(sub(z, splat(0.4f)), P2));
+}
+__device__ __forceinline__ float2 erfc_finish(float2 x, float2 r)
+{
+  const float inf = __int_as_float(0x7f800000);
   r.x = (x.x == inf) ? 0.0f : r.x;
   r.y = (x.y == inf) ? 0.0f : r.y;
   return r;
 }
 
-// normcdf(a) and normcdf(-a) from one erfc core (math::normcdf_pair), two lanes.
-__device__ __forceinline__ void normcdf_pair(float2 a0, float2& pos, float2& neg)
+// NT2's float erfc of x = |a| (math::erfc_abs), two lanes, both regions
+// computed and the right one selected per lane.
+__device__ __forceinline__ float2 erfc_abs(float2 x)
 {
-  const float2 y = mul(splat(-fbits(cf::sqrt_2o_2)), a0);
-  const float2 r1 = erfc_abs(make_float2(fabsf(y.x), fabsf(y.y)));
+  const float2 z = x_over_1px(x);
+  const float2 small = erfc_small(z), large = erfc_large(x, z);
+  const float two3 = fbits(cf::twothird);
+  return erfc_finish(x, make_float2((x.x < two3) ? small.x : large.x, (x.y < two3) ? small.y : large.y));
+}
+
+// The same for a pair whose lanes are known to lie in one region (region 0:
+// both x < 2/3, 1: both not), or not (2): only the regions needed run, and
+// each lane gets what erfc_abs gives it.
+__device__ __forceinline__ float2 erfc_abs_region(float2 x, int region)
+{
+  const float2 z = x_over_1px(x);
+  if (region == 0) return erfc_finish(x, erfc_small(z));
+  if (region == 1) return erfc_finish(x, erfc_large(x, z));
+  return erfc_abs(x);
+}
+
+// normcdf(a) and normcdf(-a) from erfc of |y|, y = -a sqrt(2)/2 (math::normcdf_pair).
+__device__ __forceinline__ float2 normcdf_arg(float2 a0) { return mul(splat(-fbits(cf::sqrt_2o_2)), a0); }
+__device__ __forceinline__ void normcdf_from_erfc(float2 y, float2 r1, float2& pos, float2& neg)
+{
   const float2 two_m = sub(splat(2.0f), r1);
   pos = mul(splat(0.5f), make_float2((y.x < 0.0f) ? two_m.x : r1.x, (y.y < 0.0f) ? two_m.y : r1.y));
   neg = mul(splat(0.5f), make_float2((y.x > 0.0f) ? two_m.x : r1.x, (y.y > 0.0f) ? two_m.y : r1.y));
 }
+__device__ __forceinline__ void normcdf_pair(float2 a0, float2& pos, float2& neg)
+{
+  const float2 y = normcdf_arg(a0);
+  normcdf_from_erfc(y, erfc_abs(make_float2(fabsf(y.x), fabsf(y.y))), pos, neg);
+}
 
 // The Black-Scholes statement of nt2cuda/blackscholes.cuh (exact mode,
-// normcdf via erfc) for two options; c = fma(sqr(v), 0.5, r).
-__device__ __forceinline__ void blackscholes(float2 S, float2 K, float2 T, float r, float v, float c, float2& call,
-                                             float2& put)
+// normcdf via erfc) for two options, c = fma(sqr(v), 0.5, r), in two halves
+// around the erfc evaluations: bs_front gives the normcdf arguments y1, y2
+// (of d1 and d2) and e = K exp(-r T); bs_back the prices from erfc(|y1|),
+// erfc(|y2|).
+__device__ __forceinline__ void bs_front(float2 S, float2 K, float2 T, float r, float v, float c, float2& y1,
+                                         float2& y2, float2& e)
 {
   const float2 da = make_float2(__fsqrt_rn(T.x), __fsqrt_rn(T.y));
   const float2 vda = mul_r(splat(v), da);
@@ -231,12 +261,26 @@ __device__ __forceinline__ void blackscholes(float2 S, float2 K, float2 T, float
   const float2 num = madd(splat(c), T, log(q));
   const float2 d1 = make_float2(__fdiv_rn(num.x, vda.x), __fdiv_rn(num.y, vda.y));
   const float2 d2 = sub(d1, vda);
-  const float2 e = mul(K, exp(mul_r(splat(-r), T)));
+  e = mul(K, exp(mul_r(splat(-r), T)));
+  y1 = normcdf_arg(d1);
+  y2 = normcdf_arg(d2);
+}
+__device__ __forceinline__ void bs_back(float2 S, float2 e, float2 y1, float2 r1, float2 y2, float2 r2, float2& call,
+                                        float2& put)
+{
   float2 n1, m1, n2, m2;
-  normcdf_pair(d1, n1, m1);
-  normcdf_pair(d2, n2, m2);
+  normcdf_from_erfc(y1, r1, n1, m1);
+  normcdf_from_erfc(y2, r2, n2, m2);
   call = nmsub(e, n2, mul_r(S, n1));
   put = nmsub(S, m1, mul_r(e, m2));
+}
+__device__ __forceinline__ void blackscholes(float2 S, float2 K, float2 T, float r, float v, float c, float2& call,
+                                             float2& put)
+{
+  float2 y1, y2, e;
+  bs_front(S, K, T, r, v, c, y1, y2, e);
+  bs_back(S, e, y1, erfc_abs(make_float2(fabsf(y1.x), fabsf(y1.y))), y2,
+          erfc_abs(make_float2(fabsf(y2.x), fabsf(y2.y))), call, put);
 }
 
 }  // namespace x2

@@ -136,6 +136,39 @@ def test_blackscholes_f32_bit_exact(gpu, oracle, cdf, n):
         assert m == 0.0, (cdf, n, w, S[w], K[w], T[w], got[w], ref[w])
 
 
+@pytest.mark.parametrize("kind", ["all_small", "all_large", "edges", "mixed_chunks"])
+def test_blackscholes_f32_regions_and_edges_bit_exact(gpu, oracle, kind):
+    """The packed exact kernel evaluates both erfc regions and selects per lane: options whose
+    arguments all fall in one region, special values (zeros, infinities, NaN, subnormals, huge
+    and tiny times) and sizes that leave partial groups must still give the oracle's bits (two
+    NaNs compare equal)."""
+    rng = np.random.default_rng(17)
+    if kind == "all_small":              # S ~ K and short T: |d| well below 2/3*sqrt(2)
+        n = 3 * 2048 + 5
+        S = rng.uniform(50, 51, n).astype(np.float32)
+        K = (S * rng.uniform(0.999, 1.001, n)).astype(np.float32)
+        T = rng.uniform(0.01, 0.02, n).astype(np.float32)
+    elif kind == "all_large":            # deep in or out of the money: |d| > 3
+        n = 2 * 2048 + 2
+        S = rng.uniform(5, 6, n).astype(np.float32)
+        K = rng.uniform(90, 100, n).astype(np.float32)
+        T = rng.uniform(0.25, 0.5, n).astype(np.float32)
+    elif kind == "edges":
+        vals = np.array([0.0, -0.0, 1e-45, 1e-38, 1e-20, 0.5, 1.0, 2.0, 1e20, 3e38, np.inf, -np.inf, np.nan, -1.0],
+                        np.float32)
+        S, K, T = (a.ravel().astype(np.float32) for a in np.meshgrid(vals, vals, vals, indexing="ij"))
+        n = S.size
+    else:                                # the configuration's distribution, chunks partly filled
+        n = 7 * 2048 + 1027
+        S, K, T = bs_inputs(n, np.float32, seed=23)
+    c, p = gpu.blackscholes(to_dev(S), to_dev(K), to_dev(T), 0.02, 0.30)
+    rc, rp = oracle.bs(S, K, T, 0.02, 0.30)
+    for got, ref in ((host(c), rc), (host(p), rp)):
+        same = (got.view(np.uint32) == ref.view(np.uint32)) | (np.isnan(got) & np.isnan(ref))
+        w = np.flatnonzero(~same)
+        assert w.size == 0, (kind, w[:5], S[w[:5]], K[w[:5]], T[w[:5]], got[w[:5]], ref[w[:5]])
+
+
 @pytest.mark.parametrize("n", [1, 3, 4099, 1 << 18])
 def test_blackscholes_f64_bit_exact(gpu, oracle, n):
     S, K, T = bs_inputs(n, np.float64, seed=n + 7)
