@@ -524,8 +524,13 @@ struct scan_tiles {
   }
 };
 
+// Compensated FP32 sums (the exact-carry look-back) fit 64 registers without
+// spilling: four blocks per SM then cover each other's look-back barriers.
+template <class Op, class T> struct scan_min_blocks { static constexpr int value = 0; };
+template <> struct scan_min_blocks<fold::op_sum<true>, float> { static constexpr int value = 4; };
+
 template <class Op, class T>
-__global__ void __launch_bounds__(256) k_scan_inner(const T* __restrict__ x, T* __restrict__ y, inner_shape sh,
+__global__ void __launch_bounds__(256, (scan_min_blocks<Op, T>::value)) k_scan_inner(const T* __restrict__ x, T* __restrict__ y, inner_shape sh,
                                                     int vec, unsigned long long* __restrict__ ticket,
                                                     unsigned* __restrict__ flags, void* __restrict__ aggv,
                                                     void* __restrict__ inclv, unsigned* __restrict__ err)
