@@ -900,7 +900,7 @@ def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: in
             api.fill_normal(Ts[i], 23 + i)
         o = torch.empty(rows * cols, device="cuda")
         it = [0]
-        for dim, note in ((1, "one 32 KB tile per column, single pass"), (2, "two passes: chunk totals, then rescan")):
+        for dim, note in ((1, "one 32 KB tile per column, single pass"), (2, "one block per 32-row strip walking the columns, TMA-staged single pass")):
             if part is not None and part not in f"cumsum(A,{dim})":
                 continue
 

@@ -402,22 +402,7 @@ __global__ void __launch_bounds__(256) k_outer_tma(const __grid_constant__ CUten
 }
 
 // ------------------------------------------------------------- launchers
-inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
-{
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    cudaDriverEntryPointQueryResult q;
-    void* p = nullptr;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    else
-      cudaGetLastError();
-  });
-  return fn;
-}
+using tma::tensor_map_encoder;
 
 template <class K> inline cudaError_t set_smem(K kernel, int bytes)
 {

@@ -26,13 +26,18 @@
 // already hold; every wait is bounded, and a tile whose wait runs out writes
 // NaN and passes a failure flag on instead of a prefix.
 //
-// outer_scan runs in two launches: the per-row totals of column chunks, then
-// each chunk rescanned from the left fold of the earlier chunks' totals.
+// outer_scan of a table with at least one 128-byte strip of rows per SM is one
+// pass (k_scan_outer_tma): each block walks the columns of its strip in order,
+// tiles streamed through shared memory by TMA, the rows' running values kept
+// on chip.  Narrower tables run in two launches: the per-row totals of column
+// chunks, then each chunk rescanned from the left fold of the earlier chunks'
+// totals.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "fold.cuh"
 #include "memory.cuh"
+#include "tma.cuh"
 
 namespace nt2cuda {
 namespace scan {
@@ -336,20 +341,27 @@ struct scan_tiles {
         a = Op::merge(a, s_wtot[ww]);
       }
       *out = a;
-      if (publish) {
-        const unsigned flag = w.k == 0 ? F_INCL : F_AGG;
-        if constexpr (CK == CARRY_EXACT) {
-          xsum xa = xzero();
-          xadd_float(xa, a.s);
-          xadd_float(xa, a.c);
-          xstore((w.k == 0 ? xincl : xagg) + t, xa);
-        } else {
-          (w.k == 0 ? incl : agg)[t] = a;
-        }
-        st_release(&flags[t], flag);
-      }
+      if (publish) publish_aggregate(a, w.k, t, flags, agg, incl, xagg, xincl);
     }
     __syncthreads();
+  }
+
+  // Publish tile t's aggregate a: as its inclusive prefix when the tile starts
+  // its column (k == 0), else as an aggregate.
+  __device__ __forceinline__ static void publish_aggregate(const S& a, size_t k, unsigned long long t,
+                                                           unsigned* flags, S* agg, S* incl, xsum* xagg,
+                                                           xsum* xincl)
+  {
+    const unsigned flag = k == 0 ? F_INCL : F_AGG;
+    if constexpr (CK == CARRY_EXACT) {
+      xsum xa = xzero();
+      xadd_float(xa, a.s);
+      xadd_float(xa, a.c);
+      xstore((k == 0 ? xincl : xagg) + t, xa);
+    } else {
+      (k == 0 ? incl : agg)[t] = a;
+    }
+    st_release(&flags[t], flag);
   }
 
   // Look-back (warp 0): the tile's prefix I(t-1) into *prefix and its inclusive
@@ -384,11 +396,13 @@ struct scan_tiles {
         p0 -= 32;
       }
       if (!fail && lane == 0) {
-        *prefix = xto_pair(ex);
-        xadd_float(ex, a.s);
-        xadd_float(ex, a.c);
-        xstore(xincl + t, ex);
+        // publish first: successors wait on it, this tile's own prefix can follow
+        xsum in = ex;
+        xadd_float(in, a.s);
+        xadd_float(in, a.c);
+        xstore(xincl + t, in);
         st_release(&flags[t], F_INCL);
+        *prefix = xto_pair(ex);
       }
     } else if constexpr (CK == CARRY_TREE) {
       // an exact operation: merge any window with a warp tree
@@ -448,6 +462,7 @@ struct scan_tiles {
     if (fail && lane == 0) st_release(&flags[t], F_FAIL);
     return !fail;
   }
+
 
   // Pass 2: every warp rescans its portion from prefix (+) its portion prefix.
   __device__ __forceinline__ static void rescan(const T* x, T* y, const where& w, int vec, const S& prefix,
@@ -760,6 +775,111 @@ __global__ void __launch_bounds__(256) k_scan_inner_short(const T* __restrict__ 
       y[j * rows + r] = (T)Op::finish(st, 0);
     }
   }
+}
+
+// ------------------------------------------------ TMA-staged row scans
+// Row scans (dim 2) of tables with enough rows: each block owns a strip of
+// 128 bytes of rows (32 floats or 16 doubles) and walks every column of it
+// in order, so the table is read and written once and each row's running
+// value stays on chip.  Thread 0 streams tiles of the strip (BR rows x 128
+// columns, 16 KB) through STAGES shared-memory stages with
+// cp.async.bulk.tensor; the threads split a tile's columns in NG groups of CG
+// consecutive columns per row (thread t: row t % BR, group t / BR).  Per
+// tile: every thread folds its CG values, the group totals of each row are
+// folded in group order from the row's carry (group g stops after g of them:
+// its prefix; the last group goes on to the next tile's carry, which it
+// leaves in shared memory), every thread rescans its values from its prefix
+// into the stage, and a TMA store writes the tile back.  Rows past the table
+// and columns past its end read as zeros and are never stored (the tensor
+// map clips both).  A stage is refilled once the store that last used it
+// has read it.
+template <class T> __host__ __device__ constexpr int outer_tma_rows() { return 128 / (int)sizeof(T); }
+constexpr int kOuterTmaCols = 128;
+
+struct outer_tma_shape {
+  size_t rows, cols, strips, ctiles;
+  uint32_t wait_rounds;
+};
+
+template <class Op, class T, int STAGES>
+__global__ void __launch_bounds__(256) k_scan_outer_tma(const __grid_constant__ CUtensorMap xmap,
+                                                        const __grid_constant__ CUtensorMap ymap, outer_tma_shape sh)
+{
+  nt2cuda::mem::pdl_begin();
+  using S = state_of<Op, T>;
+  constexpr int BR = outer_tma_rows<T>(), BC = kOuterTmaCols;
+  constexpr int NG = 256 / BR, CG = BC / NG;
+  constexpr uint32_t TBYTES = (uint32_t)(BR * BC * sizeof(T));
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  T* stage0 = reinterpret_cast<T*>(smem_raw);          // [STAGES][BC][BR], column-major boxes
+  __shared__ __align__(8) uint64_t full[STAGES];
+  __shared__ S s_tot[NG][BR];
+  __shared__ S s_carry[2][BR];
+  const int r = threadIdx.x % BR, g = threadIdx.x / BR;
+  const int row0 = (int)(blockIdx.x * BR);
+
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < STAGES; ++st) tma::mbar_init(&full[st], 1);
+    tma::fence_barrier_init();
+    for (int st = 0; st < STAGES - 1 && (size_t)st < sh.ctiles; ++st) {
+      tma::mbar_arrive_expect_tx(&full[st], TBYTES);
+      tma::tensor_g2s_2d(stage0 + (size_t)st * BR * BC, &xmap, row0, st * BC, &full[st]);
+    }
+  }
+  __syncthreads();
+
+  if (threadIdx.x < BR) s_carry[0][threadIdx.x] = Op::template init<T>();
+  for (size_t k = 0; k < sh.ctiles; ++k) {
+    const int st = (int)(k % STAGES);
+    T* buf = stage0 + (size_t)st * BR * BC;
+    const bool ok = tma::mbar_wait(&full[st], (uint32_t)((k / STAGES) & 1u), sh.wait_rounds);
+    if (__syncthreads_or(!ok)) {
+      // a copy that never landed: wait (bounded) for the rest, leave the
+      // strip's outputs from here on unwritten and count the failure
+      if (threadIdx.x == 0) {
+        atomicAdd(&g_wait_timeouts, 1ull);
+        for (size_t q = k + 1; q < k + STAGES - 1 && q < sh.ctiles; ++q)
+          tma::mbar_wait(&full[q % STAGES], (uint32_t)((q / STAGES) & 1u), sh.wait_rounds);
+        tma::bulk_wait<0>();
+      }
+      return;
+    }
+    T v[CG];
+#pragma unroll
+    for (int i = 0; i < CG; ++i) v[i] = buf[(g * CG + i) * BR + r];
+    S tot = Op::template init<T>();
+#pragma unroll
+    for (int i = 0; i < CG; ++i) Op::add(tot, v[i]);
+    s_tot[g][r] = tot;
+    __syncthreads();
+    // this group's prefix (and, in the last group, the next tile's carry),
+    // folded in group order; g is the same across a warp
+    S pre = s_carry[k & 1][r];
+    for (int gg = 0; gg < g; ++gg) pre = Op::merge(pre, s_tot[gg][r]);
+    if (g == NG - 1) s_carry[(k + 1) & 1][r] = Op::merge(pre, s_tot[g][r]);
+#pragma unroll
+    for (int i = 0; i < CG; ++i) {
+      Op::add(pre, v[i]);
+      v[i] = (T)Op::finish(pre, 0);
+    }
+#pragma unroll
+    for (int i = 0; i < CG; ++i) buf[(g * CG + i) * BR + r] = v[i];
+    tma::fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tma::tensor_s2g_2d(&ymap, row0, (int)(k * BC), buf);
+      tma::bulk_commit();
+      // refill the stage of the previous tile once its store has read it
+      const size_t nk = k + STAGES - 1;
+      if (nk < sh.ctiles) {
+        tma::bulk_wait_read<1>();
+        const int ns = (int)(nk % STAGES);
+        tma::mbar_arrive_expect_tx(&full[ns], TBYTES);
+        tma::tensor_g2s_2d(stage0 + (size_t)ns * BR * BC, &xmap, row0, (int)(nk * BC), &full[ns]);
+      }
+    }
+  }
+  if (threadIdx.x == 0) tma::bulk_wait<0>();
 }
 
 // ------------------------------------------------------------ outer scan

@@ -140,11 +140,53 @@ cudaError_t outer_scan_v(const T* x, T* y, size_t rows, size_t cols, cudaStream_
   return launch_persistent(k_scan_outer<Op, T, V, true>, units * 256, 256, 2, s, a3);
 }
 
+// The TMA-staged row scan (k_scan_outer_tma): one block per strip of
+// 128 bytes of rows walking all columns.  cudaErrorNotSupported, before
+// anything is launched, when the tensor maps cannot be made.
+template <class Op, class T>
+cudaError_t outer_scan_staged(const T* x, T* y, size_t rows, size_t cols, cudaStream_t s)
+{
+  constexpr int BR = outer_tma_rows<T>(), BC = kOuterTmaCols, STAGES = 6;
+  PFN_cuTensorMapEncodeTiled_v12000 encode = tma::tensor_map_encoder();
+  if (!encode) return cudaErrorNotSupported;
+  CUtensorMap xmap, ymap;
+  const cuuint64_t gdim[2] = {(cuuint64_t)rows, (cuuint64_t)cols};
+  const cuuint64_t gstride[1] = {(cuuint64_t)(rows * sizeof(T))};
+  const cuuint32_t box[2] = {(cuuint32_t)BR, (cuuint32_t)BC};
+  const cuuint32_t estride[2] = {1, 1};
+  const CUtensorMapDataType dt = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+  if (encode(&xmap, dt, 2, (void*)x, gdim, gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS ||
+      encode(&ymap, dt, 2, (void*)y, gdim, gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return cudaErrorNotSupported;
+  outer_tma_shape sh;
+  sh.rows = rows;
+  sh.cols = cols;
+  sh.strips = (rows + BR - 1) / BR;
+  sh.ctiles = (cols + BC - 1) / BC;
+  sh.wait_rounds = tma::kMaxRounds;
+  auto k = k_scan_outer_tma<Op, T, STAGES>;
+  const int smem = STAGES * BR * BC * (int)sizeof(T);
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  void* args[] = {(void*)&xmap, (void*)&ymap, (void*)&sh};
+  return launch_dependent(k, sh.strips, 256, s, args, smem);
+}
+
 template <class Op, class T>
 cudaError_t outer_scan(const T* x, T* y, size_t rows, size_t cols, cudaStream_t s)
 {
   if (!rows || !cols) return cudaSuccess;
   constexpr int V = 16 / (int)sizeof(T);
+  // at least one strip of 128 bytes of rows per SM: the staged single pass
+  if ((((uintptr_t)x | (uintptr_t)y) & 15u) == 0 && rows % V == 0 && rows < ((size_t)1 << 31) &&
+      cols < ((size_t)1 << 31) && rows / (size_t)outer_tma_rows<T>() >= (size_t)sm_count()) {
+    const cudaError_t e = outer_scan_staged<Op, T>(x, y, rows, cols, s);
+    if (e != cudaErrorNotSupported) return e;
+  }
   if ((((uintptr_t)x | (uintptr_t)y) & 15u) == 0 && rows % V == 0) return outer_scan_v<Op, T, V>(x, y, rows, cols, s);
   return outer_scan_v<Op, T, 1>(x, y, rows, cols, s);
 }

@@ -13,7 +13,9 @@
 #pragma once
 #include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 #include <stdint.h>
+#include <mutex>
 
 namespace nt2cuda {
 namespace tma {
@@ -90,6 +92,48 @@ __device__ __forceinline__ void tensor_g2s_2d(void* dst, const CUtensorMap* map,
           "r"(smem_u32(dst)),
       "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
       : "memory");
+}
+
+// 2-D tiled store shared -> global through a tensor map (a bulk group of
+// this thread; complete it with bulk_commit and wait with bulk_wait*)
+__device__ __forceinline__ void tensor_s2g_2d(const CUtensorMap* map, int x, int y, const void* src)
+{
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(map), "r"(x),
+               "r"(y), "r"(smem_u32(src))
+               : "memory");
+}
+
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+
+// this thread's bulk groups but the N most recent have finished reading shared memory
+template <int N> __device__ __forceinline__ void bulk_wait_read()
+{
+  asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(N) : "memory");
+}
+
+// this thread's bulk groups but the N most recent have completed
+template <int N> __device__ __forceinline__ void bulk_wait()
+{
+  asm volatile("cp.async.bulk.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// The driver's cuTensorMapEncodeTiled, looked up once (null when the driver
+// does not provide it).
+inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    else
+      cudaGetLastError();
+  });
+  return fn;
 }
 
 }  // namespace tma

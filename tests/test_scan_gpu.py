@@ -103,6 +103,31 @@ def test_cumsum_dim2_config(gpu, shape):
         assert np.array_equal(got.view(np.uint32), again.view(np.uint32))
 
 
+# Row scans of tables with at least one 128-byte strip of rows per SM take the
+# TMA-staged single pass: ragged last strips (rows not a multiple of 32) and
+# ragged last column tiles (cols not a multiple of 128), in place too.
+@pytest.mark.parametrize("shape", [(4868, 130), (8192, 129), (4864, 1), (6000, 300)])
+def test_row_scan_staged(gpu, shape):
+    rows, cols = shape
+    rng = np.random.default_rng(rows + cols)
+    A = rng.standard_normal(rows * cols).astype(np.float32)
+    for comp in (True, False):
+        got = host(gpu.cumulative("cumsum", to_dev(A), rows, cols, 2, compensated=comp))
+        check_cumsum(got, A, rows, cols, 2, comp)
+    L = lines(A, rows, cols, 2)
+    mx = back(np.maximum.accumulate(L, axis=1), rows, cols, 2).astype(np.float32)
+    assert np.array_equal(host(gpu.cumulative("cummax", to_dev(A), rows, cols, 2)), mx)
+    t = to_dev(A)
+    gpu.cumulative("cumsum", t, rows, cols, 2, out=t)
+    check_cumsum(host(t), A, rows, cols, 2, True)
+    D = rng.standard_normal(rows * cols)
+    got = host(gpu.cumulative("cumsum", to_dev(D), rows, cols, 2))
+    LD = lines(D, rows, cols, 2)
+    r = back(np.cumsum(LD, axis=1), rows, cols, 2)
+    cabs = back(np.cumsum(np.abs(LD), axis=1), rows, cols, 2)
+    assert np.all(np.abs(got - r) <= 128 * 2.0 ** -53 * cabs)
+
+
 @pytest.mark.parametrize("shape", [(5, 3), (1000, 7), (20000, 2), (3, 5000)])
 @pytest.mark.parametrize("dim", [1, 2])
 def test_cumprod_f32(gpu, shape, dim):
