@@ -73,6 +73,16 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
   return v;
 }
 
+__device__ __forceinline__ unsigned ld_relaxed(const unsigned* p)
+{
+  unsigned v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// with the relaxed loads before it that saw a released flag: acquire
+__device__ __forceinline__ void fence_acquire() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+
 __device__ __forceinline__ void st_release(unsigned* p, unsigned v)
 {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
@@ -176,8 +186,11 @@ __device__ __forceinline__ void xadd_float(xsum& a, float f)
   xadd_into(a, b);
 }
 
-// Nearest double-float pair (s, c) of the exact value: a fixed sequence of
-// operations, so equal inputs give equal pairs.
+// A float pair (s, c) for the exact value, in integer arithmetic (a fixed
+// function of the bits, so equal sums give equal pairs): s is the value
+// rounded to nearest even (the few values below the smallest subnormal read as
+// zero), c the rest (the 128 bits of the value from its leading one, minus s)
+// rounded from its leading 64 bits.
 __device__ __forceinline__ fold::acc<float> xto_pair(const xsum& x)
 {
   if (x.has_special) return fold::acc<float>{x.special, 0.f};
@@ -194,16 +207,47 @@ __device__ __forceinline__ fold::acc<float> xto_pair(const xsum& x)
       w[i] = n;
     }
   }
-  // each limb split into 32-bit halves (exact in double), summed from the top
-  double d = 0.0;
+  int top = -1;
 #pragma unroll
-  for (int i = 9; i >= 0; --i) {
-    const unsigned half = (unsigned)(w[i >> 1] >> ((i & 1) * 32));
-    d = d + ldexp((double)half, 32 * i - 160);
+  for (int i = 4; i >= 0; --i)
+    if (top < 0 && w[i]) top = i;
+  if (top < 0) return fold::acc<float>{0.f, 0.f};
+  unsigned long long hi = 0ull, mid = 0ull;
+  bool low = false;
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    if (i == top) hi = w[i];
+    if (i == top - 1) mid = w[i];
+    if (i < top - 1 && w[i]) low = true;
   }
-  if (neg) d = -d;
-  const float s = (float)d;
-  const float c = (float)(d - (double)s);
+  const int n = __clzll((long long)hi);
+  const unsigned long long T = n ? (hi << n) | (mid >> (64 - n)) : hi;   // leading one at bit 63
+  const unsigned long long R = mid << n;
+  const int E = 64 * top + 63 - n - 160;                                 // T's leading one is 2^E
+  if (E < -149) return fold::acc<float>{0.f, 0.f};
+  const int k = (E + 150 < 24) ? E + 150 : 24;                           // bits s keeps
+  unsigned long long m = T >> (64 - k);
+  const unsigned long long rest = T << k;
+  const bool up = (rest >> 63) != 0ull && ((rest << 1) != 0ull || R != 0ull || low || (m & 1ull));
+  if (up) ++m;
+  float s = ldexpf((float)m, E - k + 1);
+  float c = 0.f;
+  if (!isinf(s)) {
+    const unsigned __int128 X = ((unsigned __int128)T << 64) | R;
+    const unsigned __int128 M = (unsigned __int128)m << (128 - k);      // wraps to 0 when m = 2^k: M - X is then 2^128 - X
+    const unsigned __int128 d = up ? M - X : X - M;                       // |value - s| in units of 2^(E-127)
+    const unsigned long long dh = (unsigned long long)(d >> 64), dl = (unsigned long long)d;
+    if (dh | dl) {
+      const int rn = dh ? __clzll((long long)dh) : 64 + __clzll((long long)dl);
+      const unsigned long long top64 = (unsigned long long)((d << rn) >> 64);
+      c = ldexpf(__ull2float_rn(top64), E - 127 + 64 - rn);
+      if (up) c = -c;
+    }
+  }
+  if (neg) {
+    s = -s;
+    c = -c;
+  }
   return fold::acc<float>{s, c};
 }
 
@@ -307,8 +351,8 @@ struct scan_tiles {
   // Pass 1: the warps' portion totals, their exclusive prefixes (s_wex) and the
   // tile's aggregate (*out); thread 0 publishes the aggregate when `publish`.
   __device__ __forceinline__ static void aggregate(const T* x, const where& w, int vec, unsigned long long t,
-                                                   bool publish, S* s_wtot, S* s_wex, S* out, unsigned* flags,
-                                                   S* agg, S* incl, xsum* xagg, xsum* xincl)
+                                                   bool publish, S* s_wtot, S* s_wex, S* out, xsum* xout,
+                                                   unsigned* flags, S* agg, S* incl, xsum* xagg, xsum* xincl)
   {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int pc = portion_count(w, warp);
@@ -341,7 +385,7 @@ struct scan_tiles {
         a = Op::merge(a, s_wtot[ww]);
       }
       *out = a;
-      if (publish) publish_aggregate(a, w.k, t, flags, agg, incl, xagg, xincl);
+      if (publish) publish_aggregate(a, w.k, t, flags, agg, incl, xagg, xincl, xout);
     }
     __syncthreads();
   }
@@ -350,7 +394,7 @@ struct scan_tiles {
   // its column (k == 0), else as an aggregate.
   __device__ __forceinline__ static void publish_aggregate(const S& a, size_t k, unsigned long long t,
                                                            unsigned* flags, S* agg, S* incl, xsum* xagg,
-                                                           xsum* xincl)
+                                                           xsum* xincl, xsum* xout)
   {
     const unsigned flag = k == 0 ? F_INCL : F_AGG;
     if constexpr (CK == CARRY_EXACT) {
@@ -358,15 +402,17 @@ struct scan_tiles {
       xadd_float(xa, a.s);
       xadd_float(xa, a.c);
       xstore((k == 0 ? xincl : xagg) + t, xa);
+      *xout = xa;   // the look-back adds it to the prefix it finds
     } else {
       (k == 0 ? incl : agg)[t] = a;
     }
     st_release(&flags[t], flag);
   }
 
+
   // Look-back (warp 0): the tile's prefix I(t-1) into *prefix and its inclusive
   // prefix published; false when a wait ran out or a predecessor failed.
-  __device__ __forceinline__ static bool lookback(const where& w, unsigned long long t, const S& a, S* prefix,
+  __device__ __forceinline__ static bool lookback(const where& w, unsigned long long t, const S& a, const xsum* xa, S* prefix,
                                                   unsigned* flags, S* agg, S* incl, xsum* xagg, xsum* xincl)
   {
     const int lane = threadIdx.x & 31;
@@ -376,30 +422,57 @@ struct scan_tiles {
     }
     bool fail = false;
     if constexpr (CK == CARRY_EXACT) {
+      // A round reads 32 * LB predecessors, LB per lane (tiles p0 - 32 j - lane):
+      // their flags with relaxed loads issued together, one fence for the
+      // acquire, then their values, so a round costs two round trips to L2
+      // whatever LB is.
+      constexpr int LB = 2;
       xsum ex = xzero();                             // exact sum of everything looked at so far
       long long p0 = (long long)t - 1;
       for (unsigned round = 0;; ++round) {
-        const long long p = p0 - lane;
-        unsigned f = F_INCL;                         // before the column: an empty prefix
-        xsum v = xzero();
-        if (p >= w.first) {
-          f = wait_flag(&flags[p]);
-          if (f == F_AGG) v = xload(xagg + p);
-          else if (f == F_INCL) v = xload(xincl + p);
+        unsigned f[LB];
+#pragma unroll
+        for (int j = 0; j < LB; ++j) {
+          const long long p = p0 - 32 * j - lane;
+          f[j] = p >= w.first ? ld_relaxed(&flags[p]) : F_INCL;   // before the column: an empty prefix
         }
-        if (__any_sync(0xffffffffu, f == F_NONE || f == F_FAIL) || round >= kSpinMax) { fail = true; break; }
-        const unsigned im = __ballot_sync(0xffffffffu, f == F_INCL);
-        const int fl = im ? __ffs(im) - 1 : 32;      // nearest inclusive prefix in this window
-        if (lane > fl) v = xzero();
+        for (unsigned it = 0; it < kSpinMax; ++it) {
+          bool pending = false;
+#pragma unroll
+          for (int j = 0; j < LB; ++j) pending |= f[j] == F_NONE;
+          if (!pending) break;
+          __nanosleep(64);
+#pragma unroll
+          for (int j = 0; j < LB; ++j)
+            if (f[j] == F_NONE) f[j] = ld_relaxed(&flags[p0 - 32 * j - lane]);
+        }
+        fence_acquire();
+        bool bad = false;
+        unsigned incl_mask[LB];
+#pragma unroll
+        for (int j = 0; j < LB; ++j) {
+          bad |= f[j] == F_NONE || f[j] == F_FAIL;
+          incl_mask[j] = __ballot_sync(0xffffffffu, f[j] == F_INCL);
+        }
+        if (__any_sync(0xffffffffu, bad) || round >= kSpinMax) { fail = true; break; }
+        int fl = 32 * LB;                            // nearest inclusive prefix in this window
+#pragma unroll
+        for (int j = LB - 1; j >= 0; --j)
+          if (incl_mask[j]) fl = 32 * j + __ffs(incl_mask[j]) - 1;
+        xsum v = xzero();
+#pragma unroll
+        for (int j = 0; j < LB; ++j) {
+          const long long p = p0 - 32 * j - lane;
+          if (p >= w.first && 32 * j + lane <= fl) xadd_into(v, (f[j] == F_AGG) ? xload(xagg + p) : xload(xincl + p));
+        }
         xadd_into(ex, xwarp_sum(v));
-        if (fl < 32) break;
-        p0 -= 32;
+        if (fl < 32 * LB) break;
+        p0 -= 32 * LB;
       }
       if (!fail && lane == 0) {
         // publish first: successors wait on it, this tile's own prefix can follow
         xsum in = ex;
-        xadd_float(in, a.s);
-        xadd_float(in, a.c);
+        xadd_into(in, *xa);
         xstore(xincl + t, in);
         st_release(&flags[t], F_INCL);
         *prefix = xto_pair(ex);
@@ -462,6 +535,7 @@ struct scan_tiles {
     if (fail && lane == 0) st_release(&flags[t], F_FAIL);
     return !fail;
   }
+
 
 
   // Pass 2: every warp rescans its portion from prefix (+) its portion prefix.
@@ -561,6 +635,7 @@ __global__ void __launch_bounds__(256, (scan_min_blocks<Op, T>::value)) k_scan_i
   __shared__ S s_wtot[kWarps];
   __shared__ S s_wex[2][kWarps];
   __shared__ S s_agg[2], s_prefix;
+  __shared__ xsum s_xa[2];
   __shared__ unsigned long long s_tile[2];
   __shared__ int s_fail;
   const bool chained = sh.tiles_per_col > 1;
@@ -571,7 +646,7 @@ __global__ void __launch_bounds__(256, (scan_min_blocks<Op, T>::value)) k_scan_i
   unsigned long long t = s_tile[0];
   if (t >= sh.tiles) return;
   typename K::where w = K::locate(sh, t);
-  K::aggregate(x, w, vec, t, chained, s_wtot, s_wex[0], &s_agg[0], flags, agg, incl, xagg, xincl);
+  K::aggregate(x, w, vec, t, chained, s_wtot, s_wex[0], &s_agg[0], &s_xa[0], flags, agg, incl, xagg, xincl);
   int slot = 0;
   for (;;) {
     // take the next tile and publish its aggregate before waiting on this one's predecessors
@@ -581,13 +656,13 @@ __global__ void __launch_bounds__(256, (scan_min_blocks<Op, T>::value)) k_scan_i
     typename K::where wn{};
     if (tn < sh.tiles) {
       wn = K::locate(sh, tn);
-      K::aggregate(x, wn, vec, tn, chained, s_wtot, s_wex[slot ^ 1], &s_agg[slot ^ 1], flags, agg, incl, xagg,
-                   xincl);
+      K::aggregate(x, wn, vec, tn, chained, s_wtot, s_wex[slot ^ 1], &s_agg[slot ^ 1], &s_xa[slot ^ 1], flags, agg,
+                   incl, xagg, xincl);
     }
     if (threadIdx.x == 0) s_fail = 0;
     if (chained) {
       if (threadIdx.x < 32) {
-        const bool ok = K::lookback(w, t, s_agg[slot], &s_prefix, flags, agg, incl, xagg, xincl);
+        const bool ok = K::lookback(w, t, s_agg[slot], &s_xa[slot], &s_prefix, flags, agg, incl, xagg, xincl);
         if (!ok && threadIdx.x == 0) {
           s_fail = 1;
           atomicOr(err, 1u);
@@ -609,11 +684,10 @@ __global__ void __launch_bounds__(256, (scan_min_blocks<Op, T>::value)) k_scan_i
 
 // Columns of at most one 32 KB tile (8 warps x 32 lanes x 8 consecutive
 // 16-byte chunks): one pass, the tile read once into registers and scanned
-// with no look-back (CHAIN = false).  With CHAIN the same kernel chains tiles
-// through the look-back; it is kept for operations whose carries combine in
-// any order, but costs registers enough that the two-pass tiles above are
-// faster for long columns on this GPU.
-template <class Op, class T, bool CHAIN>
+// with no look-back.  (Chaining such register-held tiles through the
+// look-back costs registers enough that the two-pass tiles above are faster
+// for long columns on this GPU.)
+template <class Op, class T>
 __global__ void __launch_bounds__(256) k_scan_inner_1p(const T* __restrict__ x, T* __restrict__ y, inner_shape sh,
                                                        int vec, unsigned long long* __restrict__ ticket,
                                                        unsigned* __restrict__ flags, void* __restrict__ aggv,
@@ -622,21 +696,14 @@ __global__ void __launch_bounds__(256) k_scan_inner_1p(const T* __restrict__ x, 
   nt2cuda::mem::pdl_begin();
   using K = scan_tiles<Op, T>;
   using S = typename K::S;
-  constexpr int CK = carry_of<Op, T>::value;
   constexpr int CH = chunk_elems<T>();
   constexpr int E = thread_elems<T>();
   constexpr int SPAN = 32 * E;                      // elements per warp
   constexpr int TILE = kWarps * SPAN;
-  S* agg = reinterpret_cast<S*>(aggv);
-  S* incl = reinterpret_cast<S*>(inclv);
-  xsum* xagg = reinterpret_cast<xsum*>(aggv);
-  xsum* xincl = reinterpret_cast<xsum*>(inclv);
   __shared__ __align__(16) uint4 s_buf[kWarps][32 * 9];
   __shared__ S s_wex[kWarps];
   __shared__ S s_wtot[kWarps];
-  __shared__ S s_agg, s_prefix;
   __shared__ unsigned long long s_tile;
-  __shared__ int s_fail;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint4* wb = s_buf[warp];
   T* wbt = reinterpret_cast<T*>(wb);
@@ -701,45 +768,17 @@ __global__ void __launch_bounds__(256) k_scan_inner_1p(const T* __restrict__ x, 
         s_wex[ww] = a;
         a = Op::merge(a, s_wtot[ww]);
       }
-      s_agg = a;
-      s_fail = 0;
-      if (CHAIN && sh.tiles_per_col > 1) {
-        const unsigned flag = w.k == 0 ? F_INCL : F_AGG;
-        if constexpr (CK == CARRY_EXACT) {
-          xsum xa = xzero();
-          xadd_float(xa, a.s);
-          xadd_float(xa, a.c);
-          xstore((w.k == 0 ? xincl : xagg) + t, xa);
-        } else {
-          (w.k == 0 ? incl : agg)[t] = a;
-        }
-        st_release(&flags[t], flag);
-      }
-    }
-    __syncthreads();
-    if (CHAIN && sh.tiles_per_col > 1) {
-      if (warp == 0) {
-        const bool ok = K::lookback(w, t, s_agg, &s_prefix, flags, agg, incl, xagg, xincl);
-        if (!ok && lane == 0) {
-          s_fail = 1;
-          atomicOr(err, 1u);
-          atomicAdd(&g_wait_timeouts, 1ull);
-        }
-      }
-    } else if (threadIdx.x == 0) {
-      s_prefix = Op::template init<T>();
     }
     __syncthreads();
 
-    // ---- outputs from the tile prefix, the warp prefix and the lane prefix
-    const bool failed = s_fail != 0;
+    // ---- outputs from the warp prefix and the lane prefix
     S ex = Op::shfl_from(c, lane > 0 ? lane - 1 : 0);
     if (lane == 0) ex = Op::template init<T>();
-    S st = Op::merge(Op::merge(s_prefix, s_wex[warp]), ex);
+    S st = Op::merge(s_wex[warp], ex);
 #pragma unroll
     for (int e = 0; e < E; ++e) {
       Op::add(st, v[e]);
-      v[e] = failed ? nan_value<T>() : (T)Op::finish(st, 0);
+      v[e] = (T)Op::finish(st, 0);
     }
 #pragma unroll
     for (int cc = 0; cc < 8; ++cc) wb[slot_of(lane, cc)] = *reinterpret_cast<const uint4*>(&v[cc * CH]);

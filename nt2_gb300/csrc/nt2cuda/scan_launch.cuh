@@ -47,7 +47,7 @@ cudaError_t inner_scan(const T* x, T* y, size_t rows, size_t cols, cudaStream_t 
   void* incl = b + head + fbytes + sbytes;
   if ((e = cudaMemsetAsync(b, 0, head + fbytes, s)) != cudaSuccess) return e;
   int vec = ((((uintptr_t)x | (uintptr_t)y) & 15u) == 0 && (rows * sizeof(T)) % 16 == 0) ? 1 : 0;
-  auto k = one_pass ? k_scan_inner_1p<Op, T, false> : k_scan_inner<Op, T>;
+  auto k = one_pass ? k_scan_inner_1p<Op, T> : k_scan_inner<Op, T>;
   size_t grid = (size_t)sm_count() * (size_t)resident_blocks(k, 256);
   if (grid > sh.tiles) grid = sh.tiles;
   void* args[] = {(void*)&x, (void*)&y, (void*)&sh, (void*)&vec, (void*)&ticket, (void*)&flags, (void*)&agg,
