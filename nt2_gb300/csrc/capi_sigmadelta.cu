@@ -29,6 +29,7 @@ constexpr int SD_THREADS = 256;
 constexpr int SD_PIX = 16;                          // pixels per thread per tile
 constexpr size_t SD_TILE = (size_t)SD_THREADS * SD_PIX;
 constexpr int SD_MAX_FRAMES = 64;
+constexpr int SD_BATCH = 8;                         // frames whose loads are issued together
 
 struct sd_desc {
   const uint8_t* frames;
@@ -87,7 +88,7 @@ __device__ __forceinline__ void sd_step1(uint8_t& b, uint8_t f, uint8_t& v, uint
   out = (d < v) ? 0 : 1;
 }
 
-__global__ void __launch_bounds__(SD_THREADS, 4) k_sigmadelta(const sd_desc* __restrict__ desc,
+__global__ void __launch_bounds__(SD_THREADS, 3) k_sigmadelta(const sd_desc* __restrict__ desc,
                                                           const uint64_t* __restrict__ tile_start, int nstreams,
                                                           int nframes, int init)
 {
@@ -111,24 +112,29 @@ __global__ void __launch_bounds__(SD_THREADS, 4) k_sigmadelta(const sd_desc* __r
     const uint64_t p = (t - t0) * SD_TILE + (uint64_t)threadIdx.x * SD_PIX;
     if (p >= d.npix) continue;
     if (d.vec_ok && p + SD_PIX <= d.npix) {
+      // The state and up to SD_BATCH frames are loaded together (one round
+      // trip for the whole batch, 16 bytes x (2 + SD_BATCH) in flight per
+      // thread), then the frames are stepped in order and their labels stored.
+      const __half2 l1024 = __float2half2_rn(1024.0f);
+      int k = first;
+      int cnt = (nframes - k < SD_BATCH) ? nframes - k : SD_BATCH;
+      uint4 f[SD_BATCH];
+      const uint4 wb = __ldcs(reinterpret_cast<const uint4*>((init ? d.frames : d.bkg) + p));
+      uint4 wv = make_uint4(0u, 0u, 0u, 0u);
+      if (!init) wv = __ldcs(reinterpret_cast<const uint4*>(d.var + p));
+#pragma unroll
+      for (int q = 0; q < SD_BATCH; ++q)
+        if (q < cnt) f[q] = __ldcs(reinterpret_cast<const uint4*>(d.frames + (uint64_t)(k + q) * d.frame_stride + p));
       // state for 16 pixels: 8 biased bkg pairs, 8 var pairs
       __half2 b[8], v[8];
+      unpack_bytes(wb.x, b[0], b[1]);
+      unpack_bytes(wb.y, b[2], b[3]);
+      unpack_bytes(wb.z, b[4], b[5]);
+      unpack_bytes(wb.w, b[6], b[7]);
       if (init) {
-        const uint4 w = __ldcs(reinterpret_cast<const uint4*>(d.frames + p));
-        unpack_bytes(w.x, b[0], b[1]);
-        unpack_bytes(w.y, b[2], b[3]);
-        unpack_bytes(w.z, b[4], b[5]);
-        unpack_bytes(w.w, b[6], b[7]);
 #pragma unroll
         for (int q = 0; q < 8; ++q) v[q] = __float2half2_rn(1.0f);
       } else {
-        const uint4 wb = __ldcs(reinterpret_cast<const uint4*>(d.bkg + p));
-        const uint4 wv = __ldcs(reinterpret_cast<const uint4*>(d.var + p));
-        unpack_bytes(wb.x, b[0], b[1]);
-        unpack_bytes(wb.y, b[2], b[3]);
-        unpack_bytes(wb.z, b[4], b[5]);
-        unpack_bytes(wb.w, b[6], b[7]);
-        const __half2 l1024 = __float2half2_rn(1024.0f);
         unpack_bytes(wv.x, v[0], v[1]);
         unpack_bytes(wv.y, v[2], v[3]);
         unpack_bytes(wv.z, v[4], v[5]);
@@ -136,38 +142,9 @@ __global__ void __launch_bounds__(SD_THREADS, 4) k_sigmadelta(const sd_desc* __r
 #pragma unroll
         for (int q = 0; q < 8; ++q) v[q] = __hsub2(v[q], l1024);
       }
-      int k = first;
-#pragma unroll 1
-      for (; k + 4 <= nframes; k += 4) {
-        uint4 f[4];
+      for (;;) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q)
-          f[q] = __ldcs(reinterpret_cast<const uint4*>(d.frames + (uint64_t)(k + q) * d.frame_stride + p));
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const uint32_t fw[4] = {f[q].x, f[q].y, f[q].z, f[q].w};
-          uint32_t ow[4];
-#pragma unroll
-          for (int w = 0; w < 4; ++w) {
-            __half2 flo, fhi;
-            unpack_bytes(fw[w], flo, fhi);
-            const __half2 llo = sd_step_h2(b[2 * w], flo, v[2 * w]);
-            const __half2 lhi = sd_step_h2(b[2 * w + 1], fhi, v[2 * w + 1]);
-            ow[w] = pack_bytes(llo, lhi);
-          }
-          __stcs(reinterpret_cast<uint4*>(d.labels + (uint64_t)(k + q - first) * d.label_stride + p),
-                 make_uint4(ow[0], ow[1], ow[2], ow[3]));
-        }
-      }
-      if (k < nframes) {
-        // the last 1-3 frames as one batch: their loads in flight together
-        const int cnt = nframes - k;
-        uint4 f[3];
-#pragma unroll
-        for (int q = 0; q < 3; ++q)
-          if (q < cnt) f[q] = __ldcs(reinterpret_cast<const uint4*>(d.frames + (uint64_t)(k + q) * d.frame_stride + p));
-#pragma unroll
-        for (int q = 0; q < 3; ++q) {
+        for (int q = 0; q < SD_BATCH; ++q) {
           if (q >= cnt) break;
           const uint32_t fw[4] = {f[q].x, f[q].y, f[q].z, f[q].w};
           uint32_t ow[4];
@@ -182,8 +159,13 @@ __global__ void __launch_bounds__(SD_THREADS, 4) k_sigmadelta(const sd_desc* __r
           __stcs(reinterpret_cast<uint4*>(d.labels + (uint64_t)(k + q - first) * d.label_stride + p),
                  make_uint4(ow[0], ow[1], ow[2], ow[3]));
         }
+        k += cnt;
+        if (k >= nframes) break;
+        cnt = (nframes - k < SD_BATCH) ? nframes - k : SD_BATCH;
+#pragma unroll
+        for (int q = 0; q < SD_BATCH; ++q)
+          if (q < cnt) f[q] = __ldcs(reinterpret_cast<const uint4*>(d.frames + (uint64_t)(k + q) * d.frame_stride + p));
       }
-      const __half2 l1024 = __float2half2_rn(1024.0f);
       uint32_t bw[4], vw[4];
 #pragma unroll
       for (int w = 0; w < 4; ++w) {
