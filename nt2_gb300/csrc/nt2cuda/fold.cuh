@@ -56,9 +56,17 @@ template <bool COMP, class T> __device__ __forceinline__ acc<T> merge(acc<T> a, 
   }
 }
 
+// The value of a compensated pair.  Once the running sum is not finite (an
+// overflow, an infinite or NaN term) its compensation is NaN and the sum
+// itself is the result, as in NT2's plain float sum: inf stays inf.
 template <bool COMP, class T> __device__ __forceinline__ T result(acc<T> a)
 {
-  return COMP ? nt2cuda::math::add(a.s, a.c) : a.s;
+  if constexpr (COMP) {
+    const T r = nt2cuda::math::add(a.s, a.c);
+    return r != r ? a.s : r;
+  } else {
+    return a.s;
+  }
 }
 
 // ------------------------------------------------------------ operations

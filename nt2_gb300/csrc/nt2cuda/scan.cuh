@@ -398,9 +398,10 @@ struct scan_tiles {
   {
     const unsigned flag = k == 0 ? F_INCL : F_AGG;
     if constexpr (CK == CARRY_EXACT) {
+      // the pair's value: s and c, or s alone once s is not finite (fold::result)
       xsum xa = xzero();
       xadd_float(xa, a.s);
-      xadd_float(xa, a.c);
+      if (isfinite(a.s)) xadd_float(xa, a.c);
       xstore((k == 0 ? xincl : xagg) + t, xa);
       *xout = xa;   // the look-back adds it to the prefix it finds
     } else {

@@ -127,6 +127,26 @@ def test_fold_full_config_8192x4096(gpu, oracle):
     assert np.array_equal(host(gpu.sum_colmajor(Ad, rows, cols, 2)).view(np.uint32), rs.view(np.uint32))
 
 
+@pytest.mark.parametrize("comp", [True, False])
+def test_sums_that_overflow_read_inf(gpu, comp):
+    """A float sum that overflows is inf, as NT2's plain float sum gives, on the
+    compensated path too (its compensation turns NaN once the sum is infinite);
+    a NaN term still gives NaN."""
+    x = np.ones(100000, np.float32)
+    x[5000:5004] = np.float32(3.0e38)
+    assert np.isposinf(float(host(gpu.globalsum(to_dev(x), compensated=comp))[0]))
+    A = np.ones((4, 3000), np.float32)     # column-major 3000 x 4
+    A[1, 10:14] = np.float32(3.0e38)
+    A[2, 7] = np.nan
+    flat = A.reshape(-1)
+    cs = host(gpu.sum_colmajor(to_dev(flat), 3000, 4, 1, compensated=comp))
+    assert cs[0] == 3000 and np.isposinf(cs[1]) and np.isnan(cs[2]) and cs[3] == 3000
+    M = np.ones((3000, 4), np.float32)     # column-major 4 x 3000: row sums along dim 2
+    M[10:14, 1] = np.float32(3.0e38)
+    rs = host(gpu.sum_colmajor(to_dev(M.reshape(-1)), 4, 3000, 2, compensated=comp))
+    assert rs[0] == 3000 and np.isposinf(rs[1]) and rs[2] == 3000
+
+
 def test_integer_valued_sums_exact(gpu):
     # modules/core/reduction/unit/table/globalsum.cpp:22-30 and sum.cpp:29-198
     a = torch.arange(1, 10, dtype=torch.float32, device="cuda")

@@ -79,6 +79,33 @@ def test_cumsum_long_vector_reproducible(gpu):
     check_cumsum(p, host(x), n, 1, 1, False)
 
 
+def test_cumsum_long_column_wide_range(gpu):
+    """Tile carries across the look-back (16384-element tiles) over values of every
+    scale: huge terms that cancel, subnormals, exact zeros.  The carries are exact,
+    so the compensated cumsum stays within its FP64 bound; a sum that overflows
+    reads inf from there on, and a NaN poisons every later element."""
+    n = 9 * 16384 + 123
+    rng = np.random.default_rng(21)
+    A = rng.standard_normal(n).astype(np.float32)
+    A[::997] *= np.float32(1e30)                 # huge terms
+    A[1::997] = -A[::997][: len(A[1::997])]      # ... that cancel right after
+    A[2::50] = np.float32(1e-40)                 # subnormals
+    A[3::70] = np.float32(0.0)
+    got = host(gpu.cumulative("cumsum", to_dev(A), n, 1, 1))
+    check_cumsum(got, A, n, 1, 1, True)
+    # overflow: a run of +max values past a tile boundary
+    B = np.ones(n, np.float32)
+    B[40000:40004] = np.float32(3.0e38)
+    got = host(gpu.cumulative("cumsum", to_dev(B), n, 1, 1))
+    assert np.all(np.isfinite(got[:40001])) and np.all(np.isposinf(got[40001:]))
+    # a NaN in the third tile
+    C = np.ones(n, np.float32)
+    C[33000] = np.nan
+    got = host(gpu.cumulative("cumsum", to_dev(C), n, 1, 1))
+    assert np.array_equal(got[:33000], np.arange(1, 33001, dtype=np.float32))
+    assert np.all(np.isnan(got[33000:]))
+
+
 def test_cumsum_integer_valued_exact(gpu):
     # sums of small integers are exact in any order
     n = 1 << 20
