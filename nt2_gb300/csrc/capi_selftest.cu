@@ -34,34 +34,41 @@ __device__ __forceinline__ void record(x2_report* rep, uint32_t u)
   if (k < 8) rep->first[k] = u;
 }
 
-// which: 0 exp, 1 log, 2 erfc of |a|, 3 normcdf(a) and normcdf(-a)
+// which: 0 exp, 1 log, 2 erfc of |a|, 3 normcdf(a) and normcdf(-a); 4..7 the
+// same with each NT2 fma/fnms one hardware FMA (math::*<true>)
+template <bool F> __device__ __forceinline__ void x2_check_pair(int which, uint32_t u0, x2_report* rep)
+{
+  const uint32_t u1 = u0 + 1;
+  const float2 a = make_float2(__uint_as_float(u0), __uint_as_float(u1));
+  if (which == 0) {
+    const float2 r = x2::exp<F>(a);
+    if (!same(r.x, math::exp<F>(a.x))) record(rep, u0);
+    if (!same(r.y, math::exp<F>(a.y))) record(rep, u1);
+  } else if (which == 1) {
+    const float2 r = x2::log<F>(a);
+    if (!same(r.x, math::log<F>(a.x))) record(rep, u0);
+    if (!same(r.y, math::log<F>(a.y))) record(rep, u1);
+  } else if (which == 2) {
+    const float2 x = make_float2(fabsf(a.x), fabsf(a.y));
+    const float2 r = x2::erfc_abs<F>(x);
+    if (!same(r.x, math::erfc_abs<F>(x.x))) record(rep, u0);
+    if (!same(r.y, math::erfc_abs<F>(x.y))) record(rep, u1);
+  } else {
+    float2 pos, neg;
+    x2::normcdf_pair<F>(a, pos, neg);
+    float p0, n0, p1, n1;
+    math::normcdf_pair<F>(a.x, p0, n0);
+    math::normcdf_pair<F>(a.y, p1, n1);
+    if (!same(pos.x, p0) || !same(neg.x, n0)) record(rep, u0);
+    if (!same(pos.y, p1) || !same(neg.y, n1)) record(rep, u1);
+  }
+}
+
 __global__ void __launch_bounds__(256) k_x2_check(int which, uint64_t pairs, x2_report* rep)
 {
   for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < pairs; p += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t u0 = (uint32_t)(2 * p), u1 = u0 + 1;
-    const float2 a = make_float2(__uint_as_float(u0), __uint_as_float(u1));
-    if (which == 0) {
-      const float2 r = x2::exp(a);
-      if (!same(r.x, math::exp<false>(a.x))) record(rep, u0);
-      if (!same(r.y, math::exp<false>(a.y))) record(rep, u1);
-    } else if (which == 1) {
-      const float2 r = x2::log(a);
-      if (!same(r.x, math::log<false>(a.x))) record(rep, u0);
-      if (!same(r.y, math::log<false>(a.y))) record(rep, u1);
-    } else if (which == 2) {
-      const float2 x = make_float2(fabsf(a.x), fabsf(a.y));
-      const float2 r = x2::erfc_abs(x);
-      if (!same(r.x, math::erfc_abs<false>(x.x))) record(rep, u0);
-      if (!same(r.y, math::erfc_abs<false>(x.y))) record(rep, u1);
-    } else {
-      float2 pos, neg;
-      x2::normcdf_pair(a, pos, neg);
-      float p0, n0, p1, n1;
-      math::normcdf_pair<false>(a.x, p0, n0);
-      math::normcdf_pair<false>(a.y, p1, n1);
-      if (!same(pos.x, p0) || !same(neg.x, n0)) record(rep, u0);
-      if (!same(pos.y, p1) || !same(neg.y, n1)) record(rep, u1);
-    }
+    if (which < 4) x2_check_pair<false>(which, (uint32_t)(2 * p), rep);
+    else x2_check_pair<true>(which - 4, (uint32_t)(2 * p), rep);
   }
 }
 
@@ -71,7 +78,7 @@ extern "C" nt2cuda_status nt2cuda_selftest_x2(int which, unsigned long long* mis
                                               nt2cuda_stream stream)
 {
   NT2CUDA_NVTX_RANGE;
-  if (which < 0 || which > 3 || !mismatches) return NT2CUDA_ERR_ARG;
+  if (which < 0 || which > 7 || !mismatches) return NT2CUDA_ERR_ARG;
   cudaStream_t s = as_stream(stream);
   x2_report* rep = nullptr;
   cudaError_t e = cudaMalloc(&rep, sizeof(x2_report));

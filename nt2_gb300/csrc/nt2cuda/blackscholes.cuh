@@ -76,9 +76,10 @@ __device__ __forceinline__ void bs_lane(T S, T K, T Tm, T r, T v, T c, T& call, 
   put = nmsub<F>(S, m1, mul(e, m2));
 }
 
-// Statements priced two options at a time (bs_x2.cuh): exact FP32 with normcdf.
+// Statements priced two options at a time (bs_x2.cuh): FP32 with normcdf,
+// exact or fused (each NT2 fma/fnms one hardware FMA, as bs_lane's).
 template <class T, int CDF, int P>
-constexpr bool kPacked = sizeof(T) == 4 && CDF == CDF_NORMCDF && P == PREC_EXACT;
+constexpr bool kPacked = sizeof(T) == 4 && CDF == CDF_NORMCDF && (P == PREC_EXACT || P == PREC_FUSED);
 
 // V options per thread per group (16 bytes of each input), U groups in
 // flight per grid-stride trip.
@@ -118,7 +119,7 @@ __global__ void __launch_bounds__(256, (kMinBlocks<T, CDF, P, U>))
 #pragma unroll
         for (int l = 0; l < V; l += 2) {
           float2 pc, pp;
-          x2::blackscholes(make_float2(s[u][l], s[u][l + 1]), make_float2(k[u][l], k[u][l + 1]),
+          x2::blackscholes<P == PREC_FUSED>(make_float2(s[u][l], s[u][l + 1]), make_float2(k[u][l], k[u][l + 1]),
                            make_float2(t[u][l], t[u][l + 1]), r, v, c, pc, pp);
           oc[l] = pc.x; oc[l + 1] = pc.y;
           op[l] = pp.x; op[l + 1] = pp.y;
@@ -143,7 +144,7 @@ __global__ void __launch_bounds__(256, (kMinBlocks<T, CDF, P, U>))
 #pragma unroll
       for (int l = 0; l < V; l += 2) {
         float2 pc, pp;
-        x2::blackscholes(make_float2(s[l], s[l + 1]), make_float2(k[l], k[l + 1]), make_float2(t[l], t[l + 1]), r,
+        x2::blackscholes<P == PREC_FUSED>(make_float2(s[l], s[l + 1]), make_float2(k[l], k[l + 1]), make_float2(t[l], t[l + 1]), r,
                          v, c, pc, pp);
         oc[l] = pc.x; oc[l + 1] = pc.y;
         op[l] = pp.x; op[l + 1] = pp.y;

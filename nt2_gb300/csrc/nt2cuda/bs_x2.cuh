@@ -9,7 +9,9 @@
 // (its fma/fnms are a*b+c rounded twice), so the same sequence run on
 // register pairs gives, lane by lane, the same bits for half the issue
 // slots.  What does not pack stays per lane: comparisons, selects,
-// exponent-bit arithmetic and the special-function unit.
+// exponent-bit arithmetic and the special-function unit.  The functors take
+// F as math.cuh's do: F = true makes each NT2 fma/fnms (and Horner step) one
+// fma.rn.f32x2, the fused precision mode's arithmetic.
 //
 // Beyond packing, the steps below are rearranged only where the result is
 // provably the same:
@@ -89,16 +91,25 @@ __device__ __forceinline__ float2 fma(float2 a, float2 b, float2 c)
 }
 // a*b rounded once, as an operand of a later add or subtract (see above)
 __device__ __forceinline__ float2 mul_r(float2 a, float2 b) { return fma(a, b, splat(c_x2_negzero)); }
-// NT2's fma / fnms: a*b+c and c-a*b, each rounded twice
-__device__ __forceinline__ float2 madd(float2 a, float2 b, float2 c) { return add(mul_r(a, b), c); }
-__device__ __forceinline__ float2 nmsub(float2 a, float2 b, float2 c) { return sub(c, mul_r(a, b)); }
+// NT2's fma / fnms: a*b+c and c-a*b, each rounded twice (F = false), or
+// one hardware FMA each (F = true, math::madd<true> / nmsub<true>)
+template <bool F> __device__ __forceinline__ float2 madd(float2 a, float2 b, float2 c)
+{
+  if constexpr (F) return fma(a, b, c);
+  else return add(mul_r(a, b), c);
+}
+template <bool F> __device__ __forceinline__ float2 nmsub(float2 a, float2 b, float2 c)
+{
+  if constexpr (F) return fma(make_float2(-a.x, -a.y), b, c);
+  else return sub(c, mul_r(a, b));
+}
 
-template <int N>
+template <bool F, int N>
 __device__ __forceinline__ float2 horner(float2 x, const uint32_t (&c)[N])
 {
   float2 acc = splat(fbits(c[0]));
 #pragma unroll
-  for (int i = 1; i < N; ++i) acc = madd(x, acc, splat(fbits(c[i])));
+  for (int i = 1; i < N; ++i) acc = madd<F>(x, acc, splat(fbits(c[i])));
   return acc;
 }
 
@@ -113,22 +124,22 @@ __device__ __forceinline__ float scale_from_rounded(float t)
 
 // exp's reduction and polynomial (math::exp) before its selections:
 // returns c * 2^k with k = rint(a0 / ln 2); exact for minlog < a0 < maxlog.
-__device__ __forceinline__ float2 exp_core(float2 a0)
+template <bool F> __device__ __forceinline__ float2 exp_core(float2 a0)
 {
   constexpr uint32_t P[5] = {0x3ab778cfu, 0x3c098d8bu, 0x3d2aa957u, 0x3e2aa9a5u, 0x3f000000u};
   const float2 t = add(mul_r(splat(fbits(cf::invlog_2)), a0), splat(kRound));
   const float2 k = sub(t, splat(kRound));
-  float2 x = nmsub(k, splat(fbits(cf::log_2hi)), a0);
-  x = nmsub(k, splat(fbits(cf::log_2lo)), x);
-  const float2 y = horner(x, P);
-  const float2 c = add(madd(y, mul(x, x), x), splat(1.0f));
+  float2 x = nmsub<F>(k, splat(fbits(cf::log_2hi)), a0);
+  x = nmsub<F>(k, splat(fbits(cf::log_2lo)), x);
+  const float2 y = horner<F>(x, P);
+  const float2 c = add(madd<F>(y, mul(x, x), x), splat(1.0f));
   return mul(c, make_float2(scale_from_rounded(t.x), scale_from_rounded(t.y)));
 }
 
 // NT2's float exp (math::exp), two lanes.
-__device__ __forceinline__ float2 exp(float2 a0)
+template <bool F> __device__ __forceinline__ float2 exp(float2 a0)
 {
-  float2 r = exp_core(a0);
+  float2 r = exp_core<F>(a0);
   const float lo = fbits(cf::minlog), hi = fbits(cf::maxlog), inf = __int_as_float(0x7f800000);
   r.x = (a0.x <= lo) ? 0.0f : r.x;
   r.y = (a0.y <= lo) ? 0.0f : r.y;
@@ -142,10 +153,10 @@ __device__ __forceinline__ bool log_fast_ok(float a)
 {
   return __float_as_uint(a) - 0x00800000u < 0x7f000000u;   // positive, normal, finite
 }
-__device__ __forceinline__ float2 log(float2 a0)
+template <bool F> __device__ __forceinline__ float2 log(float2 a0)
 {
   if (!__all_sync(__activemask(), log_fast_ok(a0.x) && log_fast_ok(a0.y)))
-    return make_float2(math::log<false>(a0.x), math::log<false>(a0.y));
+    return make_float2(math::log<F>(a0.x), math::log<F>(a0.y));
   constexpr uint32_t P[8] = {0xbda5dff0u, 0x3e0229f9u, 0xbe04d6b7u, 0x3e116e80u,
                              0xbe2a6aa0u, 0x3e4cd0a3u, 0xbe800064u, 0x3eaaaaa9u};
   const uint32_t u0 = __float_as_uint(a0.x), u1 = __float_as_uint(a0.y);
@@ -159,10 +170,10 @@ __device__ __forceinline__ float2 log(float2 a0)
                         splat(kRound));
   x = sub(mul_r(x, make_float2(lt0 ? 2.0f : 1.0f, lt1 ? 2.0f : 1.0f)), splat(1.0f));
   const float2 x2 = mul(x, x);
-  float2 y = mul_r(mul(horner(x, P), x), x2);
-  y = madd(fe, splat(fbits(cf::log_2lo)), y);
-  y = madd(splat(-0.5f), x2, y);
-  return madd(splat(fbits(cf::log_2hi)), fe, add(add(x, y), splat(0.0f)));
+  float2 y = mul_r(mul(horner<F>(x, P), x), x2);
+  y = madd<F>(fe, splat(fbits(cf::log_2lo)), y);
+  y = madd<F>(splat(-0.5f), x2, y);
+  return madd<F>(splat(fbits(cf::log_2hi)), fe, add(add(x, y), splat(0.0f)));
 }
 
 // x/(1+x) for x >= 0 (and NaN), as __fdiv_rn(x, 1+x) with x clamped to 2^64
@@ -184,13 +195,13 @@ __device__ __forceinline__ float2 x_over_1px(float2 x)
 
 // The two regions of NT2's float erfc (math::erfc_small / erfc_large) on
 // z = x/(1+x), and the final selection for x = inf.
-__device__ __forceinline__ float2 erfc_small(float2 z)
+template <bool F> __device__ __forceinline__ float2 erfc_small(float2 z)
 {
   constexpr uint32_t P3[9] = {0x41aa8e55u, 0x401b5680u, 0xc010d956u, 0x3f2cff3bu,
                               0xc016c985u, 0xbffc9284u, 0xbfa11698u, 0xbe036d7eu, 0x3f7ffffeu};
-  return mul(sub(splat(1.0f), z), horner(z, P3));
+  return mul(sub(splat(1.0f), z), horner<F>(z, P3));
 }
-__device__ __forceinline__ float2 erfc_large(float2 x, float2 z)
+template <bool F> __device__ __forceinline__ float2 erfc_large(float2 x, float2 z)
 {
   constexpr uint32_t P2[11] = {0xc0283611u, 0x40d67e3bu, 0xc0cd1a85u, 0x4050b063u,
                                0xbfaea865u, 0x3e2006f0u, 0x3e1175c7u, 0x3ec4ca6eu,
@@ -198,11 +209,11 @@ __device__ __forceinline__ float2 erfc_large(float2 x, float2 z)
   // exp(-x*x): the argument is <= 0, so only the underflow selection applies
   const float2 m = mul_r(x, x);
   const float2 na = make_float2(-m.x, -m.y);
-  float2 ex = exp_core(na);
+  float2 ex = exp_core<F>(na);
   const float lo = fbits(cf::minlog);
   ex.x = (na.x <= lo) ? 0.0f : ex.x;
   ex.y = (na.y <= lo) ? 0.0f : ex.y;
-  return mul(ex, horner(sub(z, splat(0.4f)), P2));
+  return mul(ex, horner<F>(sub(z, splat(0.4f)), P2));
 }
 __device__ __forceinline__ float2 erfc_finish(float2 x, float2 r)
 {
@@ -214,10 +225,10 @@ __device__ __forceinline__ float2 erfc_finish(float2 x, float2 r)
 
 // NT2's float erfc of x = |a| (math::erfc_abs), two lanes, both regions
 // computed and the right one selected per lane.
-__device__ __forceinline__ float2 erfc_abs(float2 x)
+template <bool F> __device__ __forceinline__ float2 erfc_abs(float2 x)
 {
   const float2 z = x_over_1px(x);
-  const float2 small = erfc_small(z), large = erfc_large(x, z);
+  const float2 small = erfc_small<F>(z), large = erfc_large<F>(x, z);
   const float two3 = fbits(cf::twothird);
   return erfc_finish(x, make_float2((x.x < two3) ? small.x : large.x, (x.y < two3) ? small.y : large.y));
 }
@@ -225,12 +236,12 @@ __device__ __forceinline__ float2 erfc_abs(float2 x)
 // The same for a pair whose lanes are known to lie in one region (region 0:
 // both x < 2/3, 1: both not), or not (2): only the regions needed run, and
 // each lane gets what erfc_abs gives it.
-__device__ __forceinline__ float2 erfc_abs_region(float2 x, int region)
+template <bool F> __device__ __forceinline__ float2 erfc_abs_region(float2 x, int region)
 {
   const float2 z = x_over_1px(x);
-  if (region == 0) return erfc_finish(x, erfc_small(z));
-  if (region == 1) return erfc_finish(x, erfc_large(x, z));
-  return erfc_abs(x);
+  if (region == 0) return erfc_finish(x, erfc_small<F>(z));
+  if (region == 1) return erfc_finish(x, erfc_large<F>(x, z));
+  return erfc_abs<F>(x);
 }
 
 // normcdf(a) and normcdf(-a) from erfc of |y|, y = -a sqrt(2)/2 (math::normcdf_pair).
@@ -241,10 +252,10 @@ __device__ __forceinline__ void normcdf_from_erfc(float2 y, float2 r1, float2& p
   pos = mul(splat(0.5f), make_float2((y.x < 0.0f) ? two_m.x : r1.x, (y.y < 0.0f) ? two_m.y : r1.y));
   neg = mul(splat(0.5f), make_float2((y.x > 0.0f) ? two_m.x : r1.x, (y.y > 0.0f) ? two_m.y : r1.y));
 }
-__device__ __forceinline__ void normcdf_pair(float2 a0, float2& pos, float2& neg)
+template <bool F> __device__ __forceinline__ void normcdf_pair(float2 a0, float2& pos, float2& neg)
 {
   const float2 y = normcdf_arg(a0);
-  normcdf_from_erfc(y, erfc_abs(make_float2(fabsf(y.x), fabsf(y.y))), pos, neg);
+  normcdf_from_erfc(y, erfc_abs<F>(make_float2(fabsf(y.x), fabsf(y.y))), pos, neg);
 }
 
 // The Black-Scholes statement of nt2cuda/blackscholes.cuh (exact mode,
@@ -252,35 +263,38 @@ __device__ __forceinline__ void normcdf_pair(float2 a0, float2& pos, float2& neg
 // around the erfc evaluations: bs_front gives the normcdf arguments y1, y2
 // (of d1 and d2) and e = K exp(-r T); bs_back the prices from erfc(|y1|),
 // erfc(|y2|).
+template <bool F>
 __device__ __forceinline__ void bs_front(float2 S, float2 K, float2 T, float r, float v, float c, float2& y1,
                                          float2& y2, float2& e)
 {
   const float2 da = make_float2(__fsqrt_rn(T.x), __fsqrt_rn(T.y));
   const float2 vda = mul_r(splat(v), da);
   const float2 q = make_float2(__fdiv_rn(S.x, K.x), __fdiv_rn(S.y, K.y));
-  const float2 num = madd(splat(c), T, log(q));
+  const float2 num = madd<F>(splat(c), T, log<F>(q));
   const float2 d1 = make_float2(__fdiv_rn(num.x, vda.x), __fdiv_rn(num.y, vda.y));
   const float2 d2 = sub(d1, vda);
-  e = mul(K, exp(mul_r(splat(-r), T)));
+  e = mul(K, exp<F>(mul_r(splat(-r), T)));
   y1 = normcdf_arg(d1);
   y2 = normcdf_arg(d2);
 }
+template <bool F>
 __device__ __forceinline__ void bs_back(float2 S, float2 e, float2 y1, float2 r1, float2 y2, float2 r2, float2& call,
                                         float2& put)
 {
   float2 n1, m1, n2, m2;
   normcdf_from_erfc(y1, r1, n1, m1);
   normcdf_from_erfc(y2, r2, n2, m2);
-  call = nmsub(e, n2, mul_r(S, n1));
-  put = nmsub(S, m1, mul_r(e, m2));
+  call = nmsub<F>(e, n2, mul_r(S, n1));
+  put = nmsub<F>(S, m1, mul_r(e, m2));
 }
+template <bool F>
 __device__ __forceinline__ void blackscholes(float2 S, float2 K, float2 T, float r, float v, float c, float2& call,
                                              float2& put)
 {
   float2 y1, y2, e;
-  bs_front(S, K, T, r, v, c, y1, y2, e);
-  bs_back(S, e, y1, erfc_abs(make_float2(fabsf(y1.x), fabsf(y1.y))), y2,
-          erfc_abs(make_float2(fabsf(y2.x), fabsf(y2.y))), call, put);
+  bs_front<F>(S, K, T, r, v, c, y1, y2, e);
+  bs_back<F>(S, e, y1, erfc_abs<F>(make_float2(fabsf(y1.x), fabsf(y1.y))), y2,
+             erfc_abs<F>(make_float2(fabsf(y2.x), fabsf(y2.y))), call, put);
 }
 
 }  // namespace x2

@@ -83,7 +83,7 @@ __device__ __forceinline__ void bs_tile(const req_desc& d, uint64_t base)
 #pragma unroll
         for (int l = 0; l < 4; l += 2) {
           float2 pc, pp;
-          x2::blackscholes(make_float2(s[l], s[l + 1]), make_float2(k[l], k[l + 1]), make_float2(tt[l], tt[l + 1]),
+          x2::blackscholes<P == PREC_FUSED>(make_float2(s[l], s[l + 1]), make_float2(k[l], k[l + 1]), make_float2(tt[l], tt[l + 1]),
                            d.r, d.sigma, c, pc, pp);
           oc[l] = pc.x; oc[l + 1] = pc.y;
           op[l] = pp.x; op[l + 1] = pp.y;

@@ -1,8 +1,10 @@
-"""The exact FP32 Black-Scholes kernel prices two options at a time on Blackwell's
-packed FP32 instructions (nt2cuda/bs_x2.cuh).  Its two-lane exp, log, erfc and
-normcdf must give the one-lane functors' bits for every float argument: each
-check below runs over all 2^32 bit patterns on the GPU and must find no
-difference (NaN-ness must agree; payloads are not compared)."""
+"""The exact and fused FP32 Black-Scholes kernels price two options at a time on
+Blackwell's packed FP32 instructions (nt2cuda/bs_x2.cuh).  Their two-lane exp,
+log, erfc and normcdf must give the one-lane functors' bits for every float
+argument, in NT2's twice-rounded arithmetic and with each fma/fnms one hardware
+FMA (the fused mode): each check below runs over all 2^32 bit patterns on the
+GPU and must find no difference (NaN-ness must agree; payloads are not
+compared)."""
 import ctypes as C
 
 import pytest
@@ -11,10 +13,12 @@ import torch
 pytestmark = pytest.mark.gpu
 
 
+@pytest.mark.parametrize("fused", [False, True])
 @pytest.mark.parametrize("which,name", [(0, "exp"), (1, "log"), (2, "erfc(|a|)"), (3, "normcdf(a), normcdf(-a)")])
-def test_two_lane_functor_is_bit_exact_over_every_float(gpu, cuda_lib, which, name):
+def test_two_lane_functor_is_bit_exact_over_every_float(gpu, cuda_lib, which, name, fused):
     n = C.c_ulonglong(99)
     first = (C.c_uint32 * 8)()
-    st = cuda_lib.nt2cuda_selftest_x2(which, C.byref(n), first, torch.cuda.current_stream().cuda_stream)
+    st = cuda_lib.nt2cuda_selftest_x2(which + (4 if fused else 0), C.byref(n), first,
+                                      torch.cuda.current_stream().cuda_stream)
     assert st == 0
     assert n.value == 0, (name, n.value, [hex(first[i]) for i in range(min(8, n.value))])
