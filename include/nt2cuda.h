@@ -450,14 +450,16 @@ nt2cuda_status nt2cuda_selftest_wait_timeout(nt2cuda_stream stream);
 nt2cuda_status nt2cuda_selftest_fold_timeout(const float* A, size_t rows, size_t cols, float* out,
                                              nt2cuda_stream stream);
 
-/* No counterpart in the reference.  The exact and fused FP32 Black-Scholes
- * kernels price two options at a time on the packed FP32 instructions; this
- * checks their two-lane functors against the one-lane ones over every float
- * argument (2^32 values): which = 0 exp, 1 log, 2 erfc of |a|, 3 normcdf(a)
- * with normcdf(-a); 4..7 the same functors with each NT2 fma/fnms one
- * hardware FMA (the fused precision mode).  *mismatches = arguments whose results differ in any bit (two
- * NaNs are equal); first_bad (8 entries, may be NULL) gets the first ones'
- * bit patterns.  Synchronous. */
+/* No counterpart in the reference.  The FP32 Black-Scholes kernels (exact,
+ * fused and fast modes) price two options at a time on the packed FP32
+ * instructions; this checks their two-lane functors against the one-lane ones
+ * over every float argument (2^32 values): which = 0 exp, 1 log, 2 erfc of
+ * |a|, 3 normcdf(a) with normcdf(-a); 4..7 the same functors with each NT2
+ * fma/fnms one hardware FMA (the fused precision mode); 8..11 the fast mode's
+ * exp of a moderate argument, log, erfc of |a| and normcdf pair.
+ * *mismatches = arguments whose results differ in any bit (two NaNs are
+ * equal); first_bad (8 entries, may be NULL) gets the first ones' bit
+ * patterns.  Synchronous. */
 nt2cuda_status nt2cuda_selftest_x2(int which, unsigned long long* mismatches, uint32_t* first_bad,
                                    nt2cuda_stream stream);
 

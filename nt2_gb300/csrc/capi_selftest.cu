@@ -64,11 +64,41 @@ template <bool F> __device__ __forceinline__ void x2_check_pair(int which, uint3
   }
 }
 
+// 8..11: the fast mode's exp_small, log, erfc(|a|) and normcdf pair (math::fast)
+__device__ __forceinline__ void x2_check_fast(int which, uint32_t u0, x2_report* rep)
+{
+  const uint32_t u1 = u0 + 1;
+  const float2 a = make_float2(__uint_as_float(u0), __uint_as_float(u1));
+  if (which == 0) {
+    const float2 r = x2::fast::exp_small(a);
+    if (!same(r.x, math::fast::exp_small(a.x))) record(rep, u0);
+    if (!same(r.y, math::fast::exp_small(a.y))) record(rep, u1);
+  } else if (which == 1) {
+    const float2 r = x2::fast::log(a);
+    if (!same(r.x, math::fast::log(a.x))) record(rep, u0);
+    if (!same(r.y, math::fast::log(a.y))) record(rep, u1);
+  } else if (which == 2) {
+    const float2 x = make_float2(fabsf(a.x), fabsf(a.y));
+    const float2 r = x2::fast::erfc_abs_nr(x);
+    if (!same(r.x, math::fast::erfc_abs_nr(x.x))) record(rep, u0);
+    if (!same(r.y, math::fast::erfc_abs_nr(x.y))) record(rep, u1);
+  } else {
+    float2 pos, neg;
+    x2::fast::normcdf_pair(a, pos, neg);
+    float p0, n0, p1, n1;
+    math::fast::normcdf_pair(a.x, p0, n0);
+    math::fast::normcdf_pair(a.y, p1, n1);
+    if (!same(pos.x, p0) || !same(neg.x, n0)) record(rep, u0);
+    if (!same(pos.y, p1) || !same(neg.y, n1)) record(rep, u1);
+  }
+}
+
 __global__ void __launch_bounds__(256) k_x2_check(int which, uint64_t pairs, x2_report* rep)
 {
   for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < pairs; p += (uint64_t)gridDim.x * blockDim.x) {
     if (which < 4) x2_check_pair<false>(which, (uint32_t)(2 * p), rep);
-    else x2_check_pair<true>(which - 4, (uint32_t)(2 * p), rep);
+    else if (which < 8) x2_check_pair<true>(which - 4, (uint32_t)(2 * p), rep);
+    else x2_check_fast(which - 8, (uint32_t)(2 * p), rep);
   }
 }
 
@@ -78,7 +108,7 @@ extern "C" nt2cuda_status nt2cuda_selftest_x2(int which, unsigned long long* mis
                                               nt2cuda_stream stream)
 {
   NT2CUDA_NVTX_RANGE;
-  if (which < 0 || which > 7 || !mismatches) return NT2CUDA_ERR_ARG;
+  if (which < 0 || which > 11 || !mismatches) return NT2CUDA_ERR_ARG;
   cudaStream_t s = as_stream(stream);
   x2_report* rep = nullptr;
   cudaError_t e = cudaMalloc(&rep, sizeof(x2_report));

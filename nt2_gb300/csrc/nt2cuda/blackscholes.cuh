@@ -80,6 +80,9 @@ __device__ __forceinline__ void bs_lane(T S, T K, T Tm, T r, T v, T c, T& call, 
 // exact or fused (each NT2 fma/fnms one hardware FMA, as bs_lane's).
 template <class T, int CDF, int P>
 constexpr bool kPacked = sizeof(T) == 4 && CDF == CDF_NORMCDF && (P == PREC_EXACT || P == PREC_FUSED);
+// ... and the fast mode's statement (x2::fast), bit-identical to bs_lane's fast branch.
+template <class T, int CDF, int P>
+constexpr bool kPackedFast = sizeof(T) == 4 && CDF == CDF_NORMCDF && P == PREC_FAST;
 
 // V options per thread per group (16 bytes of each input), U groups in
 // flight per grid-stride trip.
@@ -115,12 +118,14 @@ __global__ void __launch_bounds__(256, (kMinBlocks<T, CDF, P, U>))
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       T oc[V], op[V];
-      if constexpr (kPacked<T, CDF, P>) {
+      if constexpr (kPacked<T, CDF, P> || kPackedFast<T, CDF, P>) {
 #pragma unroll
         for (int l = 0; l < V; l += 2) {
           float2 pc, pp;
-          x2::blackscholes<P == PREC_FUSED>(make_float2(s[u][l], s[u][l + 1]), make_float2(k[u][l], k[u][l + 1]),
-                           make_float2(t[u][l], t[u][l + 1]), r, v, c, pc, pp);
+          const float2 ps = make_float2(s[u][l], s[u][l + 1]), pk = make_float2(k[u][l], k[u][l + 1]),
+                       pt = make_float2(t[u][l], t[u][l + 1]);
+          if constexpr (kPackedFast<T, CDF, P>) x2::fast::blackscholes(ps, pk, pt, r, v, c, pc, pp);
+          else x2::blackscholes<P == PREC_FUSED>(ps, pk, pt, r, v, c, pc, pp);
           oc[l] = pc.x; oc[l + 1] = pc.y;
           op[l] = pp.x; op[l + 1] = pp.y;
         }
@@ -140,12 +145,13 @@ __global__ void __launch_bounds__(256, (kMinBlocks<T, CDF, P, U>))
     mem::load_vec<T, V, true>(S, i, s);
     mem::load_vec<T, V, true>(K, i, k);
     mem::load_vec<T, V, true>(Tm, i, t);
-    if constexpr (kPacked<T, CDF, P>) {
+    if constexpr (kPacked<T, CDF, P> || kPackedFast<T, CDF, P>) {
 #pragma unroll
       for (int l = 0; l < V; l += 2) {
         float2 pc, pp;
-        x2::blackscholes<P == PREC_FUSED>(make_float2(s[l], s[l + 1]), make_float2(k[l], k[l + 1]), make_float2(t[l], t[l + 1]), r,
-                         v, c, pc, pp);
+        const float2 ps = make_float2(s[l], s[l + 1]), pk = make_float2(k[l], k[l + 1]), pt = make_float2(t[l], t[l + 1]);
+        if constexpr (kPackedFast<T, CDF, P>) x2::fast::blackscholes(ps, pk, pt, r, v, c, pc, pp);
+        else x2::blackscholes<P == PREC_FUSED>(ps, pk, pt, r, v, c, pc, pp);
         oc[l] = pc.x; oc[l + 1] = pc.y;
         op[l] = pp.x; op[l + 1] = pp.y;
       }

@@ -297,5 +297,76 @@ __device__ __forceinline__ void blackscholes(float2 S, float2 K, float2 T, float
              erfc_abs<F>(make_float2(fabsf(y2.x), fabsf(y2.y))), call, put);
 }
 
+// ------------------------------------------------------------ fast mode
+// The fast precision mode's functors (math::fast) two lanes at a time: the
+// special-function-unit steps (ex2, lg2, rsqrt, the reciprocal divisions) per
+// lane, every FMA, multiply and add packed; a product that feeds an add is
+// formed by mul_r as above, so each lane gets the one-lane function's bits.
+namespace fast {
+
+__device__ __forceinline__ float2 ex2(float2 x) { return make_float2(math::fast::ex2(x.x), math::fast::ex2(x.y)); }
+
+__device__ __forceinline__ float2 exp_small(float2 x) { return ex2(mul(x, splat(1.4426950408889634f))); }
+
+__device__ __forceinline__ float2 log(float2 a0)
+{
+  const float2 r0 = mul(make_float2(math::fast::lg2(a0.x), math::fast::lg2(a0.y)), splat(0.69314718055994530942f));
+  float r[2] = {r0.x, r0.y};
+  const float a[2] = {a0.x, a0.y};
+#pragma unroll
+  for (int l = 0; l < 2; ++l) {
+    r[l] = (a[l] < 0.0f || a[l] != a[l]) ? __int_as_float(0x7fffffff) : r[l];
+    r[l] = (a[l] == __int_as_float(0x7f800000)) ? a[l] : r[l];
+    r[l] = (a[l] == 0.0f) ? __int_as_float(0xff800000) : r[l];
+  }
+  return make_float2(r[0], r[1]);
+}
+
+__device__ __forceinline__ float2 erfc_abs_nr(float2 x)
+{
+  const float2 y = fma(splat(0.5f), x, splat(1.0f));
+  const float2 t = make_float2(__fdividef(1.0f, y.x), __fdividef(1.0f, y.y));
+  float2 p = splat(0.17087277f);
+  p = fma(p, t, splat(-0.82215223f));
+  p = fma(p, t, splat(1.48851587f));
+  p = fma(p, t, splat(-1.13520398f));
+  p = fma(p, t, splat(0.27886807f));
+  p = fma(p, t, splat(-0.18628806f));
+  p = fma(p, t, splat(0.09678418f));
+  p = fma(p, t, splat(0.37409196f));
+  p = fma(p, t, splat(1.00002368f));
+  p = fma(p, t, splat(-1.26551223f));
+  return mul_r(t, exp_small(fma(make_float2(-x.x, -x.y), x, p)));
+}
+
+__device__ __forceinline__ void normcdf_pair(float2 a0, float2& pos, float2& neg)
+{
+  const float2 y = mul(splat(-fbits(cf::sqrt_2o_2)), a0);
+  const float2 r1 = erfc_abs_nr(make_float2(fabsf(y.x), fabsf(y.y)));
+  const float2 two_m = sub(splat(2.0f), r1);
+  pos = mul(splat(0.5f), make_float2((y.x < 0.0f) ? two_m.x : r1.x, (y.y < 0.0f) ? two_m.y : r1.y));
+  neg = mul(splat(0.5f), make_float2((-y.x < 0.0f) ? two_m.x : r1.x, (-y.y < 0.0f) ? two_m.y : r1.y));
+}
+
+// bs_lane's fast branch (normcdf), two options
+__device__ __forceinline__ void blackscholes(float2 S, float2 K, float2 T, float r, float v, float c, float2& call,
+                                             float2& put)
+{
+  const float2 rs = make_float2(rsqrtf(T.x), rsqrtf(T.y));
+  const float2 vda = mul_r(splat(v), mul(T, rs));
+  const float2 q = log(make_float2(__fdividef(S.x, K.x), __fdividef(S.y, K.y)));
+  const float2 num = fma(splat(c), T, q);
+  const float2 d1 = make_float2(__fdividef(num.x, vda.x), __fdividef(num.y, vda.y));
+  const float2 d2 = sub(d1, vda);
+  const float2 e = mul(K, exp_small(mul(splat(-r), T)));
+  float2 n1, m1, n2, m2;
+  normcdf_pair(d1, n1, m1);
+  normcdf_pair(d2, n2, m2);
+  call = fma(make_float2(-e.x, -e.y), n2, mul(S, n1));
+  put = fma(make_float2(-S.x, -S.y), m1, mul(e, m2));
+}
+
+}  // namespace fast
+
 }  // namespace x2
 }  // namespace nt2cuda

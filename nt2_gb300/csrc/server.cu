@@ -79,12 +79,14 @@ __device__ __forceinline__ void bs_tile(const req_desc& d, uint64_t base)
       mem::load_vec<float, 4, true>(d.S, i, s);
       mem::load_vec<float, 4, true>(d.K, i, k);
       mem::load_vec<float, 4, true>(d.T, i, tt);
-      if constexpr (kPacked<float, CDF, P>) {
+      if constexpr (kPacked<float, CDF, P> || kPackedFast<float, CDF, P>) {
 #pragma unroll
         for (int l = 0; l < 4; l += 2) {
           float2 pc, pp;
-          x2::blackscholes<P == PREC_FUSED>(make_float2(s[l], s[l + 1]), make_float2(k[l], k[l + 1]), make_float2(tt[l], tt[l + 1]),
-                           d.r, d.sigma, c, pc, pp);
+          const float2 ps = make_float2(s[l], s[l + 1]), pk = make_float2(k[l], k[l + 1]),
+                       pt = make_float2(tt[l], tt[l + 1]);
+          if constexpr (kPackedFast<float, CDF, P>) x2::fast::blackscholes(ps, pk, pt, d.r, d.sigma, c, pc, pp);
+          else x2::blackscholes<P == PREC_FUSED>(ps, pk, pt, d.r, d.sigma, c, pc, pp);
           oc[l] = pc.x; oc[l + 1] = pc.y;
           op[l] = pp.x; op[l + 1] = pp.y;
         }

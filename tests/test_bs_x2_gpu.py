@@ -22,3 +22,15 @@ def test_two_lane_functor_is_bit_exact_over_every_float(gpu, cuda_lib, which, na
                                       torch.cuda.current_stream().cuda_stream)
     assert st == 0
     assert n.value == 0, (name, n.value, [hex(first[i]) for i in range(min(8, n.value))])
+
+
+@pytest.mark.parametrize("which,name", [(8, "exp_small"), (9, "log"), (10, "erfc(|a|), Numerical Recipes fit"),
+                                        (11, "normcdf(a), normcdf(-a)")])
+def test_two_lane_fast_functor_matches_one_lane_over_every_float(gpu, cuda_lib, which, name):
+    """The fast precision mode's packed functors give its one-lane functors' bits
+    (ex2/lg2/reciprocals per lane, the FMAs, multiplies and adds packed)."""
+    n = C.c_ulonglong(99)
+    first = (C.c_uint32 * 8)()
+    st = cuda_lib.nt2cuda_selftest_x2(which, C.byref(n), first, torch.cuda.current_stream().cuda_stream)
+    assert st == 0
+    assert n.value == 0, (name, n.value, [hex(first[i]) for i in range(min(8, n.value))])
