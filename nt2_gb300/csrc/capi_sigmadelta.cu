@@ -69,13 +69,13 @@ __device__ __forceinline__ __half2 sd_step_h2(__half2& b, __half2 f, __half2& v)
   const __half2 one = __float2half2_rn(1.0f), mone = __float2half2_rn(-1.0f);
   const __half2 zero = __float2half2_rn(0.0f), c255 = __float2half2_rn(255.0f);
   const __half2 three = __float2half2_rn(3.0f);
-  const __half2 l1024 = __float2half2_rn(1024.0f), l1025 = __float2half2_rn(1025.0f);
+  const __half2 l1024 = __float2half2_rn(1024.0f);
   b = __hadd2(b, __hmax2(__hmin2(__hsub2(f, b), one), mone));          // bkg one step toward fr
   const __half2 d = __habs2(__hsub2(f, b));                           // |bkg - fr|
   const __half2 m = __hmin2(__hmul2(d, three), c255);                 // adds(adds(d,d),d)
   const __half2 nz = __hmin2(d, one);                                 // d != 0
   v = __hfma2(nz, __hmax2(__hmin2(__hsub2(m, v), one), mone), v);     // var one step toward m
-  return __hmax2(__hmin2(__hadd2(__hsub2(d, v), l1025), l1025), l1024);  // 1024 + (d >= var)
+  return __hadd2(__hge2(d, v), l1024);                                // 1024 + (d >= var)
 }
 
 __device__ __forceinline__ void sd_step1(uint8_t& b, uint8_t f, uint8_t& v, uint8_t& out)
