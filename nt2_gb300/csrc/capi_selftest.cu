@@ -93,12 +93,28 @@ __device__ __forceinline__ void x2_check_fast(int which, uint32_t u0, x2_report*
   }
 }
 
+// 12, 13: fastnormcdf(a) and fastnormcdf(-a), NT2's arithmetic and fused
+template <bool F> __device__ __forceinline__ void x2_check_fnc(uint32_t u0, x2_report* rep)
+{
+  const uint32_t u1 = u0 + 1;
+  const float2 a = make_float2(__uint_as_float(u0), __uint_as_float(u1));
+  float2 pos, neg;
+  x2::fastnormcdf_pair<F>(a, pos, neg);
+  float p0, n0, p1, n1;
+  math::fastnormcdf_pair<F>(a.x, p0, n0);
+  math::fastnormcdf_pair<F>(a.y, p1, n1);
+  if (!same(pos.x, p0) || !same(neg.x, n0)) record(rep, u0);
+  if (!same(pos.y, p1) || !same(neg.y, n1)) record(rep, u1);
+}
+
 __global__ void __launch_bounds__(256) k_x2_check(int which, uint64_t pairs, x2_report* rep)
 {
   for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < pairs; p += (uint64_t)gridDim.x * blockDim.x) {
     if (which < 4) x2_check_pair<false>(which, (uint32_t)(2 * p), rep);
     else if (which < 8) x2_check_pair<true>(which - 4, (uint32_t)(2 * p), rep);
-    else x2_check_fast(which - 8, (uint32_t)(2 * p), rep);
+    else if (which < 12) x2_check_fast(which - 8, (uint32_t)(2 * p), rep);
+    else if (which == 12) x2_check_fnc<false>((uint32_t)(2 * p), rep);
+    else x2_check_fnc<true>((uint32_t)(2 * p), rep);
   }
 }
 
@@ -108,7 +124,7 @@ extern "C" nt2cuda_status nt2cuda_selftest_x2(int which, unsigned long long* mis
                                               nt2cuda_stream stream)
 {
   NT2CUDA_NVTX_RANGE;
-  if (which < 0 || which > 11 || !mismatches) return NT2CUDA_ERR_ARG;
+  if (which < 0 || which > 13 || !mismatches) return NT2CUDA_ERR_ARG;
   cudaStream_t s = as_stream(stream);
   x2_report* rep = nullptr;
   cudaError_t e = cudaMalloc(&rep, sizeof(x2_report));

@@ -76,10 +76,10 @@ __device__ __forceinline__ void bs_lane(T S, T K, T Tm, T r, T v, T c, T& call, 
   put = nmsub<F>(S, m1, mul(e, m2));
 }
 
-// Statements priced two options at a time (bs_x2.cuh): FP32 with normcdf,
-// exact or fused (each NT2 fma/fnms one hardware FMA, as bs_lane's).
+// Statements priced two options at a time (bs_x2.cuh): FP32, normcdf or
+// fastnormcdf, exact or fused (each NT2 fma/fnms one hardware FMA, as bs_lane's).
 template <class T, int CDF, int P>
-constexpr bool kPacked = sizeof(T) == 4 && CDF == CDF_NORMCDF && (P == PREC_EXACT || P == PREC_FUSED);
+constexpr bool kPacked = sizeof(T) == 4 && (P == PREC_EXACT || P == PREC_FUSED);
 // ... and the fast mode's statement (x2::fast), bit-identical to bs_lane's fast branch.
 template <class T, int CDF, int P>
 constexpr bool kPackedFast = sizeof(T) == 4 && CDF == CDF_NORMCDF && P == PREC_FAST;
@@ -125,6 +125,8 @@ __global__ void __launch_bounds__(256, (kMinBlocks<T, CDF, P, U>))
           const float2 ps = make_float2(s[u][l], s[u][l + 1]), pk = make_float2(k[u][l], k[u][l + 1]),
                        pt = make_float2(t[u][l], t[u][l + 1]);
           if constexpr (kPackedFast<T, CDF, P>) x2::fast::blackscholes(ps, pk, pt, r, v, c, pc, pp);
+          else if constexpr (CDF == CDF_FASTNORMCDF)
+            x2::blackscholes_fastnormcdf<P == PREC_FUSED>(ps, pk, pt, r, v, c, pc, pp);
           else x2::blackscholes<P == PREC_FUSED>(ps, pk, pt, r, v, c, pc, pp);
           oc[l] = pc.x; oc[l + 1] = pc.y;
           op[l] = pp.x; op[l + 1] = pp.y;
@@ -151,6 +153,8 @@ __global__ void __launch_bounds__(256, (kMinBlocks<T, CDF, P, U>))
         float2 pc, pp;
         const float2 ps = make_float2(s[l], s[l + 1]), pk = make_float2(k[l], k[l + 1]), pt = make_float2(t[l], t[l + 1]);
         if constexpr (kPackedFast<T, CDF, P>) x2::fast::blackscholes(ps, pk, pt, r, v, c, pc, pp);
+        else if constexpr (CDF == CDF_FASTNORMCDF)
+          x2::blackscholes_fastnormcdf<P == PREC_FUSED>(ps, pk, pt, r, v, c, pc, pp);
         else x2::blackscholes<P == PREC_FUSED>(ps, pk, pt, r, v, c, pc, pp);
         oc[l] = pc.x; oc[l + 1] = pc.y;
         op[l] = pp.x; op[l + 1] = pp.y;

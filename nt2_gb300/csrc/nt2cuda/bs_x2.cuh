@@ -264,16 +264,23 @@ template <bool F> __device__ __forceinline__ void normcdf_pair(float2 a0, float2
 // (of d1 and d2) and e = K exp(-r T); bs_back the prices from erfc(|y1|),
 // erfc(|y2|).
 template <bool F>
-__device__ __forceinline__ void bs_front(float2 S, float2 K, float2 T, float r, float v, float c, float2& y1,
-                                         float2& y2, float2& e)
+__device__ __forceinline__ void bs_d(float2 S, float2 K, float2 T, float r, float v, float c, float2& d1, float2& d2,
+                                     float2& e)
 {
   const float2 da = make_float2(__fsqrt_rn(T.x), __fsqrt_rn(T.y));
   const float2 vda = mul_r(splat(v), da);
   const float2 q = make_float2(__fdiv_rn(S.x, K.x), __fdiv_rn(S.y, K.y));
   const float2 num = madd<F>(splat(c), T, log<F>(q));
-  const float2 d1 = make_float2(__fdiv_rn(num.x, vda.x), __fdiv_rn(num.y, vda.y));
-  const float2 d2 = sub(d1, vda);
+  d1 = make_float2(__fdiv_rn(num.x, vda.x), __fdiv_rn(num.y, vda.y));
+  d2 = sub(d1, vda);
   e = mul(K, exp<F>(mul_r(splat(-r), T)));
+}
+template <bool F>
+__device__ __forceinline__ void bs_front(float2 S, float2 K, float2 T, float r, float v, float c, float2& y1,
+                                         float2& y2, float2& e)
+{
+  float2 d1, d2;
+  bs_d<F>(S, K, T, r, v, c, d1, d2, e);
   y1 = normcdf_arg(d1);
   y2 = normcdf_arg(d2);
 }
@@ -367,6 +374,35 @@ __device__ __forceinline__ void blackscholes(float2 S, float2 K, float2 T, float
 }
 
 }  // namespace fast
+
+// NT2's fastnormcdf(a) and fastnormcdf(-a) (math::fastnormcdf_pair), two
+// lanes; the reciprocal is the IEEE division per lane.
+template <bool F> __device__ __forceinline__ void fastnormcdf_pair(float2 a0, float2& pos, float2& neg)
+{
+  constexpr uint32_t P[5] = {0x3faa466fu, 0xbfe91eeau, 0x3fe40778u, 0xbeb68f87u, 0x3ea385fau};
+  const float2 l = make_float2(fabsf(a0.x), fabsf(a0.y));
+  const float2 den = madd<F>(splat(0.2316419f), l, splat(1.0f));
+  const float2 k = make_float2(__fdiv_rn(1.0f, den.x), __fdiv_rn(1.0f, den.y));
+  const float2 ll = mul(l, l);
+  const float2 w = mul_r(horner<F>(k, P),
+                         mul(mul(k, splat(fbits(cf::invsqrt_2pi))), exp<F>(mul(make_float2(-ll.x, -ll.y), splat(0.5f)))));
+  const float2 om = sub(splat(1.0f), w);
+  pos = make_float2((a0.x > 0.0f) ? om.x : w.x, (a0.y > 0.0f) ? om.y : w.y);
+  neg = make_float2((-a0.x > 0.0f) ? om.x : w.x, (-a0.y > 0.0f) ? om.y : w.y);
+}
+
+// The statement with fastnormcdf (the demo form's cdf), two options.
+template <bool F>
+__device__ __forceinline__ void blackscholes_fastnormcdf(float2 S, float2 K, float2 T, float r, float v, float c,
+                                                         float2& call, float2& put)
+{
+  float2 d1, d2, e, n1, m1, n2, m2;
+  bs_d<F>(S, K, T, r, v, c, d1, d2, e);
+  fastnormcdf_pair<F>(d1, n1, m1);
+  fastnormcdf_pair<F>(d2, n2, m2);
+  call = nmsub<F>(e, n2, mul_r(S, n1));
+  put = nmsub<F>(S, m1, mul_r(e, m2));
+}
 
 }  // namespace x2
 }  // namespace nt2cuda

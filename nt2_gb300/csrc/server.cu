@@ -86,6 +86,8 @@ __device__ __forceinline__ void bs_tile(const req_desc& d, uint64_t base)
           const float2 ps = make_float2(s[l], s[l + 1]), pk = make_float2(k[l], k[l + 1]),
                        pt = make_float2(tt[l], tt[l + 1]);
           if constexpr (kPackedFast<float, CDF, P>) x2::fast::blackscholes(ps, pk, pt, d.r, d.sigma, c, pc, pp);
+          else if constexpr (CDF == CDF_FASTNORMCDF)
+            x2::blackscholes_fastnormcdf<P == PREC_FUSED>(ps, pk, pt, d.r, d.sigma, c, pc, pp);
           else x2::blackscholes<P == PREC_FUSED>(ps, pk, pt, d.r, d.sigma, c, pc, pp);
           oc[l] = pc.x; oc[l + 1] = pc.y;
           op[l] = pp.x; op[l + 1] = pp.y;

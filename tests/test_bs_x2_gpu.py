@@ -34,3 +34,15 @@ def test_two_lane_fast_functor_matches_one_lane_over_every_float(gpu, cuda_lib, 
     st = cuda_lib.nt2cuda_selftest_x2(which, C.byref(n), first, torch.cuda.current_stream().cuda_stream)
     assert st == 0
     assert n.value == 0, (name, n.value, [hex(first[i]) for i in range(min(8, n.value))])
+
+
+@pytest.mark.parametrize("fused", [False, True])
+def test_two_lane_fastnormcdf_is_bit_exact_over_every_float(gpu, cuda_lib, fused):
+    """The demo form's cdf (fastnormcdf, Abramowitz-Stegun 26.2.17) packed two lanes
+    per instruction gives the one-lane functor's bits, unfused and fused."""
+    n = C.c_ulonglong(99)
+    first = (C.c_uint32 * 8)()
+    st = cuda_lib.nt2cuda_selftest_x2(13 if fused else 12, C.byref(n), first,
+                                      torch.cuda.current_stream().cuda_stream)
+    assert st == 0
+    assert n.value == 0, (n.value, [hex(first[i]) for i in range(min(8, n.value))])
