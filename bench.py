@@ -862,6 +862,23 @@ def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: in
                     api.map_(op, x, out=y)
                 ms, _, _ = time_device(op_step, K(100), warmup, ws)
                 out.append(line(label, ms, 2 * n * xs[0].element_size(), n, "elements/s"))
+            # exp, log and the demo's cdf (fastnormcdf), NT2's arithmetic
+            for op, lo, hi in (("exp", -60.0, 60.0), ("log", 1e-3, 100.0), ("fastnormcdf", -6.0, 6.0)):
+                label = f"{op} {tname} 2^24 [{lo:g},{hi:g}]"
+                if part and part not in label:
+                    continue
+                zs = [torch.empty(n, dtype=dt, device="cuda") for _ in range(2)]
+                for k, t in enumerate(zs):
+                    api.fill_uniform(t, lo, hi, 61 + k)
+                it = [0]
+
+                def map_step(op=op, zs=zs):
+                    x = zs[it[0] & 1]
+                    it[0] += 1
+                    api.map_(op, x, out=y)
+                ms, _, _ = time_device(map_step, K(100), warmup, ws)
+                out.append(line(label, ms, 2 * n * xs[0].element_size(), n, "elements/s"))
+                del zs
             # z = pow(a0, a1) over NT2's cover range: a0 in [0, 100], a1 in [-10, 10];
             # 12 (float) or 24 (double) bytes per element
             label = f"pow {tname} 2^24 a0 in [0,100], a1 in [-10,10]"

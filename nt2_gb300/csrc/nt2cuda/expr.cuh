@@ -24,6 +24,7 @@
 #include <limits>
 #include <type_traits>
 #include "math.cuh"
+#include "bs_x2.cuh"
 #include "trig.cuh"
 #include "memory.cuh"
 
@@ -299,12 +300,42 @@ template <class T, int V> struct regs<scal<T>, V> {
   template <bool F> __device__ __forceinline__ T get(const scal<T>& s, int) const { return s.v; }
 };
 
+// FP32 exp, log and fastnormcdf nodes run two lanes per packed instruction
+// (nt2cuda/bs_x2.cuh, bit-identical to the one-lane functors over every
+// float): asked for an even lane, the node computes that lane and the next
+// one and hands the latter out when it is asked for (the kernels ask for
+// lanes 0..V-1 in order, as the trigonometric nodes below also rely on).
+template <class Tag> struct x2_unary { static constexpr bool value = false; };
+template <> struct x2_unary<tag::exp_> { static constexpr bool value = true; };
+template <> struct x2_unary<tag::log_> { static constexpr bool value = true; };
+template <> struct x2_unary<tag::fastnormcdf_> { static constexpr bool value = true; };
+template <class Tag, bool F> __device__ __forceinline__ float2 x2_apply(float2 a)
+{
+  if constexpr (std::is_same<Tag, tag::exp_>::value) return x2::exp<F>(a);
+  else if constexpr (std::is_same<Tag, tag::log_>::value) return x2::log<F>(a);
+  else {
+    float2 pos, neg;
+    x2::fastnormcdf_pair<F>(a, pos, neg);
+    return pos;
+  }
+}
+
 template <class Tag, class A, int V> struct regs<node<Tag, A>, V> {
+  static constexpr bool kPair = x2_unary<Tag>::value && V % 2 == 0 &&
+                                std::is_same<typename value_of<A>::type, float>::value;
   regs<A, V> ra;
+  mutable float pend;   // the odd lane of the last pair (kPair)
   template <bool S> __device__ __forceinline__ void load(const node<Tag, A>& n, size_t i) { ra.template load<S>(n.a, i); }
   template <bool S> __device__ __forceinline__ void load_one(const node<Tag, A>& n, size_t i, int l) { ra.template load_one<S>(n.a, i, l); }
   template <bool F> __device__ __forceinline__ auto get(const node<Tag, A>& n, int l) const {
-    return fn<Tag, F>::apply(ra.template get<F>(n.a, l));
+    if constexpr (kPair) {
+      if (l & 1) return pend;
+      const float2 r = x2_apply<Tag, F>(make_float2(ra.template get<F>(n.a, l), ra.template get<F>(n.a, l + 1)));
+      pend = r.y;
+      return r.x;
+    } else {
+      return fn<Tag, F>::apply(ra.template get<F>(n.a, l));
+    }
   }
 };
 
