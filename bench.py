@@ -862,8 +862,9 @@ def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: in
                     api.map_(op, x, out=y)
                 ms, _, _ = time_device(op_step, K(100), warmup, ws)
                 out.append(line(label, ms, 2 * n * xs[0].element_size(), n, "elements/s"))
-            # exp, log and the demo's cdf (fastnormcdf), NT2's arithmetic
-            for op, lo, hi in (("exp", -60.0, 60.0), ("log", 1e-3, 100.0), ("fastnormcdf", -6.0, 6.0)):
+            # exp, log, erfc and the two cdfs, NT2's arithmetic
+            for op, lo, hi in (("exp", -60.0, 60.0), ("log", 1e-3, 100.0), ("erfc", -6.0, 6.0), ("normcdf", -6.0, 6.0),
+                               ("fastnormcdf", -6.0, 6.0)):
                 label = f"{op} {tname} 2^24 [{lo:g},{hi:g}]"
                 if part and part not in label:
                     continue

@@ -300,7 +300,7 @@ template <class T, int V> struct regs<scal<T>, V> {
   template <bool F> __device__ __forceinline__ T get(const scal<T>& s, int) const { return s.v; }
 };
 
-// FP32 exp, log and fastnormcdf nodes run two lanes per packed instruction
+// FP32 exp, log, erfc, normcdf and fastnormcdf nodes run two lanes per packed instruction
 // (nt2cuda/bs_x2.cuh, bit-identical to the one-lane functors over every
 // float): asked for an even lane, the node computes that lane and the next
 // one and hands the latter out when it is asked for (the kernels ask for
@@ -309,12 +309,23 @@ template <class Tag> struct x2_unary { static constexpr bool value = false; };
 template <> struct x2_unary<tag::exp_> { static constexpr bool value = true; };
 template <> struct x2_unary<tag::log_> { static constexpr bool value = true; };
 template <> struct x2_unary<tag::fastnormcdf_> { static constexpr bool value = true; };
+template <> struct x2_unary<tag::erfc_> { static constexpr bool value = true; };
+template <> struct x2_unary<tag::normcdf_> { static constexpr bool value = true; };
 template <class Tag, bool F> __device__ __forceinline__ float2 x2_apply(float2 a)
 {
-  if constexpr (std::is_same<Tag, tag::exp_>::value) return x2::exp<F>(a);
-  else if constexpr (std::is_same<Tag, tag::log_>::value) return x2::log<F>(a);
-  else {
-    float2 pos, neg;
+  float2 pos, neg;
+  if constexpr (std::is_same<Tag, tag::exp_>::value) {
+    return x2::exp<F>(a);
+  } else if constexpr (std::is_same<Tag, tag::log_>::value) {
+    return x2::log<F>(a);
+  } else if constexpr (std::is_same<Tag, tag::erfc_>::value) {   // math::erfc
+    const float2 r1 = x2::erfc_abs<F>(make_float2(fabsf(a.x), fabsf(a.y)));
+    const float2 two_m = x2::sub(x2::splat(2.0f), r1);
+    return make_float2((a.x < 0.0f) ? two_m.x : r1.x, (a.y < 0.0f) ? two_m.y : r1.y);
+  } else if constexpr (std::is_same<Tag, tag::normcdf_>::value) {   // math::normcdf, as normcdf_pair's first
+    x2::normcdf_pair<F>(a, pos, neg);
+    return pos;
+  } else {
     x2::fastnormcdf_pair<F>(a, pos, neg);
     return pos;
   }
