@@ -467,6 +467,31 @@ def config_lines(ws: int, steps: int, warmup: int) -> dict:
                 "error": {"mismatches_vs_fp64_oracle": mism,
                           "note": "the FP64 oracle is NT2's double arithmetic restated; 0 = bit-exact"}}
 
+    def bs_demo():
+        # the demo's own statement (demo/blackscholes/nt2/blackandscholes_nt2.cpp:55-59): five input
+        # tables, one output, one fused transform; r ~ U[0.01, 0.05] and v ~ U[0.1, 0.5] per option
+        n = 1 << 24
+        tabs = [torch.empty(n, device="cuda") for _ in range(5)]
+        for t, (lo, hi), sd in zip(tabs, ((5.0, 30.0), (1.0, 100.0), (0.25, 10.0), (0.01, 0.05), (0.1, 0.5)),
+                                   (21, 22, 23, 24, 25)):
+            api.fill_uniform(t, lo, hi, sd)
+        res = torch.empty(n, device="cuda")
+        ms, _, _ = time_device(lambda: api.blackscholes_demo(*tabs, out=res), K(50), warmup, ws)
+        api.blackscholes_demo(*tabs, out=res)
+        hs = [t.cpu().numpy() for t in tabs]
+        ref = np.empty(n, np.float32)
+        L.nt2o_bs_demo_f(*hs, ref, n, 0)
+        got = res.cpu().numpy()
+        mism = int(np.count_nonzero(got.view(np.uint32) != ref.view(np.uint32)))
+        rate, reps = cpu_rate(lambda: L.nt2o_bs_demo_f(*hs, ref, n, 0), n)
+        th = nt2_threading(L, n, 4)
+        return {"ms": ms, "value": ws * n / (ms * 1e-3), "unit": "options/s",
+                "roofline": _roof(24 * n, ms, peak),
+                "inputs": "S ~ U[5,30], X ~ U[1,100], T ~ U[0.25,10], r ~ U[0.01,0.05], v ~ U[0.1,0.5] tables",
+                "cpu_baseline": _cpu(rate, "options/s", th["threads"],
+                                     "same 2^24 options; the demo statement, NT2 scalar+OpenMP restated", reps),
+                "error": {"mismatches_vs_oracle": mism, "note": "NT2's FP32 arithmetic restated; 0 = bit-exact"}}
+
     def sigmadelta():
         batch = video.make_batch(256, 8, seed=11)
         torch.cuda.synchronize()
@@ -506,6 +531,7 @@ def config_lines(ws: int, steps: int, warmup: int) -> dict:
     guarded("sdot_f32_2^26", sdot)
     guarded("folds_f32_8192x4096", folds)
     guarded("blackscholes_f64_2^24", bs_f64)
+    guarded("blackscholes_demo_f32_2^24", bs_demo)
     guarded("sigmadelta_u8_256x8", sigmadelta)
     return out
 
@@ -713,7 +739,7 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-CASES = ("bs_exact", "bs_fused", "bs_fast", "bs_fastnormcdf", "bs_f64", "saxpy", "sdot", "sdot_plain",
+CASES = ("bs_exact", "bs_fused", "bs_fast", "bs_fastnormcdf", "bs_demo", "bs_f64", "saxpy", "sdot", "sdot_plain",
          "rgb2grey_u8", "rgb2yuv", "mandelbrot", "trig", "reductions", "scans",
          "inner", "outer", "sigmadelta")
 
@@ -900,7 +926,7 @@ def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: in
                 del a1s
             del xs, y
     if not (want("inner") or want("outer") or want("reductions") or want("scans") or want("bs_f64") or want("bs_fused") or want("bs_fast")
-            or want("bs_exact") or want("bs_fastnormcdf") or want("sigmadelta")):
+            or want("bs_exact") or want("bs_fastnormcdf") or want("bs_demo") or want("sigmadelta")):
         return out
     rows, cols = 8192, 4096
     if want("scans"):
@@ -1004,6 +1030,16 @@ def suite(ws: int, only: str | None = None, steps: int | None = None, warmup: in
                                                             cdf=cdf), K(200), warmup, ws)
             out.append(line(f"Black-Scholes f32 2^24 {prec} {cdf}", ms, 20 * (1 << 24), 1 << 24, "options/s"))
         del S, Kt, T, c, p
+    if want("bs_demo"):
+        n = 1 << 24
+        tabs = [torch.empty(n, device="cuda") for _ in range(5)]
+        for t, (lo, hi), sd in zip(tabs, ((5.0, 30.0), (1.0, 100.0), (0.25, 10.0), (0.01, 0.05), (0.1, 0.5)),
+                                   (21, 22, 23, 24, 25)):
+            api.fill_uniform(t, lo, hi, sd)
+        res = torch.empty(n, device="cuda")
+        ms, _, _ = time_device(lambda: api.blackscholes_demo(*tabs, out=res), K(50), warmup, ws)
+        out.append(line("Black-Scholes demo statement f32 2^24 (5 tables in, 1 out)", ms, 24 * n, n, "options/s"))
+        del tabs, res
     if want("sigmadelta"):
         batch = video.make_batch(256, 8, seed=11)
         torch.cuda.synchronize()

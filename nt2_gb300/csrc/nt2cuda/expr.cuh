@@ -462,6 +462,26 @@ __device__ __forceinline__ void prefetch_terms(const node<Tag, A, B, C>& n, size
 { prefetch_terms(n.a, i); prefetch_terms(n.b, i); prefetch_terms(n.c, i); }
 
 // ------------------------------------------------------------- programs
+// Nodes that expand into long instruction sequences: every functor but the
+// elementwise arithmetic, comparisons and selections.  A statement with
+// several of them keeps too many temporaries live for two groups per thread
+// (the unrolled kernels are held to 64 or 80 registers and spill), so its
+// launches default to one group per thread per trip (`transform` below).
+template <class Tag> struct light_tag { static constexpr bool value = false; };
+#define NT2CUDA_LIGHT(TAG) template <> struct light_tag<tag::TAG> { static constexpr bool value = true; };
+NT2CUDA_LIGHT(plus_) NT2CUDA_LIGHT(minus_) NT2CUDA_LIGHT(multiplies_) NT2CUDA_LIGHT(unary_minus_)
+NT2CUDA_LIGHT(fma_) NT2CUDA_LIGHT(fnms_) NT2CUDA_LIGHT(sqr_) NT2CUDA_LIGHT(abs_) NT2CUDA_LIGHT(max_)
+NT2CUDA_LIGHT(min_) NT2CUDA_LIGHT(adds_) NT2CUDA_LIGHT(subs_) NT2CUDA_LIGHT(selinc_) NT2CUDA_LIGHT(seldec_)
+NT2CUDA_LIGHT(if_else_) NT2CUDA_LIGHT(if_zero_else_one_) NT2CUDA_LIGHT(is_less_) NT2CUDA_LIGHT(is_greater_)
+NT2CUDA_LIGHT(is_less_equal_) NT2CUDA_LIGHT(is_greater_equal_) NT2CUDA_LIGHT(is_equal_)
+NT2CUDA_LIGHT(is_not_equal_) NT2CUDA_LIGHT(oneminus_) NT2CUDA_LIGHT(minusone_) NT2CUDA_LIGHT(cast_)
+NT2CUDA_LIGHT(trunc_u8_)
+#undef NT2CUDA_LIGHT
+template <class E> struct heavy_nodes { static constexpr int value = 0; };
+template <class Tag, class... C> struct heavy_nodes<node<Tag, C...>> {
+  static constexpr int value = (light_tag<Tag>::value ? 0 : 1) + (0 + ... + heavy_nodes<C>::value);
+};
+
 // prog<A0, A...>: the assigns of one statement, evaluated per index in order.
 template <class... As> struct prog;
 template <> struct prog<> {};
@@ -481,6 +501,11 @@ template <class T, class E, class... As> struct prog_min_elem<prog<assign<T, E>,
   static constexpr int a = min_elem<E>::value < (int)sizeof(T) ? min_elem<E>::value : (int)sizeof(T);
   static constexpr int b = prog_min_elem<prog<As...>>::value;
   static constexpr int value = a < b ? a : b;
+};
+template <class P> struct prog_heavy;
+template <> struct prog_heavy<prog<>> { static constexpr int value = 0; };
+template <class T, class E, class... As> struct prog_heavy<prog<assign<T, E>, As...>> {
+  static constexpr int value = heavy_nodes<E>::value + prog_heavy<prog<As...>>::value;
 };
 template <class P> struct base_lanes {
   static constexpr int m = prog_min_elem<P>::value;

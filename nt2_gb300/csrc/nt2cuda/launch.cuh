@@ -148,6 +148,8 @@ inline cudaError_t transform(const P& p, size_t n, cudaStream_t s, const char* t
   alias_kind ak = classify_alias(p, n);
   if (ak == alias_kind::bad) return cudaErrorInvalidValue;
   constexpr int V = base_lanes<P>::value;
+  // statements with three or more long functors: one group per thread per trip
+  if (prog_heavy<P>::value >= 3 && def.unroll == tuning::params{}.unroll) def.unroll = 1;
   const tuning::params tp = tuning::lookup(tune_key, n, def);
   const int U = tp.unroll, W = tp.waves;
   P pc = p;
