@@ -52,7 +52,7 @@ struct scratch_slot {
 };
 scratch_slot g_scratch[kMaxDevices];
 
-// The driver's identifier of the current context: unique over the process,
+// The CUDA driver API's identifier of the current context: unique over the process,
 // so a context torn down (cudaDeviceReset) and created again gets a new one.
 using ctx_get_current_fn = int (*)(void**);
 using ctx_get_id_fn = int (*)(void*, unsigned long long*);

@@ -117,8 +117,8 @@ template <int N> __device__ __forceinline__ void bulk_wait()
   asm volatile("cp.async.bulk.wait_group %0;" ::"n"(N) : "memory");
 }
 
-// The driver's cuTensorMapEncodeTiled, looked up once (null when the driver
-// does not provide it).
+// The CUDA driver API's cuTensorMapEncodeTiled, looked up once (null when
+// the installed CUDA driver does not provide it).
 inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
