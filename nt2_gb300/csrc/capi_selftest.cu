@@ -12,6 +12,7 @@
 #include "nt2cuda/bs_x2.cuh"
 #include "nt2cuda/launch.cuh"
 #include "nt2cuda/math.cuh"
+#include "nt2cuda/trig.cuh"
 
 using namespace nt2cuda;
 using namespace nt2cuda::detail_capi;
@@ -107,6 +108,21 @@ template <bool F> __device__ __forceinline__ void x2_check_fnc(uint32_t u0, x2_r
   if (!same(pos.y, p1) || !same(neg.y, n1)) record(rep, u1);
 }
 
+// 14..17: the packed sine/cosine finish (trig::finish2) against finish, the
+// bit pattern as the reduced argument, its low bits as the quadrant and bit 2
+// as the argument's sign: 14 sin, 15 cos, 16 and 17 the same fused
+template <int K, bool F> __device__ __forceinline__ void x2_check_trig(uint32_t u0, x2_report* rep)
+{
+  const uint32_t u1 = u0 + 1;
+  const float xr0 = __uint_as_float(u0), xr1 = __uint_as_float(u1);
+  const int n0 = (int)(u0 & 3u), n1 = (int)(u1 & 3u);
+  const float a0 = (u0 & 4u) ? -1.0f : 1.0f, a1 = (u1 & 4u) ? -1.0f : 1.0f;
+  float y0, y1;
+  trig::finish2<K, F>(a0, a1, xr0, xr1, n0, n1, y0, y1);
+  if (!same(y0, trig::finish<K, F>(a0, xr0, n0))) record(rep, u0);
+  if (!same(y1, trig::finish<K, F>(a1, xr1, n1))) record(rep, u1);
+}
+
 __global__ void __launch_bounds__(256) k_x2_check(int which, uint64_t pairs, x2_report* rep)
 {
   for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < pairs; p += (uint64_t)gridDim.x * blockDim.x) {
@@ -114,7 +130,11 @@ __global__ void __launch_bounds__(256) k_x2_check(int which, uint64_t pairs, x2_
     else if (which < 8) x2_check_pair<true>(which - 4, (uint32_t)(2 * p), rep);
     else if (which < 12) x2_check_fast(which - 8, (uint32_t)(2 * p), rep);
     else if (which == 12) x2_check_fnc<false>((uint32_t)(2 * p), rep);
-    else x2_check_fnc<true>((uint32_t)(2 * p), rep);
+    else if (which == 13) x2_check_fnc<true>((uint32_t)(2 * p), rep);
+    else if (which == 14) x2_check_trig<trig::SIN, false>((uint32_t)(2 * p), rep);
+    else if (which == 15) x2_check_trig<trig::COS, false>((uint32_t)(2 * p), rep);
+    else if (which == 16) x2_check_trig<trig::SIN, true>((uint32_t)(2 * p), rep);
+    else x2_check_trig<trig::COS, true>((uint32_t)(2 * p), rep);
   }
 }
 
@@ -124,7 +144,7 @@ extern "C" nt2cuda_status nt2cuda_selftest_x2(int which, unsigned long long* mis
                                               nt2cuda_stream stream)
 {
   NT2CUDA_NVTX_RANGE;
-  if (which < 0 || which > 13 || !mismatches) return NT2CUDA_ERR_ARG;
+  if (which < 0 || which > 17 || !mismatches) return NT2CUDA_ERR_ARG;
   cudaStream_t s = as_stream(stream);
   x2_report* rep = nullptr;
   cudaError_t e = cudaMalloc(&rep, sizeof(x2_report));

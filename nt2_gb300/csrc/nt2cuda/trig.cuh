@@ -24,6 +24,8 @@
 // with NT2's unfused fma; F (fused) contracts them.
 #pragma once
 #include <stdint.h>
+#include <type_traits>
+#include "bs_x2.cuh"
 #include "math.cuh"
 
 namespace nt2cuda {
@@ -610,6 +612,55 @@ template <int K, bool F, class T> __device__ __forceinline__ T finish(T a0, T xr
   }
 }
 
+// finish for two float lanes of the sine and cosine kinds: both polynomials
+// (cos_eval, sin_eval) on packed FP32 instructions (nt2cuda/bs_x2.cuh), then
+// each lane's pick and sign as finish does; bit-identical to two finish calls
+// (checked over every float by nt2cuda_selftest_x2).
+template <int K> struct sincos_kind {
+  static constexpr bool value = K == SIN || K == COS || K == SINPI || K == COSPI || K == SIND || K == COSD;
+};
+template <int K, bool F>
+__device__ __forceinline__ void finish2(float a0, float a1, float xr0, float xr1, int n0, int n1, float& y0, float& y1)
+{
+  constexpr uint32_t CC[3] = {0x37ccf5ceu, 0xbab60619u, 0x3d2aaaa5u};
+  constexpr uint32_t SC[3] = {0xb94ca1f9u, 0x3c08839du, 0xbe2aaaa2u};
+  const float2 x = make_float2(xr0, xr1);
+  const float2 z = x2::mul(x, x);
+  // cos_eval: 1 + madd(z, -0.5, horner(z)*(z*z)); sin_eval: madd(horner(z)*z, x, x)
+  const float2 cv = x2::add(x2::splat(1.0f),
+                            x2::madd<F>(z, x2::splat(-0.5f), x2::mul_r(x2::horner<F>(z, CC), x2::mul(z, z))));
+  const float2 sv = x2::madd<F>(x2::mul(x2::horner<F>(z, SC), z), x, x);
+  const float a[2] = {a0, a1};
+  const int n[2] = {n0, n1};
+  const float c[2] = {cv.x, cv.y}, s[2] = {sv.x, sv.y};
+  float y[2];
+#pragma unroll
+  for (int l = 0; l < 2; ++l) {
+    if constexpr (K == SIN || K == SINPI || K == SIND) {
+      const float v = (n[l] & 1) ? c[l] : s[l];
+      y[l] = flip(v, sign_of(a[l]) ^ ((uint32_t)(n[l] & 2) << 30));
+    } else {
+      const float v = (n[l] & 1) ? s[l] : c[l];
+      y[l] = flip(v, (uint32_t)((n[l] ^ (n[l] >> 1)) & 1) << 31);
+    }
+  }
+  y0 = y[0];
+  y1 = y[1];
+}
+
+// finish over a group of P lanes, two at a time where finish2 applies
+template <int K, bool F, int P, class T>
+__device__ __forceinline__ void finish_group(const T (&a)[P], const T (&xr)[P], const int (&n)[P], T (&y)[P])
+{
+  if constexpr (sincos_kind<K>::value && std::is_same<T, float>::value && P % 2 == 0) {
+#pragma unroll
+    for (int l = 0; l < P; l += 2) finish2<K, F>(a[l], a[l + 1], xr[l], xr[l + 1], n[l], n[l + 1], y[l], y[l + 1]);
+  } else {
+#pragma unroll
+    for (int l = 0; l < P; ++l) y[l] = finish<K, F>(a[l], xr[l], n[l]);
+  }
+}
+
 // NT2's SIMD code over one pack of P lanes: y[l] = f(a[l]), one reduction
 // method for the pack.  SIMD selects the packed-double conversion of the pi
 // reduction (P > 1).
@@ -626,8 +677,7 @@ __device__ __forceinline__ void pack_impl(const T (&a)[P], T (&y)[P])
   } else {
     reduce_pack<P>(x, xr, n);
   }
-#pragma unroll
-  for (int l = 0; l < P; ++l) y[l] = finish<K, F>(a[l], xr[l], n[l]);
+  finish_group<K, F, P>(a, xr, n, y);
 }
 template <int K, bool F, int P, class T> __device__ __forceinline__ void pack(const T (&a)[P], T (&y)[P])
 {
@@ -811,8 +861,7 @@ template <int K, bool F, int P, class T> __device__ __forceinline__ void scalar_
       xr[l] = r1[0];
       n[l] = n1[0];
     }
-#pragma unroll
-    for (int l = 0; l < P; ++l) y[l] = finish<K, F>(a[l], xr[l], n[l]);
+    finish_group<K, F, P>(a, xr, n, y);
   }
 }
 

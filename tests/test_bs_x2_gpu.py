@@ -46,3 +46,15 @@ def test_two_lane_fastnormcdf_is_bit_exact_over_every_float(gpu, cuda_lib, fused
                                       torch.cuda.current_stream().cuda_stream)
     assert st == 0
     assert n.value == 0, (n.value, [hex(first[i]) for i in range(min(8, n.value))])
+
+
+@pytest.mark.parametrize("which,name", [(14, "sin"), (15, "cos"), (16, "sin, fused"), (17, "cos, fused")])
+def test_two_lane_sine_cosine_evaluation_over_every_float(gpu, cuda_lib, which, name):
+    """The float trigonometric functors evaluate the sine and cosine polynomials of
+    two lanes per packed instruction; over every reduced argument (and each
+    quadrant and sign) the result is the one-lane evaluation's."""
+    n = C.c_ulonglong(99)
+    first = (C.c_uint32 * 8)()
+    st = cuda_lib.nt2cuda_selftest_x2(which, C.byref(n), first, torch.cuda.current_stream().cuda_stream)
+    assert st == 0
+    assert n.value == 0, (name, n.value, [hex(first[i]) for i in range(min(8, n.value))])
