@@ -457,9 +457,9 @@ nt2cuda_status nt2cuda_selftest_fold_timeout(const float* A, size_t rows, size_t
  * |a|, 3 normcdf(a) with normcdf(-a); 4..7 the same functors with each NT2
  * fma/fnms one hardware FMA (the fused precision mode); 8..11 the fast mode's
  * exp of a moderate argument, log, erfc of |a| and normcdf pair; 12, 13
- * fastnormcdf(a) with fastnormcdf(-a), unfused and fused; 14..17 the packed
- * sine and cosine evaluation of the float trigonometric functors (sin, cos,
- * unfused; sin, cos, fused) over every reduced argument.
+ * fastnormcdf(a) with fastnormcdf(-a), unfused and fused; 14..21 the packed
+ * evaluation of the float trigonometric functors (sin, cos, then the same
+ * fused; tan, cot, then the same fused) over every reduced argument.
  * *mismatches = arguments whose results differ in any bit (two NaNs are
  * equal); first_bad (8 entries, may be NULL) gets the first ones' bit
  * patterns.  Synchronous. */

@@ -108,9 +108,10 @@ template <bool F> __device__ __forceinline__ void x2_check_fnc(uint32_t u0, x2_r
   if (!same(pos.y, p1) || !same(neg.y, n1)) record(rep, u1);
 }
 
-// 14..17: the packed sine/cosine finish (trig::finish2) against finish, the
-// bit pattern as the reduced argument, its low bits as the quadrant and bit 2
-// as the argument's sign: 14 sin, 15 cos, 16 and 17 the same fused
+// 14..21: the packed finish (trig::finish2) against finish, the bit pattern
+// as the reduced argument, its low bits as the quadrant and bit 2 as the
+// argument's sign: 14 sin, 15 cos, 16 and 17 the same fused; 18 tan, 19 cot,
+// 20 and 21 the same fused
 template <int K, bool F> __device__ __forceinline__ void x2_check_trig(uint32_t u0, x2_report* rep)
 {
   const uint32_t u1 = u0 + 1;
@@ -134,7 +135,11 @@ __global__ void __launch_bounds__(256) k_x2_check(int which, uint64_t pairs, x2_
     else if (which == 14) x2_check_trig<trig::SIN, false>((uint32_t)(2 * p), rep);
     else if (which == 15) x2_check_trig<trig::COS, false>((uint32_t)(2 * p), rep);
     else if (which == 16) x2_check_trig<trig::SIN, true>((uint32_t)(2 * p), rep);
-    else x2_check_trig<trig::COS, true>((uint32_t)(2 * p), rep);
+    else if (which == 17) x2_check_trig<trig::COS, true>((uint32_t)(2 * p), rep);
+    else if (which == 18) x2_check_trig<trig::TAN, false>((uint32_t)(2 * p), rep);
+    else if (which == 19) x2_check_trig<trig::COT, false>((uint32_t)(2 * p), rep);
+    else if (which == 20) x2_check_trig<trig::TAN, true>((uint32_t)(2 * p), rep);
+    else x2_check_trig<trig::COT, true>((uint32_t)(2 * p), rep);
   }
 }
 
@@ -144,7 +149,7 @@ extern "C" nt2cuda_status nt2cuda_selftest_x2(int which, unsigned long long* mis
                                               nt2cuda_stream stream)
 {
   NT2CUDA_NVTX_RANGE;
-  if (which < 0 || which > 17 || !mismatches) return NT2CUDA_ERR_ARG;
+  if (which < 0 || which > 21 || !mismatches) return NT2CUDA_ERR_ARG;
   cudaStream_t s = as_stream(stream);
   x2_report* rep = nullptr;
   cudaError_t e = cudaMalloc(&rep, sizeof(x2_report));

@@ -612,16 +612,47 @@ template <int K, bool F, class T> __device__ __forceinline__ T finish(T a0, T xr
   }
 }
 
-// finish for two float lanes of the sine and cosine kinds: both polynomials
-// (cos_eval, sin_eval) on packed FP32 instructions (nt2cuda/bs_x2.cuh), then
-// each lane's pick and sign as finish does; bit-identical to two finish calls
-// (checked over every float by nt2cuda_selftest_x2).
+// finish for two float lanes: for the sine and cosine kinds both polynomials
+// (cos_eval, sin_eval), for the tangent and cotangent kinds tan_eval, on
+// packed FP32 instructions (nt2cuda/bs_x2.cuh), then each lane's pick, sign
+// and reciprocal as finish does; bit-identical to two finish calls (checked
+// over every float by nt2cuda_selftest_x2).
 template <int K> struct sincos_kind {
   static constexpr bool value = K == SIN || K == COS || K == SINPI || K == COSPI || K == SIND || K == COSD;
+};
+template <int K> struct tancot_kind {
+  static constexpr bool value = K == TAN || K == TANPI || K == TAND || K == COT || K == COTPI || K == COTD;
 };
 template <int K, bool F>
 __device__ __forceinline__ void finish2(float a0, float a1, float xr0, float xr1, int n0, int n1, float& y0, float& y1)
 {
+  if constexpr (tancot_kind<K>::value) {
+    // tan_eval of both lanes packed, the rest of finish per lane
+    constexpr uint32_t TC[6] = {0x3c19c53bu, 0x3b4c779cu, 0x3cc821b5u, 0x3d5ac5c9u, 0x3e0896ddu, 0x3eaaaa6fu};
+    const float2 x = make_float2(xr0, xr1);
+    const float2 zz = x2::mul(x, x);
+    const float2 tv = x2::madd<F>(x2::mul(x2::horner<F>(zz, TC), zz), x, x);
+    const float a[2] = {a0, a1}, t[2] = {tv.x, tv.y};
+    const int n[2] = {n0, n1};
+    float y[2];
+#pragma unroll
+    for (int l = 0; l < 2; ++l) {
+      float v = t[l];
+      if constexpr (K == TAN || K == TANPI || K == TAND) {
+        if (n[l] & 1) v = -math::div(1.0f, v);
+        v = flip(v, sign_of(a[l]));
+        y[l] = tan_invalid<K>(a[l]) ? float(NAN) : v;
+      } else {
+        v = (n[l] & 1) ? -v : math::div(1.0f, v);
+        v = flip(v, sign_of(a[l]));
+        v = cot_invalid<K>(a[l]) ? float(NAN) : v;
+        y[l] = a[l] != 0.0f ? v : math::div(1.0f, a[l]);
+      }
+    }
+    y0 = y[0];
+    y1 = y[1];
+    return;
+  }
   constexpr uint32_t CC[3] = {0x37ccf5ceu, 0xbab60619u, 0x3d2aaaa5u};
   constexpr uint32_t SC[3] = {0xb94ca1f9u, 0x3c08839du, 0xbe2aaaa2u};
   const float2 x = make_float2(xr0, xr1);
@@ -652,7 +683,7 @@ __device__ __forceinline__ void finish2(float a0, float a1, float xr0, float xr1
 template <int K, bool F, int P, class T>
 __device__ __forceinline__ void finish_group(const T (&a)[P], const T (&xr)[P], const int (&n)[P], T (&y)[P])
 {
-  if constexpr (sincos_kind<K>::value && std::is_same<T, float>::value && P % 2 == 0) {
+  if constexpr ((sincos_kind<K>::value || tancot_kind<K>::value) && std::is_same<T, float>::value && P % 2 == 0) {
 #pragma unroll
     for (int l = 0; l < P; l += 2) finish2<K, F>(a[l], a[l + 1], xr[l], xr[l + 1], n[l], n[l + 1], y[l], y[l + 1]);
   } else {

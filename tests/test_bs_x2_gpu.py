@@ -48,10 +48,11 @@ def test_two_lane_fastnormcdf_is_bit_exact_over_every_float(gpu, cuda_lib, fused
     assert n.value == 0, (n.value, [hex(first[i]) for i in range(min(8, n.value))])
 
 
-@pytest.mark.parametrize("which,name", [(14, "sin"), (15, "cos"), (16, "sin, fused"), (17, "cos, fused")])
+@pytest.mark.parametrize("which,name", [(14, "sin"), (15, "cos"), (16, "sin, fused"), (17, "cos, fused"),
+                                        (18, "tan"), (19, "cot"), (20, "tan, fused"), (21, "cot, fused")])
 def test_two_lane_sine_cosine_evaluation_over_every_float(gpu, cuda_lib, which, name):
-    """The float trigonometric functors evaluate the sine and cosine polynomials of
-    two lanes per packed instruction; over every reduced argument (and each
+    """The float trigonometric functors evaluate their polynomials (sine and cosine,
+    or tangent) two lanes per packed instruction; over every reduced argument (and each
     quadrant and sign) the result is the one-lane evaluation's."""
     n = C.c_ulonglong(99)
     first = (C.c_uint32 * 8)()
