@@ -152,19 +152,30 @@ template <bool F> nt2cuda_status rgb2yuv_impl(const float* r, const float* g, co
 }
 
 // The demo statement, lowered through the generic expression engine.
+// d1 appears twice in R's tree (in d2 and in fastnormcdf(d1)), and a tree
+// evaluates each occurrence; so d1 is its own statement into stream scratch,
+// as the demo itself materialises it, and R's statement reads it.
 template <bool F> nt2cuda_status bs_demo_impl(const float* S, const float* X, const float* T, const float* r,
                                               const float* v, float* R, size_t n, nt2cuda_stream s)
 {
+  if (n == 0) return NT2CUDA_OK;
   auto Sa = tm(S); auto Xa = tm(X); auto Ta = tm(T); auto ra = tm(r); auto va = tm(v);
   auto da = nd<tag::sqrt_>(Ta);
   // log(Sa/Xa) + (fma(sqr(va),0.5,ra)*Ta)/(va*da)
   auto d1 = nd<tag::plus_>(nd<tag::log_>(nd<tag::divides_>(Sa, Xa)),
                            nd<tag::divides_>(nd<tag::multiplies_>(nd<tag::fma_>(nd<tag::sqr_>(va), sc(0.5f), ra), Ta),
                                              nd<tag::multiplies_>(va, da)));
-  auto d2 = nd<tag::fnms_>(va, da, d1);
+  void* scratch = nullptr;
+  const cudaError_t e = nt2cuda::stream_scratch(as_stream(s), n * sizeof(float), &scratch, 1);
+  if (e != cudaSuccess) return from_cuda(e);
+  float* D1 = static_cast<float*>(scratch);
+  const nt2cuda_status st = run<F>(make_prog(asg(D1, d1)), n, s, "bs_demo_d1_f32");
+  if (st != NT2CUDA_OK) return st;
+  auto d1t = tm(static_cast<const float*>(D1));
+  auto d2 = nd<tag::fnms_>(va, da, d1t);
   auto R0 = nd<tag::fnms_>(nd<tag::multiplies_>(Xa, nd<tag::exp_>(nd<tag::multiplies_>(nd<tag::unary_minus_>(ra), Ta))),
                            nd<tag::fastnormcdf_>(d2),
-                           nd<tag::multiplies_>(Sa, nd<tag::fastnormcdf_>(d1)));
+                           nd<tag::multiplies_>(Sa, nd<tag::fastnormcdf_>(d1t)));
   return run<F>(make_prog(asg(R, R0)), n, s, "bs_demo_f32");
 }
 
