@@ -54,7 +54,7 @@ using math::cf;
 // the code generator cannot merge with the add, since it does not know z.
 // Plain mul is kept for products that feed only multiplies, divisions,
 // comparisons and selections.
-static __constant__ float c_x2_negzero = -0.0f;
+__constant__ float c_x2_negzero = -0.0f;
 
 __device__ __forceinline__ float2 splat(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 add(float2 a, float2 b)
