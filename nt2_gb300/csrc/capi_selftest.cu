@@ -1,6 +1,7 @@
 // capi_selftest.cu -- exhaustive checks that the two-lane forms of NT2's
 // float functors (nt2cuda/bs_x2.cuh) give the one-lane forms' bits
-// (nt2cuda/math.cuh) for every float argument.
+// (nt2cuda/math.cuh) for every float argument (for pow: every float as
+// either argument, with drawn partners).
 //
 // Each check runs one kernel over all 2^32 float bit patterns (2^31 pairs),
 // compares the packed result of both lanes with the scalar functor bit for
@@ -124,6 +125,51 @@ template <int K, bool F> __device__ __forceinline__ void x2_check_trig(uint32_t 
   if (!same(y1, trig::finish<K, F>(a1, xr1, n1))) record(rep, u1);
 }
 
+// 22..25: pow and pow_abs (22 pow, 23 pow fused, 24 pow_abs, 25 pow_abs
+// fused) in two sweeps: the pair's bit patterns as a0 with an exponent drawn
+// from a hash of them, then as a1 with a drawn base.  The draws mix random
+// bit patterns, integers (odd and even), uniform values of both signs and
+// special values, so that over the sweeps every float meets each kind of
+// partner.
+__device__ __forceinline__ uint32_t mix32(uint32_t h)
+{
+  h ^= h >> 16; h *= 0x7feb352du; h ^= h >> 15; h *= 0x846ca68bu; h ^= h >> 16;
+  return h;
+}
+__device__ __forceinline__ float draw(uint32_t u, bool base)
+{
+  const uint32_t h = mix32(u * 2u + (base ? 1u : 0u)), g = mix32(h);
+  const float unit = (float)(g >> 8) * (1.0f / 16777216.0f);   // [0, 1)
+  switch (h & 7u) {
+    case 0: case 1: return __uint_as_float(g);                                 // any pattern
+    case 2: return (float)((int)(g & 255u) - 128);                             // integer
+    case 3: return base ? unit * 100.0f : (unit - 0.5f) * 20.0f;               // the bench's ranges
+    case 4: return (unit - 0.5f) * 512.0f;                                     // wide
+    case 5: return base ? 1.0f + (unit - 0.5f) * 1e-3f : (unit - 0.5f) * 1e-3f;   // near 1 / near 0
+    case 6: {
+      const float sp[8] = {0.0f, -0.0f, 1.0f, -1.0f, 0.5f, __int_as_float(0x7f800000),
+                           __int_as_float(0xff800000), __int_as_float(0x7fc00000)};
+      return sp[g & 7u];
+    }
+    default: return ldexpf(1.0f + unit, (int)(g & 63u) - 32) * ((g & 64u) ? -1.0f : 1.0f);
+  }
+}
+template <bool ABS, bool F> __device__ __forceinline__ void x2_check_pow(uint32_t u0, x2_report* rep)
+{
+  const uint32_t u1 = u0 + 1;
+  const float p0 = __uint_as_float(u0), p1 = __uint_as_float(u1);
+#pragma unroll
+  for (int sweep = 0; sweep < 2; ++sweep) {
+    const float2 a = sweep ? make_float2(draw(u0, true), draw(u1, true)) : make_float2(p0, p1);
+    const float2 b = sweep ? make_float2(p0, p1) : make_float2(draw(u0, false), draw(u1, false));
+    const float2 r = ABS ? x2::pow_abs<F>(a, b) : x2::pow<F>(a, b);
+    const float s0 = ABS ? math::pow_abs<F>(a.x, b.x) : math::pow<F>(a.x, b.x);
+    const float s1 = ABS ? math::pow_abs<F>(a.y, b.y) : math::pow<F>(a.y, b.y);
+    if (!same(r.x, s0)) record(rep, u0);
+    if (!same(r.y, s1)) record(rep, u1);
+  }
+}
+
 __global__ void __launch_bounds__(256) k_x2_check(int which, uint64_t pairs, x2_report* rep)
 {
   for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < pairs; p += (uint64_t)gridDim.x * blockDim.x) {
@@ -139,7 +185,11 @@ __global__ void __launch_bounds__(256) k_x2_check(int which, uint64_t pairs, x2_
     else if (which == 18) x2_check_trig<trig::TAN, false>((uint32_t)(2 * p), rep);
     else if (which == 19) x2_check_trig<trig::COT, false>((uint32_t)(2 * p), rep);
     else if (which == 20) x2_check_trig<trig::TAN, true>((uint32_t)(2 * p), rep);
-    else x2_check_trig<trig::COT, true>((uint32_t)(2 * p), rep);
+    else if (which == 21) x2_check_trig<trig::COT, true>((uint32_t)(2 * p), rep);
+    else if (which == 22) x2_check_pow<false, false>((uint32_t)(2 * p), rep);
+    else if (which == 23) x2_check_pow<false, true>((uint32_t)(2 * p), rep);
+    else if (which == 24) x2_check_pow<true, false>((uint32_t)(2 * p), rep);
+    else x2_check_pow<true, true>((uint32_t)(2 * p), rep);
   }
 }
 
@@ -149,7 +199,7 @@ extern "C" nt2cuda_status nt2cuda_selftest_x2(int which, unsigned long long* mis
                                               nt2cuda_stream stream)
 {
   NT2CUDA_NVTX_RANGE;
-  if (which < 0 || which > 21 || !mismatches) return NT2CUDA_ERR_ARG;
+  if (which < 0 || which > 25 || !mismatches) return NT2CUDA_ERR_ARG;
   cudaStream_t s = as_stream(stream);
   x2_report* rep = nullptr;
   cudaError_t e = cudaMalloc(&rep, sizeof(x2_report));

@@ -1,6 +1,6 @@
-// nt2cuda/bs_x2.cuh -- NT2's float exp, log, erfc and normcdf, two lanes at
-// a time on Blackwell's packed FP32 instructions, bit-identical to the
-// one-lane forms of math.cuh.
+// nt2cuda/bs_x2.cuh -- NT2's float exp, log, erfc, normcdf and pow, two
+// lanes at a time on Blackwell's packed FP32 instructions, bit-identical to
+// the one-lane forms of math.cuh.
 //
 // sm_100-family SMs execute add.rn.f32x2 / mul.rn.f32x2 on a 64-bit
 // register pair at the issue cost of one scalar FP32 instruction, each half
@@ -178,10 +178,12 @@ template <bool F> __device__ __forceinline__ float2 log(float2 a0)
 
 // x/(1+x) for x >= 0 (and NaN), as __fdiv_rn(x, 1+x) with x clamped to 2^64
 // (see the header comment); the reciprocals are per lane.
-__device__ __forceinline__ float2 x_over_1px(float2 x)
+// a/b for normal b and a quotient that stays normal (or is zero): one
+// reciprocal approximation per lane, a Newton step for 1/b, then Markstein's
+// correction of q = a*(1/b) (see the header comment).  Where it is used, its
+// agreement with the IEEE division is checked over every input it can get.
+__device__ __forceinline__ float2 markstein_quot(float2 a, float2 b)
 {
-  const float2 a = make_float2(fminf(x.x, 18446744073709551616.0f), fminf(x.y, 18446744073709551616.0f));
-  const float2 b = add(splat(1.0f), a);
   float2 y;
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y.x) : "f"(b.x));
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y.y) : "f"(b.y));
@@ -191,6 +193,12 @@ __device__ __forceinline__ float2 x_over_1px(float2 x)
   const float2 q = mul(a, y);
   const float2 r = fma(nb, q, a);
   return fma(r, y, q);
+}
+
+__device__ __forceinline__ float2 x_over_1px(float2 x)
+{
+  const float2 a = make_float2(fminf(x.x, 18446744073709551616.0f), fminf(x.y, 18446744073709551616.0f));
+  return markstein_quot(a, add(splat(1.0f), a));
 }
 
 // The two regions of NT2's float erfc (math::erfc_small / erfc_large) on
@@ -402,6 +410,172 @@ __device__ __forceinline__ void blackscholes_fastnormcdf(float2 S, float2 K, flo
   fastnormcdf_pair<F>(d2, n2, m2);
   call = nmsub<F>(e, n2, mul_r(S, n1));
   put = nmsub<F>(S, m1, mul_r(e, m2));
+}
+
+// ------------------------------------------------------------------- pow
+// NT2's float pow and pow_abs (math::pow, math::pow_abs), two lanes.  Per
+// lane: frexp, the table index and the table reads, the integer-to-float
+// conversions, the floors, the float-to-integer step, the exponent bits of
+// ldexp and the special cases.  Packed: every add, subtract, multiply and
+// NT2 fma.  The one division, of the reduced mantissa by its table value
+// A[i] in [1/2, 1], is markstein_quot; its operands depend on the mantissa
+// of a0 alone, so a check over every float a0 covers every quotient that
+// pow forms.  A warp whose lanes all have ordinary arguments (a0 positive,
+// or any sign for pow_abs, normal and finite; a1 finite) skips the zero,
+// infinity and sign selections, which cannot apply to them.
+__device__ __forceinline__ float2 pow_reduc(float2 x)
+{
+  // 1/16 * floor(16 x): both products are exact (powers of two, no overflow
+  // where the result is kept), so how they are scheduled cannot change them
+  const float2 t = mul(splat(16.0f), x);
+  return mul(splat(0.0625f), make_float2(floorf(t.x), floorf(t.y)));
+}
+
+// Boost.SIMD ldexp as math::pow_ldexp, the two multiplies packed
+__device__ __forceinline__ float2 pow_ldexp(float2 a, int e0, int e1)
+{
+  using C = math::powc<float>;
+  float s[2], f[2];
+  const int ein[2] = {e0, e1};
+#pragma unroll
+  for (int l = 0; l < 2; ++l) {
+    int e = ein[l];
+    const bool den = e < C::mine;
+    e = den ? e - C::mine : e;
+    float fl = den ? C::bits(C::smallest) : 1.0f;
+    const bool test = e == C::lime;
+    fl = test ? math::add(fl, 1.0f) : fl;
+    e = test ? e - 1 : e;
+    s[l] = C::bits((C::U)(unsigned)(e + C::maxe) << C::nbm);
+    f[l] = fl;
+  }
+  return mul(mul(a, make_float2(s[0], s[1])), make_float2(f[0], f[1]));
+}
+
+// math::pow_abs's selections after the arithmetic, one lane
+__device__ __forceinline__ float pow_special(float a0, float a1, float z, bool zer_ret, bool inf_ret)
+{
+  const float ax = fabsf(a0);
+  const bool gtax1 = ax > 1.0f;
+  const float inf = __int_as_float(0x7f800000);
+  if (a1 == inf) z = gtax1 ? inf : 0.0f;
+  if (a1 == -inf) z = gtax1 ? 0.0f : inf;
+  if (ax == inf) z = a1 > 0.0f ? inf : (a1 < 0.0f ? 0.0f : 1.0f);
+  if (zer_ret) z = 0.0f;
+  if (inf_ret) z = inf;
+  if (ax == 1.0f) z = ax;
+  return a0 == 0.0f ? (a1 == 0.0f ? 1.0f : 0.0f) : z;
+}
+
+// PLAIN: every lane's |a0| is normal and finite and its a1 finite, where
+// frexp is the bit split alone and the only selections that can apply are
+// the range results and |a0| = 1 (the others test for zeros and infinities).
+template <bool F, bool PLAIN> __device__ __forceinline__ float2 pow_abs_core(float2 a0, float2 a1)
+{
+  using C = math::powc<float>;
+  constexpr uint32_t P1[4] = {0xbe2a61b2u, 0x3e4d2fa3u, 0xbe800015u, 0x3eaaaaa3u};   // math::pow1
+  constexpr uint32_t P2[4] = {0x3c1a49bcu, 0x3d634d38u, 0x3e75fde1u, 0x3f317218u};   // math::pow2
+  int e[2], i[2];
+  float2 x;
+  if constexpr (PLAIN) {
+    const uint32_t b0 = __float_as_uint(a0.x) & 0x7fffffffu, b1 = __float_as_uint(a0.y) & 0x7fffffffu;
+    e[0] = (int)(b0 >> 23) - 126;
+    e[1] = (int)(b1 >> 23) - 126;
+    x = make_float2(__uint_as_float((b0 & 0x007fffffu) | 0x3f000000u), __uint_as_float((b1 & 0x007fffffu) | 0x3f000000u));
+  } else {
+    x = make_float2(math::pow_frexp(fabsf(a0.x), e[0]), math::pow_frexp(fabsf(a0.y), e[1]));
+  }
+  i[0] = math::pow_index(x.x);
+  i[1] = math::pow_index(x.y);
+  const float2 tmp = make_float2(math::pow_a(x.x, i[0]), math::pow_a(x.y, i[1]));
+  x = sub(x, tmp);
+  x = sub(x, make_float2(math::pow_b(x.x, i[0] >> 1), math::pow_b(x.y, i[1] >> 1)));
+  x = markstein_quot(x, tmp);
+  float2 z = mul(x, x);
+  float2 w = mul_r(mul(z, x), horner<F>(x, P1));
+  w = madd<F>(splat(-0.5f), z, w);
+  w = madd<F>(splat(C::bits(C::log2_em1)), w, w);
+  z = madd<F>(splat(C::bits(C::log2_em1)), x, w);
+  z = add(z, x);
+  w = madd<F>(make_float2((float)(-i[0]), (float)(-i[1])), splat(0.0625f), make_float2((float)e[0], (float)e[1]));
+  const float2 ya = pow_reduc(a1);
+  const float2 yb = sub(a1, ya);
+  float2 W = madd<F>(z, a1, mul_r(w, yb));
+  float2 Wa = pow_reduc(W);
+  float2 Wb = sub(W, Wa);
+  W = madd<F>(w, ya, Wa);
+  Wa = pow_reduc(W);
+  const float2 u = sub(W, Wa);
+  W = add(Wb, u);
+  Wb = pow_reduc(W);
+  w = mul(splat(16.0f), add(Wa, Wb));
+  const float wl[2] = {w.x, w.y};
+  bool inf_ret[2], zer_ret[2];
+#pragma unroll
+  for (int l = 0; l < 2; ++l) {
+    inf_ret[l] = wl[l] > C::bits(C::large);
+    zer_ret[l] = wl[l] < C::bits(C::low);
+    e[l] = (int)fminf(fmaxf(wl[l], -32768.0f), 32768.0f);   // as math::pow_abs
+  }
+  Wb = sub(W, Wb);
+  const bool t0 = Wb.x > 0.0f, t1 = Wb.y > 0.0f;
+  e[0] = t0 ? e[0] + 1 : e[0];
+  e[1] = t1 ? e[1] + 1 : e[1];
+  const float2 Wm = sub(Wb, splat(0.0625f));
+  Wb = make_float2(t0 ? Wm.x : Wb.x, t1 ? Wm.y : Wb.y);
+  z = mul(horner<F>(Wb, P2), Wb);
+  float wt[2];
+#pragma unroll
+  for (int l = 0; l < 2; ++l) {
+    i[l] = (e[l] > 0) ? e[l] / 16 + 1 : e[l] / 16;
+    e[l] = i[l] * 16 - e[l];
+    wt[l] = math::pow_a(0.0f, min(max(e[l], 0), 16));
+  }
+  w = make_float2(wt[0], wt[1]);
+  z = madd<F>(w, z, w);
+  z = pow_ldexp(z, i[0], i[1]);
+  if constexpr (PLAIN) {
+    const float inf = __int_as_float(0x7f800000);
+    z.x = inf_ret[0] ? inf : (zer_ret[0] ? 0.0f : z.x);
+    z.y = inf_ret[1] ? inf : (zer_ret[1] ? 0.0f : z.y);
+    z.x = (fabsf(a0.x) == 1.0f) ? 1.0f : z.x;
+    z.y = (fabsf(a0.y) == 1.0f) ? 1.0f : z.y;
+    return z;
+  } else {
+    return make_float2(pow_special(a0.x, a1.x, z.x, zer_ret[0], inf_ret[0]),
+                       pow_special(a0.y, a1.y, z.y, zer_ret[1], inf_ret[1]));
+  }
+}
+
+// |a0| normal and finite, a1 finite (pos: a0 also positive, where pow is pow_abs)
+__device__ __forceinline__ bool pow_plain(float a0, float a1, bool pos)
+{
+  const uint32_t b = pos ? __float_as_uint(a0) : (__float_as_uint(a0) & 0x7fffffffu);
+  return b - 0x00800000u < 0x7f000000u && fabsf(a1) < __int_as_float(0x7f800000);
+}
+
+template <bool F> __device__ __forceinline__ float2 pow_abs(float2 a0, float2 a1)
+{
+  if (__all_sync(__activemask(), pow_plain(a0.x, a1.x, false) && pow_plain(a0.y, a1.y, false)))
+    return pow_abs_core<F, true>(a0, a1);
+  return pow_abs_core<F, false>(a0, a1);
+}
+
+template <bool F> __device__ __forceinline__ float2 pow(float2 a0, float2 a1)
+{
+  if (__all_sync(__activemask(), pow_plain(a0.x, a1.x, true) && pow_plain(a0.y, a1.y, true)))
+    return pow_abs_core<F, true>(a0, a1);
+  float2 z = pow_abs_core<F, false>(a0, a1);
+  const float2 h = mul(sub(a1, splat(1.0f)), splat(0.5f));   // exact: a1 - 1 is 0 or normal
+  const float al0[2] = {a0.x, a0.y}, al1[2] = {a1.x, a1.y}, hl[2] = {h.x, h.y};
+  float zl[2] = {z.x, z.y};
+#pragma unroll
+  for (int l = 0; l < 2; ++l) {
+    const bool ltz = al0[l] < 0.0f;
+    if (ltz && math::is_flint(hl[l])) zl[l] = -zl[l];
+    zl[l] = (ltz && !math::is_flint(al1[l])) ? float(NAN) : zl[l];
+  }
+  return make_float2(zl[0], zl[1]);
 }
 
 }  // namespace x2

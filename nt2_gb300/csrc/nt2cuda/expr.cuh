@@ -341,7 +341,9 @@ template <class Tag, class A, int V> struct regs<node<Tag, A>, V> {
   template <bool F> __device__ __forceinline__ auto get(const node<Tag, A>& n, int l) const {
     if constexpr (kPair) {
       if (l & 1) return pend;
-      const float2 r = x2_apply<Tag, F>(make_float2(ra.template get<F>(n.a, l), ra.template get<F>(n.a, l + 1)));
+      const float a0 = ra.template get<F>(n.a, l);       // lane l before lane l + 1: the
+      const float a1 = ra.template get<F>(n.a, l + 1);   // operand may be a paired node too
+      const float2 r = x2_apply<Tag, F>(make_float2(a0, a1));
       pend = r.y;
       return r.x;
     } else {
@@ -350,8 +352,18 @@ template <class Tag, class A, int V> struct regs<node<Tag, A>, V> {
   }
 };
 
+// FP32 pow and pow_abs nodes run two lanes per packed instruction as above
+// (x2::pow, x2::pow_abs: bit-identical to math::pow, math::pow_abs).
+template <class Tag> struct x2_binary { static constexpr bool value = false; };
+template <> struct x2_binary<tag::pow_> { static constexpr bool value = true; };
+template <> struct x2_binary<tag::pow_abs_> { static constexpr bool value = true; };
+
 template <class Tag, class A, class B, int V> struct regs<node<Tag, A, B>, V> {
+  static constexpr bool kPair = x2_binary<Tag>::value && V % 2 == 0 &&
+                                std::is_same<typename value_of<A>::type, float>::value &&
+                                std::is_same<typename value_of<B>::type, float>::value;
   regs<A, V> ra; regs<B, V> rb;
+  mutable float pend;   // the odd lane of the last pair (kPair)
   template <bool S> __device__ __forceinline__ void load(const node<Tag, A, B>& n, size_t i) {
     ra.template load<S>(n.a, i); rb.template load<S>(n.b, i);
   }
@@ -365,6 +377,14 @@ template <class Tag, class A, class B, int V> struct regs<node<Tag, A, B>, V> {
     } else if constexpr (std::is_same<Tag, tag::cast_>::value) {
       using R = typename value_of<node<Tag, A, B>>::type;
       return cast_value<R>(ra.template get<F>(n.a, l));
+    } else if constexpr (kPair) {
+      if (l & 1) return pend;
+      const float a0 = ra.template get<F>(n.a, l), a1 = ra.template get<F>(n.a, l + 1);
+      const float b0 = rb.template get<F>(n.b, l), b1 = rb.template get<F>(n.b, l + 1);
+      const float2 r = std::is_same<Tag, tag::pow_>::value ? x2::pow<F>(make_float2(a0, a1), make_float2(b0, b1))
+                                                           : x2::pow_abs<F>(make_float2(a0, a1), make_float2(b0, b1));
+      pend = r.y;
+      return r.x;
     } else {
       return fn<Tag, F>::apply(ra.template get<F>(n.a, l), rb.template get<F>(n.b, l));
     }

@@ -848,7 +848,7 @@ template <> __device__ __forceinline__ double pow_ac<double>(int i)
   constexpr uint64_t A[17] = {NT2CUDA_POW_AD};
   return __longlong_as_double((long long)A[i]);
 }
-template <class T> __device__ __forceinline__ int pow_select(T& x)
+template <class T> __device__ __forceinline__ int pow_index(T x)
 {
   // The search compares x with A[9], then A[5] or A[13], then one of A[3], A[7],
   // A[11], A[15], then A[1]: values picked from constants instead of table reads.
@@ -858,7 +858,11 @@ template <class T> __device__ __forceinline__ int pow_select(T& x)
   const T a2 = i == 1 ? pow_ac<T>(3) : (i == 5 ? pow_ac<T>(7) : (i == 9 ? pow_ac<T>(11) : pow_ac<T>(15)));
   i = (x <= a2) ? i + 2 : i;
   i = (x >= pow_ac<T>(1)) ? -1 : i;
-  i = i + 1;
+  return i + 1;
+}
+template <class T> __device__ __forceinline__ int pow_select(T& x)
+{
+  const int i = pow_index(x);
   const T tmp = pow_a(x, i);
   x = sub(x, tmp);
   x = sub(x, pow_b(x, i >> 1));
