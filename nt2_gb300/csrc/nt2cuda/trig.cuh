@@ -872,10 +872,58 @@ template <class T> __device__ __forceinline__ int reduce_low(int lv, T x, T& xr)
   xr = lv == 0 ? x : (lv == 1 ? xs : xc);
   return lv == 0 ? 0 : (lv == 1 ? 1 : nc);
 }
+// reduce_low for two float elements whose levels are both at most 2, on the
+// packed instructions: the straight and cephes chains are the scalar ones
+// lane by lane (each product that feeds a subtraction formed by x2::mul_r);
+// cephes' quotient rint(x*2/pi) is at most 40 here, so it is (v + 1.5*2^23)
+// - 1.5*2^23, and its low bits are those of the sum.
+__device__ __forceinline__ void reduce_low2(int lv0, int lv1, float x0, float x1, float& xr0, float& xr1, int& n0,
+                                            int& n1)
+{
+  using x2::splat;
+  const float2 x = make_float2(x0, x1);
+  float2 xs = x2::sub(x, splat(fbits(tf::pio2_1)));
+  xs = x2::sub(xs, splat(fbits(tf::pio2_2)));
+  xs = x2::sub(xs, splat(fbits(tf::pio2_3)));
+  const float2 t = x2::add(x2::mul_r(x, splat(fbits(tf::twoopi))), splat(x2::kRound));
+  const float2 xi = x2::sub(t, splat(x2::kRound));
+  float2 xc = x2::sub(x, x2::mul_r(xi, splat(fbits(tf::pio2_1))));
+  xc = x2::sub(xc, x2::mul_r(xi, splat(fbits(tf::pio2_2))));
+  xc = x2::sub(xc, x2::mul_r(xi, splat(fbits(tf::pio2_3))));
+  const int nc0 = (int)(__float_as_uint(t.x) & 3u), nc1 = (int)(__float_as_uint(t.y) & 3u);
+  xr0 = lv0 == 0 ? x0 : (lv0 == 1 ? xs.x : xc.x);
+  xr1 = lv1 == 0 ? x1 : (lv1 == 1 ? xs.y : xc.y);
+  n0 = lv0 == 0 ? 0 : (lv0 == 1 ? 1 : nc0);
+  n1 = lv1 == 0 ? 0 : (lv1 == 1 ? 1 : nc1);
+}
 template <int K, bool F, int P, class T> __device__ __forceinline__ void scalar_group(const T (&a)[P], T (&y)[P])
 {
   if constexpr (pi_kind(K) || deg_kind(K)) {
     pack_impl<K, F, P, false>(a, y);
+  } else if constexpr (std::is_same<T, float>::value && P % 2 == 0) {
+    T xr[P];
+    int n[P];
+#pragma unroll
+    for (int l = 0; l < P; l += 2) {
+      const T xa = fabs(a[l]), xb = fabs(a[l + 1]);
+      const int la = level(xa), lb = level(xb);
+      if (la <= 2 && lb <= 2) {
+        reduce_low2(la, lb, xa, xb, xr[l], xr[l + 1], n[l], n[l + 1]);
+      } else {
+        T x1[1] = {xa}, r1[1];
+        int n1[1];
+        if (la <= 2) n1[0] = reduce_low(la, xa, r1[0]);
+        else reduce_at<1>(la, x1, r1, n1);
+        xr[l] = r1[0];
+        n[l] = n1[0];
+        x1[0] = xb;
+        if (lb <= 2) n1[0] = reduce_low(lb, xb, r1[0]);
+        else reduce_at<1>(lb, x1, r1, n1);
+        xr[l + 1] = r1[0];
+        n[l + 1] = n1[0];
+      }
+    }
+    finish_group<K, F, P>(a, xr, n, y);
   } else {
     T xr[P];
     int n[P];
