@@ -207,6 +207,47 @@ def test_blackscholes_fused_within_bound(gpu, oracle):
     assert np.max(np.abs(rc - c64) / np.maximum(np.abs(c64), 1)) < 1e-4
 
 
+@pytest.mark.parametrize("kind", ["config", "all_small", "all_large", "edges"])
+def test_blackscholes_fused_packed_matches_one_lane(gpu, kind):
+    """The fused mode's packed kernel (two options per instruction) gives the one-lane fused
+    kernel's bits.  Misaligned tables take the one-lane kernel; the same options are priced
+    through both."""
+    rng = np.random.default_rng(29)
+    if kind == "config":
+        n = 5 * 2048 + 13
+        S, K, T = bs_inputs(n, np.float32, seed=31)
+    elif kind == "all_small":
+        n = 2048 + 6
+        S = rng.uniform(50, 51, n).astype(np.float32)
+        K = (S * rng.uniform(0.999, 1.001, n)).astype(np.float32)
+        T = rng.uniform(0.01, 0.02, n).astype(np.float32)
+    elif kind == "all_large":
+        n = 2048 + 7
+        S = rng.uniform(5, 6, n).astype(np.float32)
+        K = rng.uniform(90, 100, n).astype(np.float32)
+        T = rng.uniform(0.25, 0.5, n).astype(np.float32)
+    else:
+        vals = np.array([0.0, -0.0, 1e-45, 1e-38, 0.5, 1.0, 2.0, 1e20, 3e38, np.inf, -np.inf, np.nan, -1.0],
+                        np.float32)
+        S, K, T = (a.ravel().astype(np.float32) for a in np.meshgrid(vals, vals, vals, indexing="ij"))
+        n = S.size
+
+    def misaligned(a):
+        buf = torch.empty(a.size + 1, dtype=torch.float32, device="cuda")
+        view = buf[1:]
+        view.copy_(torch.from_numpy(a))
+        return view
+
+    c, p = gpu.blackscholes(to_dev(S), to_dev(K), to_dev(T), 0.02, 0.30, fused=True)
+    oc = torch.empty(n + 1, dtype=torch.float32, device="cuda")[1:]
+    op = torch.empty(n + 1, dtype=torch.float32, device="cuda")[1:]
+    c1, p1 = gpu.blackscholes(misaligned(S), misaligned(K), misaligned(T), 0.02, 0.30, call=oc, put=op, fused=True)
+    for got, ref in ((host(c), host(c1)), (host(p), host(p1))):
+        same = (got.view(np.uint32) == ref.view(np.uint32)) | (np.isnan(got) & np.isnan(ref))
+        w = np.flatnonzero(~same)
+        assert w.size == 0, (kind, w[:5], S[w[:5]], K[w[:5]], T[w[:5]], got[w[:5]], ref[w[:5]])
+
+
 def ulp_dist_f32(a, b):
     """|a - b| in float32 ulps (ordered-integer distance); NaN against NaN is 0."""
     ia = a.view(np.int32).astype(np.int64)
