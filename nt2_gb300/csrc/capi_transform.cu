@@ -151,14 +151,33 @@ template <bool F> nt2cuda_status rgb2yuv_impl(const float* r, const float* g, co
   return launch_status(launch_persistent(k_rgb2yuv<F>, n / 4 + 1, 256, 2, s, args));
 }
 
-// The demo statement, lowered through the generic expression engine.
-// d1 appears twice in R's tree (in d2 and in fastnormcdf(d1)), and a tree
-// evaluates each occurrence; so d1 is its own statement into stream scratch,
-// as the demo itself materialises it, and R's statement reads it.
+// The demo statement.  Aligned tables (R the same table as an input, or
+// disjoint from all of them) take one pass of k_bs_demo, the demo's local
+// tables da, d1, d2 in registers.  Otherwise it is lowered through the
+// generic expression engine, which rejects partial overlaps: d1 appears twice
+// in R's tree (in d2 and in fastnormcdf(d1)), and a tree evaluates each
+// occurrence; so d1 is its own statement into stream scratch, as the demo
+// itself materialises it, and R's statement reads it.
 template <bool F> nt2cuda_status bs_demo_impl(const float* S, const float* X, const float* T, const float* r,
                                               const float* v, float* R, size_t n, nt2cuda_stream s)
 {
   if (n == 0) return NT2CUDA_OK;
+  {
+    const float* in[5] = {S, X, T, r, v};
+    bool ok = ((uintptr_t)S | (uintptr_t)X | (uintptr_t)T | (uintptr_t)r | (uintptr_t)v | (uintptr_t)R) % 16u == 0 &&
+              n <= ((size_t)1 << 60);
+    for (int k = 0; k < 5 && ok; ++k) ok = in[k] == R || !overlap(in[k], R, n * sizeof(float));
+    if (ok) {
+      void* args[] = {(void*)&S, (void*)&X, (void*)&T, (void*)&r, (void*)&v, (void*)&R, (void*)&n};
+      tuning::params def;
+      def.unroll = 1;
+      def.waves = 4;
+      const tuning::params tp = tuning::lookup("bs_demo_f32", n, def);
+      if (tp.unroll == 2)
+        return launch_status(launch_persistent(k_bs_demo<F, 2>, n / 4 + 1, 256, tp.waves, as_stream(s), args));
+      return launch_status(launch_persistent(k_bs_demo<F, 1>, n / 4 + 1, 256, tp.waves, as_stream(s), args));
+    }
+  }
   auto Sa = tm(S); auto Xa = tm(X); auto Ta = tm(T); auto ra = tm(r); auto va = tm(v);
   auto da = nd<tag::sqrt_>(Ta);
   // log(Sa/Xa) + (fma(sqr(va),0.5,ra)*Ta)/(va*da)

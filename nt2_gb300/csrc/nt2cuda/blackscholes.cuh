@@ -173,6 +173,98 @@ __global__ void __launch_bounds__(256, (kMinBlocks<T, CDF, P, U>))
   }
 }
 
+// The demo form of the statement (demo/blackscholes/nt2/blackandscholes_nt2.cpp:55-59),
+// five FP32 tables in and R out:
+//   da = sqrt(Ta);  d1 = log(Sa/Xa) + (fma(sqr(va),0.5,ra)*Ta)/(va*da);
+//   d2 = fnms(va,da,d1);
+//   R  = fnms(Xa*exp(-ra*Ta), fastnormcdf(d2), Sa*fastnormcdf(d1));
+// da, d1 and d2 are the demo's local tables, read only by the statements that
+// follow them, so here they stay in registers: one pass reads the five inputs
+// once and writes R.  Two options per packed instruction (bs_x2.cuh); every
+// value is the one the statements give element by element (each product that
+// feeds an add or subtract formed by x2::mul_r).
+template <bool F>
+__device__ __forceinline__ float2 bs_demo_pair(float2 S, float2 X, float2 T, float2 r, float2 v)
+{
+  const float2 da = make_float2(__fsqrt_rn(T.x), __fsqrt_rn(T.y));
+  const float2 L = x2::log<F>(make_float2(__fdiv_rn(S.x, X.x), __fdiv_rn(S.y, X.y)));
+  const float2 c = x2::madd<F>(x2::mul(v, v), x2::splat(0.5f), r);
+  const float2 num = x2::mul(c, T), den = x2::mul(v, da);
+  const float2 d1 = x2::add(L, make_float2(__fdiv_rn(num.x, den.x), __fdiv_rn(num.y, den.y)));
+  const float2 d2 = x2::nmsub<F>(v, da, d1);
+  const float2 e = x2::mul(X, x2::exp<F>(x2::mul_r(make_float2(-r.x, -r.y), T)));
+  float2 n1, m1, n2, m2;
+  x2::fastnormcdf_pair<F>(d2, n2, m2);
+  x2::fastnormcdf_pair<F>(d1, n1, m1);
+  return x2::nmsub<F>(e, n2, x2::mul_r(S, n1));
+}
+
+// Four options per thread per group (16 bytes of each table), U groups in
+// flight per grid-stride trip; the last n % 4 options one per thread.
+template <bool F, int U>
+__global__ void __launch_bounds__(256, U == 1 ? 4 : 3)
+    k_bs_demo(const float* __restrict__ S, const float* __restrict__ X, const float* __restrict__ T,
+              const float* __restrict__ r, const float* __restrict__ v, float* __restrict__ R, size_t n)
+{
+  nt2cuda::mem::pdl_begin();
+  constexpr int V = 4;
+  const size_t ngroups = n / V;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t g = tid;
+#pragma unroll 1
+  for (; g + (size_t)(U - 1) * stride < ngroups; g += (size_t)U * stride) {
+    float s[U][V], x[U][V], t[U][V], rr[U][V], vv[U][V];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const size_t i = (g + (size_t)u * stride) * V;
+      mem::load_vec<float, V, true>(S, i, s[u]);
+      mem::load_vec<float, V, true>(X, i, x[u]);
+      mem::load_vec<float, V, true>(T, i, t[u]);
+      mem::load_vec<float, V, true>(r, i, rr[u]);
+      mem::load_vec<float, V, true>(v, i, vv[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      float o[V];
+#pragma unroll
+      for (int l = 0; l < V; l += 2) {
+        const float2 y = bs_demo_pair<F>(make_float2(s[u][l], s[u][l + 1]), make_float2(x[u][l], x[u][l + 1]),
+                                         make_float2(t[u][l], t[u][l + 1]), make_float2(rr[u][l], rr[u][l + 1]),
+                                         make_float2(vv[u][l], vv[u][l + 1]));
+        o[l] = y.x;
+        o[l + 1] = y.y;
+      }
+      mem::store_vec<float, V>(R, (g + (size_t)u * stride) * V, o);
+    }
+  }
+#pragma unroll 1
+  for (; g < ngroups; g += stride) {
+    float s[V], x[V], t[V], rr[V], vv[V], o[V];
+    const size_t i = g * V;
+    mem::load_vec<float, V, true>(S, i, s);
+    mem::load_vec<float, V, true>(X, i, x);
+    mem::load_vec<float, V, true>(T, i, t);
+    mem::load_vec<float, V, true>(r, i, rr);
+    mem::load_vec<float, V, true>(v, i, vv);
+#pragma unroll
+    for (int l = 0; l < V; l += 2) {
+      const float2 y = bs_demo_pair<F>(make_float2(s[l], s[l + 1]), make_float2(x[l], x[l + 1]),
+                                       make_float2(t[l], t[l + 1]), make_float2(rr[l], rr[l + 1]),
+                                       make_float2(vv[l], vv[l + 1]));
+      o[l] = y.x;
+      o[l + 1] = y.y;
+    }
+    mem::store_vec<float, V>(R, i, o);
+  }
+  const size_t tail0 = ngroups * V;
+  if (tid < n - tail0) {   // one option, in both lanes of a pair (the lanes are independent)
+    const size_t i = tail0 + tid;
+    R[i] = bs_demo_pair<F>(make_float2(S[i], S[i]), make_float2(X[i], X[i]), make_float2(T[i], T[i]),
+                           make_float2(r[i], r[i]), make_float2(v[i], v[i])).x;
+  }
+}
+
 // Misaligned tables: one option per thread per trip.
 template <class T, int CDF, int P>
 __global__ void __launch_bounds__(256) k_blackscholes_scalar(const T* S, const T* K, const T* Tm, T r, T v,

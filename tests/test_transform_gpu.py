@@ -317,6 +317,52 @@ def test_blackscholes_demo_bit_exact(gpu, oracle):
     assert m == 0.0, (w, R[w], ref[w])
 
 
+def _demo_tables(kind, rng):
+    if kind == "edges":
+        vals = np.array([0.0, -0.0, 1e-45, 1e-38, 0.5, 1.0, 2.0, 1e20, 3e38, np.inf, -np.inf, np.nan, -1.0],
+                        np.float32)
+        S, X, T = (a.ravel() for a in np.meshgrid(vals, vals, vals, indexing="ij"))
+        n = S.size
+        r = np.resize(np.array([0.02, 0.0, -0.5, np.inf, np.nan], np.float32), n)
+        v = np.resize(np.array([0.3, 0.0, 1e-20, 5.0, -0.3, np.nan, np.inf], np.float32), n)
+        return [np.ascontiguousarray(a, dtype=np.float32) for a in (S, X, T, r, v)]
+    n = {"tail": 4 * 999 + 3, "config": 3 * 2048 + 1}[kind]
+    return [rng.uniform(lo, hi, n).astype(np.float32)
+            for lo, hi in ((5, 30), (1, 100), (0.25, 10), (0.0, 0.05), (0.1, 0.5))]
+
+
+@pytest.mark.parametrize("kind", ["tail", "config", "edges"])
+def test_blackscholes_demo_single_pass_and_generic_path_bit_exact(gpu, oracle, kind):
+    """Aligned tables take one pass with the demo's local tables da, d1, d2 in registers;
+    misaligned views take the generic two-statement lowering.  Both give the oracle's bits
+    (two NaNs compare equal), including in place (R the same table as S), and the fused
+    modes of the two paths agree bit for bit."""
+    tabs = _demo_tables(kind, np.random.default_rng(5))
+    n = tabs[0].size
+    ref = oracle.bs_demo(*tabs)
+
+    def check(got):
+        same = (got.view(np.uint32) == ref.view(np.uint32)) | (np.isnan(got) & np.isnan(ref))
+        w = np.flatnonzero(~same)
+        assert w.size == 0, (kind, w[:5], [t[w[:5]] for t in tabs], got[w[:5]], ref[w[:5]])
+
+    def misaligned(a):
+        view = torch.empty(a.size + 1, dtype=torch.float32, device="cuda")[1:]
+        view.copy_(torch.from_numpy(a))
+        return view
+
+    check(host(gpu.blackscholes_demo(*(to_dev(a) for a in tabs))))
+    dev = [to_dev(a) for a in tabs]
+    check(host(gpu.blackscholes_demo(*dev, out=dev[0])))           # R = S
+    mis = [misaligned(a) for a in tabs]
+    out = torch.empty(n + 1, dtype=torch.float32, device="cuda")[1:]
+    check(host(gpu.blackscholes_demo(*mis, out=out)))
+    f1 = host(gpu.blackscholes_demo(*(to_dev(a) for a in tabs), fused=True))
+    f2 = host(gpu.blackscholes_demo(*mis, out=out, fused=True))
+    same = (f1.view(np.uint32) == f2.view(np.uint32)) | (np.isnan(f1) & np.isnan(f2))
+    assert same.all(), (kind, np.flatnonzero(~same)[:5])
+
+
 def test_blackscholes_host_entry(gpu, oracle):
     n = (1 << 21) * 3 + 17   # several pipeline chunks and a ragged tail
     S, K, T = bs_inputs(n, np.float32, seed=77)
