@@ -461,7 +461,8 @@ nt2cuda_status nt2cuda_selftest_fold_timeout(const float* A, size_t rows, size_t
  * evaluation of the float trigonometric functors (sin, cos, then the same
  * fused; tan, cot, then the same fused) over every reduced argument;
  * 22..25 pow, pow fused, pow_abs, pow_abs fused, with every float once as the
- * base and once as the exponent, each against a drawn partner.
+ * base and once as the exponent, each against a drawn partner; 26, 27 cbrt,
+ * unfused and fused.
  * *mismatches = arguments whose results differ in any bit (two NaNs are
  * equal); first_bad (8 entries, may be NULL) gets the first ones' bit
  * patterns.  Synchronous. */

@@ -170,6 +170,18 @@ template <bool ABS, bool F> __device__ __forceinline__ void x2_check_pow(uint32_
   }
 }
 
+// 26, 27: cbrt, unfused and fused
+__device__ __forceinline__ void x2_check_cbrt(bool fused, uint32_t u0, x2_report* rep)
+{
+  const uint32_t u1 = u0 + 1;
+  const float2 a = make_float2(__uint_as_float(u0), __uint_as_float(u1));
+  const float2 r = fused ? x2::cbrt<true>(a) : x2::cbrt<false>(a);
+  const float s0 = fused ? math::cbrt<true>(a.x) : math::cbrt<false>(a.x);
+  const float s1 = fused ? math::cbrt<true>(a.y) : math::cbrt<false>(a.y);
+  if (!same(r.x, s0)) record(rep, u0);
+  if (!same(r.y, s1)) record(rep, u1);
+}
+
 __global__ void __launch_bounds__(256) k_x2_check(int which, uint64_t pairs, x2_report* rep)
 {
   for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < pairs; p += (uint64_t)gridDim.x * blockDim.x) {
@@ -189,7 +201,8 @@ __global__ void __launch_bounds__(256) k_x2_check(int which, uint64_t pairs, x2_
     else if (which == 22) x2_check_pow<false, false>((uint32_t)(2 * p), rep);
     else if (which == 23) x2_check_pow<false, true>((uint32_t)(2 * p), rep);
     else if (which == 24) x2_check_pow<true, false>((uint32_t)(2 * p), rep);
-    else x2_check_pow<true, true>((uint32_t)(2 * p), rep);
+    else if (which == 25) x2_check_pow<true, true>((uint32_t)(2 * p), rep);
+    else x2_check_cbrt(which == 27, (uint32_t)(2 * p), rep);
   }
 }
 
@@ -199,7 +212,7 @@ extern "C" nt2cuda_status nt2cuda_selftest_x2(int which, unsigned long long* mis
                                               nt2cuda_stream stream)
 {
   NT2CUDA_NVTX_RANGE;
-  if (which < 0 || which > 25 || !mismatches) return NT2CUDA_ERR_ARG;
+  if (which < 0 || which > 27 || !mismatches) return NT2CUDA_ERR_ARG;
   cudaStream_t s = as_stream(stream);
   x2_report* rep = nullptr;
   cudaError_t e = cudaMalloc(&rep, sizeof(x2_report));

@@ -1,5 +1,5 @@
-// nt2cuda/bs_x2.cuh -- NT2's float exp, log, erfc, normcdf and pow, two
-// lanes at a time on Blackwell's packed FP32 instructions, bit-identical to
+// nt2cuda/bs_x2.cuh -- NT2's float exp, log, erfc, normcdf, pow and cbrt,
+// two lanes at a time on Blackwell's packed FP32 instructions, bit-identical to
 // the one-lane forms of math.cuh.
 //
 // sm_100-family SMs execute add.rn.f32x2 / mul.rn.f32x2 on a 64-bit
@@ -576,6 +576,52 @@ template <bool F> __device__ __forceinline__ float2 pow(float2 a0, float2 a1)
     zl[l] = (ltz && !math::is_flint(al1[l])) ? float(NAN) : zl[l];
   }
   return make_float2(zl[0], zl[1]);
+}
+
+// ------------------------------------------------------------------ cbrt
+// NT2's float cbrt (math::cbrt), two lanes: the exponent split, the table
+// factor and the special cases per lane, the polynomial and the Newton step
+// packed.  The Newton step's division z / x^2 is markstein_quot when every
+// lane of the warp has z >= 2^-103 (or z not finite): with a quotient of
+// about z^(1/3), the residual z - x^2 q is then a multiple of at least
+// 2^-149, so it is exact and the correction holds as it does for normal
+// operands.  Other warps divide per lane.  Checked against the one-lane form
+// over every float.
+template <bool F> __device__ __forceinline__ float2 cbrt(float2 a0)
+{
+  constexpr uint32_t P[5] = {0xbe09e49au, 0x3f0bf0feu, 0xbf745265u, 0x3f91eb77u, 0x3ece0609u};
+  const float al[2] = {a0.x, a0.y};
+  float zl[2], fl[2], xl[2], factl[2], scl[2];
+#pragma unroll
+  for (int l = 0; l < 2; ++l) {
+    float z = fabsf(al[l]);
+    const bool den = z < fbits(0x00800000u);
+    z = den ? math::mul(z, 8388608.0f) : z;
+    fl[l] = den ? fbits(0x3ba14518u) : 1.0f;   // 2^(-23/3)
+    const uint32_t b = __float_as_uint(z);
+    int e = (int)((b & 0x7f800000u) >> 23) - 126;
+    xl[l] = fbits((b & ~0x7f800000u) | 0x3f000000u);
+    const bool flag = e >= 0;
+    int rem;
+    e = math::cbrt_split(e, rem);
+    float fact = rem == 1 ? (flag ? fbits(0x3fa14518u) : fbits(0x3f4b2ff5u)) : 1.0f;
+    factl[l] = rem == 2 ? (flag ? fbits(0x3fcb2ff5u) : fbits(0x3f214518u)) : fact;
+    scl[l] = fbits((uint32_t)(e + 127) << 23);
+    zl[l] = z;
+  }
+  const float2 z = make_float2(zl[0], zl[1]);
+  float2 x = horner<F>(make_float2(xl[0], xl[1]), P);
+  x = mul_r(mul(x, make_float2(factl[0], factl[1])), make_float2(scl[0], scl[1]));
+  const float2 xx = mul(x, x);
+  const bool safe0 = !(zl[0] < fbits(0x0c000000u)), safe1 = !(zl[1] < fbits(0x0c000000u));   // 2^-103
+  float2 q;
+  if (__all_sync(__activemask(), safe0 && safe1)) q = markstein_quot(z, xx);
+  else q = make_float2(__fdiv_rn(z.x, xx.x), __fdiv_rn(z.y, xx.y));
+  x = sub(x, mul_r(sub(x, q), splat(fbits(0x3eaaaaabu))));
+  x = mul(make_float2(__uint_as_float(__float_as_uint(x.x) | (__float_as_uint(a0.x) & 0x80000000u)),
+                      __uint_as_float(__float_as_uint(x.y) | (__float_as_uint(a0.y) & 0x80000000u))),
+          make_float2(fl[0], fl[1]));
+  return make_float2((a0.x == 0.0f || isinf(a0.x)) ? a0.x : x.x, (a0.y == 0.0f || isinf(a0.y)) ? a0.y : x.y);
 }
 
 }  // namespace x2

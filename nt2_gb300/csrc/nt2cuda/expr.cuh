@@ -300,7 +300,7 @@ template <class T, int V> struct regs<scal<T>, V> {
   template <bool F> __device__ __forceinline__ T get(const scal<T>& s, int) const { return s.v; }
 };
 
-// FP32 exp, log, erfc, normcdf and fastnormcdf nodes run two lanes per packed instruction
+// FP32 exp, log, erfc, normcdf, fastnormcdf and cbrt nodes run two lanes per packed instruction
 // (nt2cuda/bs_x2.cuh, bit-identical to the one-lane functors over every
 // float): asked for an even lane, the node computes that lane and the next
 // one and hands the latter out when it is asked for (the kernels ask for
@@ -311,11 +311,14 @@ template <> struct x2_unary<tag::log_> { static constexpr bool value = true; };
 template <> struct x2_unary<tag::fastnormcdf_> { static constexpr bool value = true; };
 template <> struct x2_unary<tag::erfc_> { static constexpr bool value = true; };
 template <> struct x2_unary<tag::normcdf_> { static constexpr bool value = true; };
+template <> struct x2_unary<tag::cbrt_> { static constexpr bool value = true; };
 template <class Tag, bool F> __device__ __forceinline__ float2 x2_apply(float2 a)
 {
   float2 pos, neg;
   if constexpr (std::is_same<Tag, tag::exp_>::value) {
     return x2::exp<F>(a);
+  } else if constexpr (std::is_same<Tag, tag::cbrt_>::value) {
+    return x2::cbrt<F>(a);
   } else if constexpr (std::is_same<Tag, tag::log_>::value) {
     return x2::log<F>(a);
   } else if constexpr (std::is_same<Tag, tag::erfc_>::value) {   // math::erfc

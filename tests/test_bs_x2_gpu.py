@@ -72,3 +72,15 @@ def test_two_lane_pow_matches_one_lane(gpu, cuda_lib, which, name):
     st = cuda_lib.nt2cuda_selftest_x2(which, C.byref(n), first, torch.cuda.current_stream().cuda_stream)
     assert st == 0
     assert n.value == 0, (name, n.value, [hex(first[i]) for i in range(min(8, n.value))])
+
+
+@pytest.mark.parametrize("which,name", [(26, "cbrt"), (27, "cbrt, fused")])
+def test_two_lane_cbrt_is_bit_exact_over_every_float(gpu, cuda_lib, which, name):
+    """FP32 cbrt nodes run two lanes per packed instruction, the Newton step's division by a
+    reciprocal, a Newton step and Markstein's correction where the residual stays exact; over
+    every float both lanes give the one-lane bits."""
+    n = C.c_ulonglong(99)
+    first = (C.c_uint32 * 8)()
+    st = cuda_lib.nt2cuda_selftest_x2(which, C.byref(n), first, torch.cuda.current_stream().cuda_stream)
+    assert st == 0
+    assert n.value == 0, (name, n.value, [hex(first[i]) for i in range(min(8, n.value))])
